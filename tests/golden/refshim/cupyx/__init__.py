@@ -1,0 +1,1 @@
+"""Stand-in for cupyx (maps to SciPy); golden-vector generation only."""

@@ -1,0 +1,1 @@
+from scipy.sparse import *  # noqa: F401,F403

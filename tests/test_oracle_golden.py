@@ -1,0 +1,109 @@
+"""Pin the CPU oracle against golden vectors made by the reference itself.
+
+Fixtures: tests/golden/*.npz from tests/golden/make_golden.py (reference code
+run on the CPU).  Tolerances: 1e-12 relative L2 for float64 transforms and
+tendencies (the bar the FP64 GPU path must meet as well).
+"""
+import numpy as np
+import pytest
+
+import oracle
+from oracle import models, diagnostics
+from helpers import rel_l2
+
+TOL = 1e-12
+
+
+def gauss_ops(nlat, nlon, lmax, R):
+    sh = oracle.GaussSH(nlat, nlon, lmax)
+    nf, mf = oracle.fine_dims(nlat, nlon, lmax)
+    sh_p = sh if (nf, mf) == (nlat, nlon) else oracle.GaussSH(nf, mf, lmax)
+    return oracle.Operators(sh, R, sh_p=sh_p)
+
+
+@pytest.mark.parametrize("name", ["bve_gauss32x64_L21", "bve_gauss16x32_L15_fine23x46"])
+def test_bve_golden(golden, name):
+    g = golden(name)
+    nlat, nlon, L = int(g["nlat"]), int(g["nlon"]), int(g["lmax"])
+    ops = gauss_ops(nlat, nlon, L, float(g["radius"]))
+    assert tuple(g["product_grid"]) == oracle.fine_dims(nlat, nlon, L)
+    np.testing.assert_allclose(ops.sh.lat, g["lat"], rtol=0, atol=1e-15)
+    np.testing.assert_allclose(ops.sh.weights, g["weights"], rtol=1e-14)
+    zeta = g["zeta"]
+    assert rel_l2(ops.sh.inv_transform(zeta), g["grid"]) < TOL
+    assert rel_l2(ops.sh.transform(g["grid"]), g["roundtrip"]) < TOL
+    om, nu, dt = float(g["omega"]), float(g["nu"]), float(g["dt"])
+    assert rel_l2(models.bve_tendency(ops, zeta, om, nu), g["tendency"]) < TOL
+    step = models.bve_rk4_step(ops, zeta, dt, om, nu)
+    assert rel_l2(step, g["rk4"]) < TOL
+    keys = list(g["spec_keys"])
+    d0 = diagnostics.spectral_diagnostics(zeta, ops.R, om)
+    d1 = diagnostics.spectral_diagnostics(step, ops.R, om)
+    for k, v0, v1 in zip(keys, g["spec0"], g["spec1"]):
+        assert d0[k] == pytest.approx(v0, rel=1e-12, abs=1e-300)
+        assert d1[k] == pytest.approx(v1, rel=1e-10, abs=1e-300)
+    dg = diagnostics.grid_diagnostics(zeta, ops.sh, ops.R, om)
+    for k, v in zip(list(g["grid_keys"]), g["grid0"]):
+        assert dg[k] == pytest.approx(v, rel=1e-11, abs=1e-3)
+
+
+@pytest.mark.parametrize("name", ["swe_gauss16x32_L15_fine23x46", "swe_gauss32x64_L21",
+                                  "swe_gauss128x256_L85"])
+def test_swe_golden(golden, name):
+    g = golden(name)
+    nlat, nlon, L = int(g["nlat"]), int(g["nlon"]), int(g["lmax"])
+    ops = gauss_ops(nlat, nlon, L, float(g["radius"]))
+    m = models.SWE(ops, float(g["omega"]), float(g["gravity"]), float(g["mean_depth"]))
+    s = g["state"]
+    assert rel_l2(m.tendency(s), g["tendency"]) < TOL
+    u, v = m.wind_on_state_grid(s)
+    assert rel_l2(u, g["u"]) < TOL and rel_l2(v, g["v"]) < TOL
+    np.testing.assert_allclose(m.total_geopotential_extrema(s), g["phi_extrema"], rtol=1e-13)
+    if L <= 21:
+        y = s
+        for _ in range(int(g["steps"])):
+            y = models.rk4_step_array(m.tendency, y, float(g["dt"]))
+        assert rel_l2(y, g["rk4"]) < TOL
+
+
+def test_geodesic_golden(golden):
+    g = golden("geodesic_res3_L10")
+    lat, lon, w = oracle.geodesic.geodesic_point_set(int(g["res"]), float(g["radius"]))
+    np.testing.assert_allclose(lat, g["lat"], rtol=0, atol=1e-14)
+    np.testing.assert_allclose(lon, g["lon"], rtol=0, atol=1e-14)
+    np.testing.assert_allclose(w, g["weights"], rtol=1e-12)
+    sh = oracle.PointSetSH(lat, lon, int(g["lmax"]), weights=w)
+    assert rel_l2(sh.inv_transform(g["coeffs"]), g["synth"]) < TOL
+    assert rel_l2(sh.transform(g["field"]), g["analysis"]) < TOL
+    ops = oracle.Operators(sh, float(g["radius"]))
+    t = models.bve_tendency(ops, g["zeta"], float(g["omega"]))
+    assert rel_l2(t, g["bve_tendency"]) < TOL
+
+
+def test_factored_equals_dense():
+    """GaussSH (Legendre + DFT) equals PointSetSH (reference dense form)."""
+    rng = np.random.default_rng(1)
+    for nlat, nlon, L in [(16, 32, 15), (23, 46, 15), (24, 48, 10)]:
+        gs = oracle.GaussSH(nlat, nlon, L)
+        ps = oracle.PointSetSH(gs.latitudes, gs.longitudes, L, weights=gs.weights)
+        a = rng.standard_normal((L + 1, L + 1)) + 1j * rng.standard_normal((L + 1, L + 1))
+        f = rng.standard_normal(nlat * nlon)
+        assert rel_l2(gs.inv_transform(a), ps.inv_transform(a)) < 1e-13
+        assert rel_l2(gs.transform(f), ps.transform(f)) < 1e-13
+
+
+def test_basis_matches_scipy():
+    """Normalised recurrence == scipy.special.sph_harm_y, including l_max=127."""
+    sp = pytest.importorskip("scipy.special")
+    if not hasattr(sp, "sph_harm_y"):
+        pytest.skip("scipy too old")
+    rng = np.random.default_rng(2)
+    lat = rng.uniform(-1.55, 1.55, 7)
+    lon = rng.uniform(0, 2 * np.pi, 7)
+    L = 127
+    Y = oracle.dense_basis(lat, lon, L)
+    for l in (0, 1, 40, 85, 100, 127):
+        for m in sorted({0, min(1, l), l // 2, l}):
+            ref = sp.sph_harm_y(l, m, np.pi / 2 - lat, lon)
+            k = l * (l + 1) // 2 + m
+            assert np.allclose(Y[:, k], ref, rtol=1e-10, atol=1e-14), (l, m)
