@@ -1,0 +1,150 @@
+// Plan-kind independent chains:
+//   synth chain : Derive -> synthesis -> Pointwise -> grid fields
+//   anal chain  : grid fields -> Pointwise -> weighted analysis -> Epilogue
+//   full chain  : Derive -> synthesis -> Pointwise -> analysis -> Epilogue
+// On a Gauss plan these are the fused Legendre/row kernels; on a point-set
+// plan derive_cols -> basis GEMM -> pointwise -> basis^T GEMM -> epilogue.
+#pragma once
+
+#include "pipeline.cuh"
+#include "points.cuh"
+
+namespace aeolus {
+
+inline unsigned blocks_for(long n, int t) { return (unsigned)((n + t - 1) / t); }
+
+// ---------------------------------------------------------------- sizes
+template <int NIN, int NOUT>
+size_t full_chain_bytes(const aeolus_plan_impl* p, int batch) {
+  if (p->kind == kGauss) return align256(fg_bytes(p, NIN > NOUT ? NIN : NOUT, batch));
+  const size_t nc = p->ncol, np = p->npoints;
+  return align256((size_t)batch * NIN * nc * 8) + align256((size_t)batch * NIN * np * 8) +
+         align256((size_t)batch * NOUT * np * 8) + align256((size_t)batch * NOUT * nc * 8);
+}
+
+template <int NIN, int NOUT>
+size_t synth_chain_bytes(const aeolus_plan_impl* p, int batch) {
+  if (p->kind == kGauss) return align256(fg_bytes(p, NIN, batch));
+  return align256((size_t)batch * NIN * p->ncol * 8) + align256((size_t)batch * NIN * p->npoints * 8);
+}
+
+template <int NIN, int NOUT>
+size_t anal_chain_bytes(const aeolus_plan_impl* p, int batch) {
+  if (p->kind == kGauss) return align256(fg_bytes(p, NOUT, batch));
+  return align256((size_t)batch * NOUT * p->npoints * 8) + align256((size_t)batch * NOUT * p->ncol * 8);
+}
+
+// ---------------------------------------------------------------- chains
+template <class Derive, class Pw, class Epi>
+int run_full_chain(const aeolus_plan_impl* p, const Derive& d, const Pw& pw, const Epi& e, int batch,
+                   void* work, unsigned* status, cudaStream_t st) {
+  static_assert(Derive::NF == Pw::NIN, "derive/pointwise field count");
+  static_assert(Pw::NOUT == Epi::NF, "pointwise/epilogue field count");
+  if (p->kind == kGauss) {
+    constexpr int NB = Pw::NIN > Pw::NOUT ? Pw::NIN : Pw::NOUT;
+    double2* FG = static_cast<double2*>(work);
+    int s = launch_synth(p, d, FG, NB, batch, st);
+    if (s) return s;
+    RowArgs ra{};
+    ra.batch = batch;
+    ra.FG = FG;
+    ra.nblk = NB;
+    ra.status = status;
+    if ((s = launch_rows<Pw, kInF, kOutG>(p, pw, ra, st))) return s;
+    return launch_analysis(p, e, FG, NB, batch, st);
+  }
+  const long nc = p->ncol, np = p->npoints;
+  char* w = static_cast<char*>(work);
+  double* V = reinterpret_cast<double*>(w);
+  w += align256((size_t)batch * Pw::NIN * nc * 8);
+  double* Gr = reinterpret_cast<double*>(w);
+  w += align256((size_t)batch * Pw::NIN * np * 8);
+  double* Wt = reinterpret_cast<double*>(w);
+  w += align256((size_t)batch * Pw::NOUT * np * 8);
+  double* C = reinterpret_cast<double*>(w);
+  const long nlm = n_coeff(p->lmax) * batch;
+  derive_cols_kernel<Derive><<<blocks_for(nlm, 128), 128, 0, st>>>(p->lmax, batch, nc, V, d);
+  AE_LAUNCH("derive_cols_kernel");
+  int s = points_gemm_synth(p, V, Gr, batch * Pw::NIN, st);
+  if (s) return s;
+  points_pointwise_kernel<Pw><<<blocks_for(np * batch, 128), 128, 0, st>>>(
+      np, batch, Gr, (long)Pw::NIN * np, np, Wt, (long)Pw::NOUT * np, np, p->coslat, p->fgrid, p->wpts, status, pw);
+  AE_LAUNCH("points_pointwise_kernel");
+  if ((s = points_gemm_analysis(p, Wt, C, batch * Pw::NOUT, st))) return s;
+  const long n2 = (long)(p->lmax + 1) * (p->lmax + 1) * batch;
+  epilogue_cols_kernel<Epi><<<blocks_for(n2, 128), 128, 0, st>>>(p->lmax, batch, nc, C, e);
+  AE_LAUNCH("epilogue_cols_kernel");
+  return AEOLUS_OK;
+}
+
+// Output grid: out[b * out_b + f * out_f + point].
+template <class Derive, class Pw>
+int run_synth_chain(const aeolus_plan_impl* p, const Derive& d, const Pw& pw, int batch, double* out, long out_b,
+                    long out_f, void* work, unsigned* status, cudaStream_t st) {
+  static_assert(Derive::NF == Pw::NIN, "derive/pointwise field count");
+  if (p->kind == kGauss) {
+    double2* FG = static_cast<double2*>(work);
+    int s = launch_synth(p, d, FG, Pw::NIN, batch, st);
+    if (s) return s;
+    RowArgs ra{};
+    ra.batch = batch;
+    ra.FG = FG;
+    ra.nblk = Pw::NIN;
+    ra.gout = out;
+    ra.gout_b = out_b;
+    ra.gout_f = out_f;
+    ra.status = status;
+    return launch_rows<Pw, kInF, kOutGrid>(p, pw, ra, st);
+  }
+  const long nc = p->ncol, np = p->npoints;
+  char* w = static_cast<char*>(work);
+  double* V = reinterpret_cast<double*>(w);
+  w += align256((size_t)batch * Pw::NIN * nc * 8);
+  double* Gr = reinterpret_cast<double*>(w);
+  const long nlm = n_coeff(p->lmax) * batch;
+  derive_cols_kernel<Derive><<<blocks_for(nlm, 128), 128, 0, st>>>(p->lmax, batch, nc, V, d);
+  AE_LAUNCH("derive_cols_kernel");
+  const bool direct = Pw::kIdentity && out_b == np;
+  int s = points_gemm_synth(p, V, direct ? out : Gr, batch * Pw::NIN, st);
+  if (s || direct) return s;
+  points_pointwise_kernel<Pw><<<blocks_for(np * batch, 128), 128, 0, st>>>(
+      np, batch, Gr, (long)Pw::NIN * np, np, out, out_b, out_f, p->coslat, p->fgrid, nullptr, status, pw);
+  AE_LAUNCH("points_pointwise_kernel");
+  return AEOLUS_OK;
+}
+
+// Input grid: in[b * in_b + f * in_f + point].
+template <class Pw, class Epi>
+int run_anal_chain(const aeolus_plan_impl* p, const Pw& pw, const Epi& e, int batch, const double* in, long in_b,
+                   long in_f, void* work, cudaStream_t st) {
+  static_assert(Pw::NOUT == Epi::NF, "pointwise/epilogue field count");
+  if (p->kind == kGauss) {
+    double2* FG = static_cast<double2*>(work);
+    RowArgs ra{};
+    ra.batch = batch;
+    ra.FG = FG;
+    ra.nblk = Pw::NOUT;
+    ra.gin = in;
+    ra.gin_b = in_b;
+    ra.gin_f = in_f;
+    int s = launch_rows<Pw, kInGrid, kOutG>(p, pw, ra, st);
+    if (s) return s;
+    return launch_analysis(p, e, FG, Pw::NOUT, batch, st);
+  }
+  const long nc = p->ncol, np = p->npoints;
+  char* w = static_cast<char*>(work);
+  double* Wt = reinterpret_cast<double*>(w);
+  w += align256((size_t)batch * Pw::NOUT * np * 8);
+  double* C = reinterpret_cast<double*>(w);
+  points_pointwise_kernel<Pw><<<blocks_for(np * batch, 128), 128, 0, st>>>(
+      np, batch, in, in_b, in_f, Wt, (long)Pw::NOUT * np, np, p->coslat, p->fgrid, p->wpts, nullptr, pw);
+  AE_LAUNCH("points_pointwise_kernel");
+  int s = points_gemm_analysis(p, Wt, C, batch * Pw::NOUT, st);
+  if (s) return s;
+  const long n2 = (long)(p->lmax + 1) * (p->lmax + 1) * batch;
+  epilogue_cols_kernel<Epi><<<blocks_for(n2, 128), 128, 0, st>>>(p->lmax, batch, nc, C, e);
+  AE_LAUNCH("epilogue_cols_kernel");
+  return AEOLUS_OK;
+}
+
+}  // namespace aeolus

@@ -1,0 +1,91 @@
+// Shared definitions of the sm_103a spectral library: the plan object,
+// error plumbing, complex helpers and the packed Legendre-table layout.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <string>
+#include <vector>
+
+#include "../../include/aeolus_gb300.h"
+
+namespace aeolus {
+
+// ---------------------------------------------------------------- errors
+void set_error(const std::string& msg);
+int fail(int code, const std::string& msg);
+int cuda_check(cudaError_t e, const char* what);
+#define AE_CUDA(call) do { int _s = ::aeolus::cuda_check((call), #call); if (_s) return _s; } while (0)
+#define AE_LAUNCH(what) do { int _s = ::aeolus::cuda_check(cudaGetLastError(), what); if (_s) return _s; } while (0)
+
+// --------------------------------------------------------------- complex
+__host__ __device__ inline double2 cadd(double2 a, double2 b) { return make_double2(a.x + b.x, a.y + b.y); }
+__host__ __device__ inline double2 csub(double2 a, double2 b) { return make_double2(a.x - b.x, a.y - b.y); }
+__host__ __device__ inline double2 cmul(double2 a, double2 b) {
+  return make_double2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+__host__ __device__ inline double2 cscale(double s, double2 a) { return make_double2(s * a.x, s * a.y); }
+__host__ __device__ inline double2 cconj(double2 a) { return make_double2(a.x, -a.y); }
+// i * a
+__host__ __device__ inline double2 ci(double2 a) { return make_double2(-a.y, a.x); }
+
+// --------------------------------------------------------------- layout
+// Packed m-major triangle: for order m the degrees l = m..L are contiguous.
+__host__ __device__ inline long tri_off(int m, int L) { return (long)m * (L + 1) - (long)m * (m - 1) / 2; }
+__host__ __device__ inline long n_coeff(int L) { return (long)(L + 1) * (L + 2) / 2; }
+
+constexpr int kMaxFactors = 16;
+
+struct FftInfo {
+  int N;            // transform length (nlon)
+  int n;            // complex half length N/2 (FFT path) or ceil(N/2) (buffer stride)
+  int use_fft;      // 1: half-length complex mixed-radix FFT; 0: direct DFT
+  int nfac;
+  int fac[kMaxFactors];
+};
+
+// ------------------------------------------------------------------ plan
+enum PlanKind { kGauss = 0, kPoints = 1 };
+
+struct SplitTables;  // split-precision operand slices (split.cu)
+
+struct aeolus_plan_impl {
+  int kind = kGauss;
+  int nlat = 0, nlon = 0, lmax = 0, nh = 0;
+  long npoints = 0;
+  double radius = 1.0;
+  int precision = AEOLUS_PREC_FP64;
+  int slices = 0;
+  int device = 0;
+  FftInfo fft{};
+  // device tables (Gauss)
+  double* x = nullptr;       // [nlat] cos(colatitude) = sin(latitude)
+  double* wq = nullptr;      // [nlat] w_gl * 2 pi / nlon
+  double* coslat = nullptr;  // [nlat] or [npoints], max(cos lat, 1e-8)
+  double* fgrid = nullptr;   // [nlat] or [npoints]: synthesis of the unit (1,0) mode
+  double* P = nullptr;       // [tri_off(m)*nh + (l-m)*nh + jn]  (row jn fastest)
+  double* PT = nullptr;      // [tri_off(m)*nh + jn*(L+1-m) + (l-m)] (degree fastest)
+  double2* tw = nullptr;     // [nlon] exp(-2 pi i q / nlon)
+  // device tables (points)
+  double* basis = nullptr;   // [npoints][ncol] real basis (cos / sin columns)
+  double* wpts = nullptr;    // [npoints] quadrature weights
+  double* latp = nullptr;    // [npoints]
+  int ncol = 0;              // (L+1)^2 real columns
+  int ld_basis = 0;
+  // shared spectral tables
+  double* cplus = nullptr;   // [(L+1)*(L+1)] C+[l][m], C+[L][:] = 0
+  double* cminus = nullptr;  // [(L+1)*(L+1)] C-[l][m]
+  double* cplus_true = nullptr;
+  // host copies
+  std::vector<double> h_lat, h_wgl;
+  SplitTables* split = nullptr;
+};
+
+inline bool plan_ok(const aeolus_plan_impl* p) { return p != nullptr && p->lmax >= 0; }
+
+// Spectral tables (host), identical arithmetic to spectral_operators.py:135-176.
+void sin_theta_tables(int L, std::vector<double>& cp, std::vector<double>& cm, bool clip_top);
+
+}  // namespace aeolus
+
+struct aeolus_plan_s : aeolus::aeolus_plan_impl {};

@@ -1,0 +1,97 @@
+// Launch helpers that chain the three Gauss stages
+//   legendre_synth<Derive>  ->  row_kernel<Pointwise>  ->  legendre_analysis<Epilogue>
+// and the equivalent point-set chain (points.cu) behind one interface.
+#pragma once
+
+#include <algorithm>
+
+#include "common.cuh"
+#include "legendre.cuh"
+#include "rows.cuh"
+
+namespace aeolus {
+
+constexpr int kSynthCPT = 3;
+
+inline int pick_bc(int L, int batch) {
+  const long ctas = (long)n_pairs(L) * batch;
+  int bc = (int)std::max(1L, std::min(4L, ctas / 608));
+  return std::min(bc, std::max(batch, 1));
+}
+
+template <class K>
+inline int allow_smem(K kern, size_t bytes) {
+  if (bytes > 48 * 1024) {
+    if (bytes > 227 * 1024) return fail(AEOLUS_ERR_ARG, "shared-memory tile exceeds 227 KB for this size");
+    AE_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
+  }
+  return AEOLUS_OK;
+}
+
+inline int round_threads(long items, int lo, int hi) {
+  long t = (items + 31) / 32 * 32;
+  return (int)std::max<long>(lo, std::min<long>(hi, t));
+}
+
+template <class Derive>
+int launch_synth(const aeolus_plan_impl* p, const Derive& d, double2* FG, int nblk, int batch,
+                 cudaStream_t st) {
+  const int L = p->lmax;
+  const int bc = pick_bc(L, batch);
+  LegArgs a{L, p->nlat, p->nh, batch, bc, p->P, p->PT, FG, nblk};
+  const size_t sm = synth_smem_bytes<Derive, kSynthCPT>(L, bc);
+  auto kern = legendre_synth_kernel<Derive, kSynthCPT>;
+  int s = allow_smem(kern, sm);
+  if (s) return s;
+  const int ngroups = (bc * Derive::NF + kSynthCPT - 1) / kSynthCPT;
+  const int threads = round_threads((long)p->nh * ngroups, 64, 256);
+  dim3 grid(n_pairs(L), (batch + bc - 1) / bc);
+  kern<<<grid, threads, sm, st>>>(a, d);
+  AE_LAUNCH("legendre_synth_kernel");
+  return AEOLUS_OK;
+}
+
+template <class Epi>
+int launch_analysis(const aeolus_plan_impl* p, const Epi& e, double2* FG, int nblk, int batch,
+                    cudaStream_t st) {
+  const int L = p->lmax;
+  const int bc = pick_bc(L, batch);
+  LegArgs a{L, p->nlat, p->nh, batch, bc, p->P, p->PT, FG, nblk};
+  const size_t sm = analysis_smem_bytes<Epi>(p->nh, bc);
+  auto kern = legendre_analysis_kernel<Epi>;
+  int s = allow_smem(kern, sm);
+  if (s) return s;
+  const int threads = round_threads((long)bc * (L + 2), 64, 256);
+  dim3 grid(n_pairs(L), (batch + bc - 1) / bc);
+  kern<<<grid, threads, sm, st>>>(a, e);
+  AE_LAUNCH("legendre_analysis_kernel");
+  return AEOLUS_OK;
+}
+
+template <class Pw, int IN_MODE, int OUT_MODE>
+int launch_rows(const aeolus_plan_impl* p, const Pw& pw, RowArgs a, cudaStream_t st) {
+  a.L = p->lmax;
+  a.nlat = p->nlat;
+  a.fft = p->fft;
+  a.tw = p->tw;
+  a.coslat = p->coslat;
+  a.fgrid = p->fgrid;
+  a.wq = p->wq;
+  const size_t sm = row_smem_bytes<Pw>(p->fft);
+  auto kern = row_kernel<Pw, IN_MODE, OUT_MODE>;
+  int s = allow_smem(kern, sm);
+  if (s) return s;
+  dim3 grid(p->nlat, a.batch);
+  kern<<<grid, 256, sm, st>>>(a, pw);
+  AE_LAUNCH("row_kernel");
+  return AEOLUS_OK;
+}
+
+// Bytes of the F/G block area for `nblk` fields per (member, row).
+inline size_t fg_bytes(const aeolus_plan_impl* p, int nblk, int batch) {
+  return (size_t)batch * p->nlat * nblk * (p->lmax + 1) * sizeof(double2);
+}
+
+inline size_t align256(size_t x) { return (x + 255) / 256 * 256; }
+
+}  // namespace aeolus

@@ -1,0 +1,358 @@
+// Plan construction: Gauss-Legendre nodes (FP64 Newton on the device),
+// normalised associated-Legendre tables, FFT factorisation and twiddles,
+// sin(theta) d/dtheta coupling tables; point-set plans build a dense real
+// basis on the device.
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+
+#include "common.cuh"
+
+namespace aeolus {
+
+static thread_local std::string g_last_error;
+
+void set_error(const std::string& msg) { g_last_error = msg; }
+
+int fail(int code, const std::string& msg) {
+  set_error(msg);
+  return code;
+}
+
+int cuda_check(cudaError_t e, const char* what) {
+  if (e == cudaSuccess) return AEOLUS_OK;
+  set_error(std::string(what) + ": " + cudaGetErrorString(e));
+  return AEOLUS_ERR_CUDA;
+}
+
+// C+/C- of spectral_operators.py:135-176, same operation order:
+//   C+ = l * sqrt(max((l+1)^2 - m^2, 0) / max((2l+1)(2l+3), 1))
+//   C- = -(l+1) * sqrt(max(l^2 - m^2, 0) / max((2l-1)(2l+1), 1))
+// zero where m > l; C+[L][:] = 0 when clip_top; C-[0][:] = 0.
+void sin_theta_tables(int L, std::vector<double>& cp, std::vector<double>& cm, bool clip_top) {
+  const int n = L + 1;
+  cp.assign((size_t)n * n, 0.0);
+  cm.assign((size_t)n * n, 0.0);
+  for (int l = 0; l < n; ++l) {
+    for (int m = 0; m <= l; ++m) {
+      const double lb = l, mb = m;
+      double np = (lb + 1.0) * (lb + 1.0) - mb * mb;
+      double dp = (2.0 * lb + 1.0) * (2.0 * lb + 3.0);
+      cp[(size_t)l * n + m] = lb * std::sqrt(std::fmax(np, 0.0) / std::fmax(dp, 1.0));
+      double nm = lb * lb - mb * mb;
+      double dm = (2.0 * lb - 1.0) * (2.0 * lb + 1.0);
+      cm[(size_t)l * n + m] = -(lb + 1.0) * std::sqrt(std::fmax(nm, 0.0) / std::fmax(dm, 1.0));
+    }
+  }
+  if (clip_top)
+    for (int m = 0; m < n; ++m) cp[(size_t)L * n + m] = 0.0;
+  for (int m = 0; m < n; ++m) cm[m] = 0.0;
+}
+
+namespace {
+
+constexpr double kPi = 3.14159265358979323846;
+constexpr double kInvSqrt4Pi = 0.28209479177387814347;  // 1/sqrt(4 pi)
+
+// Gauss-Legendre nodes (descending x = cos colatitude) and weights by
+// Newton's method on P_n, symmetric by construction; the middle node of an
+// odd rule is exactly 0.  One thread per northern node.
+__global__ void gauss_nodes_kernel(int n, double* x, double* w) {
+  const int nh = (n + 1) / 2;
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= nh) return;
+  const bool middle = (n & 1) && j == nh - 1;
+  double z = middle ? 0.0 : cos(kPi * (j + 0.75) / (n + 0.5));
+  double dp = 1.0;
+  for (int it = 0; it < 64; ++it) {
+    double p0 = 1.0, p1 = z;
+    for (int k = 1; k < n; ++k) {
+      double p2 = ((2.0 * k + 1.0) * z * p1 - k * p0) / (k + 1.0);
+      p0 = p1;
+      p1 = p2;
+    }
+    dp = n * (z * p1 - p0) / ((z - 1.0) * (z + 1.0));
+    if (middle) break;
+    double dz = p1 / dp;
+    z -= dz;
+    if (fabs(dz) <= 4e-17) {
+      // one refinement of dp at the converged node
+      double q0 = 1.0, q1 = z;
+      for (int k = 1; k < n; ++k) {
+        double q2 = ((2.0 * k + 1.0) * z * q1 - k * q0) / (k + 1.0);
+        q0 = q1;
+        q1 = q2;
+      }
+      dp = n * (z * q1 - q0) / ((z - 1.0) * (z + 1.0));
+      break;
+    }
+  }
+  const double wt = 2.0 / ((1.0 - z) * (1.0 + z) * dp * dp);
+  x[j] = z;
+  x[n - 1 - j] = -z;
+  w[j] = wt;
+  w[n - 1 - j] = wt;
+}
+
+// Orthonormal P_lm (Condon-Shortley phase) at the northern nodes, by the
+// stable normalised recurrence; writes both packed layouts.
+__global__ void legendre_table_kernel(int L, int nh, const double* __restrict__ x,
+                                      double* __restrict__ P, double* __restrict__ PT) {
+  const int jn = blockIdx.x * blockDim.x + threadIdx.x;
+  const int m = blockIdx.y;
+  if (jn >= nh || m > L) return;
+  const double xv = x[jn];
+  const double s = sqrt((1.0 - xv) * (1.0 + xv));
+  double pmm = kInvSqrt4Pi;
+  for (int k = 1; k <= m; ++k) pmm = -sqrt((2.0 * k + 1.0) / (2.0 * k)) * s * pmm;
+  const long base = tri_off(m, L) * nh;
+  const int K = L + 1 - m;
+  double* prow = P + base;
+  double* pcol = PT + base + (long)jn * K;
+  prow[jn] = pmm;
+  pcol[0] = pmm;
+  if (m == L) return;
+  double p2 = pmm;
+  double p1 = sqrt(2.0 * m + 3.0) * xv * pmm;
+  prow[(long)nh + jn] = p1;
+  pcol[1] = p1;
+  for (int l = m + 2; l <= L; ++l) {
+    const double a = sqrt((4.0 * l * l - 1.0) / ((double)l * l - (double)m * m));
+    const double b = sqrt(((l - 1.0) * (l - 1.0) - (double)m * m) / (4.0 * (l - 1.0) * (l - 1.0) - 1.0));
+    const double p = a * (xv * p1 - b * p2);
+    prow[(long)(l - m) * nh + jn] = p;
+    pcol[l - m] = p;
+    p2 = p1;
+    p1 = p;
+  }
+}
+
+// coslat (clamped like spherical_backend.py:72,129) and the synthesis of
+// the unit (1,0) mode, sqrt(3/(4 pi)) x, per row.
+__global__ void row_metrics_kernel(int n, const double* __restrict__ x, double* coslat, double* fgrid) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= n) return;
+  const double xv = x[j];
+  coslat[j] = fmax(sqrt((1.0 - xv) * (1.0 + xv)), 1e-8);
+  fgrid[j] = sqrt(3.0) * kInvSqrt4Pi * xv;
+}
+
+// exp(-2 pi i q / N) with octant reduction for accuracy.
+void twiddles(int N, std::vector<double2>& tw) {
+  tw.resize(N);
+  for (int q = 0; q < N; ++q) {
+    // angle = 2 pi q / N, reduced to the first octant by exact integer
+    // quadrant arithmetic when 4 | N.
+    double c, s;
+    if (N % 4 == 0) {
+      int quarter = N / 4;
+      int k = q / quarter;
+      int r = q - k * quarter;
+      double ang = 2.0 * kPi * r / N;
+      double cr, sr;
+      if (2 * r <= quarter) {
+        cr = std::cos(ang);
+        sr = std::sin(ang);
+      } else {  // use complementary angle pi/2 - ang for better accuracy
+        double comp = 2.0 * kPi * (quarter - r) / N;
+        cr = std::sin(comp);
+        sr = std::cos(comp);
+      }
+      switch (k & 3) {
+        case 0: c = cr; s = sr; break;
+        case 1: c = -sr; s = cr; break;
+        case 2: c = -cr; s = -sr; break;
+        default: c = sr; s = -cr; break;
+      }
+    } else {
+      double ang = 2.0 * kPi * q / N;
+      c = std::cos(ang);
+      s = std::sin(ang);
+    }
+    tw[q] = make_double2(c, -s);
+  }
+}
+
+void plan_fft(int N, int L, FftInfo& f) {
+  std::memset(&f, 0, sizeof(f));
+  f.N = N;
+  f.n = (N + 1) / 2;
+  f.use_fft = 0;
+  if (N % 2 != 0) return;
+  int n = N / 2;
+  if (L > n - 1) return;  // Nyquist / aliased orders: direct DFT handles them
+  int rem = n, nf = 0, fac[kMaxFactors];
+  while (rem % 4 == 0 && nf < kMaxFactors) { fac[nf++] = 4; rem /= 4; }
+  const int radices[3] = {2, 3, 5};
+  for (int r : radices)
+    while (rem % r == 0 && nf < kMaxFactors) { fac[nf++] = r; rem /= r; }
+  if (rem != 1) return;
+  f.use_fft = 1;
+  f.n = n;
+  f.nfac = nf;
+  for (int i = 0; i < nf; ++i) f.fac[i] = fac[i];
+}
+
+int upload(double** dst, const std::vector<double>& src) {
+  AE_CUDA(cudaMalloc(dst, src.size() * sizeof(double)));
+  AE_CUDA(cudaMemcpy(*dst, src.data(), src.size() * sizeof(double), cudaMemcpyHostToDevice));
+  return AEOLUS_OK;
+}
+
+int common_tables(aeolus_plan_impl* p) {
+  std::vector<double> cp, cm, cpt, dummy;
+  sin_theta_tables(p->lmax, cp, cm, true);
+  sin_theta_tables(p->lmax, cpt, dummy, false);
+  int s;
+  if ((s = upload(&p->cplus, cp))) return s;
+  if ((s = upload(&p->cminus, cm))) return s;
+  if ((s = upload(&p->cplus_true, cpt))) return s;
+  return AEOLUS_OK;
+}
+
+void free_plan(aeolus_plan_impl* p) {
+  double* bufs[] = {p->x, p->wq, p->coslat, p->fgrid, p->P, p->PT, p->basis, p->wpts,
+                    p->latp, p->cplus, p->cminus, p->cplus_true};
+  for (double* b : bufs)
+    if (b) cudaFree(b);
+  if (p->tw) cudaFree(p->tw);
+}
+
+}  // namespace
+
+void free_split(aeolus_plan_impl* p);  // split.cu
+int build_points_basis(aeolus_plan_impl* p, const double* lat, const double* lon);  // points.cu
+
+}  // namespace aeolus
+
+using namespace aeolus;
+
+extern "C" const char* aeolus_last_error(void) { return g_last_error.c_str(); }
+
+extern "C" int aeolus_version(void) { return 10000; }
+
+extern "C" int aeolus_plan_create_gauss(int nlat, int nlon, int lmax, double radius, int flags,
+                                        aeolus_plan* out) {
+  (void)flags;
+  if (!out) return fail(AEOLUS_ERR_ARG, "aeolus_plan_create_gauss: out is NULL");
+  *out = nullptr;
+  if (nlat < 2 || nlon < 4)
+    return fail(AEOLUS_ERR_ARG, "GaussLatLonGridGeometry needs nlat >= 2 and nlon >= 4, got (" +
+                                    std::to_string(nlat) + ", " + std::to_string(nlon) + ")");
+  if (lmax < 0 || lmax > 2047) return fail(AEOLUS_ERR_ARG, "lmax must be in [0, 2047]");
+  if (!(radius > 0.0) || !std::isfinite(radius)) return fail(AEOLUS_ERR_ARG, "radius must be finite and > 0");
+  auto* p = new aeolus_plan_s();
+  p->kind = kGauss;
+  p->nlat = nlat;
+  p->nlon = nlon;
+  p->lmax = lmax;
+  p->nh = (nlat + 1) / 2;
+  p->npoints = (long)nlat * nlon;
+  p->radius = radius;
+  cudaGetDevice(&p->device);
+  plan_fft(nlon, lmax, p->fft);
+  int s = AEOLUS_OK;
+  auto bail = [&](int st) { free_plan(p); delete p; return st; };
+  const int L = lmax, nh = p->nh;
+  const long ntab = n_coeff(L) * nh;
+  double* wgl = nullptr;
+  if ((s = cuda_check(cudaMalloc(&p->x, nlat * sizeof(double)), "cudaMalloc"))) return bail(s);
+  if ((s = cuda_check(cudaMalloc(&wgl, nlat * sizeof(double)), "cudaMalloc"))) return bail(s);
+  gauss_nodes_kernel<<<(nh + 127) / 128, 128>>>(nlat, p->x, wgl);
+  if ((s = cuda_check(cudaGetLastError(), "gauss_nodes_kernel"))) { cudaFree(wgl); return bail(s); }
+  p->h_lat.resize(nlat);
+  p->h_wgl.resize(nlat);
+  std::vector<double> hx(nlat);
+  if ((s = cuda_check(cudaMemcpy(hx.data(), p->x, nlat * sizeof(double), cudaMemcpyDeviceToHost), "nodes"))) {
+    cudaFree(wgl);
+    return bail(s);
+  }
+  s = cuda_check(cudaMemcpy(p->h_wgl.data(), wgl, nlat * sizeof(double), cudaMemcpyDeviceToHost), "weights");
+  cudaFree(wgl);
+  if (s) return bail(s);
+  std::vector<double> hwq(nlat);
+  for (int j = 0; j < nlat; ++j) {
+    p->h_lat[j] = kPi / 2.0 - std::acos(hx[j]);  // latlon_grid.py:63-64
+    hwq[j] = p->h_wgl[j] * (2.0 * kPi / nlon);   // latlon_grid.py:82
+  }
+  if ((s = upload(&p->wq, hwq))) return bail(s);
+  if ((s = cuda_check(cudaMalloc(&p->coslat, nlat * sizeof(double)), "cudaMalloc"))) return bail(s);
+  if ((s = cuda_check(cudaMalloc(&p->fgrid, nlat * sizeof(double)), "cudaMalloc"))) return bail(s);
+  row_metrics_kernel<<<(nlat + 127) / 128, 128>>>(nlat, p->x, p->coslat, p->fgrid);
+  if ((s = cuda_check(cudaGetLastError(), "row_metrics_kernel"))) return bail(s);
+  if ((s = cuda_check(cudaMalloc(&p->P, ntab * sizeof(double)), "cudaMalloc P"))) return bail(s);
+  if ((s = cuda_check(cudaMalloc(&p->PT, ntab * sizeof(double)), "cudaMalloc PT"))) return bail(s);
+  dim3 g((nh + 63) / 64, L + 1);
+  legendre_table_kernel<<<g, 64>>>(L, nh, p->x, p->P, p->PT);
+  if ((s = cuda_check(cudaGetLastError(), "legendre_table_kernel"))) return bail(s);
+  std::vector<double2> tw;
+  twiddles(nlon, tw);
+  if ((s = cuda_check(cudaMalloc(&p->tw, nlon * sizeof(double2)), "cudaMalloc tw"))) return bail(s);
+  if ((s = cuda_check(cudaMemcpy(p->tw, tw.data(), nlon * sizeof(double2), cudaMemcpyHostToDevice), "tw")))
+    return bail(s);
+  if ((s = common_tables(p))) return bail(s);
+  if ((s = cuda_check(cudaDeviceSynchronize(), "plan build"))) return bail(s);
+  *out = p;
+  return AEOLUS_OK;
+}
+
+extern "C" int aeolus_plan_create_points(long n, const double* lat, const double* lon, const double* w,
+                                         int lmax, double radius, int flags, aeolus_plan* out) {
+  (void)flags;
+  if (!out) return fail(AEOLUS_ERR_ARG, "aeolus_plan_create_points: out is NULL");
+  *out = nullptr;
+  if (n < 1 || !lat || !lon) return fail(AEOLUS_ERR_ARG, "point set needs n >= 1 and lat/lon arrays");
+  if (lmax < 0 || lmax > 1023) return fail(AEOLUS_ERR_ARG, "lmax must be in [0, 1023]");
+  if (!(radius > 0.0) || !std::isfinite(radius)) return fail(AEOLUS_ERR_ARG, "radius must be finite and > 0");
+  auto* p = new aeolus_plan_s();
+  p->kind = kPoints;
+  p->npoints = n;
+  p->lmax = lmax;
+  p->radius = radius;
+  p->ncol = (lmax + 1) * (lmax + 1);
+  cudaGetDevice(&p->device);
+  auto bail = [&](int st) { free_plan(p); delete p; return st; };
+  std::vector<double> hw(n), hlat(lat, lat + n), hcos(n), hf(n);
+  for (long i = 0; i < n; ++i) {
+    hw[i] = w ? w[i] : 4.0 * kPi / n;  // fast_geodesic_sh.py:35-39
+    hcos[i] = std::fmax(std::cos(lat[i]), 1e-8);
+    hf[i] = std::sqrt(3.0) * kInvSqrt4Pi * std::sin(lat[i]);
+  }
+  int s;
+  if ((s = upload(&p->wpts, hw))) return bail(s);
+  if ((s = upload(&p->latp, hlat))) return bail(s);
+  if ((s = upload(&p->coslat, hcos))) return bail(s);
+  if ((s = upload(&p->fgrid, hf))) return bail(s);
+  if ((s = build_points_basis(p, lat, lon))) return bail(s);
+  if ((s = common_tables(p))) return bail(s);
+  if ((s = cuda_check(cudaDeviceSynchronize(), "plan build"))) return bail(s);
+  *out = p;
+  return AEOLUS_OK;
+}
+
+extern "C" int aeolus_plan_destroy(aeolus_plan plan) {
+  if (!plan) return AEOLUS_OK;
+  free_split(plan);
+  free_plan(plan);
+  delete plan;
+  return AEOLUS_OK;
+}
+
+extern "C" int aeolus_plan_info(aeolus_plan plan, int* kind, int* nlat, int* nlon, int* lmax, long* npts) {
+  if (!plan) return fail(AEOLUS_ERR_ARG, "plan is NULL");
+  if (kind) *kind = plan->kind;
+  if (nlat) *nlat = plan->nlat;
+  if (nlon) *nlon = plan->nlon;
+  if (lmax) *lmax = plan->lmax;
+  if (npts) *npts = plan->npoints;
+  return AEOLUS_OK;
+}
+
+extern "C" int aeolus_plan_nodes(aeolus_plan plan, double* lat, double* w_gl) {
+  if (!plan) return fail(AEOLUS_ERR_ARG, "plan is NULL");
+  if (plan->kind != kGauss) return fail(AEOLUS_ERR_ARG, "aeolus_plan_nodes needs a Gauss plan");
+  if (lat) std::memcpy(lat, plan->h_lat.data(), plan->nlat * sizeof(double));
+  if (w_gl) std::memcpy(w_gl, plan->h_wgl.data(), plan->nlat * sizeof(double));
+  return AEOLUS_OK;
+}

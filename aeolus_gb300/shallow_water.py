@@ -1,0 +1,174 @@
+"""Rotating shallow-water core on the GB300 path.
+
+Mirrors src/planetary_sandbox/physics/shallow_water.py:102-539 (flat
+bottom).  ``tendency`` is one fused chain on the product space: nine
+syntheses (u cos, v cos, eta_lam, eta_snt, phi_lam, phi_snt, zeta, delta,
+phi), the pointwise flux products, four analyses, the 2/3 cut and the exact
+linear terms.  ``rk4`` advances whole steps on the device and checks every
+stage state (NaN/Inf, fluid thickness) without host synchronisation.
+"""
+from __future__ import annotations
+
+import math
+from dataclasses import dataclass
+
+import torch
+
+from . import _lib
+from .ops import spectral_op, swe_invariants, swe_rk4, swe_tendency, swe_validate, winds
+
+WILLIAMSON_GRAVITY = 9.80616
+ZETA, DELTA, PHI = 0, 1, 2
+PROGNOSTICS = ("zeta", "delta", "phi")
+
+
+def _or_bits(status: torch.Tensor) -> int:
+    bits = 0
+    for v in status.reshape(-1).tolist():
+        bits |= int(v)
+    return bits
+
+
+class ShallowWaterStateError(ValueError):
+    """A shallow-water state violated a hard physical/numerical constraint."""
+
+
+@dataclass
+class ShallowWaterState:
+    coeffs: torch.Tensor
+
+    @classmethod
+    def from_fields(cls, zeta_lm, delta_lm, phi_lm) -> "ShallowWaterState":
+        return cls(torch.stack([torch.as_tensor(x, dtype=torch.complex128) for x in (zeta_lm, delta_lm, phi_lm)]))
+
+    @classmethod
+    def zeros(cls, l_max: int, device=None) -> "ShallowWaterState":
+        n = l_max + 1
+        return cls(torch.zeros((3, n, n), dtype=torch.complex128, device=device or "cuda"))
+
+    zeta = property(lambda self: self.coeffs[ZETA])
+    delta = property(lambda self: self.coeffs[DELTA])
+    phi = property(lambda self: self.coeffs[PHI])
+
+
+class ShallowWaterModel:
+    _MONOPOLE_RTOL = 1e-10
+
+    def __init__(self, planet, *, gravity: float = WILLIAMSON_GRAVITY, mean_depth: float,
+                 hyperdiffusion_nu4: float = 0.0, topography=None):
+        if not (math.isfinite(gravity) and gravity > 0):
+            raise ValueError(f"gravity must be finite and > 0, got {gravity}")
+        if not (math.isfinite(mean_depth) and mean_depth > 0):
+            raise ValueError(f"mean_depth must be finite and > 0, got {mean_depth}")
+        if not (math.isfinite(hyperdiffusion_nu4) and hyperdiffusion_nu4 >= 0):
+            raise ValueError(f"hyperdiffusion_nu4 must be finite and >= 0, got {hyperdiffusion_nu4}")
+        if topography is not None and not getattr(topography, "is_flat", False):
+            raise ValueError("bottom topography is not part of the GB300 shallow-water path (flat bottom only)")
+        self.planet = planet
+        self.sh = planet.sh
+        self.so = planet.so
+        self.grid = planet.grid
+        self.R = float(planet.params.radius)
+        self.Omega = float(planet.params.angular_velocity)
+        self.gravity = float(gravity)
+        self.mean_depth = float(mean_depth)
+        self.phi0 = self.gravity * self.mean_depth
+        self.nu4 = float(hyperdiffusion_nu4)
+        self.l_max = self.sh.l_max
+        dev = self.sh.weights.device
+        self.f_lm = torch.zeros((self.l_max + 1, self.l_max + 1), dtype=torch.complex128, device=dev)
+        self.f_lm[1, 0] = 2.0 * self.Omega * math.sqrt(4.0 * math.pi / 3.0)
+        l = torch.arange(self.l_max + 1, dtype=torch.float64, device=dev)
+        self.lap_eigs = -l * (l + 1.0) / self.R ** 2
+        self._ps = self.so.backend.product_space(self.so.product_quadrature)
+        self._plan = self._ps.sh.plan
+        self._state_plan = self.sh.plan
+        self.has_topography = False
+        self.surface_elevation_extrema = (0.0, 0.0)
+
+    # -- Helmholtz / winds -------------------------------------------------
+    def _inv_laplacian(self, coeffs):
+        return spectral_op(_lib.SOP_INV_LAPLACIAN_ZERO, self.R, coeffs)
+
+    def helmholtz(self, state: ShallowWaterState):
+        return self._inv_laplacian(state.coeffs[ZETA]), self._inv_laplacian(state.coeffs[DELTA])
+
+    def wind_on_state_grid(self, state: ShallowWaterState):
+        psi, chi = self.helmholtz(state)
+        uv = winds(self._state_plan.id, self.R, psi, chi)
+        return uv[0], uv[1]
+
+    def surface_geopotential_on_state_grid(self):
+        return None
+
+    # -- tendencies ----------------------------------------------------------
+    def tendency(self, coeffs: torch.Tensor) -> torch.Tensor:
+        """d/dt of the (..., 3, L+1, L+1) stack, shallow_water.py:347-418."""
+        return swe_tendency(self._plan.id, self.R, self.Omega, self.gravity, self.mean_depth, self.nu4, coeffs)
+
+    def tendency_state(self, state: ShallowWaterState) -> ShallowWaterState:
+        return ShallowWaterState(self.tendency(state.coeffs))
+
+    def rk4(self, coeffs: torch.Tensor, dt: float, nsteps: int = 1, check: bool = True):
+        """nsteps fused RK4 steps.  Stage states are checked on the product
+        grid on the device; with ``check`` the bits are read once at the end
+        and a violation raises ShallowWaterStateError."""
+        y, status = swe_rk4(self._plan.id, self.R, self.Omega, self.gravity, self.mean_depth, self.nu4, coeffs,
+                            float(dt), int(nsteps))
+        if check:
+            bits = _or_bits(status)
+            if bits:
+                raise ShallowWaterStateError(self._describe_bits(bits, "during RK4 stages"))
+        return y
+
+    # -- validation ----------------------------------------------------------
+    def _validate_raw(self, coeffs):
+        return swe_validate(self._state_plan.id, self._plan.id, self.R, self.Omega, self.gravity,
+                            self.mean_depth, coeffs)
+
+    def total_geopotential_extrema(self, state: ShallowWaterState):
+        """(min, max) of Phi0 + phi over the state and product samplings."""
+        _, ext = self._validate_raw(state.coeffs)
+        e = ext.reshape(-1, 2)[0].tolist()
+        return e[0], e[1]
+
+    def characteristic_fields(self, state: ShallowWaterState) -> dict:
+        u, v = self.wind_on_state_grid(state)
+        wind = torch.sqrt(u * u + v * v)
+        phi_total = self.phi0 + self.sh.inv_transform(state.coeffs[PHI])
+        return {"u": u, "v": v, "wind_speed": wind, "phi_total": phi_total,
+                "phi_total_extrema": self.total_geopotential_extrema(state)}
+
+    def max_characteristic_speed(self, state: ShallowWaterState) -> float:
+        f = self.characteristic_fields(state)
+        _, phi_max = f["phi_total_extrema"]
+        return float(f["wind_speed"].max()) + math.sqrt(max(phi_max, 0.0))
+
+    def _describe_bits(self, bits: int, where: str) -> str:
+        parts = []
+        if bits & _lib.STATE_NONFINITE:
+            parts.append("shallow-water state contains NaN/Inf coefficients")
+        if bits & _lib.STATE_MONOPOLE:
+            parts.append("a monopole (zeta, delta or phi a00) is nonzero; the global mean must stay exactly zero")
+        if bits & _lib.STATE_THICKNESS:
+            parts.append(f"fluid thickness is not strictly positive (min(Phi0 + phi) <= 0, Phi0 = {self.phi0:g}); "
+                         "the fluid depth has collapsed")
+        return "; ".join(parts) + (f" {where}" if where else "")
+
+    def validate_state(self, state: ShallowWaterState, *, context: str = "") -> None:
+        """Raise ShallowWaterStateError on a violated constraint, :494-539."""
+        status, ext = self._validate_raw(state.coeffs)
+        bits = _or_bits(status)
+        if bits:
+            msg = self._describe_bits(bits, context)
+            if bits & _lib.STATE_THICKNESS:
+                msg += f" (min(Phi0 + phi) = {float(ext.reshape(-1, 2)[:, 0].min()):g} m^2/s^2)"
+            raise ShallowWaterStateError(msg)
+
+    # -- diagnostics -------------------------------------------------------
+    def invariants(self, state: ShallowWaterState) -> dict:
+        """Spectral mass, quadrature energy and L2 norms (run/swe/diagnostics.py:76-173)."""
+        out = swe_invariants(self._state_plan.id, self.R, self.Omega, self.gravity, self.mean_depth, state.coeffs)
+        keys = ("total_mass", "total_energy", "zeta_l2", "delta_l2", "phi_l2")
+        vals = out.reshape(-1, 5)[0].tolist()
+        return dict(zip(keys, vals))

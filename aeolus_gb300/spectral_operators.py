@@ -1,0 +1,114 @@
+"""Spectral operators on the shared (L+1, L+1) complex layout.
+
+Mirrors src/planetary_sandbox/numerics/spectral_operators.py:53-658.  The
+diagonal / tridiagonal operators run as one elementwise kernel each
+(``aeolus_spectral_op``); the pseudospectral Jacobian is one fused chain
+(derivative coefficients -> synthesis -> product -> analysis -> 2/3 cut).
+"""
+from __future__ import annotations
+
+import torch
+
+from . import _lib
+from .ops import jacobian, spectral_op, winds
+from .spherical_backend import make_backend
+
+
+class SpectralOperators:
+    def __init__(self, sh, radius: float, grid=None, product_quadrature: str = "coarse", backend=None):
+        self.sh = sh
+        self.R = float(radius)
+        self.l_max = sh.l_max
+        self.grid = grid
+        self.backend = backend if backend is not None else make_backend(grid, sh)
+        self.product_quadrature = product_quadrature
+        self._product_space = self.backend.product_space(product_quadrature)
+        self.product_grid = self._product_space.geometry
+        self.product_sh = self._product_space.sh if self._product_space.geometry is not None else None
+        dev = getattr(sh, "weights").device
+        l = torch.arange(self.l_max + 1, dtype=torch.float64, device=dev)
+        self.lap_eigs = -l * (l + 1.0) / self.R ** 2          # :114
+
+    # -- diagonal / tridiagonal operators (one kernel each) --------------
+    def laplacian_coeffs(self, coeffs):
+        return spectral_op(_lib.SOP_LAPLACIAN, self.R, coeffs)
+
+    def d_lambda_coeffs(self, coeffs):
+        return spectral_op(_lib.SOP_D_LAMBDA, self.R, coeffs)
+
+    def sin_theta_d_theta_coeffs(self, coeffs):
+        return spectral_op(_lib.SOP_SIN_THETA_D_THETA, self.R, coeffs)
+
+    def adjoint_sin_theta_d_theta_coeffs(self, coeffs):
+        return spectral_op(_lib.SOP_ADJOINT_SIN_THETA_D_THETA, self.R, coeffs)
+
+    def inv_laplacian(self, coeffs):
+        """l = 0 mode divided by 1/R^2 (i.e. times R^2), :275-292."""
+        return spectral_op(_lib.SOP_INV_LAPLACIAN, self.R, coeffs)
+
+    def inv_d_lambda(self, coeffs):
+        """(R / (i m)) a for m >= 1, zero at m = 0, :294-311."""
+        m = torch.arange(self.l_max + 1, dtype=torch.float64, device=coeffs.device)
+        inv = torch.zeros(self.l_max + 1, dtype=torch.complex128, device=coeffs.device)
+        inv[1:] = 1.0 / (1j * m[1:] / self.R)
+        return inv[None, :] * coeffs
+
+    def _truncate_product(self, coeffs):
+        return spectral_op(_lib.SOP_TRUNCATE, self.R, coeffs)
+
+    def laplacian_field(self, coeffs):
+        return self.sh.inv_transform(self.laplacian_coeffs(coeffs))
+
+    def d_lambda_field(self, coeffs):
+        return self.sh.inv_transform(self.d_lambda_coeffs(coeffs))
+
+    def sin_theta_d_theta_field(self, coeffs):
+        return self.sh.inv_transform(self.sin_theta_d_theta_coeffs(coeffs))
+
+    # -- nonlinear ---------------------------------------------------------
+    def jacobian_pseudospectral(self, a_lm, b_lm, dealias: bool = True, return_spectral: bool = False):
+        """J(a, b) = (a_snt b_lam - a_lam b_snt) / cos^2 on the product space,
+        :590-658.  The (dealias, return_spectral) = (True, True) form is one
+        fused chain; the legacy grid-returning forms are composed from it."""
+        ps = self._product_space
+        sh_p = ps.sh
+        if dealias:
+            J_lm = jacobian(sh_p.plan.id, a_lm, b_lm)
+            return J_lm if return_spectral else self.sh.inv_transform(J_lm)
+        a_lam = sh_p.inv_transform(self.d_lambda_coeffs(a_lm))
+        b_lam = sh_p.inv_transform(self.d_lambda_coeffs(b_lm))
+        a_snt = sh_p.inv_transform(self.sin_theta_d_theta_coeffs(a_lm)) / self.R
+        b_snt = sh_p.inv_transform(self.sin_theta_d_theta_coeffs(b_lm)) / self.R
+        J_grid = (a_snt * b_lam - a_lam * b_snt) / ps.coslat ** 2
+        if return_spectral:
+            return sh_p.transform(J_grid)
+        if sh_p is self.sh:
+            return J_grid
+        return self.sh.inv_transform(sh_p.transform(J_grid))
+
+    def velocity_from_streamfunction(self, psi_lm):
+        """(u, v) on the state sampling, |cos lat| < 1e-6 -> 0; :517-538."""
+        uv = winds(self.sh.plan.id, self.R, psi_lm, None)
+        return uv[0], uv[1]
+
+    def grad_from_scalar(self, q_lm):
+        """((1/(R cos)) q_lam, (1/R) q_phi) on the state sampling, :542-560."""
+        coslat = torch.cos(self.sh.latitudes)
+        q_lam = self.sh.inv_transform(self.d_lambda_coeffs(q_lm))
+        gq = self.sh.inv_transform(self.sin_theta_d_theta_coeffs(q_lm))
+        return q_lam / coslat, -gq / (self.R * coslat)
+
+    def advect_scalar_by_streamfunction(self, psi_lm, q_lm, dealias: bool = True, return_spectral: bool = False):
+        """u . grad(q) on the state sampling, :564-588."""
+        u, v = self.velocity_from_streamfunction(psi_lm)
+        dq_dx, dq_dy = self.grad_from_scalar(q_lm)
+        adv = u * dq_dx + v * dq_dy
+        if not (dealias or return_spectral):
+            return adv
+        adv_lm = self.sh.transform(adv)
+        if dealias:
+            adv_lm = self._truncate_product(adv_lm)
+        return adv_lm if return_spectral else self.sh.inv_transform(adv_lm)
+
+
+__all__ = ["SpectralOperators"]

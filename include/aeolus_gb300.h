@@ -1,0 +1,212 @@
+/*
+ * aeolus_gb300 -- C ABI of the GB300 (sm_103a) spectral hot path.
+ *
+ * Spherical-harmonic synthesis/analysis on a Gauss-Legendre grid (per-order
+ * Legendre contraction + longitude real FFT) or on an arbitrary point set
+ * (dense basis product), and the barotropic-vorticity (BVE) and
+ * shallow-water (SWE) tendencies and RK4 steps built on them.
+ *
+ * Conventions (all citations are paths inside the reference project,
+ * planetary_sandbox):
+ *  - Spectral arrays use the reference's dense layout: complex128 values
+ *    stored as interleaved (re, im) doubles, shape [batch][L+1][L+1],
+ *    axis 0 = degree l, axis 1 = order m >= 0 (spectral_operators.py:56-61).
+ *    Slots with m > l are ignored on input and written as zero on output.
+ *  - SWE state stacks are [batch][3][L+1][L+1] (zeta, delta, phi),
+ *    physics/shallow_water.py:106-115.
+ *  - Grid arrays are float64 [batch][n_points]; on a Gauss plan the points
+ *    are lat-major with rows north -> south (latlon_grid.py:72-76).
+ *  - Every data pointer is a DEVICE pointer owned by the caller, except the
+ *    host arrays passed to plan creation / returned by aeolus_plan_nodes.
+ *  - `stream` is a cudaStream_t (NULL = legacy default stream).
+ *  - Calls that need scratch take (work, work_bytes); the size comes from
+ *    aeolus_workspace_bytes().  Hot-path calls never allocate.
+ *  - Status: 0 = ok, nonzero = error; aeolus_last_error() gives the message
+ *    for the calling thread.  Invalid arguments are rejected before any
+ *    launch (the reference raises ValueError, spherical_backend.py:92-97).
+ */
+#ifndef AEOLUS_GB300_H
+#define AEOLUS_GB300_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct aeolus_plan_s* aeolus_plan;
+
+enum aeolus_status {
+  AEOLUS_OK = 0,
+  AEOLUS_ERR_ARG = 1,        /* invalid argument / unsupported shape       */
+  AEOLUS_ERR_CUDA = 2,       /* CUDA runtime error                         */
+  AEOLUS_ERR_WORKSPACE = 3,  /* work buffer missing or too small           */
+  AEOLUS_ERR_STATE = 4       /* state validation failed (see status words) */
+};
+
+enum aeolus_precision {
+  AEOLUS_PREC_FP64 = 0,        /* plain float64 contraction (the drop-in)   */
+  AEOLUS_PREC_SPLIT_BF16 = 1   /* FP64 operands sliced to bf16, tcgen05 MMA */
+};
+
+/* Operation ids for aeolus_workspace_bytes. */
+enum aeolus_op {
+  AEOLUS_OP_SYNTHESIZE = 0,
+  AEOLUS_OP_ANALYZE = 1,
+  AEOLUS_OP_JACOBIAN = 2,
+  AEOLUS_OP_WINDS = 3,
+  AEOLUS_OP_BVE_TENDENCY = 4,
+  AEOLUS_OP_SWE_TENDENCY = 5,
+  AEOLUS_OP_BVE_RK4 = 6,
+  AEOLUS_OP_SWE_RK4 = 7,
+  AEOLUS_OP_SWE_VALIDATE = 8,
+  AEOLUS_OP_SWE_INVARIANTS = 9
+};
+
+/* SWE state-check bits (physics/shallow_water.py:494-539). */
+enum aeolus_state_bits {
+  AEOLUS_STATE_NONFINITE = 1,  /* NaN/Inf coefficient or grid value        */
+  AEOLUS_STATE_MONOPOLE = 2,   /* |a00| > 1e-10 * ||field||                 */
+  AEOLUS_STATE_THICKNESS = 4   /* min(Phi0 + phi) <= 0 on a sampling        */
+};
+
+typedef struct {
+  double radius;     /* a [m]                                             */
+  double omega;      /* rotation rate [1/s]                               */
+  double viscosity;  /* nu [m^2/s], barotropic.py:158                      */
+} aeolus_bve_params;
+
+typedef struct {
+  double radius;       /* a [m]                                           */
+  double omega;        /* [1/s]                                           */
+  double gravity;      /* g [m/s^2]                                       */
+  double mean_depth;   /* H [m]; Phi0 = g H                               */
+  double nu4;          /* hyperdiffusion [m^4/s], shallow_water.py:405-413 */
+} aeolus_swe_params;
+
+const char* aeolus_last_error(void);
+int aeolus_version(void);
+
+/* ---- plans ---------------------------------------------------------- */
+
+/* Gauss-Legendre nlat x nlon grid at truncation lmax: nodes/weights by an
+ * FP64 Newton iteration on the device, normalised P_lm tables, FFT
+ * twiddles.  Replaces GaussLatLonGridGeometry + GaussLatLonSphericalHarmonics
+ * (numerics/latlon_grid.py:43-199) and the basis build of
+ * PointSetSphericalHarmonics (numerics/fast_geodesic_sh.py:15-66,
+ * numerics/cuda/sh_matrix.cu:7-76).  radius only sets operator metrics. */
+int aeolus_plan_create_gauss(int nlat, int nlon, int lmax, double radius,
+                             int flags, aeolus_plan* out);
+
+/* Arbitrary point set (host arrays, n points): dense real basis built on
+ * the device.  Replaces PointSetSphericalHarmonics
+ * (numerics/fast_geodesic_sh.py:15-66); w == NULL gives the reference's
+ * uniform 4*pi/n default (:35-37). */
+int aeolus_plan_create_points(long n, const double* lat, const double* lon,
+                              const double* w, int lmax, double radius,
+                              int flags, aeolus_plan* out);
+
+int aeolus_plan_destroy(aeolus_plan plan);
+
+/* kind: 0 = Gauss, 1 = points.  Any pointer may be NULL. */
+int aeolus_plan_info(aeolus_plan plan, int* kind, int* nlat, int* nlon,
+                     int* lmax, long* n_points);
+
+/* Host copies of the Gauss nodes (latitudes [nlat], north -> south) and
+ * Gauss-Legendre weights [nlat] (sum 2), latlon_grid.py:59-67. */
+int aeolus_plan_nodes(aeolus_plan plan, double* lat, double* w_gl);
+
+/* Contraction precision for later calls on this plan (slices: number of
+ * bf16 slices per FP64 operand, 0 = default). */
+int aeolus_plan_set_precision(aeolus_plan plan, int precision, int slices);
+
+int aeolus_workspace_bytes(aeolus_plan plan, int op, int batch, size_t* bytes);
+
+/* ---- transforms ------------------------------------------------------ */
+
+/* grid[b] = 2 Re(Y a_b) - Re(Y a_b|m=0), fast_geodesic_sh.py:89-107. */
+int aeolus_synthesize(aeolus_plan plan, const double* coeffs, double* grid,
+                      int batch, void* work, size_t work_bytes, void* stream);
+
+/* coeffs[b] = Y^H (w * grid[b]) scattered to the dense layout,
+ * fast_geodesic_sh.py:68-87. */
+int aeolus_analyze(aeolus_plan plan, const double* grid, double* coeffs,
+                   int batch, void* work, size_t work_bytes, void* stream);
+
+/* ---- spectral operators (numerics/spectral_operators.py) -------------- */
+
+/* op: 0 laplacian (:213-218), 1 inverse laplacian with l=0 -> l=0 * R^2
+ * (:275-292), 2 inverse laplacian with l=0 -> 0 (physics/barotropic.py:91,
+ * physics/shallow_water.py:277-281), 3 d/dlambda = i m / R (:220-226),
+ * 4 sin(theta) d/dtheta coupling (:228-241), 5 its adjoint (:243-270),
+ * 6 2/3-rule truncation of rows and columns (:329-334). */
+int aeolus_spectral_op(int op, int lmax, double radius, const double* in,
+                       double* out, int batch, void* stream);
+
+/* J(a, b) analysed on the plan's grid and 2/3-truncated,
+ * spectral_operators.py:590-658 (dealias=True, return_spectral=True). */
+int aeolus_jacobian(aeolus_plan plan, const double* a, const double* b,
+                    double* out, int batch, void* work, size_t work_bytes,
+                    void* stream);
+
+/* Winds on the plan's points from psi, chi: u = (psi_snt + chi_lam)/cos,
+ * v = (psi_lam - chi_snt)/cos (physics/shallow_water.py:305-319), written
+ * as uv[2][batch][n_points] (uv[0] = u, uv[1] = v); chi == NULL gives
+ * velocity_from_streamfunction (spectral_operators.py:517-538). */
+int aeolus_winds(aeolus_plan plan, double radius, const double* psi,
+                 const double* chi, double* uv, int batch,
+                 void* work, size_t work_bytes, void* stream);
+
+/* ---- models ----------------------------------------------------------- */
+
+/* d(zeta)/dt = -J(psi, zeta + f) + nu lap zeta (+ forcing), l = 0 row zero;
+ * physics/barotropic.py:120-167.  `plan` is the product-space plan. */
+int aeolus_bve_tendency(aeolus_plan plan, const aeolus_bve_params* p,
+                        const double* zeta, const double* forcing,
+                        double* tend, int batch, void* work,
+                        size_t work_bytes, void* stream);
+
+/* SWE tendency of [batch][3][L+1][L+1], physics/shallow_water.py:347-418. */
+int aeolus_swe_tendency(aeolus_plan plan, const aeolus_swe_params* p,
+                        const double* state, double* tend, int batch,
+                        void* work, size_t work_bytes, void* stream);
+
+/* nsteps classical RK4 steps in place (run/bve/runner.py:211-216). */
+int aeolus_bve_rk4(aeolus_plan plan, const aeolus_bve_params* p, double* zeta,
+                   int batch, double dt, int nsteps, void* work,
+                   size_t work_bytes, void* stream);
+
+/* nsteps classical RK4 steps in place (run/engine.py:406-431).  When
+ * `status` (device, [batch] uint32) is non-NULL every stage's state is
+ * checked on the product grid and offending AEOLUS_STATE_* bits are OR-ed
+ * in -- the stage validator of run/swe/runner.py:90-95 without host syncs. */
+int aeolus_swe_rk4(aeolus_plan plan, const aeolus_swe_params* p, double* state,
+                   int batch, double dt, int nsteps, unsigned* status,
+                   void* work, size_t work_bytes, void* stream);
+
+/* validate_state (physics/shallow_water.py:494-539) on the state plan and
+ * (when product != state) the product plan: status[b] gets AEOLUS_STATE_*
+ * bits, extrema[b] = (min, max) of Phi0 + phi over the samplings
+ * (total_geopotential_extrema, :428-454).  Either output may be NULL. */
+int aeolus_swe_validate(aeolus_plan state_plan, aeolus_plan product_plan,
+                        const aeolus_swe_params* p, const double* state,
+                        unsigned* status, double* extrema, int batch,
+                        void* work, size_t work_bytes, void* stream);
+
+/* BVE spectral diagnostics, run/bve/diagnostics.py:61-97: out[b][6] =
+ * circulation, energy, enstrophy_rel, enstrophy_abs, energy_l1,
+ * high_l_enstrophy_frac. */
+int aeolus_bve_spectral_diagnostics(int lmax, double radius, double omega,
+                                    const double* zeta, double* out,
+                                    int batch, void* stream);
+
+/* SWE invariants, run/swe/diagnostics.py:76-173: out[b][5] = total_mass,
+ * total_energy (quadrature on the state plan), zeta_l2, delta_l2, phi_l2. */
+int aeolus_swe_invariants(aeolus_plan state_plan, const aeolus_swe_params* p,
+                          const double* state, double* out, int batch,
+                          void* work, size_t work_bytes, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* AEOLUS_GB300_H */
