@@ -37,6 +37,9 @@ class SweParams(ctypes.Structure):
 SIGNATURES = {
     "aeolus_last_error": (c_char_p, []),
     "aeolus_version": (c_int, []),
+    "aeolus_profile_enable": (c_int, [c_int]),
+    "aeolus_profile_collect": (c_int, [c_char_p, c_size_t]),
+    "aeolus_profile_reset": (c_int, []),
     "aeolus_plan_create_gauss": (c_int, [c_int, c_int, c_int, c_double, c_int, POINTER(c_void_p)]),
     "aeolus_plan_create_points": (c_int, [c_long, c_void_p, c_void_p, c_void_p, c_int, c_double, c_int,
                                           POINTER(c_void_p)]),

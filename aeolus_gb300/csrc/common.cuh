@@ -18,6 +18,36 @@ int cuda_check(cudaError_t e, const char* what);
 #define AE_CUDA(call) do { int _s = ::aeolus::cuda_check((call), #call); if (_s) return _s; } while (0)
 #define AE_LAUNCH(what) do { int _s = ::aeolus::cuda_check(cudaGetLastError(), what); if (_s) return _s; } while (0)
 
+// ------------------------------------------------------------- profiling
+// Optional per-kernel CUDA-event timing (aeolus_profile_*).  When enabled,
+// every library launch is bracketed by two events on its own stream; the
+// elapsed times are summed per kernel name at collection.  Disabled by
+// default and never on during stream capture.
+bool prof_enabled();
+void prof_record(const char* name, cudaEvent_t a, cudaEvent_t b);
+cudaEvent_t prof_event();
+
+struct ProfScope {
+  const char* name = nullptr;
+  cudaStream_t st = nullptr;
+  cudaEvent_t a = nullptr;
+  ProfScope(const char* n, cudaStream_t s) {
+    if (prof_enabled()) {
+      name = n;
+      st = s;
+      a = prof_event();
+      cudaEventRecord(a, st);
+    }
+  }
+  ~ProfScope() {
+    if (a) {
+      cudaEvent_t b = prof_event();
+      cudaEventRecord(b, st);
+      prof_record(name, a, b);
+    }
+  }
+};
+
 // --------------------------------------------------------------- complex
 __host__ __device__ inline double2 cadd(double2 a, double2 b) { return make_double2(a.x + b.x, a.y + b.y); }
 __host__ __device__ inline double2 csub(double2 a, double2 b) { return make_double2(a.x - b.x, a.y - b.y); }

@@ -46,6 +46,7 @@ int launch_synth(const aeolus_plan_impl* p, const Derive& d, double2* FG, int nb
   const int ngroups = (bc * Derive::NF + kSynthCPT - 1) / kSynthCPT;
   const int threads = round_threads((long)p->nh * ngroups, 64, 256);
   dim3 grid(n_pairs(L), (batch + bc - 1) / bc);
+  ProfScope prof("legendre_synth_f64", st);
   kern<<<grid, threads, sm, st>>>(a, d);
   AE_LAUNCH("legendre_synth_kernel");
   return AEOLUS_OK;
@@ -63,6 +64,7 @@ int launch_analysis(const aeolus_plan_impl* p, const Epi& e, double2* FG, int nb
   if (s) return s;
   const int threads = round_threads((long)bc * (L + 2), 64, 256);
   dim3 grid(n_pairs(L), (batch + bc - 1) / bc);
+  ProfScope prof("legendre_analysis_f64", st);
   kern<<<grid, threads, sm, st>>>(a, e);
   AE_LAUNCH("legendre_analysis_kernel");
   return AEOLUS_OK;
@@ -82,6 +84,7 @@ int launch_rows(const aeolus_plan_impl* p, const Pw& pw, RowArgs a, cudaStream_t
   int s = allow_smem(kern, sm);
   if (s) return s;
   dim3 grid(p->nlat, a.batch);
+  ProfScope prof(IN_MODE == kInF ? (OUT_MODE == kOutG ? "rows_c2r_products_r2c" : "rows_c2r") : "rows_r2c", st);
   kern<<<grid, 256, sm, st>>>(a, pw);
   AE_LAUNCH("row_kernel");
   return AEOLUS_OK;

@@ -52,58 +52,109 @@ void sin_theta_tables(int L, std::vector<double>& cp, std::vector<double>& cm, b
 
 namespace {
 
+struct ProfState {
+  std::mutex mu;
+  bool enabled = false;
+  std::vector<cudaEvent_t> pool;
+  struct Pending { std::string name; cudaEvent_t a, b; };
+  std::vector<Pending> pending;
+  struct Stat { long launches = 0; double ms = 0.0; };
+  std::vector<std::pair<std::string, Stat>> stats;
+};
+
+ProfState& prof() {
+  static ProfState s;
+  return s;
+}
+
+}  // namespace
+
+bool prof_enabled() { return prof().enabled; }
+
+cudaEvent_t prof_event() {
+  ProfState& s = prof();
+  std::lock_guard<std::mutex> g(s.mu);
+  if (!s.pool.empty()) {
+    cudaEvent_t e = s.pool.back();
+    s.pool.pop_back();
+    return e;
+  }
+  cudaEvent_t e = nullptr;
+  cudaEventCreate(&e);
+  return e;
+}
+
+void prof_record(const char* name, cudaEvent_t a, cudaEvent_t b) {
+  ProfState& s = prof();
+  std::lock_guard<std::mutex> g(s.mu);
+  s.pending.push_back({name, a, b});
+}
+
+namespace {
+
 constexpr double kPi = 3.14159265358979323846;
 constexpr double kInvSqrt4Pi = 0.28209479177387814347;  // 1/sqrt(4 pi)
 
-// Gauss-Legendre nodes (descending x = cos colatitude) and weights by
-// Newton's method on P_n, symmetric by construction; the middle node of an
-// odd rule is exactly 0.  One thread per northern node.
-__global__ void gauss_nodes_kernel(int n, double* x, double* w) {
+// Gauss-Legendre nodes and weights by Newton's method in colatitude theta
+// (x = cos theta), so sin(theta) -- which sets the polar weights and the
+// Legendre seeds -- keeps full relative precision near the poles.  Nodes are
+// symmetric by construction; the middle node of an odd rule is exactly
+// x = 0.  One thread per northern node.
+__device__ void legendre_pn(int n, double x, double* pn, double* pn1) {
+  double p0 = 1.0, p1 = x;
+  for (int k = 1; k < n; ++k) {
+    const double p2 = ((2.0 * k + 1.0) * x * p1 - k * p0) / (k + 1.0);
+    p0 = p1;
+    p1 = p2;
+  }
+  *pn = p1;
+  *pn1 = p0;
+}
+
+__global__ void gauss_nodes_kernel(int n, double* x, double* sth, double* theta, double* w) {
   const int nh = (n + 1) / 2;
   const int j = blockIdx.x * blockDim.x + threadIdx.x;
   if (j >= nh) return;
   const bool middle = (n & 1) && j == nh - 1;
-  double z = middle ? 0.0 : cos(kPi * (j + 0.75) / (n + 0.5));
-  double dp = 1.0;
-  for (int it = 0; it < 64; ++it) {
-    double p0 = 1.0, p1 = z;
-    for (int k = 1; k < n; ++k) {
-      double p2 = ((2.0 * k + 1.0) * z * p1 - k * p0) / (k + 1.0);
-      p0 = p1;
-      p1 = p2;
+  double t = middle ? 0.5 * kPi : kPi * (j + 0.75) / (n + 0.5);
+  double xv = cos(t), sv = sin(t), pn, pn1;
+  if (!middle) {
+    for (int it = 0; it < 64; ++it) {
+      legendre_pn(n, xv, &pn, &pn1);
+      // f(t) = P_n(cos t), f'(t) = n (x P_n - P_{n-1}) / sin t
+      const double dt = pn * sv / (n * (xv * pn - pn1));
+      t -= dt;
+      xv = cos(t);
+      sv = sin(t);
+      if (fabs(dt) <= 1e-17) break;
     }
-    dp = n * (z * p1 - p0) / ((z - 1.0) * (z + 1.0));
-    if (middle) break;
-    double dz = p1 / dp;
-    z -= dz;
-    if (fabs(dz) <= 4e-17) {
-      // one refinement of dp at the converged node
-      double q0 = 1.0, q1 = z;
-      for (int k = 1; k < n; ++k) {
-        double q2 = ((2.0 * k + 1.0) * z * q1 - k * q0) / (k + 1.0);
-        q0 = q1;
-        q1 = q2;
-      }
-      dp = n * (z * q1 - q0) / ((z - 1.0) * (z + 1.0));
-      break;
-    }
+  } else {
+    xv = 0.0;
+    sv = 1.0;
   }
-  const double wt = 2.0 / ((1.0 - z) * (1.0 + z) * dp * dp);
-  x[j] = z;
-  x[n - 1 - j] = -z;
+  legendre_pn(n, xv, &pn, &pn1);
+  // w = 2 / ((1 - x^2) P_n'(x)^2),  P_n'(x) = -n (x P_n - P_{n-1}) / sin^2 t
+  const double q = n * (xv * pn - pn1);
+  const double wt = 2.0 * sv * sv / (q * q);
+  x[j] = xv;
+  x[n - 1 - j] = -xv;
+  sth[j] = sv;
+  sth[n - 1 - j] = sv;
+  theta[j] = t;
+  theta[n - 1 - j] = kPi - t;
   w[j] = wt;
   w[n - 1 - j] = wt;
 }
 
 // Orthonormal P_lm (Condon-Shortley phase) at the northern nodes, by the
 // stable normalised recurrence; writes both packed layouts.
-__global__ void legendre_table_kernel(int L, int nh, const double* __restrict__ x,
+__global__ void legendre_table_kernel(int L, int nh, const double* __restrict__ x, const double* __restrict__ sth,
                                       double* __restrict__ P, double* __restrict__ PT) {
   const int jn = blockIdx.x * blockDim.x + threadIdx.x;
   const int m = blockIdx.y;
   if (jn >= nh || m > L) return;
   const double xv = x[jn];
-  const double s = sqrt((1.0 - xv) * (1.0 + xv));
+  const double s = sth[jn];
   double pmm = kInvSqrt4Pi;
   for (int k = 1; k <= m; ++k) pmm = -sqrt((2.0 * k + 1.0) / (2.0 * k)) * s * pmm;
   const long base = tri_off(m, L) * nh;
@@ -130,11 +181,12 @@ __global__ void legendre_table_kernel(int L, int nh, const double* __restrict__ 
 
 // coslat (clamped like spherical_backend.py:72,129) and the synthesis of
 // the unit (1,0) mode, sqrt(3/(4 pi)) x, per row.
-__global__ void row_metrics_kernel(int n, const double* __restrict__ x, double* coslat, double* fgrid) {
+__global__ void row_metrics_kernel(int n, const double* __restrict__ x, const double* __restrict__ sth,
+                                   double* coslat, double* fgrid) {
   const int j = blockIdx.x * blockDim.x + threadIdx.x;
   if (j >= n) return;
   const double xv = x[j];
-  coslat[j] = fmax(sqrt((1.0 - xv) * (1.0 + xv)), 1e-8);
+  coslat[j] = fmax(sth[j], 1e-8);
   fgrid[j] = sqrt(3.0) * kInvSqrt4Pi * xv;
 }
 
@@ -232,6 +284,60 @@ extern "C" const char* aeolus_last_error(void) { return g_last_error.c_str(); }
 
 extern "C" int aeolus_version(void) { return 10000; }
 
+extern "C" int aeolus_profile_enable(int enable) {
+  ProfState& s = prof();
+  std::lock_guard<std::mutex> g(s.mu);
+  s.enabled = enable != 0;
+  return AEOLUS_OK;
+}
+
+extern "C" int aeolus_profile_collect(char* buf, size_t len) {
+  ProfState& s = prof();
+  std::lock_guard<std::mutex> g(s.mu);
+  for (auto& p : s.pending) {
+    float ms = 0.0f;
+    cudaError_t e = cudaEventSynchronize(p.b);
+    if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, p.a, p.b);
+    if (e != cudaSuccess) return cuda_check(e, "aeolus_profile_collect");
+    auto it = s.stats.begin();
+    for (; it != s.stats.end(); ++it)
+      if (it->first == p.name) break;
+    if (it == s.stats.end()) {
+      s.stats.push_back({p.name, {}});
+      it = s.stats.end() - 1;
+    }
+    it->second.launches += 1;
+    it->second.ms += ms;
+    s.pool.push_back(p.a);
+    s.pool.push_back(p.b);
+  }
+  s.pending.clear();
+  std::string out;
+  for (auto& kv : s.stats) {
+    char line[256];
+    std::snprintf(line, sizeof(line), "%s %ld %.6f\n", kv.first.c_str(), kv.second.launches, kv.second.ms);
+    out += line;
+  }
+  if (buf && len) {
+    std::snprintf(buf, len, "%s", out.c_str());
+    if (out.size() + 1 > len) return fail(AEOLUS_ERR_ARG, "aeolus_profile_collect: buffer too small");
+  }
+  return AEOLUS_OK;
+}
+
+extern "C" int aeolus_profile_reset(void) {
+  ProfState& s = prof();
+  std::lock_guard<std::mutex> g(s.mu);
+  for (auto& p : s.pending) {
+    cudaEventSynchronize(p.b);
+    s.pool.push_back(p.a);
+    s.pool.push_back(p.b);
+  }
+  s.pending.clear();
+  s.stats.clear();
+  return AEOLUS_OK;
+}
+
 extern "C" int aeolus_plan_create_gauss(int nlat, int nlon, int lmax, double radius, int flags,
                                         aeolus_plan* out) {
   (void)flags;
@@ -256,35 +362,37 @@ extern "C" int aeolus_plan_create_gauss(int nlat, int nlon, int lmax, double rad
   auto bail = [&](int st) { free_plan(p); delete p; return st; };
   const int L = lmax, nh = p->nh;
   const long ntab = n_coeff(L) * nh;
-  double* wgl = nullptr;
+  struct Tmp {  // node temporaries, freed on every exit path
+    double* p = nullptr;
+    ~Tmp() { if (p) cudaFree(p); }
+  } t_w, t_s, t_t;
+  double *&wgl = t_w.p, *&sth = t_s.p, *&theta = t_t.p;
   if ((s = cuda_check(cudaMalloc(&p->x, nlat * sizeof(double)), "cudaMalloc"))) return bail(s);
   if ((s = cuda_check(cudaMalloc(&wgl, nlat * sizeof(double)), "cudaMalloc"))) return bail(s);
-  gauss_nodes_kernel<<<(nh + 127) / 128, 128>>>(nlat, p->x, wgl);
-  if ((s = cuda_check(cudaGetLastError(), "gauss_nodes_kernel"))) { cudaFree(wgl); return bail(s); }
+  if ((s = cuda_check(cudaMalloc(&sth, nlat * sizeof(double)), "cudaMalloc"))) return bail(s);
+  if ((s = cuda_check(cudaMalloc(&theta, nlat * sizeof(double)), "cudaMalloc"))) return bail(s);
+  gauss_nodes_kernel<<<(nh + 127) / 128, 128>>>(nlat, p->x, sth, theta, wgl);
+  if ((s = cuda_check(cudaGetLastError(), "gauss_nodes_kernel"))) return bail(s);
   p->h_lat.resize(nlat);
   p->h_wgl.resize(nlat);
-  std::vector<double> hx(nlat);
-  if ((s = cuda_check(cudaMemcpy(hx.data(), p->x, nlat * sizeof(double), cudaMemcpyDeviceToHost), "nodes"))) {
-    cudaFree(wgl);
-    return bail(s);
-  }
-  s = cuda_check(cudaMemcpy(p->h_wgl.data(), wgl, nlat * sizeof(double), cudaMemcpyDeviceToHost), "weights");
-  cudaFree(wgl);
+  std::vector<double> htheta(nlat);
+  s = cuda_check(cudaMemcpy(htheta.data(), theta, nlat * sizeof(double), cudaMemcpyDeviceToHost), "nodes");
+  if (!s) s = cuda_check(cudaMemcpy(p->h_wgl.data(), wgl, nlat * sizeof(double), cudaMemcpyDeviceToHost), "weights");
   if (s) return bail(s);
   std::vector<double> hwq(nlat);
   for (int j = 0; j < nlat; ++j) {
-    p->h_lat[j] = kPi / 2.0 - std::acos(hx[j]);  // latlon_grid.py:63-64
-    hwq[j] = p->h_wgl[j] * (2.0 * kPi / nlon);   // latlon_grid.py:82
+    p->h_lat[j] = kPi / 2.0 - htheta[j];        // latlon_grid.py:63-64
+    hwq[j] = p->h_wgl[j] * (2.0 * kPi / nlon);  // latlon_grid.py:82
   }
   if ((s = upload(&p->wq, hwq))) return bail(s);
   if ((s = cuda_check(cudaMalloc(&p->coslat, nlat * sizeof(double)), "cudaMalloc"))) return bail(s);
   if ((s = cuda_check(cudaMalloc(&p->fgrid, nlat * sizeof(double)), "cudaMalloc"))) return bail(s);
-  row_metrics_kernel<<<(nlat + 127) / 128, 128>>>(nlat, p->x, p->coslat, p->fgrid);
+  row_metrics_kernel<<<(nlat + 127) / 128, 128>>>(nlat, p->x, sth, p->coslat, p->fgrid);
   if ((s = cuda_check(cudaGetLastError(), "row_metrics_kernel"))) return bail(s);
   if ((s = cuda_check(cudaMalloc(&p->P, ntab * sizeof(double)), "cudaMalloc P"))) return bail(s);
   if ((s = cuda_check(cudaMalloc(&p->PT, ntab * sizeof(double)), "cudaMalloc PT"))) return bail(s);
   dim3 g((nh + 63) / 64, L + 1);
-  legendre_table_kernel<<<g, 64>>>(L, nh, p->x, p->P, p->PT);
+  legendre_table_kernel<<<g, 64>>>(L, nh, p->x, sth, p->P, p->PT);
   if ((s = cuda_check(cudaGetLastError(), "legendre_table_kernel"))) return bail(s);
   std::vector<double2> tw;
   twiddles(nlon, tw);

@@ -87,6 +87,16 @@ typedef struct {
 const char* aeolus_last_error(void);
 int aeolus_version(void);
 
+/* Per-kernel CUDA-event timing for measurement (no reference counterpart;
+ * the reference times whole calls with time.time(), tests/speed_showdown.py).
+ * enable != 0 brackets every library launch with events on its stream;
+ * collect synchronises the pending events and writes one line per kernel,
+ * "name launches total_ms\n", into buf; reset clears the totals.  Keep it
+ * disabled during CUDA-graph capture. */
+int aeolus_profile_enable(int enable);
+int aeolus_profile_collect(char* buf, size_t len);
+int aeolus_profile_reset(void);
+
 /* ---- plans ---------------------------------------------------------- */
 
 /* Gauss-Legendre nlat x nlon grid at truncation lmax: nodes/weights by an
