@@ -95,20 +95,30 @@ namespace {
 constexpr double kPi = 3.14159265358979323846;
 constexpr double kInvSqrt4Pi = 0.28209479177387814347;  // 1/sqrt(4 pi)
 
-// Gauss-Legendre nodes and weights by Newton's method in colatitude theta
-// (x = cos theta), so sin(theta) -- which sets the polar weights and the
-// Legendre seeds -- keeps full relative precision near the poles.  Nodes are
-// symmetric by construction; the middle node of an odd rule is exactly
-// x = 0.  One thread per northern node.
-__device__ void legendre_pn(int n, double x, double* pn, double* pn1) {
-  double p0 = 1.0, p1 = x;
-  for (int k = 1; k < n; ++k) {
-    const double p2 = ((2.0 * k + 1.0) * x * p1 - k * p0) / (k + 1.0);
-    p0 = p1;
-    p1 = p2;
+// Gauss-Legendre nodes and weights by Newton's method in colatitude theta.
+// P_n is evaluated with Reinsch's modification of the three-term recurrence
+// in u = 1 - x = 2 sin^2(theta/2):
+//   d_{k+1} = (k d_k - (2k+1) u P_k) / (k+1),  P_{k+1} = P_k + d_{k+1},
+// which keeps full relative precision near the pole where x = cos(theta)
+// no longer resolves theta.  With q = n (x P_n - P_{n-1}) = n (d_n - u P_n):
+//   d/dtheta P_n(cos theta) = q / sin(theta),  w = 2 sin^2(theta) / q^2.
+// Nodes are symmetric by construction; the middle node of an odd rule is
+// exactly x = 0.  One thread per northern node.
+__device__ void legendre_reinsch(int n, double u, double* pn, double* q) {
+  double p = 1.0, d = -u;  // P_1 = x = 1 - u, d_1 = P_1 - P_0
+  double pk = 1.0 - u;
+  if (n == 0) {
+    *pn = 1.0;
+    *q = 0.0;
+    return;
   }
-  *pn = p1;
-  *pn1 = p0;
+  p = pk;
+  for (int k = 1; k < n; ++k) {
+    d = (k * d - (2.0 * k + 1.0) * u * p) / (k + 1.0);
+    p += d;
+  }
+  *pn = p;
+  *q = n * (d - u * p);
 }
 
 __global__ void gauss_nodes_kernel(int n, double* x, double* sth, double* theta, double* w) {
@@ -117,24 +127,20 @@ __global__ void gauss_nodes_kernel(int n, double* x, double* sth, double* theta,
   if (j >= nh) return;
   const bool middle = (n & 1) && j == nh - 1;
   double t = middle ? 0.5 * kPi : kPi * (j + 0.75) / (n + 0.5);
-  double xv = cos(t), sv = sin(t), pn, pn1;
+  double pn, q;
   if (!middle) {
     for (int it = 0; it < 64; ++it) {
-      legendre_pn(n, xv, &pn, &pn1);
-      // f(t) = P_n(cos t), f'(t) = n (x P_n - P_{n-1}) / sin t
-      const double dt = pn * sv / (n * (xv * pn - pn1));
+      const double sh = sin(0.5 * t);
+      legendre_reinsch(n, 2.0 * sh * sh, &pn, &q);
+      const double dt = pn * sin(t) / q;
       t -= dt;
-      xv = cos(t);
-      sv = sin(t);
       if (fabs(dt) <= 1e-17) break;
     }
-  } else {
-    xv = 0.0;
-    sv = 1.0;
   }
-  legendre_pn(n, xv, &pn, &pn1);
-  // w = 2 / ((1 - x^2) P_n'(x)^2),  P_n'(x) = -n (x P_n - P_{n-1}) / sin^2 t
-  const double q = n * (xv * pn - pn1);
+  const double sv = middle ? 1.0 : sin(t);
+  const double xv = middle ? 0.0 : cos(t);
+  const double sh = sin(0.5 * t);
+  legendre_reinsch(n, middle ? 1.0 : 2.0 * sh * sh, &pn, &q);
   const double wt = 2.0 * sv * sv / (q * q);
   x[j] = xv;
   x[n - 1 - j] = -xv;
