@@ -48,6 +48,7 @@ SIGNATURES = {
                                  POINTER(c_long)]),
     "aeolus_plan_nodes": (c_int, [c_void_p, c_void_p, c_void_p]),
     "aeolus_plan_set_precision": (c_int, [c_void_p, c_int, c_int]),
+    "aeolus_plan_device_error": (c_int, [c_void_p, POINTER(c_int)]),
     "aeolus_workspace_bytes": (c_int, [c_void_p, c_int, c_int, POINTER(c_size_t)]),
     "aeolus_synthesize": (c_int, [c_void_p, c_void_p, c_void_p, c_int, c_void_p, c_size_t, c_void_p]),
     "aeolus_analyze": (c_int, [c_void_p, c_void_p, c_void_p, c_int, c_void_p, c_size_t, c_void_p]),

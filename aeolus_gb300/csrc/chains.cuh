@@ -8,14 +8,22 @@
 
 #include "pipeline.cuh"
 #include "points.cuh"
+#include "split.cuh"
 
 namespace aeolus {
 
 inline unsigned blocks_for(long n, int t) { return (unsigned)((n + t - 1) / t); }
 
 // ---------------------------------------------------------------- sizes
+inline bool split_on(const aeolus_plan_impl* p) {
+  return p->kind == kGauss && p->precision == AEOLUS_PREC_SPLIT_BF16 && p->split != nullptr;
+}
+
 template <int NIN, int NOUT>
 size_t full_chain_bytes(const aeolus_plan_impl* p, int batch) {
+  if (split_on(p))
+    return align256(fg_bytes(p, NIN > NOUT ? NIN : NOUT, batch)) +
+           std::max(split_synth_bytes(p, NIN, batch), split_anal_bytes(p, NOUT, batch));
   if (p->kind == kGauss) return align256(fg_bytes(p, NIN > NOUT ? NIN : NOUT, batch));
   const size_t nc = p->ncol, np = p->npoints;
   return align256((size_t)batch * NIN * nc * 8) + align256((size_t)batch * NIN * np * 8) +
@@ -24,12 +32,14 @@ size_t full_chain_bytes(const aeolus_plan_impl* p, int batch) {
 
 template <int NIN, int NOUT>
 size_t synth_chain_bytes(const aeolus_plan_impl* p, int batch) {
+  if (split_on(p)) return align256(fg_bytes(p, NIN, batch)) + split_synth_bytes(p, NIN, batch);
   if (p->kind == kGauss) return align256(fg_bytes(p, NIN, batch));
   return align256((size_t)batch * NIN * p->ncol * 8) + align256((size_t)batch * NIN * p->npoints * 8);
 }
 
 template <int NIN, int NOUT>
 size_t anal_chain_bytes(const aeolus_plan_impl* p, int batch) {
+  if (split_on(p)) return align256(fg_bytes(p, NOUT, batch)) + split_anal_bytes(p, NOUT, batch);
   if (p->kind == kGauss) return align256(fg_bytes(p, NOUT, batch));
   return align256((size_t)batch * NOUT * p->npoints * 8) + align256((size_t)batch * NOUT * p->ncol * 8);
 }
@@ -43,7 +53,9 @@ int run_full_chain(const aeolus_plan_impl* p, const Derive& d, const Pw& pw, con
   if (p->kind == kGauss) {
     constexpr int NB = Pw::NIN > Pw::NOUT ? Pw::NIN : Pw::NOUT;
     double2* FG = static_cast<double2*>(work);
-    int s = launch_synth(p, d, FG, NB, batch, st);
+    void* scratch = static_cast<char*>(work) + align256(fg_bytes(p, NB, batch));
+    const bool split = split_on(p);
+    int s = split ? launch_split_synth(p, d, FG, NB, batch, scratch, st) : launch_synth(p, d, FG, NB, batch, st);
     if (s) return s;
     RowArgs ra{};
     ra.batch = batch;
@@ -51,7 +63,7 @@ int run_full_chain(const aeolus_plan_impl* p, const Derive& d, const Pw& pw, con
     ra.nblk = NB;
     ra.status = status;
     if ((s = launch_rows<Pw, kInF, kOutG>(p, pw, ra, st))) return s;
-    return launch_analysis(p, e, FG, NB, batch, st);
+    return split ? launch_split_anal(p, e, FG, NB, batch, scratch, st) : launch_analysis(p, e, FG, NB, batch, st);
   }
   const long nc = p->ncol, np = p->npoints;
   char* w = static_cast<char*>(work);
@@ -84,7 +96,9 @@ int run_synth_chain(const aeolus_plan_impl* p, const Derive& d, const Pw& pw, in
   static_assert(Derive::NF == Pw::NIN, "derive/pointwise field count");
   if (p->kind == kGauss) {
     double2* FG = static_cast<double2*>(work);
-    int s = launch_synth(p, d, FG, Pw::NIN, batch, st);
+    void* scratch = static_cast<char*>(work) + align256(fg_bytes(p, Pw::NIN, batch));
+    int s = split_on(p) ? launch_split_synth(p, d, FG, Pw::NIN, batch, scratch, st)
+                        : launch_synth(p, d, FG, Pw::NIN, batch, st);
     if (s) return s;
     RowArgs ra{};
     ra.batch = batch;
@@ -129,6 +143,10 @@ int run_anal_chain(const aeolus_plan_impl* p, const Pw& pw, const Epi& e, int ba
     ra.gin_f = in_f;
     int s = launch_rows<Pw, kInGrid, kOutG>(p, pw, ra, st);
     if (s) return s;
+    if (split_on(p)) {
+      void* scratch = static_cast<char*>(work) + align256(fg_bytes(p, Pw::NOUT, batch));
+      return launch_split_anal(p, e, FG, Pw::NOUT, batch, scratch, st);
+    }
     return launch_analysis(p, e, FG, Pw::NOUT, batch, st);
   }
   const long nc = p->ncol, np = p->npoints;

@@ -1,21 +1,155 @@
-// Contraction precision control.  The split-precision (bf16-sliced,
-// tcgen05) Legendre contraction is selected per plan here.
-#include "common.cuh"
+// Split-precision Legendre contraction on tcgen05 tensor cores.
+//
+// Both operands of every per-order contraction are cut into balanced
+// base-256 digits: with a per-row (basis) or per-column (data) exponent E,
+//   X = rint(x * 2^(40-E)) = sum_{s=1..5} d_s 256^(5-s),  |d_s| <= 128,
+// so each digit is exact in bf16.  The digit products of level k = s + t
+// (k = 2..6, 15 (s,t) pairs) are accumulated in their own f32 TMEM
+// accumulator; every partial sum is an integer below pairs*K*2^14 < 2^24
+// (K <= 128 degrees in synthesis, <= 192 latitudes in analysis), so the
+// tensor-core accumulation is exact.  The levels are recombined in 64-bit
+// integers, T = sum_k I_k 256^(6-k), and one conversion gives the FP64
+// result T * 2^(E_row + E_col - 48).  Dropped levels k >= 7 bound the
+// relative error near 2^-40 of max|P| max|a| per term.
+//
+// Synthesis GEMM (per order m):   F[j, n] = sum_l P_lm(x_j) a[l, n]
+//   A = basis digits  (128 latitude rows x Kpad degrees, K-major)
+//   B = data digits   (64 data columns  x Kpad degrees, K-major)
+// Analysis GEMM (per order m):    a[l, n] = sum_j P_lm(x_j) G[j, n]
+//   A = basis digits  (128 degree rows x NK latitudes)
+//   B = data digits   (64 data columns x NK latitudes)
+// Data columns are (member, field, re/im).  Basis tiles stream through the
+// TMA bulk-copy engine into a double buffer; the data tile stays resident.
+#include <algorithm>
+#include <vector>
+
+#include "chains.cuh"
+#include "split.cuh"
 
 namespace aeolus {
 
-struct SplitTables {
-  int slices = 0;
-};
-
 void free_split(aeolus_plan_impl* p) {
-  delete p->split;
+  if (!p->split) return;
+  SplitTables* t = p->split;
+  if (t->psyn) cudaFree(t->psyn);
+  if (t->pana) cudaFree(t->pana);
+  if (t->esyn) cudaFree(t->esyn);
+  if (t->eana) cudaFree(t->eana);
+  if (t->kcum) cudaFree(t->kcum);
+  if (t->err) cudaFree(t->err);
+  delete t;
   p->split = nullptr;
+}
+
+namespace {
+
+// Basis digit tables.  Synthesis: one thread per (m, latitude row).
+__global__ void split_psyn_kernel(int L, int nlat, int nh, int Mt, const double* __restrict__ P,
+                                  const long long* __restrict__ kcum, __nv_bfloat16* __restrict__ out,
+                                  int* __restrict__ eout) {
+  const int m = blockIdx.y;
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (m > L || j >= Mt * 128) return;
+  const int K = L + 1 - m, Kp = kpad(K);
+  const int mt = j / 128, r = j % 128;
+  __nv_bfloat16* blk = out + kcum[m] * (long long)Mt * kSlices * 128 + (long long)mt * kSlices * 128 * Kp;
+  const long long slice = 128LL * Kp;
+  if (j >= nlat) {
+    for (int t = 0; t < Kp; ++t)
+      for (int s = 0; s < kSlices; ++s) blk[s * slice + tc::core_index(r, t, Kp)] = __float2bfloat16(0.0f);
+    eout[m * Mt * 128 + j] = 0;
+    return;
+  }
+  const bool south = j >= nh;
+  const int jn = south ? nlat - 1 - j : j;
+  const double* Pm = P + tri_off(m, L) * nh + jn;
+  double mx = 0.0;
+  for (int t = 0; t < K; ++t) mx = fmax(mx, fabs(Pm[(long)t * nh]));
+  const int E = exponent_for(mx);
+  eout[m * Mt * 128 + j] = E;
+  for (int t = 0; t < Kp; ++t) {
+    double v = 0.0;
+    if (t < K) v = Pm[(long)t * nh] * ((south && (t & 1)) ? -1.0 : 1.0);
+    float d[kSlices];
+    digits(v, E, d);
+    for (int s = 0; s < kSlices; ++s) blk[s * slice + tc::core_index(r, t, Kp)] = __float2bfloat16(d[s]);
+  }
+}
+
+// Analysis: one thread per (m, degree row).
+__global__ void split_pana_kernel(int L, int nlat, int nh, int NK, const double* __restrict__ P,
+                                  __nv_bfloat16* __restrict__ out, int* __restrict__ eout) {
+  const int m = blockIdx.y;
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (m > L || t >= 128) return;
+  const int K = L + 1 - m;
+  __nv_bfloat16* blk = out + (long long)m * kSlices * 128 * NK;
+  const long long slice = 128LL * NK;
+  const double* Pm = P + tri_off(m, L) * nh + (long)t * nh;
+  double mx = 0.0;
+  if (t < K)
+    for (int jn = 0; jn < nh; ++jn) mx = fmax(mx, fabs(Pm[jn]));
+  const int E = t < K ? exponent_for(mx) : 0;
+  eout[m * 128 + t] = E;
+  for (int j = 0; j < NK; ++j) {
+    double v = 0.0;
+    if (t < K && j < nlat) {
+      const bool south = j >= nh;
+      v = Pm[south ? nlat - 1 - j : j] * ((south && (t & 1)) ? -1.0 : 1.0);
+    }
+    float d[kSlices];
+    digits(v, E, d);
+    for (int s = 0; s < kSlices; ++s) blk[s * slice + tc::core_index(t, j, NK)] = __float2bfloat16(d[s]);
+  }
+}
+
+}  // namespace
+
+int split_build(aeolus_plan_impl* p) {
+  if (p->split) return AEOLUS_OK;
+  if (p->kind != kGauss) return fail(AEOLUS_ERR_ARG, "split precision is implemented for Gauss plans");
+  const int L = p->lmax;
+  if (L > 127) return fail(AEOLUS_ERR_ARG, "split precision supports l_max <= 127");
+  if (p->nlat > 192) return fail(AEOLUS_ERR_ARG, "split precision supports nlat <= 192 (exact f32 accumulation)");
+  auto* t = new SplitTables();
+  p->split = t;
+  t->L = L;
+  t->nlat = p->nlat;
+  t->nh = p->nh;
+  t->NK = kpad(p->nlat);
+  t->Mt = (p->nlat + 127) / 128;
+  t->h_kcum.assign(L + 2, 0);
+  for (int m = 0; m <= L; ++m) t->h_kcum[m + 1] = t->h_kcum[m] + kpad(L + 1 - m);
+  const size_t nsyn = (size_t)t->h_kcum[L + 1] * t->Mt * kSlices * 128;
+  const size_t nana = (size_t)(L + 1) * kSlices * 128 * t->NK;
+  AE_CUDA(cudaMalloc(&t->kcum, (L + 2) * sizeof(long long)));
+  AE_CUDA(cudaMemcpy(t->kcum, t->h_kcum.data(), (L + 2) * sizeof(long long), cudaMemcpyHostToDevice));
+  AE_CUDA(cudaMalloc(&t->psyn, nsyn * sizeof(__nv_bfloat16)));
+  AE_CUDA(cudaMalloc(&t->pana, nana * sizeof(__nv_bfloat16)));
+  AE_CUDA(cudaMalloc(&t->esyn, (size_t)(L + 1) * t->Mt * 128 * sizeof(int)));
+  AE_CUDA(cudaMalloc(&t->eana, (size_t)(L + 1) * 128 * sizeof(int)));
+  AE_CUDA(cudaMalloc(&t->err, sizeof(int)));
+  AE_CUDA(cudaMemset(t->err, 0, sizeof(int)));
+  split_psyn_kernel<<<dim3((t->Mt * 128 + 127) / 128, L + 1), 128>>>(L, p->nlat, p->nh, t->Mt, p->P, t->kcum, t->psyn,
+                                                                      t->esyn);
+  AE_LAUNCH("split_psyn_kernel");
+  split_pana_kernel<<<dim3(1, L + 1), 128>>>(L, p->nlat, p->nh, t->NK, p->P, t->pana, t->eana);
+  AE_LAUNCH("split_pana_kernel");
+  AE_CUDA(cudaDeviceSynchronize());
+  return AEOLUS_OK;
 }
 
 }  // namespace aeolus
 
 using namespace aeolus;
+
+extern "C" int aeolus_plan_device_error(aeolus_plan plan, int* flag) {
+  if (!plan || !flag) return fail(AEOLUS_ERR_ARG, "aeolus_plan_device_error: bad arguments");
+  *flag = 0;
+  if (!plan->split) return AEOLUS_OK;
+  AE_CUDA(cudaMemcpy(flag, plan->split->err, sizeof(int), cudaMemcpyDeviceToHost));
+  return AEOLUS_OK;
+}
 
 extern "C" int aeolus_plan_set_precision(aeolus_plan plan, int precision, int slices) {
   if (!plan) return fail(AEOLUS_ERR_ARG, "aeolus_plan_set_precision: plan is NULL");
@@ -24,6 +158,13 @@ extern "C" int aeolus_plan_set_precision(aeolus_plan plan, int precision, int sl
     plan->slices = 0;
     return AEOLUS_OK;
   }
-  (void)slices;
-  return fail(AEOLUS_ERR_ARG, "aeolus_plan_set_precision: unsupported precision mode");
+  if (precision != AEOLUS_PREC_SPLIT_BF16)
+    return fail(AEOLUS_ERR_ARG, "aeolus_plan_set_precision: unknown precision mode");
+  if (slices != 0 && slices != kSlices)
+    return fail(AEOLUS_ERR_ARG, "aeolus_plan_set_precision: this build uses 5 bf16 slices per operand");
+  const int s = split_build(plan);
+  if (s) return s;
+  plan->precision = precision;
+  plan->slices = kSlices;
+  return AEOLUS_OK;
 }

@@ -130,6 +130,12 @@ int aeolus_plan_nodes(aeolus_plan plan, double* lat, double* w_gl);
  * bf16 slices per FP64 operand, 0 = default). */
 int aeolus_plan_set_precision(aeolus_plan plan, int precision, int slices);
 
+/* Sticky device error flag of the plan's tensor-core kernels: nonzero when a
+ * bounded wait on a copy or MMA completion expired (the kernel then skipped
+ * its outputs).  Reading it synchronises the device.  No reference
+ * counterpart (the reference has no device-side waits). */
+int aeolus_plan_device_error(aeolus_plan plan, int* flag);
+
 int aeolus_workspace_bytes(aeolus_plan plan, int op, int batch, size_t* bytes);
 
 /* ---- transforms ------------------------------------------------------ */

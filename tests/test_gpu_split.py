@@ -1,0 +1,94 @@
+"""Split-precision (bf16-digit tcgen05) contraction against the FP64 path.
+
+The split path must stay within 1e-11 relative L2 of the FP64 path for
+single transforms and tendencies, and within 1e-10 after RK4 integration
+(the stated accuracy target of the split-precision form).
+"""
+import numpy as np
+import pytest
+import torch
+
+import aeolus_gb300 as ae
+from aeolus_gb300 import _lib, workloads as W
+from aeolus_gb300.ops import Plan, analyze, synthesize
+from aeolus_gb300.shallow_water import ShallowWaterModel
+from aeolus_gb300.barotropic import BarotropicVorticity, BarotropicState
+from helpers import rel_l2
+
+pytestmark = pytest.mark.gpu
+DEV = "cuda"
+
+
+def T(x):
+    return torch.as_tensor(np.asarray(x), device=DEV)
+
+
+def N(x):
+    return x.detach().cpu().numpy()
+
+
+def device_error(plan):
+    import ctypes
+    f = ctypes.c_int()
+    _lib.check(_lib.load().aeolus_plan_device_error(plan.handle, ctypes.byref(f)))
+    return f.value
+
+
+@pytest.mark.parametrize("nlat,nlon,L", [(32, 64, 21), (17, 40, 12), (128, 256, 85), (160, 320, 106),
+                                         (192, 384, 127)])
+def test_split_transforms_match_fp64(nlat, nlon, L):
+    rng = np.random.default_rng(L)
+    p64 = Plan.gauss(nlat, nlon, L)
+    ps = Plan.gauss(nlat, nlon, L)
+    ps.set_precision(_lib.PREC_SPLIT_BF16)
+    a = np.stack([W.random_spectrum(rng, L, -1.5, 1.0, zero_monopole=False) for _ in range(5)])
+    f = rng.standard_normal((5, nlat * nlon))
+    g64, gs = N(synthesize(p64.id, T(a))), N(synthesize(ps.id, T(a)))
+    c64, cs = N(analyze(p64.id, T(f))), N(analyze(ps.id, T(f)))
+    assert device_error(ps) == 0
+    for b in range(5):
+        assert rel_l2(gs[b], g64[b]) < 1e-11, rel_l2(gs[b], g64[b])
+        assert rel_l2(cs[b], c64[b]) < 1e-11, rel_l2(cs[b], c64[b])
+
+
+def _swe(nlat, nlon, L, precision, members=4, seed=3):
+    planet = ae.make_planet("latlon", nlat=nlat, nlon=nlon, l_max=L)
+    if precision == "split":
+        planet.so._product_space.sh.plan.set_precision(_lib.PREC_SPLIT_BF16)
+    s, depth = W.member_states(L, members, seed=seed)
+    return planet, ShallowWaterModel(planet, gravity=W.GRAVITY, mean_depth=depth), s
+
+
+@pytest.mark.parametrize("nlat,nlon,L", [(32, 64, 21), (128, 256, 85), (192, 384, 127)])
+def test_split_swe_tendency_and_steps(nlat, nlon, L):
+    _, m64, s = _swe(nlat, nlon, L, "fp64")
+    planet, ms, _ = _swe(nlat, nlon, L, "split")
+    t64, ts = N(m64.tendency(T(s))), N(ms.tendency(T(s)))
+    for b in range(s.shape[0]):
+        for f in range(3):
+            assert rel_l2(ts[b, f], t64[b, f]) < 1e-11, (b, f, rel_l2(ts[b, f], t64[b, f]))
+    y64 = N(m64.rk4(T(s), 240.0, 10))
+    ys = N(ms.rk4(T(s), 240.0, 10))
+    for b in range(s.shape[0]):
+        for f in range(3):
+            assert rel_l2(ys[b, f], y64[b, f]) < 1e-10, (b, f, rel_l2(ys[b, f], y64[b, f]))
+    assert device_error(planet.so._product_space.sh.plan) == 0
+
+
+def test_split_bve_matches_fp64():
+    L = 63
+    p64 = ae.make_planet("latlon", nlat=96, nlon=192, l_max=L)
+    ps = ae.make_planet("latlon", nlat=96, nlon=192, l_max=L)
+    ps.so._product_space.sh.plan.set_precision(_lib.PREC_SPLIT_BF16)
+    z = np.stack([W.bve_vorticity(L, s) for s in range(6)])
+    m64, ms = BarotropicVorticity(p64, viscosity=1e5), BarotropicVorticity(ps, viscosity=1e5)
+    t64 = N(m64.tendency(BarotropicState(T(z))))
+    ts = N(ms.tendency(BarotropicState(T(z))))
+    assert rel_l2(ts, t64) < 1e-11
+    assert rel_l2(N(ms.rk4(T(z), 900.0, 5)), N(m64.rk4(T(z), 900.0, 5))) < 1e-10
+
+
+def test_split_rejects_unsupported_shapes():
+    p = Plan.gauss(256, 512, 170)
+    with pytest.raises(ValueError, match="l_max"):
+        p.set_precision(_lib.PREC_SPLIT_BF16)
