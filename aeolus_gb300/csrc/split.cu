@@ -2,15 +2,16 @@
 //
 // Both operands of every per-order contraction are cut into balanced
 // base-256 digits: with a per-row (basis) or per-column (data) exponent E,
-//   X = rint(x * 2^(40-E)) = sum_{s=1..5} d_s 256^(5-s),  |d_s| <= 128,
+//   X = rint(x * 2^(48-E)) = sum_{s=1..6} d_s 256^(6-s),  |d_s| <= 128,
 // so each digit is exact in bf16.  The digit products of level k = s + t
-// (k = 2..6, 15 (s,t) pairs) are accumulated in their own f32 TMEM
-// accumulator; every partial sum is an integer below pairs*K*2^14 < 2^24
-// (K <= 128 degrees in synthesis, <= 192 latitudes in analysis), so the
-// tensor-core accumulation is exact.  The levels are recombined in 64-bit
-// integers, T = sum_k I_k 256^(6-k), and one conversion gives the FP64
-// result T * 2^(E_row + E_col - 48).  Dropped levels k >= 7 bound the
-// relative error near 2^-40 of max|P| max|a| per term.
+// (k = 2..7, 21 (s,t) pairs) are accumulated in f32 TMEM accumulators, one
+// per level except the 6-pair top level which uses two; every partial sum
+// is an integer below pairs*K*2^14 < 2^24 (K <= 128 degrees in synthesis,
+// <= 192 latitudes in analysis), so the tensor-core accumulation is exact.
+// The levels are recombined in 64-bit integers, T = sum_k I_k 256^(7-k),
+// and one conversion gives the FP64 result T * 2^(E_row + E_col - 56).
+// Dropped levels k >= 8 bound the error near 2^-48 of max|P| max|a| per
+// term.
 //
 // Synthesis GEMM (per order m):   F[j, n] = sum_l P_lm(x_j) a[l, n]
 //   A = basis digits  (128 latitude rows x Kpad degrees, K-major)
@@ -161,7 +162,7 @@ extern "C" int aeolus_plan_set_precision(aeolus_plan plan, int precision, int sl
   if (precision != AEOLUS_PREC_SPLIT_BF16)
     return fail(AEOLUS_ERR_ARG, "aeolus_plan_set_precision: unknown precision mode");
   if (slices != 0 && slices != kSlices)
-    return fail(AEOLUS_ERR_ARG, "aeolus_plan_set_precision: this build uses 5 bf16 slices per operand");
+    return fail(AEOLUS_ERR_ARG, "aeolus_plan_set_precision: this build uses 6 bf16 slices per operand");
   const int s = split_build(plan);
   if (s) return s;
   plan->precision = precision;

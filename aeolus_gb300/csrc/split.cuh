@@ -11,10 +11,13 @@
 
 namespace aeolus {
 
-constexpr int kSlices = 5;   // base-256 digits per operand
-constexpr int kLevels = 5;   // accumulated levels k = s + t = 2..6
-constexpr int kNT = 64;      // data columns per tensor-core tile (MMA N)
+constexpr int kSlices = 6;   // base-256 digits per operand (48 bits)
+constexpr int kLevels = 6;   // kept levels k = s + t = 2..7 (1-based digits)
+constexpr int kAccs = 7;     // TMEM accumulators: the 6-pair top level is split in two
+constexpr int kNT = 64;      // data columns per synthesis tile (MMA N)
+constexpr int kNTa = 48;     // data columns per analysis tile
 constexpr int kTmemCols = 512;
+constexpr int kShift = 8 * kSlices;  // X = rint(x 2^(kShift - E))
 constexpr int kMaxKp = 128;  // degrees per order (l_max <= 127)
 
 struct SplitTables {
@@ -40,9 +43,9 @@ __device__ inline int exponent_for(double mx) {
   return e + 1;
 }
 
-// Balanced base-256 digits of rint(x 2^(40-E)), most significant first.
+// Balanced base-256 digits of rint(x 2^(48-E)), most significant first.
 __device__ inline void digits(double x, int E, float* d) {
-  long long X = (E == -1000) ? 0LL : __double2ll_rn(ldexp(x, 40 - E));
+  long long X = (E == -1000) ? 0LL : __double2ll_rn(ldexp(x, kShift - E));
 #pragma unroll
   for (int i = kSlices - 1; i >= 1; --i) {
     const long long r = ((X + 128) & 255) - 128;
@@ -52,13 +55,24 @@ __device__ inline void digits(double x, int E, float* d) {
   d[0] = (float)X;
 }
 
-// Level recombination: T = sum_k I_k 256^(4-k) (k = 0..4 <-> s+t = 2..6).
+// Level recombination: T = sum_k I_k 256^(5-k), k = 0..5 <-> s+t = 2..7,
+// the top level held in two accumulators.  |T| < 2^62.
 __device__ inline long long combine_levels(const float* acc) {
   long long T = 0;
 #pragma unroll
-  for (int k = 0; k < kLevels; ++k) T = (T << 8) + __float2ll_rn(acc[k]);
-  return T;
+  for (int k = 0; k < kLevels - 1; ++k) T = (T << 8) + __float2ll_rn(acc[k]);
+  return (T << 8) + __float2ll_rn(acc[kLevels - 1]) + __float2ll_rn(acc[kLevels]);
 }
+
+// Accumulator of digit pair (s, t) (0-based): one per level, except the
+// top level whose 6 pairs are split 3 + 3 so that each f32 sum stays an
+// exact integer for K <= 192 (3 * 192 * 2^14 < 2^24).
+__host__ __device__ constexpr int acc_of(int s, int t) {
+  return (s + t < kLevels - 1) ? s + t : (s < kSlices / 2 ? kLevels - 1 : kLevels);
+}
+
+// Result exponent offset: x y = T 2^(Ex + Ey - kOut).
+constexpr int kOut = 2 * kShift - 8 * (kSlices - 1);
 
 // ----------------------------------------------------------- layouts
 struct SplitDims {
@@ -73,9 +87,9 @@ __host__ __device__ inline long long dsyn_block(const long long* kcum, const Spl
   return kcum[m] * (long long)d.ntiles * kSlices * kNT + ((long long)ntile * kSlices + s) * kNT * Kp;
 }
 
-// Analysis data digits, block (m, ntile, slice): kNT x NK.
+// Analysis data digits, block (m, ntile, slice): kNTa x NK.
 __host__ __device__ inline long long dana_block(const SplitDims& d, int m, int ntile, int s) {
-  return (((long long)m * d.ntiles + ntile) * kSlices + s) * kNT * (long long)d.NK;
+  return (((long long)m * d.ntiles + ntile) * kSlices + s) * kNTa * (long long)d.NK;
 }
 
 // ------------------------------------------------- synthesis data slicing
@@ -171,7 +185,7 @@ __global__ void __launch_bounds__(256) split_anal_slice_kernel(SplitDims dm, int
     if (lane == 0) {
       const int E = exponent_for(mx);
       s_exp[c] = E;
-      ecol[(long long)m * dm.ntiles * kNT + (long long)b0 * NF * 2 + c] = E;
+      ecol[(long long)m * dm.ntiles * kNTa + (long long)b0 * NF * 2 + c] = E;
     }
   }
   __syncthreads();
@@ -182,24 +196,24 @@ __global__ void __launch_bounds__(256) split_anal_slice_kernel(SplitDims dm, int
     digits(j < nlat ? s_val[c * nlat + j] : 0.0, s_exp[c], d);
 #pragma unroll
     for (int s = 0; s < kSlices; ++s)
-      dana[dana_block(dm, m, n / kNT, s) + tc::core_index(n % kNT, j, NK)] = __float2bfloat16(d[s]);
+      dana[dana_block(dm, m, n / kNTa, s) + tc::core_index(n % kNTa, j, NK)] = __float2bfloat16(d[s]);
   }
   if (blockIdx.y == gridDim.y - 1) {
-    const int n0 = batch * NF * 2, n1 = dm.ntiles * kNT;
+    const int n0 = batch * NF * 2, n1 = dm.ntiles * kNTa;
     for (int idx = threadIdx.x; idx < (n1 - n0) * NK; idx += blockDim.x) {
       const int n = n0 + idx / NK, j = idx % NK;
 #pragma unroll
       for (int s = 0; s < kSlices; ++s)
-        dana[dana_block(dm, m, n / kNT, s) + tc::core_index(n % kNT, j, NK)] = __float2bfloat16(0.0f);
-      if (j == 0) ecol[(long long)m * dm.ntiles * kNT + n] = 0;
+        dana[dana_block(dm, m, n / kNTa, s) + tc::core_index(n % kNTa, j, NK)] = __float2bfloat16(0.0f);
+      if (j == 0) ecol[(long long)m * dm.ntiles * kNTa + n] = 0;
     }
   }
 }
 
 // ---------------------------------------------------- tensor-core GEMM core
-// Shared by synthesis and analysis: A = 5 basis-digit tiles (128 x KK,
-// streamed, double-buffered), B = 5 data-digit tiles (kNT x KK, resident).
-// On return the 5 level accumulators sit in TMEM columns [k*kNT, (k+1)*kNT).
+// Shared by synthesis and analysis: A = kSlices basis-digit tiles (128 x KK,
+// streamed through a double buffer), B = kSlices data-digit tiles (NT x KK,
+// resident).  On return accumulator a sits in TMEM columns [a*NT, (a+1)*NT).
 // Returns false (and sets *err) if a bounded wait expired.
 struct TcSmem {
   __nv_bfloat16* A[2];
@@ -207,23 +221,25 @@ struct TcSmem {
   uint64_t* bar;  // [0..1] A buffers loaded, [2..3] A buffers free, [4] B loaded, [5] MMAs done
 };
 
+template <int NT>
 __device__ inline bool tc_levels(const TcSmem& sm, const __nv_bfloat16* gA, long long a_slice_elems,
                                  const __nv_bfloat16* gB, long long b_slice_elems, int KK, uint32_t tmem,
                                  int* err) {
-  const uint32_t abytes = 128u * KK * 2u, bbytes = (uint32_t)kNT * KK * 2u;
+  const uint32_t abytes = 128u * KK * 2u, bbytes = (uint32_t)NT * KK * 2u;
   bool ok = true;
   if (threadIdx.x == 0) {
     int issued[2] = {0, 0}, waited[2] = {0, 0};
+    unsigned started = 0u;  // accumulators already holding a partial sum
     bool b_ok = false;
     tc::mbar_expect_tx(&sm.bar[4], kSlices * bbytes);
     for (int t = 0; t < kSlices; ++t)
-      tc::bulk_g2s(sm.B + (long long)t * kNT * KK, gB + t * b_slice_elems, bbytes, &sm.bar[4]);
+      tc::bulk_g2s(sm.B + (long long)t * NT * KK, gB + t * b_slice_elems, bbytes, &sm.bar[4]);
     for (int s = 0; s < 2; ++s) {
       tc::mbar_expect_tx(&sm.bar[s], abytes);
       tc::bulk_g2s(sm.A[s], gA + s * a_slice_elems, abytes, &sm.bar[s]);
       issued[s] = 1;
     }
-    const uint32_t idesc = tc::idesc_bf16_f32(128, kNT);
+    const uint32_t idesc = tc::idesc_bf16_f32(128, NT);
     const uint32_t sbo = (uint32_t)KK * 16u;
     ok = b_ok = tc::mbar_wait(&sm.bar[4], 0);
     for (int s = 0; s < kSlices && ok; ++s) {
@@ -232,11 +248,13 @@ __device__ inline bool tc_levels(const TcSmem& sm, const __nv_bfloat16* gA, long
       if (!ok) break;
       ++waited[buf];
       for (int t = 0; s + t < kSlices; ++t) {
-        const uint32_t dcol = tmem + (uint32_t)(s + t) * kNT;
+        const int a = acc_of(s, t);
+        const uint32_t dcol = tmem + (uint32_t)a * NT;
         for (int ks = 0; ks < KK / 16; ++ks) {
           const uint64_t da = tc::smem_desc(sm.A[buf] + ks * 128, 128, sbo);
-          const uint64_t db = tc::smem_desc(sm.B + (long long)t * kNT * KK + ks * 128, 128, sbo);
-          tc::mma_bf16(dcol, da, db, idesc, (s > 0 || ks > 0) ? 1u : 0u);
+          const uint64_t db = tc::smem_desc(sm.B + (long long)t * NT * KK + ks * 128, 128, sbo);
+          tc::mma_bf16(dcol, da, db, idesc, ((started >> a) & 1u) ? 1u : 0u);
+          started |= 1u << a;
         }
       }
       if (s + 2 < kSlices) {
@@ -265,19 +283,20 @@ __device__ inline bool tc_levels(const TcSmem& sm, const __nv_bfloat16* gA, long
   return __syncthreads_and((done && ok) ? 1 : 0) != 0;
 }
 
-// At least 116 KB so that one CTA holds an SM (each CTA takes all 512 TMEM
-// columns; a second resident CTA would only stall in tcgen05.alloc).
-inline size_t tc_smem_bytes(int KK) {
-  const size_t need = 2 * 128 * (size_t)KK * 2 + (size_t)kSlices * kNT * KK * 2 + 1024 + 128;
+// Dynamic shared memory: at least 116 KB so that one CTA holds an SM (each
+// CTA takes all 512 TMEM columns; a second resident CTA would only stall in
+// tcgen05.alloc).
+inline size_t tc_smem_bytes(int KK, int NT) {
+  const size_t need = 2 * 128 * (size_t)KK * 2 + (size_t)kSlices * NT * KK * 2 + 1024 + 128;
   return std::max<size_t>(need, 116 * 1024);
 }
 
-__device__ inline void tc_carve(char* base, int KK, TcSmem& sm, uint32_t*& tmem_slot) {
+__device__ inline void tc_carve(char* base, int KK, int NT, TcSmem& sm, uint32_t*& tmem_slot) {
   char* p = reinterpret_cast<char*>((reinterpret_cast<uintptr_t>(base) + 1023) & ~uintptr_t(1023));
   sm.A[0] = reinterpret_cast<__nv_bfloat16*>(p);
   sm.A[1] = sm.A[0] + 128 * KK;
   sm.B = sm.A[1] + 128 * KK;
-  char* q = reinterpret_cast<char*>(sm.B + kSlices * kNT * KK);
+  char* q = reinterpret_cast<char*>(sm.B + (long long)kSlices * NT * KK);
   sm.bar = reinterpret_cast<uint64_t*>(q);
   tmem_slot = reinterpret_cast<uint32_t*>(q + 8 * 8);
 }
@@ -300,14 +319,15 @@ __device__ inline void tc_end(uint32_t tmem) {
   if (threadIdx.x < 32) tc::tmem_dealloc(tmem, kTmemCols);
 }
 
-// Read the 5 level accumulators of 16 columns starting at c0 for this
-// thread's lane (TMEM lane quadrant of its warp).
-__device__ inline void tc_read16(uint32_t tmem, int c0, float (*acc)[kLevels]) {
+// The kAccs accumulators of 16 columns starting at c0, for this thread's
+// lane (the TMEM lane quadrant of its warp).
+template <int NT>
+__device__ inline void tc_read16(uint32_t tmem, int c0, float (*acc)[kAccs]) {
   const uint32_t lane_base = (uint32_t)((threadIdx.x >> 5) * 32) << 16;
   uint32_t r[16];
 #pragma unroll
-  for (int k = 0; k < kLevels; ++k) {
-    tc::tmem_ld16(tmem + lane_base + (uint32_t)(k * kNT + c0), r);
+  for (int k = 0; k < kAccs; ++k) {
+    tc::tmem_ld16(tmem + lane_base + (uint32_t)(k * NT + c0), r);
     tc::tmem_wait_ld();
 #pragma unroll
     for (int i = 0; i < 16; ++i) acc[i][k] = __uint_as_float(r[i]);
@@ -317,36 +337,36 @@ __device__ inline void tc_read16(uint32_t tmem, int c0, float (*acc)[kLevels]) {
 // --------------------------------------------------------- synthesis GEMM
 // grid (m, latitude tile, data tile), 128 threads.  Writes F blocks.
 static __global__ void __launch_bounds__(128, 1) tc_synth_kernel(SplitDims dm, const long long* __restrict__ kcum,
-                                                          const __nv_bfloat16* __restrict__ psyn,
-                                                          const int* __restrict__ esyn,
-                                                          const __nv_bfloat16* __restrict__ dsyn,
-                                                          const int* __restrict__ ecol, int nf, int nblk,
-                                                          double2* __restrict__ F, int* err) {
+                                                                 const __nv_bfloat16* __restrict__ psyn,
+                                                                 const int* __restrict__ esyn,
+                                                                 const __nv_bfloat16* __restrict__ dsyn,
+                                                                 const int* __restrict__ ecol, int nf, int nblk,
+                                                                 double2* __restrict__ F, int* err) {
   extern __shared__ char smem_raw[];
   const int m = blockIdx.x, mt = blockIdx.y, tile = blockIdx.z;
   const int L = dm.L, Kp = kpad(L + 1 - m);
   TcSmem sm;
   uint32_t* tslot;
-  tc_carve(smem_raw, Kp, sm, tslot);
+  tc_carve(smem_raw, Kp, kNT, sm, tslot);
   tc_begin(sm, tslot);
   const uint32_t tmem = *tslot;
   const __nv_bfloat16* gA = psyn + kcum[m] * (long long)dm.Mt * kSlices * 128 + (long long)mt * kSlices * 128 * Kp;
   const __nv_bfloat16* gB = dsyn + dsyn_block(kcum, dm, m, tile, 0);
-  const bool ok = tc_levels(sm, gA, 128LL * Kp, gB, (long long)kNT * Kp, Kp, tmem, err);
+  const bool ok = tc_levels<kNT>(sm, gA, 128LL * Kp, gB, (long long)kNT * Kp, Kp, tmem, err);
   if (ok) {
     const int j = mt * 128 + threadIdx.x;
     const int Ej = j < dm.nlat ? esyn[m * dm.Mt * 128 + j] : 0;
     const int* ec = ecol + (long long)m * dm.ntiles * kNT + tile * kNT;
     for (int c0 = 0; c0 < kNT; c0 += 16) {
-      float acc[16][kLevels];
-      tc_read16(tmem, c0, acc);
+      float acc[16][kAccs];
+      tc_read16<kNT>(tmem, c0, acc);
       if (j < dm.nlat) {
 #pragma unroll
         for (int i = 0; i < 16; i += 2) {
           const int n = tile * kNT + c0 + i;  // even: real part, n + 1: imaginary part
           if (n >= dm.ncol) break;
-          const double re = ldexp((double)combine_levels(acc[i]), Ej + ec[c0 + i] - 48);
-          const double im = ldexp((double)combine_levels(acc[i + 1]), Ej + ec[c0 + i + 1] - 48);
+          const double re = ldexp((double)combine_levels(acc[i]), Ej + ec[c0 + i] - kOut);
+          const double im = ldexp((double)combine_levels(acc[i + 1]), Ej + ec[c0 + i + 1] - kOut);
           const int bf = n >> 1;
           const int b = bf / nf, f = bf - b * nf;
           F[(((long long)b * dm.nlat + j) * nblk + f) * (L + 1) + m] = make_double2(re, im);
@@ -371,71 +391,70 @@ __global__ void __launch_bounds__(128, 1) tc_anal_kernel(SplitDims dm, const __n
   const int L = dm.L, NK = dm.NK, K = L + 1 - m;
   TcSmem sm;
   uint32_t* tslot;
-  tc_carve(smem_raw, NK, sm, tslot);
+  tc_carve(smem_raw, NK, kNTa, sm, tslot);
   tc_begin(sm, tslot);
   const uint32_t tmem = *tslot;
   const __nv_bfloat16* gA = pana + (long long)m * kSlices * 128 * NK;
   const __nv_bfloat16* gB = dana + dana_block(dm, m, tile, 0);
-  const bool ok = tc_levels(sm, gA, 128LL * NK, gB, (long long)kNT * NK, NK, tmem, err);
+  const bool ok = tc_levels<kNTa>(sm, gA, 128LL * NK, gB, (long long)kNTa * NK, NK, tmem, err);
   const int t = threadIdx.x;
   if (ok) {
     const int Et = eana[m * 128 + t];
-    const int* ec = ecol + (long long)m * dm.ntiles * kNT + tile * kNT;
-    for (int c0 = 0; c0 < kNT; c0 += 16) {
-      float acc[16][kLevels];
-      tc_read16(tmem, c0, acc);
+    const int* ec = ecol + (long long)m * dm.ntiles * kNTa + tile * kNTa;
+    for (int c0 = 0; c0 < kNTa; c0 += 16) {
+      float acc[16][kAccs];
+      tc_read16<kNTa>(tmem, c0, acc);
       if (t < K) {
 #pragma unroll
         for (int i = 0; i < 16; i += 2 * NF) {
-          const int n = tile * kNT + c0 + i;
+          const int n = tile * kNTa + c0 + i;
           const int b = n / (2 * NF);
           if (b >= batch) break;
           double2 a[NF];
 #pragma unroll
           for (int f = 0; f < NF; ++f) {
-            a[f].x = ldexp((double)combine_levels(acc[i + 2 * f]), Et + ec[c0 + i + 2 * f] - 48);
-            a[f].y = ldexp((double)combine_levels(acc[i + 2 * f + 1]), Et + ec[c0 + i + 2 * f + 1] - 48);
+            a[f].x = ldexp((double)combine_levels(acc[i + 2 * f]), Et + ec[c0 + i + 2 * f] - kOut);
+            a[f].y = ldexp((double)combine_levels(acc[i + 2 * f + 1]), Et + ec[c0 + i + 2 * f + 1] - kOut);
           }
           epi.finish(b, m + t, m, a);
         }
       }
     }
     // slots l < m of column m for this tile's members
-    const int mb0 = tile * kNT / (2 * NF), mb1 = min(batch, (tile + 1) * kNT / (2 * NF));
+    const int mb0 = tile * kNTa / (2 * NF), mb1 = min(batch, (tile + 1) * kNTa / (2 * NF));
     for (int idx = threadIdx.x; idx < (mb1 - mb0) * m; idx += blockDim.x) epi.zero(mb0 + idx / m, idx % m, m);
   }
   tc_end(tmem);
 }
 
 // ------------------------------------------------------------ launchers
-inline SplitDims split_dims(const aeolus_plan_impl* p, int ncol) {
+inline SplitDims split_dims(const aeolus_plan_impl* p, int ncol, int nt) {
   const SplitTables* t = p->split;
-  return SplitDims{t->L, t->nlat, t->nh, t->NK, t->Mt, ncol, (ncol + kNT - 1) / kNT};
+  return SplitDims{t->L, t->nlat, t->nh, t->NK, t->Mt, ncol, (ncol + nt - 1) / nt};
 }
 
 inline size_t split_synth_bytes(const aeolus_plan_impl* p, int nf, int batch) {
-  const SplitDims d = split_dims(p, batch * nf * 2);
+  const SplitDims d = split_dims(p, batch * nf * 2, kNT);
   return align256((size_t)p->split->h_kcum[d.L + 1] * d.ntiles * kSlices * kNT * 2) +
          align256((size_t)(d.L + 1) * d.ntiles * kNT * 4);
 }
 
 inline size_t split_anal_bytes(const aeolus_plan_impl* p, int nf, int batch) {
-  const SplitDims d = split_dims(p, batch * nf * 2);
-  return align256((size_t)(d.L + 1) * d.ntiles * kSlices * kNT * d.NK * 2) +
-         align256((size_t)(d.L + 1) * d.ntiles * kNT * 4);
+  const SplitDims d = split_dims(p, batch * nf * 2, kNTa);
+  return align256((size_t)(d.L + 1) * d.ntiles * kSlices * kNTa * d.NK * 2) +
+         align256((size_t)(d.L + 1) * d.ntiles * kNTa * 4);
 }
 
 inline int slice_members(int nf, int K) {
-  // members per slicing CTA: keep the staged values within 64 KB and 256 columns
-  int mb = std::max(1, std::min(256 / (2 * nf), (64 * 1024) / (2 * nf * K * 8)));
-  return mb;
+  // members per slicing CTA: staged values within 64 KB and at most 256 columns
+  return std::max(1, std::min(256 / (2 * nf), (64 * 1024) / (2 * nf * K * 8)));
 }
 
 template <class Derive>
 int launch_split_synth(const aeolus_plan_impl* p, const Derive& d, double2* FG, int nblk, int batch, void* scratch,
                        cudaStream_t st) {
   constexpr int NF = Derive::NF;
-  const SplitDims dm = split_dims(p, batch * NF * 2);
+  const SplitDims dm = split_dims(p, batch * NF * 2, kNT);
   char* w = static_cast<char*>(scratch);
   __nv_bfloat16* dsyn = reinterpret_cast<__nv_bfloat16*>(w);
   w += align256((size_t)p->split->h_kcum[dm.L + 1] * dm.ntiles * kSlices * kNT * 2);
@@ -450,9 +469,9 @@ int launch_split_synth(const aeolus_plan_impl* p, const Derive& d, double2* FG, 
     k1<<<dim3(dm.L + 1, (batch + mb - 1) / mb), 256, sm1, st>>>(dm, p->split->kcum, batch, mb, d, dsyn, ecol);
     AE_LAUNCH("split_synth_slice_kernel");
   }
-  const size_t sm2 = tc_smem_bytes(kpad(dm.L + 1));
+  const size_t sm2 = tc_smem_bytes(kpad(dm.L + 1), kNT);
   if ((s = allow_smem(tc_synth_kernel, sm2))) return s;
-  ProfScope prof("tc_synth_bf16x5", st);
+  ProfScope prof("tc_synth_bf16x6", st);
   tc_synth_kernel<<<dim3(dm.L + 1, dm.Mt, dm.ntiles), 128, sm2, st>>>(dm, p->split->kcum, p->split->psyn,
                                                                       p->split->esyn, dsyn, ecol, NF, nblk, FG,
                                                                       p->split->err);
@@ -464,10 +483,10 @@ template <class Epi>
 int launch_split_anal(const aeolus_plan_impl* p, const Epi& e, const double2* FG, int nblk, int batch, void* scratch,
                       cudaStream_t st) {
   constexpr int NF = Epi::NF;
-  const SplitDims dm = split_dims(p, batch * NF * 2);
+  const SplitDims dm = split_dims(p, batch * NF * 2, kNTa);
   char* w = static_cast<char*>(scratch);
   __nv_bfloat16* dana = reinterpret_cast<__nv_bfloat16*>(w);
-  w += align256((size_t)(dm.L + 1) * dm.ntiles * kSlices * kNT * dm.NK * 2);
+  w += align256((size_t)(dm.L + 1) * dm.ntiles * kSlices * kNTa * dm.NK * 2);
   int* ecol = reinterpret_cast<int*>(w);
   const int mb = slice_members(NF, dm.nlat);
   const size_t sm1 = (size_t)mb * NF * 2 * dm.nlat * 8;
@@ -479,10 +498,10 @@ int launch_split_anal(const aeolus_plan_impl* p, const Epi& e, const double2* FG
     k1<<<dim3(dm.L + 1, (batch + mb - 1) / mb), 256, sm1, st>>>(dm, batch, mb, nblk, FG, dana, ecol);
     AE_LAUNCH("split_anal_slice_kernel");
   }
-  const size_t sm2 = tc_smem_bytes(dm.NK);
+  const size_t sm2 = tc_smem_bytes(dm.NK, kNTa);
   auto k2 = tc_anal_kernel<Epi>;
   if ((s = allow_smem(k2, sm2))) return s;
-  ProfScope prof("tc_anal_bf16x5", st);
+  ProfScope prof("tc_anal_bf16x6", st);
   k2<<<dim3(dm.L + 1, dm.ntiles), 128, sm2, st>>>(dm, p->split->pana, p->split->eana, dana, ecol, batch, e,
                                                    p->split->err);
   AE_LAUNCH("tc_anal_kernel");

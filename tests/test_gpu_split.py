@@ -1,8 +1,10 @@
 """Split-precision (bf16-digit tcgen05) contraction against the FP64 path.
 
-The split path must stay within 1e-11 relative L2 of the FP64 path for
-single transforms and tendencies, and within 1e-10 after RK4 integration
-(the stated accuracy target of the split-precision form).
+Tolerances (relative L2 against the FP64 path): 1e-12 for single
+transforms (measured ~1e-13); 1e-10 per field for SWE tendencies and RK4
+states -- the divergence tendency is a near-cancellation of curl and
+Laplacian terms (geostrophic balance), which amplifies the ~1e-13 transform
+error by ~100x; 1e-10 is the stated accuracy target of the split form.
 """
 import numpy as np
 import pytest
@@ -47,8 +49,8 @@ def test_split_transforms_match_fp64(nlat, nlon, L):
     c64, cs = N(analyze(p64.id, T(f))), N(analyze(ps.id, T(f)))
     assert device_error(ps) == 0
     for b in range(5):
-        assert rel_l2(gs[b], g64[b]) < 1e-11, rel_l2(gs[b], g64[b])
-        assert rel_l2(cs[b], c64[b]) < 1e-11, rel_l2(cs[b], c64[b])
+        assert rel_l2(gs[b], g64[b]) < 1e-12, rel_l2(gs[b], g64[b])
+        assert rel_l2(cs[b], c64[b]) < 1e-12, rel_l2(cs[b], c64[b])
 
 
 def _swe(nlat, nlon, L, precision, members=4, seed=3):
@@ -66,7 +68,7 @@ def test_split_swe_tendency_and_steps(nlat, nlon, L):
     t64, ts = N(m64.tendency(T(s))), N(ms.tendency(T(s)))
     for b in range(s.shape[0]):
         for f in range(3):
-            assert rel_l2(ts[b, f], t64[b, f]) < 1e-11, (b, f, rel_l2(ts[b, f], t64[b, f]))
+            assert rel_l2(ts[b, f], t64[b, f]) < 1e-10, (b, f, rel_l2(ts[b, f], t64[b, f]))
     y64 = N(m64.rk4(T(s), 240.0, 10))
     ys = N(ms.rk4(T(s), 240.0, 10))
     for b in range(s.shape[0]):
@@ -84,8 +86,8 @@ def test_split_bve_matches_fp64():
     m64, ms = BarotropicVorticity(p64, viscosity=1e5), BarotropicVorticity(ps, viscosity=1e5)
     t64 = N(m64.tendency(BarotropicState(T(z))))
     ts = N(ms.tendency(BarotropicState(T(z))))
-    assert rel_l2(ts, t64) < 1e-11
-    assert rel_l2(N(ms.rk4(T(z), 900.0, 5)), N(m64.rk4(T(z), 900.0, 5))) < 1e-10
+    assert rel_l2(ts, t64) < 1e-12
+    assert rel_l2(N(ms.rk4(T(z), 900.0, 5)), N(m64.rk4(T(z), 900.0, 5))) < 1e-11
 
 
 def test_split_rejects_unsupported_shapes():
