@@ -96,6 +96,8 @@ struct aeolus_plan_impl {
   double* P = nullptr;       // [tri_off(m)*nh + (l-m)*nh + jn]  (row jn fastest)
   double* PT = nullptr;      // [tri_off(m)*nh + jn*(L+1-m) + (l-m)] (degree fastest)
   double2* tw = nullptr;     // [nlon] exp(-2 pi i q / nlon)
+  float4* twdf = nullptr;    // [nlon] the same twiddles as double-float (re.hi, re.lo, im.hi, im.lo)
+  double* invlap = nullptr;  // [L+1] 1 / (-l(l+1)/R^2), 0 at l = 0 (radius of the plan)
   // device tables (points)
   double* basis = nullptr;   // [npoints][ncol] real basis (cos / sin columns)
   double* wpts = nullptr;    // [npoints] quadrature weights

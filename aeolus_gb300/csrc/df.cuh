@@ -1,0 +1,92 @@
+// Double-float ("df") arithmetic: a value is hi + lo with two f32 words
+// (~48-bit significand), built from error-free transforms (Knuth two-sum,
+// FMA two-product; Dekker 1971, Hida-Li-Bailey 2001).  Used by the split-
+// precision row stage, where GB300's f32 pipe is ~64x its f64 pipe.
+#pragma once
+
+#include <cuda_runtime.h>
+
+namespace aeolus {
+
+struct df {
+  float hi, lo;
+};
+
+struct cdf {  // complex df, 16 bytes (same footprint as double2)
+  df re, im;
+};
+
+__device__ __forceinline__ df df_make(float h, float l) { return df{h, l}; }
+
+__device__ __forceinline__ df two_sum(float a, float b) {
+  const float s = a + b;
+  const float bb = s - a;
+  return df{s, (a - (s - bb)) + (b - bb)};
+}
+
+__device__ __forceinline__ df fast_two_sum(float a, float b) {
+  const float s = a + b;
+  return df{s, b - (s - a)};
+}
+
+// Accurate addition: error ~2^-48 relative to the result.
+__device__ __forceinline__ df df_add(df a, df b) {
+  df s = two_sum(a.hi, b.hi);
+  const df t = two_sum(a.lo, b.lo);
+  s.lo += t.hi;
+  s = fast_two_sum(s.hi, s.lo);
+  s.lo += t.lo;
+  return fast_two_sum(s.hi, s.lo);
+}
+
+__device__ __forceinline__ df df_neg(df a) { return df{-a.hi, -a.lo}; }
+__device__ __forceinline__ df df_sub(df a, df b) { return df_add(a, df_neg(b)); }
+
+__device__ __forceinline__ df df_mul(df a, df b) {
+  const float p = a.hi * b.hi;
+  float e = fmaf(a.hi, b.hi, -p);
+  e = fmaf(a.hi, b.lo, e);
+  e = fmaf(a.lo, b.hi, e);
+  return fast_two_sum(p, e);
+}
+
+// Multiplication by a power of two (exact).
+__device__ __forceinline__ df df_scale2(df a, float p2) { return df{a.hi * p2, a.lo * p2}; }
+
+// From / to double (f64 conversions: used only at stage boundaries).
+__device__ __forceinline__ df df_from_double(double x) {
+  const float h = __double2float_rn(x);
+  return df{h, __double2float_rn(x - (double)h)};
+}
+__device__ __forceinline__ double df_to_double(df a) { return (double)a.hi + (double)a.lo; }
+
+__device__ __forceinline__ cdf cdf_add(cdf a, cdf b) { return cdf{df_add(a.re, b.re), df_add(a.im, b.im)}; }
+__device__ __forceinline__ cdf cdf_sub(cdf a, cdf b) { return cdf{df_sub(a.re, b.re), df_sub(a.im, b.im)}; }
+__device__ __forceinline__ cdf cdf_mul(cdf a, cdf b) {
+  return cdf{df_sub(df_mul(a.re, b.re), df_mul(a.im, b.im)), df_add(df_mul(a.re, b.im), df_mul(a.im, b.re))};
+}
+__device__ __forceinline__ cdf cdf_conj(cdf a) { return cdf{a.re, df_neg(a.im)}; }
+__device__ __forceinline__ cdf cdf_i(cdf a) { return cdf{df_neg(a.im), a.re}; }  // i * a
+__device__ __forceinline__ cdf cdf_scale(df s, cdf a) { return cdf{df_mul(s, a.re), df_mul(s, a.im)}; }
+__device__ __forceinline__ cdf cdf_scale2(float p2, cdf a) { return cdf{df_scale2(a.re, p2), df_scale2(a.im, p2)}; }
+__device__ __forceinline__ cdf cdf_zero() { return cdf{df{0.f, 0.f}, df{0.f, 0.f}}; }
+
+__device__ __forceinline__ cdf cdf_from_double2(double2 v) { return cdf{df_from_double(v.x), df_from_double(v.y)}; }
+__device__ __forceinline__ double2 cdf_to_double2(cdf v) { return make_double2(df_to_double(v.re), df_to_double(v.im)); }
+
+// Twiddles are stored as float4 (re.hi, re.lo, im.hi, im.lo).
+__device__ __forceinline__ cdf cdf_from_f4(float4 v) { return cdf{df{v.x, v.y}, df{v.z, v.w}}; }
+
+// Per-row constants handed to the pointwise functors' df_op.
+struct RowDf {
+  df invc;  // 1 / cos(latitude) (clamped)
+  df fj;    // planetary vorticity at the row (2 Omega sin lat), 0 if unused
+  float c;  // cos(latitude) (for guards)
+};
+
+// Constants of the radix-3/5 butterflies as df (hi + lo of the double value).
+struct DfConst {
+  df h3, c1, c2, s1, s2;
+};
+
+}  // namespace aeolus

@@ -20,14 +20,20 @@ struct Spec {  // shared spectral context
   double R;
   const double* cplus;   // [(L+1)^2], C+[L][:] = 0
   const double* cminus;  // [(L+1)^2]
+  const double* invlap;  // [L+1] 1 / lap(l), 0 at l = 0
   __device__ double lap(int l) const { return -(double)l * (l + 1.0) / (R * R); }
   __device__ double2 at(const double2* a, int l, int m) const { return a[(long)l * (L + 1) + m]; }
-  // Helmholtz inverse with l = 0 -> 0 (physics/barotropic.py:91)
+  // Helmholtz inverse with l = 0 -> 0 (physics/barotropic.py:91); a
+  // multiplication by the tabulated reciprocal (within 1 ulp of the divide).
   __device__ double2 invlap0(const double2* a, int l, int m) const {
-    if (l == 0) return make_double2(0.0, 0.0);
-    const double d = lap(l);
     const double2 v = at(a, l, m);
-    return make_double2(v.x / d, v.y / d);
+    if (!invlap) {
+      if (l == 0) return make_double2(0.0, 0.0);
+      const double d = lap(l);
+      return make_double2(v.x / d, v.y / d);
+    }
+    const double r = invlap[l];
+    return make_double2(v.x * r, v.y * r);
   }
   // (i m / R) v
   __device__ double2 dlam(double2 v, int m) const {
@@ -74,6 +80,11 @@ struct JacPw {  // J = (a_snt b_lam - a_lam b_snt) / cos^2
   static constexpr bool kIdentity = false;
   __device__ unsigned operator()(double c, double, const double* in, double* out) const {
     out[0] = (in[1] * in[2] - in[0] * in[3]) / (c * c);
+    return 0u;
+  }
+  __device__ RowDf df_row(double c, double) const { return RowDf{df_from_double(1.0 / (c * c)), df{0.f, 0.f}, (float)c}; }
+  __device__ unsigned df_op(const RowDf& r, const df* in, df* out) const {
+    out[0] = df_mul(df_sub(df_mul(in[1], in[2]), df_mul(in[0], in[3])), r.invc);
     return 0u;
   }
 };
@@ -202,6 +213,16 @@ struct WindPw {
     }
     return 0u;
   }
+  __device__ RowDf df_row(double c, double) const { return RowDf{df_from_double(1.0 / c), df{0.f, 0.f}, (float)c}; }
+  __device__ unsigned df_op(const RowDf& r, const df* in, df* out) const {
+    if (nan_guard && r.c < 1e-6f) {
+      out[0] = out[1] = df{0.f, 0.f};
+    } else {
+      out[0] = df_mul(in[0], r.invc);
+      out[1] = df_mul(in[1], r.invc);
+    }
+    return 0u;
+  }
 };
 
 // ------------------------------------------------------------------ SWE
@@ -262,6 +283,24 @@ struct SwePw {
     unsigned bits = 0u;
     if (!(isfinite(out[0]) && isfinite(out[1]) && isfinite(out[2]) && isfinite(out[3]))) bits |= AEOLUS_STATE_NONFINITE;
     if (!(phi0 + phi > 0.0)) bits |= AEOLUS_STATE_THICKNESS;
+    return bits;
+  }
+  __device__ RowDf df_row(double c, double fg) const {
+    return RowDf{df_from_double(1.0 / c), df_from_double(f10 * fg), (float)c};
+  }
+  __device__ unsigned df_op(const RowDf& r, const df* in, df* out) const {
+    const df u = df_mul(in[0], r.invc), v = df_mul(in[1], r.invc);
+    const df eta_lam = in[2], eta_snt = in[3], phi_lam = in[4], phi_snt = in[5];
+    const df zeta = in[6], delta = in[7], phi = in[8];
+    const df eta = df_add(zeta, r.fj);
+    out[0] = df_neg(df_add(df_mul(df_sub(df_mul(u, eta_lam), df_mul(v, eta_snt)), r.invc), df_mul(eta, delta)));
+    out[1] = df_add(df_mul(eta, zeta), df_mul(df_add(df_mul(v, eta_lam), df_mul(u, eta_snt)), r.invc));
+    out[2] = df_scale2(df_add(df_mul(u, u), df_mul(v, v)), 0.5f);
+    out[3] = df_neg(df_add(df_mul(df_sub(df_mul(u, phi_lam), df_mul(v, phi_snt)), r.invc), df_mul(phi, delta)));
+    unsigned bits = 0u;
+    if (!(isfinite(out[0].hi) && isfinite(out[1].hi) && isfinite(out[2].hi) && isfinite(out[3].hi)))
+      bits |= AEOLUS_STATE_NONFINITE;
+    if (!((float)phi0 + phi.hi > 0.0f)) bits |= AEOLUS_STATE_THICKNESS;
     return bits;
   }
 };
@@ -347,9 +386,20 @@ struct WindPhiPw {
     out[2] = in[2];
     return 0u;
   }
+  __device__ RowDf df_row(double c, double) const { return RowDf{df_from_double(1.0 / c), df{0.f, 0.f}, (float)c}; }
+  __device__ unsigned df_op(const RowDf& r, const df* in, df* out) const {
+    out[0] = df_mul(in[0], r.invc);
+    out[1] = df_mul(in[1], r.invc);
+    out[2] = in[2];
+    return 0u;
+  }
 };
 
-Spec make_spec(const aeolus_plan_impl* p, double R) { return Spec{p->lmax, R, p->cplus, p->cminus}; }
+// The reciprocal table is tabulated with the plan's radius; a call with a
+// different radius must not use it.
+Spec make_spec(const aeolus_plan_impl* p, double R) {
+  return Spec{p->lmax, R, p->cplus, p->cminus, R == p->radius ? p->invlap : nullptr};
+}
 
 // ------------------------------------------------------- reductions
 // Deterministic fixed-order block reduction helpers (256 threads).

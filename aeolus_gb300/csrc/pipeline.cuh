@@ -8,6 +8,7 @@
 #include "common.cuh"
 #include "legendre.cuh"
 #include "rows.cuh"
+#include "rows_df.cuh"
 
 namespace aeolus {
 
@@ -26,6 +27,16 @@ inline int allow_smem(K kern, size_t bytes) {
     AE_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
   }
   return AEOLUS_OK;
+}
+
+// Radix-3/5 butterfly constants split into f32 hi + lo words.
+inline DfConst df_consts() {
+  auto split = [](double v) {
+    const float h = (float)v;
+    return df{h, (float)(v - (double)h)};
+  };
+  return DfConst{split(0.86602540378443864676), split(0.30901699437494742410), split(-0.80901699437494742410),
+                 split(0.95105651629515357212), split(0.58778525229247312917)};
 }
 
 inline int round_threads(long items, int lo, int hi) {
@@ -80,10 +91,21 @@ int launch_rows(const aeolus_plan_impl* p, const Pw& pw, RowArgs a, cudaStream_t
   a.fgrid = p->fgrid;
   a.wq = p->wq;
   const size_t sm = row_smem_bytes<Pw>(p->fft);
+  dim3 grid(p->nlat, a.batch);
+  if (p->precision == AEOLUS_PREC_SPLIT_BF16) {
+    // split-precision path: double-float FFTs and products on the f32 pipe
+    auto kern = row_kernel_df<Pw, IN_MODE, OUT_MODE>;
+    int s = allow_smem(kern, sm);
+    if (s) return s;
+    ProfScope prof(IN_MODE == kInF ? (OUT_MODE == kOutG ? "rows_df_c2r_products_r2c" : "rows_df_c2r") : "rows_df_r2c",
+                   st);
+    kern<<<grid, 256, sm, st>>>(a, pw, p->twdf, df_consts());
+    AE_LAUNCH("row_kernel_df");
+    return AEOLUS_OK;
+  }
   auto kern = row_kernel<Pw, IN_MODE, OUT_MODE>;
   int s = allow_smem(kern, sm);
   if (s) return s;
-  dim3 grid(p->nlat, a.batch);
   ProfScope prof(IN_MODE == kInF ? (OUT_MODE == kOutG ? "rows_c2r_products_r2c" : "rows_c2r") : "rows_r2c", st);
   kern<<<grid, 256, sm, st>>>(a, pw);
   AE_LAUNCH("row_kernel");

@@ -259,6 +259,10 @@ int upload(double** dst, const std::vector<double>& src) {
 }
 
 int common_tables(aeolus_plan_impl* p) {
+  std::vector<double> inv(p->lmax + 1, 0.0);
+  for (int l = 1; l <= p->lmax; ++l) inv[l] = 1.0 / (-(double)l * (l + 1.0) / (p->radius * p->radius));
+  int s0 = upload(&p->invlap, inv);
+  if (s0) return s0;
   std::vector<double> cp, cm, cpt, dummy;
   sin_theta_tables(p->lmax, cp, cm, true);
   sin_theta_tables(p->lmax, cpt, dummy, false);
@@ -271,10 +275,11 @@ int common_tables(aeolus_plan_impl* p) {
 
 void free_plan(aeolus_plan_impl* p) {
   double* bufs[] = {p->x, p->wq, p->coslat, p->fgrid, p->P, p->PT, p->basis, p->wpts,
-                    p->latp, p->cplus, p->cminus, p->cplus_true};
+                    p->latp, p->cplus, p->cminus, p->cplus_true, p->invlap};
   for (double* b : bufs)
     if (b) cudaFree(b);
   if (p->tw) cudaFree(p->tw);
+  if (p->twdf) cudaFree(p->twdf);
 }
 
 }  // namespace
@@ -403,6 +408,16 @@ extern "C" int aeolus_plan_create_gauss(int nlat, int nlon, int lmax, double rad
   std::vector<double2> tw;
   twiddles(nlon, tw);
   if ((s = cuda_check(cudaMalloc(&p->tw, nlon * sizeof(double2)), "cudaMalloc tw"))) return bail(s);
+  {
+    std::vector<float4> twf(nlon);
+    for (int q = 0; q < nlon; ++q) {
+      const float rh = (float)tw[q].x, ih = (float)tw[q].y;
+      twf[q] = make_float4(rh, (float)(tw[q].x - (double)rh), ih, (float)(tw[q].y - (double)ih));
+    }
+    if ((s = cuda_check(cudaMalloc(&p->twdf, nlon * sizeof(float4)), "cudaMalloc twdf"))) return bail(s);
+    if ((s = cuda_check(cudaMemcpy(p->twdf, twf.data(), nlon * sizeof(float4), cudaMemcpyHostToDevice), "twdf")))
+      return bail(s);
+  }
   if ((s = cuda_check(cudaMemcpy(p->tw, tw.data(), nlon * sizeof(double2), cudaMemcpyHostToDevice), "tw")))
     return bail(s);
   if ((s = common_tables(p))) return bail(s);

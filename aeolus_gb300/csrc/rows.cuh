@@ -7,6 +7,7 @@
 #pragma once
 
 #include "common.cuh"
+#include "df.cuh"
 
 namespace aeolus {
 
@@ -249,6 +250,11 @@ struct PwCopy {
   static constexpr int NIN = 1, NOUT = 1;
   static constexpr bool kIdentity = true;
   __device__ unsigned operator()(double, double, const double* in, double* out) const {
+    out[0] = in[0];
+    return 0u;
+  }
+  __device__ RowDf df_row(double c, double) const { return RowDf{df{0.f, 0.f}, df{0.f, 0.f}, (float)c}; }
+  __device__ unsigned df_op(const RowDf&, const df* in, df* out) const {
     out[0] = in[0];
     return 0u;
   }

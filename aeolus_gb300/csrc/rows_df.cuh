@@ -1,0 +1,209 @@
+// Longitude stage in double-float arithmetic (split-precision path).
+//
+// Same structure as row_kernel (rows.cuh): per (latitude row, member) the
+// order spectra go through a half-length complex Stockham FFT (radix 2/3/4/5)
+// to grid values, the pointwise products are formed, and a forward FFT
+// gives the weighted order spectra -- but every operation is a df (f32
+// pair) operation, ~2^-48 relative error, on GB300's f32 pipe.  Spectra in
+// the F/G blocks stay float64; they are converted at load and store.
+#pragma once
+
+#include "df.cuh"
+#include "rows.cuh"
+
+namespace aeolus {
+
+template <bool INV>
+__device__ __forceinline__ void butterfly_df(cdf* v, int r, const DfConst& k) {
+  const float sg = INV ? 1.0f : -1.0f;
+  if (r == 2) {
+    const cdf a = v[0], b = v[1];
+    v[0] = cdf_add(a, b);
+    v[1] = cdf_sub(a, b);
+  } else if (r == 4) {
+    const cdf s02 = cdf_add(v[0], v[2]), d02 = cdf_sub(v[0], v[2]);
+    const cdf s13 = cdf_add(v[1], v[3]), d13 = cdf_sub(v[1], v[3]);
+    const cdf id13 = cdf_scale2(sg, cdf_i(d13));
+    v[0] = cdf_add(s02, s13);
+    v[2] = cdf_sub(s02, s13);
+    v[1] = cdf_add(d02, id13);
+    v[3] = cdf_sub(d02, id13);
+  } else if (r == 3) {
+    const cdf s = cdf_add(v[1], v[2]), d = cdf_sub(v[1], v[2]);
+    const cdf t = cdf_sub(v[0], cdf_scale2(0.5f, s));
+    const cdf id = cdf_scale(k.h3, cdf_scale2(sg, cdf_i(d)));
+    v[0] = cdf_add(v[0], s);
+    v[1] = cdf_add(t, id);
+    v[2] = cdf_sub(t, id);
+  } else {  // r == 5
+    const cdf a1 = cdf_add(v[1], v[4]), a2 = cdf_add(v[2], v[3]);
+    const cdf b1 = cdf_sub(v[1], v[4]), b2 = cdf_sub(v[2], v[3]);
+    const cdf t1 = cdf_add(v[0], cdf_add(cdf_scale(k.c1, a1), cdf_scale(k.c2, a2)));
+    const cdf t2 = cdf_add(v[0], cdf_add(cdf_scale(k.c2, a1), cdf_scale(k.c1, a2)));
+    const cdf u1 = cdf_add(cdf_scale(k.s1, b1), cdf_scale(k.s2, b2));
+    const cdf u2 = cdf_sub(cdf_scale(k.s2, b1), cdf_scale(k.s1, b2));
+    const cdf iu1 = cdf_scale2(sg, cdf_i(u1)), iu2 = cdf_scale2(sg, cdf_i(u2));
+    v[0] = cdf_add(v[0], cdf_add(a1, a2));
+    v[1] = cdf_add(t1, iu1);
+    v[4] = cdf_sub(t1, iu1);
+    v[2] = cdf_add(t2, iu2);
+    v[3] = cdf_sub(t2, iu2);
+  }
+}
+
+template <bool INV>
+__device__ cdf* fft_run_df(cdf* src, cdf* dst, int nf, const FftInfo& fi, const float4* __restrict__ tw,
+                           const DfConst& kc) {
+  const int n = fi.n;
+  int Ls = 1;
+  for (int s = 0; s < fi.nfac; ++s) {
+    const int r = fi.fac[s];
+    const int Ns = Ls * r, nb = n / r, stride = n / Ns;
+    for (int idx = threadIdx.x; idx < nf * nb; idx += blockDim.x) {
+      const int f = idx / nb, jj = idx - f * nb;
+      const cdf* x = src + (long)f * n;
+      cdf* y = dst + (long)f * n;
+      const int k = jj % Ls;
+      cdf v[5];
+      for (int t = 0; t < r; ++t) v[t] = x[jj + t * nb];
+      if (k != 0) {
+        for (int t = 1; t < r; ++t) {
+          cdf w = cdf_from_f4(__ldg(&tw[2 * (k * t * stride)]));
+          if (INV) w = cdf_conj(w);
+          v[t] = cdf_mul(v[t], w);
+        }
+      }
+      butterfly_df<INV>(v, r, kc);
+      const int base = (jj / Ls) * Ns + k;
+      for (int t = 0; t < r; ++t) y[base + t * Ls] = v[t];
+    }
+    __syncthreads();
+    cdf* tmp = src;
+    src = dst;
+    dst = tmp;
+    Ls = Ns;
+  }
+  return src;
+}
+
+template <class Pw, int IN_MODE, int OUT_MODE>
+__global__ void __launch_bounds__(256) row_kernel_df(RowArgs a, Pw pw, const float4* __restrict__ twdf, DfConst kc) {
+  constexpr int NIN = Pw::NIN, NOUT = Pw::NOUT;
+  constexpr int NF = NIN > NOUT ? NIN : NOUT;
+  extern __shared__ cdf smem_df[];
+  __shared__ unsigned s_bits;
+  const int j = blockIdx.x, b = blockIdx.y;
+  const int N = a.fft.N, n = a.fft.n, L = a.L;
+  const int ldm = L + 1;
+  cdf* buf0 = smem_df;
+  cdf* buf1 = smem_df + (long)NF * n;
+  if (threadIdx.x == 0) s_bits = 0u;
+  double2* block = nullptr;
+  if (IN_MODE == kInF || OUT_MODE == kOutG) block = a.FG + ((long)b * a.nlat + j) * a.nblk * ldm;
+
+  // ---- 1. grid rows of the inputs (real df rows, field stride 2n)
+  df* xin = reinterpret_cast<df*>(buf0);
+  if (IN_MODE == kInF) {
+    if (a.fft.use_fft) {
+      for (int idx = threadIdx.x; idx < NIN * n; idx += blockDim.x) {
+        const int f = idx / n, q = idx - f * n;
+        const double2* Ff = block + (long)f * ldm;
+        cdf hq = q <= L ? cdf_from_double2(Ff[q]) : cdf_zero();
+        if (q == 0) hq.im = df{0.f, 0.f};
+        const int qn = n - q;
+        const cdf hn = (q > 0 && qn <= L) ? cdf_from_double2(Ff[qn]) : cdf_zero();
+        const cdf A = cdf_add(hq, cdf_conj(hn));
+        const cdf B = cdf_sub(hq, cdf_conj(hn));
+        const cdf e = cdf_conj(cdf_from_f4(__ldg(&twdf[q])));
+        buf0[idx] = cdf_add(A, cdf_i(cdf_mul(e, B)));
+      }
+      __syncthreads();
+      xin = reinterpret_cast<df*>(fft_run_df<true>(buf0, buf1, NIN, a.fft, twdf, kc));
+    } else {
+      df* x0 = reinterpret_cast<df*>(buf0);
+      for (int idx = threadIdx.x; idx < NIN * N; idx += blockDim.x) {
+        const int f = idx / N, k = idx - f * N;
+        const double2* Ff = block + (long)f * ldm;
+        df acc = df{0.f, 0.f};
+        int e = 0;
+        for (int m = 1; m <= L; ++m) {
+          e += k;
+          if (e >= N) e -= N;
+          const cdf w = cdf_from_f4(__ldg(&twdf[e]));
+          const cdf F = cdf_from_double2(Ff[m]);
+          acc = df_add(acc, df_add(df_mul(F.re, w.re), df_mul(F.im, w.im)));
+        }
+        x0[(long)f * 2 * n + k] = df_add(df_from_double(Ff[0].x), df_scale2(acc, 2.0f));
+      }
+      __syncthreads();
+    }
+  } else {
+    df* x0 = reinterpret_cast<df*>(buf0);
+    for (int idx = threadIdx.x; idx < NIN * N; idx += blockDim.x) {
+      const int f = idx / N, k = idx - f * N;
+      x0[(long)f * 2 * n + k] = df_from_double(a.gin[(long)b * a.gin_b + (long)f * a.gin_f + (long)j * N + k]);
+    }
+    __syncthreads();
+  }
+
+  // ---- 2. pointwise products
+  df* xout = (xin == reinterpret_cast<df*>(buf0)) ? reinterpret_cast<df*>(buf1) : reinterpret_cast<df*>(buf0);
+  {
+    const RowDf rc = pw.df_row(a.coslat[j], a.fgrid ? a.fgrid[j] : 0.0);
+    unsigned bits = 0u;
+    for (int k = threadIdx.x; k < N; k += blockDim.x) {
+      df in[NIN], out[NOUT];
+#pragma unroll
+      for (int f = 0; f < NIN; ++f) in[f] = xin[(long)f * 2 * n + k];
+      bits |= pw.df_op(rc, in, out);
+#pragma unroll
+      for (int f = 0; f < NOUT; ++f) xout[(long)f * 2 * n + k] = out[f];
+    }
+    if (a.status && bits) atomicOr(&s_bits, bits);
+  }
+  __syncthreads();
+  if (a.status && threadIdx.x == 0 && s_bits) atomicOr(&a.status[b], s_bits);
+
+  // ---- 3. outputs
+  if (OUT_MODE == kOutGrid) {
+    for (int idx = threadIdx.x; idx < NOUT * N; idx += blockDim.x) {
+      const int f = idx / N, k = idx - f * N;
+      a.gout[(long)b * a.gout_b + (long)f * a.gout_f + (long)j * N + k] = df_to_double(xout[(long)f * 2 * n + k]);
+    }
+  } else {
+    const df wj = df_from_double(a.wq[j]);
+    if (a.fft.use_fft) {
+      cdf* zin = reinterpret_cast<cdf*>(xout);
+      cdf* zother = (zin == buf0) ? buf1 : buf0;
+      cdf* Z = fft_run_df<false>(zin, zother, NOUT, a.fft, twdf, kc);
+      for (int idx = threadIdx.x; idx < NOUT * ldm; idx += blockDim.x) {
+        const int f = idx / ldm, q = idx - f * ldm;
+        const cdf* Zf = Z + (long)f * n;
+        const cdf zq = Zf[q];
+        const cdf zn = cdf_conj(Zf[q == 0 ? 0 : n - q]);
+        const cdf E = cdf_scale2(0.5f, cdf_add(zq, zn));
+        const cdf D = cdf_sub(zq, zn);
+        const cdf O = cdf{df_scale2(D.im, 0.5f), df_scale2(D.re, -0.5f)};  // -(i/2) D
+        const cdf R = cdf_add(E, cdf_mul(cdf_from_f4(__ldg(&twdf[q])), O));
+        block[(long)f * ldm + q] = cdf_to_double2(cdf_scale(wj, R));
+      }
+    } else {
+      for (int idx = threadIdx.x; idx < NOUT * ldm; idx += blockDim.x) {
+        const int f = idx / ldm, q = idx - f * ldm;
+        const df* x = xout + (long)f * 2 * n;
+        df sr = df{0.f, 0.f}, si = df{0.f, 0.f};
+        int e = 0;
+        for (int k = 0; k < N; ++k) {
+          const cdf w = cdf_from_f4(__ldg(&twdf[e]));
+          sr = df_add(sr, df_mul(x[k], w.re));
+          si = df_add(si, df_mul(x[k], w.im));
+          e += q;
+          while (e >= N) e -= N;
+        }
+        block[(long)f * ldm + q] = make_double2(df_to_double(df_mul(wj, sr)), df_to_double(df_mul(wj, si)));
+      }
+    }
+  }
+}
+
+}  // namespace aeolus

@@ -64,9 +64,9 @@ __global__ void split_psyn_kernel(int L, int nlat, int nh, int Mt, const double*
   const bool south = j >= nh;
   const int jn = south ? nlat - 1 - j : j;
   const double* Pm = P + tri_off(m, L) * nh + jn;
-  double mx = 0.0;
-  for (int t = 0; t < K; ++t) mx = fmax(mx, fabs(Pm[(long)t * nh]));
-  const int E = exponent_for(mx);
+  unsigned long long mx = 0ull;
+  for (int t = 0; t < K; ++t) mx = max(mx, abs_key(Pm[(long)t * nh]));
+  const int E = exponent_for_key(mx);
   eout[m * Mt * 128 + j] = E;
   for (int t = 0; t < Kp; ++t) {
     double v = 0.0;
@@ -87,10 +87,10 @@ __global__ void split_pana_kernel(int L, int nlat, int nh, int NK, const double*
   __nv_bfloat16* blk = out + (long long)m * kSlices * 128 * NK;
   const long long slice = 128LL * NK;
   const double* Pm = P + tri_off(m, L) * nh + (long)t * nh;
-  double mx = 0.0;
+  unsigned long long mx = 0ull;
   if (t < K)
-    for (int jn = 0; jn < nh; ++jn) mx = fmax(mx, fabs(Pm[jn]));
-  const int E = t < K ? exponent_for(mx) : 0;
+    for (int jn = 0; jn < nh; ++jn) mx = max(mx, abs_key(Pm[jn]));
+  const int E = t < K ? exponent_for_key(mx) : 0;
   eout[m * 128 + t] = E;
   for (int j = 0; j < NK; ++j) {
     double v = 0.0;

@@ -35,17 +35,46 @@ int split_build(aeolus_plan_impl* p);
 
 __host__ __device__ inline int kpad(int k) { return (k + 15) / 16 * 16; }
 
-// Exponent E with |x| 2^-E < 1/2 for all |x| <= mx (E = -1000 for mx == 0).
-__device__ inline int exponent_for(double mx) {
-  if (!(mx > 0.0)) return -1000;
-  int e;
-  frexp(mx, &e);
-  return e + 1;
+// All conversions below work on IEEE-754 bit patterns with integer
+// instructions: GB300's FP64 pipe is ~1/64 of its FP32/INT32 rate, and the
+// digit split / recombination touch every element of every contraction.
+
+// |x| as an order-preserving integer key (for the column maxima).
+__device__ inline unsigned long long abs_key(double x) {
+  return static_cast<unsigned long long>(__double_as_longlong(x)) & 0x7FFFFFFFFFFFFFFFull;
+}
+
+// Exponent E with |x| 2^-E < 1/2 for every |x| <= the value whose abs_key
+// is k (E = -1000 for zero or subnormal maxima, which then slice to 0).
+__device__ inline int exponent_for_key(unsigned long long k) {
+  const int ex = static_cast<int>(k >> 52);
+  return ex == 0 ? -1000 : ex - 1021;
+}
+
+// X = rint(x 2^(48-E)) (round half to even), |X| <= 2^47.
+__device__ inline long long fixed_point(double x, int E) {
+  const unsigned long long b = static_cast<unsigned long long>(__double_as_longlong(x));
+  const int ex = static_cast<int>((b >> 52) & 0x7FF);
+  if (ex == 0 || E == -1000) return 0;
+  const unsigned long long m = (b & 0xFFFFFFFFFFFFFull) | (1ull << 52);  // |x| = m 2^(ex-1075)
+  const int sh = 1075 - kShift + E - ex;                                   // right shift
+  unsigned long long q;
+  if (sh >= 54) {
+    q = 0;
+  } else if (sh <= 0) {
+    q = m << (-sh);
+  } else {
+    q = m >> sh;
+    const unsigned long long rem = m & ((1ull << sh) - 1), half = 1ull << (sh - 1);
+    if (rem > half || (rem == half && (q & 1ull))) ++q;
+  }
+  const long long X = static_cast<long long>(q);
+  return (b >> 63) ? -X : X;
 }
 
 // Balanced base-256 digits of rint(x 2^(48-E)), most significant first.
 __device__ inline void digits(double x, int E, float* d) {
-  long long X = (E == -1000) ? 0LL : __double2ll_rn(ldexp(x, kShift - E));
+  long long X = fixed_point(x, E);
 #pragma unroll
   for (int i = kSlices - 1; i >= 1; --i) {
     const long long r = ((X + 128) & 255) - 128;
@@ -55,13 +84,41 @@ __device__ inline void digits(double x, int E, float* d) {
   d[0] = (float)X;
 }
 
+// T 2^e as a double (round to nearest even; results below the normal range
+// flush to zero), integer instructions only.
+__device__ inline double scaled_to_double(long long T, int e) {
+  if (T == 0) return 0.0;
+  const unsigned long long sign = T < 0 ? (1ull << 63) : 0ull;
+  unsigned long long a = T < 0 ? static_cast<unsigned long long>(-T) : static_cast<unsigned long long>(T);
+  int msb = 63 - __clzll(static_cast<long long>(a));
+  unsigned long long mant;
+  if (msb > 52) {
+    const int sh = msb - 52;
+    const unsigned long long rem = a & ((1ull << sh) - 1), half = 1ull << (sh - 1);
+    mant = a >> sh;
+    if (rem > half || (rem == half && (mant & 1ull))) {
+      ++mant;
+      if (mant >> 53) {
+        mant >>= 1;
+        ++msb;
+      }
+    }
+  } else {
+    mant = a << (52 - msb);
+  }
+  const int ex = msb + e + 1023;
+  if (ex <= 0) return 0.0;
+  return __longlong_as_double(static_cast<long long>(sign | (static_cast<unsigned long long>(ex) << 52) |
+                                                     (mant & 0xFFFFFFFFFFFFFull)));
+}
+
 // Level recombination: T = sum_k I_k 256^(5-k), k = 0..5 <-> s+t = 2..7,
 // the top level held in two accumulators.  |T| < 2^62.
 __device__ inline long long combine_levels(const float* acc) {
   long long T = 0;
 #pragma unroll
-  for (int k = 0; k < kLevels - 1; ++k) T = (T << 8) + __float2ll_rn(acc[k]);
-  return (T << 8) + __float2ll_rn(acc[kLevels - 1]) + __float2ll_rn(acc[kLevels]);
+  for (int k = 0; k < kLevels - 1; ++k) T = (T << 8) + __float2int_rn(acc[k]);
+  return (T << 8) + ((long long)__float2int_rn(acc[kLevels - 1]) + __float2int_rn(acc[kLevels]));
 }
 
 // Accumulator of digit pair (s, t) (0-based): one per level, except the
@@ -121,11 +178,11 @@ __global__ void __launch_bounds__(256) split_synth_slice_kernel(SplitDims dm, co
   // column exponents (one warp per column)
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
   for (int c = warp; c < nc; c += nwarp) {
-    double mx = 0.0;
-    for (int t = lane; t < K; t += 32) mx = fmax(mx, fabs(s_val[c * K + t]));
-    for (int o = 16; o > 0; o >>= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+    unsigned long long mx = 0ull;
+    for (int t = lane; t < K; t += 32) mx = max(mx, abs_key(s_val[c * K + t]));
+    for (int o = 16; o > 0; o >>= 1) mx = max(mx, __shfl_xor_sync(0xffffffffu, mx, o));
     if (lane == 0) {
-      const int E = exponent_for(mx);
+      const int E = exponent_for_key(mx);
       s_exp[c] = E;
       ecol[(long long)m * dm.ntiles * kNT + (long long)b0 * NF * 2 + c] = E;
     }
@@ -179,11 +236,11 @@ __global__ void __launch_bounds__(256) split_anal_slice_kernel(SplitDims dm, int
   __syncthreads();
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
   for (int c = warp; c < nc; c += nwarp) {
-    double mx = 0.0;
-    for (int j = lane; j < nlat; j += 32) mx = fmax(mx, fabs(s_val[c * nlat + j]));
-    for (int o = 16; o > 0; o >>= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+    unsigned long long mx = 0ull;
+    for (int j = lane; j < nlat; j += 32) mx = max(mx, abs_key(s_val[c * nlat + j]));
+    for (int o = 16; o > 0; o >>= 1) mx = max(mx, __shfl_xor_sync(0xffffffffu, mx, o));
     if (lane == 0) {
-      const int E = exponent_for(mx);
+      const int E = exponent_for_key(mx);
       s_exp[c] = E;
       ecol[(long long)m * dm.ntiles * kNTa + (long long)b0 * NF * 2 + c] = E;
     }
@@ -365,8 +422,8 @@ static __global__ void __launch_bounds__(128, 1) tc_synth_kernel(SplitDims dm, c
         for (int i = 0; i < 16; i += 2) {
           const int n = tile * kNT + c0 + i;  // even: real part, n + 1: imaginary part
           if (n >= dm.ncol) break;
-          const double re = ldexp((double)combine_levels(acc[i]), Ej + ec[c0 + i] - kOut);
-          const double im = ldexp((double)combine_levels(acc[i + 1]), Ej + ec[c0 + i + 1] - kOut);
+          const double re = scaled_to_double(combine_levels(acc[i]), Ej + ec[c0 + i] - kOut);
+          const double im = scaled_to_double(combine_levels(acc[i + 1]), Ej + ec[c0 + i + 1] - kOut);
           const int bf = n >> 1;
           const int b = bf / nf, f = bf - b * nf;
           F[(((long long)b * dm.nlat + j) * nblk + f) * (L + 1) + m] = make_double2(re, im);
@@ -413,8 +470,8 @@ __global__ void __launch_bounds__(128, 1) tc_anal_kernel(SplitDims dm, const __n
           double2 a[NF];
 #pragma unroll
           for (int f = 0; f < NF; ++f) {
-            a[f].x = ldexp((double)combine_levels(acc[i + 2 * f]), Et + ec[c0 + i + 2 * f] - kOut);
-            a[f].y = ldexp((double)combine_levels(acc[i + 2 * f + 1]), Et + ec[c0 + i + 2 * f + 1] - kOut);
+            a[f].x = scaled_to_double(combine_levels(acc[i + 2 * f]), Et + ec[c0 + i + 2 * f] - kOut);
+            a[f].y = scaled_to_double(combine_levels(acc[i + 2 * f + 1]), Et + ec[c0 + i + 2 * f + 1] - kOut);
           }
           epi.finish(b, m + t, m, a);
         }
