@@ -5,7 +5,9 @@
 // to grid values, the pointwise products are formed, and a forward FFT
 // gives the weighted order spectra -- but every operation is a df (f32
 // pair) operation, ~2^-48 relative error, on GB300's f32 pipe.  Spectra in
-// the F/G blocks stay float64; they are converted at load and store.
+// the F/G blocks hold double-float words (float4 = re.hi, re.lo, im.hi,
+// im.lo per complex value) written and read by the tensor-core stages, so
+// the row stage touches no f64 arithmetic at all.
 #pragma once
 
 #include "df.cuh"
@@ -98,8 +100,8 @@ __global__ void __launch_bounds__(256) row_kernel_df(RowArgs a, Pw pw, const flo
   cdf* buf0 = smem_df;
   cdf* buf1 = smem_df + (long)NF * n;
   if (threadIdx.x == 0) s_bits = 0u;
-  double2* block = nullptr;
-  if (IN_MODE == kInF || OUT_MODE == kOutG) block = a.FG + ((long)b * a.nlat + j) * a.nblk * ldm;
+  float4* block = nullptr;
+  if (IN_MODE == kInF || OUT_MODE == kOutG) block = reinterpret_cast<float4*>(a.FG) + ((long)b * a.nlat + j) * a.nblk * ldm;
 
   // ---- 1. grid rows of the inputs (real df rows, field stride 2n)
   df* xin = reinterpret_cast<df*>(buf0);
@@ -107,11 +109,11 @@ __global__ void __launch_bounds__(256) row_kernel_df(RowArgs a, Pw pw, const flo
     if (a.fft.use_fft) {
       for (int idx = threadIdx.x; idx < NIN * n; idx += blockDim.x) {
         const int f = idx / n, q = idx - f * n;
-        const double2* Ff = block + (long)f * ldm;
-        cdf hq = q <= L ? cdf_from_double2(Ff[q]) : cdf_zero();
+        const float4* Ff = block + (long)f * ldm;
+        cdf hq = q <= L ? cdf_from_f4(Ff[q]) : cdf_zero();
         if (q == 0) hq.im = df{0.f, 0.f};
         const int qn = n - q;
-        const cdf hn = (q > 0 && qn <= L) ? cdf_from_double2(Ff[qn]) : cdf_zero();
+        const cdf hn = (q > 0 && qn <= L) ? cdf_from_f4(Ff[qn]) : cdf_zero();
         const cdf A = cdf_add(hq, cdf_conj(hn));
         const cdf B = cdf_sub(hq, cdf_conj(hn));
         const cdf e = cdf_conj(cdf_from_f4(__ldg(&twdf[q])));
@@ -123,17 +125,17 @@ __global__ void __launch_bounds__(256) row_kernel_df(RowArgs a, Pw pw, const flo
       df* x0 = reinterpret_cast<df*>(buf0);
       for (int idx = threadIdx.x; idx < NIN * N; idx += blockDim.x) {
         const int f = idx / N, k = idx - f * N;
-        const double2* Ff = block + (long)f * ldm;
+        const float4* Ff = block + (long)f * ldm;
         df acc = df{0.f, 0.f};
         int e = 0;
         for (int m = 1; m <= L; ++m) {
           e += k;
           if (e >= N) e -= N;
           const cdf w = cdf_from_f4(__ldg(&twdf[e]));
-          const cdf F = cdf_from_double2(Ff[m]);
+          const cdf F = cdf_from_f4(Ff[m]);
           acc = df_add(acc, df_add(df_mul(F.re, w.re), df_mul(F.im, w.im)));
         }
-        x0[(long)f * 2 * n + k] = df_add(df_from_double(Ff[0].x), df_scale2(acc, 2.0f));
+        x0[(long)f * 2 * n + k] = df_add(df{Ff[0].x, Ff[0].y}, df_scale2(acc, 2.0f));
       }
       __syncthreads();
     }
@@ -184,8 +186,8 @@ __global__ void __launch_bounds__(256) row_kernel_df(RowArgs a, Pw pw, const flo
         const cdf E = cdf_scale2(0.5f, cdf_add(zq, zn));
         const cdf D = cdf_sub(zq, zn);
         const cdf O = cdf{df_scale2(D.im, 0.5f), df_scale2(D.re, -0.5f)};  // -(i/2) D
-        const cdf R = cdf_add(E, cdf_mul(cdf_from_f4(__ldg(&twdf[q])), O));
-        block[(long)f * ldm + q] = cdf_to_double2(cdf_scale(wj, R));
+        const cdf R = cdf_scale(wj, cdf_add(E, cdf_mul(cdf_from_f4(__ldg(&twdf[q])), O)));
+        block[(long)f * ldm + q] = make_float4(R.re.hi, R.re.lo, R.im.hi, R.im.lo);
       }
     } else {
       for (int idx = threadIdx.x; idx < NOUT * ldm; idx += blockDim.x) {
@@ -200,7 +202,8 @@ __global__ void __launch_bounds__(256) row_kernel_df(RowArgs a, Pw pw, const flo
           e += q;
           while (e >= N) e -= N;
         }
-        block[(long)f * ldm + q] = make_double2(df_to_double(df_mul(wj, sr)), df_to_double(df_mul(wj, si)));
+        const df gr = df_mul(wj, sr), gi = df_mul(wj, si);
+        block[(long)f * ldm + q] = make_float4(gr.hi, gr.lo, gi.hi, gi.lo);
       }
     }
   }

@@ -53,11 +53,10 @@ __global__ void split_psyn_kernel(int L, int nlat, int nh, int Mt, const double*
   if (m > L || j >= Mt * 128) return;
   const int K = L + 1 - m, Kp = kpad(K);
   const int mt = j / 128, r = j % 128;
-  __nv_bfloat16* blk = out + kcum[m] * (long long)Mt * kSlices * 128 + (long long)mt * kSlices * 128 * Kp;
-  const long long slice = 128LL * Kp;
+  __nv_bfloat16* blk = out + psyn_tile(kcum, Mt, m, mt, Kp);
   if (j >= nlat) {
     for (int t = 0; t < Kp; ++t)
-      for (int s = 0; s < kSlices; ++s) blk[s * slice + tc::core_index(r, t, Kp)] = __float2bfloat16(0.0f);
+      for (int s = 0; s < kSlices; ++s) blk[tile_elem(128, s, r, t)] = __float2bfloat16(0.0f);
     eout[m * Mt * 128 + j] = 0;
     return;
   }
@@ -73,7 +72,7 @@ __global__ void split_psyn_kernel(int L, int nlat, int nh, int Mt, const double*
     if (t < K) v = Pm[(long)t * nh] * ((south && (t & 1)) ? -1.0 : 1.0);
     float d[kSlices];
     digits(v, E, d);
-    for (int s = 0; s < kSlices; ++s) blk[s * slice + tc::core_index(r, t, Kp)] = __float2bfloat16(d[s]);
+    for (int s = 0; s < kSlices; ++s) blk[tile_elem(128, s, r, t)] = __float2bfloat16(d[s]);
   }
 }
 
@@ -84,8 +83,7 @@ __global__ void split_pana_kernel(int L, int nlat, int nh, int NK, const double*
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (m > L || t >= 128) return;
   const int K = L + 1 - m;
-  __nv_bfloat16* blk = out + (long long)m * kSlices * 128 * NK;
-  const long long slice = 128LL * NK;
+  __nv_bfloat16* blk = out + pana_tile(NK, m);
   const double* Pm = P + tri_off(m, L) * nh + (long)t * nh;
   unsigned long long mx = 0ull;
   if (t < K)
@@ -100,7 +98,7 @@ __global__ void split_pana_kernel(int L, int nlat, int nh, int NK, const double*
     }
     float d[kSlices];
     digits(v, E, d);
-    for (int s = 0; s < kSlices; ++s) blk[s * slice + tc::core_index(t, j, NK)] = __float2bfloat16(d[s]);
+    for (int s = 0; s < kSlices; ++s) blk[tile_elem(128, s, t, j)] = __float2bfloat16(d[s]);
   }
 }
 

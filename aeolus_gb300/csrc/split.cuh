@@ -6,6 +6,7 @@
 #include <cuda_bf16.h>
 
 #include "common.cuh"
+#include "df.cuh"
 #include "legendre.cuh"
 #include "tc.cuh"
 
@@ -14,9 +15,10 @@ namespace aeolus {
 constexpr int kSlices = 6;   // base-256 digits per operand (48 bits)
 constexpr int kLevels = 6;   // kept levels k = s + t = 2..7 (1-based digits)
 constexpr int kAccs = 7;     // TMEM accumulators: the 6-pair top level is split in two
-constexpr int kNT = 64;      // data columns per synthesis tile (MMA N)
-constexpr int kNTa = 48;     // data columns per analysis tile
-constexpr int kTmemCols = 512;
+constexpr int kNT = 32;      // data columns per tensor-core tile (MMA N)
+constexpr int kKC = 16;      // contraction depth per pipeline chunk (one MMA K step)
+constexpr int kStages = 3;   // shared-memory pipeline depth (chunks in flight)
+constexpr int kTmemCols = 256;  // kAccs * kNT = 224 columns, two CTAs per SM
 constexpr int kShift = 8 * kSlices;  // X = rint(x 2^(kShift - E))
 constexpr int kMaxKp = 128;  // degrees per order (l_max <= 127)
 
@@ -112,6 +114,94 @@ __device__ inline double scaled_to_double(long long T, int e) {
                                                      (mant & 0xFFFFFFFFFFFFFull)));
 }
 
+// ------------------------------------------------ double-float conversions
+// Round a > 0 to 24 significant bits: a ~ q 2^sh with q < 2^24 (RNE).
+__device__ inline void round24(unsigned long long a, unsigned long long& q, int& sh) {
+  const int msb = 63 - __clzll(static_cast<long long>(a));
+  if (msb <= 23) {
+    q = a;
+    sh = 0;
+    return;
+  }
+  sh = msb - 23;
+  q = a >> sh;
+  const unsigned long long rem = a & ((1ull << sh) - 1), half = 1ull << (sh - 1);
+  if (rem > half || (rem == half && (q & 1ull))) {
+    ++q;
+    if (q >> 24) {
+      q >>= 1;
+      ++sh;
+    }
+  }
+}
+
+// q 2^(sh+e) as a float (q < 2^24 exact); below the normal range -> 0.
+__device__ inline float make_float(unsigned long long q, int sh, int e, bool neg) {
+  if (q == 0) return 0.0f;
+  const int msb = 63 - __clzll(static_cast<long long>(q));
+  const int ex = msb + sh + e + 127;
+  if (ex <= 0) return 0.0f;
+  if (ex >= 255) return neg ? -INFINITY : INFINITY;
+  const unsigned m = static_cast<unsigned>((q << (23 - msb)) & 0x7FFFFFull);
+  return __uint_as_float((neg ? 0x80000000u : 0u) | (static_cast<unsigned>(ex) << 23) | m);
+}
+
+// T 2^e as a double-float (hi = fl(T 2^e), lo = fl((T - hi) 2^e)), integer ops.
+__device__ inline df scaled_to_df(long long T, int e) {
+  if (T == 0) return df{0.f, 0.f};
+  const bool neg = T < 0;
+  const unsigned long long a = neg ? static_cast<unsigned long long>(-T) : static_cast<unsigned long long>(T);
+  unsigned long long q;
+  int sh;
+  round24(a, q, sh);
+  const float hi = make_float(q, sh, e, neg);
+  const long long r = static_cast<long long>(a) - static_cast<long long>(q << sh);
+  if (r == 0) return df{hi, 0.f};
+  const bool rneg = (r < 0) != neg;
+  unsigned long long q2;
+  int sh2;
+  round24(static_cast<unsigned long long>(r < 0 ? -r : r), q2, sh2);
+  return df{hi, make_float(q2, sh2, e, rneg)};
+}
+
+// rint(f 2^(48-E)) for a float f, integer ops (|result| < 2^47 by choice of E).
+__device__ inline long long fixed_point_f(float f, int E) {
+  const unsigned b = __float_as_uint(f);
+  const int ex = static_cast<int>((b >> 23) & 0xFF);
+  if (ex == 0 || E == -1000) return 0;
+  const unsigned long long m = (b & 0x7FFFFFu) | 0x800000u;  // |f| = m 2^(ex-150)
+  const int sh = 150 - kShift + E - ex;
+  unsigned long long q;
+  if (sh >= 25) {
+    q = 0;
+  } else if (sh <= 0) {
+    q = m << (-sh);
+  } else {
+    q = m >> sh;
+    const unsigned long long rem = m & ((1ull << sh) - 1), half = 1ull << (sh - 1);
+    if (rem > half || (rem == half && (q & 1ull))) ++q;
+  }
+  const long long X = static_cast<long long>(q);
+  return (b >> 31) ? -X : X;
+}
+
+// Exponent for a column of double-floats from the largest |hi| bit key:
+// |hi + lo| 2^-E < 1/4 (one spare bit for the lo word).
+__device__ inline int exponent_for_fkey(unsigned k) {
+  const int ex = static_cast<int>(k >> 23);
+  return ex == 0 ? -1000 : ex - 124;
+}
+
+__device__ inline void digits_from_fixed(long long X, float* d) {
+#pragma unroll
+  for (int i = kSlices - 1; i >= 1; --i) {
+    const long long r = ((X + 128) & 255) - 128;
+    d[i] = (float)r;
+    X = (X - r) >> 8;
+  }
+  d[0] = (float)X;
+}
+
 // Level recombination: T = sum_k I_k 256^(5-k), k = 0..5 <-> s+t = 2..7,
 // the top level held in two accumulators.  |T| < 2^62.
 __device__ inline long long combine_levels(const float* acc) {
@@ -132,21 +222,35 @@ __host__ __device__ constexpr int acc_of(int s, int t) {
 constexpr int kOut = 2 * kShift - 8 * (kSlices - 1);
 
 // ----------------------------------------------------------- layouts
+// Every operand is stored chunk-major: for each 16-deep K chunk, the
+// kSlices digit tiles (rows x 16, core-matrix layout with K = 16) are
+// contiguous, so one bulk copy moves a whole pipeline stage.
 struct SplitDims {
   int L, nlat, nh, NK, Mt;
   int ncol;     // data columns (members x fields x 2)
   int ntiles;   // ceil(ncol / kNT)
 };
 
-// Synthesis data digits, block (m, ntile, slice): kNT x Kpad_m.
-__host__ __device__ inline long long dsyn_block(const long long* kcum, const SplitDims& d, int m, int ntile, int s) {
-  const int Kp = kpad(d.L + 1 - m);
-  return kcum[m] * (long long)d.ntiles * kSlices * kNT + ((long long)ntile * kSlices + s) * kNT * Kp;
-}
+__host__ __device__ constexpr long long chunk_elems(int rows) { return (long long)kSlices * rows * kKC; }
 
-// Analysis data digits, block (m, ntile, slice): kNTa x NK.
-__host__ __device__ inline long long dana_block(const SplitDims& d, int m, int ntile, int s) {
-  return (((long long)m * d.ntiles + ntile) * kSlices + s) * kNTa * (long long)d.NK;
+// Synthesis basis, tile (m, latitude tile mt): chunks of 128 rows.
+__host__ __device__ inline long long psyn_tile(const long long* kcum, int Mt, int m, int mt, int Kp) {
+  return kcum[m] * (long long)Mt * kSlices * 128 + (long long)mt * kSlices * 128 * Kp;
+}
+// Analysis basis, tile m: NK/16 chunks of 128 degree rows.
+__host__ __device__ inline long long pana_tile(int NK, int m) { return (long long)m * kSlices * 128 * NK; }
+// Synthesis data, tile (m, ntile): Kp/16 chunks of kNT rows.
+__host__ __device__ inline long long dsyn_tile(const long long* kcum, const SplitDims& d, int m, int ntile) {
+  const int Kp = kpad(d.L + 1 - m);
+  return kcum[m] * (long long)d.ntiles * kSlices * kNT + (long long)ntile * kSlices * kNT * Kp;
+}
+// Analysis data, tile (m, ntile): NK/16 chunks of kNT rows.
+__host__ __device__ inline long long dana_tile(const SplitDims& d, int m, int ntile) {
+  return ((long long)m * d.ntiles + ntile) * kSlices * kNT * (long long)d.NK;
+}
+// Element (row r, contraction index k) of slice s inside a tile.
+__host__ __device__ inline long long tile_elem(int rows, int s, int r, int k) {
+  return (long long)(k / kKC) * chunk_elems(rows) + (long long)s * rows * kKC + tc::core_index(r, k % kKC, kKC);
 }
 
 // ------------------------------------------------- synthesis data slicing
@@ -175,7 +279,6 @@ __global__ void __launch_bounds__(256) split_synth_slice_kernel(SplitDims dm, co
     }
   }
   __syncthreads();
-  // column exponents (one warp per column)
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
   for (int c = warp; c < nc; c += nwarp) {
     unsigned long long mx = 0ull;
@@ -191,34 +294,32 @@ __global__ void __launch_bounds__(256) split_synth_slice_kernel(SplitDims dm, co
   for (int idx = threadIdx.x; idx < nc * Kp; idx += blockDim.x) {
     const int c = idx / Kp, t = idx - c * Kp;
     const int n = b0 * NF * 2 + c;
-    const int tile = n / kNT, nl = n % kNT;
     float d[kSlices];
     digits(t < K ? s_val[c * K + t] : 0.0, s_exp[c], d);
+    __nv_bfloat16* tile = dsyn + dsyn_tile(kcum, dm, m, n / kNT);
 #pragma unroll
-    for (int s = 0; s < kSlices; ++s)
-      dsyn[dsyn_block(kcum, dm, m, tile, s) + tc::core_index(nl, t, Kp)] = __float2bfloat16(d[s]);
+    for (int s = 0; s < kSlices; ++s) tile[tile_elem(kNT, s, n % kNT, t)] = __float2bfloat16(d[s]);
   }
-  // zero columns that pad the last tile
-  if (blockIdx.y == gridDim.y - 1) {
+  if (blockIdx.y == gridDim.y - 1) {  // zero the columns that pad the last tile
     const int n0 = batch * NF * 2, n1 = dm.ntiles * kNT;
     for (int idx = threadIdx.x; idx < (n1 - n0) * Kp; idx += blockDim.x) {
       const int n = n0 + idx / Kp, t = idx % Kp;
+      __nv_bfloat16* tile = dsyn + dsyn_tile(kcum, dm, m, n / kNT);
 #pragma unroll
-      for (int s = 0; s < kSlices; ++s)
-        dsyn[dsyn_block(kcum, dm, m, n / kNT, s) + tc::core_index(n % kNT, t, Kp)] = __float2bfloat16(0.0f);
+      for (int s = 0; s < kSlices; ++s) tile[tile_elem(kNT, s, n % kNT, t)] = __float2bfloat16(0.0f);
       if (t == 0) ecol[(long long)m * dm.ntiles * kNT + n] = 0;
     }
   }
 }
 
 // ------------------------------------------------- analysis data slicing
-// Reads G[b][j][f][m] (F/G blocks of nblk fields), grid (m, member chunk).
+// Reads the double-float G blocks (float4 per complex value), grid (m, chunk).
 template <int NF>
 __global__ void __launch_bounds__(256) split_anal_slice_kernel(SplitDims dm, int batch, int mb, int nblk,
-                                                              const double2* __restrict__ FG,
+                                                              const float4* __restrict__ FG,
                                                               __nv_bfloat16* __restrict__ dana,
                                                               int* __restrict__ ecol) {
-  extern __shared__ double s_val[];  // [mb*NF*2][nlat]
+  extern __shared__ df s_dval[];  // [mb*NF*2][nlat]
   __shared__ int s_exp[256];
   const int m = blockIdx.x, L = dm.L, nlat = dm.nlat, NK = dm.NK;
   const int ldm = L + 1;
@@ -229,20 +330,20 @@ __global__ void __launch_bounds__(256) split_anal_slice_kernel(SplitDims dm, int
     const int j = idx % nlat;
     const int r = idx / nlat;
     const int f = r % NF, bl = r / NF;
-    const double2 g = FG[(((long long)(b0 + bl) * nlat + j) * nblk + f) * ldm + m];
-    s_val[((bl * NF + f) * 2 + 0) * nlat + j] = g.x;
-    s_val[((bl * NF + f) * 2 + 1) * nlat + j] = g.y;
+    const float4 g = FG[(((long long)(b0 + bl) * nlat + j) * nblk + f) * ldm + m];
+    s_dval[((bl * NF + f) * 2 + 0) * nlat + j] = df{g.x, g.y};
+    s_dval[((bl * NF + f) * 2 + 1) * nlat + j] = df{g.z, g.w};
   }
   __syncthreads();
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
   for (int c = warp; c < nc; c += nwarp) {
-    unsigned long long mx = 0ull;
-    for (int j = lane; j < nlat; j += 32) mx = max(mx, abs_key(s_val[c * nlat + j]));
+    unsigned mx = 0u;
+    for (int j = lane; j < nlat; j += 32) mx = max(mx, __float_as_uint(s_dval[c * nlat + j].hi) & 0x7FFFFFFFu);
     for (int o = 16; o > 0; o >>= 1) mx = max(mx, __shfl_xor_sync(0xffffffffu, mx, o));
     if (lane == 0) {
-      const int E = exponent_for_key(mx);
+      const int E = exponent_for_fkey(mx);
       s_exp[c] = E;
-      ecol[(long long)m * dm.ntiles * kNTa + (long long)b0 * NF * 2 + c] = E;
+      ecol[(long long)m * dm.ntiles * kNT + (long long)b0 * NF * 2 + c] = E;
     }
   }
   __syncthreads();
@@ -250,121 +351,125 @@ __global__ void __launch_bounds__(256) split_anal_slice_kernel(SplitDims dm, int
     const int c = idx / NK, j = idx - c * NK;
     const int n = b0 * NF * 2 + c;
     float d[kSlices];
-    digits(j < nlat ? s_val[c * nlat + j] : 0.0, s_exp[c], d);
+    long long X = 0;
+    if (j < nlat) {
+      const df v = s_dval[c * nlat + j];
+      X = fixed_point_f(v.hi, s_exp[c]) + fixed_point_f(v.lo, s_exp[c]);
+    }
+    digits_from_fixed(X, d);
+    __nv_bfloat16* tile = dana + dana_tile(dm, m, n / kNT);
 #pragma unroll
-    for (int s = 0; s < kSlices; ++s)
-      dana[dana_block(dm, m, n / kNTa, s) + tc::core_index(n % kNTa, j, NK)] = __float2bfloat16(d[s]);
+    for (int s = 0; s < kSlices; ++s) tile[tile_elem(kNT, s, n % kNT, j)] = __float2bfloat16(d[s]);
   }
   if (blockIdx.y == gridDim.y - 1) {
-    const int n0 = batch * NF * 2, n1 = dm.ntiles * kNTa;
+    const int n0 = batch * NF * 2, n1 = dm.ntiles * kNT;
     for (int idx = threadIdx.x; idx < (n1 - n0) * NK; idx += blockDim.x) {
       const int n = n0 + idx / NK, j = idx % NK;
+      __nv_bfloat16* tile = dana + dana_tile(dm, m, n / kNT);
 #pragma unroll
-      for (int s = 0; s < kSlices; ++s)
-        dana[dana_block(dm, m, n / kNTa, s) + tc::core_index(n % kNTa, j, NK)] = __float2bfloat16(0.0f);
-      if (j == 0) ecol[(long long)m * dm.ntiles * kNTa + n] = 0;
+      for (int s = 0; s < kSlices; ++s) tile[tile_elem(kNT, s, n % kNT, j)] = __float2bfloat16(0.0f);
+      if (j == 0) ecol[(long long)m * dm.ntiles * kNT + n] = 0;
     }
   }
 }
 
-// ---------------------------------------------------- tensor-core GEMM core
-// Shared by synthesis and analysis: A = kSlices basis-digit tiles (128 x KK,
-// streamed through a double buffer), B = kSlices data-digit tiles (NT x KK,
-// resident).  On return accumulator a sits in TMEM columns [a*NT, (a+1)*NT).
-// Returns false (and sets *err) if a bounded wait expired.
-struct TcSmem {
-  __nv_bfloat16* A[2];
-  __nv_bfloat16* B;
-  uint64_t* bar;  // [0..1] A buffers loaded, [2..3] A buffers free, [4] B loaded, [5] MMAs done
+// ---------------------------------------------------- tensor-core mainloop
+// One CTA = one 128 x kNT output tile.  Warp 0 lane 0 produces: it streams
+// K chunks (kSlices basis tiles 128 x 16 + kSlices data tiles kNT x 16)
+// through kStages shared-memory stages with the TMA bulk-copy engine.  Warp
+// 1 lane 0 issues, per chunk, the 21 digit-pair MMAs into the level
+// accumulators and commits the stage back to the producer.  All waits are
+// bounded; an expired wait sets *err and the CTA skips its outputs.
+struct TcPipe {
+  __nv_bfloat16* A[kStages];
+  __nv_bfloat16* B[kStages];
+  uint64_t* full;   // [kStages]
+  uint64_t* empty;  // [kStages]
+  uint64_t* done;
+  uint32_t* tmem_slot;
 };
 
-template <int NT>
-__device__ inline bool tc_levels(const TcSmem& sm, const __nv_bfloat16* gA, long long a_slice_elems,
-                                 const __nv_bfloat16* gB, long long b_slice_elems, int KK, uint32_t tmem,
-                                 int* err) {
-  const uint32_t abytes = 128u * KK * 2u, bbytes = (uint32_t)NT * KK * 2u;
+constexpr size_t kStageBytesA = chunk_elems(128) * 2;
+constexpr size_t kStageBytesB = chunk_elems(kNT) * 2;
+
+inline size_t tc_smem_bytes() {
+  // 1 KB alignment slack + stages + barriers; >= 77 KB so at most two CTAs
+  // (2 x 256 TMEM columns) are resident on an SM.
+  const size_t need = 1024 + kStages * (kStageBytesA + kStageBytesB) + 256;
+  return std::max<size_t>(need, 77 * 1024);
+}
+
+__device__ inline void tc_carve(char* base, TcPipe& p) {
+  char* q = reinterpret_cast<char*>((reinterpret_cast<uintptr_t>(base) + 1023) & ~uintptr_t(1023));
+  for (int s = 0; s < kStages; ++s) {
+    p.A[s] = reinterpret_cast<__nv_bfloat16*>(q);
+    q += kStageBytesA;
+    p.B[s] = reinterpret_cast<__nv_bfloat16*>(q);
+    q += kStageBytesB;
+  }
+  uint64_t* bars = reinterpret_cast<uint64_t*>(q);
+  p.full = bars;
+  p.empty = bars + kStages;
+  p.done = bars + 2 * kStages;
+  p.tmem_slot = reinterpret_cast<uint32_t*>(bars + 2 * kStages + 1);
+}
+
+// Runs the whole contraction; on return (all threads) the accumulators are
+// complete in TMEM, or the function returned false.
+__device__ inline bool tc_mainloop(TcPipe& p, const __nv_bfloat16* gA, const __nv_bfloat16* gB, int nchunks,
+                                   uint32_t tmem, int* err) {
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   bool ok = true;
-  if (threadIdx.x == 0) {
-    int issued[2] = {0, 0}, waited[2] = {0, 0};
-    unsigned started = 0u;  // accumulators already holding a partial sum
-    bool b_ok = false;
-    tc::mbar_expect_tx(&sm.bar[4], kSlices * bbytes);
-    for (int t = 0; t < kSlices; ++t)
-      tc::bulk_g2s(sm.B + (long long)t * NT * KK, gB + t * b_slice_elems, bbytes, &sm.bar[4]);
-    for (int s = 0; s < 2; ++s) {
-      tc::mbar_expect_tx(&sm.bar[s], abytes);
-      tc::bulk_g2s(sm.A[s], gA + s * a_slice_elems, abytes, &sm.bar[s]);
-      issued[s] = 1;
-    }
-    const uint32_t idesc = tc::idesc_bf16_f32(128, NT);
-    const uint32_t sbo = (uint32_t)KK * 16u;
-    ok = b_ok = tc::mbar_wait(&sm.bar[4], 0);
-    for (int s = 0; s < kSlices && ok; ++s) {
-      const int buf = s & 1;
-      ok = tc::mbar_wait(&sm.bar[buf], waited[buf] & 1);
+  if (warp == 0 && lane == 0) {  // producer
+    for (int kc = 0; kc < nchunks && ok; ++kc) {
+      const int st = kc % kStages;
+      if (kc >= kStages) ok = tc::mbar_wait(&p.empty[st], ((kc / kStages) - 1) & 1);
       if (!ok) break;
-      ++waited[buf];
-      for (int t = 0; s + t < kSlices; ++t) {
-        const int a = acc_of(s, t);
-        const uint32_t dcol = tmem + (uint32_t)a * NT;
-        for (int ks = 0; ks < KK / 16; ++ks) {
-          const uint64_t da = tc::smem_desc(sm.A[buf] + ks * 128, 128, sbo);
-          const uint64_t db = tc::smem_desc(sm.B + (long long)t * NT * KK + ks * 128, 128, sbo);
-          tc::mma_bf16(dcol, da, db, idesc, ((started >> a) & 1u) ? 1u : 0u);
+      tc::mbar_expect_tx(&p.full[st], (uint32_t)(kStageBytesA + kStageBytesB));
+      tc::bulk_g2s(p.A[st], gA + (long long)kc * chunk_elems(128), (uint32_t)kStageBytesA, &p.full[st]);
+      tc::bulk_g2s(p.B[st], gB + (long long)kc * chunk_elems(kNT), (uint32_t)kStageBytesB, &p.full[st]);
+    }
+    // no copy may still be in flight when the CTA ends: wait for the last loads
+    const int first = nchunks > kStages ? nchunks - kStages : 0;
+    for (int kc = first; kc < nchunks; ++kc)
+      if (!tc::mbar_wait(&p.full[kc % kStages], (kc / kStages) & 1)) ok = false;
+    if (!ok) atomicExch(err, 1);
+  } else if (warp == 1 && lane == 0) {  // MMA issuer
+    const uint32_t idesc = tc::idesc_bf16_f32(128, kNT);
+    unsigned started = 0u;
+    for (int kc = 0; kc < nchunks && ok; ++kc) {
+      const int st = kc % kStages;
+      ok = tc::mbar_wait(&p.full[st], (kc / kStages) & 1);
+      if (!ok) break;
+      tc::fence_after_sync();
+      for (int s = 0; s < kSlices; ++s) {
+        const uint64_t da = tc::smem_desc(p.A[st] + (long long)s * 128 * kKC, 128, kKC * 16);
+        for (int t = 0; s + t < kSlices; ++t) {
+          const int a = acc_of(s, t);
+          const uint64_t db = tc::smem_desc(p.B[st] + (long long)t * kNT * kKC, 128, kKC * 16);
+          tc::mma_bf16(tmem + (uint32_t)a * kNT, da, db, idesc, ((started >> a) & 1u) ? 1u : 0u);
           started |= 1u << a;
         }
       }
-      if (s + 2 < kSlices) {
-        // refill this buffer once the MMAs that read it have completed
-        tc::mma_commit(&sm.bar[2 + buf]);
-        ok = tc::mbar_wait(&sm.bar[2 + buf], (s >> 1) & 1);
-        if (!ok) break;
-        tc::mbar_expect_tx(&sm.bar[buf], abytes);
-        tc::bulk_g2s(sm.A[buf], gA + (s + 2) * a_slice_elems, abytes, &sm.bar[buf]);
-        ++issued[buf];
-      }
+      tc::mma_commit(&p.empty[st]);
     }
-    tc::mma_commit(&sm.bar[5]);
-    if (!ok) {
-      // drain copies still in flight (bounded) before the CTA gives up
-      atomicExch(err, 1);
-      if (!b_ok) tc::mbar_wait(&sm.bar[4], 0);
-      for (int b = 0; b < 2; ++b)
-        for (; waited[b] < issued[b]; ++waited[b]) tc::mbar_wait(&sm.bar[b], waited[b] & 1);
-    }
+    tc::mma_commit(p.done);
+    if (!ok) atomicExch(err, 3);
   }
-  __syncthreads();
-  const bool done = tc::mbar_wait(&sm.bar[5], 0);
-  if (!done && threadIdx.x == 0) atomicExch(err, 2);
+  __syncwarp();
+  const bool done = tc::mbar_wait(p.done, 0);
+  if (!done && lane == 0) atomicExch(err, 2);
   tc::fence_after_sync();
   return __syncthreads_and((done && ok) ? 1 : 0) != 0;
 }
 
-// Dynamic shared memory: at least 116 KB so that one CTA holds an SM (each
-// CTA takes all 512 TMEM columns; a second resident CTA would only stall in
-// tcgen05.alloc).
-inline size_t tc_smem_bytes(int KK, int NT) {
-  const size_t need = 2 * 128 * (size_t)KK * 2 + (size_t)kSlices * NT * KK * 2 + 1024 + 128;
-  return std::max<size_t>(need, 116 * 1024);
-}
-
-__device__ inline void tc_carve(char* base, int KK, int NT, TcSmem& sm, uint32_t*& tmem_slot) {
-  char* p = reinterpret_cast<char*>((reinterpret_cast<uintptr_t>(base) + 1023) & ~uintptr_t(1023));
-  sm.A[0] = reinterpret_cast<__nv_bfloat16*>(p);
-  sm.A[1] = sm.A[0] + 128 * KK;
-  sm.B = sm.A[1] + 128 * KK;
-  char* q = reinterpret_cast<char*>(sm.B + (long long)kSlices * NT * KK);
-  sm.bar = reinterpret_cast<uint64_t*>(q);
-  tmem_slot = reinterpret_cast<uint32_t*>(q + 8 * 8);
-}
-
-__device__ inline void tc_begin(TcSmem& sm, uint32_t* tmem_slot) {
+__device__ inline void tc_begin(TcPipe& p) {
   if (threadIdx.x == 0) {
-    for (int i = 0; i < 6; ++i) tc::mbar_init(&sm.bar[i], 1);
+    for (int i = 0; i < 2 * kStages + 1; ++i) tc::mbar_init(&p.full[i], 1);
     tc::fence_mbar_init();
   }
   __syncthreads();
-  if (threadIdx.x < 32) tc::tmem_alloc(tmem_slot, kTmemCols);
+  if (threadIdx.x < 32) tc::tmem_alloc(p.tmem_slot, kTmemCols);
   tc::fence_before_sync();
   __syncthreads();
   tc::fence_after_sync();
@@ -376,15 +481,14 @@ __device__ inline void tc_end(uint32_t tmem) {
   if (threadIdx.x < 32) tc::tmem_dealloc(tmem, kTmemCols);
 }
 
-// The kAccs accumulators of 16 columns starting at c0, for this thread's
+// The kAccs accumulators of 16 columns starting at c0 for this thread's
 // lane (the TMEM lane quadrant of its warp).
-template <int NT>
 __device__ inline void tc_read16(uint32_t tmem, int c0, float (*acc)[kAccs]) {
   const uint32_t lane_base = (uint32_t)((threadIdx.x >> 5) * 32) << 16;
   uint32_t r[16];
 #pragma unroll
   for (int k = 0; k < kAccs; ++k) {
-    tc::tmem_ld16(tmem + lane_base + (uint32_t)(k * NT + c0), r);
+    tc::tmem_ld16(tmem + lane_base + (uint32_t)(k * kNT + c0), r);
     tc::tmem_wait_ld();
 #pragma unroll
     for (int i = 0; i < 16; ++i) acc[i][k] = __uint_as_float(r[i]);
@@ -392,41 +496,40 @@ __device__ inline void tc_read16(uint32_t tmem, int c0, float (*acc)[kAccs]) {
 }
 
 // --------------------------------------------------------- synthesis GEMM
-// grid (m, latitude tile, data tile), 128 threads.  Writes F blocks.
-static __global__ void __launch_bounds__(128, 1) tc_synth_kernel(SplitDims dm, const long long* __restrict__ kcum,
+// grid (m, latitude tile, data tile), 128 threads.  Writes double-float F
+// blocks (float4 per complex value).
+static __global__ void __launch_bounds__(128, 2) tc_synth_kernel(SplitDims dm, const long long* __restrict__ kcum,
                                                                  const __nv_bfloat16* __restrict__ psyn,
                                                                  const int* __restrict__ esyn,
                                                                  const __nv_bfloat16* __restrict__ dsyn,
                                                                  const int* __restrict__ ecol, int nf, int nblk,
-                                                                 double2* __restrict__ F, int* err) {
+                                                                 float4* __restrict__ F, int* err) {
   extern __shared__ char smem_raw[];
   const int m = blockIdx.x, mt = blockIdx.y, tile = blockIdx.z;
   const int L = dm.L, Kp = kpad(L + 1 - m);
-  TcSmem sm;
-  uint32_t* tslot;
-  tc_carve(smem_raw, Kp, kNT, sm, tslot);
-  tc_begin(sm, tslot);
-  const uint32_t tmem = *tslot;
-  const __nv_bfloat16* gA = psyn + kcum[m] * (long long)dm.Mt * kSlices * 128 + (long long)mt * kSlices * 128 * Kp;
-  const __nv_bfloat16* gB = dsyn + dsyn_block(kcum, dm, m, tile, 0);
-  const bool ok = tc_levels<kNT>(sm, gA, 128LL * Kp, gB, (long long)kNT * Kp, Kp, tmem, err);
+  TcPipe pp;
+  tc_carve(smem_raw, pp);
+  tc_begin(pp);
+  const uint32_t tmem = *pp.tmem_slot;
+  const bool ok = tc_mainloop(pp, psyn + psyn_tile(kcum, dm.Mt, m, mt, Kp), dsyn + dsyn_tile(kcum, dm, m, tile),
+                              Kp / kKC, tmem, err);
   if (ok) {
     const int j = mt * 128 + threadIdx.x;
     const int Ej = j < dm.nlat ? esyn[m * dm.Mt * 128 + j] : 0;
     const int* ec = ecol + (long long)m * dm.ntiles * kNT + tile * kNT;
     for (int c0 = 0; c0 < kNT; c0 += 16) {
       float acc[16][kAccs];
-      tc_read16<kNT>(tmem, c0, acc);
+      tc_read16(tmem, c0, acc);
       if (j < dm.nlat) {
 #pragma unroll
         for (int i = 0; i < 16; i += 2) {
           const int n = tile * kNT + c0 + i;  // even: real part, n + 1: imaginary part
           if (n >= dm.ncol) break;
-          const double re = scaled_to_double(combine_levels(acc[i]), Ej + ec[c0 + i] - kOut);
-          const double im = scaled_to_double(combine_levels(acc[i + 1]), Ej + ec[c0 + i + 1] - kOut);
+          const df re = scaled_to_df(combine_levels(acc[i]), Ej + ec[c0 + i] - kOut);
+          const df im = scaled_to_df(combine_levels(acc[i + 1]), Ej + ec[c0 + i + 1] - kOut);
           const int bf = n >> 1;
           const int b = bf / nf, f = bf - b * nf;
-          F[(((long long)b * dm.nlat + j) * nblk + f) * (L + 1) + m] = make_double2(re, im);
+          F[(((long long)b * dm.nlat + j) * nblk + f) * (L + 1) + m] = make_float4(re.hi, re.lo, im.hi, im.lo);
         }
       }
     }
@@ -437,7 +540,7 @@ static __global__ void __launch_bounds__(128, 1) tc_synth_kernel(SplitDims dm, c
 // --------------------------------------------------------- analysis GEMM
 // grid (m, data tile), 128 threads; lane = degree offset l - m.
 template <class Epi>
-__global__ void __launch_bounds__(128, 1) tc_anal_kernel(SplitDims dm, const __nv_bfloat16* __restrict__ pana,
+__global__ void __launch_bounds__(128, 2) tc_anal_kernel(SplitDims dm, const __nv_bfloat16* __restrict__ pana,
                                                          const int* __restrict__ eana,
                                                          const __nv_bfloat16* __restrict__ dana,
                                                          const int* __restrict__ ecol, int batch, Epi epi, int* err) {
@@ -445,26 +548,23 @@ __global__ void __launch_bounds__(128, 1) tc_anal_kernel(SplitDims dm, const __n
   static_assert(16 % (2 * NF) == 0, "a 16-column chunk must hold whole members");
   extern __shared__ char smem_raw[];
   const int m = blockIdx.x, tile = blockIdx.y;
-  const int L = dm.L, NK = dm.NK, K = L + 1 - m;
-  TcSmem sm;
-  uint32_t* tslot;
-  tc_carve(smem_raw, NK, kNTa, sm, tslot);
-  tc_begin(sm, tslot);
-  const uint32_t tmem = *tslot;
-  const __nv_bfloat16* gA = pana + (long long)m * kSlices * 128 * NK;
-  const __nv_bfloat16* gB = dana + dana_block(dm, m, tile, 0);
-  const bool ok = tc_levels<kNTa>(sm, gA, 128LL * NK, gB, (long long)kNTa * NK, NK, tmem, err);
+  const int L = dm.L, K = L + 1 - m;
+  TcPipe pp;
+  tc_carve(smem_raw, pp);
+  tc_begin(pp);
+  const uint32_t tmem = *pp.tmem_slot;
+  const bool ok = tc_mainloop(pp, pana + pana_tile(dm.NK, m), dana + dana_tile(dm, m, tile), dm.NK / kKC, tmem, err);
   const int t = threadIdx.x;
   if (ok) {
     const int Et = eana[m * 128 + t];
-    const int* ec = ecol + (long long)m * dm.ntiles * kNTa + tile * kNTa;
-    for (int c0 = 0; c0 < kNTa; c0 += 16) {
+    const int* ec = ecol + (long long)m * dm.ntiles * kNT + tile * kNT;
+    for (int c0 = 0; c0 < kNT; c0 += 16) {
       float acc[16][kAccs];
-      tc_read16<kNTa>(tmem, c0, acc);
+      tc_read16(tmem, c0, acc);
       if (t < K) {
 #pragma unroll
         for (int i = 0; i < 16; i += 2 * NF) {
-          const int n = tile * kNTa + c0 + i;
+          const int n = tile * kNT + c0 + i;
           const int b = n / (2 * NF);
           if (b >= batch) break;
           double2 a[NF];
@@ -478,28 +578,28 @@ __global__ void __launch_bounds__(128, 1) tc_anal_kernel(SplitDims dm, const __n
       }
     }
     // slots l < m of column m for this tile's members
-    const int mb0 = tile * kNTa / (2 * NF), mb1 = min(batch, (tile + 1) * kNTa / (2 * NF));
+    const int mb0 = tile * kNT / (2 * NF), mb1 = min(batch, (tile + 1) * kNT / (2 * NF));
     for (int idx = threadIdx.x; idx < (mb1 - mb0) * m; idx += blockDim.x) epi.zero(mb0 + idx / m, idx % m, m);
   }
   tc_end(tmem);
 }
 
 // ------------------------------------------------------------ launchers
-inline SplitDims split_dims(const aeolus_plan_impl* p, int ncol, int nt) {
+inline SplitDims split_dims(const aeolus_plan_impl* p, int ncol) {
   const SplitTables* t = p->split;
-  return SplitDims{t->L, t->nlat, t->nh, t->NK, t->Mt, ncol, (ncol + nt - 1) / nt};
+  return SplitDims{t->L, t->nlat, t->nh, t->NK, t->Mt, ncol, (ncol + kNT - 1) / kNT};
 }
 
 inline size_t split_synth_bytes(const aeolus_plan_impl* p, int nf, int batch) {
-  const SplitDims d = split_dims(p, batch * nf * 2, kNT);
+  const SplitDims d = split_dims(p, batch * nf * 2);
   return align256((size_t)p->split->h_kcum[d.L + 1] * d.ntiles * kSlices * kNT * 2) +
          align256((size_t)(d.L + 1) * d.ntiles * kNT * 4);
 }
 
 inline size_t split_anal_bytes(const aeolus_plan_impl* p, int nf, int batch) {
-  const SplitDims d = split_dims(p, batch * nf * 2, kNTa);
-  return align256((size_t)(d.L + 1) * d.ntiles * kSlices * kNTa * d.NK * 2) +
-         align256((size_t)(d.L + 1) * d.ntiles * kNTa * 4);
+  const SplitDims d = split_dims(p, batch * nf * 2);
+  return align256((size_t)(d.L + 1) * d.ntiles * kSlices * kNT * d.NK * 2) +
+         align256((size_t)(d.L + 1) * d.ntiles * kNT * 4);
 }
 
 inline int slice_members(int nf, int K) {
@@ -511,7 +611,7 @@ template <class Derive>
 int launch_split_synth(const aeolus_plan_impl* p, const Derive& d, double2* FG, int nblk, int batch, void* scratch,
                        cudaStream_t st) {
   constexpr int NF = Derive::NF;
-  const SplitDims dm = split_dims(p, batch * NF * 2, kNT);
+  const SplitDims dm = split_dims(p, batch * NF * 2);
   char* w = static_cast<char*>(scratch);
   __nv_bfloat16* dsyn = reinterpret_cast<__nv_bfloat16*>(w);
   w += align256((size_t)p->split->h_kcum[dm.L + 1] * dm.ntiles * kSlices * kNT * 2);
@@ -526,12 +626,12 @@ int launch_split_synth(const aeolus_plan_impl* p, const Derive& d, double2* FG, 
     k1<<<dim3(dm.L + 1, (batch + mb - 1) / mb), 256, sm1, st>>>(dm, p->split->kcum, batch, mb, d, dsyn, ecol);
     AE_LAUNCH("split_synth_slice_kernel");
   }
-  const size_t sm2 = tc_smem_bytes(kpad(dm.L + 1), kNT);
+  const size_t sm2 = tc_smem_bytes();
   if ((s = allow_smem(tc_synth_kernel, sm2))) return s;
   ProfScope prof("tc_synth_bf16x6", st);
   tc_synth_kernel<<<dim3(dm.L + 1, dm.Mt, dm.ntiles), 128, sm2, st>>>(dm, p->split->kcum, p->split->psyn,
-                                                                      p->split->esyn, dsyn, ecol, NF, nblk, FG,
-                                                                      p->split->err);
+                                                                      p->split->esyn, dsyn, ecol, NF, nblk,
+                                                                      reinterpret_cast<float4*>(FG), p->split->err);
   AE_LAUNCH("tc_synth_kernel");
   return AEOLUS_OK;
 }
@@ -540,10 +640,10 @@ template <class Epi>
 int launch_split_anal(const aeolus_plan_impl* p, const Epi& e, const double2* FG, int nblk, int batch, void* scratch,
                       cudaStream_t st) {
   constexpr int NF = Epi::NF;
-  const SplitDims dm = split_dims(p, batch * NF * 2, kNTa);
+  const SplitDims dm = split_dims(p, batch * NF * 2);
   char* w = static_cast<char*>(scratch);
   __nv_bfloat16* dana = reinterpret_cast<__nv_bfloat16*>(w);
-  w += align256((size_t)(dm.L + 1) * dm.ntiles * kSlices * kNTa * dm.NK * 2);
+  w += align256((size_t)(dm.L + 1) * dm.ntiles * kSlices * kNT * dm.NK * 2);
   int* ecol = reinterpret_cast<int*>(w);
   const int mb = slice_members(NF, dm.nlat);
   const size_t sm1 = (size_t)mb * NF * 2 * dm.nlat * 8;
@@ -552,10 +652,11 @@ int launch_split_anal(const aeolus_plan_impl* p, const Epi& e, const double2* FG
   if (s) return s;
   {
     ProfScope prof("split_anal_slice", st);
-    k1<<<dim3(dm.L + 1, (batch + mb - 1) / mb), 256, sm1, st>>>(dm, batch, mb, nblk, FG, dana, ecol);
+    k1<<<dim3(dm.L + 1, (batch + mb - 1) / mb), 256, sm1, st>>>(dm, batch, mb, nblk,
+                                                                 reinterpret_cast<const float4*>(FG), dana, ecol);
     AE_LAUNCH("split_anal_slice_kernel");
   }
-  const size_t sm2 = tc_smem_bytes(dm.NK, kNTa);
+  const size_t sm2 = tc_smem_bytes();
   auto k2 = tc_anal_kernel<Epi>;
   if ((s = allow_smem(k2, sm2))) return s;
   ProfScope prof("tc_anal_bf16x6", st);
