@@ -40,6 +40,22 @@ struct Spec {  // shared spectral context
     const double mr = (double)m / R;
     return make_double2(-mr * v.y, mr * v.x);
   }
+  // (x q)_lm, x = cos(colatitude) = sin(latitude):
+  //   x Y_lm = a_lm Y_{l+1,m} + b_lm Y_{l-1,m},
+  //   a_lm = sqrt(((l+1)^2 - m^2)/((2l+1)(2l+3))), b_lm = sqrt((l^2 - m^2)/((2l-1)(2l+1)))
+  // (C+_lm = l a_lm and C-_lm = -(l+1) b_lm of the sin(theta) d/dtheta coupling).
+  __device__ double2 xmul(double2 lo, double2 hi, int l, int m) const {
+    double2 g = make_double2(0.0, 0.0);
+    if (l >= 1 && l - 1 >= m) {
+      const double lb = l - 1.0;
+      g = cadd(g, cscale(sqrt(((lb + 1.0) * (lb + 1.0) - (double)m * m) / ((2.0 * lb + 1.0) * (2.0 * lb + 3.0))), lo));
+    }
+    if (l + 1 <= L) {
+      const double lb = l + 1.0;
+      g = cadd(g, cscale(sqrt((lb * lb - (double)m * m) / ((2.0 * lb - 1.0) * (2.0 * lb + 1.0))), hi));
+    }
+    return g;
+  }
   // sin(theta) d/dtheta coupling of a column given its values at l-1, l+1
   __device__ double2 snt(double2 lo, double2 hi, int l, int m) const {
     double2 g = make_double2(0.0, 0.0);
@@ -232,7 +248,7 @@ struct SweDerive {
   static constexpr int NF = 9;
   Spec s;
   const double2* state;  // [b][3][L+1][L+1]
-  double f10;
+  double f10;            // 0 when the Coriolis terms are taken spectrally (SweEpi::coriolis)
   __device__ void column(int b, int l, int m, double2* v) const {
     const int L = s.L;
     const long n2 = (long)(L + 1) * (L + 1);
@@ -269,7 +285,7 @@ struct SweDerive {
 struct SwePw {
   static constexpr int NIN = 9, NOUT = 4;
   static constexpr bool kIdentity = false;
-  double f10;   // eta = zeta + f10 * fgrid
+  double f10;   // eta = zeta + f10 * fgrid (0: products of the relative vorticity only)
   double phi0;  // positivity check of Phi0 + phi
   __device__ unsigned operator()(double c, double fg, const double* in, double* out) const {
     const double u = in[0] / c, v = in[1] / c;
@@ -305,19 +321,46 @@ struct SwePw {
   }
 };
 
+// Spectral epilogue of the SWE tendency.  With `coriolis` set (split-
+// precision path) the pointwise products carry only the relative vorticity
+// and the planetary-vorticity terms are added here exactly:
+//   eta u products with eta = zeta + f, f = 2 Omega x, f_snt = -(2 Omega/a) cos^2(lat):
+//   zeta_dot += -(2 Omega/a) V - 2 Omega (x delta),  curl += 2 Omega (x zeta) - (2 Omega/a) U
+// with U = u cos(lat), V = v cos(lat) the Helmholtz fields of the stage state.
+// The Gauss product quadrature is exact for these degree-(L+1) products, so
+// this equals the analysed product up to rounding, while the terms that pass
+// through the split contraction shrink ~10x (|zeta| << |f|).
 struct SweEpi {
   static constexpr int NF = 4;
   Spec s;
   const double2* state;  // stage input [b][3][L+1][L+1]
   double phi0, nu4;
   Rk4 rk;
-  __device__ void finish(int b, int l, int m, const double2* an) const {
+  double two_omega;      // > 0: add the Coriolis terms spectrally
+  __device__ void finish(int b, int l, int m, const double2* an_in) const {
     const int L = s.L;
     const int cut = (2 * L) / 3;
     const long n2 = (long)(L + 1) * (L + 1);
     const long base = (long)b * 3 * n2 + (long)l * (L + 1) + m;
     const bool tr = l > cut || m > cut;
     const double2 z0 = make_double2(0.0, 0.0);
+    double2 an[4] = {an_in[0], an_in[1], an_in[2], an_in[3]};
+    if (two_omega > 0.0 && !tr) {
+      const double2* z = state + (long)b * 3 * n2;
+      const double2* d = z + n2;
+      const bool lo = l >= 1, hi = l + 1 <= L;
+      const double ir = 1.0 / s.R;
+      const double2 psi = s.invlap0(z, l, m), chi = s.invlap0(d, l, m);
+      const double2 psi_lo = lo ? s.invlap0(z, l - 1, m) : z0, psi_hi = hi ? s.invlap0(z, l + 1, m) : z0;
+      const double2 chi_lo = lo ? s.invlap0(d, l - 1, m) : z0, chi_hi = hi ? s.invlap0(d, l + 1, m) : z0;
+      const double2 U = cadd(cscale(ir, s.snt(psi_lo, psi_hi, l, m)), s.dlam(chi, m));
+      const double2 V = csub(s.dlam(psi, m), cscale(ir, s.snt(chi_lo, chi_hi, l, m)));
+      const double2 xz = s.xmul(lo ? s.at(z, l - 1, m) : z0, hi ? s.at(z, l + 1, m) : z0, l, m);
+      const double2 xd = s.xmul(lo ? s.at(d, l - 1, m) : z0, hi ? s.at(d, l + 1, m) : z0, l, m);
+      const double wr = two_omega * ir;
+      an[0] = csub(an[0], cadd(cscale(wr, V), cscale(two_omega, xd)));
+      an[1] = cadd(an[1], csub(cscale(two_omega, xz), cscale(wr, U)));
+    }
     const double2 a0 = tr ? z0 : an[0], a1 = tr ? z0 : an[1], a2 = tr ? z0 : an[2], a3 = tr ? z0 : an[3];
     const double2 zs = state[base], ds = state[base + n2], ps = state[base + 2 * n2];
     const double lap = s.lap(l);
@@ -720,10 +763,12 @@ extern "C" int aeolus_swe_tendency(aeolus_plan plan, const aeolus_swe_params* p,
   const Spec sp = make_spec(plan, p->radius);
   const double f10 = 2.0 * p->omega * kSqrt4PiOver3;
   const double phi0 = p->gravity * p->mean_depth;
-  SweDerive d{sp, reinterpret_cast<const double2*>(state), f10};
-  SwePw pw{f10, phi0};
+  const bool spec_cor = plan->precision == AEOLUS_PREC_SPLIT_BF16;
+  const double fp = spec_cor ? 0.0 : f10;
+  SweDerive d{sp, reinterpret_cast<const double2*>(state), fp};
+  SwePw pw{fp, phi0};
   Rk4 rk{0, 0.0, nullptr, nullptr, nullptr, reinterpret_cast<double2*>(tend)};
-  SweEpi e{sp, reinterpret_cast<const double2*>(state), phi0, p->nu4, rk};
+  SweEpi e{sp, reinterpret_cast<const double2*>(state), phi0, p->nu4, rk, spec_cor ? 2.0 * p->omega : 0.0};
   return run_full_chain(plan, d, pw, e, batch, work, nullptr, static_cast<cudaStream_t>(stream));
 }
 
@@ -771,13 +816,15 @@ extern "C" int aeolus_swe_rk4(aeolus_plan plan, const aeolus_swe_params* p, doub
   w += align256(state_bytes(plan, 3, batch));
   double2* acc = reinterpret_cast<double2*>(w);
   double2* y0 = reinterpret_cast<double2*>(state);
-  SwePw pw{f10, phi0};
+  const bool spec_cor = plan->precision == AEOLUS_PREC_SPLIT_BF16;
+  const double fp = spec_cor ? 0.0 : f10;
+  SwePw pw{fp, phi0};
   for (int it = 0; it < nsteps; ++it)
     for (int stage = 1; stage <= 4; ++stage) {
       const double2* in = stage == 1 ? y0 : ystage;
-      SweDerive d{sp, in, f10};
+      SweDerive d{sp, in, fp};
       Rk4 rk{stage, dt, y0, ystage, acc, nullptr};
-      SweEpi e{sp, in, phi0, p->nu4, rk};
+      SweEpi e{sp, in, phi0, p->nu4, rk, spec_cor ? 2.0 * p->omega : 0.0};
       if ((s = run_full_chain(plan, d, pw, e, batch, chain, status, st))) return s;
     }
   return AEOLUS_OK;

@@ -1,5 +1,9 @@
 // Longitude stage in double-float arithmetic (split-precision path).
 //
+// Butterflies and twiddle rotations use the Dekker-style df addition (error
+// relative to the operands, the bound FFT backward stability rests on); the
+// real-FFT pre/post-processing and the products use the accurate one.
+//
 // Same structure as row_kernel (rows.cuh): per (latitude row, member) the
 // order spectra go through a half-length complex Stockham FFT (radix 2/3/4/5)
 // to grid values, the pointwise products are formed, and a forward FFT
@@ -20,36 +24,36 @@ __device__ __forceinline__ void butterfly_df(cdf* v, int r, const DfConst& k) {
   const float sg = INV ? 1.0f : -1.0f;
   if (r == 2) {
     const cdf a = v[0], b = v[1];
-    v[0] = cdf_add(a, b);
-    v[1] = cdf_sub(a, b);
+    v[0] = cdf_addf(a, b);
+    v[1] = cdf_subf(a, b);
   } else if (r == 4) {
-    const cdf s02 = cdf_add(v[0], v[2]), d02 = cdf_sub(v[0], v[2]);
-    const cdf s13 = cdf_add(v[1], v[3]), d13 = cdf_sub(v[1], v[3]);
+    const cdf s02 = cdf_addf(v[0], v[2]), d02 = cdf_subf(v[0], v[2]);
+    const cdf s13 = cdf_addf(v[1], v[3]), d13 = cdf_subf(v[1], v[3]);
     const cdf id13 = cdf_scale2(sg, cdf_i(d13));
-    v[0] = cdf_add(s02, s13);
-    v[2] = cdf_sub(s02, s13);
-    v[1] = cdf_add(d02, id13);
-    v[3] = cdf_sub(d02, id13);
+    v[0] = cdf_addf(s02, s13);
+    v[2] = cdf_subf(s02, s13);
+    v[1] = cdf_addf(d02, id13);
+    v[3] = cdf_subf(d02, id13);
   } else if (r == 3) {
-    const cdf s = cdf_add(v[1], v[2]), d = cdf_sub(v[1], v[2]);
-    const cdf t = cdf_sub(v[0], cdf_scale2(0.5f, s));
+    const cdf s = cdf_addf(v[1], v[2]), d = cdf_subf(v[1], v[2]);
+    const cdf t = cdf_subf(v[0], cdf_scale2(0.5f, s));
     const cdf id = cdf_scale(k.h3, cdf_scale2(sg, cdf_i(d)));
-    v[0] = cdf_add(v[0], s);
-    v[1] = cdf_add(t, id);
-    v[2] = cdf_sub(t, id);
+    v[0] = cdf_addf(v[0], s);
+    v[1] = cdf_addf(t, id);
+    v[2] = cdf_subf(t, id);
   } else {  // r == 5
-    const cdf a1 = cdf_add(v[1], v[4]), a2 = cdf_add(v[2], v[3]);
-    const cdf b1 = cdf_sub(v[1], v[4]), b2 = cdf_sub(v[2], v[3]);
-    const cdf t1 = cdf_add(v[0], cdf_add(cdf_scale(k.c1, a1), cdf_scale(k.c2, a2)));
-    const cdf t2 = cdf_add(v[0], cdf_add(cdf_scale(k.c2, a1), cdf_scale(k.c1, a2)));
-    const cdf u1 = cdf_add(cdf_scale(k.s1, b1), cdf_scale(k.s2, b2));
-    const cdf u2 = cdf_sub(cdf_scale(k.s2, b1), cdf_scale(k.s1, b2));
+    const cdf a1 = cdf_addf(v[1], v[4]), a2 = cdf_addf(v[2], v[3]);
+    const cdf b1 = cdf_subf(v[1], v[4]), b2 = cdf_subf(v[2], v[3]);
+    const cdf t1 = cdf_addf(v[0], cdf_addf(cdf_scale(k.c1, a1), cdf_scale(k.c2, a2)));
+    const cdf t2 = cdf_addf(v[0], cdf_addf(cdf_scale(k.c2, a1), cdf_scale(k.c1, a2)));
+    const cdf u1 = cdf_addf(cdf_scale(k.s1, b1), cdf_scale(k.s2, b2));
+    const cdf u2 = cdf_subf(cdf_scale(k.s2, b1), cdf_scale(k.s1, b2));
     const cdf iu1 = cdf_scale2(sg, cdf_i(u1)), iu2 = cdf_scale2(sg, cdf_i(u2));
-    v[0] = cdf_add(v[0], cdf_add(a1, a2));
-    v[1] = cdf_add(t1, iu1);
-    v[4] = cdf_sub(t1, iu1);
-    v[2] = cdf_add(t2, iu2);
-    v[3] = cdf_sub(t2, iu2);
+    v[0] = cdf_addf(v[0], cdf_addf(a1, a2));
+    v[1] = cdf_addf(t1, iu1);
+    v[4] = cdf_subf(t1, iu1);
+    v[2] = cdf_addf(t2, iu2);
+    v[3] = cdf_subf(t2, iu2);
   }
 }
 
@@ -72,7 +76,7 @@ __device__ cdf* fft_run_df(cdf* src, cdf* dst, int nf, const FftInfo& fi, const 
         for (int t = 1; t < r; ++t) {
           cdf w = cdf_from_f4(__ldg(&tw[2 * (k * t * stride)]));
           if (INV) w = cdf_conj(w);
-          v[t] = cdf_mul(v[t], w);
+          v[t] = cdf_mulf(v[t], w);
         }
       }
       butterfly_df<INV>(v, r, kc);

@@ -202,6 +202,21 @@ __device__ inline void digits_from_fixed(long long X, float* d) {
   d[0] = (float)X;
 }
 
+// Level recombination on the f32 pipe: every accumulator holds an exact
+// integer below 2^24, so acc_k 256^(5-k) is an exact float; their double-
+// float sum (smallest first, error-free two-sums) is T to ~2^-48, and the
+// power-of-two scaling 2^e is applied in two exact steps.
+__device__ inline float pow2f(int p) { return __int_as_float((p + 127) << 23); }  // p in [-126, 127]
+
+__device__ inline df levels_to_df(const float* acc, int e) {
+  df s = two_sum(acc[kLevels], acc[kLevels - 1]);
+#pragma unroll
+  for (int k = kLevels - 2; k >= 0; --k) s = df_add(s, df{acc[k] * pow2f(8 * (kLevels - 1 - k)), 0.f});
+  // s * 2^e, e = e1 + e2 with both factors normal floats
+  const int e1 = max(-126, min(127, e)), e2 = max(-126, min(127, e - e1));
+  return df{s.hi * pow2f(e1) * pow2f(e2), s.lo * pow2f(e1) * pow2f(e2)};
+}
+
 // Level recombination: T = sum_k I_k 256^(5-k), k = 0..5 <-> s+t = 2..7,
 // the top level held in two accumulators.  |T| < 2^62.
 __device__ inline long long combine_levels(const float* acc) {
@@ -525,8 +540,8 @@ static __global__ void __launch_bounds__(128, 2) tc_synth_kernel(SplitDims dm, c
         for (int i = 0; i < 16; i += 2) {
           const int n = tile * kNT + c0 + i;  // even: real part, n + 1: imaginary part
           if (n >= dm.ncol) break;
-          const df re = scaled_to_df(combine_levels(acc[i]), Ej + ec[c0 + i] - kOut);
-          const df im = scaled_to_df(combine_levels(acc[i + 1]), Ej + ec[c0 + i + 1] - kOut);
+          const df re = levels_to_df(acc[i], Ej + ec[c0 + i] - kOut);
+          const df im = levels_to_df(acc[i + 1], Ej + ec[c0 + i + 1] - kOut);
           const int bf = n >> 1;
           const int b = bf / nf, f = bf - b * nf;
           F[(((long long)b * dm.nlat + j) * nblk + f) * (L + 1) + m] = make_float4(re.hi, re.lo, im.hi, im.lo);
@@ -572,6 +587,7 @@ __global__ void __launch_bounds__(128, 2) tc_anal_kernel(SplitDims dm, const __n
           for (int f = 0; f < NF; ++f) {
             a[f].x = scaled_to_double(combine_levels(acc[i + 2 * f]), Et + ec[c0 + i + 2 * f] - kOut);
             a[f].y = scaled_to_double(combine_levels(acc[i + 2 * f + 1]), Et + ec[c0 + i + 2 * f + 1] - kOut);
+            // (analysis output feeds the FP64 epilogue: exact 64-bit recombination)
           }
           epi.finish(b, m + t, m, a);
         }
