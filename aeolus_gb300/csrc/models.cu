@@ -665,7 +665,7 @@ size_t op_bytes(const aeolus_plan_impl* p, int op, int batch) {
     case AEOLUS_OP_BVE_RK4:
       return full_chain_bytes<4, 1>(p, batch) + 2 * align256(state_bytes(p, 1, batch));
     case AEOLUS_OP_SWE_RK4:
-      return full_chain_bytes<9, 4>(p, batch) + 2 * align256(state_bytes(p, 3, batch));
+      return full_chain_bytes<9, 4>(p, batch) + 3 * align256(state_bytes(p, 3, batch));
     case AEOLUS_OP_SWE_VALIDATE:
       return synth_chain_bytes<1, 1>(p, batch) + align256((size_t)batch * p->npoints * 8) +
              align256((size_t)batch * sizeof(double2));
@@ -812,7 +812,13 @@ extern "C" int aeolus_swe_rk4(aeolus_plan plan, const aeolus_swe_params* p, doub
   char* w = static_cast<char*>(work);
   void* chain = w;
   w += full_chain_bytes<9, 4>(plan, batch);
-  double2* ystage = reinterpret_cast<double2*>(w);
+  // Two stage buffers in turn: the epilogue of a stage reads neighbouring
+  // degrees of its input (spectral Coriolis terms) while writing the next
+  // stage's input, so the two must not alias.
+  double2* stage_buf[2];
+  stage_buf[0] = reinterpret_cast<double2*>(w);
+  w += align256(state_bytes(plan, 3, batch));
+  stage_buf[1] = reinterpret_cast<double2*>(w);
   w += align256(state_bytes(plan, 3, batch));
   double2* acc = reinterpret_cast<double2*>(w);
   double2* y0 = reinterpret_cast<double2*>(state);
@@ -821,9 +827,10 @@ extern "C" int aeolus_swe_rk4(aeolus_plan plan, const aeolus_swe_params* p, doub
   SwePw pw{fp, phi0};
   for (int it = 0; it < nsteps; ++it)
     for (int stage = 1; stage <= 4; ++stage) {
-      const double2* in = stage == 1 ? y0 : ystage;
+      const double2* in = stage == 1 ? y0 : stage_buf[stage & 1];        // 2 -> buf0, 3 -> buf1, 4 -> buf0
+      double2* next = stage_buf[(stage + 1) & 1];                        // 1 -> buf0, 2 -> buf1, 3 -> buf0
       SweDerive d{sp, in, fp};
-      Rk4 rk{stage, dt, y0, ystage, acc, nullptr};
+      Rk4 rk{stage, dt, y0, next, acc, nullptr};
       SweEpi e{sp, in, phi0, p->nu4, rk, spec_cor ? 2.0 * p->omega : 0.0};
       if ((s = run_full_chain(plan, d, pw, e, batch, chain, status, st))) return s;
     }
