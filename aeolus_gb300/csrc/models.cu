@@ -45,15 +45,11 @@ struct Spec {  // shared spectral context
   //   a_lm = sqrt(((l+1)^2 - m^2)/((2l+1)(2l+3))), b_lm = sqrt((l^2 - m^2)/((2l-1)(2l+1)))
   // (C+_lm = l a_lm and C-_lm = -(l+1) b_lm of the sin(theta) d/dtheta coupling).
   __device__ double2 xmul(double2 lo, double2 hi, int l, int m) const {
+    // a_{l-1,m} = C+_{l-1,m} / (l-1),  b_{l+1,m} = -C-_{l+1,m} / (l+2)
     double2 g = make_double2(0.0, 0.0);
-    if (l >= 1 && l - 1 >= m) {
-      const double lb = l - 1.0;
-      g = cadd(g, cscale(sqrt(((lb + 1.0) * (lb + 1.0) - (double)m * m) / ((2.0 * lb + 1.0) * (2.0 * lb + 3.0))), lo));
-    }
-    if (l + 1 <= L) {
-      const double lb = l + 1.0;
-      g = cadd(g, cscale(sqrt((lb * lb - (double)m * m) / ((2.0 * lb - 1.0) * (2.0 * lb + 1.0))), hi));
-    }
+    if (l >= 2 && l - 1 >= m) g = cadd(g, cscale(cplus[(long)(l - 1) * (L + 1) + m] / (l - 1.0), lo));
+    if (l == 1 && m == 0) g = cadd(g, cscale(0.57735026918962576451, lo));  // a_00 = 1/sqrt(3)
+    if (l + 1 <= L) g = cadd(g, cscale(-cminus[(long)(l + 1) * (L + 1) + m] / (l + 2.0), hi));
     return g;
   }
   // sin(theta) d/dtheta coupling of a column given its values at l-1, l+1

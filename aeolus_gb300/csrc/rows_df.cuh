@@ -1,8 +1,7 @@
 // Longitude stage in double-float arithmetic (split-precision path).
 //
-// Butterflies and twiddle rotations use the Dekker-style df addition (error
-// relative to the operands, the bound FFT backward stability rests on); the
-// real-FFT pre/post-processing and the products use the accurate one.
+// All additions use the Dekker-style df addition (error relative to the
+// operands -- the normwise bound that FFT backward stability rests on).
 //
 // Same structure as row_kernel (rows.cuh): per (latitude row, member) the
 // order spectra go through a half-length complex Stockham FFT (radix 2/3/4/5)
@@ -118,10 +117,10 @@ __global__ void __launch_bounds__(256) row_kernel_df(RowArgs a, Pw pw, const flo
         if (q == 0) hq.im = df{0.f, 0.f};
         const int qn = n - q;
         const cdf hn = (q > 0 && qn <= L) ? cdf_from_f4(Ff[qn]) : cdf_zero();
-        const cdf A = cdf_add(hq, cdf_conj(hn));
-        const cdf B = cdf_sub(hq, cdf_conj(hn));
+        const cdf A = cdf_addf(hq, cdf_conj(hn));
+        const cdf B = cdf_subf(hq, cdf_conj(hn));
         const cdf e = cdf_conj(cdf_from_f4(__ldg(&twdf[q])));
-        buf0[idx] = cdf_add(A, cdf_i(cdf_mul(e, B)));
+        buf0[idx] = cdf_addf(A, cdf_i(cdf_mulf(e, B)));
       }
       __syncthreads();
       xin = reinterpret_cast<df*>(fft_run_df<true>(buf0, buf1, NIN, a.fft, twdf, kc));
@@ -137,9 +136,9 @@ __global__ void __launch_bounds__(256) row_kernel_df(RowArgs a, Pw pw, const flo
           if (e >= N) e -= N;
           const cdf w = cdf_from_f4(__ldg(&twdf[e]));
           const cdf F = cdf_from_f4(Ff[m]);
-          acc = df_add(acc, df_add(df_mul(F.re, w.re), df_mul(F.im, w.im)));
+          acc = df_add_fast(acc, df_add_fast(df_mul(F.re, w.re), df_mul(F.im, w.im)));
         }
-        x0[(long)f * 2 * n + k] = df_add(df{Ff[0].x, Ff[0].y}, df_scale2(acc, 2.0f));
+        x0[(long)f * 2 * n + k] = df_add_fast(df{Ff[0].x, Ff[0].y}, df_scale2(acc, 2.0f));
       }
       __syncthreads();
     }
@@ -187,10 +186,10 @@ __global__ void __launch_bounds__(256) row_kernel_df(RowArgs a, Pw pw, const flo
         const cdf* Zf = Z + (long)f * n;
         const cdf zq = Zf[q];
         const cdf zn = cdf_conj(Zf[q == 0 ? 0 : n - q]);
-        const cdf E = cdf_scale2(0.5f, cdf_add(zq, zn));
-        const cdf D = cdf_sub(zq, zn);
+        const cdf E = cdf_scale2(0.5f, cdf_addf(zq, zn));
+        const cdf D = cdf_subf(zq, zn);
         const cdf O = cdf{df_scale2(D.im, 0.5f), df_scale2(D.re, -0.5f)};  // -(i/2) D
-        const cdf R = cdf_scale(wj, cdf_add(E, cdf_mul(cdf_from_f4(__ldg(&twdf[q])), O)));
+        const cdf R = cdf_scale(wj, cdf_addf(E, cdf_mulf(cdf_from_f4(__ldg(&twdf[q])), O)));
         block[(long)f * ldm + q] = make_float4(R.re.hi, R.re.lo, R.im.hi, R.im.lo);
       }
     } else {
@@ -201,8 +200,8 @@ __global__ void __launch_bounds__(256) row_kernel_df(RowArgs a, Pw pw, const flo
         int e = 0;
         for (int k = 0; k < N; ++k) {
           const cdf w = cdf_from_f4(__ldg(&twdf[e]));
-          sr = df_add(sr, df_mul(x[k], w.re));
-          si = df_add(si, df_mul(x[k], w.im));
+          sr = df_add_fast(sr, df_mul(x[k], w.re));
+          si = df_add_fast(si, df_mul(x[k], w.im));
           e += q;
           while (e >= N) e -= N;
         }
