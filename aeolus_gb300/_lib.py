@@ -52,6 +52,7 @@ SIGNATURES = {
     "aeolus_workspace_bytes": (c_int, [c_void_p, c_int, c_int, POINTER(c_size_t)]),
     "aeolus_synthesize": (c_int, [c_void_p, c_void_p, c_void_p, c_int, c_void_p, c_size_t, c_void_p]),
     "aeolus_analyze": (c_int, [c_void_p, c_void_p, c_void_p, c_int, c_void_p, c_size_t, c_void_p]),
+    "aeolus_synthesize_noalloc": (c_int, [c_void_p, c_void_p, c_void_p, c_int, c_void_p]),
     "aeolus_spectral_op": (c_int, [c_int, c_int, c_double, c_void_p, c_void_p, c_int, c_void_p]),
     "aeolus_jacobian": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p, c_int, c_void_p, c_size_t, c_void_p]),
     "aeolus_winds": (c_int, [c_void_p, c_double, c_void_p, c_void_p, c_void_p, c_int, c_void_p, c_size_t,

@@ -1,7 +1,23 @@
 // Public transform and spectral-operator entry points.
+#include <mutex>
+
 #include "chains.cuh"
 
 namespace aeolus {
+
+// Fixed device scratch of aeolus_synthesize_noalloc: a file-scope array that
+// every GPU loading this library holds until process exit.  Host code must
+// not pass the symbol itself to a kernel (on the host it is only a stand-in
+// for the device object); the device address comes from
+// cudaGetSymbolAddress, looked up once per device.
+constexpr size_t kNoAllocScratchBytes = size_t(16) << 20;  // 16 MiB
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
+
+namespace {
+std::mutex g_noalloc_mu;
+constexpr int kMaxDevices = 64;
+void* g_noalloc_addr[kMaxDevices] = {};
+}  // namespace
 
 namespace {
 
@@ -109,6 +125,43 @@ extern "C" int aeolus_analyze(aeolus_plan plan, const double* grid, double* coef
   EpiStore e{reinterpret_cast<double2*>(coeffs), L, (long)(L + 1) * (L + 1)};
   return run_anal_chain(plan, PwCopy{}, e, batch, grid, plan->npoints, plan->npoints, work,
                         static_cast<cudaStream_t>(stream));
+}
+
+extern "C" int aeolus_synthesize_noalloc(aeolus_plan plan, const double* coeffs, double* grid, int batch,
+                                         void* stream) {
+  if (!plan_ok(plan)) return fail(AEOLUS_ERR_ARG, "aeolus_synthesize_noalloc: invalid plan");
+  if (batch < 0 || (batch > 0 && (!coeffs || !grid)))
+    return fail(AEOLUS_ERR_ARG, "aeolus_synthesize_noalloc: bad arguments");
+  if (plan->kind != kGauss || plan->precision != AEOLUS_PREC_FP64)
+    return fail(AEOLUS_ERR_ARG, "aeolus_synthesize_noalloc: needs a Gauss plan with the FP64 contraction");
+  if (batch == 0) return AEOLUS_OK;
+  const size_t need = transform_bytes(plan, AEOLUS_OP_SYNTHESIZE, batch);
+  if (need > kNoAllocScratchBytes)
+    return fail(AEOLUS_ERR_WORKSPACE, "aeolus_synthesize_noalloc: " + std::to_string(batch) +
+                                          " fields need " + std::to_string(need) +
+                                          " bytes of scratch, above the fixed 16 MiB; split the batch or use "
+                                          "aeolus_synthesize with a caller-provided workspace");
+  int dev = -1;
+  AE_CUDA(cudaGetDevice(&dev));
+  if (dev != plan->device)
+    return fail(AEOLUS_ERR_ARG, "aeolus_synthesize_noalloc: the current device is not the plan's device");
+  if (dev < 0 || dev >= kMaxDevices) return fail(AEOLUS_ERR_ARG, "aeolus_synthesize_noalloc: device ordinal too large");
+  void* scratch = nullptr;
+  {
+    std::lock_guard<std::mutex> g(g_noalloc_mu);
+    if (!g_noalloc_addr[dev]) {
+      void* addr = nullptr;
+      AE_CUDA(cudaGetSymbolAddress(&addr, g_noalloc_scratch));
+      g_noalloc_addr[dev] = addr;
+    }
+    scratch = g_noalloc_addr[dev];
+  }
+  // The synthesis writes every scratch entry it later reads (all orders of
+  // every latitude row), so nothing left by an earlier call needs clearing.
+  const int L = plan->lmax;
+  DeriveCopy d{reinterpret_cast<const double2*>(coeffs), L, (long)(L + 1) * (L + 1)};
+  return run_synth_chain(plan, d, PwCopy{}, batch, grid, plan->npoints, plan->npoints, scratch, nullptr,
+                         static_cast<cudaStream_t>(stream));
 }
 
 extern "C" int aeolus_spectral_op(int op, int lmax, double radius, const double* in, double* out, int batch,

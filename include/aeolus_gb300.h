@@ -144,6 +144,21 @@ int aeolus_workspace_bytes(aeolus_plan plan, int op, int batch, size_t* bytes);
 int aeolus_synthesize(aeolus_plan plan, const double* coeffs, double* grid,
                       int batch, void* work, size_t work_bytes, void* stream);
 
+/* Synthesis that allocates nothing and takes no workspace: same result as
+ * aeolus_synthesize on a Gauss plan with the FP64 contraction.  It has no
+ * counterpart in the reference.  It serves callers that cannot call
+ * cudaMalloc or own a device buffer -- e.g. FFI hosts (Go, Java, plain C)
+ * without a device allocator of their own, or code that must not trigger the
+ * implicit device synchronisation of cudaMalloc/cudaFree.  Scratch is one
+ * fixed 16 MiB device array inside the library, held by every GPU that
+ * loads it until process exit; batches needing more scratch are rejected
+ * with AEOLUS_ERR_WORKSPACE.  The first call on a device looks up the
+ * array's device address (cudaGetSymbolAddress) and must come before any
+ * stream capture.  All calls share the array: calls that overlap on the GPU
+ * (different streams, or threads without ordering) race on it. */
+int aeolus_synthesize_noalloc(aeolus_plan plan, const double* coeffs,
+                              double* grid, int batch, void* stream);
+
 /* coeffs[b] = Y^H (w * grid[b]) scattered to the dense layout,
  * fast_geodesic_sh.py:68-87. */
 int aeolus_analyze(aeolus_plan plan, const double* grid, double* coeffs,
