@@ -11,8 +11,12 @@ step of the whole member batch (4 fused tendency chains).  Synthetic inputs
   python bench.py [--gpus N] [--steps K] [--warmup W] [--members B]
                   [--precision fp64|split] [--impl ours|reference]
 
-Prints one JSON line (rank 0).  `value` is device-timed with the state
-resident in HBM (CUDA events around each step, L2 flushed between steps);
+Prints one JSON line (rank 0).  `value` is the split-precision path (bf16-
+digit tcgen05 contractions, double-float longitude stage); `split_vs_fp64`
+times the plain FP64 path on the same states and reports the per-field
+relative L2 between the two after the timed steps.  `value` is device-timed
+with the state resident in HBM (CUDA events around each step, L2 flushed
+between steps);
 `e2e` goes through the public API with the state copied host->device from
 pinned memory and back every step.  `--impl reference` times the
 reference's algorithm (dense complex basis matrix-vector transforms, the
@@ -51,7 +55,7 @@ def parse():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--members", type=int, default=64)
-    ap.add_argument("--precision", choices=["fp64", "split"], default="fp64")
+    ap.add_argument("--precision", choices=["fp64", "split"], default="split")
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-flush", action="store_true")
@@ -183,6 +187,80 @@ class ClockSampler:
 
 
 # ------------------------------------------------------------ GPU arm
+def _collect_kernels(lib, _lib):
+    import ctypes
+    buf = ctypes.create_string_buffer(1 << 16)
+    _lib.check(lib.aeolus_profile_collect(buf, len(buf)))
+    out = {}
+    for line in buf.value.decode().splitlines():
+        name, n, ms = line.split()
+        out[name] = (int(n), float(ms))
+    return out
+
+
+def _timed_steps(model, y0, steps, flush, stream, lib, _lib):
+    """K RK4 steps from y0, each bracketed by CUDA events on the launching
+    stream, L2 flushed (outside the events) before each step."""
+    import torch
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+    lib.aeolus_profile_reset()
+    lib.aeolus_profile_enable(1)
+    y = y0
+    for i in range(steps):
+        if flush is not None:
+            flush.zero_()
+        evs[i][0].record(stream)
+        y = model.rk4(y, DT, 1, check=False)
+        evs[i][1].record(stream)
+    torch.cuda.synchronize()
+    lib.aeolus_profile_enable(0)
+    kstats = _collect_kernels(lib, _lib)
+    return sum(a.elapsed_time(b) for a, b in evs), kstats, y
+
+
+def _rel_l2_fields(a, b):
+    import torch
+    d = (a - b).reshape(a.shape[0], 3, -1)
+    r = b.reshape(b.shape[0], 3, -1)
+    num = torch.linalg.vector_norm(d, dim=-1)
+    den = torch.linalg.vector_norm(r, dim=-1).clamp_min(1e-300)
+    worst = (num / den).amax(dim=0)
+    return {name: float(v) for name, v in zip(("zeta", "delta", "phi"), worst)}
+
+
+def _roofline(kstats, B, peaks):
+    """Roofline entry for every library kernel; the dominant one first."""
+    ftx = 2.0 * NLAT * (LMAX + 1) * (LMAX + 2)  # flops of one real-field Legendre transform (no fold credit)
+    hbm = peaks.get("hbm_gbs", 6800.0)
+    tensor = peaks.get("bf16_tflops", 1900.0)
+    entries = {}
+    for name, (n, ms) in kstats.items():
+        t = ms / n / 1000.0
+        if name.startswith("tc_synth") or name.startswith("tc_anal"):
+            fields = 9 if name.startswith("tc_synth") else 4
+            useful = ftx * fields * B
+            entries[name] = {"kernel": name, "bound": "tensor", "achieved": useful / t / 1e12, "peak": tensor,
+                             "unit": "TFLOP/s", "frac": useful / t / 1e12 / tensor, "traffic": None,
+                             "launch_ms": t * 1000.0,
+                             "work_per_launch": f"{fields} fields x {B} members x 2*nlat*(L+1)(L+2) useful flops "
+                                                "(the 21 bf16 digit-pair products are not counted)"}
+        elif name.startswith("rows"):
+            byt = B * NLAT * (9 + 4) * (LMAX + 1) * 16.0
+            entries[name] = {"kernel": name, "bound": "hbm", "achieved": byt / t / 1e9, "peak": hbm, "unit": "GB/s",
+                             "frac": byt / t / 1e9 / hbm, "traffic": None, "launch_ms": t * 1000.0,
+                             "work_per_launch": f"{B} members x {NLAT} rows x 13 spectra x (L+1) x 16 B"}
+        elif name.endswith("_f64"):
+            fields = 9 if "synth" in name else 4
+            useful = ftx * fields * B
+            entries[name] = {"kernel": name, "bound": "fp64", "achieved": useful / t / 1e12,
+                             "peak": FP64_NOMINAL_GFLOPS / 1000.0, "unit": "TFLOP/s",
+                             "frac": useful / t / 1e12 / (FP64_NOMINAL_GFLOPS / 1000.0), "traffic": None,
+                             "launch_ms": t * 1000.0, "peak_source": "nominal (no FP64 figure measured)"}
+    order = sorted(kstats, key=lambda k: -kstats[k][1])
+    dom = next((entries[k] for k in order if k in entries), None)
+    return dom, [entries[k] for k in order if k in entries]
+
+
 def main():
     args = parse()
     if args.impl == "reference":
@@ -205,53 +283,51 @@ def main():
 
     lib = _lib.load()
     B = args.members
-    planet = ae.make_planet("latlon", nlat=NLAT, nlon=NLON, l_max=LMAX, device=dev)
     states, depth = W.member_states(LMAX, B, seed=1000 * rank)
-    model = ShallowWaterModel(planet, gravity=W.GRAVITY, mean_depth=depth)
-    if args.precision == "split":
-        planet.so._product_space.sh.plan.set_precision(_lib.PREC_SPLIT_BF16)
+
+    def build(precision):
+        planet = ae.make_planet("latlon", nlat=NLAT, nlon=NLON, l_max=LMAX, device=dev)
+        if precision == "split":
+            planet.so._product_space.sh.plan.set_precision(_lib.PREC_SPLIT_BF16)
+        return ShallowWaterModel(planet, gravity=W.GRAVITY, mean_depth=depth)
+
+    model = build(args.precision)
+    other = build("fp64") if args.precision == "split" else None
     y0 = torch.as_tensor(states, device=dev)
-    y = y0.clone()
     flush = None if args.no_flush else torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+    stream = torch.cuda.current_stream(dev)
 
     def barrier():
         if world > 1:
             dist.barrier()
         torch.cuda.synchronize(dev)
 
-    # warm-up
-    for _ in range(max(args.warmup, 3)):
-        y = model.rk4(y, DT, 1, check=False)
+    warm = max(args.warmup, 3)
+    for m in (model, other):
+        if m is not None:
+            y = y0
+            for _ in range(warm):
+                y = m.rk4(y, DT, 1, check=False)
     barrier()
 
-    # device-timed region: per-step events, L2 flush between steps
-    stream = torch.cuda.current_stream(dev)
-    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
-    lib.aeolus_profile_reset()
-    lib.aeolus_profile_enable(1)
     with ClockSampler(local) as clk:
         barrier()
-        for i in range(args.steps):
-            if flush is not None:
-                flush.zero_()
-            evs[i][0].record(stream)
-            y = model.rk4(y, DT, 1, check=False)
-            evs[i][1].record(stream)
+        total_ms, kstats, y_main = _timed_steps(model, y0, args.steps, flush, stream, lib, _lib)
         barrier()
-    lib.aeolus_profile_enable(0)
-    buf = __import__("ctypes").create_string_buffer(1 << 16)
-    _lib.check(lib.aeolus_profile_collect(buf, len(buf)))
-    kstats = {}
-    for line in buf.value.decode().splitlines():
-        name, n, ms = line.split()
-        kstats[name] = (int(n), float(ms))
-    step_ms = [a.elapsed_time(b) for a, b in evs]
-    total_ms = sum(step_ms)
     if world > 1:
         t = torch.tensor([total_ms], device=dev, dtype=torch.float64)
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         total_ms = float(t.item())
     value = world * args.steps / (total_ms / 1000.0)
+
+    comparison = None
+    if other is not None:
+        ms64, k64, y64 = _timed_steps(other, y0, args.steps, flush, stream, lib, _lib)
+        comparison = {"fp64_steps_per_s": args.steps / (ms64 / 1000.0),
+                      "fp64_ms_per_step": ms64 / args.steps,
+                      "speedup_split_vs_fp64": (ms64 / total_ms),
+                      "rel_l2_split_vs_fp64_after_steps": _rel_l2_fields(y_main, y64),
+                      "fp64_kernels": {k: {"launches": n, "ms": ms} for k, (n, ms) in k64.items()}}
 
     # end-to-end through the public API: pinned host state in, state out
     host_in = torch.as_tensor(states).pin_memory()
@@ -275,31 +351,8 @@ def main():
         e2e_ms = float(t.item())
     bytes_state = host_in.numel() * host_in.element_size()
 
-    # roofline of the dominant kernel (algorithmic work per launch)
-    dom = max(kstats.items(), key=lambda kv: kv[1][1]) if kstats else None
-    roof = None
-    if dom is not None:
-        name, (n, ms) = dom
-        per_launch_s = ms / n / 1000.0
-        nh = NLAT // 2
-        ftx = 2.0 * NLAT * (LMAX + 1) * (LMAX + 2)  # flops of one real-field Legendre transform
-        fields = {"legendre_synth_f64": 9, "legendre_analysis_f64": 4}.get(name)
-        peaks = json.loads(PEAKS_FILE.read_text()) if PEAKS_FILE.exists() else {}
-        if fields is not None:
-            flops = ftx * fields * B
-            achieved = flops / per_launch_s / 1e12
-            roof = {"kernel": name, "bound": "fp64", "achieved": achieved, "peak": FP64_NOMINAL_GFLOPS / 1000.0,
-                    "unit": "TFLOP/s", "frac": achieved / (FP64_NOMINAL_GFLOPS / 1000.0), "traffic": None,
-                    "peak_source": "nominal GB300 FP64 (not in MEASURED_PEAKS.json)",
-                    "work_per_launch": f"{fields} fields x {B} members x 2*nlat*(L+1)(L+2) flops",
-                    "launch_ms": per_launch_s * 1000.0}
-        else:
-            # row kernel: HBM-bound view -- read F blocks, write G blocks
-            byt = B * NLAT * (9 + 4) * (LMAX + 1) * 16.0
-            achieved = byt / per_launch_s / 1e9
-            pk = peaks.get("hbm_gbs", 6800.0)
-            roof = {"kernel": name, "bound": "hbm", "achieved": achieved, "peak": pk, "unit": "GB/s",
-                    "frac": achieved / pk, "traffic": None, "launch_ms": per_launch_s * 1000.0}
+    peaks = json.loads(PEAKS_FILE.read_text()) if PEAKS_FILE.exists() else {}
+    roof, roof_all = _roofline(kstats, B, peaks)
     launches = sum(n for n, _ in kstats.values())
 
     cpu = None
@@ -310,17 +363,19 @@ def main():
 
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
-                "warmup": max(args.warmup, 3), "ms_per_step": total_ms / args.steps, "higher_is_better": True,
-                "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+                "warmup": warm, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None,
+                "dtype": "bf16x6-digit/f32x2/f64" if args.precision == "split" else "f64", "data": "synthetic",
                 "config": dict(workload_config(args, B), l2="flushed between steps (256 MiB write)"
                                if flush is not None else "not flushed"),
                 "member_steps_per_s": value * B,
+                "split_vs_fp64": comparison,
                 "e2e": {"value": world * args.steps / (e2e_ms / 1000.0), "unit": UNIT,
                         "h2d_bytes_per_step": bytes_state, "d2h_bytes_per_step": bytes_state + 4 * B,
                         "wall_ms": e2e_wall_ms},
                 "gpu_launches": launches,
                 "kernels": {k: {"launches": n, "ms": ms} for k, (n, ms) in kstats.items()},
-                "roofline": roof, "cpu_baseline": cpu, "clocks": clk.summary()}
+                "roofline": roof, "roofline_all": roof_all, "cpu_baseline": cpu, "clocks": clk.summary()}
         print(json.dumps(line), flush=True)
     if world > 1:
         dist.destroy_process_group()
