@@ -16,7 +16,9 @@ LIB_PATH = Path(__file__).resolve().parent / "libaeolus_gb300.so"
 OK, ERR_ARG, ERR_CUDA, ERR_WORKSPACE, ERR_STATE = 0, 1, 2, 3, 4
 PREC_FP64, PREC_SPLIT_BF16 = 0, 1
 (OP_SYNTHESIZE, OP_ANALYZE, OP_JACOBIAN, OP_WINDS, OP_BVE_TENDENCY, OP_SWE_TENDENCY,
- OP_BVE_RK4, OP_SWE_RK4, OP_SWE_VALIDATE, OP_SWE_INVARIANTS) = range(10)
+ OP_BVE_RK4, OP_SWE_RK4, OP_SWE_VALIDATE, OP_SWE_INVARIANTS,
+ OP_SYNTHESIZE_ADJOINT, OP_ANALYZE_ADJOINT, OP_BVE_TENDENCY_ADJOINT, OP_SWE_TENDENCY_ADJOINT,
+ OP_BVE_RK4_ADJOINT, OP_SWE_RK4_ADJOINT) = range(16)
 STATE_NONFINITE, STATE_MONOPOLE, STATE_THICKNESS = 1, 2, 4
 
 # Spectral operator ids of aeolus_spectral_op.
@@ -70,6 +72,16 @@ SIGNATURES = {
     "aeolus_bve_spectral_diagnostics": (c_int, [c_int, c_double, c_double, c_void_p, c_void_p, c_int, c_void_p]),
     "aeolus_swe_invariants": (c_int, [c_void_p, POINTER(SweParams), c_void_p, c_void_p, c_int, c_void_p, c_size_t,
                                       c_void_p]),
+    "aeolus_synthesize_adjoint": (c_int, [c_void_p, c_void_p, c_void_p, c_int, c_void_p, c_size_t, c_void_p]),
+    "aeolus_analyze_adjoint": (c_int, [c_void_p, c_void_p, c_void_p, c_int, c_void_p, c_size_t, c_void_p]),
+    "aeolus_bve_tendency_adjoint": (c_int, [c_void_p, POINTER(BveParams), c_void_p, c_void_p, c_void_p, c_int,
+                                            c_void_p, c_size_t, c_void_p]),
+    "aeolus_swe_tendency_adjoint": (c_int, [c_void_p, POINTER(SweParams), c_void_p, c_void_p, c_void_p, c_int,
+                                            c_void_p, c_size_t, c_void_p]),
+    "aeolus_bve_rk4_adjoint": (c_int, [c_void_p, POINTER(BveParams), c_void_p, c_void_p, c_int, c_double, c_void_p,
+                                       c_size_t, c_void_p]),
+    "aeolus_swe_rk4_adjoint": (c_int, [c_void_p, POINTER(SweParams), c_void_p, c_void_p, c_int, c_double, c_void_p,
+                                       c_size_t, c_void_p]),
 }
 
 _lib = None

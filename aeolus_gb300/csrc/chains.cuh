@@ -127,10 +127,11 @@ int run_synth_chain(const aeolus_plan_impl* p, const Derive& d, const Pw& pw, in
   return AEOLUS_OK;
 }
 
-// Input grid: in[b * in_b + f * in_f + point].
+// Input grid: in[b * in_b + f * in_f + point].  unit_weights drops the
+// quadrature weights (the transpose of synthesis instead of the analysis).
 template <class Pw, class Epi>
 int run_anal_chain(const aeolus_plan_impl* p, const Pw& pw, const Epi& e, int batch, const double* in, long in_b,
-                   long in_f, void* work, cudaStream_t st) {
+                   long in_f, void* work, cudaStream_t st, bool unit_weights = false) {
   static_assert(Pw::NOUT == Epi::NF, "pointwise/epilogue field count");
   if (p->kind == kGauss) {
     double2* FG = static_cast<double2*>(work);
@@ -141,6 +142,7 @@ int run_anal_chain(const aeolus_plan_impl* p, const Pw& pw, const Epi& e, int ba
     ra.gin = in;
     ra.gin_b = in_b;
     ra.gin_f = in_f;
+    ra.unit_weights = unit_weights ? 1 : 0;
     int s = launch_rows<Pw, kInGrid, kOutG>(p, pw, ra, st);
     if (s) return s;
     if (split_on(p)) {
@@ -155,7 +157,8 @@ int run_anal_chain(const aeolus_plan_impl* p, const Pw& pw, const Epi& e, int ba
   w += align256((size_t)batch * Pw::NOUT * np * 8);
   double* C = reinterpret_cast<double*>(w);
   points_pointwise_kernel<Pw><<<blocks_for(np * batch, 128), 128, 0, st>>>(
-      np, batch, in, in_b, in_f, Wt, (long)Pw::NOUT * np, np, p->coslat, p->fgrid, p->wpts, nullptr, pw);
+      np, batch, in, in_b, in_f, Wt, (long)Pw::NOUT * np, np, p->coslat, p->fgrid, unit_weights ? nullptr : p->wpts,
+      nullptr, pw);
   AE_LAUNCH("points_pointwise_kernel");
   int s = points_gemm_analysis(p, Wt, C, batch * Pw::NOUT, st);
   if (s) return s;

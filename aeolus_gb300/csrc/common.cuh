@@ -72,7 +72,13 @@ struct FftInfo {
   int use_fft;      // 1: half-length complex mixed-radix FFT; 0: direct DFT
   int nfac;
   int fac[kMaxFactors];
+  // per stage: 32-bit reciprocals ceil(2^32 / d) of the butterfly count n/r
+  // and of the sub-transform length Ls (0 when d = 1); x / d = umulhi(x, .)
+  // exactly while x * d < 2^32, which n <= kMaxFftHalf guarantees
+  unsigned nbm[kMaxFactors];
+  unsigned lsm[kMaxFactors];
 };
+constexpr int kMaxFftHalf = 8192;
 
 // ------------------------------------------------------------------ plan
 enum PlanKind { kGauss = 0, kPoints = 1 };

@@ -48,7 +48,8 @@ template <class Derive>
 int launch_synth(const aeolus_plan_impl* p, const Derive& d, double2* FG, int nblk, int batch,
                  cudaStream_t st) {
   const int L = p->lmax;
-  const int bc = pick_bc(L, batch);
+  int bc = pick_bc(L, batch);
+  while (bc > 1 && synth_smem_bytes<Derive, kSynthCPT>(L, bc) > 200 * 1024) --bc;
   LegArgs a{L, p->nlat, p->nh, batch, bc, p->P, p->PT, FG, nblk};
   const size_t sm = synth_smem_bytes<Derive, kSynthCPT>(L, bc);
   auto kern = legendre_synth_kernel<Derive, kSynthCPT>;
@@ -67,7 +68,8 @@ template <class Epi>
 int launch_analysis(const aeolus_plan_impl* p, const Epi& e, double2* FG, int nblk, int batch,
                     cudaStream_t st) {
   const int L = p->lmax;
-  const int bc = pick_bc(L, batch);
+  int bc = pick_bc(L, batch);
+  while (bc > 1 && analysis_smem_bytes<Epi>(p->nh, bc) > 220 * 1024) --bc;
   LegArgs a{L, p->nlat, p->nh, batch, bc, p->P, p->PT, FG, nblk};
   const size_t sm = analysis_smem_bytes<Epi>(p->nh, bc);
   auto kern = legendre_analysis_kernel<Epi>;
@@ -89,7 +91,7 @@ int launch_rows(const aeolus_plan_impl* p, const Pw& pw, RowArgs a, cudaStream_t
   a.tw = p->tw;
   a.coslat = p->coslat;
   a.fgrid = p->fgrid;
-  a.wq = p->wq;
+  a.wq = a.unit_weights ? nullptr : p->wq;
   const size_t sm = row_smem_bytes<Pw>(p->fft);
   dim3 grid(p->nlat, a.batch);
   if (p->precision == AEOLUS_PREC_SPLIT_BF16) {

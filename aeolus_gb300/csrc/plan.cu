@@ -129,12 +129,16 @@ __global__ void gauss_nodes_kernel(int n, double* x, double* sth, double* theta,
   double t = middle ? 0.5 * kPi : kPi * (j + 0.75) / (n + 0.5);
   double pn, q;
   if (!middle) {
-    for (int it = 0; it < 64; ++it) {
+    // Newton converges quadratically from this guess (~4 steps); once the
+    // step is at the rounding level, one more step polishes the node.
+    int polish = -1;
+    for (int it = 0; it < 32 && polish != 0; ++it) {
       const double sh = sin(0.5 * t);
       legendre_reinsch(n, 2.0 * sh * sh, &pn, &q);
       const double dt = pn * sin(t) / q;
       t -= dt;
-      if (fabs(dt) <= 1e-17) break;
+      if (polish > 0) --polish;
+      else if (polish < 0 && fabs(dt) <= 1e-15 * t) polish = 1;
     }
   }
   const double sv = middle ? 1.0 : sin(t);
@@ -245,11 +249,18 @@ void plan_fft(int N, int L, FftInfo& f) {
   const int radices[3] = {2, 3, 5};
   for (int r : radices)
     while (rem % r == 0 && nf < kMaxFactors) { fac[nf++] = r; rem /= r; }
-  if (rem != 1) return;
+  if (rem != 1 || n > kMaxFftHalf) return;
   f.use_fft = 1;
   f.n = n;
   f.nfac = nf;
-  for (int i = 0; i < nf; ++i) f.fac[i] = fac[i];
+  auto recip = [](long long d) { return d == 1 ? 0u : (unsigned)(((1LL << 32) + d - 1) / d); };
+  long long ls = 1;
+  for (int i = 0; i < nf; ++i) {
+    f.fac[i] = fac[i];
+    f.nbm[i] = recip(n / fac[i]);
+    f.lsm[i] = recip(ls);
+    ls *= fac[i];
+  }
 }
 
 int upload(double** dst, const std::vector<double>& src) {

@@ -20,7 +20,8 @@ struct RowArgs {
   const double2* tw;      // [N] exp(-2 pi i q / N)
   const double* coslat;   // [nlat] clamped cos(latitude)
   const double* fgrid;    // [nlat] synthesis of the unit (1,0) mode
-  const double* wq;       // [nlat] quadrature weight of a point of row j
+  const double* wq;       // [nlat] quadrature weight of a point of row j (NULL: unit weights)
+  int unit_weights;       // launch_rows: leave wq NULL (adjoint of synthesis)
   // kInF: spectra F[b][j][nblk][L+1]; kOutG writes G into the same blocks
   double2* FG;
   int nblk;
@@ -33,15 +34,21 @@ struct RowArgs {
   unsigned* status;       // optional per-member state bits
 };
 
-// Radix-r butterfly, forward (INV=false, exp(-2 pi i/r)) or inverse.
-template <bool INV>
-__device__ __forceinline__ void butterfly(double2* v, int r) {
+// x / d through the stage's 32-bit reciprocal (exact for x * d < 2^32).
+__device__ __forceinline__ int div_rcp(int x, int d, unsigned rcp) {
+  return d == 1 ? x : (int)__umulhi((unsigned)x, rcp);
+}
+
+// Radix-R butterfly, forward (INV=false, exp(-2 pi i/R)) or inverse.  R is a
+// compile-time constant so the R values stay in registers.
+template <bool INV, int R>
+__device__ __forceinline__ void butterfly(double2* v) {
   const double sg = INV ? 1.0 : -1.0;  // sign of the imaginary exponent
-  if (r == 2) {
+  if constexpr (R == 2) {
     double2 a = v[0], b = v[1];
     v[0] = cadd(a, b);
     v[1] = csub(a, b);
-  } else if (r == 4) {
+  } else if constexpr (R == 4) {
     double2 s02 = cadd(v[0], v[2]), d02 = csub(v[0], v[2]);
     double2 s13 = cadd(v[1], v[3]), d13 = csub(v[1], v[3]);
     double2 id13 = cscale(sg, ci(d13));  // sg * i * (v1 - v3)
@@ -49,7 +56,7 @@ __device__ __forceinline__ void butterfly(double2* v, int r) {
     v[2] = csub(s02, s13);
     v[1] = cadd(d02, id13);
     v[3] = csub(d02, id13);
-  } else if (r == 3) {
+  } else if constexpr (R == 3) {
     const double h = 0.86602540378443864676;  // sin(2 pi / 3)
     double2 s = cadd(v[1], v[2]), d = csub(v[1], v[2]);
     double2 t = make_double2(v[0].x - 0.5 * s.x, v[0].y - 0.5 * s.y);
@@ -57,7 +64,7 @@ __device__ __forceinline__ void butterfly(double2* v, int r) {
     v[0] = cadd(v[0], s);
     v[1] = cadd(t, id);
     v[2] = csub(t, id);
-  } else {  // r == 5
+  } else {  // R == 5
     const double c1 = 0.30901699437494742410, c2 = -0.80901699437494742410;
     const double s1 = 0.95105651629515357212, s2 = 0.58778525229247312917;
     double2 a1 = cadd(v[1], v[4]), a2 = cadd(v[2], v[3]);
@@ -75,6 +82,36 @@ __device__ __forceinline__ void butterfly(double2* v, int r) {
   }
 }
 
+// One Stockham stage of radix R over nf transforms of length n (sub-
+// transform length Ls before the stage).
+template <bool INV, int R>
+__device__ __forceinline__ void fft_stage(const double2* __restrict__ src, double2* __restrict__ dst, int nf, int n,
+                                          int Ls, unsigned nb_rcp, unsigned ls_rcp,
+                                          const double2* __restrict__ tw) {
+  const int nb = n / R, Ns = Ls * R, stride = n / Ns;
+  for (int idx = threadIdx.x; idx < nf * nb; idx += blockDim.x) {
+    const int f = div_rcp(idx, nb, nb_rcp), jj = idx - f * nb;
+    const int q = div_rcp(jj, Ls, ls_rcp), k = jj - q * Ls;
+    const double2* x = src + (long)f * n;
+    double2* y = dst + (long)f * n;
+    double2 v[R];
+#pragma unroll
+    for (int t = 0; t < R; ++t) v[t] = x[jj + t * nb];
+    if (k != 0) {
+#pragma unroll
+      for (int t = 1; t < R; ++t) {
+        double2 w = __ldg(&tw[2 * (k * t * stride)]);
+        if (INV) w.y = -w.y;
+        v[t] = cmul(v[t], w);
+      }
+    }
+    butterfly<INV, R>(v);
+    const int base = q * Ns + k;
+#pragma unroll
+    for (int t = 0; t < R; ++t) y[base + t * Ls] = v[t];
+  }
+}
+
 // nf independent length-n complex FFTs (field stride n) in shared memory,
 // Stockham autosort, ping-pong between src and dst; returns the buffer that
 // holds the result.  Ends with __syncthreads().
@@ -85,30 +122,17 @@ __device__ double2* fft_run(double2* src, double2* dst, int nf, const FftInfo& f
   int Ls = 1;
   for (int s = 0; s < fi.nfac; ++s) {
     const int r = fi.fac[s];
-    const int Ns = Ls * r, nb = n / r, stride = n / Ns;
-    for (int idx = threadIdx.x; idx < nf * nb; idx += blockDim.x) {
-      const int f = idx / nb, jj = idx - f * nb;
-      const double2* x = src + (long)f * n;
-      double2* y = dst + (long)f * n;
-      const int k = jj % Ls;
-      double2 v[5];
-      for (int t = 0; t < r; ++t) v[t] = x[jj + t * nb];
-      if (k != 0) {
-        for (int t = 1; t < r; ++t) {
-          double2 w = __ldg(&tw[2 * (k * t * stride)]);
-          if (INV) w.y = -w.y;
-          v[t] = cmul(v[t], w);
-        }
-      }
-      butterfly<INV>(v, r);
-      const int base = (jj / Ls) * Ns + k;
-      for (int t = 0; t < r; ++t) y[base + t * Ls] = v[t];
+    switch (r) {
+      case 4: fft_stage<INV, 4>(src, dst, nf, n, Ls, fi.nbm[s], fi.lsm[s], tw); break;
+      case 2: fft_stage<INV, 2>(src, dst, nf, n, Ls, fi.nbm[s], fi.lsm[s], tw); break;
+      case 3: fft_stage<INV, 3>(src, dst, nf, n, Ls, fi.nbm[s], fi.lsm[s], tw); break;
+      default: fft_stage<INV, 5>(src, dst, nf, n, Ls, fi.nbm[s], fi.lsm[s], tw); break;
     }
     __syncthreads();
     double2* tmp = src;
     src = dst;
     dst = tmp;
-    Ls = Ns;
+    Ls *= r;
   }
   return src;
 }
@@ -203,7 +227,7 @@ __global__ void __launch_bounds__(256) row_kernel(RowArgs a, Pw pw) {
       a.gout[(long)b * a.gout_b + (long)f * a.gout_f + (long)j * N + k] = xout[(long)f * 2 * n + k];
     }
   } else {
-    const double wj = a.wq[j];
+    const double wj = a.wq ? a.wq[j] : 1.0;
     if (a.fft.use_fft) {
       double2* zin = reinterpret_cast<double2*>(xout);
       double2* zother = (zin == buf0) ? buf1 : buf0;

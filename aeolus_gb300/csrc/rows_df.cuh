@@ -18,14 +18,14 @@
 
 namespace aeolus {
 
-template <bool INV>
-__device__ __forceinline__ void butterfly_df(cdf* v, int r, const DfConst& k) {
+template <bool INV, int R>
+__device__ __forceinline__ void butterfly_df(cdf* v, const DfConst& k) {
   const float sg = INV ? 1.0f : -1.0f;
-  if (r == 2) {
+  if constexpr (R == 2) {
     const cdf a = v[0], b = v[1];
     v[0] = cdf_addf(a, b);
     v[1] = cdf_subf(a, b);
-  } else if (r == 4) {
+  } else if constexpr (R == 4) {
     const cdf s02 = cdf_addf(v[0], v[2]), d02 = cdf_subf(v[0], v[2]);
     const cdf s13 = cdf_addf(v[1], v[3]), d13 = cdf_subf(v[1], v[3]);
     const cdf id13 = cdf_scale2(sg, cdf_i(d13));
@@ -33,14 +33,14 @@ __device__ __forceinline__ void butterfly_df(cdf* v, int r, const DfConst& k) {
     v[2] = cdf_subf(s02, s13);
     v[1] = cdf_addf(d02, id13);
     v[3] = cdf_subf(d02, id13);
-  } else if (r == 3) {
+  } else if constexpr (R == 3) {
     const cdf s = cdf_addf(v[1], v[2]), d = cdf_subf(v[1], v[2]);
     const cdf t = cdf_subf(v[0], cdf_scale2(0.5f, s));
     const cdf id = cdf_scale(k.h3, cdf_scale2(sg, cdf_i(d)));
     v[0] = cdf_addf(v[0], s);
     v[1] = cdf_addf(t, id);
     v[2] = cdf_subf(t, id);
-  } else {  // r == 5
+  } else {  // R == 5
     const cdf a1 = cdf_addf(v[1], v[4]), a2 = cdf_addf(v[2], v[3]);
     const cdf b1 = cdf_subf(v[1], v[4]), b2 = cdf_subf(v[2], v[3]);
     const cdf t1 = cdf_addf(v[0], cdf_addf(cdf_scale(k.c1, a1), cdf_scale(k.c2, a2)));
@@ -56,6 +56,34 @@ __device__ __forceinline__ void butterfly_df(cdf* v, int r, const DfConst& k) {
   }
 }
 
+template <bool INV, int R>
+__device__ __forceinline__ void fft_stage_df(const cdf* __restrict__ src, cdf* __restrict__ dst, int nf, int n, int Ls,
+                                             unsigned nb_rcp, unsigned ls_rcp, const float4* __restrict__ tw,
+                                             const DfConst& kc) {
+  const int nb = n / R, Ns = Ls * R, stride = n / Ns;
+  for (int idx = threadIdx.x; idx < nf * nb; idx += blockDim.x) {
+    const int f = div_rcp(idx, nb, nb_rcp), jj = idx - f * nb;
+    const int q = div_rcp(jj, Ls, ls_rcp), k = jj - q * Ls;
+    const cdf* x = src + (long)f * n;
+    cdf* y = dst + (long)f * n;
+    cdf v[R];
+#pragma unroll
+    for (int t = 0; t < R; ++t) v[t] = x[jj + t * nb];
+    if (k != 0) {
+#pragma unroll
+      for (int t = 1; t < R; ++t) {
+        cdf w = cdf_from_f4(__ldg(&tw[2 * (k * t * stride)]));
+        if (INV) w = cdf_conj(w);
+        v[t] = cdf_mulf(v[t], w);
+      }
+    }
+    butterfly_df<INV, R>(v, kc);
+    const int base = q * Ns + k;
+#pragma unroll
+    for (int t = 0; t < R; ++t) y[base + t * Ls] = v[t];
+  }
+}
+
 template <bool INV>
 __device__ cdf* fft_run_df(cdf* src, cdf* dst, int nf, const FftInfo& fi, const float4* __restrict__ tw,
                            const DfConst& kc) {
@@ -63,30 +91,17 @@ __device__ cdf* fft_run_df(cdf* src, cdf* dst, int nf, const FftInfo& fi, const 
   int Ls = 1;
   for (int s = 0; s < fi.nfac; ++s) {
     const int r = fi.fac[s];
-    const int Ns = Ls * r, nb = n / r, stride = n / Ns;
-    for (int idx = threadIdx.x; idx < nf * nb; idx += blockDim.x) {
-      const int f = idx / nb, jj = idx - f * nb;
-      const cdf* x = src + (long)f * n;
-      cdf* y = dst + (long)f * n;
-      const int k = jj % Ls;
-      cdf v[5];
-      for (int t = 0; t < r; ++t) v[t] = x[jj + t * nb];
-      if (k != 0) {
-        for (int t = 1; t < r; ++t) {
-          cdf w = cdf_from_f4(__ldg(&tw[2 * (k * t * stride)]));
-          if (INV) w = cdf_conj(w);
-          v[t] = cdf_mulf(v[t], w);
-        }
-      }
-      butterfly_df<INV>(v, r, kc);
-      const int base = (jj / Ls) * Ns + k;
-      for (int t = 0; t < r; ++t) y[base + t * Ls] = v[t];
+    switch (r) {
+      case 4: fft_stage_df<INV, 4>(src, dst, nf, n, Ls, fi.nbm[s], fi.lsm[s], tw, kc); break;
+      case 2: fft_stage_df<INV, 2>(src, dst, nf, n, Ls, fi.nbm[s], fi.lsm[s], tw, kc); break;
+      case 3: fft_stage_df<INV, 3>(src, dst, nf, n, Ls, fi.nbm[s], fi.lsm[s], tw, kc); break;
+      default: fft_stage_df<INV, 5>(src, dst, nf, n, Ls, fi.nbm[s], fi.lsm[s], tw, kc); break;
     }
     __syncthreads();
     cdf* tmp = src;
     src = dst;
     dst = tmp;
-    Ls = Ns;
+    Ls *= r;
   }
   return src;
 }
@@ -176,7 +191,7 @@ __global__ void __launch_bounds__(256) row_kernel_df(RowArgs a, Pw pw, const flo
       a.gout[(long)b * a.gout_b + (long)f * a.gout_f + (long)j * N + k] = df_to_double(xout[(long)f * 2 * n + k]);
     }
   } else {
-    const df wj = df_from_double(a.wq[j]);
+    const df wj = a.wq ? df_from_double(a.wq[j]) : df{1.f, 0.f};
     if (a.fft.use_fft) {
       cdf* zin = reinterpret_cast<cdf*>(xout);
       cdf* zother = (zin == buf0) ? buf1 : buf0;

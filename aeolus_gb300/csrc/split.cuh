@@ -395,17 +395,24 @@ __global__ void __launch_bounds__(256) split_anal_slice_kernel(SplitDims dm, int
 // 1 lane 0 issues, per chunk, the 21 digit-pair MMAs into the level
 // accumulators and commits the stage back to the producer.  All waits are
 // bounded; an expired wait sets *err and the CTA skips its outputs.
+constexpr size_t kStageBytesA = chunk_elems(128) * 2;
+constexpr size_t kStageBytesB = chunk_elems(kNT) * 2;
+
+// Stage buffers are addressed arithmetically (no pointer arrays indexed by
+// the runtime stage number, which would live in local memory).
 struct TcPipe {
-  __nv_bfloat16* A[kStages];
-  __nv_bfloat16* B[kStages];
+  char* stages;     // kStages x (A tile, B tile)
+  __device__ __nv_bfloat16* A(int st) const {
+    return reinterpret_cast<__nv_bfloat16*>(stages + (size_t)st * (kStageBytesA + kStageBytesB));
+  }
+  __device__ __nv_bfloat16* B(int st) const {
+    return reinterpret_cast<__nv_bfloat16*>(stages + (size_t)st * (kStageBytesA + kStageBytesB) + kStageBytesA);
+  }
   uint64_t* full;   // [kStages]
   uint64_t* empty;  // [kStages]
   uint64_t* done;
   uint32_t* tmem_slot;
 };
-
-constexpr size_t kStageBytesA = chunk_elems(128) * 2;
-constexpr size_t kStageBytesB = chunk_elems(kNT) * 2;
 
 inline size_t tc_smem_bytes() {
   // 1 KB alignment slack + stages + barriers; >= 77 KB so at most two CTAs
@@ -416,12 +423,8 @@ inline size_t tc_smem_bytes() {
 
 __device__ inline void tc_carve(char* base, TcPipe& p) {
   char* q = reinterpret_cast<char*>((reinterpret_cast<uintptr_t>(base) + 1023) & ~uintptr_t(1023));
-  for (int s = 0; s < kStages; ++s) {
-    p.A[s] = reinterpret_cast<__nv_bfloat16*>(q);
-    q += kStageBytesA;
-    p.B[s] = reinterpret_cast<__nv_bfloat16*>(q);
-    q += kStageBytesB;
-  }
+  p.stages = q;
+  q += kStages * (kStageBytesA + kStageBytesB);
   uint64_t* bars = reinterpret_cast<uint64_t*>(q);
   p.full = bars;
   p.empty = bars + kStages;
@@ -441,8 +444,8 @@ __device__ inline bool tc_mainloop(TcPipe& p, const __nv_bfloat16* gA, const __n
       if (kc >= kStages) ok = tc::mbar_wait(&p.empty[st], ((kc / kStages) - 1) & 1);
       if (!ok) break;
       tc::mbar_expect_tx(&p.full[st], (uint32_t)(kStageBytesA + kStageBytesB));
-      tc::bulk_g2s(p.A[st], gA + (long long)kc * chunk_elems(128), (uint32_t)kStageBytesA, &p.full[st]);
-      tc::bulk_g2s(p.B[st], gB + (long long)kc * chunk_elems(kNT), (uint32_t)kStageBytesB, &p.full[st]);
+      tc::bulk_g2s(p.A(st), gA + (long long)kc * chunk_elems(128), (uint32_t)kStageBytesA, &p.full[st]);
+      tc::bulk_g2s(p.B(st), gB + (long long)kc * chunk_elems(kNT), (uint32_t)kStageBytesB, &p.full[st]);
     }
     // no copy may still be in flight when the CTA ends: wait for the last loads
     const int first = nchunks > kStages ? nchunks - kStages : 0;
@@ -458,10 +461,10 @@ __device__ inline bool tc_mainloop(TcPipe& p, const __nv_bfloat16* gA, const __n
       if (!ok) break;
       tc::fence_after_sync();
       for (int s = 0; s < kSlices; ++s) {
-        const uint64_t da = tc::smem_desc(p.A[st] + (long long)s * 128 * kKC, 128, kKC * 16);
+        const uint64_t da = tc::smem_desc(p.A(st) + (long long)s * 128 * kKC, 128, kKC * 16);
         for (int t = 0; s + t < kSlices; ++t) {
           const int a = acc_of(s, t);
-          const uint64_t db = tc::smem_desc(p.B[st] + (long long)t * kNT * kKC, 128, kKC * 16);
+          const uint64_t db = tc::smem_desc(p.B(st) + (long long)t * kNT * kKC, 128, kKC * 16);
           tc::mma_bf16(tmem + (uint32_t)a * kNT, da, db, idesc, ((started >> a) & 1u) ? 1u : 0u);
           started |= 1u << a;
         }
@@ -560,7 +563,9 @@ __global__ void __launch_bounds__(128, 2) tc_anal_kernel(SplitDims dm, const __n
                                                          const __nv_bfloat16* __restrict__ dana,
                                                          const int* __restrict__ ecol, int batch, Epi epi, int* err) {
   constexpr int NF = Epi::NF;
-  static_assert(16 % (2 * NF) == 0, "a 16-column chunk must hold whole members");
+  // Whole members per 16-column chunk -> Epi::finish(b, l, m, a[NF]);
+  // otherwise (NF = 9, ...) one field at a time -> Epi::finish_field.
+  constexpr bool kWhole = 16 % (2 * NF) == 0;
   extern __shared__ char smem_raw[];
   const int m = blockIdx.x, tile = blockIdx.y;
   const int L = dm.L, K = L + 1 - m;
@@ -577,24 +582,38 @@ __global__ void __launch_bounds__(128, 2) tc_anal_kernel(SplitDims dm, const __n
       float acc[16][kAccs];
       tc_read16(tmem, c0, acc);
       if (t < K) {
+        if constexpr (kWhole) {
 #pragma unroll
-        for (int i = 0; i < 16; i += 2 * NF) {
-          const int n = tile * kNT + c0 + i;
-          const int b = n / (2 * NF);
-          if (b >= batch) break;
-          double2 a[NF];
+          for (int i = 0; i < 16; i += 2 * NF) {
+            const int n = tile * kNT + c0 + i;
+            const int b = n / (2 * NF);
+            if (b >= batch) break;
+            double2 a[NF];
 #pragma unroll
-          for (int f = 0; f < NF; ++f) {
-            a[f].x = scaled_to_double(combine_levels(acc[i + 2 * f]), Et + ec[c0 + i + 2 * f] - kOut);
-            a[f].y = scaled_to_double(combine_levels(acc[i + 2 * f + 1]), Et + ec[c0 + i + 2 * f + 1] - kOut);
-            // (analysis output feeds the FP64 epilogue: exact 64-bit recombination)
+            for (int f = 0; f < NF; ++f) {
+              a[f].x = scaled_to_double(combine_levels(acc[i + 2 * f]), Et + ec[c0 + i + 2 * f] - kOut);
+              a[f].y = scaled_to_double(combine_levels(acc[i + 2 * f + 1]), Et + ec[c0 + i + 2 * f + 1] - kOut);
+              // (analysis output feeds the FP64 epilogue: exact 64-bit recombination)
+            }
+            epi.finish(b, m + t, m, a);
           }
-          epi.finish(b, m + t, m, a);
+        } else {
+#pragma unroll
+          for (int i = 0; i < 16; i += 2) {
+            const int n = tile * kNT + c0 + i;
+            const int bf = n >> 1;
+            const int b = bf / NF, f = bf - b * NF;
+            if (b >= batch) break;
+            double2 a;
+            a.x = scaled_to_double(combine_levels(acc[i]), Et + ec[c0 + i] - kOut);
+            a.y = scaled_to_double(combine_levels(acc[i + 1]), Et + ec[c0 + i + 1] - kOut);
+            epi.finish_field(b, f, m + t, m, a);
+          }
         }
       }
     }
-    // slots l < m of column m for this tile's members
-    const int mb0 = tile * kNT / (2 * NF), mb1 = min(batch, (tile + 1) * kNT / (2 * NF));
+    // slots l < m of column m for the members this tile touches
+    const int mb0 = tile * kNT / (2 * NF), mb1 = min(batch, ((tile + 1) * kNT + 2 * NF - 1) / (2 * NF));
     for (int idx = threadIdx.x; idx < (mb1 - mb0) * m; idx += blockDim.x) epi.zero(mb0 + idx / m, idx % m, m);
   }
   tc_end(tmem);

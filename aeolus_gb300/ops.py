@@ -304,6 +304,131 @@ def swe_invariants(plan_id: int, radius: float, omega: float, gravity: float, me
     return out.reshape(lead + (5,))
 
 
+# ------------------------------------------------------------ adjoints
+@torch.library.custom_op("aeolus::synthesize_adjoint", mutates_args=())
+def synthesize_adjoint(plan_id: int, grid_bar: torch.Tensor) -> torch.Tensor:
+    """S^T grid_bar (the backward of synthesize)."""
+    p = _PLANS[plan_id]
+    _require_cuda(grid_bar, "grid adjoint")
+    if grid_bar.shape[-1] != p.n_points:
+        raise ValueError(f"expected [..., {p.n_points}] grid values, got {tuple(grid_bar.shape)}")
+    lead = tuple(grid_bar.shape[:-1])
+    g = grid_bar.to(torch.float64).contiguous().reshape(-1, p.n_points)
+    B = g.shape[0]
+    out = torch.empty((B,) + _spec_shape(p.lmax), dtype=torch.complex128, device=g.device)
+    if B:
+        w = p.workspace(_lib.OP_SYNTHESIZE_ADJOINT, B)
+        check(_lib.load().aeolus_synthesize_adjoint(p.handle, _ptr(g), _ptr(out), B, _ptr(w), w.numel(),
+                                                    _stream(g.device)))
+    return out.reshape(lead + _spec_shape(p.lmax))
+
+
+@torch.library.custom_op("aeolus::analyze_adjoint", mutates_args=())
+def analyze_adjoint(plan_id: int, coeffs_bar: torch.Tensor) -> torch.Tensor:
+    """A^T coeffs_bar (the backward of analyze)."""
+    p = _PLANS[plan_id]
+    c, lead = _flat_spec(coeffs_bar, p.lmax)
+    B = c.shape[0]
+    out = torch.empty((B, p.n_points), dtype=torch.float64, device=c.device)
+    if B:
+        w = p.workspace(_lib.OP_ANALYZE_ADJOINT, B)
+        check(_lib.load().aeolus_analyze_adjoint(p.handle, _ptr(c), _ptr(out), B, _ptr(w), w.numel(),
+                                                 _stream(c.device)))
+    return out.reshape(lead + (p.n_points,))
+
+
+@torch.library.custom_op("aeolus::swe_tendency_adjoint", mutates_args=())
+def swe_tendency_adjoint(plan_id: int, radius: float, omega: float, gravity: float, mean_depth: float, nu4: float,
+                         state: torch.Tensor, tend_bar: torch.Tensor) -> torch.Tensor:
+    """(d tendency / d state)^T tend_bar."""
+    p = _PLANS[plan_id]
+    s, lead = _flat_spec(state, p.lmax, 3)
+    kb, _ = _flat_spec(tend_bar, p.lmax, 3)
+    out = torch.empty_like(s)
+    B = s.shape[0]
+    if B:
+        w = p.workspace(_lib.OP_SWE_TENDENCY_ADJOINT, B)
+        prm = _swe_params(radius, omega, gravity, mean_depth, nu4)
+        check(_lib.load().aeolus_swe_tendency_adjoint(p.handle, byref(prm), _ptr(s), _ptr(kb), _ptr(out), B,
+                                                      _ptr(w), w.numel(), _stream(s.device)))
+    return out.reshape(lead + (3,) + _spec_shape(p.lmax))
+
+
+@torch.library.custom_op("aeolus::bve_tendency_adjoint", mutates_args=())
+def bve_tendency_adjoint(plan_id: int, radius: float, omega: float, nu: float, zeta: torch.Tensor,
+                         tend_bar: torch.Tensor) -> torch.Tensor:
+    p = _PLANS[plan_id]
+    z, lead = _flat_spec(zeta, p.lmax)
+    kb, _ = _flat_spec(tend_bar, p.lmax)
+    out = torch.empty_like(z)
+    B = z.shape[0]
+    if B:
+        w = p.workspace(_lib.OP_BVE_TENDENCY_ADJOINT, B)
+        prm = _bve_params(radius, omega, nu)
+        check(_lib.load().aeolus_bve_tendency_adjoint(p.handle, byref(prm), _ptr(z), _ptr(kb), _ptr(out), B,
+                                                      _ptr(w), w.numel(), _stream(z.device)))
+    return out.reshape(lead + _spec_shape(p.lmax))
+
+
+@torch.library.custom_op("aeolus::swe_rk4_adjoint", mutates_args=())
+def swe_rk4_adjoint(plan_id: int, radius: float, omega: float, gravity: float, mean_depth: float, nu4: float,
+                    state: torch.Tensor, state_bar: torch.Tensor, dt: float) -> torch.Tensor:
+    """Adjoint of one RK4 step taken from `state`: maps the adjoint of the
+    step's output to that of its input."""
+    p = _PLANS[plan_id]
+    s, lead = _flat_spec(state, p.lmax, 3)
+    yb = _flat_spec(state_bar, p.lmax, 3)[0].clone()
+    B = s.shape[0]
+    if B:
+        w = p.workspace(_lib.OP_SWE_RK4_ADJOINT, B)
+        prm = _swe_params(radius, omega, gravity, mean_depth, nu4)
+        check(_lib.load().aeolus_swe_rk4_adjoint(p.handle, byref(prm), _ptr(s), _ptr(yb), B, float(dt), _ptr(w),
+                                                 w.numel(), _stream(s.device)))
+    return yb.reshape(lead + (3,) + _spec_shape(p.lmax))
+
+
+@torch.library.custom_op("aeolus::bve_rk4_adjoint", mutates_args=())
+def bve_rk4_adjoint(plan_id: int, radius: float, omega: float, nu: float, zeta: torch.Tensor,
+                    zeta_bar: torch.Tensor, dt: float) -> torch.Tensor:
+    p = _PLANS[plan_id]
+    z, lead = _flat_spec(zeta, p.lmax)
+    yb = _flat_spec(zeta_bar, p.lmax)[0].clone()
+    B = z.shape[0]
+    if B:
+        w = p.workspace(_lib.OP_BVE_RK4_ADJOINT, B)
+        prm = _bve_params(radius, omega, nu)
+        check(_lib.load().aeolus_bve_rk4_adjoint(p.handle, byref(prm), _ptr(z), _ptr(yb), B, float(dt), _ptr(w),
+                                                 w.numel(), _stream(z.device)))
+    return yb.reshape(lead + _spec_shape(p.lmax))
+
+
+# Autograd: the backward of each transform is its hand-written transpose.
+def _synth_setup(ctx, inputs, output):
+    ctx.plan_id = inputs[0]
+
+
+def _synth_backward(ctx, grad):
+    return None, synthesize_adjoint(ctx.plan_id, grad.contiguous())
+
+
+def _anal_backward(ctx, grad):
+    return None, analyze_adjoint(ctx.plan_id, grad.contiguous())
+
+
+def _synth_adj_backward(ctx, grad):
+    return None, synthesize(ctx.plan_id, grad.contiguous())
+
+
+def _anal_adj_backward(ctx, grad):
+    return None, analyze(ctx.plan_id, grad.contiguous())
+
+
+torch.library.register_autograd("aeolus::synthesize", _synth_backward, setup_context=_synth_setup)
+torch.library.register_autograd("aeolus::analyze", _anal_backward, setup_context=_synth_setup)
+torch.library.register_autograd("aeolus::synthesize_adjoint", _synth_adj_backward, setup_context=_synth_setup)
+torch.library.register_autograd("aeolus::analyze_adjoint", _anal_adj_backward, setup_context=_synth_setup)
+
+
 def f10(omega: float) -> float:
     """Spectral (1,0) coefficient of f = 2 Omega sin(lat), barotropic.py:59-61."""
     return 2.0 * omega * math.sqrt(4.0 * math.pi / 3.0)

@@ -133,7 +133,43 @@ def run_reference(args):
 
 
 # ------------------------------------------------------------ clocks
+class _Nvml:
+    """Read-only NVML queries through ctypes (SM clock, max SM clock, clock
+    event reasons), polled from a thread every few milliseconds so that a
+    timed region of ~0.1 s still gets dozens of samples."""
+    SW_POWER_CAP, HW_SLOWDOWN, SW_THERMAL, HW_THERMAL = 0x4, 0x8, 0x20, 0x40
+
+    def __init__(self, torch_index: int):
+        import ctypes
+        self.ct = ctypes
+        self.lib = ctypes.CDLL("libnvidia-ml.so.1")
+        if self.lib.nvmlInit_v2() != 0:
+            raise RuntimeError("nvmlInit failed")
+        self.h = ctypes.c_void_p()
+        import torch
+        uuid = str(getattr(torch.cuda.get_device_properties(torch_index), "uuid", ""))
+        ok = False
+        if uuid:
+            key = uuid if uuid.startswith("GPU-") else "GPU-" + uuid
+            ok = self.lib.nvmlDeviceGetHandleByUUID(key.encode(), ctypes.byref(self.h)) == 0
+        if not ok and self.lib.nvmlDeviceGetHandleByIndex_v2(torch_index, ctypes.byref(self.h)) != 0:
+            raise RuntimeError("no NVML handle")
+        fn = getattr(self.lib, "nvmlDeviceGetCurrentClocksEventReasons", None)
+        self.reasons_fn = fn or self.lib.nvmlDeviceGetCurrentClocksThrottleReasons
+
+    def sample(self):
+        ct = self.ct
+        clk, mx, rs = ct.c_uint(), ct.c_uint(), ct.c_ulonglong()
+        if self.lib.nvmlDeviceGetClockInfo(self.h, 1, ct.byref(clk)) != 0:
+            return None
+        self.lib.nvmlDeviceGetMaxClockInfo(self.h, 1, ct.byref(mx))
+        self.reasons_fn(self.h, ct.byref(rs))
+        return clk.value, mx.value, rs.value
+
+
 class ClockSampler:
+    """SM clock and clock-event reasons during the timed region: NVML polled
+    every 2 ms when libnvidia-ml loads, else nvidia-smi at 200 ms."""
     FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
               "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
               "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
@@ -141,9 +177,28 @@ class ClockSampler:
     def __init__(self, index: int):
         self.index = index
         self.proc = None
+        self.nvml = None
+        self.samples = []
         self.path = ROOT / "gpurun_out" / f"clocks_rank{index}.csv"
 
+    def _poll(self):
+        while not self._stop.is_set():
+            v = self.nvml.sample()
+            if v is not None:
+                self.samples.append(v)
+            self._stop.wait(0.002)
+
     def __enter__(self):
+        import threading
+        try:
+            self.nvml = _Nvml(self.index)
+        except Exception:
+            self.nvml = None
+        if self.nvml is not None:
+            self._stop = threading.Event()
+            self._thr = threading.Thread(target=self._poll, daemon=True)
+            self._thr.start()
+            return self
         try:
             self.path.parent.mkdir(exist_ok=True)
             self.fh = open(self.path, "w")
@@ -155,6 +210,9 @@ class ClockSampler:
         return self
 
     def __exit__(self, *exc):
+        if self.nvml is not None:
+            self._stop.set()
+            self._thr.join(timeout=5)
         if self.proc is not None:
             self.proc.terminate()
             try:
@@ -164,10 +222,17 @@ class ClockSampler:
             self.fh.close()
 
     def summary(self):
+        names = {_Nvml.HW_SLOWDOWN: "hw_slowdown", _Nvml.HW_THERMAL: "hw_thermal_slowdown",
+                 _Nvml.SW_THERMAL: "sw_thermal_slowdown", _Nvml.SW_POWER_CAP: "sw_power_cap"}
+        if self.samples:
+            reasons = sorted({nm for _, _, r in self.samples for bit, nm in names.items() if r & bit})
+            return {"sm_mhz": statistics.median(c for c, _, _ in self.samples),
+                    "sm_max_mhz": max(m for _, m, _ in self.samples), "reasons": reasons,
+                    "samples": len(self.samples), "source": "nvml 2 ms"}
         if self.proc is None or not self.path.exists():
             return None
         sm, smax, reasons = [], None, set()
-        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        order = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
         for line in self.path.read_text().splitlines():
             parts = [p.strip() for p in line.split(",")]
             if len(parts) < 9:
@@ -177,13 +242,13 @@ class ClockSampler:
                 smax = float(parts[2])
             except ValueError:
                 continue
-            for name, val in zip(names, parts[5:9]):
+            for name, val in zip(order, parts[5:9]):
                 if val.lower().startswith("active"):
                     reasons.add(name)
         if not sm:
             return None
         return {"sm_mhz": statistics.median(sm), "sm_max_mhz": smax, "reasons": sorted(reasons),
-                "samples": len(sm)}
+                "samples": len(sm), "source": "nvidia-smi 200 ms"}
 
 
 # ------------------------------------------------------------ GPU arm

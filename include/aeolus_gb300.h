@@ -60,7 +60,13 @@ enum aeolus_op {
   AEOLUS_OP_BVE_RK4 = 6,
   AEOLUS_OP_SWE_RK4 = 7,
   AEOLUS_OP_SWE_VALIDATE = 8,
-  AEOLUS_OP_SWE_INVARIANTS = 9
+  AEOLUS_OP_SWE_INVARIANTS = 9,
+  AEOLUS_OP_SYNTHESIZE_ADJOINT = 10,
+  AEOLUS_OP_ANALYZE_ADJOINT = 11,
+  AEOLUS_OP_BVE_TENDENCY_ADJOINT = 12,
+  AEOLUS_OP_SWE_TENDENCY_ADJOINT = 13,
+  AEOLUS_OP_BVE_RK4_ADJOINT = 14,
+  AEOLUS_OP_SWE_RK4_ADJOINT = 15
 };
 
 /* SWE state-check bits (physics/shallow_water.py:494-539). */
@@ -236,6 +242,55 @@ int aeolus_bve_spectral_diagnostics(int lmax, double radius, double omega,
 int aeolus_swe_invariants(aeolus_plan state_plan, const aeolus_swe_params* p,
                           const double* state, double* out, int batch,
                           void* work, size_t work_bytes, void* stream);
+
+/* ---- adjoints (differentiation) ----------------------------------------
+ * The reference differentiates nothing; these are the transposes of the
+ * linear maps above and the vector-Jacobian products of the tendencies and
+ * RK4 steps, for gradients through the forward model.  Inner products: a
+ * spectral array is the real vector of the (Re, Im) parts of its m <= l
+ * slots (m > l slots are written as zero), a grid array the real vector of
+ * its values.  Each VJP is the exact transpose of the linearisation of the
+ * FP64 forward map (planetary vorticity inside the products); on a split-
+ * precision plan the contractions run in split precision. */
+
+/* coeffs_bar = S^T grid_bar, S = aeolus_synthesize (a unit-weight analysis:
+ * factor 2 on m > 0, Im of m = 0 zero). */
+int aeolus_synthesize_adjoint(aeolus_plan plan, const double* grid_bar,
+                              double* coeffs_bar, int batch, void* work,
+                              size_t work_bytes, void* stream);
+
+/* grid_bar = A^T coeffs_bar, A = aeolus_analyze (a synthesis of the m > 0
+ * slots halved, times the quadrature weight of each point). */
+int aeolus_analyze_adjoint(aeolus_plan plan, const double* coeffs_bar,
+                           double* grid_bar, int batch, void* work,
+                           size_t work_bytes, void* stream);
+
+/* zeta_bar = (d tendency / d zeta)^T tend_bar at zeta (aeolus_bve_tendency
+ * without forcing; the forcing does not depend on zeta). */
+int aeolus_bve_tendency_adjoint(aeolus_plan plan, const aeolus_bve_params* p,
+                                const double* zeta, const double* tend_bar,
+                                double* zeta_bar, int batch, void* work,
+                                size_t work_bytes, void* stream);
+
+/* state_bar = (d tendency / d state)^T tend_bar at state
+ * (aeolus_swe_tendency). */
+int aeolus_swe_tendency_adjoint(aeolus_plan plan, const aeolus_swe_params* p,
+                                const double* state, const double* tend_bar,
+                                double* state_bar, int batch, void* work,
+                                size_t work_bytes, void* stream);
+
+/* Adjoint of ONE RK4 step taken from `zeta` / `state` (the step's input,
+ * unchanged): on entry *_bar holds the adjoint of the step's output, on exit
+ * that of its input.  The stage inputs are recomputed from the step input;
+ * multi-step gradients checkpoint step inputs on the host side. */
+int aeolus_bve_rk4_adjoint(aeolus_plan plan, const aeolus_bve_params* p,
+                           const double* zeta, double* zeta_bar, int batch,
+                           double dt, void* work, size_t work_bytes,
+                           void* stream);
+int aeolus_swe_rk4_adjoint(aeolus_plan plan, const aeolus_swe_params* p,
+                           const double* state, double* state_bar, int batch,
+                           double dt, void* work, size_t work_bytes,
+                           void* stream);
 
 #ifdef __cplusplus
 }
