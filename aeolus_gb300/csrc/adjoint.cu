@@ -173,7 +173,7 @@ __global__ void swe_adjoint_finish_kernel(Spec s, double phi0, double nu4, const
   if (m <= l) {
     const double2* vb = vbar + (long)b * 9 * n2;
     auto V = [&](int f, int ll) -> double2 { return (ll < 0 || ll > L) ? z0 : vb[f * n2 + (long)ll * (L + 1) + m]; };
-    const double ir = 1.0 / s.R;
+    const double ir = s.ir;
     // U = snt(psi)/R + dlam(chi), V = dlam(psi) - snt(chi)/R
     const double2 psib = csub(cscale(ir, s.snt_t(V(0, l - 1), V(0, l + 1), l, m)), s.dlam(V(1, l), m));
     const double2 chib = csub(make_double2(0.0, 0.0),
@@ -259,7 +259,7 @@ __global__ void bve_adjoint_finish_kernel(Spec s, double nu, const double2* __re
   if (m <= l) {
     const double2* vb = vbar + (long)b * 4 * n2;
     auto V = [&](int f, int ll) -> double2 { return (ll < 0 || ll > L) ? z0 : vb[f * n2 + (long)ll * (L + 1) + m]; };
-    const double ir = 1.0 / s.R;
+    const double ir = s.ir;
     // v0 = dlam(psi), v1 = snt(psi)/R, v2 = dlam(zeta), v3 = snt(zeta + f)/R
     const double2 psib = csub(cscale(ir, s.snt_t(V(1, l - 1), V(1, l + 1), l, m)), s.dlam(V(0, l), m));
     const double il = l == 0 ? 0.0 : (s.invlap ? s.invlap[l] : 1.0 / s.lap(l));

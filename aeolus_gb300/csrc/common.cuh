@@ -93,6 +93,7 @@ struct aeolus_plan_impl {
   int precision = AEOLUS_PREC_FP64;
   int slices = 0;
   int device = 0;
+  int sm_count = 1;  // streaming multiprocessors of `device` (persistent grids)
   FftInfo fft{};
   // device tables (Gauss)
   double* x = nullptr;       // [nlat] cos(colatitude) = sin(latitude)
@@ -104,6 +105,8 @@ struct aeolus_plan_impl {
   double2* tw = nullptr;     // [nlon] exp(-2 pi i q / nlon)
   float4* twdf = nullptr;    // [nlon] the same twiddles as double-float (re.hi, re.lo, im.hi, im.lo)
   double* invlap = nullptr;  // [L+1] 1 / (-l(l+1)/R^2), 0 at l = 0 (radius of the plan)
+  double* xa = nullptr;      // [(L+1)^2] x Y_lm = xa_lm Y_{l+1,m} + xb_lm Y_{l-1,m}
+  double* xb = nullptr;      // [(L+1)^2]
   // device tables (points)
   double* basis = nullptr;   // [npoints][ncol] real basis (cos / sin columns)
   double* wpts = nullptr;    // [npoints] quadrature weights

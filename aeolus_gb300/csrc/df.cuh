@@ -47,6 +47,13 @@ __device__ __forceinline__ df df_add_fast(df a, df b) {
   return fast_two_sum(s.hi, s.lo);
 }
 
+// df + float: two-sum of the high words, the low word folded in once.
+__device__ __forceinline__ df df_add_f(df a, float b) {
+  df s = two_sum(a.hi, b);
+  s.lo += a.lo;
+  return fast_two_sum(s.hi, s.lo);
+}
+
 __device__ __forceinline__ df df_neg(df a) { return df{-a.hi, -a.lo}; }
 __device__ __forceinline__ df df_sub(df a, df b) { return df_add(a, df_neg(b)); }
 

@@ -25,9 +25,9 @@ struct JacDerive {  // a_lam, a_snt, b_lam, b_snt
     const double2 zero = make_double2(0.0, 0.0);
     const int L = s.L;
     v[0] = s.dlam(s.at(a, l, m), m);
-    v[1] = cscale(1.0 / s.R, s.snt(l >= 1 ? s.at(a, l - 1, m) : zero, l + 1 <= L ? s.at(a, l + 1, m) : zero, l, m));
+    v[1] = cscale(s.ir, s.snt(l >= 1 ? s.at(a, l - 1, m) : zero, l + 1 <= L ? s.at(a, l + 1, m) : zero, l, m));
     v[2] = s.dlam(s.at(c, l, m), m);
-    v[3] = cscale(1.0 / s.R, s.snt(l >= 1 ? s.at(c, l - 1, m) : zero, l + 1 <= L ? s.at(c, l + 1, m) : zero, l, m));
+    v[3] = cscale(s.ir, s.snt(l >= 1 ? s.at(c, l - 1, m) : zero, l + 1 <= L ? s.at(c, l + 1, m) : zero, l, m));
   }
 };
 
@@ -55,12 +55,12 @@ struct WindDerive {  // U = S(psi)/R + (im/R) chi,  V = (im/R) psi - S(chi)/R
     const double2 zero = make_double2(0.0, 0.0);
     const int L = s.L;
     const double2* p = psi + off;
-    double2 U = cscale(1.0 / s.R, s.snt(l >= 1 ? s.at(p, l - 1, m) : zero, l + 1 <= L ? s.at(p, l + 1, m) : zero, l, m));
+    double2 U = cscale(s.ir, s.snt(l >= 1 ? s.at(p, l - 1, m) : zero, l + 1 <= L ? s.at(p, l + 1, m) : zero, l, m));
     double2 V = s.dlam(s.at(p, l, m), m);
     if (chi) {
       const double2* c = chi + off;
       U = cadd(U, s.dlam(s.at(c, l, m), m));
-      V = csub(V, cscale(1.0 / s.R, s.snt(l >= 1 ? s.at(c, l - 1, m) : zero, l + 1 <= L ? s.at(c, l + 1, m) : zero, l, m)));
+      V = csub(V, cscale(s.ir, s.snt(l >= 1 ? s.at(c, l - 1, m) : zero, l + 1 <= L ? s.at(c, l + 1, m) : zero, l, m)));
     }
     v[0] = U;
     v[1] = V;
@@ -114,7 +114,7 @@ struct WindPhiDerive {
     const double2* d = z + n2;
     const double2 zero = make_double2(0.0, 0.0);
     const bool lo = l >= 1, hi = l + 1 <= L;
-    const double ir = 1.0 / s.R;
+    const double ir = s.ir;
     const double2 psi = s.invlap0(z, l, m), chi = s.invlap0(d, l, m);
     const double2 psi_lo = lo ? s.invlap0(z, l - 1, m) : zero, psi_hi = hi ? s.invlap0(z, l + 1, m) : zero;
     const double2 chi_lo = lo ? s.invlap0(d, l - 1, m) : zero, chi_hi = hi ? s.invlap0(d, l + 1, m) : zero;

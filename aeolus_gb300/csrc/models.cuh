@@ -20,10 +20,13 @@ constexpr double kFourPi = 12.56637061435917295384;
 struct Spec {  // shared spectral context
   int L;
   double R;
+  double ir, ir2;        // 1 / R, 1 / R^2 (no FP64 divides on the device)
   const double* cplus;   // [(L+1)^2], C+[L][:] = 0
   const double* cminus;  // [(L+1)^2]
   const double* invlap;  // [L+1] 1 / lap(l), 0 at l = 0
-  __device__ double lap(int l) const { return -(double)l * (l + 1.0) / (R * R); }
+  const double* xa;      // [(L+1)^2] x-multiplication coefficients (see xmul)
+  const double* xb;
+  __device__ double lap(int l) const { return -(double)l * (l + 1.0) * ir2; }
   __device__ double2 at(const double2* a, int l, int m) const { return a[(long)l * (L + 1) + m]; }
   // Helmholtz inverse with l = 0 -> 0 (physics/barotropic.py:91); a
   // multiplication by the tabulated reciprocal (within 1 ulp of the divide).
@@ -39,7 +42,7 @@ struct Spec {  // shared spectral context
   }
   // (i m / R) v
   __device__ double2 dlam(double2 v, int m) const {
-    const double mr = (double)m / R;
+    const double mr = (double)m * ir;
     return make_double2(-mr * v.y, mr * v.x);
   }
   // (x q)_lm, x = cos(colatitude) = sin(latitude):
@@ -47,11 +50,10 @@ struct Spec {  // shared spectral context
   //   a_lm = sqrt(((l+1)^2 - m^2)/((2l+1)(2l+3))), b_lm = sqrt((l^2 - m^2)/((2l-1)(2l+1)))
   // (C+_lm = l a_lm and C-_lm = -(l+1) b_lm of the sin(theta) d/dtheta coupling).
   __device__ double2 xmul(double2 lo, double2 hi, int l, int m) const {
-    // a_{l-1,m} = C+_{l-1,m} / (l-1),  b_{l+1,m} = -C-_{l+1,m} / (l+2)
+    // a_{l-1,m} = C+_{l-1,m} / (l-1) (a_00 = 1/sqrt(3)),  b_{l+1,m} = -C-_{l+1,m} / (l+2), tabulated
     double2 g = make_double2(0.0, 0.0);
-    if (l >= 2 && l - 1 >= m) g = cadd(g, cscale(cplus[(long)(l - 1) * (L + 1) + m] / (l - 1.0), lo));
-    if (l == 1 && m == 0) g = cadd(g, cscale(0.57735026918962576451, lo));  // a_00 = 1/sqrt(3)
-    if (l + 1 <= L) g = cadd(g, cscale(-cminus[(long)(l + 1) * (L + 1) + m] / (l + 2.0), hi));
+    if (l >= 1 && l - 1 >= m) g = cadd(g, cscale(xa[(long)(l - 1) * (L + 1) + m], lo));
+    if (l + 1 <= L) g = cadd(g, cscale(xb[(long)(l + 1) * (L + 1) + m], hi));
     return g;
   }
   // sin(theta) d/dtheta coupling of a column given its values at l-1, l+1
@@ -91,9 +93,9 @@ struct BveDerive {  // psi_lam, psi_snt, eta_lam, eta_snt
       if (l + 1 == 1) eta_hi.x += f10;
     }
     v[0] = s.dlam(psi, m);
-    v[1] = cscale(1.0 / s.R, s.snt(psi_lo, psi_hi, l, m));
+    v[1] = cscale(s.ir, s.snt(psi_lo, psi_hi, l, m));
     v[2] = s.dlam(s.at(z, l, m), m);
-    v[3] = cscale(1.0 / s.R, s.snt(eta_lo, eta_hi, l, m));
+    v[3] = cscale(s.ir, s.snt(eta_lo, eta_hi, l, m));
   }
 };
 
@@ -183,7 +185,7 @@ struct SweDerive {
     const double2* ph = d + n2;
     const double2 zero = make_double2(0.0, 0.0);
     const bool lo = l >= 1, hi = l + 1 <= L;
-    const double ir = 1.0 / s.R;
+    const double ir = s.ir;
     // psi, chi (l = 0 zero) at l-1, l, l+1
     const double2 psi = s.invlap0(z, l, m), chi = s.invlap0(d, l, m);
     const double2 psi_lo = lo ? s.invlap0(z, l - 1, m) : zero, psi_hi = hi ? s.invlap0(z, l + 1, m) : zero;
@@ -275,7 +277,7 @@ struct SweEpi {
       const double2* z = state + (long)b * 3 * n2;
       const double2* d = z + n2;
       const bool lo = l >= 1, hi = l + 1 <= L;
-      const double ir = 1.0 / s.R;
+      const double ir = s.ir;
       const double2 psi = s.invlap0(z, l, m), chi = s.invlap0(d, l, m);
       const double2 psi_lo = lo ? s.invlap0(z, l - 1, m) : z0, psi_hi = hi ? s.invlap0(z, l + 1, m) : z0;
       const double2 chi_lo = lo ? s.invlap0(d, l - 1, m) : z0, chi_hi = hi ? s.invlap0(d, l + 1, m) : z0;
@@ -317,7 +319,8 @@ struct SweEpi {
 // The reciprocal table is tabulated with the plan's radius; a call with a
 // different radius must not use it.
 Spec make_spec(const aeolus_plan_impl* p, double R) {
-  return Spec{p->lmax, R, p->cplus, p->cminus, R == p->radius ? p->invlap : nullptr};
+  return Spec{p->lmax, R, 1.0 / R, 1.0 / (R * R), p->cplus, p->cminus, R == p->radius ? p->invlap : nullptr,
+              p->xa, p->xb};
 }
 
 // ---------------------------------------------------------- helpers

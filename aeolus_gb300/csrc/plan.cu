@@ -281,12 +281,23 @@ int common_tables(aeolus_plan_impl* p) {
   if ((s = upload(&p->cplus, cp))) return s;
   if ((s = upload(&p->cminus, cm))) return s;
   if ((s = upload(&p->cplus_true, cpt))) return s;
+  // x = cos(colatitude) multiplication coefficients: xa_lm = C+_lm / l
+  // (xa_00 = 1/sqrt(3)), xb_lm = -C-_lm / (l + 1), from the unclipped C+.
+  const int n = p->lmax + 1;
+  std::vector<double> xa((size_t)n * n, 0.0), xb((size_t)n * n, 0.0);
+  for (int l = 0; l < n; ++l)
+    for (int m = 0; m <= l; ++m) {
+      xa[(size_t)l * n + m] = l == 0 ? 0.57735026918962576451 : cpt[(size_t)l * n + m] / l;
+      xb[(size_t)l * n + m] = -cm[(size_t)l * n + m] / (l + 1.0);
+    }
+  if ((s = upload(&p->xa, xa))) return s;
+  if ((s = upload(&p->xb, xb))) return s;
   return AEOLUS_OK;
 }
 
 void free_plan(aeolus_plan_impl* p) {
   double* bufs[] = {p->x, p->wq, p->coslat, p->fgrid, p->P, p->PT, p->basis, p->wpts,
-                    p->latp, p->cplus, p->cminus, p->cplus_true, p->invlap};
+                    p->latp, p->cplus, p->cminus, p->cplus_true, p->invlap, p->xa, p->xb};
   for (double* b : bufs)
     if (b) cudaFree(b);
   if (p->tw) cudaFree(p->tw);
@@ -379,6 +390,7 @@ extern "C" int aeolus_plan_create_gauss(int nlat, int nlon, int lmax, double rad
   p->npoints = (long)nlat * nlon;
   p->radius = radius;
   cudaGetDevice(&p->device);
+  cudaDeviceGetAttribute(&p->sm_count, cudaDevAttrMultiProcessorCount, p->device);
   plan_fft(nlon, lmax, p->fft);
   int s = AEOLUS_OK;
   auto bail = [&](int st) { free_plan(p); delete p; return st; };
@@ -452,6 +464,7 @@ extern "C" int aeolus_plan_create_points(long n, const double* lat, const double
   p->radius = radius;
   p->ncol = (lmax + 1) * (lmax + 1);
   cudaGetDevice(&p->device);
+  cudaDeviceGetAttribute(&p->sm_count, cudaDevAttrMultiProcessorCount, p->device);
   auto bail = [&](int st) { free_plan(p); delete p; return st; };
   std::vector<double> hw(n), hlat(lat, lat + n), hcos(n), hf(n);
   for (long i = 0; i < n; ++i) {

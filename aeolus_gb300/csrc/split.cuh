@@ -17,8 +17,6 @@ constexpr int kLevels = 6;   // kept levels k = s + t = 2..7 (1-based digits)
 constexpr int kAccs = 7;     // TMEM accumulators: the 6-pair top level is split in two
 constexpr int kNT = 32;      // data columns per tensor-core tile (MMA N)
 constexpr int kKC = 16;      // contraction depth per pipeline chunk (one MMA K step)
-constexpr int kStages = 3;   // shared-memory pipeline depth (chunks in flight)
-constexpr int kTmemCols = 256;  // kAccs * kNT = 224 columns, two CTAs per SM
 constexpr int kShift = 8 * kSlices;  // X = rint(x 2^(kShift - E))
 constexpr int kMaxKp = 128;  // degrees per order (l_max <= 127)
 
@@ -211,7 +209,7 @@ __device__ inline float pow2f(int p) { return __int_as_float((p + 127) << 23); }
 __device__ inline df levels_to_df(const float* acc, int e) {
   df s = two_sum(acc[kLevels], acc[kLevels - 1]);
 #pragma unroll
-  for (int k = kLevels - 2; k >= 0; --k) s = df_add(s, df{acc[k] * pow2f(8 * (kLevels - 1 - k)), 0.f});
+  for (int k = kLevels - 2; k >= 0; --k) s = df_add_f(s, acc[k] * pow2f(8 * (kLevels - 1 - k)));
   // s * 2^e, e = e1 + e2 with both factors normal floats
   const int e1 = max(-126, min(127, e)), e2 = max(-126, min(127, e - e1));
   return df{s.hi * pow2f(e1) * pow2f(e2), s.lo * pow2f(e1) * pow2f(e2)};
@@ -388,199 +386,294 @@ __global__ void __launch_bounds__(256) split_anal_slice_kernel(SplitDims dm, int
   }
 }
 
-// ---------------------------------------------------- tensor-core mainloop
-// One CTA = one 128 x kNT output tile.  Warp 0 lane 0 produces: it streams
-// K chunks (kSlices basis tiles 128 x 16 + kSlices data tiles kNT x 16)
-// through kStages shared-memory stages with the TMA bulk-copy engine.  Warp
-// 1 lane 0 issues, per chunk, the 21 digit-pair MMAs into the level
-// accumulators and commits the stage back to the producer.  All waits are
-// bounded; an expired wait sets *err and the CTA skips its outputs.
+// ---------------------------------------------------- tensor-core kernels
+// Persistent warp-specialised GEMM: one CTA per SM walks a static list of
+// output tiles (tile t, t + gridDim.x, ...).  Each tile is a 128 x kNT
+// output block contracted over nchunks 16-deep K chunks; every chunk moves
+// kSlices basis tiles (128 x 16) and kSlices data tiles (kNT x 16) with two
+// TMA bulk copies.
+//   warp 0 lane 0   producer: streams chunks through kStages smem stages
+//                   (across tile boundaries);
+//   warp 1 lane 0   MMA issuer: per chunk the 21 digit-pair MMAs into the
+//                   kAccs level accumulators of one of two TMEM buffers;
+//   warps 2..9      epilogue: drain the other TMEM buffer while the next
+//                   tile's MMAs run; warp w reads TMEM lane quadrant w % 4
+//                   and the 16-column half (w - 2) / 4 of the tile.
+// Barriers: full/empty per stage (TMA bytes / MMA commit), tfull/tempty per
+// TMEM buffer (MMA commit / 8 epilogue-warp arrivals).  Every wait is
+// bounded: an expired wait sets *err and that role stops; the others then
+// time out in turn, copies in flight are waited for and TMEM is freed.
+constexpr int kStages = 6;          // smem pipeline depth (30 KB per stage)
+constexpr int kTmemBuf = 256;       // column offset of the second accumulator buffer
+constexpr int kTmemCols = 512;      // 2 x kAccs * kNT = 448 columns used
+constexpr int kEpiWarps = 8;        // two per TMEM lane quadrant
+constexpr int kTcThreads = 64 + 32 * kEpiWarps;
 constexpr size_t kStageBytesA = chunk_elems(128) * 2;
 constexpr size_t kStageBytesB = chunk_elems(kNT) * 2;
+constexpr size_t kStageBytes = kStageBytesA + kStageBytesB;
 
-// Stage buffers are addressed arithmetically (no pointer arrays indexed by
-// the runtime stage number, which would live in local memory).
-struct TcPipe {
-  char* stages;     // kStages x (A tile, B tile)
-  __device__ __nv_bfloat16* A(int st) const {
-    return reinterpret_cast<__nv_bfloat16*>(stages + (size_t)st * (kStageBytesA + kStageBytesB));
-  }
-  __device__ __nv_bfloat16* B(int st) const {
-    return reinterpret_cast<__nv_bfloat16*>(stages + (size_t)st * (kStageBytesA + kStageBytesB) + kStageBytesA);
-  }
-  uint64_t* full;   // [kStages]
-  uint64_t* empty;  // [kStages]
-  uint64_t* done;
-  uint32_t* tmem_slot;
+struct TcTile {
+  const __nv_bfloat16* A;  // chunk-major basis tile
+  const __nv_bfloat16* B;  // chunk-major data tile
+  int nchunks;
 };
 
-inline size_t tc_smem_bytes() {
-  // 1 KB alignment slack + stages + barriers; >= 77 KB so at most two CTAs
-  // (2 x 256 TMEM columns) are resident on an SM.
-  const size_t need = 1024 + kStages * (kStageBytesA + kStageBytesB) + 256;
-  return std::max<size_t>(need, 77 * 1024);
-}
+inline size_t tc_smem_bytes() { return 1024 + kStages * kStageBytes + 256; }
 
-__device__ inline void tc_carve(char* base, TcPipe& p) {
+struct TcSmem {
+  char* stages;
+  uint64_t* full;    // [kStages]
+  uint64_t* empty;   // [kStages]
+  uint64_t* tfull;   // [2]
+  uint64_t* tempty;  // [2]
+  uint64_t* done;
+  uint32_t* tmem_slot;
+  __device__ __nv_bfloat16* A(int st) const {
+    return reinterpret_cast<__nv_bfloat16*>(stages + (size_t)st * kStageBytes);
+  }
+  __device__ __nv_bfloat16* B(int st) const {
+    return reinterpret_cast<__nv_bfloat16*>(stages + (size_t)st * kStageBytes + kStageBytesA);
+  }
+};
+
+__device__ inline TcSmem tc_carve(char* base) {
+  TcSmem s;
   char* q = reinterpret_cast<char*>((reinterpret_cast<uintptr_t>(base) + 1023) & ~uintptr_t(1023));
-  p.stages = q;
-  q += kStages * (kStageBytesA + kStageBytesB);
+  s.stages = q;
+  q += kStages * kStageBytes;
   uint64_t* bars = reinterpret_cast<uint64_t*>(q);
-  p.full = bars;
-  p.empty = bars + kStages;
-  p.done = bars + 2 * kStages;
-  p.tmem_slot = reinterpret_cast<uint32_t*>(bars + 2 * kStages + 1);
+  s.full = bars;
+  s.empty = bars + kStages;
+  s.tfull = bars + 2 * kStages;
+  s.tempty = bars + 2 * kStages + 2;
+  s.done = bars + 2 * kStages + 4;
+  s.tmem_slot = reinterpret_cast<uint32_t*>(bars + 2 * kStages + 5);
+  return s;
 }
 
-// Runs the whole contraction; on return (all threads) the accumulators are
-// complete in TMEM, or the function returned false.
-__device__ inline bool tc_mainloop(TcPipe& p, const __nv_bfloat16* gA, const __nv_bfloat16* gB, int nchunks,
-                                   uint32_t tmem, int* err) {
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  bool ok = true;
-  if (warp == 0 && lane == 0) {  // producer
-    for (int kc = 0; kc < nchunks && ok; ++kc) {
-      const int st = kc % kStages;
-      if (kc >= kStages) ok = tc::mbar_wait(&p.empty[st], ((kc / kStages) - 1) & 1);
-      if (!ok) break;
-      tc::mbar_expect_tx(&p.full[st], (uint32_t)(kStageBytesA + kStageBytesB));
-      tc::bulk_g2s(p.A(st), gA + (long long)kc * chunk_elems(128), (uint32_t)kStageBytesA, &p.full[st]);
-      tc::bulk_g2s(p.B(st), gB + (long long)kc * chunk_elems(kNT), (uint32_t)kStageBytesB, &p.full[st]);
-    }
-    // no copy may still be in flight when the CTA ends: wait for the last loads
-    const int first = nchunks > kStages ? nchunks - kStages : 0;
-    for (int kc = first; kc < nchunks; ++kc)
-      if (!tc::mbar_wait(&p.full[kc % kStages], (kc / kStages) & 1)) ok = false;
-    if (!ok) atomicExch(err, 1);
-  } else if (warp == 1 && lane == 0) {  // MMA issuer
-    const uint32_t idesc = tc::idesc_bf16_f32(128, kNT);
-    unsigned started = 0u;
-    for (int kc = 0; kc < nchunks && ok; ++kc) {
-      const int st = kc % kStages;
-      ok = tc::mbar_wait(&p.full[st], (kc / kStages) & 1);
-      if (!ok) break;
-      tc::fence_after_sync();
-      for (int s = 0; s < kSlices; ++s) {
-        const uint64_t da = tc::smem_desc(p.A(st) + (long long)s * 128 * kKC, 128, kKC * 16);
-        for (int t = 0; s + t < kSlices; ++t) {
-          const int a = acc_of(s, t);
-          const uint64_t db = tc::smem_desc(p.B(st) + (long long)t * kNT * kKC, 128, kKC * 16);
-          tc::mma_bf16(tmem + (uint32_t)a * kNT, da, db, idesc, ((started >> a) & 1u) ? 1u : 0u);
-          started |= 1u << a;
-        }
-      }
-      tc::mma_commit(&p.empty[st]);
-    }
-    tc::mma_commit(p.done);
-    if (!ok) atomicExch(err, 3);
-  }
-  __syncwarp();
-  const bool done = tc::mbar_wait(p.done, 0);
-  if (!done && lane == 0) atomicExch(err, 2);
-  tc::fence_after_sync();
-  return __syncthreads_and((done && ok) ? 1 : 0) != 0;
-}
-
-__device__ inline void tc_begin(TcPipe& p) {
-  if (threadIdx.x == 0) {
-    for (int i = 0; i < 2 * kStages + 1; ++i) tc::mbar_init(&p.full[i], 1);
-    tc::fence_mbar_init();
-  }
-  __syncthreads();
-  if (threadIdx.x < 32) tc::tmem_alloc(p.tmem_slot, kTmemCols);
-  tc::fence_before_sync();
-  __syncthreads();
-  tc::fence_after_sync();
-}
-
-__device__ inline void tc_end(uint32_t tmem) {
-  tc::fence_before_sync();
-  __syncthreads();
-  if (threadIdx.x < 32) tc::tmem_dealloc(tmem, kTmemCols);
-}
-
-// The kAccs accumulators of 16 columns starting at c0 for this thread's
-// lane (the TMEM lane quadrant of its warp).
-__device__ inline void tc_read16(uint32_t tmem, int c0, float (*acc)[kAccs]) {
-  const uint32_t lane_base = (uint32_t)((threadIdx.x >> 5) * 32) << 16;
+// The kAccs accumulators of 16 columns starting at c0 for lane `lane` of the
+// TMEM quadrant q (the calling warp's own quadrant).
+__device__ inline void tc_read16(uint32_t tbuf, int q, int c0, float (*acc)[kAccs]) {
+  const uint32_t lane_base = (uint32_t)(q * 32) << 16;
   uint32_t r[16];
 #pragma unroll
   for (int k = 0; k < kAccs; ++k) {
-    tc::tmem_ld16(tmem + lane_base + (uint32_t)(k * kNT + c0), r);
+    tc::tmem_ld16(tbuf + lane_base + (uint32_t)(k * kNT + c0), r);
     tc::tmem_wait_ld();
 #pragma unroll
     for (int i = 0; i < 16; ++i) acc[i][k] = __uint_as_float(r[i]);
   }
 }
 
-// --------------------------------------------------------- synthesis GEMM
-// grid (m, latitude tile, data tile), 128 threads.  Writes double-float F
-// blocks (float4 per complex value).
-static __global__ void __launch_bounds__(128, 2) tc_synth_kernel(SplitDims dm, const long long* __restrict__ kcum,
-                                                                 const __nv_bfloat16* __restrict__ psyn,
-                                                                 const int* __restrict__ esyn,
-                                                                 const __nv_bfloat16* __restrict__ dsyn,
-                                                                 const int* __restrict__ ecol, int nf, int nblk,
-                                                                 float4* __restrict__ F, int* err) {
+// Sched: int count() const; TcTile tile(int t) const.
+// Epi:   void run(int t, uint32_t tbuf, int q, int row, int c0, int etid) const
+//        -- consumes columns [c0, c0 + 16) of the accumulators of tile t for
+//        TMEM lane row = q * 32 + lane (etid = epilogue thread 0..255).
+template <class Sched, class Epi>
+__global__ void __launch_bounds__(kTcThreads, 1) tc_persistent_kernel(Sched sc, Epi ep, int* err) {
   extern __shared__ char smem_raw[];
-  const int m = blockIdx.x, mt = blockIdx.y, tile = blockIdx.z;
-  const int L = dm.L, Kp = kpad(L + 1 - m);
-  TcPipe pp;
-  tc_carve(smem_raw, pp);
-  tc_begin(pp);
-  const uint32_t tmem = *pp.tmem_slot;
-  const bool ok = tc_mainloop(pp, psyn + psyn_tile(kcum, dm.Mt, m, mt, Kp), dsyn + dsyn_tile(kcum, dm, m, tile),
-                              Kp / kKC, tmem, err);
-  if (ok) {
-    const int j = mt * 128 + threadIdx.x;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const TcSmem sm = tc_carve(smem_raw);
+  if (threadIdx.x == 0) {
+    for (int i = 0; i < kStages; ++i) {
+      tc::mbar_init(&sm.full[i], 1);
+      tc::mbar_init(&sm.empty[i], 1);
+    }
+    for (int i = 0; i < 2; ++i) {
+      tc::mbar_init(&sm.tfull[i], 1);
+      tc::mbar_init(&sm.tempty[i], kEpiWarps);
+    }
+    tc::mbar_init(sm.done, 1);
+    tc::fence_mbar_init();
+  }
+  if (warp == 0) tc::tmem_alloc(sm.tmem_slot, kTmemCols);
+  tc::fence_before_sync();
+  __syncthreads();
+  tc::fence_after_sync();
+  const uint32_t tmem = *sm.tmem_slot;
+  const int ntiles = sc.count();
+
+  if (warp == 0) {
+    if (lane == 0) {  // ---------------- producer
+      bool ok = true;
+      uint32_t g = 0;
+      for (int t = blockIdx.x; t < ntiles && ok; t += gridDim.x) {
+        const TcTile tl = sc.tile(t);
+        for (int kc = 0; kc < tl.nchunks; ++kc) {
+          const int st = (int)(g % kStages);
+          const uint32_t u = g / kStages;
+          if (u > 0 && !tc::mbar_wait(&sm.empty[st], (u - 1) & 1)) {
+            ok = false;
+            break;
+          }
+          tc::mbar_expect_tx(&sm.full[st], (uint32_t)kStageBytes);
+          tc::bulk_g2s(sm.A(st), tl.A + (long long)kc * chunk_elems(128), (uint32_t)kStageBytesA, &sm.full[st]);
+          tc::bulk_g2s(sm.B(st), tl.B + (long long)kc * chunk_elems(kNT), (uint32_t)kStageBytesB, &sm.full[st]);
+          ++g;
+        }
+      }
+      // no copy may still be in flight when the CTA ends
+      for (uint32_t h = g > (uint32_t)kStages ? g - kStages : 0; h < g; ++h)
+        if (!tc::mbar_wait(&sm.full[h % kStages], (h / kStages) & 1)) ok = false;
+      if (!ok) atomicExch(err, 1);
+    }
+  } else if (warp == 1) {
+    if (lane == 0) {  // ---------------- MMA issuer
+      bool ok = true;
+      const uint32_t idesc = tc::idesc_bf16_f32(128, kNT);
+      uint32_t g = 0;
+      int i = 0;
+      for (int t = blockIdx.x; t < ntiles && ok; t += gridDim.x, ++i) {
+        const TcTile tl = sc.tile(t);
+        const int buf = i & 1;
+        const uint32_t ub = (uint32_t)i >> 1;
+        if (ub > 0 && !tc::mbar_wait(&sm.tempty[buf], (ub - 1) & 1)) {
+          ok = false;
+          break;
+        }
+        tc::fence_after_sync();
+        const uint32_t dbase = tmem + (uint32_t)(buf * kTmemBuf);
+        unsigned started = 0u;
+        for (int kc = 0; kc < tl.nchunks; ++kc, ++g) {
+          const int st = (int)(g % kStages);
+          if (!tc::mbar_wait(&sm.full[st], (g / kStages) & 1)) {
+            ok = false;
+            break;
+          }
+          tc::fence_after_sync();
+          for (int s = 0; s < kSlices; ++s) {
+            const uint64_t da = tc::smem_desc(sm.A(st) + (long long)s * 128 * kKC, 128, kKC * 16);
+            for (int u = 0; s + u < kSlices; ++u) {
+              const int a = acc_of(s, u);
+              const uint64_t db = tc::smem_desc(sm.B(st) + (long long)u * kNT * kKC, 128, kKC * 16);
+              tc::mma_bf16(dbase + (uint32_t)a * kNT, da, db, idesc, ((started >> a) & 1u) ? 1u : 0u);
+              started |= 1u << a;
+            }
+          }
+          tc::mma_commit(&sm.empty[st]);
+        }
+        if (!ok) break;
+        tc::mma_commit(&sm.tfull[buf]);
+      }
+      // every MMA issued has completed before TMEM is released
+      tc::mma_commit(sm.done);
+      if (!tc::mbar_wait(sm.done, 0)) ok = false;
+      if (!ok) atomicExch(err, 3);
+    }
+  } else {  // ------------------------ epilogue warps 2..9
+    const int q = warp & 3;
+    const int c0 = ((warp - 2) >> 2) * 16;
+    const int etid = (warp - 2) * 32 + lane;
+    int i = 0;
+    for (int t = blockIdx.x; t < ntiles; t += gridDim.x, ++i) {
+      const int buf = i & 1;
+      const uint32_t ub = (uint32_t)i >> 1;
+      // lane 0 waits and the warp follows its verdict, so the warp stays
+      // converged for the .sync.aligned TMEM loads
+      int ready = 0;
+      if (lane == 0) ready = tc::mbar_wait(&sm.tfull[buf], ub & 1) ? 1 : 0;
+      ready = __shfl_sync(0xffffffffu, ready, 0);
+      if (!ready) {
+        if (lane == 0) atomicExch(err, 2);
+        break;
+      }
+      tc::fence_after_sync();
+      ep.run(t, tmem + (uint32_t)(buf * kTmemBuf), q, q * 32 + lane, c0, etid);
+      tc::fence_before_sync();
+      __syncwarp();
+      if (lane == 0) tc::mbar_arrive(&sm.tempty[buf]);
+    }
+  }
+  // reconverge each warp (lanes 1..31 of warps 0 and 1 wait here for their
+  // lane 0) before the CTA barrier and the warp-wide TMEM release
+  __syncwarp();
+  tc::fence_before_sync();
+  __syncthreads();
+  if (warp == 0) tc::tmem_dealloc(tmem, kTmemCols);
+}
+
+// --------------------------------------------------------- synthesis GEMM
+// Tiles (m, latitude tile, data tile), m-major so tiles of equal depth are
+// adjacent (largest depth first: a greedy balance of the static schedule).
+struct SynthSched {
+  SplitDims dm;
+  const long long* kcum;
+  const __nv_bfloat16* psyn;
+  const __nv_bfloat16* dsyn;
+  __device__ int count() const { return (dm.L + 1) * dm.Mt * dm.ntiles; }
+  __device__ TcTile tile(int t) const {
+    const int per_m = dm.Mt * dm.ntiles;
+    const int m = t / per_m, r = t - m * per_m;
+    const int mt = r / dm.ntiles, nt = r - mt * dm.ntiles;
+    const int Kp = kpad(dm.L + 1 - m);
+    return TcTile{psyn + psyn_tile(kcum, dm.Mt, m, mt, Kp), dsyn + dsyn_tile(kcum, dm, m, nt), Kp / kKC};
+  }
+};
+
+// Writes double-float F blocks (float4 per complex value).
+struct SynthEpi {
+  SplitDims dm;
+  const int* esyn;
+  const int* ecol;
+  int nf, nblk;
+  float4* F;
+  __device__ void run(int t, uint32_t tbuf, int q, int row, int c0, int) const {
+    const int per_m = dm.Mt * dm.ntiles;
+    const int m = t / per_m, r = t - m * per_m;
+    const int mt = r / dm.ntiles, tile = r - mt * dm.ntiles;
+    const int L = dm.L;
+    const int j = mt * 128 + row;
     const int Ej = j < dm.nlat ? esyn[m * dm.Mt * 128 + j] : 0;
     const int* ec = ecol + (long long)m * dm.ntiles * kNT + tile * kNT;
-    for (int c0 = 0; c0 < kNT; c0 += 16) {
-      float acc[16][kAccs];
-      tc_read16(tmem, c0, acc);
-      if (j < dm.nlat) {
+    float acc[16][kAccs];
+    tc_read16(tbuf, q, c0, acc);
+    if (j < dm.nlat) {
 #pragma unroll
-        for (int i = 0; i < 16; i += 2) {
-          const int n = tile * kNT + c0 + i;  // even: real part, n + 1: imaginary part
-          if (n >= dm.ncol) break;
-          const df re = levels_to_df(acc[i], Ej + ec[c0 + i] - kOut);
-          const df im = levels_to_df(acc[i + 1], Ej + ec[c0 + i + 1] - kOut);
-          const int bf = n >> 1;
-          const int b = bf / nf, f = bf - b * nf;
-          F[(((long long)b * dm.nlat + j) * nblk + f) * (L + 1) + m] = make_float4(re.hi, re.lo, im.hi, im.lo);
-        }
+      for (int i = 0; i < 16; i += 2) {
+        const int n = tile * kNT + c0 + i;  // even: real part, n + 1: imaginary part
+        if (n >= dm.ncol) break;
+        const df re = levels_to_df(acc[i], Ej + ec[c0 + i] - kOut);
+        const df im = levels_to_df(acc[i + 1], Ej + ec[c0 + i + 1] - kOut);
+        const int bf = n >> 1;
+        const int b = bf / nf, f = bf - b * nf;
+        F[(((long long)b * dm.nlat + j) * nblk + f) * (L + 1) + m] = make_float4(re.hi, re.lo, im.hi, im.lo);
       }
     }
   }
-  tc_end(tmem);
-}
+};
 
 // --------------------------------------------------------- analysis GEMM
-// grid (m, data tile), 128 threads; lane = degree offset l - m.
+struct AnalSched {
+  SplitDims dm;
+  const __nv_bfloat16* pana;
+  const __nv_bfloat16* dana;
+  __device__ int count() const { return (dm.L + 1) * dm.ntiles; }
+  __device__ TcTile tile(int t) const {
+    const int m = t / dm.ntiles, nt = t - m * dm.ntiles;
+    return TcTile{pana + pana_tile(dm.NK, m), dana + dana_tile(dm, m, nt), dm.NK / kKC};
+  }
+};
+
+// Row = degree offset l - m.  Exact 64-bit level recombination, FP64
+// epilogue functor (whole members: Epi::finish; else Epi::finish_field).
 template <class Epi>
-__global__ void __launch_bounds__(128, 2) tc_anal_kernel(SplitDims dm, const __nv_bfloat16* __restrict__ pana,
-                                                         const int* __restrict__ eana,
-                                                         const __nv_bfloat16* __restrict__ dana,
-                                                         const int* __restrict__ ecol, int batch, Epi epi, int* err) {
-  constexpr int NF = Epi::NF;
-  // Whole members per 16-column chunk -> Epi::finish(b, l, m, a[NF]);
-  // otherwise (NF = 9, ...) one field at a time -> Epi::finish_field.
-  constexpr bool kWhole = 16 % (2 * NF) == 0;
-  extern __shared__ char smem_raw[];
-  const int m = blockIdx.x, tile = blockIdx.y;
-  const int L = dm.L, K = L + 1 - m;
-  TcPipe pp;
-  tc_carve(smem_raw, pp);
-  tc_begin(pp);
-  const uint32_t tmem = *pp.tmem_slot;
-  const bool ok = tc_mainloop(pp, pana + pana_tile(dm.NK, m), dana + dana_tile(dm, m, tile), dm.NK / kKC, tmem, err);
-  const int t = threadIdx.x;
-  if (ok) {
+struct AnalEpi {
+  SplitDims dm;
+  const int* eana;
+  const int* ecol;
+  int batch;
+  Epi epi;
+  __device__ void run(int tt, uint32_t tbuf, int q, int row, int c0, int etid) const {
+    constexpr int NF = Epi::NF;
+    constexpr bool kWhole = 16 % (2 * NF) == 0;
+    const int m = tt / dm.ntiles, tile = tt - m * dm.ntiles;
+    const int K = dm.L + 1 - m;
+    const int t = row;
     const int Et = eana[m * 128 + t];
     const int* ec = ecol + (long long)m * dm.ntiles * kNT + tile * kNT;
-    for (int c0 = 0; c0 < kNT; c0 += 16) {
+    {
       float acc[16][kAccs];
-      tc_read16(tmem, c0, acc);
+      tc_read16(tbuf, q, c0, acc);
       if (t < K) {
         if constexpr (kWhole) {
 #pragma unroll
@@ -593,7 +686,6 @@ __global__ void __launch_bounds__(128, 2) tc_anal_kernel(SplitDims dm, const __n
             for (int f = 0; f < NF; ++f) {
               a[f].x = scaled_to_double(combine_levels(acc[i + 2 * f]), Et + ec[c0 + i + 2 * f] - kOut);
               a[f].y = scaled_to_double(combine_levels(acc[i + 2 * f + 1]), Et + ec[c0 + i + 2 * f + 1] - kOut);
-              // (analysis output feeds the FP64 epilogue: exact 64-bit recombination)
             }
             epi.finish(b, m + t, m, a);
           }
@@ -614,10 +706,11 @@ __global__ void __launch_bounds__(128, 2) tc_anal_kernel(SplitDims dm, const __n
     }
     // slots l < m of column m for the members this tile touches
     const int mb0 = tile * kNT / (2 * NF), mb1 = min(batch, ((tile + 1) * kNT + 2 * NF - 1) / (2 * NF));
-    for (int idx = threadIdx.x; idx < (mb1 - mb0) * m; idx += blockDim.x) epi.zero(mb0 + idx / m, idx % m, m);
+    for (int idx = etid; idx < (mb1 - mb0) * m; idx += 32 * kEpiWarps) epi.zero(mb0 + idx / m, idx % m, m);
   }
-  tc_end(tmem);
-}
+};
+
+inline int tc_grid(const aeolus_plan_impl* p, int ntiles) { return std::max(1, std::min(ntiles, p->sm_count)); }
 
 // ------------------------------------------------------------ launchers
 inline SplitDims split_dims(const aeolus_plan_impl* p, int ncol) {
@@ -662,11 +755,12 @@ int launch_split_synth(const aeolus_plan_impl* p, const Derive& d, double2* FG, 
     AE_LAUNCH("split_synth_slice_kernel");
   }
   const size_t sm2 = tc_smem_bytes();
-  if ((s = allow_smem(tc_synth_kernel, sm2))) return s;
+  auto k2 = tc_persistent_kernel<SynthSched, SynthEpi>;
+  if ((s = allow_smem(k2, sm2))) return s;
+  const SynthSched sc{dm, p->split->kcum, p->split->psyn, dsyn};
+  const SynthEpi ep{dm, p->split->esyn, ecol, NF, nblk, reinterpret_cast<float4*>(FG)};
   ProfScope prof("tc_synth_bf16x6", st);
-  tc_synth_kernel<<<dim3(dm.L + 1, dm.Mt, dm.ntiles), 128, sm2, st>>>(dm, p->split->kcum, p->split->psyn,
-                                                                      p->split->esyn, dsyn, ecol, NF, nblk,
-                                                                      reinterpret_cast<float4*>(FG), p->split->err);
+  k2<<<tc_grid(p, (dm.L + 1) * dm.Mt * dm.ntiles), kTcThreads, sm2, st>>>(sc, ep, p->split->err);
   AE_LAUNCH("tc_synth_kernel");
   return AEOLUS_OK;
 }
@@ -692,11 +786,12 @@ int launch_split_anal(const aeolus_plan_impl* p, const Epi& e, const double2* FG
     AE_LAUNCH("split_anal_slice_kernel");
   }
   const size_t sm2 = tc_smem_bytes();
-  auto k2 = tc_anal_kernel<Epi>;
+  auto k2 = tc_persistent_kernel<AnalSched, AnalEpi<Epi>>;
   if ((s = allow_smem(k2, sm2))) return s;
+  const AnalSched sc{dm, p->split->pana, dana};
+  const AnalEpi<Epi> ep{dm, p->split->eana, ecol, batch, e};
   ProfScope prof("tc_anal_bf16x6", st);
-  k2<<<dim3(dm.L + 1, dm.ntiles), 128, sm2, st>>>(dm, p->split->pana, p->split->eana, dana, ecol, batch, e,
-                                                   p->split->err);
+  k2<<<tc_grid(p, (dm.L + 1) * dm.ntiles), kTcThreads, sm2, st>>>(sc, ep, p->split->err);
   AE_LAUNCH("tc_anal_kernel");
   return AEOLUS_OK;
 }
