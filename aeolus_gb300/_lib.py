@@ -82,6 +82,15 @@ SIGNATURES = {
                                        c_size_t, c_void_p]),
     "aeolus_swe_rk4_adjoint": (c_int, [c_void_p, POINTER(SweParams), c_void_p, c_void_p, c_int, c_double, c_void_p,
                                        c_size_t, c_void_p]),
+    "aeolus_ensemble_create": (c_int, [c_int, POINTER(c_void_p), POINTER(c_int), POINTER(BveParams),
+                                       POINTER(c_void_p)]),
+    "aeolus_ensemble_destroy": (c_int, [c_void_p]),
+    "aeolus_ensemble_workspace_bytes": (c_int, [c_void_p, POINTER(c_size_t)]),
+    "aeolus_ensemble_bve_rk4": (c_int, [c_void_p, POINTER(c_void_p), c_double, c_int, c_void_p, c_size_t, c_void_p]),
+    "aeolus_ensemble_capture": (c_int, [c_void_p, POINTER(c_void_p), c_double, c_void_p, c_size_t, c_void_p]),
+    "aeolus_ensemble_launch": (c_int, [c_void_p, c_int, c_void_p]),
+    "aeolus_ensemble_autotune": (c_int, [c_void_p, POINTER(c_void_p), c_void_p, c_size_t, c_void_p, c_char_p,
+                                         c_size_t]),
 }
 
 _lib = None

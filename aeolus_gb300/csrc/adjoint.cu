@@ -449,7 +449,7 @@ extern "C" int aeolus_swe_rk4_adjoint(aeolus_plan plan, const aeolus_swe_params*
   // forward stage inputs, with the same functors (and precision form) as aeolus_swe_rk4
   const bool spec_cor = plan->precision == AEOLUS_PREC_SPLIT_BF16;
   const double fp = spec_cor ? 0.0 : f10;
-  SwePw pw{fp, phi0};
+  SwePw pw{fp, phi0, (float)phi0};
   double2* next[3] = {y1, y2, y3};
   const double2* in = y0;
   for (int stage = 1; stage <= 3; ++stage) {

@@ -32,7 +32,9 @@ struct ProfScope {
   cudaStream_t st = nullptr;
   cudaEvent_t a = nullptr;
   ProfScope(const char* n, cudaStream_t s) {
-    if (prof_enabled()) {
+    // no timing events inside a stream capture (they would become graph nodes)
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    if (prof_enabled() && cudaStreamIsCapturing(s, &cs) == cudaSuccess && cs == cudaStreamCaptureStatusNone) {
       name = n;
       st = s;
       a = prof_event();
@@ -94,6 +96,10 @@ struct aeolus_plan_impl {
   int slices = 0;
   int device = 0;
   int sm_count = 1;  // streaming multiprocessors of `device` (persistent grids)
+  // launch shapes chosen by the autotuner (0: built-in heuristics): members
+  // per CTA of the FP64 Legendre synthesis / analysis, threads of the row
+  // stage, members per CTA of the split-path slicing kernels
+  int tune_bc_synth = 0, tune_bc_anal = 0, tune_row_threads = 0, tune_slice_mb = 0;
   FftInfo fft{};
   // device tables (Gauss)
   double* x = nullptr;       // [nlat] cos(colatitude) = sin(latitude)

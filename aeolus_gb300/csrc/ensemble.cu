@@ -1,0 +1,578 @@
+// Batched uneven ensemble of BVE members: groups of members on Gauss plans
+// of different l_max advanced together.  Every RK4 stage launches each stage
+// kernel ONCE for all groups (a block-to-group table maps each CTA -- or, in
+// the persistent tensor-core kernels, each tile -- to its group), a whole RK4
+// step can be captured into a CUDA graph and replayed, and an autotuner times
+// candidate launch shapes per group and keeps the fastest.
+//
+// Reference: the run loop of run/bve/runner.py:211-216 applied to many
+// independent states; the reference has no batched or grouped form.
+#include <algorithm>
+#include <cstdio>
+#include <string>
+#include <vector>
+
+#include "models.cuh"
+
+struct aeolus_ensemble_s {
+  int ng = 0;
+  aeolus_plan plan[8] = {};
+  int batch[8] = {};
+  aeolus_bve_params prm[8] = {};
+  int split = 0;
+  int device = 0;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+};
+
+namespace aeolus {
+namespace {
+
+constexpr int kMaxGroups = 8;
+
+// Per-group block ranges of a grouped launch: CTA b belongs to the group k
+// with start[k] <= b < start[k + 1]; inside it, bx = local % gx, by = local / gx.
+template <class Arg>
+struct Grouped {
+  int n;
+  int start[kMaxGroups + 1];
+  int gx[kMaxGroups];
+  int gy[kMaxGroups];
+  Arg arg[kMaxGroups];
+  __device__ int find(int b) const {
+    int k = 0;
+    while (k + 1 < n && b >= start[k + 1]) ++k;
+    return k;
+  }
+};
+
+template <class Arg>
+void grouped_add(Grouped<Arg>& g, const Arg& a, dim3 grid) {
+  const int k = g.n++;
+  g.arg[k] = a;
+  g.gx[k] = (int)grid.x;
+  g.gy[k] = (int)grid.y;
+  g.start[k + 1] = g.start[k] + (int)(grid.x * grid.y);
+}
+
+template <class Derive>
+struct SynthArg {
+  LegArgs a;
+  Derive d;
+};
+template <class Epi>
+struct AnalArg {
+  LegArgs a;
+  Epi e;
+};
+template <class Pw>
+struct RowArg {
+  RowArgs a;
+  Pw pw;
+  const float4* twdf;
+};
+template <class Derive>
+struct SliceSynthArg {
+  SplitDims dm;
+  const long long* kcum;
+  int batch, mb;
+  Derive d;
+  __nv_bfloat16* digits;
+  int* ecol;
+};
+struct SliceAnalArg {
+  SplitDims dm;
+  int batch, mb, nblk;
+  const float4* FG;
+  __nv_bfloat16* digits;
+  int* ecol;
+};
+
+template <class Derive, int CPT>
+__global__ void __launch_bounds__(256) g_legendre_synth(Grouped<SynthArg<Derive>> g) {
+  const int k = g.find(blockIdx.x);
+  const int loc = blockIdx.x - g.start[k];
+  legendre_synth_body<Derive, CPT>(g.arg[k].a, g.arg[k].d, loc % g.gx[k], loc / g.gx[k]);
+}
+
+template <class Epi>
+__global__ void __launch_bounds__(256) g_legendre_analysis(Grouped<AnalArg<Epi>> g) {
+  const int k = g.find(blockIdx.x);
+  const int loc = blockIdx.x - g.start[k];
+  legendre_analysis_body<Epi>(g.arg[k].a, g.arg[k].e, loc % g.gx[k], loc / g.gx[k]);
+}
+
+template <class Pw>
+__global__ void __launch_bounds__(256) g_rows(Grouped<RowArg<Pw>> g) {
+  const int k = g.find(blockIdx.x);
+  const int loc = blockIdx.x - g.start[k];
+  row_body<Pw, kInF, kOutG>(g.arg[k].a, g.arg[k].pw, loc % g.gx[k], loc / g.gx[k]);
+}
+
+template <class Pw>
+__global__ void __launch_bounds__(256) g_rows_df(Grouped<RowArg<Pw>> g, DfConst kc) {
+  const int k = g.find(blockIdx.x);
+  const int loc = blockIdx.x - g.start[k];
+  row_df_body<Pw, kInF, kOutG>(g.arg[k].a, g.arg[k].pw, g.arg[k].twdf, kc, loc % g.gx[k], loc / g.gx[k]);
+}
+
+template <class Derive>
+__global__ void __launch_bounds__(256) g_slice_synth(Grouped<SliceSynthArg<Derive>> g) {
+  const int k = g.find(blockIdx.x);
+  const int loc = blockIdx.x - g.start[k];
+  const SliceSynthArg<Derive>& a = g.arg[k];
+  split_synth_slice_body<Derive>(a.dm, a.kcum, a.batch, a.mb, a.d, a.digits, a.ecol, loc % g.gx[k], loc / g.gx[k],
+                                 g.gy[k]);
+}
+
+template <int NF>
+__global__ void __launch_bounds__(256) g_slice_anal(Grouped<SliceAnalArg> g) {
+  const int k = g.find(blockIdx.x);
+  const int loc = blockIdx.x - g.start[k];
+  const SliceAnalArg& a = g.arg[k];
+  split_anal_slice_body<NF>(a.dm, a.batch, a.mb, a.nblk, a.FG, a.digits, a.ecol, loc % g.gx[k], loc / g.gx[k],
+                            g.gy[k]);
+}
+
+// Persistent tensor-core tiles of all groups in one list.
+template <class Sched>
+struct GroupedSched {
+  int n;
+  int start[kMaxGroups + 1];
+  Sched s[kMaxGroups];
+  __device__ int find(int t) const {
+    int k = 0;
+    while (k + 1 < n && t >= start[k + 1]) ++k;
+    return k;
+  }
+  __device__ int count() const { return start[n]; }
+  __device__ TcTile tile(int t) const {
+    const int k = find(t);
+    return s[k].tile(t - start[k]);
+  }
+};
+
+template <class Sched, class Epi>
+struct GroupedEpi {
+  static constexpr int kWarps = Epi::kWarps, kCols = Epi::kCols;
+  GroupedSched<Sched> gs;  // for the tile -> group map
+  Epi e[kMaxGroups];
+  __device__ void run(int t, uint32_t tbuf, int q, int row, int c0, int etid) const {
+    const int k = gs.find(t);
+    e[k].run(t - gs.start[k], tbuf, q, row, c0, etid);
+  }
+};
+
+// Workspace of one group: chain scratch, stage input, RK4 accumulator.
+size_t group_bytes(const aeolus_plan_impl* p, int batch) {
+  return align256(full_chain_bytes<4, 1>(p, batch)) + 2 * align256(state_bytes(p, 1, batch));
+}
+
+struct GroupBufs {
+  char* chain;
+  double2* ystage;
+  double2* acc;
+};
+
+GroupBufs group_bufs(const aeolus_plan_impl* p, int batch, char* base) {
+  GroupBufs b;
+  b.chain = base;
+  base += align256(full_chain_bytes<4, 1>(p, batch));
+  b.ystage = reinterpret_cast<double2*>(base);
+  base += align256(state_bytes(p, 1, batch));
+  b.acc = reinterpret_cast<double2*>(base);
+  return b;
+}
+
+size_t ens_bytes(const aeolus_ensemble_s* e) {
+  size_t n = 0;
+  for (int k = 0; k < e->ng; ++k) n += group_bytes(e->plan[k], e->batch[k]);
+  return n;
+}
+
+// One RK4 stage of every group: 3 (FP64) or 5 (split) grouped launches.
+int ens_stage(const aeolus_ensemble_s* E, double2* const* y0, int stage, double dt, char* work, cudaStream_t st) {
+  const int ng = E->ng;
+  BveDerive der[kMaxGroups];
+  BveEpi epi[kMaxGroups];
+  GroupBufs gb[kMaxGroups];
+  char* w = work;
+  for (int k = 0; k < ng; ++k) {
+    const aeolus_plan_impl* p = E->plan[k];
+    gb[k] = group_bufs(p, E->batch[k], w);
+    w += group_bytes(p, E->batch[k]);
+    const Spec sp = make_spec(p, E->prm[k].radius);
+    const double2* in = stage == 1 ? y0[k] : gb[k].ystage;
+    der[k] = BveDerive{sp, in, 2.0 * E->prm[k].omega * kSqrt4PiOver3};
+    epi[k] = BveEpi{sp, in, nullptr, E->prm[k].viscosity, Rk4{stage, dt, y0[k], gb[k].ystage, gb[k].acc, nullptr}};
+  }
+  int s;
+  // rows (shared by both paths)
+  Grouped<RowArg<JacPw>> gr{};
+  size_t sm_rows = 0;
+  int row_thr = 0;
+  for (int k = 0; k < ng; ++k) {
+    const aeolus_plan_impl* p = E->plan[k];
+    RowArgs ra{};
+    ra.batch = E->batch[k];
+    ra.FG = reinterpret_cast<double2*>(gb[k].chain);
+    ra.nblk = 4;
+    row_args(p, ra);
+    grouped_add(gr, RowArg<JacPw>{ra, JacPw{}, p->twdf}, dim3(p->nlat, E->batch[k]));
+    sm_rows = std::max(sm_rows, row_smem_bytes<JacPw>(p->fft));
+    row_thr = std::max(row_thr, row_threads(p));
+  }
+  if (!E->split) {
+    Grouped<SynthArg<BveDerive>> gs{};
+    Grouped<AnalArg<BveEpi>> ga{};
+    size_t sm_s = 0, sm_a = 0;
+    int thr_s = 64, thr_a = 64;
+    for (int k = 0; k < ng; ++k) {
+      const aeolus_plan_impl* p = E->plan[k];
+      double2* FG = reinterpret_cast<double2*>(gb[k].chain);
+      const LegCfg cs = synth_cfg<BveDerive>(p, E->batch[k]);
+      const LegCfg ca = analysis_cfg<BveEpi>(p, E->batch[k]);
+      grouped_add(gs, SynthArg<BveDerive>{LegArgs{p->lmax, p->nlat, p->nh, E->batch[k], cs.bc, p->P, p->PT, FG, 4},
+                                          der[k]},
+                  cs.grid);
+      grouped_add(ga, AnalArg<BveEpi>{LegArgs{p->lmax, p->nlat, p->nh, E->batch[k], ca.bc, p->P, p->PT, FG, 4},
+                                      epi[k]},
+                  ca.grid);
+      sm_s = std::max(sm_s, cs.smem);
+      sm_a = std::max(sm_a, ca.smem);
+      thr_s = std::max(thr_s, cs.threads);
+      thr_a = std::max(thr_a, ca.threads);
+    }
+    auto k1 = g_legendre_synth<BveDerive, kSynthCPT>;
+    auto k2 = g_rows<JacPw>;
+    auto k3 = g_legendre_analysis<BveEpi>;
+    if ((s = allow_smem(k1, sm_s)) || (s = allow_smem(k2, sm_rows)) || (s = allow_smem(k3, sm_a))) return s;
+    {
+      ProfScope prof("ens_legendre_synth_f64", st);
+      k1<<<gs.start[ng], thr_s, sm_s, st>>>(gs);
+      AE_LAUNCH("g_legendre_synth");
+    }
+    {
+      ProfScope prof("ens_rows", st);
+      k2<<<gr.start[ng], row_thr, sm_rows, st>>>(gr);
+      AE_LAUNCH("g_rows");
+    }
+    ProfScope prof("ens_legendre_analysis_f64", st);
+    k3<<<ga.start[ng], thr_a, sm_a, st>>>(ga);
+    AE_LAUNCH("g_legendre_analysis");
+    return AEOLUS_OK;
+  }
+  // split precision
+  Grouped<SliceSynthArg<BveDerive>> gss{};
+  Grouped<SliceAnalArg> gsa{};
+  GroupedSched<SynthSched> tsyn{};
+  GroupedEpi<SynthSched, SynthEpi<4>> esyn{};
+  GroupedSched<AnalSched> tana{};
+  GroupedEpi<AnalSched, AnalEpi<BveEpi>> eana{};
+  size_t sm_ss = 0, sm_sa = 0;
+  int sm_count = 1, err_dev = 0;
+  int* err = nullptr;
+  for (int k = 0; k < ng; ++k) {
+    const aeolus_plan_impl* p = E->plan[k];
+    const int B = E->batch[k];
+    double2* FG = reinterpret_cast<double2*>(gb[k].chain);
+    void* scratch = gb[k].chain + align256(fg_bytes(p, 4, B));
+    const SplitParts r1 = split_synth_parts<4>(p, B, scratch);
+    const SplitParts r2 = split_anal_parts<1>(p, B, scratch);
+    grouped_add(gss, SliceSynthArg<BveDerive>{r1.dm, p->split->kcum, B, r1.mb, der[k], r1.digits, r1.ecol}, r1.grid);
+    grouped_add(gsa, SliceAnalArg{r2.dm, B, r2.mb, 4, reinterpret_cast<const float4*>(FG), r2.digits, r2.ecol},
+                r2.grid);
+    sm_ss = std::max(sm_ss, r1.smem);
+    sm_sa = std::max(sm_sa, r2.smem);
+    const SynthSched sc{r1.dm, p->split->kcum, p->split->psyn, r1.digits};
+    tsyn.s[k] = sc;
+    tsyn.start[k + 1] = tsyn.start[k] + sc.count_host();
+    esyn.e[k] = SynthEpi<4>{r1.dm, p->split->esyn, r1.ecol, 4, reinterpret_cast<float4*>(FG)};
+    const AnalSched sa{r2.dm, p->split->pana, r2.digits};
+    tana.s[k] = sa;
+    tana.start[k + 1] = tana.start[k] + sa.count_host();
+    eana.e[k] = AnalEpi<BveEpi>{r2.dm, p->split->eana, r2.ecol, B, epi[k]};
+    sm_count = std::max(sm_count, p->sm_count);
+    err = p->split->err;  // any group's flag: a device error marks every plan's kernels suspect
+    (void)err_dev;
+  }
+  tsyn.n = tana.n = ng;
+  esyn.gs = tsyn;
+  eana.gs = tana;
+  auto k1 = g_slice_synth<BveDerive>;
+  auto k2 = tc_persistent_kernel<GroupedSched<SynthSched>, GroupedEpi<SynthSched, SynthEpi<4>>>;
+  auto k3 = g_rows_df<JacPw>;
+  auto k4 = g_slice_anal<1>;
+  auto k5 = tc_persistent_kernel<GroupedSched<AnalSched>, GroupedEpi<AnalSched, AnalEpi<BveEpi>>>;
+  const size_t smt = tc_smem_bytes();
+  if ((s = allow_smem(k1, sm_ss)) || (s = allow_smem(k2, smt)) || (s = allow_smem(k3, sm_rows)) ||
+      (s = allow_smem(k4, sm_sa)) || (s = allow_smem(k5, smt)))
+    return s;
+  {
+    ProfScope prof("ens_split_synth_slice", st);
+    k1<<<gss.start[ng], 256, sm_ss, st>>>(gss);
+    AE_LAUNCH("g_slice_synth");
+  }
+  {
+    ProfScope prof("ens_tc_synth_bf16x6", st);
+    k2<<<std::max(1, std::min(tsyn.start[ng], sm_count)), tc_threads<GroupedEpi<SynthSched, SynthEpi<4>>>(), smt, st>>>(
+        tsyn, esyn, err);
+    AE_LAUNCH("tc_persistent_kernel(ensemble synthesis)");
+  }
+  {
+    ProfScope prof("ens_rows_df", st);
+    k3<<<gr.start[ng], row_thr, sm_rows, st>>>(gr, df_consts());
+    AE_LAUNCH("g_rows_df");
+  }
+  {
+    ProfScope prof("ens_split_anal_slice", st);
+    k4<<<gsa.start[ng], 256, sm_sa, st>>>(gsa);
+    AE_LAUNCH("g_slice_anal");
+  }
+  ProfScope prof("ens_tc_anal_bf16x6", st);
+  k5<<<std::max(1, std::min(tana.start[ng], sm_count)), tc_threads<GroupedEpi<AnalSched, AnalEpi<BveEpi>>>(), smt,
+     st>>>(tana, eana, err);
+  AE_LAUNCH("tc_persistent_kernel(ensemble analysis)");
+  return AEOLUS_OK;
+}
+
+int ens_step(const aeolus_ensemble_s* E, double2* const* y0, double dt, char* work, cudaStream_t st) {
+  for (int stage = 1; stage <= 4; ++stage) {
+    const int s = ens_stage(E, y0, stage, dt, work, st);
+    if (s) return s;
+  }
+  return AEOLUS_OK;
+}
+
+bool ens_ok(const aeolus_ensemble_s* e) { return e != nullptr && e->ng > 0 && e->ng <= kMaxGroups; }
+
+void drop_graph(aeolus_ensemble_s* e) {
+  if (e->exec) cudaGraphExecDestroy(e->exec);
+  if (e->graph) cudaGraphDestroy(e->graph);
+  e->exec = nullptr;
+  e->graph = nullptr;
+}
+
+// Times `reps` RK4 stages (stage 1, which leaves the state untouched) of the
+// ensemble on `st`, in ms per stage.
+int time_stage(const aeolus_ensemble_s* E, double2* const* y0, char* work, cudaStream_t st, int reps, float* ms) {
+  cudaEvent_t a, b;
+  AE_CUDA(cudaEventCreate(&a));
+  AE_CUDA(cudaEventCreate(&b));
+  int s = ens_stage(E, y0, 1, 0.0, work, st);  // warm-up
+  if (!s) {
+    cudaEventRecord(a, st);
+    for (int i = 0; i < reps && !s; ++i) s = ens_stage(E, y0, 1, 0.0, work, st);
+    cudaEventRecord(b, st);
+  }
+  if (!s) s = cuda_check(cudaEventSynchronize(b), "cudaEventSynchronize");
+  if (!s) {
+    cudaEventElapsedTime(ms, a, b);
+    *ms /= reps;
+  }
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  return s;
+}
+
+}  // namespace
+}  // namespace aeolus
+
+using namespace aeolus;
+
+extern "C" int aeolus_ensemble_create(int ngroups, const aeolus_plan* plans, const int* batch,
+                                      const aeolus_bve_params* params, aeolus_ensemble* out) {
+  if (!out || !plans || !batch || !params || ngroups < 1 || ngroups > kMaxGroups)
+    return fail(AEOLUS_ERR_ARG, "aeolus_ensemble_create: need 1.." + std::to_string(kMaxGroups) + " groups");
+  int prec = -1, dev = -1;
+  for (int k = 0; k < ngroups; ++k) {
+    const aeolus_plan_impl* p = plans[k];
+    if (!plan_ok(p) || p->kind != kGauss)
+      return fail(AEOLUS_ERR_ARG, "aeolus_ensemble_create: group " + std::to_string(k) + " needs a Gauss plan");
+    if (batch[k] < 1 || batch[k] > 65535)
+      return fail(AEOLUS_ERR_ARG, "aeolus_ensemble_create: group " + std::to_string(k) + " batch out of range");
+    int s = bve_check(plans[k], &params[k], "aeolus_ensemble_create");
+    if (s) return s;
+    if (prec >= 0 && p->precision != prec)
+      return fail(AEOLUS_ERR_ARG, "aeolus_ensemble_create: all groups must use the same contraction precision");
+    if (dev >= 0 && p->device != dev)
+      return fail(AEOLUS_ERR_ARG, "aeolus_ensemble_create: all groups must live on one device");
+    if (p->precision == AEOLUS_PREC_SPLIT_BF16 && !p->split)
+      return fail(AEOLUS_ERR_ARG, "aeolus_ensemble_create: split precision without split tables");
+    prec = p->precision;
+    dev = p->device;
+  }
+  auto* e = new aeolus_ensemble_s;
+  e->ng = ngroups;
+  for (int k = 0; k < ngroups; ++k) {
+    e->plan[k] = plans[k];
+    e->batch[k] = batch[k];
+    e->prm[k] = params[k];
+  }
+  e->split = prec == AEOLUS_PREC_SPLIT_BF16;
+  e->device = dev;
+  *out = e;
+  return AEOLUS_OK;
+}
+
+extern "C" int aeolus_ensemble_destroy(aeolus_ensemble e) {
+  if (!e) return AEOLUS_OK;
+  drop_graph(e);
+  delete e;
+  return AEOLUS_OK;
+}
+
+extern "C" int aeolus_ensemble_workspace_bytes(aeolus_ensemble e, size_t* bytes) {
+  if (!ens_ok(e) || !bytes) return fail(AEOLUS_ERR_ARG, "aeolus_ensemble_workspace_bytes: bad arguments");
+  *bytes = std::max<size_t>(ens_bytes(e), 256);
+  return AEOLUS_OK;
+}
+
+#define ENS_CHECK(who)                                                                                     \
+  do {                                                                                                     \
+    if (!ens_ok(e) || !zeta) return fail(AEOLUS_ERR_ARG, std::string(who) + ": bad arguments");           \
+    for (int k = 0; k < e->ng; ++k)                                                                        \
+      if (!zeta[k]) return fail(AEOLUS_ERR_ARG, std::string(who) + ": NULL state of group " + std::to_string(k)); \
+    if (!work || work_bytes < ens_bytes(e))                                                                \
+      return fail(AEOLUS_ERR_WORKSPACE, std::string(who) + ": workspace too small (" +                    \
+                                            std::to_string(ens_bytes(e)) + " bytes needed)");              \
+  } while (0)
+
+extern "C" int aeolus_ensemble_bve_rk4(aeolus_ensemble e, double* const* zeta, double dt, int nsteps, void* work,
+                                       size_t work_bytes, void* stream) {
+  ENS_CHECK("aeolus_ensemble_bve_rk4");
+  if (!std::isfinite(dt)) return fail(AEOLUS_ERR_ARG, "aeolus_ensemble_bve_rk4: dt must be finite");
+  double2* y[kMaxGroups];
+  for (int k = 0; k < e->ng; ++k) y[k] = reinterpret_cast<double2*>(zeta[k]);
+  const cudaStream_t st = static_cast<cudaStream_t>(stream);
+  for (int it = 0; it < nsteps; ++it) {
+    const int s = ens_step(e, y, dt, static_cast<char*>(work), st);
+    if (s) return s;
+  }
+  return AEOLUS_OK;
+}
+
+extern "C" int aeolus_ensemble_capture(aeolus_ensemble e, double* const* zeta, double dt, void* work,
+                                       size_t work_bytes, void* stream) {
+  ENS_CHECK("aeolus_ensemble_capture");
+  if (!stream) return fail(AEOLUS_ERR_ARG, "aeolus_ensemble_capture: the legacy default stream cannot be captured");
+  if (!std::isfinite(dt)) return fail(AEOLUS_ERR_ARG, "aeolus_ensemble_capture: dt must be finite");
+  drop_graph(e);
+  double2* y[kMaxGroups];
+  for (int k = 0; k < e->ng; ++k) y[k] = reinterpret_cast<double2*>(zeta[k]);
+  const cudaStream_t st = static_cast<cudaStream_t>(stream);
+  // Set every kernel attribute before capturing: a stage-1 pass (which only
+  // writes the workspace) runs uncaptured first.
+  int s = ens_stage(e, y, 1, dt, static_cast<char*>(work), st);
+  if (s) return s;
+  AE_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+  s = ens_step(e, y, dt, static_cast<char*>(work), st);
+  cudaGraph_t g = nullptr;
+  const cudaError_t ce = cudaStreamEndCapture(st, &g);
+  if (s) {
+    if (g) cudaGraphDestroy(g);
+    return s;
+  }
+  if (ce != cudaSuccess) return cuda_check(ce, "cudaStreamEndCapture");
+  cudaGraphExec_t x = nullptr;
+  const cudaError_t ie = cudaGraphInstantiate(&x, g, 0);
+  if (ie != cudaSuccess) {
+    cudaGraphDestroy(g);
+    return cuda_check(ie, "cudaGraphInstantiate");
+  }
+  e->graph = g;
+  e->exec = x;
+  return AEOLUS_OK;
+}
+
+extern "C" int aeolus_ensemble_launch(aeolus_ensemble e, int nsteps, void* stream) {
+  if (!ens_ok(e) || !e->exec) return fail(AEOLUS_ERR_ARG, "aeolus_ensemble_launch: no captured step");
+  const cudaStream_t st = static_cast<cudaStream_t>(stream);
+  for (int i = 0; i < nsteps; ++i) AE_CUDA(cudaGraphLaunch(e->exec, st));
+  return AEOLUS_OK;
+}
+
+// Autotuner: per group, candidate members-per-CTA counts of the FP64
+// Legendre kernels (or of the split slicing kernels), then the row-stage
+// thread count shared by the grouped row launch; each candidate is timed over
+// `reps` ensemble stages (stage 1 leaves the states untouched) and the
+// fastest kept in the plans.  Results never depend on these shapes.
+extern "C" int aeolus_ensemble_autotune(aeolus_ensemble e, double* const* zeta, void* work, size_t work_bytes,
+                                        void* stream, char* report, size_t report_len) {
+  ENS_CHECK("aeolus_ensemble_autotune");
+  drop_graph(e);  // a captured step would keep the old shapes
+  double2* y[kMaxGroups];
+  for (int k = 0; k < e->ng; ++k) y[k] = reinterpret_cast<double2*>(zeta[k]);
+  const cudaStream_t st = static_cast<cudaStream_t>(stream);
+  char* w = static_cast<char*>(work);
+  const int reps = 3;
+  std::string rep;
+  char line[256];
+  float base = 0.f;
+  int s = time_stage(e, y, w, st, reps, &base);
+  if (s) return s;
+  std::snprintf(line, sizeof(line), "default shapes: %.4f ms per stage\n", base);
+  rep += line;
+  const int cands[] = {1, 2, 3, 4, 6, 8};
+  for (int k = 0; k < e->ng; ++k) {
+    aeolus_plan_impl* p = e->plan[k];
+    if (!e->split) {
+      for (int which = 0; which < 2; ++which) {
+        int& knob = which == 0 ? p->tune_bc_synth : p->tune_bc_anal;
+        int best_v = knob;
+        float best = 1e30f;
+        for (int c : cands) {
+          if (c > e->batch[k]) break;
+          knob = c;
+          float ms = 0.f;
+          if ((s = time_stage(e, y, w, st, reps, &ms))) return s;
+          if (ms < best) {
+            best = ms;
+            best_v = c;
+          }
+        }
+        knob = best_v;
+        std::snprintf(line, sizeof(line), "group %d (l_max %d, %d members): %s members/CTA = %d (%.4f ms)\n", k,
+                      p->lmax, e->batch[k], which == 0 ? "synthesis" : "analysis", best_v, best);
+        rep += line;
+      }
+    } else {
+      int best_v = p->tune_slice_mb;
+      float best = 1e30f;
+      for (int c : cands) {
+        p->tune_slice_mb = c;
+        float ms = 0.f;
+        if ((s = time_stage(e, y, w, st, reps, &ms))) return s;
+        if (ms < best) {
+          best = ms;
+          best_v = c;
+        }
+      }
+      p->tune_slice_mb = best_v;
+      std::snprintf(line, sizeof(line), "group %d (l_max %d, %d members): slicing members/CTA = %d (%.4f ms)\n", k,
+                    p->lmax, e->batch[k], best_v, best);
+      rep += line;
+    }
+  }
+  {
+    const int thr[] = {128, 192, 256};
+    int best_v = 256;
+    float best = 1e30f;
+    for (int t : thr) {
+      for (int k = 0; k < e->ng; ++k) e->plan[k]->tune_row_threads = t;
+      float ms = 0.f;
+      if ((s = time_stage(e, y, w, st, reps, &ms))) return s;
+      if (ms < best) {
+        best = ms;
+        best_v = t;
+      }
+    }
+    for (int k = 0; k < e->ng; ++k) e->plan[k]->tune_row_threads = best_v;
+    std::snprintf(line, sizeof(line), "row stage: %d threads/CTA (%.4f ms per stage)\n", best_v, best);
+    rep += line;
+  }
+  if (report && report_len) {
+    std::snprintf(report, report_len, "%s", rep.c_str());
+  }
+  return AEOLUS_OK;
+}

@@ -28,15 +28,15 @@ struct LegArgs {
 inline int n_pairs(int L) { return L / 2 + 1; }
 
 template <class Derive, int CPT>
-__global__ void __launch_bounds__(256) legendre_synth_kernel(LegArgs a, Derive d) {
+__device__ __forceinline__ void legendre_synth_body(const LegArgs& a, const Derive& d, int bx, int by) {
   constexpr int NF = Derive::NF;
   extern __shared__ double2 s_a[];
   const int L = a.L, nh = a.nh, ldm = L + 1;
-  const int i = blockIdx.x;
+  const int i = bx;
   const int mA = i, mB = L - i;
   const bool two = mB != mA;
   const int KA = L + 1 - mA, KB = two ? L + 1 - mB : 0;
-  const int b0 = blockIdx.y * a.bc;
+  const int b0 = by * a.bc;
   const int nb = min(a.bc, a.batch - b0);
   const int ncols = nb * NF;
   const int ngroups = (ncols + CPT - 1) / CPT;
@@ -115,6 +115,11 @@ __global__ void __launch_bounds__(256) legendre_synth_kernel(LegArgs a, Derive d
 }
 
 template <class Derive, int CPT>
+__global__ void __launch_bounds__(256) legendre_synth_kernel(LegArgs a, Derive d) {
+  legendre_synth_body<Derive, CPT>(a, d, blockIdx.x, blockIdx.y);
+}
+
+template <class Derive, int CPT>
 inline size_t synth_smem_bytes(int L, int bc) {
   const int ncols = bc * Derive::NF;
   const int ncp = (ncols + CPT - 1) / CPT * CPT;
@@ -122,15 +127,15 @@ inline size_t synth_smem_bytes(int L, int bc) {
 }
 
 template <class Epi>
-__global__ void __launch_bounds__(256) legendre_analysis_kernel(LegArgs a, Epi e) {
+__device__ __forceinline__ void legendre_analysis_body(const LegArgs& a, const Epi& e, int bx, int by) {
   constexpr int NF = Epi::NF;
   extern __shared__ double2 s_g[];  // [2 orders][nb][NF][2 parities][nh]
   const int L = a.L, nh = a.nh, ldm = L + 1;
-  const int i = blockIdx.x;
+  const int i = bx;
   const int mA = i, mB = L - i;
   const bool two = mB != mA;
   const int KA = L + 1 - mA, KB = two ? L + 1 - mB : 0;
-  const int b0 = blockIdx.y * a.bc;
+  const int b0 = by * a.bc;
   const int nb = min(a.bc, a.batch - b0);
   const long per_order = (long)a.bc * NF * 2 * nh;
 
@@ -184,6 +189,11 @@ __global__ void __launch_bounds__(256) legendre_analysis_kernel(LegArgs a, Epi e
     if (r < mA) e.zero(b0 + bl, r, mA);
     else e.zero(b0 + bl, r - mA, mB);
   }
+}
+
+template <class Epi>
+__global__ void __launch_bounds__(256) legendre_analysis_kernel(LegArgs a, Epi e) {
+  legendre_analysis_body<Epi>(a, e, blockIdx.x, blockIdx.y);
 }
 
 template <class Epi>

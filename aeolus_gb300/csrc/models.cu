@@ -432,7 +432,7 @@ extern "C" int aeolus_swe_tendency(aeolus_plan plan, const aeolus_swe_params* p,
   const bool spec_cor = plan->precision == AEOLUS_PREC_SPLIT_BF16;
   const double fp = spec_cor ? 0.0 : f10;
   SweDerive d{sp, reinterpret_cast<const double2*>(state), fp};
-  SwePw pw{fp, phi0};
+  SwePw pw{fp, phi0, (float)phi0};
   Rk4 rk{0, 0.0, nullptr, nullptr, nullptr, reinterpret_cast<double2*>(tend)};
   SweEpi e{sp, reinterpret_cast<const double2*>(state), phi0, p->nu4, rk, spec_cor ? 2.0 * p->omega : 0.0};
   return run_full_chain(plan, d, pw, e, batch, work, nullptr, static_cast<cudaStream_t>(stream));
@@ -490,7 +490,7 @@ extern "C" int aeolus_swe_rk4(aeolus_plan plan, const aeolus_swe_params* p, doub
   double2* y0 = reinterpret_cast<double2*>(state);
   const bool spec_cor = plan->precision == AEOLUS_PREC_SPLIT_BF16;
   const double fp = spec_cor ? 0.0 : f10;
-  SwePw pw{fp, phi0};
+  SwePw pw{fp, phi0, (float)phi0};
   for (int it = 0; it < nsteps; ++it)
     for (int stage = 1; stage <= 4; ++stage) {
       const double2* in = stage == 1 ? y0 : stage_buf[stage & 1];        // 2 -> buf0, 3 -> buf1, 4 -> buf0

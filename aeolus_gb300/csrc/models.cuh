@@ -215,6 +215,7 @@ struct SwePw {
   static constexpr bool kIdentity = false;
   double f10;   // eta = zeta + f10 * fgrid (0: products of the relative vorticity only)
   double phi0;  // positivity check of Phi0 + phi
+  float phi0f;  // the same as a float (double-float path)
   __device__ unsigned operator()(double c, double fg, const double* in, double* out) const {
     const double u = in[0] / c, v = in[1] / c;
     const double eta_lam = in[2], eta_snt = in[3], phi_lam = in[4], phi_snt = in[5];
@@ -244,7 +245,7 @@ struct SwePw {
     unsigned bits = 0u;
     if (!(isfinite(out[0].hi) && isfinite(out[1].hi) && isfinite(out[2].hi) && isfinite(out[3].hi)))
       bits |= AEOLUS_STATE_NONFINITE;
-    if (!((float)phi0 + phi.hi > 0.0f)) bits |= AEOLUS_STATE_THICKNESS;
+    if (!(phi0f + phi.hi > 0.0f)) bits |= AEOLUS_STATE_THICKNESS;
     return bits;
   }
 };

@@ -20,13 +20,16 @@ inline int pick_bc(int L, int batch) {
   return std::min(bc, std::max(batch, 1));
 }
 
+// Raises a kernel's dynamic shared-memory limit once per (kernel, device):
+// later calls -- including calls made while a stream is being captured
+// into a CUDA graph -- do not touch the function attributes again.
+int allow_smem_raw(const void* kern, size_t bytes);  // plan.cu
+
 template <class K>
 inline int allow_smem(K kern, size_t bytes) {
-  if (bytes > 48 * 1024) {
-    if (bytes > 227 * 1024) return fail(AEOLUS_ERR_ARG, "shared-memory tile exceeds 227 KB for this size");
-    AE_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
-  }
-  return AEOLUS_OK;
+  if (bytes <= 48 * 1024) return AEOLUS_OK;
+  if (bytes > 227 * 1024) return fail(AEOLUS_ERR_ARG, "shared-memory tile exceeds 227 KB for this size");
+  return allow_smem_raw(reinterpret_cast<const void*>(kern), bytes);
 }
 
 // Radix-3/5 butterfly constants split into f32 hi + lo words.
@@ -44,22 +47,46 @@ inline int round_threads(long items, int lo, int hi) {
   return (int)std::max<long>(lo, std::min<long>(hi, t));
 }
 
+// Launch shapes of the three Gauss stages (the autotuner's knobs are the
+// plan's tune_* fields; 0 keeps the built-in heuristic).
+struct LegCfg {
+  int bc;          // members per CTA
+  int threads;
+  size_t smem;
+  dim3 grid;
+};
+
+template <class Derive>
+LegCfg synth_cfg(const aeolus_plan_impl* p, int batch) {
+  const int L = p->lmax;
+  int bc = p->tune_bc_synth > 0 ? std::min(p->tune_bc_synth, std::max(batch, 1)) : pick_bc(L, batch);
+  while (bc > 1 && synth_smem_bytes<Derive, kSynthCPT>(L, bc) > 200 * 1024) --bc;
+  const int ngroups = (bc * Derive::NF + kSynthCPT - 1) / kSynthCPT;
+  return LegCfg{bc, round_threads((long)p->nh * ngroups, 64, 256), synth_smem_bytes<Derive, kSynthCPT>(L, bc),
+                dim3(n_pairs(L), (batch + bc - 1) / bc)};
+}
+
+template <class Epi>
+LegCfg analysis_cfg(const aeolus_plan_impl* p, int batch) {
+  const int L = p->lmax;
+  int bc = p->tune_bc_anal > 0 ? std::min(p->tune_bc_anal, std::max(batch, 1)) : pick_bc(L, batch);
+  while (bc > 1 && analysis_smem_bytes<Epi>(p->nh, bc) > 220 * 1024) --bc;
+  return LegCfg{bc, round_threads((long)bc * (L + 2), 64, 256), analysis_smem_bytes<Epi>(p->nh, bc),
+                dim3(n_pairs(L), (batch + bc - 1) / bc)};
+}
+
+inline int row_threads(const aeolus_plan_impl* p) { return p->tune_row_threads > 0 ? p->tune_row_threads : 256; }
+
 template <class Derive>
 int launch_synth(const aeolus_plan_impl* p, const Derive& d, double2* FG, int nblk, int batch,
                  cudaStream_t st) {
-  const int L = p->lmax;
-  int bc = pick_bc(L, batch);
-  while (bc > 1 && synth_smem_bytes<Derive, kSynthCPT>(L, bc) > 200 * 1024) --bc;
-  LegArgs a{L, p->nlat, p->nh, batch, bc, p->P, p->PT, FG, nblk};
-  const size_t sm = synth_smem_bytes<Derive, kSynthCPT>(L, bc);
+  const LegCfg c = synth_cfg<Derive>(p, batch);
+  LegArgs a{p->lmax, p->nlat, p->nh, batch, c.bc, p->P, p->PT, FG, nblk};
   auto kern = legendre_synth_kernel<Derive, kSynthCPT>;
-  int s = allow_smem(kern, sm);
+  int s = allow_smem(kern, c.smem);
   if (s) return s;
-  const int ngroups = (bc * Derive::NF + kSynthCPT - 1) / kSynthCPT;
-  const int threads = round_threads((long)p->nh * ngroups, 64, 256);
-  dim3 grid(n_pairs(L), (batch + bc - 1) / bc);
   ProfScope prof("legendre_synth_f64", st);
-  kern<<<grid, threads, sm, st>>>(a, d);
+  kern<<<c.grid, c.threads, c.smem, st>>>(a, d);
   AE_LAUNCH("legendre_synth_kernel");
   return AEOLUS_OK;
 }
@@ -67,24 +94,19 @@ int launch_synth(const aeolus_plan_impl* p, const Derive& d, double2* FG, int nb
 template <class Epi>
 int launch_analysis(const aeolus_plan_impl* p, const Epi& e, double2* FG, int nblk, int batch,
                     cudaStream_t st) {
-  const int L = p->lmax;
-  int bc = pick_bc(L, batch);
-  while (bc > 1 && analysis_smem_bytes<Epi>(p->nh, bc) > 220 * 1024) --bc;
-  LegArgs a{L, p->nlat, p->nh, batch, bc, p->P, p->PT, FG, nblk};
-  const size_t sm = analysis_smem_bytes<Epi>(p->nh, bc);
+  const LegCfg c = analysis_cfg<Epi>(p, batch);
+  LegArgs a{p->lmax, p->nlat, p->nh, batch, c.bc, p->P, p->PT, FG, nblk};
   auto kern = legendre_analysis_kernel<Epi>;
-  int s = allow_smem(kern, sm);
+  int s = allow_smem(kern, c.smem);
   if (s) return s;
-  const int threads = round_threads((long)bc * (L + 2), 64, 256);
-  dim3 grid(n_pairs(L), (batch + bc - 1) / bc);
   ProfScope prof("legendre_analysis_f64", st);
-  kern<<<grid, threads, sm, st>>>(a, e);
+  kern<<<c.grid, c.threads, c.smem, st>>>(a, e);
   AE_LAUNCH("legendre_analysis_kernel");
   return AEOLUS_OK;
 }
 
-template <class Pw, int IN_MODE, int OUT_MODE>
-int launch_rows(const aeolus_plan_impl* p, const Pw& pw, RowArgs a, cudaStream_t st) {
+// Fills the plan-derived fields of a row stage's arguments.
+inline void row_args(const aeolus_plan_impl* p, RowArgs& a) {
   a.L = p->lmax;
   a.nlat = p->nlat;
   a.fft = p->fft;
@@ -92,8 +114,14 @@ int launch_rows(const aeolus_plan_impl* p, const Pw& pw, RowArgs a, cudaStream_t
   a.coslat = p->coslat;
   a.fgrid = p->fgrid;
   a.wq = a.unit_weights ? nullptr : p->wq;
+}
+
+template <class Pw, int IN_MODE, int OUT_MODE>
+int launch_rows(const aeolus_plan_impl* p, const Pw& pw, RowArgs a, cudaStream_t st) {
+  row_args(p, a);
   const size_t sm = row_smem_bytes<Pw>(p->fft);
   dim3 grid(p->nlat, a.batch);
+  const int threads = row_threads(p);
   if (p->precision == AEOLUS_PREC_SPLIT_BF16) {
     // split-precision path: double-float FFTs and products on the f32 pipe
     auto kern = row_kernel_df<Pw, IN_MODE, OUT_MODE>;
@@ -101,7 +129,7 @@ int launch_rows(const aeolus_plan_impl* p, const Pw& pw, RowArgs a, cudaStream_t
     if (s) return s;
     ProfScope prof(IN_MODE == kInF ? (OUT_MODE == kOutG ? "rows_df_c2r_products_r2c" : "rows_df_c2r") : "rows_df_r2c",
                    st);
-    kern<<<grid, 256, sm, st>>>(a, pw, p->twdf, df_consts());
+    kern<<<grid, threads, sm, st>>>(a, pw, p->twdf, df_consts());
     AE_LAUNCH("row_kernel_df");
     return AEOLUS_OK;
   }
@@ -109,7 +137,7 @@ int launch_rows(const aeolus_plan_impl* p, const Pw& pw, RowArgs a, cudaStream_t
   int s = allow_smem(kern, sm);
   if (s) return s;
   ProfScope prof(IN_MODE == kInF ? (OUT_MODE == kOutG ? "rows_c2r_products_r2c" : "rows_c2r") : "rows_r2c", st);
-  kern<<<grid, 256, sm, st>>>(a, pw);
+  kern<<<grid, threads, sm, st>>>(a, pw);
   AE_LAUNCH("row_kernel");
   return AEOLUS_OK;
 }

@@ -5,6 +5,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <map>
 #include <mutex>
 
 #include "common.cuh"
@@ -305,6 +306,20 @@ void free_plan(aeolus_plan_impl* p) {
 }
 
 }  // namespace
+
+int allow_smem_raw(const void* kern, size_t bytes) {
+  static std::mutex mu;
+  static std::map<std::pair<const void*, int>, size_t> done;
+  int dev = 0;
+  AE_CUDA(cudaGetDevice(&dev));
+  std::lock_guard<std::mutex> g(mu);
+  size_t& have = done[{kern, dev}];
+  if (have >= bytes) return AEOLUS_OK;
+  AE_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
+  have = bytes;
+  return AEOLUS_OK;
+}
+
 
 void free_split(aeolus_plan_impl* p);  // split.cu
 int build_points_basis(aeolus_plan_impl* p, const double* lat, const double* lon);  // points.cu

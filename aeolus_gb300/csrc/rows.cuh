@@ -138,12 +138,12 @@ __device__ double2* fft_run(double2* src, double2* dst, int nf, const FftInfo& f
 }
 
 template <class Pw, int IN_MODE, int OUT_MODE>
-__global__ void __launch_bounds__(256) row_kernel(RowArgs a, Pw pw) {
+__device__ __forceinline__ void row_body(const RowArgs& a, const Pw& pw, int bx, int by) {
   constexpr int NIN = Pw::NIN, NOUT = Pw::NOUT;
   constexpr int NF = NIN > NOUT ? NIN : NOUT;
   extern __shared__ double2 smem[];
   __shared__ unsigned s_bits;
-  const int j = blockIdx.x, b = blockIdx.y;
+  const int j = bx, b = by;
   const int N = a.fft.N, n = a.fft.n, L = a.L;
   const int ldm = L + 1;
   double2* buf0 = smem;
@@ -261,6 +261,11 @@ __global__ void __launch_bounds__(256) row_kernel(RowArgs a, Pw pw) {
       }
     }
   }
+}
+
+template <class Pw, int IN_MODE, int OUT_MODE>
+__global__ void __launch_bounds__(256) row_kernel(RowArgs a, Pw pw) {
+  row_body<Pw, IN_MODE, OUT_MODE>(a, pw, blockIdx.x, blockIdx.y);
 }
 
 template <class Pw>

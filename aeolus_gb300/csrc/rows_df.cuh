@@ -107,12 +107,13 @@ __device__ cdf* fft_run_df(cdf* src, cdf* dst, int nf, const FftInfo& fi, const 
 }
 
 template <class Pw, int IN_MODE, int OUT_MODE>
-__global__ void __launch_bounds__(256) row_kernel_df(RowArgs a, Pw pw, const float4* __restrict__ twdf, DfConst kc) {
+__device__ __forceinline__ void row_df_body(const RowArgs& a, const Pw& pw, const float4* __restrict__ twdf,
+                                            const DfConst& kc, int bx, int by) {
   constexpr int NIN = Pw::NIN, NOUT = Pw::NOUT;
   constexpr int NF = NIN > NOUT ? NIN : NOUT;
   extern __shared__ cdf smem_df[];
   __shared__ unsigned s_bits;
-  const int j = blockIdx.x, b = blockIdx.y;
+  const int j = bx, b = by;
   const int N = a.fft.N, n = a.fft.n, L = a.L;
   const int ldm = L + 1;
   cdf* buf0 = smem_df;
@@ -225,6 +226,11 @@ __global__ void __launch_bounds__(256) row_kernel_df(RowArgs a, Pw pw, const flo
       }
     }
   }
+}
+
+template <class Pw, int IN_MODE, int OUT_MODE>
+__global__ void __launch_bounds__(256) row_kernel_df(RowArgs a, Pw pw, const float4* __restrict__ twdf, DfConst kc) {
+  row_df_body<Pw, IN_MODE, OUT_MODE>(a, pw, twdf, kc, blockIdx.x, blockIdx.y);
 }
 
 }  // namespace aeolus

@@ -269,16 +269,16 @@ __host__ __device__ inline long long tile_elem(int rows, int s, int r, int k) {
 // ------------------------------------------------- synthesis data slicing
 // grid (m, member chunk of `mb` members); columns (b, f, re/im).
 template <class Derive>
-__global__ void __launch_bounds__(256) split_synth_slice_kernel(SplitDims dm, const long long* __restrict__ kcum,
-                                                               int batch, int mb, Derive der,
-                                                               __nv_bfloat16* __restrict__ dsyn,
-                                                               int* __restrict__ ecol) {
+__device__ __forceinline__ void split_synth_slice_body(const SplitDims& dm, const long long* __restrict__ kcum,
+                                                       int batch, int mb, const Derive& der,
+                                                       __nv_bfloat16* __restrict__ dsyn, int* __restrict__ ecol,
+                                                       int bx, int by, int gy) {
   constexpr int NF = Derive::NF;
   extern __shared__ double s_val[];  // [mb*NF*2][K]
   __shared__ int s_exp[256];
-  const int m = blockIdx.x, L = dm.L;
+  const int m = bx, L = dm.L;
   const int K = L + 1 - m, Kp = kpad(K);
-  const int b0 = blockIdx.y * mb;
+  const int b0 = by * mb;
   const int nb = min(mb, batch - b0);
   const int nc = nb * NF * 2;
   for (int idx = threadIdx.x; idx < nb * K; idx += blockDim.x) {
@@ -313,7 +313,7 @@ __global__ void __launch_bounds__(256) split_synth_slice_kernel(SplitDims dm, co
 #pragma unroll
     for (int s = 0; s < kSlices; ++s) tile[tile_elem(kNT, s, n % kNT, t)] = __float2bfloat16(d[s]);
   }
-  if (blockIdx.y == gridDim.y - 1) {  // zero the columns that pad the last tile
+  if (by == gy - 1) {  // zero the columns that pad the last tile
     const int n0 = batch * NF * 2, n1 = dm.ntiles * kNT;
     for (int idx = threadIdx.x; idx < (n1 - n0) * Kp; idx += blockDim.x) {
       const int n = n0 + idx / Kp, t = idx % Kp;
@@ -325,18 +325,25 @@ __global__ void __launch_bounds__(256) split_synth_slice_kernel(SplitDims dm, co
   }
 }
 
+template <class Derive>
+__global__ void __launch_bounds__(256) split_synth_slice_kernel(SplitDims dm, const long long* __restrict__ kcum,
+                                                               int batch, int mb, Derive der,
+                                                               __nv_bfloat16* __restrict__ dsyn,
+                                                               int* __restrict__ ecol) {
+  split_synth_slice_body<Derive>(dm, kcum, batch, mb, der, dsyn, ecol, blockIdx.x, blockIdx.y, gridDim.y);
+}
+
 // ------------------------------------------------- analysis data slicing
 // Reads the double-float G blocks (float4 per complex value), grid (m, chunk).
 template <int NF>
-__global__ void __launch_bounds__(256) split_anal_slice_kernel(SplitDims dm, int batch, int mb, int nblk,
-                                                              const float4* __restrict__ FG,
-                                                              __nv_bfloat16* __restrict__ dana,
-                                                              int* __restrict__ ecol) {
+__device__ __forceinline__ void split_anal_slice_body(const SplitDims& dm, int batch, int mb, int nblk,
+                                                      const float4* __restrict__ FG, __nv_bfloat16* __restrict__ dana,
+                                                      int* __restrict__ ecol, int bx, int by, int gy) {
   extern __shared__ df s_dval[];  // [mb*NF*2][nlat]
   __shared__ int s_exp[256];
-  const int m = blockIdx.x, L = dm.L, nlat = dm.nlat, NK = dm.NK;
+  const int m = bx, L = dm.L, nlat = dm.nlat, NK = dm.NK;
   const int ldm = L + 1;
-  const int b0 = blockIdx.y * mb;
+  const int b0 = by * mb;
   const int nb = min(mb, batch - b0);
   const int nc = nb * NF * 2;
   for (int idx = threadIdx.x; idx < nb * NF * nlat; idx += blockDim.x) {
@@ -374,7 +381,7 @@ __global__ void __launch_bounds__(256) split_anal_slice_kernel(SplitDims dm, int
 #pragma unroll
     for (int s = 0; s < kSlices; ++s) tile[tile_elem(kNT, s, n % kNT, j)] = __float2bfloat16(d[s]);
   }
-  if (blockIdx.y == gridDim.y - 1) {
+  if (by == gy - 1) {
     const int n0 = batch * NF * 2, n1 = dm.ntiles * kNT;
     for (int idx = threadIdx.x; idx < (n1 - n0) * NK; idx += blockDim.x) {
       const int n = n0 + idx / NK, j = idx % NK;
@@ -384,6 +391,14 @@ __global__ void __launch_bounds__(256) split_anal_slice_kernel(SplitDims dm, int
       if (j == 0) ecol[(long long)m * dm.ntiles * kNT + n] = 0;
     }
   }
+}
+
+template <int NF>
+__global__ void __launch_bounds__(256) split_anal_slice_kernel(SplitDims dm, int batch, int mb, int nblk,
+                                                              const float4* __restrict__ FG,
+                                                              __nv_bfloat16* __restrict__ dana,
+                                                              int* __restrict__ ecol) {
+  split_anal_slice_body<NF>(dm, batch, mb, nblk, FG, dana, ecol, blockIdx.x, blockIdx.y, gridDim.y);
 }
 
 // ---------------------------------------------------- tensor-core kernels
@@ -396,21 +411,42 @@ __global__ void __launch_bounds__(256) split_anal_slice_kernel(SplitDims dm, int
 //                   (across tile boundaries);
 //   warp 1 lane 0   MMA issuer: per chunk the 21 digit-pair MMAs into the
 //                   kAccs level accumulators of one of two TMEM buffers;
-//   warps 2..9      epilogue: drain the other TMEM buffer while the next
-//                   tile's MMAs run; warp w reads TMEM lane quadrant w % 4
-//                   and the 16-column half (w - 2) / 4 of the tile.
+//   warps 2..      Epi::kWarps epilogue warps drain the other TMEM buffer
+//                   while the next tile's MMAs run; warp w reads TMEM lane
+//                   quadrant w % 4 and the Epi::kCols-column group (w - 2) / 4.
 // Barriers: full/empty per stage (TMA bytes / MMA commit), tfull/tempty per
-// TMEM buffer (MMA commit / 8 epilogue-warp arrivals).  Every wait is
+// TMEM buffer (MMA commit / one arrival per epilogue warp).  Every wait is
 // bounded: an expired wait sets *err and that role stops; the others then
 // time out in turn, copies in flight are waited for and TMEM is freed.
 constexpr int kStages = 6;          // smem pipeline depth (30 KB per stage)
 constexpr int kTmemBuf = 256;       // column offset of the second accumulator buffer
 constexpr int kTmemCols = 512;      // 2 x kAccs * kNT = 448 columns used
-constexpr int kEpiWarps = 8;        // two per TMEM lane quadrant
-constexpr int kTcThreads = 64 + 32 * kEpiWarps;
 constexpr size_t kStageBytesA = chunk_elems(128) * 2;
 constexpr size_t kStageBytesB = chunk_elems(kNT) * 2;
 constexpr size_t kStageBytes = kStageBytesA + kStageBytesB;
+
+// The 21 digit pairs (s, u), s + u < kSlices, in issue order, with their
+// level accumulator and whether the pair is the first to write it (its MMA
+// then overwrites instead of accumulating on a tile's first chunk).
+constexpr int kPairs = kSlices * (kSlices + 1) / 2;
+struct DigitPairs {
+  int s[kPairs], u[kPairs], a[kPairs], first[kPairs];
+};
+__host__ __device__ constexpr DigitPairs digit_pairs() {
+  DigitPairs t{};
+  int p = 0;
+  unsigned seen = 0u;
+  for (int s = 0; s < kSlices; ++s)
+    for (int u = 0; s + u < kSlices; ++u) {
+      t.s[p] = s;
+      t.u[p] = u;
+      t.a[p] = acc_of(s, u);
+      t.first[p] = ((seen >> t.a[p]) & 1u) ? 0 : 1;
+      seen |= 1u << t.a[p];
+      ++p;
+    }
+  return t;
+}
 
 struct TcTile {
   const __nv_bfloat16* A;  // chunk-major basis tile
@@ -453,24 +489,42 @@ __device__ inline TcSmem tc_carve(char* base) {
 
 // The kAccs accumulators of 16 columns starting at c0 for lane `lane` of the
 // TMEM quadrant q (the calling warp's own quadrant).
-__device__ inline void tc_read16(uint32_t tbuf, int q, int c0, float (*acc)[kAccs]) {
+// NC (8 or 16) columns of all kAccs accumulators: every load is issued
+// before one wait (one TMEM round trip); the register fences keep every use
+// of the loaded values after the wait.
+template <int NC>
+__device__ inline void tc_read(uint32_t tbuf, int q, int c0, float (*acc)[kAccs]) {
+  static_assert(NC == 8 || NC == 16, "8 or 16 columns");
   const uint32_t lane_base = (uint32_t)(q * 32) << 16;
-  uint32_t r[16];
+  uint32_t r[kAccs][NC];
 #pragma unroll
   for (int k = 0; k < kAccs; ++k) {
-    tc::tmem_ld16(tbuf + lane_base + (uint32_t)(k * kNT + c0), r);
-    tc::tmem_wait_ld();
-#pragma unroll
-    for (int i = 0; i < 16; ++i) acc[i][k] = __uint_as_float(r[i]);
+    if constexpr (NC == 16) tc::tmem_ld16(tbuf + lane_base + (uint32_t)(k * kNT + c0), r[k]);
+    else tc::tmem_ld8(tbuf + lane_base + (uint32_t)(k * kNT + c0), r[k]);
   }
+  if constexpr (NC == 16) tc::tmem_wait_ld_dep(r[0]);
+  else tc::tmem_wait_ld_dep8(r[0]);
+#pragma unroll
+  for (int k = 1; k < kAccs; ++k) {
+    if constexpr (NC == 16) tc::reg_fence16(r[k]);
+    else tc::reg_fence8(r[k]);
+  }
+#pragma unroll
+  for (int k = 0; k < kAccs; ++k)
+#pragma unroll
+    for (int i = 0; i < NC; ++i) acc[i][k] = __uint_as_float(r[k][i]);
 }
 
+template <class Epi>
+constexpr int tc_threads() { return 64 + 32 * Epi::kWarps; }
+
 // Sched: int count() const; TcTile tile(int t) const.
-// Epi:   void run(int t, uint32_t tbuf, int q, int row, int c0, int etid) const
-//        -- consumes columns [c0, c0 + 16) of the accumulators of tile t for
-//        TMEM lane row = q * 32 + lane (etid = epilogue thread 0..255).
+// Epi:   kWarps (4, 8 or 16 epilogue warps), kCols = 4 kNT / kWarps, and
+//        void run(int t, uint32_t tbuf, int q, int row, int c0, int etid) const
+//        -- consumes columns [c0, c0 + kCols) of the accumulators of tile t
+//        for TMEM lane row = q * 32 + lane (etid = epilogue thread index).
 template <class Sched, class Epi>
-__global__ void __launch_bounds__(kTcThreads, 1) tc_persistent_kernel(Sched sc, Epi ep, int* err) {
+__global__ void __launch_bounds__(tc_threads<Epi>(), 1) tc_persistent_kernel(Sched sc, Epi ep, int* err) {
   extern __shared__ char smem_raw[];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const TcSmem sm = tc_carve(smem_raw);
@@ -481,7 +535,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_persistent_kernel(Sched sc, 
     }
     for (int i = 0; i < 2; ++i) {
       tc::mbar_init(&sm.tfull[i], 1);
-      tc::mbar_init(&sm.tempty[i], kEpiWarps);
+      tc::mbar_init(&sm.tempty[i], Epi::kWarps);
     }
     tc::mbar_init(sm.done, 1);
     tc::fence_mbar_init();
@@ -519,8 +573,14 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_persistent_kernel(Sched sc, 
     }
   } else if (warp == 1) {
     if (lane == 0) {  // ---------------- MMA issuer
+      // Descriptors differ between stages and digit slices only in the
+      // start-address field: stage/slice byte offsets >> 4 are added to the
+      // descriptors of stage 0, slice 0 (smem addresses < 256 KB, no carry).
+      constexpr DigitPairs dp = digit_pairs();
       bool ok = true;
       const uint32_t idesc = tc::idesc_bf16_f32(128, kNT);
+      const uint64_t dA0 = tc::smem_desc(sm.A(0), 128, kKC * 16);
+      const uint64_t dB0 = tc::smem_desc(sm.B(0), 128, kKC * 16);
       uint32_t g = 0;
       int i = 0;
       for (int t = blockIdx.x; t < ntiles && ok; t += gridDim.x, ++i) {
@@ -533,7 +593,6 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_persistent_kernel(Sched sc, 
         }
         tc::fence_after_sync();
         const uint32_t dbase = tmem + (uint32_t)(buf * kTmemBuf);
-        unsigned started = 0u;
         for (int kc = 0; kc < tl.nchunks; ++kc, ++g) {
           const int st = (int)(g % kStages);
           if (!tc::mbar_wait(&sm.full[st], (g / kStages) & 1)) {
@@ -541,14 +600,13 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_persistent_kernel(Sched sc, 
             break;
           }
           tc::fence_after_sync();
-          for (int s = 0; s < kSlices; ++s) {
-            const uint64_t da = tc::smem_desc(sm.A(st) + (long long)s * 128 * kKC, 128, kKC * 16);
-            for (int u = 0; s + u < kSlices; ++u) {
-              const int a = acc_of(s, u);
-              const uint64_t db = tc::smem_desc(sm.B(st) + (long long)u * kNT * kKC, 128, kKC * 16);
-              tc::mma_bf16(dbase + (uint32_t)a * kNT, da, db, idesc, ((started >> a) & 1u) ? 1u : 0u);
-              started |= 1u << a;
-            }
+          const uint64_t off = (uint64_t)(((size_t)st * kStageBytes) >> 4);
+          const uint64_t da0 = dA0 + off, db0 = dB0 + off;
+#pragma unroll
+          for (int q = 0; q < kPairs; ++q) {
+            const uint64_t da = da0 + (uint64_t)(((size_t)dp.s[q] * 128 * kKC * 2) >> 4);
+            const uint64_t db = db0 + (uint64_t)(((size_t)dp.u[q] * kNT * kKC * 2) >> 4);
+            tc::mma_bf16(dbase + (uint32_t)(dp.a[q] * kNT), da, db, idesc, (kc > 0 || !dp.first[q]) ? 1u : 0u);
           }
           tc::mma_commit(&sm.empty[st]);
         }
@@ -560,9 +618,9 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_persistent_kernel(Sched sc, 
       if (!tc::mbar_wait(sm.done, 0)) ok = false;
       if (!ok) atomicExch(err, 3);
     }
-  } else {  // ------------------------ epilogue warps 2..9
+  } else {  // ------------------------ epilogue warps
     const int q = warp & 3;
-    const int c0 = ((warp - 2) >> 2) * 16;
+    const int c0 = ((warp - 2) >> 2) * Epi::kCols;
     const int etid = (warp - 2) * 32 + lane;
     int i = 0;
     for (int t = blockIdx.x; t < ntiles; t += gridDim.x, ++i) {
@@ -600,7 +658,8 @@ struct SynthSched {
   const long long* kcum;
   const __nv_bfloat16* psyn;
   const __nv_bfloat16* dsyn;
-  __device__ int count() const { return (dm.L + 1) * dm.Mt * dm.ntiles; }
+  __host__ __device__ int count() const { return (dm.L + 1) * dm.Mt * dm.ntiles; }
+  int count_host() const { return count(); }
   __device__ TcTile tile(int t) const {
     const int per_m = dm.Mt * dm.ntiles;
     const int m = t / per_m, r = t - m * per_m;
@@ -610,12 +669,14 @@ struct SynthSched {
   }
 };
 
-// Writes double-float F blocks (float4 per complex value).
+// Writes double-float F blocks (float4 per complex value); NF fields.
+template <int NF>
 struct SynthEpi {
+  static constexpr int kWarps = 16, kCols = 4 * kNT / kWarps;
   SplitDims dm;
   const int* esyn;
   const int* ecol;
-  int nf, nblk;
+  int nblk;
   float4* F;
   __device__ void run(int t, uint32_t tbuf, int q, int row, int c0, int) const {
     const int per_m = dm.Mt * dm.ntiles;
@@ -624,19 +685,23 @@ struct SynthEpi {
     const int L = dm.L;
     const int j = mt * 128 + row;
     const int Ej = j < dm.nlat ? esyn[m * dm.Mt * 128 + j] : 0;
-    const int* ec = ecol + (long long)m * dm.ntiles * kNT + tile * kNT;
-    float acc[16][kAccs];
-    tc_read16(tbuf, q, c0, acc);
+    const int* ec = ecol + (long long)m * dm.ntiles * kNT + tile * kNT + c0;
+    int e[kCols];
+#pragma unroll
+    for (int i = 0; i < kCols; ++i) e[i] = Ej + __ldg(ec + i) - kOut;
+    float acc[kCols][kAccs];
+    tc_read<kCols>(tbuf, q, c0, acc);
     if (j < dm.nlat) {
 #pragma unroll
-      for (int i = 0; i < 16; i += 2) {
+      for (int i = 0; i < kCols; i += 2) {
         const int n = tile * kNT + c0 + i;  // even: real part, n + 1: imaginary part
-        if (n >= dm.ncol) break;
-        const df re = levels_to_df(acc[i], Ej + ec[c0 + i] - kOut);
-        const df im = levels_to_df(acc[i + 1], Ej + ec[c0 + i + 1] - kOut);
-        const int bf = n >> 1;
-        const int b = bf / nf, f = bf - b * nf;
-        F[(((long long)b * dm.nlat + j) * nblk + f) * (L + 1) + m] = make_float4(re.hi, re.lo, im.hi, im.lo);
+        if (n < dm.ncol) {
+          const df re = levels_to_df(acc[i], e[i]);
+          const df im = levels_to_df(acc[i + 1], e[i + 1]);
+          const int bf = n >> 1;
+          const int b = bf / NF, f = bf - b * NF;
+          F[(((long long)b * dm.nlat + j) * nblk + f) * (L + 1) + m] = make_float4(re.hi, re.lo, im.hi, im.lo);
+        }
       }
     }
   }
@@ -647,7 +712,8 @@ struct AnalSched {
   SplitDims dm;
   const __nv_bfloat16* pana;
   const __nv_bfloat16* dana;
-  __device__ int count() const { return (dm.L + 1) * dm.ntiles; }
+  __host__ __device__ int count() const { return (dm.L + 1) * dm.ntiles; }
+  int count_host() const { return count(); }
   __device__ TcTile tile(int t) const {
     const int m = t / dm.ntiles, nt = t - m * dm.ntiles;
     return TcTile{pana + pana_tile(dm.NK, m), dana + dana_tile(dm, m, nt), dm.NK / kKC};
@@ -658,6 +724,7 @@ struct AnalSched {
 // epilogue functor (whole members: Epi::finish; else Epi::finish_field).
 template <class Epi>
 struct AnalEpi {
+  static constexpr int kWarps = 8, kCols = 4 * kNT / kWarps;  // FP64 epilogue: 16 columns per warp
   SplitDims dm;
   const int* eana;
   const int* ecol;
@@ -672,8 +739,8 @@ struct AnalEpi {
     const int Et = eana[m * 128 + t];
     const int* ec = ecol + (long long)m * dm.ntiles * kNT + tile * kNT;
     {
-      float acc[16][kAccs];
-      tc_read16(tbuf, q, c0, acc);
+      float acc[kCols][kAccs];
+      tc_read<kCols>(tbuf, q, c0, acc);
       if (t < K) {
         if constexpr (kWhole) {
 #pragma unroll
@@ -706,7 +773,7 @@ struct AnalEpi {
     }
     // slots l < m of column m for the members this tile touches
     const int mb0 = tile * kNT / (2 * NF), mb1 = min(batch, ((tile + 1) * kNT + 2 * NF - 1) / (2 * NF));
-    for (int idx = etid; idx < (mb1 - mb0) * m; idx += 32 * kEpiWarps) epi.zero(mb0 + idx / m, idx % m, m);
+    for (int idx = etid; idx < (mb1 - mb0) * m; idx += 32 * kWarps) epi.zero(mb0 + idx / m, idx % m, m);
   }
 };
 
@@ -730,37 +797,72 @@ inline size_t split_anal_bytes(const aeolus_plan_impl* p, int nf, int batch) {
          align256((size_t)(d.L + 1) * d.ntiles * kNT * 4);
 }
 
-inline int slice_members(int nf, int K) {
-  // members per slicing CTA: staged values within 64 KB and at most 256 columns
-  return std::max(1, std::min(256 / (2 * nf), (64 * 1024) / (2 * nf * K * 8)));
+inline int slice_members(int nf, int K, int tuned) {
+  // members per slicing CTA: at most 256 columns (the exponent array) and the
+  // staged values within 64 KB, or the tuned count within 160 KB
+  const int cap_cols = std::max(1, 256 / (2 * nf));
+  if (tuned > 0) return std::max(1, std::min({tuned, cap_cols, (160 * 1024) / (2 * nf * K * 8)}));
+  return std::max(1, std::min(cap_cols, (64 * 1024) / (2 * nf * K * 8)));
+}
+
+// Scratch carving and slicing shapes of the two split stages.
+struct SplitParts {
+  SplitDims dm;
+  __nv_bfloat16* digits;  // data digit planes
+  int* ecol;              // per-column exponents
+  int mb;                 // members per slicing CTA
+  size_t smem;            // slicing kernel dynamic shared memory
+  dim3 grid;              // slicing grid
+};
+
+template <int NF>
+SplitParts split_synth_parts(const aeolus_plan_impl* p, int batch, void* scratch) {
+  SplitParts r;
+  r.dm = split_dims(p, batch * NF * 2);
+  char* w = static_cast<char*>(scratch);
+  r.digits = reinterpret_cast<__nv_bfloat16*>(w);
+  w += align256((size_t)p->split->h_kcum[r.dm.L + 1] * r.dm.ntiles * kSlices * kNT * 2);
+  r.ecol = reinterpret_cast<int*>(w);
+  r.mb = slice_members(NF, r.dm.L + 1, p->tune_slice_mb);
+  r.smem = (size_t)r.mb * NF * 2 * (r.dm.L + 1) * 8;
+  r.grid = dim3(r.dm.L + 1, (batch + r.mb - 1) / r.mb);
+  return r;
+}
+
+template <int NF>
+SplitParts split_anal_parts(const aeolus_plan_impl* p, int batch, void* scratch) {
+  SplitParts r;
+  r.dm = split_dims(p, batch * NF * 2);
+  char* w = static_cast<char*>(scratch);
+  r.digits = reinterpret_cast<__nv_bfloat16*>(w);
+  w += align256((size_t)(r.dm.L + 1) * r.dm.ntiles * kSlices * kNT * r.dm.NK * 2);
+  r.ecol = reinterpret_cast<int*>(w);
+  r.mb = slice_members(NF, r.dm.nlat, p->tune_slice_mb);
+  r.smem = (size_t)r.mb * NF * 2 * r.dm.nlat * 8;
+  r.grid = dim3(r.dm.L + 1, (batch + r.mb - 1) / r.mb);
+  return r;
 }
 
 template <class Derive>
 int launch_split_synth(const aeolus_plan_impl* p, const Derive& d, double2* FG, int nblk, int batch, void* scratch,
                        cudaStream_t st) {
   constexpr int NF = Derive::NF;
-  const SplitDims dm = split_dims(p, batch * NF * 2);
-  char* w = static_cast<char*>(scratch);
-  __nv_bfloat16* dsyn = reinterpret_cast<__nv_bfloat16*>(w);
-  w += align256((size_t)p->split->h_kcum[dm.L + 1] * dm.ntiles * kSlices * kNT * 2);
-  int* ecol = reinterpret_cast<int*>(w);
-  const int mb = slice_members(NF, dm.L + 1);
-  const size_t sm1 = (size_t)mb * NF * 2 * (dm.L + 1) * 8;
+  const SplitParts r = split_synth_parts<NF>(p, batch, scratch);
   auto k1 = split_synth_slice_kernel<Derive>;
-  int s = allow_smem(k1, sm1);
+  int s = allow_smem(k1, r.smem);
   if (s) return s;
   {
     ProfScope prof("split_synth_slice", st);
-    k1<<<dim3(dm.L + 1, (batch + mb - 1) / mb), 256, sm1, st>>>(dm, p->split->kcum, batch, mb, d, dsyn, ecol);
+    k1<<<r.grid, 256, r.smem, st>>>(r.dm, p->split->kcum, batch, r.mb, d, r.digits, r.ecol);
     AE_LAUNCH("split_synth_slice_kernel");
   }
   const size_t sm2 = tc_smem_bytes();
-  auto k2 = tc_persistent_kernel<SynthSched, SynthEpi>;
+  auto k2 = tc_persistent_kernel<SynthSched, SynthEpi<NF>>;
   if ((s = allow_smem(k2, sm2))) return s;
-  const SynthSched sc{dm, p->split->kcum, p->split->psyn, dsyn};
-  const SynthEpi ep{dm, p->split->esyn, ecol, NF, nblk, reinterpret_cast<float4*>(FG)};
+  const SynthSched sc{r.dm, p->split->kcum, p->split->psyn, r.digits};
+  const SynthEpi<NF> ep{r.dm, p->split->esyn, r.ecol, nblk, reinterpret_cast<float4*>(FG)};
   ProfScope prof("tc_synth_bf16x6", st);
-  k2<<<tc_grid(p, (dm.L + 1) * dm.Mt * dm.ntiles), kTcThreads, sm2, st>>>(sc, ep, p->split->err);
+  k2<<<tc_grid(p, sc.count_host()), tc_threads<SynthEpi<NF>>(), sm2, st>>>(sc, ep, p->split->err);
   AE_LAUNCH("tc_synth_kernel");
   return AEOLUS_OK;
 }
@@ -769,29 +871,22 @@ template <class Epi>
 int launch_split_anal(const aeolus_plan_impl* p, const Epi& e, const double2* FG, int nblk, int batch, void* scratch,
                       cudaStream_t st) {
   constexpr int NF = Epi::NF;
-  const SplitDims dm = split_dims(p, batch * NF * 2);
-  char* w = static_cast<char*>(scratch);
-  __nv_bfloat16* dana = reinterpret_cast<__nv_bfloat16*>(w);
-  w += align256((size_t)(dm.L + 1) * dm.ntiles * kSlices * kNT * dm.NK * 2);
-  int* ecol = reinterpret_cast<int*>(w);
-  const int mb = slice_members(NF, dm.nlat);
-  const size_t sm1 = (size_t)mb * NF * 2 * dm.nlat * 8;
+  const SplitParts r = split_anal_parts<NF>(p, batch, scratch);
   auto k1 = split_anal_slice_kernel<NF>;
-  int s = allow_smem(k1, sm1);
+  int s = allow_smem(k1, r.smem);
   if (s) return s;
   {
     ProfScope prof("split_anal_slice", st);
-    k1<<<dim3(dm.L + 1, (batch + mb - 1) / mb), 256, sm1, st>>>(dm, batch, mb, nblk,
-                                                                 reinterpret_cast<const float4*>(FG), dana, ecol);
+    k1<<<r.grid, 256, r.smem, st>>>(r.dm, batch, r.mb, nblk, reinterpret_cast<const float4*>(FG), r.digits, r.ecol);
     AE_LAUNCH("split_anal_slice_kernel");
   }
   const size_t sm2 = tc_smem_bytes();
   auto k2 = tc_persistent_kernel<AnalSched, AnalEpi<Epi>>;
   if ((s = allow_smem(k2, sm2))) return s;
-  const AnalSched sc{dm, p->split->pana, dana};
-  const AnalEpi<Epi> ep{dm, p->split->eana, ecol, batch, e};
+  const AnalSched sc{r.dm, p->split->pana, r.digits};
+  const AnalEpi<Epi> ep{r.dm, p->split->eana, r.ecol, batch, e};
   ProfScope prof("tc_anal_bf16x6", st);
-  k2<<<tc_grid(p, (dm.L + 1) * dm.ntiles), kTcThreads, sm2, st>>>(sc, ep, p->split->err);
+  k2<<<tc_grid(p, sc.count_host()), tc_threads<AnalEpi<Epi>>(), sm2, st>>>(sc, ep, p->split->err);
   AE_LAUNCH("tc_anal_kernel");
   return AEOLUS_OK;
 }

@@ -60,6 +60,8 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-flush", action="store_true")
     ap.add_argument("--cpu-rows", type=int, default=8, help="latitude rows in the CPU sample")
+    ap.add_argument("--no-extras", action="store_true",
+                    help="skip the ensemble (uneven l_max BVE) and adjoint (SWE gradient) side measurements")
     return ap.parse_args()
 
 
@@ -69,6 +71,118 @@ def workload_config(args, B):
             "initial_state": "williamson2 + 1% seeded (l+1)^-2 perturbation per member",
             "precision": args.precision, "global_batch": B * max(args.gpus, 1),
             "parallelism": f"replicas x{max(args.gpus, 1)} (members shard, no collective)"}
+
+
+# ------------------------------------------------------------ side measurements
+ENSEMBLE_GROUPS = [(42, 64, 128, 52), (63, 96, 192, 51), (85, 128, 256, 51), (106, 160, 320, 51),
+                   (127, 192, 384, 51)]   # (l_max, nlat, nlon, members): 256 BVE members
+
+
+def ensemble_measure(dev, steps: int = 10, dt: float = 600.0):
+    """256 BVE members over l_max 42..127 on matching Gauss grids (nu = 1e5):
+    autotuned grouped launches, one RK4 step captured in a CUDA graph and
+    replayed `steps` times, FP64 and split precision; members*steps/s."""
+    import torch
+    import aeolus_gb300 as ae
+    from aeolus_gb300 import _lib, workloads as W
+    from aeolus_gb300.barotropic import BarotropicVorticity
+    from aeolus_gb300.ensemble import BarotropicEnsemble
+
+    out = {"workload": "bve_ensemble_256members_lmax42-127", "groups": [
+        {"l_max": L, "grid": f"{nlat}x{nlon}", "members": B} for L, nlat, nlon, B in ENSEMBLE_GROUPS],
+        "dt_s": dt, "viscosity": 1e5, "steps": steps}
+    finals = {}
+    for prec in ("fp64", "split"):
+        models = []
+        for L, nlat, nlon, _ in ENSEMBLE_GROUPS:
+            planet = ae.make_planet("latlon", nlat=nlat, nlon=nlon, l_max=L, device=dev)
+            if prec == "split":
+                planet.so._product_space.sh.plan.set_precision(_lib.PREC_SPLIT_BF16)
+            models.append(BarotropicVorticity(planet, viscosity=1e5))
+        ens = BarotropicEnsemble(models, [g[3] for g in ENSEMBLE_GROUPS])
+        init = [torch.as_tensor(np.stack([W.bve_vorticity(L, 7919 * g + b) for b in range(B)]), device=dev)
+                for g, (L, _, _, B) in enumerate(ENSEMBLE_GROUPS)]
+        states = [x.clone() for x in init]
+        report = ens.autotune(states)
+        ens.rk4(states, dt, 3)                       # warm-up
+        torch.cuda.synchronize(dev)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        ens.rk4(states, dt, steps)
+        e1.record()
+        torch.cuda.synchronize(dev)
+        direct_ms = e0.elapsed_time(e1)
+        graph_states = [x.clone() for x in init]
+        ens.capture(graph_states, dt)
+        ens.replay(3)                                # warm-up
+        torch.cuda.synchronize(dev)
+        e0.record()
+        ens.replay(steps)
+        e1.record()
+        torch.cuda.synchronize(dev)
+        graph_ms = e0.elapsed_time(e1)
+        # same trajectory through both paths: compare after 3 + steps steps
+        same = all(torch.equal(a, b) for a, b in zip(states, graph_states))
+        finals[prec] = states
+        out[prec] = {"members_per_s": ens.members * steps / (graph_ms / 1000.0),
+                     "ms_per_step_graph": graph_ms / steps, "ms_per_step_direct": direct_ms / steps,
+                     "graph_equals_direct": bool(same), "autotune": report.strip().splitlines()}
+        ens.close()
+    rel = []
+    for a, b in zip(finals["split"], finals["fp64"]):
+        rel.append(float(torch.linalg.vector_norm(a - b) / torch.linalg.vector_norm(b)))
+    out["rel_l2_split_vs_fp64_per_group"] = rel
+    out["split_vs_fp64_speedup"] = out["fp64"]["ms_per_step_graph"] / out["split"]["ms_per_step_graph"]
+    return out
+
+
+def adjoint_measure(dev, members: int = 8, nsteps: int = 48, every: int = 8, dt: float = 240.0):
+    """Gradient of the area-weighted final-geopotential misfit through 48 SWE
+    RK4 steps (192x384, l_max 127, checkpoints every 8 steps) for `members`
+    independent initial states per evaluation; FP64 and split precision."""
+    import torch
+    import aeolus_gb300 as ae
+    from aeolus_gb300 import _lib, workloads as W
+    from aeolus_gb300.adjoint import swe_rk4_checkpointed, weighted_phi_misfit
+    from aeolus_gb300.ops import synthesize
+    from aeolus_gb300.shallow_water import ShallowWaterModel
+
+    out = {"workload": f"swe_adjoint_gauss{NLAT}x{NLON}_lmax{LMAX}_{nsteps}steps_ckpt{every}",
+           "members_per_evaluation": members, "dt_s": dt}
+    grads = {}
+    for prec in ("fp64", "split"):
+        planet = ae.make_planet("latlon", nlat=NLAT, nlon=NLON, l_max=LMAX, device=dev)
+        if prec == "split":
+            planet.so._product_space.sh.plan.set_precision(_lib.PREC_SPLIT_BF16)
+        s0, depth = W.member_states(LMAX, members, seed=11)
+        st, _ = W.member_states(LMAX, members, seed=12)
+        model = ShallowWaterModel(planet, gravity=W.GRAVITY, mean_depth=depth)
+        y0 = torch.as_tensor(s0, device=dev)
+        target = synthesize(model._state_plan.id, model.rk4(torch.as_tensor(st, device=dev), dt, nsteps,
+                                                            check=False)[:, 2])
+
+        def evaluate():
+            y = y0.clone().requires_grad_(True)
+            J = weighted_phi_misfit(model, swe_rk4_checkpointed(model, y, dt, nsteps, every), target).sum()
+            (g,) = torch.autograd.grad(J, y)
+            return g
+
+        evaluate()                                   # warm-up
+        torch.cuda.synchronize(dev)
+        torch.cuda.reset_peak_memory_stats(dev)
+        t0 = time.perf_counter()
+        reps = 2
+        for _ in range(reps):
+            g = evaluate()
+        torch.cuda.synchronize(dev)
+        sec = (time.perf_counter() - t0) / reps
+        grads[prec] = g
+        out[prec] = {"gradient_evaluations_per_s": members / sec, "seconds_per_batch": sec,
+                     "peak_memory_bytes": int(torch.cuda.max_memory_allocated(dev))}
+    d = grads["split"] - grads["fp64"]
+    out["rel_l2_split_vs_fp64_gradient"] = [
+        float(torch.linalg.vector_norm(d[:, f]) / torch.linalg.vector_norm(grads["fp64"][:, f])) for f in range(3)]
+    return out
 
 
 # ------------------------------------------------------------ CPU baseline
@@ -420,6 +534,11 @@ def main():
     roof, roof_all = _roofline(kstats, B, peaks)
     launches = sum(n for n, _ in kstats.values())
 
+    extras = {}
+    if rank == 0 and not args.no_extras:
+        extras["ensemble"] = ensemble_measure(dev)
+        extras["adjoint"] = adjoint_measure(dev)
+
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
         v, desc, _ = cpu_reference_sample(B, args.cpu_rows, 1)
@@ -441,6 +560,7 @@ def main():
                 "gpu_launches": launches,
                 "kernels": {k: {"launches": n, "ms": ms} for k, (n, ms) in kstats.items()},
                 "roofline": roof, "roofline_all": roof_all, "cpu_baseline": cpu, "clocks": clk.summary()}
+        line.update(extras)
         print(json.dumps(line), flush=True)
     if world > 1:
         dist.destroy_process_group()

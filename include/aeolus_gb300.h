@@ -243,6 +243,41 @@ int aeolus_swe_invariants(aeolus_plan state_plan, const aeolus_swe_params* p,
                           const double* state, double* out, int batch,
                           void* work, size_t work_bytes, void* stream);
 
+/* ---- batched uneven ensembles (BVE) --------------------------------------
+ * Groups of BVE members, each group on its own Gauss product-space plan
+ * (any l_max; all plans on one device and one contraction precision),
+ * advanced together: every RK4 stage launches each stage kernel once for all
+ * groups.  The reference runs one state per process (run/bve/runner.py:
+ * 211-216); this has no counterpart there.  zeta[g] is group g's device
+ * state [batch_g][L_g+1][L_g+1], advanced in place. */
+typedef struct aeolus_ensemble_s* aeolus_ensemble;
+
+int aeolus_ensemble_create(int ngroups, const aeolus_plan* plans,
+                           const int* batch, const aeolus_bve_params* params,
+                           aeolus_ensemble* out);
+int aeolus_ensemble_destroy(aeolus_ensemble e);
+int aeolus_ensemble_workspace_bytes(aeolus_ensemble e, size_t* bytes);
+int aeolus_ensemble_bve_rk4(aeolus_ensemble e, double* const* zeta, double dt,
+                            int nsteps, void* work, size_t work_bytes,
+                            void* stream);
+
+/* Captures one RK4 step of the ensemble (these zeta pointers, dt and
+ * workspace, which must stay valid) into a CUDA graph; `stream` must not be
+ * the legacy default stream.  The states are not advanced.  Replay with
+ * aeolus_ensemble_launch (nsteps graph launches on `stream`). */
+int aeolus_ensemble_capture(aeolus_ensemble e, double* const* zeta,
+                            double dt, void* work, size_t work_bytes,
+                            void* stream);
+int aeolus_ensemble_launch(aeolus_ensemble e, int nsteps, void* stream);
+
+/* Times candidate launch shapes (members per CTA of the Legendre or slicing
+ * kernels per group, threads of the row stage) on the ensemble's own states,
+ * keeps the fastest in the plans and writes a text report.  States are not
+ * advanced; results do not depend on the shapes.  Drops a captured graph. */
+int aeolus_ensemble_autotune(aeolus_ensemble e, double* const* zeta,
+                             void* work, size_t work_bytes, void* stream,
+                             char* report, size_t report_len);
+
 /* ---- adjoints (differentiation) ----------------------------------------
  * The reference differentiates nothing; these are the transposes of the
  * linear maps above and the vector-Jacobian products of the tendencies and
