@@ -346,7 +346,7 @@ size_t adjoint_op_bytes(const aeolus_plan_impl* p, int op, int batch) {
              7 * align256(state_bytes(p, 1, batch));
     case AEOLUS_OP_SWE_RK4_ADJOINT:
       return std::max(swe_tadj_bytes(p, batch), full_chain_bytes<9, 4>(p, batch)) +
-             7 * align256(state_bytes(p, 3, batch));
+             7 * align256(state_bytes(p, 3, batch)) + align256(state_bytes(p, 2, batch));
     default:
       return 0;
   }
@@ -448,14 +448,15 @@ extern "C" int aeolus_swe_rk4_adjoint(aeolus_plan plan, const aeolus_swe_params*
   double2* yb = reinterpret_cast<double2*>(state_bar);
   // forward stage inputs, with the same functors (and precision form) as aeolus_swe_rk4
   const bool spec_cor = plan->precision == AEOLUS_PREC_SPLIT_BF16;
+  double2* cor = spec_cor ? reinterpret_cast<double2*>(w + 7 * sb) : nullptr;
   const double fp = spec_cor ? 0.0 : f10;
   SwePw pw{fp, phi0, (float)phi0};
   double2* next[3] = {y1, y2, y3};
   const double2* in = y0;
   for (int stage = 1; stage <= 3; ++stage) {
-    SweDerive d{sp, in, fp};
+    SweDerive d{sp, in, fp, cor, 2.0 * p->omega};
     Rk4 rk{stage, dt, y0, next[stage - 1], kacc, nullptr};
-    SweEpi e{sp, in, phi0, p->nu4, rk, spec_cor ? 2.0 * p->omega : 0.0};
+    SweEpi e{sp, in, phi0, p->nu4, rk, spec_cor ? 2.0 * p->omega : 0.0, cor};
     if ((s = run_full_chain(plan, d, pw, e, batch, chain, nullptr, st))) return s;
     in = next[stage - 1];
   }

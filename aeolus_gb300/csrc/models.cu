@@ -346,11 +346,12 @@ size_t op_bytes(const aeolus_plan_impl* p, int op, int batch) {
     case AEOLUS_OP_WINDS:
       return synth_chain_bytes<2, 2>(p, batch);
     case AEOLUS_OP_SWE_TENDENCY:
-      return full_chain_bytes<9, 4>(p, batch);
+      return full_chain_bytes<9, 4>(p, batch) + align256(state_bytes(p, 2, batch));
     case AEOLUS_OP_BVE_RK4:
       return full_chain_bytes<4, 1>(p, batch) + 2 * align256(state_bytes(p, 1, batch));
     case AEOLUS_OP_SWE_RK4:
-      return full_chain_bytes<9, 4>(p, batch) + 3 * align256(state_bytes(p, 3, batch));
+      return full_chain_bytes<9, 4>(p, batch) + 3 * align256(state_bytes(p, 3, batch)) +
+             align256(state_bytes(p, 2, batch));
     case AEOLUS_OP_SWE_VALIDATE:
       return synth_chain_bytes<1, 1>(p, batch) + align256((size_t)batch * p->npoints * 8) +
              align256((size_t)batch * sizeof(double2));
@@ -431,10 +432,13 @@ extern "C" int aeolus_swe_tendency(aeolus_plan plan, const aeolus_swe_params* p,
   const double phi0 = p->gravity * p->mean_depth;
   const bool spec_cor = plan->precision == AEOLUS_PREC_SPLIT_BF16;
   const double fp = spec_cor ? 0.0 : f10;
-  SweDerive d{sp, reinterpret_cast<const double2*>(state), fp};
+  // split path: the Coriolis spectra are tabulated by the derive stage after the chain scratch
+  double2* cor = spec_cor ? reinterpret_cast<double2*>(static_cast<char*>(work) + full_chain_bytes<9, 4>(plan, batch))
+                          : nullptr;
+  SweDerive d{sp, reinterpret_cast<const double2*>(state), fp, cor, 2.0 * p->omega};
   SwePw pw{fp, phi0, (float)phi0};
   Rk4 rk{0, 0.0, nullptr, nullptr, nullptr, reinterpret_cast<double2*>(tend)};
-  SweEpi e{sp, reinterpret_cast<const double2*>(state), phi0, p->nu4, rk, spec_cor ? 2.0 * p->omega : 0.0};
+  SweEpi e{sp, reinterpret_cast<const double2*>(state), phi0, p->nu4, rk, spec_cor ? 2.0 * p->omega : 0.0, cor};
   return run_full_chain(plan, d, pw, e, batch, work, nullptr, static_cast<cudaStream_t>(stream));
 }
 
@@ -487,17 +491,19 @@ extern "C" int aeolus_swe_rk4(aeolus_plan plan, const aeolus_swe_params* p, doub
   stage_buf[1] = reinterpret_cast<double2*>(w);
   w += align256(state_bytes(plan, 3, batch));
   double2* acc = reinterpret_cast<double2*>(w);
+  w += align256(state_bytes(plan, 3, batch));
   double2* y0 = reinterpret_cast<double2*>(state);
   const bool spec_cor = plan->precision == AEOLUS_PREC_SPLIT_BF16;
+  double2* cor = spec_cor ? reinterpret_cast<double2*>(w) : nullptr;  // Coriolis spectra of the stage input
   const double fp = spec_cor ? 0.0 : f10;
   SwePw pw{fp, phi0, (float)phi0};
   for (int it = 0; it < nsteps; ++it)
     for (int stage = 1; stage <= 4; ++stage) {
       const double2* in = stage == 1 ? y0 : stage_buf[stage & 1];        // 2 -> buf0, 3 -> buf1, 4 -> buf0
       double2* next = stage_buf[(stage + 1) & 1];                        // 1 -> buf0, 2 -> buf1, 3 -> buf0
-      SweDerive d{sp, in, fp};
+      SweDerive d{sp, in, fp, cor, 2.0 * p->omega};
       Rk4 rk{stage, dt, y0, next, acc, nullptr};
-      SweEpi e{sp, in, phi0, p->nu4, rk, spec_cor ? 2.0 * p->omega : 0.0};
+      SweEpi e{sp, in, phi0, p->nu4, rk, spec_cor ? 2.0 * p->omega : 0.0, cor};
       if ((s = run_full_chain(plan, d, pw, e, batch, chain, status, st))) return s;
     }
   return AEOLUS_OK;

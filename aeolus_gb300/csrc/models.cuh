@@ -206,7 +206,20 @@ struct SweDerive {
     v[6] = zl;
     v[7] = s.at(d, l, m);
     v[8] = pl;
+    if (cor) {
+      // planetary-vorticity terms of the split path (added by SweEpi), from the
+      // fields at hand: zeta_dot += -(2 Omega/a) V - 2 Omega (x delta),
+      // curl += 2 Omega (x zeta) - (2 Omega/a) U
+      const double wr = two_omega * ir;
+      const double2 xz = s.xmul(eta_lo, eta_hi, l, m);
+      const double2 xd = s.xmul(lo ? s.at(d, l - 1, m) : zero, hi ? s.at(d, l + 1, m) : zero, l, m);
+      double2* c = cor + (long)b * 2 * n2 + (long)l * (L + 1) + m;
+      c[0] = make_double2(-(wr * v[1].x + two_omega * xd.x), -(wr * v[1].y + two_omega * xd.y));
+      c[n2] = make_double2(two_omega * xz.x - wr * v[0].x, two_omega * xz.y - wr * v[0].y);
+    }
   }
+  double2* cor = nullptr;   // optional [b][2][L+1][L+1] Coriolis spectra (split path, f10 = 0)
+  double two_omega = 0.0;
 };
 
 // Products of physics/shallow_water.py:375-386 (module docstring identities).
@@ -266,6 +279,7 @@ struct SweEpi {
   double phi0, nu4;
   Rk4 rk;
   double two_omega;      // > 0: add the Coriolis terms spectrally
+  const double2* cor = nullptr;  // their spectra tabulated by SweDerive (else computed here)
   __device__ void finish(int b, int l, int m, const double2* an_in) const {
     const int L = s.L;
     const int cut = (2 * L) / 3;
@@ -275,20 +289,26 @@ struct SweEpi {
     const double2 z0 = make_double2(0.0, 0.0);
     double2 an[4] = {an_in[0], an_in[1], an_in[2], an_in[3]};
     if (two_omega > 0.0 && !tr) {
-      const double2* z = state + (long)b * 3 * n2;
-      const double2* d = z + n2;
-      const bool lo = l >= 1, hi = l + 1 <= L;
-      const double ir = s.ir;
-      const double2 psi = s.invlap0(z, l, m), chi = s.invlap0(d, l, m);
-      const double2 psi_lo = lo ? s.invlap0(z, l - 1, m) : z0, psi_hi = hi ? s.invlap0(z, l + 1, m) : z0;
-      const double2 chi_lo = lo ? s.invlap0(d, l - 1, m) : z0, chi_hi = hi ? s.invlap0(d, l + 1, m) : z0;
-      const double2 U = cadd(cscale(ir, s.snt(psi_lo, psi_hi, l, m)), s.dlam(chi, m));
-      const double2 V = csub(s.dlam(psi, m), cscale(ir, s.snt(chi_lo, chi_hi, l, m)));
-      const double2 xz = s.xmul(lo ? s.at(z, l - 1, m) : z0, hi ? s.at(z, l + 1, m) : z0, l, m);
-      const double2 xd = s.xmul(lo ? s.at(d, l - 1, m) : z0, hi ? s.at(d, l + 1, m) : z0, l, m);
-      const double wr = two_omega * ir;
-      an[0] = csub(an[0], cadd(cscale(wr, V), cscale(two_omega, xd)));
-      an[1] = cadd(an[1], csub(cscale(two_omega, xz), cscale(wr, U)));
+      if (cor) {  // tabulated by SweDerive for this stage input
+        const double2* c = cor + (long)b * 2 * n2 + (long)l * (L + 1) + m;
+        an[0] = cadd(an[0], c[0]);
+        an[1] = cadd(an[1], c[n2]);
+      } else {
+        const double2* z = state + (long)b * 3 * n2;
+        const double2* d = z + n2;
+        const bool lo = l >= 1, hi = l + 1 <= L;
+        const double ir = s.ir;
+        const double2 psi = s.invlap0(z, l, m), chi = s.invlap0(d, l, m);
+        const double2 psi_lo = lo ? s.invlap0(z, l - 1, m) : z0, psi_hi = hi ? s.invlap0(z, l + 1, m) : z0;
+        const double2 chi_lo = lo ? s.invlap0(d, l - 1, m) : z0, chi_hi = hi ? s.invlap0(d, l + 1, m) : z0;
+        const double2 U = cadd(cscale(ir, s.snt(psi_lo, psi_hi, l, m)), s.dlam(chi, m));
+        const double2 V = csub(s.dlam(psi, m), cscale(ir, s.snt(chi_lo, chi_hi, l, m)));
+        const double2 xz = s.xmul(lo ? s.at(z, l - 1, m) : z0, hi ? s.at(z, l + 1, m) : z0, l, m);
+        const double2 xd = s.xmul(lo ? s.at(d, l - 1, m) : z0, hi ? s.at(d, l + 1, m) : z0, l, m);
+        const double wr = two_omega * ir;
+        an[0] = csub(an[0], cadd(cscale(wr, V), cscale(two_omega, xd)));
+        an[1] = cadd(an[1], csub(cscale(two_omega, xz), cscale(wr, U)));
+      }
     }
     const double2 a0 = tr ? z0 : an[0], a1 = tr ? z0 : an[1], a2 = tr ? z0 : an[2], a3 = tr ? z0 : an[3];
     const double2 zs = state[base], ds = state[base + n2], ps = state[base + 2 * n2];

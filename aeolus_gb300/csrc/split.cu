@@ -167,3 +167,25 @@ extern "C" int aeolus_plan_set_precision(aeolus_plan plan, int precision, int sl
   plan->slices = kSlices;
   return AEOLUS_OK;
 }
+
+extern "C" int aeolus_plan_set_tuning(aeolus_plan plan, const int* knobs) {
+  if (!plan_ok(plan) || !knobs) return fail(AEOLUS_ERR_ARG, "aeolus_plan_set_tuning: bad arguments");
+  if (knobs[0] < 0 || knobs[1] < 0 || knobs[3] < 0 || knobs[0] > 64 || knobs[1] > 64 || knobs[3] > 64)
+    return fail(AEOLUS_ERR_ARG, "aeolus_plan_set_tuning: members per CTA must be in 0..64");
+  if (knobs[2] != 0 && (knobs[2] < 64 || knobs[2] > 256 || knobs[2] % 32 != 0))
+    return fail(AEOLUS_ERR_ARG, "aeolus_plan_set_tuning: row threads must be 0 or a multiple of 32 in 64..256");
+  plan->tune_bc_synth = knobs[0];
+  plan->tune_bc_anal = knobs[1];
+  plan->tune_row_threads = knobs[2];
+  plan->tune_slice_mb = knobs[3];
+  return AEOLUS_OK;
+}
+
+extern "C" int aeolus_plan_get_tuning(aeolus_plan plan, int* knobs) {
+  if (!plan_ok(plan) || !knobs) return fail(AEOLUS_ERR_ARG, "aeolus_plan_get_tuning: bad arguments");
+  knobs[0] = plan->tune_bc_synth;
+  knobs[1] = plan->tune_bc_anal;
+  knobs[2] = plan->tune_row_threads;
+  knobs[3] = plan->tune_slice_mb;
+  return AEOLUS_OK;
+}

@@ -46,6 +46,7 @@ class Plan:
         check(lib.aeolus_plan_info(self.handle, byref(kind), byref(nlat), byref(nlon), byref(lmax), byref(npts)))
         self.kind, self.nlat, self.nlon = kind.value, nlat.value, nlon.value
         self.lmax, self.n_points = lmax.value, npts.value
+        self.precision = _lib.PREC_FP64
         self.id = handle
         with _LOCK:
             _PLANS[self.id] = self
@@ -83,6 +84,17 @@ class Plan:
 
     def set_precision(self, precision: int, slices: int = 0):
         check(_lib.load().aeolus_plan_set_precision(self.handle, int(precision), int(slices)))
+        self.precision = int(precision)
+
+    def tuning(self) -> tuple[int, int, int, int]:
+        """(bc_synth, bc_anal, row_threads, slice_members); 0 = heuristic."""
+        k = (c_int * 4)()
+        check(_lib.load().aeolus_plan_get_tuning(self.handle, k))
+        return tuple(k)
+
+    def set_tuning(self, knobs) -> None:
+        k = (c_int * 4)(*[int(x) for x in knobs])
+        check(_lib.load().aeolus_plan_set_tuning(self.handle, k))
 
     def workspace(self, op: int, batch: int) -> torch.Tensor:
         n = c_size_t()

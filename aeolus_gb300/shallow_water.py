@@ -121,6 +121,46 @@ class ShallowWaterModel:
                 raise ShallowWaterStateError(self._describe_bits(bits, "during RK4 stages"))
         return y
 
+    def autotune(self, coeffs: torch.Tensor, dt: float, reps: int = 3) -> dict:
+        """Pick the product plan's launch shapes for this batch by timing one
+        RK4 step per candidate with CUDA events (results are bitwise
+        independent of the shapes).  Returns {knobs: ms per step}."""
+        plan = self._plan
+        split = getattr(plan, "precision", _lib.PREC_FP64) == _lib.PREC_SPLIT_BF16
+        base = list(plan.tuning())
+        stream = torch.cuda.current_stream(coeffs.device)
+
+        def time_knobs(knobs):
+            plan.set_tuning(knobs)
+            self.rk4(coeffs, dt, 1, check=False)
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            for _ in range(reps):
+                self.rk4(coeffs, dt, 1, check=False)
+            b.record(stream)
+            b.synchronize()
+            return a.elapsed_time(b) / reps
+
+        results = {}
+        best = list(base)
+        best_ms = time_knobs(best)
+        results[tuple(best)] = best_ms
+        B = coeffs.reshape(-1, 3, self.l_max + 1, self.l_max + 1).shape[0]
+        # knob 2: row-stage threads; 0/1: FP64 Legendre members per CTA; 3: split slicing members per CTA
+        choices = [(2, (128, 192, 256))] + ([(3, (1, 2, 4, 8))] if split else [(0, (1, 2, 3, 4)), (1, (1, 2, 3, 4))])
+        for idx, cands in choices:
+            for c in cands:
+                if idx != 2 and c > B:
+                    continue
+                knobs = list(best)
+                knobs[idx] = c
+                ms = time_knobs(knobs)
+                results[tuple(knobs)] = ms
+                if ms < best_ms:
+                    best, best_ms = knobs, ms
+        plan.set_tuning(best)
+        return {"chosen": tuple(best), "ms_per_step": best_ms, "timed": {str(k): v for k, v in results.items()}}
+
     # -- validation ----------------------------------------------------------
     def _validate_raw(self, coeffs):
         return swe_validate(self._state_plan.id, self._plan.id, self.R, self.Omega, self.gravity,

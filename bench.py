@@ -482,11 +482,15 @@ def main():
         torch.cuda.synchronize(dev)
 
     warm = max(args.warmup, 3)
-    for m in (model, other):
+    tuning = {}
+    for name, m in (("split" if args.precision == "split" else "fp64", model), ("fp64", other)):
         if m is not None:
             y = y0
             for _ in range(warm):
                 y = m.rk4(y, DT, 1, check=False)
+            tuned = m.autotune(y0, DT)   # launch shapes for this batch; results do not depend on them
+            tuning[name] = {"knobs_bc_synth_bc_anal_row_threads_slice_mb": list(tuned["chosen"]),
+                            "ms_per_step": tuned["ms_per_step"]}
     barrier()
 
     with ClockSampler(local) as clk:
@@ -553,6 +557,7 @@ def main():
                 "config": dict(workload_config(args, B), l2="flushed between steps (256 MiB write)"
                                if flush is not None else "not flushed"),
                 "member_steps_per_s": value * B,
+                "autotune": tuning,
                 "split_vs_fp64": comparison,
                 "e2e": {"value": world * args.steps / (e2e_ms / 1000.0), "unit": UNIT,
                         "h2d_bytes_per_step": bytes_state, "d2h_bytes_per_step": bytes_state + 4 * B,

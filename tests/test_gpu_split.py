@@ -94,3 +94,20 @@ def test_split_rejects_unsupported_shapes():
     p = Plan.gauss(256, 512, 170)
     with pytest.raises(ValueError, match="l_max"):
         p.set_precision(_lib.PREC_SPLIT_BF16)
+
+
+@pytest.mark.parametrize("precision", ["fp64", "split"])
+def test_swe_autotune_is_bitwise_neutral(precision):
+    """Launch shapes picked by the autotuner change no result bit."""
+    L = 85
+    planet = ae.make_planet("latlon", nlat=128, nlon=256, l_max=L)
+    if precision == "split":
+        planet.so._product_space.sh.plan.set_precision(_lib.PREC_SPLIT_BF16)
+    s, depth = W.member_states(L, 5, seed=21)
+    model = ShallowWaterModel(planet, gravity=W.GRAVITY, mean_depth=depth)
+    y0 = torch.as_tensor(s, device="cuda")
+    before = model.rk4(y0, 300.0, 2, check=False)
+    out = model.autotune(y0, 300.0, reps=1)
+    assert len(out["chosen"]) == 4 and out["ms_per_step"] > 0
+    after = model.rk4(y0, 300.0, 2, check=False)
+    assert torch.equal(before, after)
