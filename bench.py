@@ -462,7 +462,8 @@ def main():
 
     lib = _lib.load()
     B = args.members
-    states, depth = W.member_states(LMAX, B, seed=1000 * rank)
+    from aeolus_gb300.replicas import max_over_ranks, member_seed_base
+    states, depth = W.member_states(LMAX, B, seed=member_seed_base(rank, B))
 
     def build(precision):
         planet = ae.make_planet("latlon", nlat=NLAT, nlon=NLON, l_max=LMAX, device=dev)
@@ -497,10 +498,7 @@ def main():
         barrier()
         total_ms, kstats, y_main = _timed_steps(model, y0, args.steps, flush, stream, lib, _lib)
         barrier()
-    if world > 1:
-        t = torch.tensor([total_ms], device=dev, dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total_ms = float(t.item())
+    total_ms = max_over_ranks(total_ms, dev)
     value = world * args.steps / (total_ms / 1000.0)
 
     comparison = None
@@ -528,10 +526,7 @@ def main():
     barrier()
     e2e_ms = e0.elapsed_time(e1)
     e2e_wall_ms = (time.perf_counter() - t_wall) * 1000.0
-    if world > 1:
-        t = torch.tensor([e2e_ms], device=dev, dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_ms = float(t.item())
+    e2e_ms = max_over_ranks(e2e_ms, dev)
     bytes_state = host_in.numel() * host_in.element_size()
 
     peaks = json.loads(PEAKS_FILE.read_text()) if PEAKS_FILE.exists() else {}
