@@ -9,6 +9,7 @@
 #include "pipeline.cuh"
 #include "points.cuh"
 #include "split.cuh"
+#include "dense.cuh"
 
 namespace aeolus {
 
@@ -17,6 +18,26 @@ inline unsigned blocks_for(long n, int t) { return (unsigned)((n + t - 1) / t); 
 // ---------------------------------------------------------------- sizes
 inline bool split_on(const aeolus_plan_impl* p) {
   return p->kind == kGauss && p->precision == AEOLUS_PREC_SPLIT_BF16 && p->split != nullptr;
+}
+// point-set plan with split-precision (tensor-core) basis products
+inline bool dense_on(const aeolus_plan_impl* p) {
+  return p->kind == kPoints && p->precision == AEOLUS_PREC_SPLIT_BF16 && p->split != nullptr;
+}
+inline size_t dense_extra(const aeolus_plan_impl* p, int ncols) { return dense_on(p) ? dense_bytes(p, ncols) : 0; }
+
+// Basis products of a point-set plan (FP64 GEMM or the split-precision
+// tensor-core product), see points.cuh / dense.cuh.
+inline int points_synth(const aeolus_plan_impl* p, const double* V, double* out, int ncols, void* scratch,
+                        cudaStream_t st) {
+  if (!dense_on(p)) return points_gemm_synth(p, V, out, ncols, st);
+  return dense_split_gemm(p, dense_synth_dims(p, ncols), p->split->bsyn, p->split->ebsyn, V, p->ncol, p->ncol, out,
+                          p->npoints, scratch, st, "tc_dense_synth_bf16x6");
+}
+inline int points_analysis(const aeolus_plan_impl* p, const double* W, double* C, int ncols, void* scratch,
+                           cudaStream_t st) {
+  if (!dense_on(p)) return points_gemm_analysis(p, W, C, ncols, st);
+  return dense_split_gemm(p, dense_anal_dims(p, ncols), p->split->bana, p->split->ebana, W, p->npoints,
+                          (int)p->npoints, C, p->ncol, scratch, st, "tc_dense_anal_bf16x6");
 }
 
 template <int NIN, int NOUT>
@@ -27,21 +48,24 @@ size_t full_chain_bytes(const aeolus_plan_impl* p, int batch) {
   if (p->kind == kGauss) return align256(fg_bytes(p, NIN > NOUT ? NIN : NOUT, batch));
   const size_t nc = p->ncol, np = p->npoints;
   return align256((size_t)batch * NIN * nc * 8) + align256((size_t)batch * NIN * np * 8) +
-         align256((size_t)batch * NOUT * np * 8) + align256((size_t)batch * NOUT * nc * 8);
+         align256((size_t)batch * NOUT * np * 8) + align256((size_t)batch * NOUT * nc * 8) +
+         dense_extra(p, batch * (NIN > NOUT ? NIN : NOUT));
 }
 
 template <int NIN, int NOUT>
 size_t synth_chain_bytes(const aeolus_plan_impl* p, int batch) {
   if (split_on(p)) return align256(fg_bytes(p, NIN, batch)) + split_synth_bytes(p, NIN, batch);
   if (p->kind == kGauss) return align256(fg_bytes(p, NIN, batch));
-  return align256((size_t)batch * NIN * p->ncol * 8) + align256((size_t)batch * NIN * p->npoints * 8);
+  return align256((size_t)batch * NIN * p->ncol * 8) + align256((size_t)batch * NIN * p->npoints * 8) +
+         dense_extra(p, batch * NIN);
 }
 
 template <int NIN, int NOUT>
 size_t anal_chain_bytes(const aeolus_plan_impl* p, int batch) {
   if (split_on(p)) return align256(fg_bytes(p, NOUT, batch)) + split_anal_bytes(p, NOUT, batch);
   if (p->kind == kGauss) return align256(fg_bytes(p, NOUT, batch));
-  return align256((size_t)batch * NOUT * p->npoints * 8) + align256((size_t)batch * NOUT * p->ncol * 8);
+  return align256((size_t)batch * NOUT * p->npoints * 8) + align256((size_t)batch * NOUT * p->ncol * 8) +
+         dense_extra(p, batch * NOUT);
 }
 
 // ---------------------------------------------------------------- chains
@@ -74,15 +98,17 @@ int run_full_chain(const aeolus_plan_impl* p, const Derive& d, const Pw& pw, con
   double* Wt = reinterpret_cast<double*>(w);
   w += align256((size_t)batch * Pw::NOUT * np * 8);
   double* C = reinterpret_cast<double*>(w);
+  w += align256((size_t)batch * Pw::NOUT * nc * 8);
+  void* dscratch = w;
   const long nlm = n_coeff(p->lmax) * batch;
   derive_cols_kernel<Derive><<<blocks_for(nlm, 128), 128, 0, st>>>(p->lmax, batch, nc, V, d);
   AE_LAUNCH("derive_cols_kernel");
-  int s = points_gemm_synth(p, V, Gr, batch * Pw::NIN, st);
+  int s = points_synth(p, V, Gr, batch * Pw::NIN, dscratch, st);
   if (s) return s;
   points_pointwise_kernel<Pw><<<blocks_for(np * batch, 128), 128, 0, st>>>(
       np, batch, Gr, (long)Pw::NIN * np, np, Wt, (long)Pw::NOUT * np, np, p->coslat, p->fgrid, p->wpts, status, pw);
   AE_LAUNCH("points_pointwise_kernel");
-  if ((s = points_gemm_analysis(p, Wt, C, batch * Pw::NOUT, st))) return s;
+  if ((s = points_analysis(p, Wt, C, batch * Pw::NOUT, dscratch, st))) return s;
   const long n2 = (long)(p->lmax + 1) * (p->lmax + 1) * batch;
   epilogue_cols_kernel<Epi><<<blocks_for(n2, 128), 128, 0, st>>>(p->lmax, batch, nc, C, e);
   AE_LAUNCH("epilogue_cols_kernel");
@@ -115,11 +141,13 @@ int run_synth_chain(const aeolus_plan_impl* p, const Derive& d, const Pw& pw, in
   double* V = reinterpret_cast<double*>(w);
   w += align256((size_t)batch * Pw::NIN * nc * 8);
   double* Gr = reinterpret_cast<double*>(w);
+  w += align256((size_t)batch * Pw::NIN * np * 8);
+  void* dscratch = w;
   const long nlm = n_coeff(p->lmax) * batch;
   derive_cols_kernel<Derive><<<blocks_for(nlm, 128), 128, 0, st>>>(p->lmax, batch, nc, V, d);
   AE_LAUNCH("derive_cols_kernel");
   const bool direct = Pw::kIdentity && out_b == np;
-  int s = points_gemm_synth(p, V, direct ? out : Gr, batch * Pw::NIN, st);
+  int s = points_synth(p, V, direct ? out : Gr, batch * Pw::NIN, dscratch, st);
   if (s || direct) return s;
   points_pointwise_kernel<Pw><<<blocks_for(np * batch, 128), 128, 0, st>>>(
       np, batch, Gr, (long)Pw::NIN * np, np, out, out_b, out_f, p->coslat, p->fgrid, nullptr, status, pw);
@@ -156,11 +184,13 @@ int run_anal_chain(const aeolus_plan_impl* p, const Pw& pw, const Epi& e, int ba
   double* Wt = reinterpret_cast<double*>(w);
   w += align256((size_t)batch * Pw::NOUT * np * 8);
   double* C = reinterpret_cast<double*>(w);
+  w += align256((size_t)batch * Pw::NOUT * nc * 8);
+  void* dscratch = w;
   points_pointwise_kernel<Pw><<<blocks_for(np * batch, 128), 128, 0, st>>>(
       np, batch, in, in_b, in_f, Wt, (long)Pw::NOUT * np, np, p->coslat, p->fgrid, unit_weights ? nullptr : p->wpts,
       nullptr, pw);
   AE_LAUNCH("points_pointwise_kernel");
-  int s = points_gemm_analysis(p, Wt, C, batch * Pw::NOUT, st);
+  int s = points_analysis(p, Wt, C, batch * Pw::NOUT, dscratch, st);
   if (s) return s;
   const long n2 = (long)(p->lmax + 1) * (p->lmax + 1) * batch;
   epilogue_cols_kernel<Epi><<<blocks_for(n2, 128), 128, 0, st>>>(p->lmax, batch, nc, C, e);

@@ -137,6 +137,7 @@ __global__ void __launch_bounds__(256) g_slice_anal(Grouped<SliceAnalArg> g) {
 // Persistent tensor-core tiles of all groups in one list.
 template <class Sched>
 struct GroupedSched {
+  static constexpr int kSegChunks = Sched::kSegChunks;
   int n;
   int start[kMaxGroups + 1];
   Sched s[kMaxGroups];

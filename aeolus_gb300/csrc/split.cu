@@ -38,6 +38,10 @@ void free_split(aeolus_plan_impl* p) {
   if (t->eana) cudaFree(t->eana);
   if (t->kcum) cudaFree(t->kcum);
   if (t->err) cudaFree(t->err);
+  if (t->bsyn) cudaFree(t->bsyn);
+  if (t->bana) cudaFree(t->bana);
+  if (t->ebsyn) cudaFree(t->ebsyn);
+  if (t->ebana) cudaFree(t->ebana);
   delete t;
   p->split = nullptr;
 }
@@ -102,11 +106,93 @@ __global__ void split_pana_kernel(int L, int nlat, int nh, int NK, const double*
   }
 }
 
+// Point-set basis digits, synthesis role (rows = points, K = the ncol real
+// columns).  The basis is column-major (point fastest): per-point maxima
+// with one thread per point, then the digits over a (point tile, 8-chunk
+// group) grid, coalesced along the points.
+__global__ void dense_rowmax_kernel(long np, int ncol, const double* __restrict__ B, int* __restrict__ eout) {
+  const long p = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  const long npad = (np + 127) / 128 * 128;
+  if (p >= npad) return;
+  unsigned long long mx = 0ull;
+  if (p < np)
+    for (int c = 0; c < ncol; ++c) mx = max(mx, abs_key(B[(long)c * np + p]));
+  eout[p] = p < np ? exponent_for_key(mx) : 0;
+}
+
+__global__ void dense_bsyn_kernel(long np, int ncol, int nkc, const double* __restrict__ B,
+                                  const int* __restrict__ erow, __nv_bfloat16* __restrict__ out) {
+  const long p = (long)blockIdx.x * 128 + threadIdx.x;  // 128 threads = one point tile
+  const int E = erow[p];
+  __nv_bfloat16* tile = out + (long long)blockIdx.x * nkc * chunk_elems(128);
+  const int c0 = blockIdx.y * 8 * kKC, c1 = min(nkc * kKC, c0 + 8 * kKC);
+  for (int c = c0; c < c1; ++c) {
+    float d[kSlices];
+    digits((p < np && c < ncol) ? B[(long)c * np + p] : 0.0, E, d);
+    for (int s = 0; s < kSlices; ++s) tile[tile_elem(128, s, threadIdx.x, c)] = __float2bfloat16(d[s]);
+  }
+}
+
+// Analysis role (rows = basis columns, K = points): one CTA per (padded)
+// column.
+__global__ void __launch_bounds__(256) dense_bana_kernel(long np, int ncol, int nkc, const double* __restrict__ B,
+                                                         __nv_bfloat16* __restrict__ out, int* __restrict__ eout) {
+  __shared__ unsigned long long s_mx[8];
+  __shared__ int s_e;
+  const int c = blockIdx.x;
+  const double* col = B + (long)c * np;
+  unsigned long long mx = 0ull;
+  if (c < ncol)
+    for (long p = threadIdx.x; p < np; p += blockDim.x) mx = max(mx, abs_key(col[p]));
+  for (int o = 16; o > 0; o >>= 1) mx = max(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+  if ((threadIdx.x & 31) == 0) s_mx[threadIdx.x >> 5] = mx;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    unsigned long long m2 = 0ull;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) m2 = max(m2, s_mx[w]);
+    s_e = c < ncol ? exponent_for_key(m2) : 0;
+    eout[c] = s_e;
+  }
+  __syncthreads();
+  const int E = s_e;
+  __nv_bfloat16* tile = out + (long long)(c / 128) * nkc * chunk_elems(128);
+  for (long p = threadIdx.x; p < (long)nkc * kKC; p += blockDim.x) {
+    float d[kSlices];
+    digits((c < ncol && p < np) ? col[p] : 0.0, E, d);
+    for (int s = 0; s < kSlices; ++s) tile[tile_elem(128, s, c % 128, (int)p)] = __float2bfloat16(d[s]);
+  }
+}
+
+int split_build_points(aeolus_plan_impl* p) {
+  auto* t = new SplitTables();
+  p->split = t;
+  t->L = p->lmax;
+  const long np = p->npoints;
+  const int ncol = p->ncol;
+  const long mp = (np + 127) / 128, mc = (ncol + 127) / 128;
+  const long nkc_s = (ncol + kKC - 1) / kKC, nkc_a = (np + kKC - 1) / kKC;
+  AE_CUDA(cudaMalloc(&t->bsyn, (size_t)mp * nkc_s * chunk_elems(128) * sizeof(__nv_bfloat16)));
+  AE_CUDA(cudaMalloc(&t->bana, (size_t)mc * nkc_a * chunk_elems(128) * sizeof(__nv_bfloat16)));
+  AE_CUDA(cudaMalloc(&t->ebsyn, (size_t)mp * 128 * sizeof(int)));
+  AE_CUDA(cudaMalloc(&t->ebana, (size_t)mc * 128 * sizeof(int)));
+  AE_CUDA(cudaMalloc(&t->err, sizeof(int)));
+  AE_CUDA(cudaMemset(t->err, 0, sizeof(int)));
+  dense_rowmax_kernel<<<(unsigned)mp, 128>>>(np, ncol, p->basis, t->ebsyn);
+  AE_LAUNCH("dense_rowmax_kernel");
+  dense_bsyn_kernel<<<dim3((unsigned)mp, (unsigned)((nkc_s + 7) / 8)), 128>>>(np, ncol, (int)nkc_s, p->basis, t->ebsyn,
+                                                                             t->bsyn);
+  AE_LAUNCH("dense_bsyn_kernel");
+  dense_bana_kernel<<<(unsigned)(mc * 128), 256>>>(np, ncol, (int)nkc_a, p->basis, t->bana, t->ebana);
+  AE_LAUNCH("dense_bana_kernel");
+  AE_CUDA(cudaDeviceSynchronize());
+  return AEOLUS_OK;
+}
+
 }  // namespace
 
 int split_build(aeolus_plan_impl* p) {
   if (p->split) return AEOLUS_OK;
-  if (p->kind != kGauss) return fail(AEOLUS_ERR_ARG, "split precision is implemented for Gauss plans");
+  if (p->kind == kPoints) return split_build_points(p);
   const int L = p->lmax;
   if (L > 127) return fail(AEOLUS_ERR_ARG, "split precision supports l_max <= 127");
   if (p->nlat > 192) return fail(AEOLUS_ERR_ARG, "split precision supports nlat <= 192 (exact f32 accumulation)");

@@ -29,6 +29,11 @@ struct SplitTables {
   long long* kcum = nullptr;      // [L+2] prefix sums of padded degree counts
   int* err = nullptr;             // sticky device error flag (bounded waits)
   std::vector<long long> h_kcum;
+  // point-set plans: dense real basis digits in both operand roles
+  __nv_bfloat16* bsyn = nullptr;  // rows = points, K = basis columns
+  __nv_bfloat16* bana = nullptr;  // rows = basis columns, K = points
+  int* ebsyn = nullptr;           // per point (padded to 128)
+  int* ebana = nullptr;           // per basis column (padded to 128)
 };
 
 int split_build(aeolus_plan_impl* p);
@@ -583,35 +588,42 @@ __global__ void __launch_bounds__(tc_threads<Epi>(), 1) tc_persistent_kernel(Sch
       const uint64_t dB0 = tc::smem_desc(sm.B(0), 128, kKC * 16);
       uint32_t g = 0;
       int i = 0;
-      for (int t = blockIdx.x; t < ntiles && ok; t += gridDim.x, ++i) {
+      for (int t = blockIdx.x; t < ntiles && ok; t += gridDim.x) {
         const TcTile tl = sc.tile(t);
-        const int buf = i & 1;
-        const uint32_t ub = (uint32_t)i >> 1;
-        if (ub > 0 && !tc::mbar_wait(&sm.tempty[buf], (ub - 1) & 1)) {
-          ok = false;
-          break;
-        }
-        tc::fence_after_sync();
-        const uint32_t dbase = tmem + (uint32_t)(buf * kTmemBuf);
-        for (int kc = 0; kc < tl.nchunks; ++kc, ++g) {
-          const int st = (int)(g % kStages);
-          if (!tc::mbar_wait(&sm.full[st], (g / kStages) & 1)) {
+        // K segments of one tile: each is contracted into a fresh accumulator
+        // buffer and drained by the epilogue (one segment unless the
+        // schedule bounds the depth of an exact f32 sum)
+        const int segc = Sched::kSegChunks > 0 ? Sched::kSegChunks : tl.nchunks;
+        for (int k0 = 0; k0 < tl.nchunks && ok; k0 += segc, ++i) {
+          const int buf = i & 1;
+          const uint32_t ub = (uint32_t)i >> 1;
+          if (ub > 0 && !tc::mbar_wait(&sm.tempty[buf], (ub - 1) & 1)) {
             ok = false;
             break;
           }
           tc::fence_after_sync();
-          const uint64_t off = (uint64_t)(((size_t)st * kStageBytes) >> 4);
-          const uint64_t da0 = dA0 + off, db0 = dB0 + off;
+          const uint32_t dbase = tmem + (uint32_t)(buf * kTmemBuf);
+          const int k1 = min(tl.nchunks, k0 + segc);
+          for (int kc = k0; kc < k1; ++kc, ++g) {
+            const int st = (int)(g % kStages);
+            if (!tc::mbar_wait(&sm.full[st], (g / kStages) & 1)) {
+              ok = false;
+              break;
+            }
+            tc::fence_after_sync();
+            const uint64_t off = (uint64_t)(((size_t)st * kStageBytes) >> 4);
+            const uint64_t da0 = dA0 + off, db0 = dB0 + off;
 #pragma unroll
-          for (int q = 0; q < kPairs; ++q) {
-            const uint64_t da = da0 + (uint64_t)(((size_t)dp.s[q] * 128 * kKC * 2) >> 4);
-            const uint64_t db = db0 + (uint64_t)(((size_t)dp.u[q] * kNT * kKC * 2) >> 4);
-            tc::mma_bf16(dbase + (uint32_t)(dp.a[q] * kNT), da, db, idesc, (kc > 0 || !dp.first[q]) ? 1u : 0u);
+            for (int q = 0; q < kPairs; ++q) {
+              const uint64_t da = da0 + (uint64_t)(((size_t)dp.s[q] * 128 * kKC * 2) >> 4);
+              const uint64_t db = db0 + (uint64_t)(((size_t)dp.u[q] * kNT * kKC * 2) >> 4);
+              tc::mma_bf16(dbase + (uint32_t)(dp.a[q] * kNT), da, db, idesc, (kc > k0 || !dp.first[q]) ? 1u : 0u);
+            }
+            tc::mma_commit(&sm.empty[st]);
           }
-          tc::mma_commit(&sm.empty[st]);
+          if (!ok) break;
+          tc::mma_commit(&sm.tfull[buf]);
         }
-        if (!ok) break;
-        tc::mma_commit(&sm.tfull[buf]);
       }
       // every MMA issued has completed before TMEM is released
       tc::mma_commit(sm.done);
@@ -623,23 +635,40 @@ __global__ void __launch_bounds__(tc_threads<Epi>(), 1) tc_persistent_kernel(Sch
     const int c0 = ((warp - 2) >> 2) * Epi::kCols;
     const int etid = (warp - 2) * 32 + lane;
     int i = 0;
-    for (int t = blockIdx.x; t < ntiles; t += gridDim.x, ++i) {
-      const int buf = i & 1;
-      const uint32_t ub = (uint32_t)i >> 1;
-      // lane 0 waits and the warp follows its verdict, so the warp stays
-      // converged for the .sync.aligned TMEM loads
+    bool ok = true;
+    // lane 0 waits and the warp follows its verdict, so the warp stays
+    // converged for the .sync.aligned TMEM loads
+    auto wait_full = [&](int unit) {
       int ready = 0;
-      if (lane == 0) ready = tc::mbar_wait(&sm.tfull[buf], ub & 1) ? 1 : 0;
+      if (lane == 0) ready = tc::mbar_wait(&sm.tfull[unit & 1], ((uint32_t)unit >> 1) & 1) ? 1 : 0;
       ready = __shfl_sync(0xffffffffu, ready, 0);
-      if (!ready) {
-        if (lane == 0) atomicExch(err, 2);
-        break;
-      }
-      tc::fence_after_sync();
-      ep.run(t, tmem + (uint32_t)(buf * kTmemBuf), q, q * 32 + lane, c0, etid);
+      if (!ready && lane == 0) atomicExch(err, 2);
+      return ready != 0;
+    };
+    auto release = [&](int unit) {
       tc::fence_before_sync();
       __syncwarp();
-      if (lane == 0) tc::mbar_arrive(&sm.tempty[buf]);
+      if (lane == 0) tc::mbar_arrive(&sm.tempty[unit & 1]);
+    };
+    for (int t = blockIdx.x; t < ntiles && ok; t += gridDim.x) {
+      if constexpr (Sched::kSegChunks > 0) {
+        const int nseg = (sc.tile(t).nchunks + Sched::kSegChunks - 1) / Sched::kSegChunks;
+        typename Epi::State es;
+        ep.seg_begin(es);
+        for (int sg = 0; sg < nseg; ++sg, ++i) {
+          if (!(ok = wait_full(i))) break;
+          tc::fence_after_sync();
+          ep.seg_add(es, tmem + (uint32_t)((i & 1) * kTmemBuf), q, c0);
+          release(i);
+        }
+        if (ok) ep.seg_end(t, es, q * 32 + lane, c0);
+      } else {
+        if (!(ok = wait_full(i))) break;
+        tc::fence_after_sync();
+        ep.run(t, tmem + (uint32_t)((i & 1) * kTmemBuf), q, q * 32 + lane, c0, etid);
+        release(i);
+        ++i;
+      }
     }
   }
   // reconverge each warp (lanes 1..31 of warps 0 and 1 wait here for their
@@ -654,6 +683,7 @@ __global__ void __launch_bounds__(tc_threads<Epi>(), 1) tc_persistent_kernel(Sch
 // Tiles (m, latitude tile, data tile), m-major so tiles of equal depth are
 // adjacent (largest depth first: a greedy balance of the static schedule).
 struct SynthSched {
+  static constexpr int kSegChunks = 0;  // K <= 128: one exact segment per tile
   SplitDims dm;
   const long long* kcum;
   const __nv_bfloat16* psyn;
@@ -709,6 +739,7 @@ struct SynthEpi {
 
 // --------------------------------------------------------- analysis GEMM
 struct AnalSched {
+  static constexpr int kSegChunks = 0;  // K = nlat <= 192: one exact segment per tile
   SplitDims dm;
   const __nv_bfloat16* pana;
   const __nv_bfloat16* dana;

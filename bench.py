@@ -185,6 +185,54 @@ def adjoint_measure(dev, members: int = 8, nsteps: int = 48, every: int = 8, dt:
     return out
 
 
+def geodesic_measure(dev, fields: int = 64, reps: int = 3):
+    """Config c3: level-6 icosahedral grid (40,962 points, Voronoi weights),
+    l_max 127 (16,384 real basis columns), one synthesis and one quadrature
+    analysis of `fields` seeded fields, FP64 basis GEMMs vs the bf16-digit
+    tcgen05 products; ms per (synthesis + analysis) and the split error."""
+    import torch
+    from aeolus_gb300 import _lib, workloads as W
+    from aeolus_gb300.geodesic_grid import GeodesicGridGeometry, GeodesicSphericalHarmonics
+    from aeolus_gb300.ops import Plan, analyze, synthesize
+
+    t0 = time.perf_counter()
+    sh = GeodesicSphericalHarmonics(GeodesicGridGeometry(6, 6.371e6, dev), 127, weights="voronoi")
+    p64 = sh.plan
+    psp = Plan.points(sh.latitudes.cpu().numpy(), sh.longitudes.cpu().numpy(), sh.weights.cpu().numpy(), 127,
+                      device=dev)
+    psp.set_precision(_lib.PREC_SPLIT_BF16)
+    torch.cuda.synchronize(dev)
+    build_s = time.perf_counter() - t0
+    rng = np.random.default_rng(5)
+    a = torch.as_tensor(np.stack([W.random_spectrum(rng, 127, -1.5, 1.0, zero_monopole=False)
+                                  for _ in range(fields)]), device=dev)
+    out = {"workload": "geodesic_level6_40962pts_lmax127_64fields", "points": p64.n_points,
+           "basis_columns": 128 * 128, "fields": fields, "plans_build_s": build_s}
+    res = {}
+    for name, plan in (("fp64", p64), ("split", psp)):
+        g = synthesize(plan.id, a)
+        c = analyze(plan.id, g)
+        torch.cuda.synchronize(dev)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(reps):
+            g = synthesize(plan.id, a)
+            c = analyze(plan.id, g)
+        e1.record()
+        torch.cuda.synchronize(dev)
+        ms = e0.elapsed_time(e1) / reps
+        useful = 2.0 * 2.0 * p64.n_points * 128 * 128 * fields
+        res[name] = (g, c)
+        out[name] = {"ms_synthesis_plus_analysis": ms, "useful_tflops": useful / ms / 1e9}
+    out["rel_l2_split_vs_fp64"] = {
+        "synthesis": float(torch.linalg.vector_norm(res["split"][0] - res["fp64"][0])
+                           / torch.linalg.vector_norm(res["fp64"][0])),
+        "analysis": float(torch.linalg.vector_norm(res["split"][1] - res["fp64"][1])
+                          / torch.linalg.vector_norm(res["fp64"][1]))}
+    out["split_vs_fp64_speedup"] = out["fp64"]["ms_synthesis_plus_analysis"] / out["split"]["ms_synthesis_plus_analysis"]
+    return out
+
+
 # ------------------------------------------------------------ CPU baseline
 def cpu_reference_sample(B: int, rows: int, reps: int = 1):
     """Time the reference algorithm for one RK4 step on a row sample.
@@ -537,6 +585,7 @@ def main():
     if rank == 0 and not args.no_extras:
         extras["ensemble"] = ensemble_measure(dev)
         extras["adjoint"] = adjoint_measure(dev)
+        extras["geodesic"] = geodesic_measure(dev)
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
