@@ -63,6 +63,15 @@ __host__ __device__ inline double2 ci(double2 a) { return make_double2(-a.y, a.x
 
 // --------------------------------------------------------------- layout
 // Packed m-major triangle: for order m the degrees l = m..L are contiguous.
+// F/G blocks (order spectra of the latitude rows) are [member][order m]
+// [latitude row][field], fields fastest: a tensor-core epilogue thread owns
+// one row and consecutive fields of one member (whole 32-byte sectors per
+// store), and the row stage reads / writes all fields of its row per order
+// as one contiguous run.
+__host__ __device__ inline long fg_index(long b, int m, int f, int j, int L, int nblk, int nlat) {
+  return ((b * (L + 1) + m) * (long)nlat + j) * nblk + f;
+}
+
 __host__ __device__ inline long tri_off(int m, int L) { return (long)m * (L + 1) - (long)m * (m - 1) / 2; }
 __host__ __device__ inline long n_coeff(int L) { return (long)(L + 1) * (L + 2) / 2; }
 

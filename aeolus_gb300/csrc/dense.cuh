@@ -5,12 +5,12 @@
 //   analysis   out[n][c] = sum_p B[p][c] W[n][p]      (K = points)
 //
 // with the same balanced base-256 digits as the Gauss contraction (per-row
-// basis exponents, per-column data exponents, 21 digit pairs, 7 level
-// accumulators).  K runs to 16384 (synthesis at l_max 127) or 40962
+// basis exponents, per-column data exponents, 21 digit pairs in 6 MMAs, 6
+// level accumulators).  K runs to 16384 (synthesis at l_max 127) or 40962
 // (analysis on a level-6 grid), far beyond the depth at which an f32 sum of
 // digit products stays exact, so every output tile is contracted in K
-// segments of kSegChunks * 16 <= 192: each segment's level sums are exact
-// integers below 5 * 192 * 2^14 < 2^24, drained from TMEM into two int64
+// segments of kSegChunks * 16 <= 160: each segment's level sums are exact
+// integers below 6 * 160 * 2^14 < 2^24, drained from TMEM into two int64
 // running sums per output (exact over at most kMaxPartChunks chunks), and
 // the K range of a tile is split into parts whose partial results (one
 // rounding each, to FP64) are added by a final pass.  The error is that of the dropped
@@ -22,7 +22,7 @@
 
 namespace aeolus {
 
-constexpr int kDenseSegChunks = 12;                    // 192-deep exact segments
+constexpr int kDenseSegChunks = kExactChunks;          // 160-deep exact segments
 constexpr int kMaxPartChunks = 136 * kDenseSegChunks;  // exact int64 running sums per part
 
 struct DenseDims {
@@ -70,8 +70,8 @@ __device__ inline double pow2d(int e) { return __longlong_as_double((long long)(
 
 // Running sums of one output: with a segment's level sums I_k (|I_k| < 2^24)
 // the segment value is T = (I0 2^8 + I1) 2^32 + (I2 2^24 + I3 2^16 + I4 2^8
-// + I5 + I6); both parts are summed over segments in int64 (below 2^41 and
-// 2^57 for at most 136 segments) and rounded once to FP64 at the end.
+// + I5); both parts are summed over segments in int64 (below 2^41 and 2^57
+// for at most 136 segments) and rounded once to FP64 at the end.
 __device__ inline double hr_to_double(long long H, long long R, int e) {
   if (H == 0 && R == 0) return 0.0;
   const double t = fma((double)H, 4294967296.0, (double)R);
@@ -101,10 +101,10 @@ struct DenseEpi {
 #pragma unroll
       for (int k = 0; k < kAccs; ++k) I[k] = __float2int_rn(acc[i][k]);
       st.H[i] += ((long long)I[0] << 8) + I[1];
-      st.R[i] += ((long long)I[2] << 24) + ((long long)I[3] << 16) + ((long long)I[4] << 8) + I[5] + I[6];
+      st.R[i] += ((long long)I[2] << 24) + ((long long)I[3] << 16) + ((long long)I[4] << 8) + I[5];
     }
   }
-  __device__ void seg_end(int t, const State& st, int row, int c0) const {
+  __device__ void seg_end(int t, const State& st, int row, int c0, int) const {
     const int kp = t / (d.Mt * d.Nt), r = t - kp * d.Mt * d.Nt;
     const int nt = r / d.Mt, mt = r - nt * d.Mt;
     const int m = mt * 128 + row;

@@ -153,7 +153,7 @@ struct GroupedSched {
   }
 };
 
-template <class Sched, class Epi>
+template <class Sched, class Epi, bool SEG = (Sched::kSegChunks > 0)>
 struct GroupedEpi {
   static constexpr int kWarps = Epi::kWarps, kCols = Epi::kCols;
   GroupedSched<Sched> gs;  // for the tile -> group map
@@ -161,6 +161,22 @@ struct GroupedEpi {
   __device__ void run(int t, uint32_t tbuf, int q, int row, int c0, int etid) const {
     const int k = gs.find(t);
     e[k].run(t - gs.start[k], tbuf, q, row, c0, etid);
+  }
+};
+
+// K-segmented epilogues: the per-thread running state is the group-
+// independent State of the wrapped epilogue.
+template <class Sched, class Epi>
+struct GroupedEpi<Sched, Epi, true> {
+  static constexpr int kWarps = Epi::kWarps, kCols = Epi::kCols;
+  using State = typename Epi::State;
+  GroupedSched<Sched> gs;
+  Epi e[kMaxGroups];
+  __device__ void seg_begin(State& st) const { e[0].seg_begin(st); }
+  __device__ void seg_add(State& st, uint32_t tbuf, int q, int c0) const { e[0].seg_add(st, tbuf, q, c0); }
+  __device__ void seg_end(int t, const State& st, int row, int c0, int etid) const {
+    const int k = gs.find(t);
+    e[k].seg_end(t - gs.start[k], st, row, c0, etid);
   }
 };
 
@@ -271,7 +287,7 @@ int ens_stage(const aeolus_ensemble_s* E, double2* const* y0, int stage, double 
   GroupedSched<AnalSched> tana{};
   GroupedEpi<AnalSched, AnalEpi<BveEpi>> eana{};
   size_t sm_ss = 0, sm_sa = 0;
-  int sm_count = 1, err_dev = 0;
+  int sm_count = 1;
   int* err = nullptr;
   for (int k = 0; k < ng; ++k) {
     const aeolus_plan_impl* p = E->plan[k];
@@ -295,7 +311,6 @@ int ens_stage(const aeolus_ensemble_s* E, double2* const* y0, int stage, double 
     eana.e[k] = AnalEpi<BveEpi>{r2.dm, p->split->eana, r2.ecol, B, epi[k]};
     sm_count = std::max(sm_count, p->sm_count);
     err = p->split->err;  // any group's flag: a device error marks every plan's kernels suspect
-    (void)err_dev;
   }
   tsyn.n = tana.n = ng;
   esyn.gs = tsyn;

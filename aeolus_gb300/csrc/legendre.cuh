@@ -107,8 +107,8 @@ __device__ __forceinline__ void legendre_synth_body(const LegArgs& a, const Deri
         if (c >= ncols) break;
         const int bl = c / NF, f = c - bl * NF;
         const long bb = b0 + bl;
-        a.FG[((bb * a.nlat + jn) * a.nblk + f) * ldm + m] = cadd(E[q], O[q]);
-        if (jS != jn) a.FG[((bb * a.nlat + jS) * a.nblk + f) * ldm + m] = csub(E[q], O[q]);
+        a.FG[fg_index(bb, m, f, jn, L, a.nblk, a.nlat)] = cadd(E[q], O[q]);
+        if (jS != jn) a.FG[fg_index(bb, m, f, jS, L, a.nblk, a.nlat)] = csub(E[q], O[q]);
       }
     }
   }
@@ -148,8 +148,8 @@ __device__ __forceinline__ void legendre_analysis_body(const LegArgs& a, const E
     const int m = which ? mB : mA;
     const long bb = b0 + bl;
     const int jS = a.nlat - 1 - jn;
-    const double2 gN = a.FG[((bb * a.nlat + jn) * a.nblk + f) * ldm + m];
-    const double2 gS = jS != jn ? a.FG[((bb * a.nlat + jS) * a.nblk + f) * ldm + m] : make_double2(0.0, 0.0);
+    const double2 gN = a.FG[fg_index(bb, m, f, jn, L, a.nblk, a.nlat)];
+    const double2 gS = jS != jn ? a.FG[fg_index(bb, m, f, jS, L, a.nblk, a.nlat)] : make_double2(0.0, 0.0);
     double2* dst = s_g + which * per_order + ((long)(bl * NF + f) * 2) * nh;
     dst[jn] = cadd(gN, gS);
     dst[nh + jn] = csub(gN, gS);

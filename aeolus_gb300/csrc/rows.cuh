@@ -149,8 +149,10 @@ __device__ __forceinline__ void row_body(const RowArgs& a, const Pw& pw, int bx,
   double2* buf0 = smem;
   double2* buf1 = smem + (long)NF * n;
   if (threadIdx.x == 0) s_bits = 0u;
+  // this row's order spectra: field f, order q at block[q * sq + f]
+  const long sq = (long)a.nblk * a.nlat;
   double2* block = nullptr;
-  if (IN_MODE == kInF || OUT_MODE == kOutG) block = a.FG + ((long)b * a.nlat + j) * a.nblk * ldm;
+  if (IN_MODE == kInF || OUT_MODE == kOutG) block = a.FG + fg_index(b, 0, 0, j, L, a.nblk, a.nlat);
 
   // ---- 1. grid rows of the NIN input fields (real rows, field stride 2n doubles)
   double* xin = reinterpret_cast<double*>(buf0);
@@ -160,11 +162,11 @@ __device__ __forceinline__ void row_body(const RowArgs& a, const Pw& pw, int bx,
       // H_q = F_q for 1 <= q <= L, H_0 = Re F_0, zero above L.
       for (int idx = threadIdx.x; idx < NIN * n; idx += blockDim.x) {
         const int f = idx / n, q = idx - f * n;
-        const double2* Ff = block + (long)f * ldm;
-        double2 hq = q <= L ? Ff[q] : make_double2(0.0, 0.0);
+        const double2* Ff = block + f;
+        double2 hq = q <= L ? Ff[(long)(q) * sq] : make_double2(0.0, 0.0);
         if (q == 0) hq.y = 0.0;
         const int qn = n - q;
-        double2 hn = (q > 0 && qn <= L) ? Ff[qn] : make_double2(0.0, 0.0);
+        double2 hn = (q > 0 && qn <= L) ? Ff[(long)(qn) * sq] : make_double2(0.0, 0.0);
         double2 A = cadd(hq, cconj(hn));
         double2 B = csub(hq, cconj(hn));
         double2 e = cconj(__ldg(&a.tw[q]));
@@ -177,17 +179,17 @@ __device__ __forceinline__ void row_body(const RowArgs& a, const Pw& pw, int bx,
       double* x0 = reinterpret_cast<double*>(buf0);
       for (int idx = threadIdx.x; idx < NIN * N; idx += blockDim.x) {
         const int f = idx / N, k = idx - f * N;
-        const double2* Ff = block + (long)f * ldm;
+        const double2* Ff = block + f;
         double acc = 0.0;
         int e = 0;
         for (int m = 1; m <= L; ++m) {
           e += k;
           if (e >= N) e -= N;
           double2 w = __ldg(&a.tw[e]);
-          double2 F = Ff[m];
+          double2 F = Ff[(long)(m) * sq];
           acc += F.x * w.x + F.y * w.y;
         }
-        x0[(long)f * 2 * n + k] = Ff[0].x + 2.0 * acc;
+        x0[(long)f * 2 * n + k] = Ff[(long)(0) * sq].x + 2.0 * acc;
       }
       __syncthreads();
     }
@@ -242,7 +244,7 @@ __device__ __forceinline__ void row_body(const RowArgs& a, const Pw& pw, int bx,
         double2 D = csub(zq, zn);
         double2 O = make_double2(0.5 * D.y, -0.5 * D.x);  // -(i/2) D
         double2 R = cadd(E, cmul(__ldg(&a.tw[q]), O));
-        block[(long)f * ldm + q] = cscale(wj, R);
+        block[(long)q * sq + f] = cscale(wj, R);
       }
     } else {
       for (int idx = threadIdx.x; idx < NOUT * ldm; idx += blockDim.x) {
@@ -257,7 +259,7 @@ __device__ __forceinline__ void row_body(const RowArgs& a, const Pw& pw, int bx,
           e += q;
           while (e >= N) e -= N;
         }
-        block[(long)f * ldm + q] = make_double2(wj * sr, wj * si);
+        block[(long)q * sq + f] = make_double2(wj * sr, wj * si);
       }
     }
   }

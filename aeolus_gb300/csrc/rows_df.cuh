@@ -119,8 +119,11 @@ __device__ __forceinline__ void row_df_body(const RowArgs& a, const Pw& pw, cons
   cdf* buf0 = smem_df;
   cdf* buf1 = smem_df + (long)NF * n;
   if (threadIdx.x == 0) s_bits = 0u;
+  // this row's order spectra: field f, order q at block[q * sq + f]
+  const long sq = (long)a.nblk * a.nlat;
   float4* block = nullptr;
-  if (IN_MODE == kInF || OUT_MODE == kOutG) block = reinterpret_cast<float4*>(a.FG) + ((long)b * a.nlat + j) * a.nblk * ldm;
+  if (IN_MODE == kInF || OUT_MODE == kOutG)
+    block = reinterpret_cast<float4*>(a.FG) + fg_index(b, 0, 0, j, L, a.nblk, a.nlat);
 
   // ---- 1. grid rows of the inputs (real df rows, field stride 2n)
   df* xin = reinterpret_cast<df*>(buf0);
@@ -128,11 +131,11 @@ __device__ __forceinline__ void row_df_body(const RowArgs& a, const Pw& pw, cons
     if (a.fft.use_fft) {
       for (int idx = threadIdx.x; idx < NIN * n; idx += blockDim.x) {
         const int f = idx / n, q = idx - f * n;
-        const float4* Ff = block + (long)f * ldm;
-        cdf hq = q <= L ? cdf_from_f4(Ff[q]) : cdf_zero();
+        const float4* Ff = block + f;
+        cdf hq = q <= L ? cdf_from_f4(Ff[(long)(q) * sq]) : cdf_zero();
         if (q == 0) hq.im = df{0.f, 0.f};
         const int qn = n - q;
-        const cdf hn = (q > 0 && qn <= L) ? cdf_from_f4(Ff[qn]) : cdf_zero();
+        const cdf hn = (q > 0 && qn <= L) ? cdf_from_f4(Ff[(long)(qn) * sq]) : cdf_zero();
         const cdf A = cdf_addf(hq, cdf_conj(hn));
         const cdf B = cdf_subf(hq, cdf_conj(hn));
         const cdf e = cdf_conj(cdf_from_f4(__ldg(&twdf[q])));
@@ -144,17 +147,17 @@ __device__ __forceinline__ void row_df_body(const RowArgs& a, const Pw& pw, cons
       df* x0 = reinterpret_cast<df*>(buf0);
       for (int idx = threadIdx.x; idx < NIN * N; idx += blockDim.x) {
         const int f = idx / N, k = idx - f * N;
-        const float4* Ff = block + (long)f * ldm;
+        const float4* Ff = block + f;
         df acc = df{0.f, 0.f};
         int e = 0;
         for (int m = 1; m <= L; ++m) {
           e += k;
           if (e >= N) e -= N;
           const cdf w = cdf_from_f4(__ldg(&twdf[e]));
-          const cdf F = cdf_from_f4(Ff[m]);
+          const cdf F = cdf_from_f4(Ff[(long)(m) * sq]);
           acc = df_add_fast(acc, df_add_fast(df_mul(F.re, w.re), df_mul(F.im, w.im)));
         }
-        x0[(long)f * 2 * n + k] = df_add_fast(df{Ff[0].x, Ff[0].y}, df_scale2(acc, 2.0f));
+        x0[(long)f * 2 * n + k] = df_add_fast(df{Ff[(long)(0) * sq].x, Ff[(long)(0) * sq].y}, df_scale2(acc, 2.0f));
       }
       __syncthreads();
     }
@@ -206,7 +209,7 @@ __device__ __forceinline__ void row_df_body(const RowArgs& a, const Pw& pw, cons
         const cdf D = cdf_subf(zq, zn);
         const cdf O = cdf{df_scale2(D.im, 0.5f), df_scale2(D.re, -0.5f)};  // -(i/2) D
         const cdf R = cdf_scale(wj, cdf_addf(E, cdf_mulf(cdf_from_f4(__ldg(&twdf[q])), O)));
-        block[(long)f * ldm + q] = make_float4(R.re.hi, R.re.lo, R.im.hi, R.im.lo);
+        block[(long)q * sq + f] = make_float4(R.re.hi, R.re.lo, R.im.hi, R.im.lo);
       }
     } else {
       for (int idx = threadIdx.x; idx < NOUT * ldm; idx += blockDim.x) {
@@ -222,7 +225,7 @@ __device__ __forceinline__ void row_df_body(const RowArgs& a, const Pw& pw, cons
           while (e >= N) e -= N;
         }
         const df gr = df_mul(wj, sr), gi = df_mul(wj, si);
-        block[(long)f * ldm + q] = make_float4(gr.hi, gr.lo, gi.hi, gi.lo);
+        block[(long)q * sq + f] = make_float4(gr.hi, gr.lo, gi.hi, gi.lo);
       }
     }
   }

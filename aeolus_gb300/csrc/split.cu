@@ -4,10 +4,12 @@
 // base-256 digits: with a per-row (basis) or per-column (data) exponent E,
 //   X = rint(x * 2^(48-E)) = sum_{s=1..6} d_s 256^(6-s),  |d_s| <= 128,
 // so each digit is exact in bf16.  The digit products of level k = s + t
-// (k = 2..7, 21 (s,t) pairs) are accumulated in f32 TMEM accumulators, one
-// per level except the 6-pair top level which uses two; every partial sum
-// is an integer below pairs*K*2^14 < 2^24 (K <= 128 degrees in synthesis,
-// <= 192 latitudes in analysis), so the tensor-core accumulation is exact.
+// (k = 2..7, 21 (s,t) pairs) are accumulated in one f32 TMEM accumulator
+// per level; every partial sum is an integer below pairs*K*2^14 <= 6*K*2^14
+// < 2^24 for K <= 160, so the tensor-core accumulation is exact (analysis
+// over 192 latitudes runs two K segments).  The data digit slices sit side
+// by side along the MMA's N dimension, so basis slice s meets data slices
+// 0..6-s in one MMA whose output columns are the level accumulators s..7.
 // The levels are recombined in 64-bit integers, T = sum_k I_k 256^(7-k),
 // and one conversion gives the FP64 result T * 2^(E_row + E_col - 56).
 // Dropped levels k >= 8 bound the error near 2^-48 of max|P| max|a| per
@@ -15,12 +17,12 @@
 //
 // Synthesis GEMM (per order m):   F[j, n] = sum_l P_lm(x_j) a[l, n]
 //   A = basis digits  (128 latitude rows x Kpad degrees, K-major)
-//   B = data digits   (64 data columns  x Kpad degrees, K-major)
+//   B = data digits   (32 data columns x 6 slices x Kpad degrees, K-major)
 // Analysis GEMM (per order m):    a[l, n] = sum_j P_lm(x_j) G[j, n]
 //   A = basis digits  (128 degree rows x NK latitudes)
-//   B = data digits   (64 data columns x NK latitudes)
-// Data columns are (member, field, re/im).  Basis tiles stream through the
-// TMA bulk-copy engine into a double buffer; the data tile stays resident.
+//   B = data digits   (32 data columns x 6 slices x NK latitudes)
+// Data columns are (member, field, re/im).  Operand chunks stream through a
+// 6-stage TMA bulk-copy pipeline of the persistent kernel (split.cuh).
 #include <algorithm>
 #include <vector>
 

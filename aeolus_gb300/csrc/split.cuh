@@ -14,8 +14,8 @@ namespace aeolus {
 
 constexpr int kSlices = 6;   // base-256 digits per operand (48 bits)
 constexpr int kLevels = 6;   // kept levels k = s + t = 2..7 (1-based digits)
-constexpr int kAccs = 7;     // TMEM accumulators: the 6-pair top level is split in two
-constexpr int kNT = 32;      // data columns per tensor-core tile (MMA N)
+constexpr int kAccs = 6;     // TMEM accumulators, one per kept level
+constexpr int kNT = 32;      // data columns per tensor-core tile (one digit slice of the MMA N)
 constexpr int kKC = 16;      // contraction depth per pipeline chunk (one MMA K step)
 constexpr int kShift = 8 * kSlices;  // X = rint(x 2^(kShift - E))
 constexpr int kMaxKp = 128;  // degrees per order (l_max <= 127)
@@ -212,7 +212,7 @@ __device__ inline void digits_from_fixed(long long X, float* d) {
 __device__ inline float pow2f(int p) { return __int_as_float((p + 127) << 23); }  // p in [-126, 127]
 
 __device__ inline df levels_to_df(const float* acc, int e) {
-  df s = two_sum(acc[kLevels], acc[kLevels - 1]);
+  df s = df{acc[kLevels - 1], 0.f};
 #pragma unroll
   for (int k = kLevels - 2; k >= 0; --k) s = df_add_f(s, acc[k] * pow2f(8 * (kLevels - 1 - k)));
   // s * 2^e, e = e1 + e2 with both factors normal floats
@@ -220,21 +220,18 @@ __device__ inline df levels_to_df(const float* acc, int e) {
   return df{s.hi * pow2f(e1) * pow2f(e2), s.lo * pow2f(e1) * pow2f(e2)};
 }
 
-// Level recombination: T = sum_k I_k 256^(5-k), k = 0..5 <-> s+t = 2..7,
-// the top level held in two accumulators.  |T| < 2^62.
+// Level recombination: T = sum_k I_k 256^(5-k), k = 0..5 <-> s+t = 2..7.
+// One K segment (<= 160 deep): |I_0| < 160 * 2^14, so |T| < 2^62.
 __device__ inline long long combine_levels(const float* acc) {
   long long T = 0;
 #pragma unroll
-  for (int k = 0; k < kLevels - 1; ++k) T = (T << 8) + __float2int_rn(acc[k]);
-  return (T << 8) + ((long long)__float2int_rn(acc[kLevels - 1]) + __float2int_rn(acc[kLevels]));
+  for (int k = 0; k < kLevels; ++k) T = (T << 8) + __float2int_rn(acc[k]);
+  return T;
 }
 
-// Accumulator of digit pair (s, t) (0-based): one per level, except the
-// top level whose 6 pairs are split 3 + 3 so that each f32 sum stays an
-// exact integer for K <= 192 (3 * 192 * 2^14 < 2^24).
-__host__ __device__ constexpr int acc_of(int s, int t) {
-  return (s + t < kLevels - 1) ? s + t : (s < kSlices / 2 ? kLevels - 1 : kLevels);
-}
+// Exact-accumulation depth: the deepest level (6 digit pairs) sums at most
+// 6 * K * 2^14 in an f32 accumulator, an exact integer while K <= 160.
+constexpr int kExactChunks = 10;
 
 // Result exponent offset: x y = T 2^(Ex + Ey - kOut).
 constexpr int kOut = 2 * kShift - 8 * (kSlices - 1);
@@ -352,10 +349,10 @@ __device__ __forceinline__ void split_anal_slice_body(const SplitDims& dm, int b
   const int nb = min(mb, batch - b0);
   const int nc = nb * NF * 2;
   for (int idx = threadIdx.x; idx < nb * NF * nlat; idx += blockDim.x) {
-    const int j = idx % nlat;
-    const int r = idx / nlat;
-    const int f = r % NF, bl = r / NF;
-    const float4 g = FG[(((long long)(b0 + bl) * nlat + j) * nblk + f) * ldm + m];
+    const int f = idx % NF;
+    const int r = idx / NF;
+    const int j = r % nlat, bl = r / nlat;
+    const float4 g = FG[fg_index(b0 + bl, m, f, j, L, nblk, nlat)];
     s_dval[((bl * NF + f) * 2 + 0) * nlat + j] = df{g.x, g.y};
     s_dval[((bl * NF + f) * 2 + 1) * nlat + j] = df{g.z, g.w};
   }
@@ -414,8 +411,10 @@ __global__ void __launch_bounds__(256) split_anal_slice_kernel(SplitDims dm, int
 // TMA bulk copies.
 //   warp 0 lane 0   producer: streams chunks through kStages smem stages
 //                   (across tile boundaries);
-//   warp 1 lane 0   MMA issuer: per chunk the 21 digit-pair MMAs into the
-//                   kAccs level accumulators of one of two TMEM buffers;
+//   warp 1 lane 0   MMA issuer: per chunk 6 MMAs (one per basis digit slice,
+//                   N = the data slices it pairs with) carry the 21 digit
+//                   pairs into the kAccs level accumulators of one of two
+//                   TMEM buffers;
 //   warps 2..      Epi::kWarps epilogue warps drain the other TMEM buffer
 //                   while the next tile's MMAs run; warp w reads TMEM lane
 //                   quadrant w % 4 and the Epi::kCols-column group (w - 2) / 4.
@@ -429,29 +428,6 @@ constexpr int kTmemCols = 512;      // 2 x kAccs * kNT = 448 columns used
 constexpr size_t kStageBytesA = chunk_elems(128) * 2;
 constexpr size_t kStageBytesB = chunk_elems(kNT) * 2;
 constexpr size_t kStageBytes = kStageBytesA + kStageBytesB;
-
-// The 21 digit pairs (s, u), s + u < kSlices, in issue order, with their
-// level accumulator and whether the pair is the first to write it (its MMA
-// then overwrites instead of accumulating on a tile's first chunk).
-constexpr int kPairs = kSlices * (kSlices + 1) / 2;
-struct DigitPairs {
-  int s[kPairs], u[kPairs], a[kPairs], first[kPairs];
-};
-__host__ __device__ constexpr DigitPairs digit_pairs() {
-  DigitPairs t{};
-  int p = 0;
-  unsigned seen = 0u;
-  for (int s = 0; s < kSlices; ++s)
-    for (int u = 0; s + u < kSlices; ++u) {
-      t.s[p] = s;
-      t.u[p] = u;
-      t.a[p] = acc_of(s, u);
-      t.first[p] = ((seen >> t.a[p]) & 1u) ? 0 : 1;
-      seen |= 1u << t.a[p];
-      ++p;
-    }
-  return t;
-}
 
 struct TcTile {
   const __nv_bfloat16* A;  // chunk-major basis tile
@@ -523,11 +499,14 @@ __device__ inline void tc_read(uint32_t tbuf, int q, int c0, float (*acc)[kAccs]
 template <class Epi>
 constexpr int tc_threads() { return 64 + 32 * Epi::kWarps; }
 
-// Sched: int count() const; TcTile tile(int t) const.
+// Sched: int count() const; TcTile tile(int t) const; kSegChunks (0: one
+//        K segment per tile, else K segments of that many chunks).
 // Epi:   kWarps (4, 8 or 16 epilogue warps), kCols = 4 kNT / kWarps, and
 //        void run(int t, uint32_t tbuf, int q, int row, int c0, int etid) const
 //        -- consumes columns [c0, c0 + kCols) of the accumulators of tile t
-//        for TMEM lane row = q * 32 + lane (etid = epilogue thread index).
+//        for TMEM lane row = q * 32 + lane (etid = epilogue thread index);
+//        with K segments instead State, seg_begin(State&), seg_add(State&,
+//        tbuf, q, c0) per segment and seg_end(t, State, row, c0, etid).
 template <class Sched, class Epi>
 __global__ void __launch_bounds__(tc_threads<Epi>(), 1) tc_persistent_kernel(Sched sc, Epi ep, int* err) {
   extern __shared__ char smem_raw[];
@@ -578,12 +557,14 @@ __global__ void __launch_bounds__(tc_threads<Epi>(), 1) tc_persistent_kernel(Sch
     }
   } else if (warp == 1) {
     if (lane == 0) {  // ---------------- MMA issuer
-      // Descriptors differ between stages and digit slices only in the
-      // start-address field: stage/slice byte offsets >> 4 are added to the
-      // descriptors of stage 0, slice 0 (smem addresses < 256 KB, no carry).
-      constexpr DigitPairs dp = digit_pairs();
+      // Digit slices are concatenated along N: the data tile of a stage is
+      // the kSlices slices (kNT rows each) back to back, so one MMA per basis
+      // slice s multiplies it by data slices 0..5-s (N = (6-s) kNT) and writes
+      // levels s..5 at TMEM column s * kNT onwards: 6 MMAs per chunk carry
+      // the 21 digit pairs.  Descriptors differ between stages and slices
+      // only in the start-address field (stage/slice byte offsets >> 4 added
+      // to the descriptors of stage 0, slice 0; smem addresses < 256 KB).
       bool ok = true;
-      const uint32_t idesc = tc::idesc_bf16_f32(128, kNT);
       const uint64_t dA0 = tc::smem_desc(sm.A(0), 128, kKC * 16);
       const uint64_t dB0 = tc::smem_desc(sm.B(0), 128, kKC * 16);
       uint32_t g = 0;
@@ -612,12 +593,12 @@ __global__ void __launch_bounds__(tc_threads<Epi>(), 1) tc_persistent_kernel(Sch
             }
             tc::fence_after_sync();
             const uint64_t off = (uint64_t)(((size_t)st * kStageBytes) >> 4);
-            const uint64_t da0 = dA0 + off, db0 = dB0 + off;
+            const uint64_t da0 = dA0 + off, db = dB0 + off;
 #pragma unroll
-            for (int q = 0; q < kPairs; ++q) {
-              const uint64_t da = da0 + (uint64_t)(((size_t)dp.s[q] * 128 * kKC * 2) >> 4);
-              const uint64_t db = db0 + (uint64_t)(((size_t)dp.u[q] * kNT * kKC * 2) >> 4);
-              tc::mma_bf16(dbase + (uint32_t)(dp.a[q] * kNT), da, db, idesc, (kc > k0 || !dp.first[q]) ? 1u : 0u);
+            for (int sl = 0; sl < kSlices; ++sl) {
+              const uint64_t da = da0 + (uint64_t)(((size_t)sl * 128 * kKC * 2) >> 4);
+              tc::mma_bf16(dbase + (uint32_t)(sl * kNT), da, db, tc::idesc_bf16_f32(128, (kSlices - sl) * kNT),
+                           (kc > k0 || sl > 0) ? 1u : 0u);
             }
             tc::mma_commit(&sm.empty[st]);
           }
@@ -661,7 +642,7 @@ __global__ void __launch_bounds__(tc_threads<Epi>(), 1) tc_persistent_kernel(Sch
           ep.seg_add(es, tmem + (uint32_t)((i & 1) * kTmemBuf), q, c0);
           release(i);
         }
-        if (ok) ep.seg_end(t, es, q * 32 + lane, c0);
+        if (ok) ep.seg_end(t, es, q * 32 + lane, c0, etid);
       } else {
         if (!(ok = wait_full(i))) break;
         tc::fence_after_sync();
@@ -730,7 +711,7 @@ struct SynthEpi {
           const df im = levels_to_df(acc[i + 1], e[i + 1]);
           const int bf = n >> 1;
           const int b = bf / NF, f = bf - b * NF;
-          F[(((long long)b * dm.nlat + j) * nblk + f) * (L + 1) + m] = make_float4(re.hi, re.lo, im.hi, im.lo);
+          F[fg_index(b, m, f, j, L, nblk, dm.nlat)] = make_float4(re.hi, re.lo, im.hi, im.lo);
         }
       }
     }
@@ -739,7 +720,7 @@ struct SynthEpi {
 
 // --------------------------------------------------------- analysis GEMM
 struct AnalSched {
-  static constexpr int kSegChunks = 0;  // K = nlat <= 192: one exact segment per tile
+  static constexpr int kSegChunks = kExactChunks;  // K = nlat <= 192: one or two exact segments
   SplitDims dm;
   const __nv_bfloat16* pana;
   const __nv_bfloat16* dana;
@@ -751,54 +732,64 @@ struct AnalSched {
   }
 };
 
-// Row = degree offset l - m.  Exact 64-bit level recombination, FP64
-// epilogue functor (whole members: Epi::finish; else Epi::finish_field).
+// Row = degree offset l - m.  Exact 64-bit level recombination summed over
+// the (at most two) K segments, FP64 epilogue functor (whole members:
+// Epi::finish; else Epi::finish_field).
 template <class Epi>
 struct AnalEpi {
   static constexpr int kWarps = 8, kCols = 4 * kNT / kWarps;  // FP64 epilogue: 16 columns per warp
+  struct State {
+    long long T[kCols];
+  };
   SplitDims dm;
   const int* eana;
   const int* ecol;
   int batch;
   Epi epi;
-  __device__ void run(int tt, uint32_t tbuf, int q, int row, int c0, int etid) const {
+  __device__ void seg_begin(State& st) const {
+#pragma unroll
+    for (int i = 0; i < kCols; ++i) st.T[i] = 0;
+  }
+  __device__ void seg_add(State& st, uint32_t tbuf, int q, int c0) const {
+    float acc[kCols][kAccs];
+    tc_read<kCols>(tbuf, q, c0, acc);
+#pragma unroll
+    for (int i = 0; i < kCols; ++i) st.T[i] += combine_levels(acc[i]);
+  }
+  __device__ void seg_end(int tt, const State& st, int row, int c0, int etid) const {
     constexpr int NF = Epi::NF;
-    constexpr bool kWhole = 16 % (2 * NF) == 0;
+    constexpr bool kWhole = kCols % (2 * NF) == 0;
     const int m = tt / dm.ntiles, tile = tt - m * dm.ntiles;
     const int K = dm.L + 1 - m;
     const int t = row;
     const int Et = eana[m * 128 + t];
     const int* ec = ecol + (long long)m * dm.ntiles * kNT + tile * kNT;
-    {
-      float acc[kCols][kAccs];
-      tc_read<kCols>(tbuf, q, c0, acc);
-      if (t < K) {
-        if constexpr (kWhole) {
+    if (t < K) {
+      if constexpr (kWhole) {
 #pragma unroll
-          for (int i = 0; i < 16; i += 2 * NF) {
-            const int n = tile * kNT + c0 + i;
-            const int b = n / (2 * NF);
-            if (b >= batch) break;
-            double2 a[NF];
+        for (int i = 0; i < kCols; i += 2 * NF) {
+          const int n = tile * kNT + c0 + i;
+          const int b = n / (2 * NF);
+          if (b >= batch) break;
+          double2 a[NF];
 #pragma unroll
-            for (int f = 0; f < NF; ++f) {
-              a[f].x = scaled_to_double(combine_levels(acc[i + 2 * f]), Et + ec[c0 + i + 2 * f] - kOut);
-              a[f].y = scaled_to_double(combine_levels(acc[i + 2 * f + 1]), Et + ec[c0 + i + 2 * f + 1] - kOut);
-            }
-            epi.finish(b, m + t, m, a);
+          for (int f = 0; f < NF; ++f) {
+            a[f].x = scaled_to_double(st.T[i + 2 * f], Et + ec[c0 + i + 2 * f] - kOut);
+            a[f].y = scaled_to_double(st.T[i + 2 * f + 1], Et + ec[c0 + i + 2 * f + 1] - kOut);
           }
-        } else {
+          epi.finish(b, m + t, m, a);
+        }
+      } else {
 #pragma unroll
-          for (int i = 0; i < 16; i += 2) {
-            const int n = tile * kNT + c0 + i;
-            const int bf = n >> 1;
-            const int b = bf / NF, f = bf - b * NF;
-            if (b >= batch) break;
-            double2 a;
-            a.x = scaled_to_double(combine_levels(acc[i]), Et + ec[c0 + i] - kOut);
-            a.y = scaled_to_double(combine_levels(acc[i + 1]), Et + ec[c0 + i + 1] - kOut);
-            epi.finish_field(b, f, m + t, m, a);
-          }
+        for (int i = 0; i < kCols; i += 2) {
+          const int n = tile * kNT + c0 + i;
+          const int bf = n >> 1;
+          const int b = bf / NF, f = bf - b * NF;
+          if (b >= batch) break;
+          double2 a;
+          a.x = scaled_to_double(st.T[i], Et + ec[c0 + i] - kOut);
+          a.y = scaled_to_double(st.T[i + 1], Et + ec[c0 + i + 1] - kOut);
+          epi.finish_field(b, f, m + t, m, a);
         }
       }
     }
