@@ -86,14 +86,14 @@ __device__ __forceinline__ void butterfly(double2* v) {
 // transform length Ls before the stage).
 template <bool INV, int R>
 __device__ __forceinline__ void fft_stage(const double2* __restrict__ src, double2* __restrict__ dst, int nf, int n,
-                                          int Ls, unsigned nb_rcp, unsigned ls_rcp,
+                                          int fs, int Ls, unsigned nb_rcp, unsigned ls_rcp,
                                           const double2* __restrict__ tw) {
   const int nb = n / R, Ns = Ls * R, stride = n / Ns;
   for (int idx = threadIdx.x; idx < nf * nb; idx += blockDim.x) {
     const int f = div_rcp(idx, nb, nb_rcp), jj = idx - f * nb;
     const int q = div_rcp(jj, Ls, ls_rcp), k = jj - q * Ls;
-    const double2* x = src + (long)f * n;
-    double2* y = dst + (long)f * n;
+    const double2* x = src + (long)f * fs;
+    double2* y = dst + (long)f * fs;
     double2 v[R];
 #pragma unroll
     for (int t = 0; t < R; ++t) v[t] = x[jj + t * nb];
@@ -112,21 +112,21 @@ __device__ __forceinline__ void fft_stage(const double2* __restrict__ src, doubl
   }
 }
 
-// nf independent length-n complex FFTs (field stride n) in shared memory,
+// nf independent length-n complex FFTs (field stride fs) in shared memory,
 // Stockham autosort, ping-pong between src and dst; returns the buffer that
 // holds the result.  Ends with __syncthreads().
 template <bool INV>
-__device__ double2* fft_run(double2* src, double2* dst, int nf, const FftInfo& fi,
+__device__ double2* fft_run(double2* src, double2* dst, int nf, int fs, const FftInfo& fi,
                             const double2* __restrict__ tw) {
   const int n = fi.n;
   int Ls = 1;
   for (int s = 0; s < fi.nfac; ++s) {
     const int r = fi.fac[s];
     switch (r) {
-      case 4: fft_stage<INV, 4>(src, dst, nf, n, Ls, fi.nbm[s], fi.lsm[s], tw); break;
-      case 2: fft_stage<INV, 2>(src, dst, nf, n, Ls, fi.nbm[s], fi.lsm[s], tw); break;
-      case 3: fft_stage<INV, 3>(src, dst, nf, n, Ls, fi.nbm[s], fi.lsm[s], tw); break;
-      default: fft_stage<INV, 5>(src, dst, nf, n, Ls, fi.nbm[s], fi.lsm[s], tw); break;
+      case 4: fft_stage<INV, 4>(src, dst, nf, n, fs, Ls, fi.nbm[s], fi.lsm[s], tw); break;
+      case 2: fft_stage<INV, 2>(src, dst, nf, n, fs, Ls, fi.nbm[s], fi.lsm[s], tw); break;
+      case 3: fft_stage<INV, 3>(src, dst, nf, n, fs, Ls, fi.nbm[s], fi.lsm[s], tw); break;
+      default: fft_stage<INV, 5>(src, dst, nf, n, fs, Ls, fi.nbm[s], fi.lsm[s], tw); break;
     }
     __syncthreads();
     double2* tmp = src;
@@ -146,8 +146,11 @@ __device__ __forceinline__ void row_body(const RowArgs& a, const Pw& pw, int bx,
   const int j = bx, b = by;
   const int N = a.fft.N, n = a.fft.n, L = a.L;
   const int ldm = L + 1;
+  // smem rows: field stride ns = n + 1 complex values, so accesses that
+  // interleave the fields (field-fastest global order) are bank-conflict free
+  const int ns = n + 1;
   double2* buf0 = smem;
-  double2* buf1 = smem + (long)NF * n;
+  double2* buf1 = smem + (long)NF * ns;
   if (threadIdx.x == 0) s_bits = 0u;
   // this row's order spectra: field f, order q at block[q * sq + f]
   const long sq = (long)a.nblk * a.nlat;
@@ -161,7 +164,7 @@ __device__ __forceinline__ void row_body(const RowArgs& a, const Pw& pw, int bx,
       // Z_q = (H_q + conj H_{n-q}) + i e^{+2 pi i q/N} (H_q - conj H_{n-q}),
       // H_q = F_q for 1 <= q <= L, H_0 = Re F_0, zero above L.
       for (int idx = threadIdx.x; idx < NIN * n; idx += blockDim.x) {
-        const int f = idx / n, q = idx - f * n;
+        const int q = idx / NIN, f = idx - q * NIN;  // fields fastest: contiguous global reads
         const double2* Ff = block + f;
         double2 hq = q <= L ? Ff[(long)(q) * sq] : make_double2(0.0, 0.0);
         if (q == 0) hq.y = 0.0;
@@ -170,10 +173,10 @@ __device__ __forceinline__ void row_body(const RowArgs& a, const Pw& pw, int bx,
         double2 A = cadd(hq, cconj(hn));
         double2 B = csub(hq, cconj(hn));
         double2 e = cconj(__ldg(&a.tw[q]));
-        buf0[idx] = cadd(A, ci(cmul(e, B)));
+        buf0[(long)f * ns + q] = cadd(A, ci(cmul(e, B)));
       }
       __syncthreads();
-      xin = reinterpret_cast<double*>(fft_run<true>(buf0, buf1, NIN, a.fft, a.tw));
+      xin = reinterpret_cast<double*>(fft_run<true>(buf0, buf1, NIN, ns, a.fft, a.tw));
     } else {
       // x_k = Re F_0 + 2 sum_{m=1..L} Re(F_m e^{+2 pi i m k/N})
       double* x0 = reinterpret_cast<double*>(buf0);
@@ -189,7 +192,7 @@ __device__ __forceinline__ void row_body(const RowArgs& a, const Pw& pw, int bx,
           double2 F = Ff[(long)(m) * sq];
           acc += F.x * w.x + F.y * w.y;
         }
-        x0[(long)f * 2 * n + k] = Ff[(long)(0) * sq].x + 2.0 * acc;
+        x0[(long)f * 2 * ns + k] = Ff[(long)(0) * sq].x + 2.0 * acc;
       }
       __syncthreads();
     }
@@ -197,7 +200,7 @@ __device__ __forceinline__ void row_body(const RowArgs& a, const Pw& pw, int bx,
     double* x0 = reinterpret_cast<double*>(buf0);
     for (int idx = threadIdx.x; idx < NIN * N; idx += blockDim.x) {
       const int f = idx / N, k = idx - f * N;
-      x0[(long)f * 2 * n + k] = a.gin[(long)b * a.gin_b + (long)f * a.gin_f + (long)j * N + k];
+      x0[(long)f * 2 * ns + k] = a.gin[(long)b * a.gin_b + (long)f * a.gin_f + (long)j * N + k];
     }
     __syncthreads();
   }
@@ -212,10 +215,10 @@ __device__ __forceinline__ void row_body(const RowArgs& a, const Pw& pw, int bx,
     for (int k = threadIdx.x; k < N; k += blockDim.x) {
       double in[NIN], out[NOUT];
 #pragma unroll
-      for (int f = 0; f < NIN; ++f) in[f] = xin[(long)f * 2 * n + k];
+      for (int f = 0; f < NIN; ++f) in[f] = xin[(long)f * 2 * ns + k];
       bits |= pw(c, fg, in, out);
 #pragma unroll
-      for (int f = 0; f < NOUT; ++f) xout[(long)f * 2 * n + k] = out[f];
+      for (int f = 0; f < NOUT; ++f) xout[(long)f * 2 * ns + k] = out[f];
     }
     if (a.status && bits) atomicOr(&s_bits, bits);
   }
@@ -226,18 +229,18 @@ __device__ __forceinline__ void row_body(const RowArgs& a, const Pw& pw, int bx,
   if (OUT_MODE == kOutGrid) {
     for (int idx = threadIdx.x; idx < NOUT * N; idx += blockDim.x) {
       const int f = idx / N, k = idx - f * N;
-      a.gout[(long)b * a.gout_b + (long)f * a.gout_f + (long)j * N + k] = xout[(long)f * 2 * n + k];
+      a.gout[(long)b * a.gout_b + (long)f * a.gout_f + (long)j * N + k] = xout[(long)f * 2 * ns + k];
     }
   } else {
     const double wj = a.wq ? a.wq[j] : 1.0;
     if (a.fft.use_fft) {
       double2* zin = reinterpret_cast<double2*>(xout);
       double2* zother = (zin == buf0) ? buf1 : buf0;
-      double2* Z = fft_run<false>(zin, zother, NOUT, a.fft, a.tw);
+      double2* Z = fft_run<false>(zin, zother, NOUT, ns, a.fft, a.tw);
       // R_q = (Z_q + conj Z_{n-q})/2 - (i/2) e^{-2 pi i q/N} (Z_q - conj Z_{n-q})
       for (int idx = threadIdx.x; idx < NOUT * ldm; idx += blockDim.x) {
-        const int f = idx / ldm, q = idx - f * ldm;
-        const double2* Zf = Z + (long)f * n;
+        const int q = idx / NOUT, f = idx - q * NOUT;  // fields fastest: contiguous global writes
+        const double2* Zf = Z + (long)f * ns;
         double2 zq = Zf[q];
         double2 zn = cconj(Zf[q == 0 ? 0 : n - q]);
         double2 E = cscale(0.5, cadd(zq, zn));
@@ -248,8 +251,8 @@ __device__ __forceinline__ void row_body(const RowArgs& a, const Pw& pw, int bx,
       }
     } else {
       for (int idx = threadIdx.x; idx < NOUT * ldm; idx += blockDim.x) {
-        const int f = idx / ldm, q = idx - f * ldm;
-        const double* x = xout + (long)f * 2 * n;
+        const int q = idx / NOUT, f = idx - q * NOUT;
+        const double* x = xout + (long)f * 2 * ns;
         double sr = 0.0, si = 0.0;
         int e = 0;
         for (int k = 0; k < N; ++k) {
@@ -273,7 +276,7 @@ __global__ void __launch_bounds__(256) row_kernel(RowArgs a, Pw pw) {
 template <class Pw>
 inline size_t row_smem_bytes(const FftInfo& f) {
   constexpr int NF = Pw::NIN > Pw::NOUT ? Pw::NIN : Pw::NOUT;
-  return (size_t)2 * NF * f.n * sizeof(double2);
+  return (size_t)2 * NF * (f.n + 1) * sizeof(double2);
 }
 
 // Identity pointwise op for plain synthesis / analysis.

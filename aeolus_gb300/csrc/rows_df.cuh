@@ -57,15 +57,15 @@ __device__ __forceinline__ void butterfly_df(cdf* v, const DfConst& k) {
 }
 
 template <bool INV, int R>
-__device__ __forceinline__ void fft_stage_df(const cdf* __restrict__ src, cdf* __restrict__ dst, int nf, int n, int Ls,
-                                             unsigned nb_rcp, unsigned ls_rcp, const float4* __restrict__ tw,
+__device__ __forceinline__ void fft_stage_df(const cdf* __restrict__ src, cdf* __restrict__ dst, int nf, int n, int fs,
+                                             int Ls, unsigned nb_rcp, unsigned ls_rcp, const float4* __restrict__ tw,
                                              const DfConst& kc) {
   const int nb = n / R, Ns = Ls * R, stride = n / Ns;
   for (int idx = threadIdx.x; idx < nf * nb; idx += blockDim.x) {
     const int f = div_rcp(idx, nb, nb_rcp), jj = idx - f * nb;
     const int q = div_rcp(jj, Ls, ls_rcp), k = jj - q * Ls;
-    const cdf* x = src + (long)f * n;
-    cdf* y = dst + (long)f * n;
+    const cdf* x = src + (long)f * fs;
+    cdf* y = dst + (long)f * fs;
     cdf v[R];
 #pragma unroll
     for (int t = 0; t < R; ++t) v[t] = x[jj + t * nb];
@@ -85,17 +85,17 @@ __device__ __forceinline__ void fft_stage_df(const cdf* __restrict__ src, cdf* _
 }
 
 template <bool INV>
-__device__ cdf* fft_run_df(cdf* src, cdf* dst, int nf, const FftInfo& fi, const float4* __restrict__ tw,
+__device__ cdf* fft_run_df(cdf* src, cdf* dst, int nf, int fs, const FftInfo& fi, const float4* __restrict__ tw,
                            const DfConst& kc) {
   const int n = fi.n;
   int Ls = 1;
   for (int s = 0; s < fi.nfac; ++s) {
     const int r = fi.fac[s];
     switch (r) {
-      case 4: fft_stage_df<INV, 4>(src, dst, nf, n, Ls, fi.nbm[s], fi.lsm[s], tw, kc); break;
-      case 2: fft_stage_df<INV, 2>(src, dst, nf, n, Ls, fi.nbm[s], fi.lsm[s], tw, kc); break;
-      case 3: fft_stage_df<INV, 3>(src, dst, nf, n, Ls, fi.nbm[s], fi.lsm[s], tw, kc); break;
-      default: fft_stage_df<INV, 5>(src, dst, nf, n, Ls, fi.nbm[s], fi.lsm[s], tw, kc); break;
+      case 4: fft_stage_df<INV, 4>(src, dst, nf, n, fs, Ls, fi.nbm[s], fi.lsm[s], tw, kc); break;
+      case 2: fft_stage_df<INV, 2>(src, dst, nf, n, fs, Ls, fi.nbm[s], fi.lsm[s], tw, kc); break;
+      case 3: fft_stage_df<INV, 3>(src, dst, nf, n, fs, Ls, fi.nbm[s], fi.lsm[s], tw, kc); break;
+      default: fft_stage_df<INV, 5>(src, dst, nf, n, fs, Ls, fi.nbm[s], fi.lsm[s], tw, kc); break;
     }
     __syncthreads();
     cdf* tmp = src;
@@ -116,8 +116,9 @@ __device__ __forceinline__ void row_df_body(const RowArgs& a, const Pw& pw, cons
   const int j = bx, b = by;
   const int N = a.fft.N, n = a.fft.n, L = a.L;
   const int ldm = L + 1;
+  const int ns = n + 1;  // padded field stride of the smem rows (see row_body)
   cdf* buf0 = smem_df;
-  cdf* buf1 = smem_df + (long)NF * n;
+  cdf* buf1 = smem_df + (long)NF * ns;
   if (threadIdx.x == 0) s_bits = 0u;
   // this row's order spectra: field f, order q at block[q * sq + f]
   const long sq = (long)a.nblk * a.nlat;
@@ -130,7 +131,7 @@ __device__ __forceinline__ void row_df_body(const RowArgs& a, const Pw& pw, cons
   if (IN_MODE == kInF) {
     if (a.fft.use_fft) {
       for (int idx = threadIdx.x; idx < NIN * n; idx += blockDim.x) {
-        const int f = idx / n, q = idx - f * n;
+        const int q = idx / NIN, f = idx - q * NIN;  // fields fastest: contiguous global reads
         const float4* Ff = block + f;
         cdf hq = q <= L ? cdf_from_f4(Ff[(long)(q) * sq]) : cdf_zero();
         if (q == 0) hq.im = df{0.f, 0.f};
@@ -139,10 +140,10 @@ __device__ __forceinline__ void row_df_body(const RowArgs& a, const Pw& pw, cons
         const cdf A = cdf_addf(hq, cdf_conj(hn));
         const cdf B = cdf_subf(hq, cdf_conj(hn));
         const cdf e = cdf_conj(cdf_from_f4(__ldg(&twdf[q])));
-        buf0[idx] = cdf_addf(A, cdf_i(cdf_mulf(e, B)));
+        buf0[(long)f * ns + q] = cdf_addf(A, cdf_i(cdf_mulf(e, B)));
       }
       __syncthreads();
-      xin = reinterpret_cast<df*>(fft_run_df<true>(buf0, buf1, NIN, a.fft, twdf, kc));
+      xin = reinterpret_cast<df*>(fft_run_df<true>(buf0, buf1, NIN, ns, a.fft, twdf, kc));
     } else {
       df* x0 = reinterpret_cast<df*>(buf0);
       for (int idx = threadIdx.x; idx < NIN * N; idx += blockDim.x) {
@@ -157,7 +158,7 @@ __device__ __forceinline__ void row_df_body(const RowArgs& a, const Pw& pw, cons
           const cdf F = cdf_from_f4(Ff[(long)(m) * sq]);
           acc = df_add_fast(acc, df_add_fast(df_mul(F.re, w.re), df_mul(F.im, w.im)));
         }
-        x0[(long)f * 2 * n + k] = df_add_fast(df{Ff[(long)(0) * sq].x, Ff[(long)(0) * sq].y}, df_scale2(acc, 2.0f));
+        x0[(long)f * 2 * ns + k] = df_add_fast(df{Ff[(long)(0) * sq].x, Ff[(long)(0) * sq].y}, df_scale2(acc, 2.0f));
       }
       __syncthreads();
     }
@@ -165,7 +166,7 @@ __device__ __forceinline__ void row_df_body(const RowArgs& a, const Pw& pw, cons
     df* x0 = reinterpret_cast<df*>(buf0);
     for (int idx = threadIdx.x; idx < NIN * N; idx += blockDim.x) {
       const int f = idx / N, k = idx - f * N;
-      x0[(long)f * 2 * n + k] = df_from_double(a.gin[(long)b * a.gin_b + (long)f * a.gin_f + (long)j * N + k]);
+      x0[(long)f * 2 * ns + k] = df_from_double(a.gin[(long)b * a.gin_b + (long)f * a.gin_f + (long)j * N + k]);
     }
     __syncthreads();
   }
@@ -178,10 +179,10 @@ __device__ __forceinline__ void row_df_body(const RowArgs& a, const Pw& pw, cons
     for (int k = threadIdx.x; k < N; k += blockDim.x) {
       df in[NIN], out[NOUT];
 #pragma unroll
-      for (int f = 0; f < NIN; ++f) in[f] = xin[(long)f * 2 * n + k];
+      for (int f = 0; f < NIN; ++f) in[f] = xin[(long)f * 2 * ns + k];
       bits |= pw.df_op(rc, in, out);
 #pragma unroll
-      for (int f = 0; f < NOUT; ++f) xout[(long)f * 2 * n + k] = out[f];
+      for (int f = 0; f < NOUT; ++f) xout[(long)f * 2 * ns + k] = out[f];
     }
     if (a.status && bits) atomicOr(&s_bits, bits);
   }
@@ -192,17 +193,17 @@ __device__ __forceinline__ void row_df_body(const RowArgs& a, const Pw& pw, cons
   if (OUT_MODE == kOutGrid) {
     for (int idx = threadIdx.x; idx < NOUT * N; idx += blockDim.x) {
       const int f = idx / N, k = idx - f * N;
-      a.gout[(long)b * a.gout_b + (long)f * a.gout_f + (long)j * N + k] = df_to_double(xout[(long)f * 2 * n + k]);
+      a.gout[(long)b * a.gout_b + (long)f * a.gout_f + (long)j * N + k] = df_to_double(xout[(long)f * 2 * ns + k]);
     }
   } else {
     const df wj = a.wq ? df_from_double(a.wq[j]) : df{1.f, 0.f};
     if (a.fft.use_fft) {
       cdf* zin = reinterpret_cast<cdf*>(xout);
       cdf* zother = (zin == buf0) ? buf1 : buf0;
-      cdf* Z = fft_run_df<false>(zin, zother, NOUT, a.fft, twdf, kc);
+      cdf* Z = fft_run_df<false>(zin, zother, NOUT, ns, a.fft, twdf, kc);
       for (int idx = threadIdx.x; idx < NOUT * ldm; idx += blockDim.x) {
-        const int f = idx / ldm, q = idx - f * ldm;
-        const cdf* Zf = Z + (long)f * n;
+        const int q = idx / NOUT, f = idx - q * NOUT;  // fields fastest: contiguous global writes
+        const cdf* Zf = Z + (long)f * ns;
         const cdf zq = Zf[q];
         const cdf zn = cdf_conj(Zf[q == 0 ? 0 : n - q]);
         const cdf E = cdf_scale2(0.5f, cdf_addf(zq, zn));
@@ -213,8 +214,8 @@ __device__ __forceinline__ void row_df_body(const RowArgs& a, const Pw& pw, cons
       }
     } else {
       for (int idx = threadIdx.x; idx < NOUT * ldm; idx += blockDim.x) {
-        const int f = idx / ldm, q = idx - f * ldm;
-        const df* x = xout + (long)f * 2 * n;
+        const int q = idx / NOUT, f = idx - q * NOUT;
+        const df* x = xout + (long)f * 2 * ns;
         df sr = df{0.f, 0.f}, si = df{0.f, 0.f};
         int e = 0;
         for (int k = 0; k < N; ++k) {
