@@ -122,6 +122,7 @@ struct aeolus_plan_impl {
   double* invlap = nullptr;  // [L+1] 1 / (-l(l+1)/R^2), 0 at l = 0 (radius of the plan)
   double* xa = nullptr;      // [(L+1)^2] x Y_lm = xa_lm Y_{l+1,m} + xb_lm Y_{l-1,m}
   double* xb = nullptr;      // [(L+1)^2]
+  double* dcoef = nullptr;   // [(L+1)^2][8] SWE derive coefficients at the plan radius (see SweDerive)
   // device tables (points)
   double* basis = nullptr;   // [npoints][ncol] real basis (cos / sin columns)
   double* wpts = nullptr;    // [npoints] quadrature weights

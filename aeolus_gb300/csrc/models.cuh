@@ -26,6 +26,7 @@ struct Spec {  // shared spectral context
   const double* invlap;  // [L+1] 1 / lap(l), 0 at l = 0
   const double* xa;      // [(L+1)^2] x-multiplication coefficients (see xmul)
   const double* xb;
+  const double* dcoef;   // [(L+1)^2][8] combined SWE derive coefficients (plan radius only)
   __device__ double lap(int l) const { return -(double)l * (l + 1.0) * ir2; }
   __device__ double2 at(const double2* a, int l, int m) const { return a[(long)l * (L + 1) + m]; }
   // Helmholtz inverse with l = 0 -> 0 (physics/barotropic.py:91); a
@@ -178,6 +179,10 @@ struct SweDerive {
   const double2* state;  // [b][3][L+1][L+1]
   double f10;            // 0 when the Coriolis terms are taken spectrally (SweEpi::coriolis)
   __device__ void column(int b, int l, int m, double2* v) const {
+    if (s.dcoef) {
+      column_tab(b, l, m, v);
+      return;
+    }
     const int L = s.L;
     const long n2 = (long)(L + 1) * (L + 1);
     const double2* z = state + (long)b * 3 * n2;
@@ -220,6 +225,53 @@ struct SweDerive {
   }
   double2* cor = nullptr;   // optional [b][2][L+1][L+1] Coriolis spectra (split path, f10 = 0)
   double two_omega = 0.0;
+
+  // The same fields with the per-(l, m) coefficient products tabulated at the
+  // plan radius (Spec::dcoef): U = A1 zeta_{l-1} + A2 zeta_{l+1} + i A3 delta_l,
+  // V = i A3 zeta_l - A1 delta_{l-1} - A2 delta_{l+1}, ... -- about half the
+  // FP64 operations of the operator-by-operator form (the FP64 pipe is the
+  // slow one on GB300).  Neighbour slots outside m..L are not read.
+  __device__ void column_tab(int b, int l, int m, double2* v) const {
+    const int L = s.L;
+    const long n2 = (long)(L + 1) * (L + 1);
+    const long r = (long)l * (L + 1) + m;
+    const double2* z = state + (long)b * 3 * n2;
+    const double2* d = z + n2;
+    const double2* ph = d + n2;
+    const double* c = s.dcoef + r * 8;
+    const double A1 = c[0], A2 = c[1], A3 = c[2], B1 = c[3], B2 = c[4], B3 = c[5];
+    const bool lo = l >= 1 && l - 1 >= m, hi = l + 1 <= L;
+    const double2 zero = make_double2(0.0, 0.0);
+    const double2 zl = z[r], dl = d[r], pl = ph[r];
+    double2 z_lo = lo ? z[r - (L + 1)] : zero, z_hi = hi ? z[r + (L + 1)] : zero;
+    const double2 d_lo = lo ? d[r - (L + 1)] : zero, d_hi = hi ? d[r + (L + 1)] : zero;
+    const double2 p_lo = lo ? ph[r - (L + 1)] : zero, p_hi = hi ? ph[r + (L + 1)] : zero;
+    // U, V from psi = zeta / lap, chi = delta / lap (the 1/lap folded into A1..A3)
+    const double2 U = make_double2(fma(A1, z_lo.x, fma(A2, z_hi.x, -A3 * dl.y)), fma(A1, z_lo.y, fma(A2, z_hi.y, A3 * dl.x)));
+    const double2 V = make_double2(-fma(A1, d_lo.x, fma(A2, d_hi.x, A3 * zl.y)), fma(A3, zl.x, -fma(A1, d_lo.y, A2 * d_hi.y)));
+    if (m == 0) {  // planetary vorticity of the (1, 0) mode in eta
+      if (l - 1 == 1) z_lo.x += f10;
+      if (l + 1 == 1) z_hi.x += f10;
+    }
+    v[0] = U;
+    v[1] = V;
+    v[2] = make_double2(-B3 * zl.y, B3 * zl.x);
+    v[3] = make_double2(fma(B1, z_lo.x, B2 * z_hi.x), fma(B1, z_lo.y, B2 * z_hi.y));
+    v[4] = make_double2(-B3 * pl.y, B3 * pl.x);
+    v[5] = make_double2(fma(B1, p_lo.x, B2 * p_hi.x), fma(B1, p_lo.y, B2 * p_hi.y));
+    v[6] = zl;
+    v[7] = dl;
+    v[8] = pl;
+    if (cor) {
+      const double X1 = c[6], X2 = c[7];
+      const double wr = two_omega * s.ir;
+      const double2 xz = make_double2(fma(X1, z_lo.x, X2 * z_hi.x), fma(X1, z_lo.y, X2 * z_hi.y));
+      const double2 xd = make_double2(fma(X1, d_lo.x, X2 * d_hi.x), fma(X1, d_lo.y, X2 * d_hi.y));
+      double2* co = cor + (long)b * 2 * n2 + r;
+      co[0] = make_double2(-fma(wr, V.x, two_omega * xd.x), -fma(wr, V.y, two_omega * xd.y));
+      co[n2] = make_double2(fma(two_omega, xz.x, -wr * U.x), fma(two_omega, xz.y, -wr * U.y));
+    }
+  }
 };
 
 // Products of physics/shallow_water.py:375-386 (module docstring identities).
@@ -341,7 +393,7 @@ struct SweEpi {
 // different radius must not use it.
 Spec make_spec(const aeolus_plan_impl* p, double R) {
   return Spec{p->lmax, R, 1.0 / R, 1.0 / (R * R), p->cplus, p->cminus, R == p->radius ? p->invlap : nullptr,
-              p->xa, p->xb};
+              p->xa, p->xb, R == p->radius ? p->dcoef : nullptr};
 }
 
 // ---------------------------------------------------------- helpers

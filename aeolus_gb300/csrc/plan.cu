@@ -293,12 +293,34 @@ int common_tables(aeolus_plan_impl* p) {
     }
   if ((s = upload(&p->xa, xa))) return s;
   if ((s = upload(&p->xb, xb))) return s;
+  // Combined coefficients of the SWE derive stage at the plan radius, per
+  // (l, m): 1/R C+_{l-1} / lap(l-1), 1/R C-_{l+1} / lap(l+1), m/R / lap(l),
+  // 1/R C+_{l-1}, 1/R C-_{l+1}, m/R, xa_{l-1}, xb_{l+1} (0 where the neighbour
+  // degree is outside m..L, and 1/lap(0) = 0).
+  std::vector<double> dc((size_t)n * n * 8, 0.0);
+  const double ir = 1.0 / p->radius;
+  for (int l = 0; l < n; ++l)
+    for (int m = 0; m <= l; ++m) {
+      double* c = &dc[((size_t)l * n + m) * 8];
+      const bool lo = l >= 1 && l - 1 >= m, hi = l + 1 < n;
+      const double cpl = lo ? cp[(size_t)(l - 1) * n + m] : 0.0;
+      const double cmh = hi ? cm[(size_t)(l + 1) * n + m] : 0.0;
+      c[0] = lo ? ir * cpl * inv[l - 1] : 0.0;
+      c[1] = hi ? ir * cmh * inv[l + 1] : 0.0;
+      c[2] = m * ir * inv[l];
+      c[3] = ir * cpl;
+      c[4] = ir * cmh;
+      c[5] = m * ir;
+      c[6] = lo ? xa[(size_t)(l - 1) * n + m] : 0.0;
+      c[7] = hi ? xb[(size_t)(l + 1) * n + m] : 0.0;
+    }
+  if ((s = upload(&p->dcoef, dc))) return s;
   return AEOLUS_OK;
 }
 
 void free_plan(aeolus_plan_impl* p) {
   double* bufs[] = {p->x, p->wq, p->coslat, p->fgrid, p->P, p->PT, p->basis, p->wpts,
-                    p->latp, p->cplus, p->cminus, p->cplus_true, p->invlap, p->xa, p->xb};
+                    p->latp, p->cplus, p->cminus, p->cplus_true, p->invlap, p->xa, p->xb, p->dcoef};
   for (double* b : bufs)
     if (b) cudaFree(b);
   if (p->tw) cudaFree(p->tw);
