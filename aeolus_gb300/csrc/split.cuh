@@ -737,7 +737,7 @@ struct AnalSched {
 // Epi::finish; else Epi::finish_field).
 template <class Epi>
 struct AnalEpi {
-  static constexpr int kWarps = 8, kCols = 4 * kNT / kWarps;  // FP64 epilogue: 16 columns per warp
+  static constexpr int kWarps = 16, kCols = 4 * kNT / kWarps;  // FP64 epilogue: 8 columns per warp
   struct State {
     long long T[kCols];
   };
