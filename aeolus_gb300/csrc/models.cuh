@@ -84,6 +84,23 @@ struct BveDerive {  // psi_lam, psi_snt, eta_lam, eta_snt
     const double2* z = zeta + (long)b * (s.L + 1) * (s.L + 1);
     const int L = s.L;
     const double2 zero = make_double2(0.0, 0.0);
+    if (s.dcoef) {  // coefficient products tabulated at the plan radius (see SweDerive::column_tab)
+      const long r = (long)l * (L + 1) + m;
+      const double* c = s.dcoef + r * 8;
+      const double A1 = c[0], A2 = c[1], A3 = c[2], B1 = c[3], B2 = c[4], B3 = c[5];
+      const bool lo = l >= 1 && l - 1 >= m, hi = l + 1 <= L;
+      const double2 zl = z[r];
+      double2 z_lo = lo ? z[r - (L + 1)] : zero, z_hi = hi ? z[r + (L + 1)] : zero;
+      v[0] = make_double2(-A3 * zl.y, A3 * zl.x);
+      v[1] = make_double2(fma(A1, z_lo.x, A2 * z_hi.x), fma(A1, z_lo.y, A2 * z_hi.y));
+      v[2] = make_double2(-B3 * zl.y, B3 * zl.x);
+      if (m == 0) {
+        if (l - 1 == 1) z_lo.x += f10;
+        if (l + 1 == 1) z_hi.x += f10;
+      }
+      v[3] = make_double2(fma(B1, z_lo.x, B2 * z_hi.x), fma(B1, z_lo.y, B2 * z_hi.y));
+      return;
+    }
     double2 psi = s.invlap0(z, l, m);
     double2 psi_lo = l >= 1 ? s.invlap0(z, l - 1, m) : zero;
     double2 psi_hi = l + 1 <= L ? s.invlap0(z, l + 1, m) : zero;

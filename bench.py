@@ -455,6 +455,18 @@ def _rel_l2_fields(a, b):
     return {name: float(v) for name, v in zip(("zeta", "delta", "phi"), worst)}
 
 
+# DRAM bytes (read + write) per launch of the split-path kernels on this
+# workload: dram__bytes_read.sum + dram__bytes_write.sum from one ncu capture
+# of the first RK4 stage (cold L2).
+NCU_TRAFFIC = {
+    "split_synth_slice": 28.211712e6 + 89.324032e6,
+    "tc_synth_bf16x6": 162.591744e6 + 171.899136e6,
+    "rows_df_c2r_products_r2c": 226.601472e6 + 94.253568e6,
+    "split_anal_slice": 231.8528e6 + 104.237312e6,
+    "tc_anal_bf16x6": 230.18496e6 + 67.749888e6,
+}
+
+
 def _roofline(kstats, B, peaks):
     """Roofline entry for every library kernel; the dominant one first."""
     ftx = 2.0 * NLAT * (LMAX + 1) * (LMAX + 2)  # flops of one real-field Legendre transform (no fold credit)
@@ -467,15 +479,16 @@ def _roofline(kstats, B, peaks):
             fields = 9 if name.startswith("tc_synth") else 4
             useful = ftx * fields * B
             entries[name] = {"kernel": name, "bound": "tensor", "achieved": useful / t / 1e12, "peak": tensor,
-                             "unit": "TFLOP/s", "frac": useful / t / 1e12 / tensor, "traffic": None,
-                             "launch_ms": t * 1000.0,
+                             "unit": "TFLOP/s", "frac": useful / t / 1e12 / tensor,
+                             "traffic": NCU_TRAFFIC.get(name), "launch_ms": t * 1000.0,
                              "work_per_launch": f"{fields} fields x {B} members x 2*nlat*(L+1)(L+2) useful flops "
                                                 "(the 21 bf16 digit-pair products are not counted)"}
         elif name.startswith("rows"):
             byt = B * NLAT * (9 + 4) * (LMAX + 1) * 16.0
             entries[name] = {"kernel": name, "bound": "hbm", "achieved": byt / t / 1e9, "peak": hbm, "unit": "GB/s",
-                             "frac": byt / t / 1e9 / hbm, "traffic": None, "launch_ms": t * 1000.0,
-                             "work_per_launch": f"{B} members x {NLAT} rows x 13 spectra x (L+1) x 16 B"}
+                             "frac": byt / t / 1e9 / hbm, "traffic": NCU_TRAFFIC.get(name), "launch_ms": t * 1000.0,
+                             "work_per_launch": f"{B} members x {NLAT} rows x 13 spectra x (L+1) x 16 B",
+                             "note": "issue-bound on double-float FFT arithmetic, not on HBM"}
         elif name.endswith("_f64"):
             fields = 9 if "synth" in name else 4
             useful = ftx * fields * B

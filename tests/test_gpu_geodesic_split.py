@@ -86,3 +86,49 @@ def test_geodesic_level6_lmax127_64_fields():
     psp = Plan.points(N(sh.latitudes), N(sh.longitudes), N(sh.weights), 127)
     psp.set_precision(_lib.PREC_SPLIT_BF16)
     _check(p64, psp, 127, 64, 7, tol=5e-12)
+
+
+@pytest.mark.parametrize("precision", ["fp64", "split"])
+def test_weighted_least_squares_analysis_matches_dense_lstsq(precision):
+    """WLS analysis (preconditioned CG on the normal equations with the
+    plan's own products) against numpy's weighted least squares on the
+    oracle's dense basis; irregular points, so the quadrature analysis alone
+    is not the least-squares fit.  Tolerance 1e-9 relative L2."""
+    import oracle
+    from aeolus_gb300.wls import wls_analysis
+    rng = np.random.default_rng(11)
+    n, L = 900, 12
+    lat = np.arcsin(rng.uniform(-1, 1, n))
+    lon = rng.uniform(-math.pi, math.pi, n)
+    w = rng.uniform(0.5, 1.5, n)
+    w *= 4 * math.pi / w.sum()
+    p = Plan.points(lat, lon, w, L)
+    if precision == "split":
+        p.set_precision(_lib.PREC_SPLIT_BF16)
+    f = rng.standard_normal((2, n))
+    a, iters, res = wls_analysis(p, T(f), iters=60, rtol=1e-13)
+    assert float(res.max()) < 1e-11 and iters < 60
+    # real design matrix of the synthesis f = sum Re Y_l0 Re a_l0 + 2 Re(Y_lm a_lm)
+    Y = oracle.sht.dense_basis(lat, lon, L)
+    cols, idx = [], []
+    for l in range(L + 1):
+        for m in range(l + 1):
+            y = Y[:, l * (l + 1) // 2 + m]
+            if m == 0:
+                cols.append(y.real)
+                idx.append((l, m, 0))
+            else:
+                cols += [2 * y.real, -2 * y.imag]
+                idx += [(l, m, 0), (l, m, 1)]
+    D = np.stack(cols, axis=1)
+    sw = np.sqrt(w)[:, None]
+    ref = np.linalg.lstsq(sw * D, (sw * f.T), rcond=None)[0]
+    got = N(a)
+    out = np.zeros_like(ref)
+    for k, (l, m, c) in enumerate(idx):
+        out[k] = got[:, l, m].imag if c else got[:, l, m].real
+    assert rel_l2(out, ref) < 1e-9
+    # and the quadrature analysis is not the least-squares fit on these points
+    q = N(analyze(p.id, T(f)))
+    qv = np.array([q[:, l, m].imag if c else q[:, l, m].real for (l, m, c) in idx])
+    assert rel_l2(qv, ref) > 1e-3
