@@ -11,6 +11,8 @@
 
 namespace aeolus {
 
+struct FxW;  // fx.cuh
+
 // ---------------------------------------------------------------- errors
 void set_error(const std::string& msg);
 int fail(int code, const std::string& msg);
@@ -119,6 +121,7 @@ struct aeolus_plan_impl {
   double* PT = nullptr;      // [tri_off(m)*nh + jn*(L+1-m) + (l-m)] (degree fastest)
   double2* tw = nullptr;     // [nlon] exp(-2 pi i q / nlon)
   float4* twdf = nullptr;    // [nlon] the same twiddles as double-float (re.hi, re.lo, im.hi, im.lo)
+  FxW* twfx = nullptr;       // [nlon] the same twiddles as Q61 31-bit limbs (fixed-point rows)
   double* invlap = nullptr;  // [L+1] 1 / (-l(l+1)/R^2), 0 at l = 0 (radius of the plan)
   double* xa = nullptr;      // [(L+1)^2] x Y_lm = xa_lm Y_{l+1,m} + xb_lm Y_{l-1,m}
   double* xb = nullptr;      // [(L+1)^2]

@@ -108,9 +108,4 @@ struct RowDf {
   float c;  // cos(latitude) (for guards)
 };
 
-// Constants of the radix-3/5 butterflies as df (hi + lo of the double value).
-struct DfConst {
-  df h3, c1, c2, s1, s2;
-};
-
 }  // namespace aeolus

@@ -69,6 +69,7 @@ template <class Pw>
 struct RowArg {
   RowArgs a;
   Pw pw;
+  const FxW* twfx;
   const float4* twdf;
 };
 template <class Derive>
@@ -83,7 +84,7 @@ struct SliceSynthArg {
 struct SliceAnalArg {
   SplitDims dm;
   int batch, mb, nblk;
-  const float4* FG;
+  const long long* FG;
   __nv_bfloat16* digits;
   int* ecol;
 };
@@ -110,10 +111,11 @@ __global__ void __launch_bounds__(256) g_rows(Grouped<RowArg<Pw>> g) {
 }
 
 template <class Pw>
-__global__ void __launch_bounds__(256) g_rows_df(Grouped<RowArg<Pw>> g, DfConst kc) {
+__global__ void __launch_bounds__(256) g_rows_fx(Grouped<RowArg<Pw>> g, FxConst kc) {
   const int k = g.find(blockIdx.x);
   const int loc = blockIdx.x - g.start[k];
-  row_df_body<Pw, kInF, kOutG>(g.arg[k].a, g.arg[k].pw, g.arg[k].twdf, kc, loc % g.gx[k], loc / g.gx[k]);
+  row_fx_body<Pw, kInF, kOutG>(g.arg[k].a, g.arg[k].pw, g.arg[k].twfx, g.arg[k].twdf, kc, loc % g.gx[k],
+                               loc / g.gx[k]);
 }
 
 template <class Derive>
@@ -235,7 +237,7 @@ int ens_stage(const aeolus_ensemble_s* E, double2* const* y0, int stage, double 
     ra.FG = reinterpret_cast<double2*>(gb[k].chain);
     ra.nblk = 4;
     row_args(p, ra);
-    grouped_add(gr, RowArg<JacPw>{ra, JacPw{}, p->twdf}, dim3(p->nlat, E->batch[k]));
+    grouped_add(gr, RowArg<JacPw>{ra, JacPw{}, p->twfx, p->twdf}, dim3(p->nlat, E->batch[k]));
     sm_rows = std::max(sm_rows, row_smem_bytes<JacPw>(p->fft));
     row_thr = std::max(row_thr, row_threads(p));
   }
@@ -297,7 +299,7 @@ int ens_stage(const aeolus_ensemble_s* E, double2* const* y0, int stage, double 
     const SplitParts r1 = split_synth_parts<4>(p, B, scratch);
     const SplitParts r2 = split_anal_parts<1>(p, B, scratch);
     grouped_add(gss, SliceSynthArg<BveDerive>{r1.dm, p->split->kcum, B, r1.mb, der[k], r1.digits, r1.ecol}, r1.grid);
-    grouped_add(gsa, SliceAnalArg{r2.dm, B, r2.mb, 4, reinterpret_cast<const float4*>(FG), r2.digits, r2.ecol},
+    grouped_add(gsa, SliceAnalArg{r2.dm, B, r2.mb, 4, reinterpret_cast<const long long*>(FG), r2.digits, r2.ecol},
                 r2.grid);
     sm_ss = std::max(sm_ss, r1.smem);
     sm_sa = std::max(sm_sa, r2.smem);
@@ -317,7 +319,7 @@ int ens_stage(const aeolus_ensemble_s* E, double2* const* y0, int stage, double 
   eana.gs = tana;
   auto k1 = g_slice_synth<BveDerive>;
   auto k2 = tc_persistent_kernel<GroupedSched<SynthSched>, GroupedEpi<SynthSched, SynthEpi<4>>>;
-  auto k3 = g_rows_df<JacPw>;
+  auto k3 = g_rows_fx<JacPw>;
   auto k4 = g_slice_anal<1>;
   auto k5 = tc_persistent_kernel<GroupedSched<AnalSched>, GroupedEpi<AnalSched, AnalEpi<BveEpi>>>;
   const size_t smt = tc_smem_bytes();
@@ -336,9 +338,9 @@ int ens_stage(const aeolus_ensemble_s* E, double2* const* y0, int stage, double 
     AE_LAUNCH("tc_persistent_kernel(ensemble synthesis)");
   }
   {
-    ProfScope prof("ens_rows_df", st);
-    k3<<<gr.start[ng], row_thr, sm_rows, st>>>(gr, df_consts());
-    AE_LAUNCH("g_rows_df");
+    ProfScope prof("ens_rows_fx", st);
+    k3<<<gr.start[ng], row_thr, sm_rows, st>>>(gr, fx_consts());
+    AE_LAUNCH("g_rows_fx");
   }
   {
     ProfScope prof("ens_split_anal_slice", st);

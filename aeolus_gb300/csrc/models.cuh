@@ -319,11 +319,15 @@ struct SwePw {
     const df u = df_mul(in[0], r.invc), v = df_mul(in[1], r.invc);
     const df eta_lam = in[2], eta_snt = in[3], phi_lam = in[4], phi_snt = in[5];
     const df zeta = in[6], delta = in[7], phi = in[8];
-    const df eta = df_add(zeta, r.fj);
-    out[0] = df_neg(df_add(df_mul(df_sub(df_mul(u, eta_lam), df_mul(v, eta_snt)), r.invc), df_mul(eta, delta)));
-    out[1] = df_add(df_mul(eta, zeta), df_mul(df_add(df_mul(v, eta_lam), df_mul(u, eta_snt)), r.invc));
-    out[2] = df_scale2(df_add(df_mul(u, u), df_mul(v, v)), 0.5f);
-    out[3] = df_neg(df_add(df_mul(df_sub(df_mul(u, phi_lam), df_mul(v, phi_snt)), r.invc), df_mul(phi, delta)));
+    // Dekker additions: error relative to the operands, the normwise bound
+    // the transforms around these products carry anyway
+    const df eta = df_add_fast(zeta, r.fj);
+    out[0] = df_neg(df_add_fast(df_mul(df_add_fast(df_mul(u, eta_lam), df_neg(df_mul(v, eta_snt))), r.invc),
+                                df_mul(eta, delta)));
+    out[1] = df_add_fast(df_mul(eta, zeta), df_mul(df_add_fast(df_mul(v, eta_lam), df_mul(u, eta_snt)), r.invc));
+    out[2] = df_scale2(df_add_fast(df_mul(u, u), df_mul(v, v)), 0.5f);
+    out[3] = df_neg(df_add_fast(df_mul(df_add_fast(df_mul(u, phi_lam), df_neg(df_mul(v, phi_snt))), r.invc),
+                                df_mul(phi, delta)));
     unsigned bits = 0u;
     if (!(isfinite(out[0].hi) && isfinite(out[1].hi) && isfinite(out[2].hi) && isfinite(out[3].hi)))
       bits |= AEOLUS_STATE_NONFINITE;

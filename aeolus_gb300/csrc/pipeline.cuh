@@ -8,7 +8,7 @@
 #include "common.cuh"
 #include "legendre.cuh"
 #include "rows.cuh"
-#include "rows_df.cuh"
+#include "rows_fx.cuh"
 
 namespace aeolus {
 
@@ -30,16 +30,6 @@ inline int allow_smem(K kern, size_t bytes) {
   if (bytes <= 48 * 1024) return AEOLUS_OK;
   if (bytes > 227 * 1024) return fail(AEOLUS_ERR_ARG, "shared-memory tile exceeds 227 KB for this size");
   return allow_smem_raw(reinterpret_cast<const void*>(kern), bytes);
-}
-
-// Radix-3/5 butterfly constants split into f32 hi + lo words.
-inline DfConst df_consts() {
-  auto split = [](double v) {
-    const float h = (float)v;
-    return df{h, (float)(v - (double)h)};
-  };
-  return DfConst{split(0.86602540378443864676), split(0.30901699437494742410), split(-0.80901699437494742410),
-                 split(0.95105651629515357212), split(0.58778525229247312917)};
 }
 
 inline int round_threads(long items, int lo, int hi) {
@@ -123,14 +113,14 @@ int launch_rows(const aeolus_plan_impl* p, const Pw& pw, RowArgs a, cudaStream_t
   dim3 grid(p->nlat, a.batch);
   const int threads = row_threads(p);
   if (p->precision == AEOLUS_PREC_SPLIT_BF16) {
-    // split-precision path: double-float FFTs and products on the f32 pipe
-    auto kern = row_kernel_df<Pw, IN_MODE, OUT_MODE>;
+    // split-precision path: fixed-point FFTs, double-float products
+    auto kern = row_kernel_fx<Pw, IN_MODE, OUT_MODE>;
     int s = allow_smem(kern, sm);
     if (s) return s;
-    ProfScope prof(IN_MODE == kInF ? (OUT_MODE == kOutG ? "rows_df_c2r_products_r2c" : "rows_df_c2r") : "rows_df_r2c",
+    ProfScope prof(IN_MODE == kInF ? (OUT_MODE == kOutG ? "rows_fx_c2r_products_r2c" : "rows_fx_c2r") : "rows_fx_r2c",
                    st);
-    kern<<<grid, threads, sm, st>>>(a, pw, p->twdf, df_consts());
-    AE_LAUNCH("row_kernel_df");
+    kern<<<grid, threads, sm, st>>>(a, pw, p->twfx, p->twdf, fx_consts());
+    AE_LAUNCH("row_kernel_fx");
     return AEOLUS_OK;
   }
   auto kern = row_kernel<Pw, IN_MODE, OUT_MODE>;

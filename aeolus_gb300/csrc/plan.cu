@@ -9,6 +9,7 @@
 #include <mutex>
 
 #include "common.cuh"
+#include "fx.cuh"
 
 namespace aeolus {
 
@@ -325,6 +326,7 @@ void free_plan(aeolus_plan_impl* p) {
     if (b) cudaFree(b);
   if (p->tw) cudaFree(p->tw);
   if (p->twdf) cudaFree(p->twdf);
+  if (p->twfx) cudaFree(p->twfx);
 }
 
 }  // namespace
@@ -476,6 +478,14 @@ extern "C" int aeolus_plan_create_gauss(int nlat, int nlon, int lmax, double rad
     }
     if ((s = cuda_check(cudaMalloc(&p->twdf, nlon * sizeof(float4)), "cudaMalloc twdf"))) return bail(s);
     if ((s = cuda_check(cudaMemcpy(p->twdf, twf.data(), nlon * sizeof(float4), cudaMemcpyHostToDevice), "twdf")))
+      return bail(s);
+    std::vector<FxW> twx(nlon);
+    for (int q = 0; q < nlon; ++q) {
+      const FxK c = fx_const(tw[q].x), sn = fx_const(tw[q].y);
+      twx[q] = FxW{c.h, c.l, sn.h, sn.l};
+    }
+    if ((s = cuda_check(cudaMalloc(&p->twfx, nlon * sizeof(FxW)), "cudaMalloc twfx"))) return bail(s);
+    if ((s = cuda_check(cudaMemcpy(p->twfx, twx.data(), nlon * sizeof(FxW), cudaMemcpyHostToDevice), "twfx")))
       return bail(s);
   }
   if ((s = cuda_check(cudaMemcpy(p->tw, tw.data(), nlon * sizeof(double2), cudaMemcpyHostToDevice), "tw")))

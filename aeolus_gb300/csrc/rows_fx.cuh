@@ -1,0 +1,390 @@
+// Longitude stage of the split-precision path: 64-bit fixed-point FFTs
+// around double-float pointwise products.
+//
+// Per (latitude row j, member b), as in row_kernel (rows.cuh):
+//   1. the order spectra F_m of every input field arrive as double-floats
+//      written by the tensor-core synthesis; each field's row is rounded to
+//      integers X at one block exponent S_f chosen from its largest element
+//      so that |X| < 2^hb, hb = min(52, 56 - ceil(log2 n));
+//   2. the half-length complex inverse FFT (Stockham, radix 4/2/3/5) runs in
+//      exact 64-bit additions and 31-bit-limb twiddle products -- the bound
+//      on hb keeps every butterfly below 2^59, and the error is ~2^-(hb+1) of
+//      the row's largest input (~2^-49 at n = 192);
+//   3. grid values become double-floats for the pointwise products
+//      (Pw::df_op), weighted by the quadrature weight of the row;
+//   4. each output field is aligned to its own block exponent, forward
+//      FFT'd in fixed point, and the order spectra G_m are written back as
+//      packed words for the analysis slicer.
+// Lengths without a 2/3/5 FFT fall back to a direct double-float DFT.
+#pragma once
+
+#include "df.cuh"
+#include "fx.cuh"
+#include "rows.cuh"
+
+namespace aeolus {
+
+template <bool INV, int R>
+__device__ __forceinline__ void butterfly_fx(cfx* v, const FxConst& k) {
+  if constexpr (R == 2) {
+    const cfx a = v[0], b = v[1];
+    v[0] = fx_add(a, b);
+    v[1] = fx_sub(a, b);
+  } else if constexpr (R == 4) {
+    const cfx s02 = fx_add(v[0], v[2]), d02 = fx_sub(v[0], v[2]);
+    const cfx s13 = fx_add(v[1], v[3]), d13 = fx_sub(v[1], v[3]);
+    const cfx id13 = fx_i<INV>(d13);
+    v[0] = fx_add(s02, s13);
+    v[2] = fx_sub(s02, s13);
+    v[1] = fx_add(d02, id13);
+    v[3] = fx_sub(d02, id13);
+  } else if constexpr (R == 3) {
+    const cfx s = fx_add(v[1], v[2]), d = fx_sub(v[1], v[2]);
+    const cfx t = cfx{v[0].re - (s.re >> 1), v[0].im - (s.im >> 1)};
+    const cfx id = fx_i<INV>(cfx{fx_mulk(d.re, k.h3), fx_mulk(d.im, k.h3)});
+    v[0] = fx_add(v[0], s);
+    v[1] = fx_add(t, id);
+    v[2] = fx_sub(t, id);
+  } else {  // R == 5
+    const cfx a1 = fx_add(v[1], v[4]), a2 = fx_add(v[2], v[3]);
+    const cfx b1 = fx_sub(v[1], v[4]), b2 = fx_sub(v[2], v[3]);
+    const cfx t1 = cfx{v[0].re + fx_mulk(a1.re, k.c1) + fx_mulk(a2.re, k.c2),
+                       v[0].im + fx_mulk(a1.im, k.c1) + fx_mulk(a2.im, k.c2)};
+    const cfx t2 = cfx{v[0].re + fx_mulk(a1.re, k.c2) + fx_mulk(a2.re, k.c1),
+                       v[0].im + fx_mulk(a1.im, k.c2) + fx_mulk(a2.im, k.c1)};
+    const cfx u1 = cfx{fx_mulk(b1.re, k.s1) + fx_mulk(b2.re, k.s2), fx_mulk(b1.im, k.s1) + fx_mulk(b2.im, k.s2)};
+    const cfx u2 = cfx{fx_mulk(b1.re, k.s2) - fx_mulk(b2.re, k.s1), fx_mulk(b1.im, k.s2) - fx_mulk(b2.im, k.s1)};
+    const cfx iu1 = fx_i<INV>(u1), iu2 = fx_i<INV>(u2);
+    v[0] = fx_add(v[0], fx_add(a1, a2));
+    v[1] = fx_add(t1, iu1);
+    v[4] = fx_sub(t1, iu1);
+    v[2] = fx_add(t2, iu2);
+    v[3] = fx_sub(t2, iu2);
+  }
+}
+
+// One Stockham stage.  TW = false for the first stage (Ls = 1, no
+// twiddles); later stages multiply every input, the k = 0 ones by the exact
+// unit twiddle, so the loop has no data-dependent branch.
+template <bool INV, int R, bool TW>
+__device__ __forceinline__ void fft_stage_fx(const cfx* __restrict__ src, cfx* __restrict__ dst, int nf, int n, int fs,
+                                             int Ls, unsigned nb_rcp, unsigned ls_rcp, const FxW* __restrict__ tw,
+                                             const FxConst& kc) {
+  const int nb = n / R, Ns = Ls * R, stride = n / Ns;
+  for (int idx = threadIdx.x; idx < nf * nb; idx += blockDim.x) {
+    const int f = div_rcp(idx, nb, nb_rcp), jj = idx - f * nb;
+    const int q = div_rcp(jj, Ls, ls_rcp), k = jj - q * Ls;
+    const cfx* x = src + (long)f * fs;
+    cfx* y = dst + (long)f * fs;
+    cfx v[R];
+#pragma unroll
+    for (int t = 0; t < R; ++t) v[t] = x[jj + t * nb];
+    if (TW) {
+#pragma unroll
+      for (int t = 1; t < R; ++t) v[t] = fx_cmul<INV>(v[t], fx_ldw(&tw[2 * (k * t * stride)]));
+    }
+    butterfly_fx<INV, R>(v, kc);
+    const int base = q * Ns + k;
+#pragma unroll
+    for (int t = 0; t < R; ++t) y[base + t * Ls] = v[t];
+  }
+}
+
+template <bool INV>
+__device__ cfx* fft_run_fx(cfx* src, cfx* dst, int nf, int fs, const FftInfo& fi, const FxW* __restrict__ tw,
+                           const FxConst& kc) {
+  const int n = fi.n;
+  int Ls = 1;
+  for (int s = 0; s < fi.nfac; ++s) {
+    const int r = fi.fac[s];
+    if (s == 0) {
+      switch (r) {
+        case 4: fft_stage_fx<INV, 4, false>(src, dst, nf, n, fs, Ls, fi.nbm[s], fi.lsm[s], tw, kc); break;
+        case 2: fft_stage_fx<INV, 2, false>(src, dst, nf, n, fs, Ls, fi.nbm[s], fi.lsm[s], tw, kc); break;
+        case 3: fft_stage_fx<INV, 3, false>(src, dst, nf, n, fs, Ls, fi.nbm[s], fi.lsm[s], tw, kc); break;
+        default: fft_stage_fx<INV, 5, false>(src, dst, nf, n, fs, Ls, fi.nbm[s], fi.lsm[s], tw, kc); break;
+      }
+    } else {
+      switch (r) {
+        case 4: fft_stage_fx<INV, 4, true>(src, dst, nf, n, fs, Ls, fi.nbm[s], fi.lsm[s], tw, kc); break;
+        case 2: fft_stage_fx<INV, 2, true>(src, dst, nf, n, fs, Ls, fi.nbm[s], fi.lsm[s], tw, kc); break;
+        case 3: fft_stage_fx<INV, 3, true>(src, dst, nf, n, fs, Ls, fi.nbm[s], fi.lsm[s], tw, kc); break;
+        default: fft_stage_fx<INV, 5, true>(src, dst, nf, n, fs, Ls, fi.nbm[s], fi.lsm[s], tw, kc); break;
+      }
+    }
+    __syncthreads();
+    cfx* tmp = src;
+    src = dst;
+    dst = tmp;
+    Ls *= r;
+  }
+  return src;
+}
+
+// X 2^S as a double-float for |X| < 2^59 (pa pb = 2^S), on the FMA/ALU
+// pipes: X = c2 2^40 + c1 2^20 + c0 with 20-bit limbs, each limb made exact
+// by the magic-number construction (the limb placed in the mantissa of a
+// float of known exponent, that float's offset subtracted), then summed
+// with error-free transformations.
+__device__ __forceinline__ df fx_to_df(long long X, float pa, float pb) {
+  const unsigned lo = static_cast<unsigned>(X), hi = static_cast<unsigned>(X >> 32);
+  const unsigned c0 = lo & 0xFFFFFu;
+  const unsigned c1 = __funnelshift_r(lo, hi, 20) & 0xFFFFFu;
+  const int c2 = static_cast<int>(X >> 40);
+  const float f0 = __int_as_float(0x4B000000 | c0) - 8388608.0f;                    // c0
+  const float f1 = __int_as_float((170u << 23) | c1) - 8796093022208.0f;            // c1 2^20
+  const float f2 = __int_as_float((190 << 23) + 0x400000 + c2) - 13835058055282163712.0f;  // c2 2^40
+  const float s = f2 + f1;
+  const float e1 = f1 - (s - f2);  // exact: |f2| >= |f1| or f2 = 0
+  const float t = e1 + f0;
+  const float h = s + t;
+  const float l = t - (h - s);
+  return df{h * pa * pb, l * pa * pb};
+}
+
+// rint(v 2^-S) for pa pb = 2^-S and |v 2^-S| < 2^52: the high word splits
+// into u 2^30 + r (u by the magic-number rounding, r exact by FMA), r and
+// the low word are rounded by 32-bit conversions.
+__device__ __forceinline__ long long df_to_fx(df v, float pa, float pb) {
+  const float th = v.hi * pa * pb, tl = v.lo * pa * pb;
+  const float um = fmaf(th, 9.31322574615478515625e-10f, 12582912.0f);  // th 2^-30 + 1.5 2^23
+  const int u = __float_as_int(um) - 0x4B400000;
+  const float r = fmaf(-(um - 12582912.0f), 1073741824.0f, th);
+  const int rl = __float2int_rn(r) + __float2int_rn(tl);
+  return fx_madw(u, 1 << 30, static_cast<long long>(rl));
+}
+// Exponent E with |x| < 2^E for every float whose |bits| <= key.
+__device__ __forceinline__ int fkey_exp(unsigned key) { return static_cast<int>(key >> 23) - 126; }
+// A double-float as a packed word (52-bit mantissa).
+__device__ __forceinline__ long long df_to_pk(df v) {
+  const unsigned key = __float_as_uint(v.hi) & 0x7FFFFFFFu;
+  if ((key >> 23) == 0) return 0;
+  const int S = fkey_exp(key) - kPackMant;
+  float pa, pb;
+  fx_pow2_split(-S, pa, pb);
+  return pk_pack(df_to_fx(v, pa, pb), S);
+}
+
+template <class Pw, int IN_MODE, int OUT_MODE>
+__device__ __forceinline__ void row_fx_body(const RowArgs& a, const Pw& pw, const FxW* __restrict__ twfx,
+                                            const float4* __restrict__ twdf, const FxConst& kc, int bx, int by) {
+  constexpr int NIN = Pw::NIN, NOUT = Pw::NOUT;
+  constexpr int NF = NIN > NOUT ? NIN : NOUT;
+  extern __shared__ cfx smem_fx[];
+  __shared__ unsigned s_bits;
+  __shared__ int s_in[NF];        // block exponents (inputs, then outputs)
+  __shared__ unsigned s_key[NF];   // largest |hi| bit key of each input field
+  __shared__ unsigned s_omax[NF];  // largest |hi| bit key of each output field
+  __shared__ float s_pa[NF], s_pb[NF], s_qa[NF], s_qb[NF];  // 2^S, 2^-S in two factors
+  __shared__ RowDf s_rc;
+  __shared__ df s_wj;
+  const int j = bx, b = by;
+  const int N = a.fft.N, n = a.fft.n, L = a.L;
+  const int ldm = L + 1;
+  const int ns = n + 1;  // padded field stride of the smem rows (see row_body)
+  const bool use_fft = a.fft.use_fft != 0;
+  const int hb = min(52, 56 - (32 - __clz(max(n - 1, 1))));  // |fixed-point FFT input| < 2^hb
+  cfx* buf0 = smem_fx;
+  cfx* buf1 = smem_fx + (long)NF * ns;
+  if (threadIdx.x == 0) s_bits = 0u;
+  if (threadIdx.x < NF) {
+    s_key[threadIdx.x] = 0u;
+    s_omax[threadIdx.x] = 0u;
+  }
+  if (threadIdx.x == 0) {  // row constants, once per block (FP64 work)
+    s_rc = pw.df_row(a.coslat[j], a.fgrid ? a.fgrid[j] : 0.0);
+    s_wj = (OUT_MODE == kOutG && a.wq) ? df_from_double(a.wq[j]) : df{1.f, 0.f};
+  }
+  // this row's order spectra: field f, order q at block[q sq + f]; spectra
+  // in: double-floats (float4), spectra out: packed words (two per float4 slot)
+  const long sq = (long)a.nblk * a.nlat;
+  float4* block = nullptr;
+  if (IN_MODE == kInF || OUT_MODE == kOutG)
+    block = reinterpret_cast<float4*>(a.FG) + fg_index(b, 0, 0, j, L, a.nblk, a.nlat);
+  __syncthreads();
+
+  // ---- 1. grid rows of the inputs
+  // in_fx: fixed-point rows X (field stride 2 ns, value X 2^s_in[f]);
+  // otherwise double-float rows.
+  const bool in_fx = IN_MODE == kInF && use_fft;
+  void* xin = buf0;
+  if (IN_MODE == kInF) {
+    // largest |hi| of each field's spectra (fields fastest: contiguous reads)
+    for (int idx = threadIdx.x; idx < NIN * ldm; idx += blockDim.x) {
+      const int q = idx / NIN, f = idx - q * NIN;
+      const float4 w = block[(long)q * sq + f];
+      const unsigned key = max(__float_as_uint(w.x) & 0x7FFFFFFFu,
+                               q == 0 ? 0u : __float_as_uint(w.z) & 0x7FFFFFFFu);  // m = 0: Im dropped
+      if (key) atomicMax(&s_key[f], key);
+    }
+    __syncthreads();
+    if (threadIdx.x < NIN) {  // block exponent: |F| < 2^E -> |X| < 2^hb
+      const unsigned key = s_key[threadIdx.x];
+      const int S = (key >> 23) == 0 ? 0 : fkey_exp(key) - hb;
+      s_in[threadIdx.x] = S;
+      fx_pow2_split(S, s_pa[threadIdx.x], s_pb[threadIdx.x]);
+      fx_pow2_split(-S, s_qa[threadIdx.x], s_qb[threadIdx.x]);
+    }
+    __syncthreads();
+    if (use_fft) {
+      // half-length complex input of the real inverse FFT, by pairs (q, n-q):
+      //   A = h_q + conj(h_{n-q}), B = h_q - conj(h_{n-q}), P = i conj(e_q) B,
+      //   z_q = A + P, z_{n-q} = conj(A - P)   (e_{n-q} = -conj(e_q))
+      const int half = n / 2;
+      for (int idx = threadIdx.x; idx < NIN * (half + 1); idx += blockDim.x) {
+        const int q = idx / NIN, f = idx - q * NIN;
+        const float qa = s_qa[f], qb = s_qb[f];
+        const int qn = n - q;
+        cfx hq = cfx{0, 0}, hn = cfx{0, 0};
+        if (q <= L) {
+          const float4 w = block[(long)q * sq + f];
+          hq = cfx{df_to_fx(df{w.x, w.y}, qa, qb), q == 0 ? 0LL : df_to_fx(df{w.z, w.w}, qa, qb)};
+        }
+        if (q > 0 && qn <= L) {
+          const float4 w = block[(long)qn * sq + f];
+          hn = cfx{df_to_fx(df{w.x, w.y}, qa, qb), df_to_fx(df{w.z, w.w}, qa, qb)};
+        }
+        const cfx A = fx_add(hq, fx_conj(hn));
+        const cfx B = fx_sub(hq, fx_conj(hn));
+        const cfx P = fx_i<true>(fx_cmul<true>(B, fx_ldw(&twfx[q])));
+        cfx* z = buf0 + (long)f * ns;
+        z[q] = fx_add(A, P);
+        if (q > 0 && qn > q) z[qn] = fx_conj(fx_sub(A, P));
+      }
+      __syncthreads();
+      xin = fft_run_fx<true>(buf0, buf1, NIN, ns, a.fft, twfx, kc);
+    } else {
+      // direct DFT in double-float: stage the spectra in buf1
+      cdf* Fs = reinterpret_cast<cdf*>(buf1);
+      for (int idx = threadIdx.x; idx < NIN * ldm; idx += blockDim.x) {
+        const int q = idx / NIN, f = idx - q * NIN;
+        float4 w = block[(long)q * sq + f];
+        if (q == 0) w.z = w.w = 0.f;
+        Fs[(long)f * ns + q] = cdf_from_f4(w);
+      }
+      __syncthreads();
+      df* x0 = reinterpret_cast<df*>(buf0);
+      for (int idx = threadIdx.x; idx < NIN * N; idx += blockDim.x) {
+        const int f = idx / N, k = idx - f * N;
+        const cdf* Ff = Fs + (long)f * ns;
+        df acc = df{0.f, 0.f};
+        int e = 0;
+        for (int m = 1; m <= L; ++m) {
+          e += k;
+          if (e >= N) e -= N;
+          const cdf w = cdf_from_f4(__ldg(&twdf[e]));
+          const cdf F = Ff[m];
+          acc = df_add_fast(acc, df_add_fast(df_mul(F.re, w.re), df_mul(F.im, w.im)));
+        }
+        x0[(long)f * 2 * ns + k] = df_add_fast(Ff[0].re, df_scale2(acc, 2.0f));
+      }
+      __syncthreads();
+    }
+  } else {
+    df* x0 = reinterpret_cast<df*>(buf0);
+    for (int idx = threadIdx.x; idx < NIN * N; idx += blockDim.x) {
+      const int f = idx / N, k = idx - f * N;
+      x0[(long)f * 2 * ns + k] = df_from_double(a.gin[(long)b * a.gin_b + (long)f * a.gin_f + (long)j * N + k]);
+    }
+    __syncthreads();
+  }
+
+  // ---- 2. pointwise products (double-float), weighted by the row's quadrature weight
+  cfx* zout = (xin == static_cast<void*>(buf0)) ? buf1 : buf0;
+  df* xout = reinterpret_cast<df*>(zout);
+  {
+    const RowDf rc = s_rc;
+    const df wj = s_wj;
+    const long long* xi = static_cast<const long long*>(xin);
+    const df* xd = static_cast<const df*>(xin);
+    unsigned bits = 0u;
+    unsigned omax[NOUT];
+#pragma unroll
+    for (int f = 0; f < NOUT; ++f) omax[f] = 0u;
+    for (int k = threadIdx.x; k < N; k += blockDim.x) {
+      df in[NIN], out[NOUT];
+#pragma unroll
+      for (int f = 0; f < NIN; ++f)
+        in[f] = in_fx ? fx_to_df(xi[(long)f * 2 * ns + k], s_pa[f], s_pb[f]) : xd[(long)f * 2 * ns + k];
+      bits |= pw.df_op(rc, in, out);
+#pragma unroll
+      for (int f = 0; f < NOUT; ++f) {
+        if (OUT_MODE == kOutG && a.wq) out[f] = df_mul(out[f], wj);
+        xout[(long)f * 2 * ns + k] = out[f];
+        omax[f] = max(omax[f], __float_as_uint(out[f].hi) & 0x7FFFFFFFu);
+      }
+    }
+    if (a.status && bits) atomicOr(&s_bits, bits);
+    if (OUT_MODE == kOutG && use_fft) {
+#pragma unroll
+      for (int f = 0; f < NOUT; ++f) {
+        unsigned v = omax[f];
+        for (int o = 16; o > 0; o >>= 1) v = max(v, __shfl_xor_sync(0xffffffffu, v, o));
+        if ((threadIdx.x & 31) == 0 && v) atomicMax(&s_omax[f], v);
+      }
+    }
+  }
+  __syncthreads();
+  if (a.status && threadIdx.x == 0 && s_bits) atomicOr(&a.status[b], s_bits);
+
+  // ---- 3. outputs
+  if (OUT_MODE == kOutGrid) {
+    for (int idx = threadIdx.x; idx < NOUT * N; idx += blockDim.x) {
+      const int f = idx / N, k = idx - f * N;
+      a.gout[(long)b * a.gout_b + (long)f * a.gout_f + (long)j * N + k] = df_to_double(xout[(long)f * 2 * ns + k]);
+    }
+  } else if (use_fft) {
+    // output block exponents (|X| < 2^hb), rows to fixed point in place
+    if (threadIdx.x < NOUT) {
+      const unsigned key = s_omax[threadIdx.x];
+      const int S = (key >> 23) == 0 ? 0 : fkey_exp(key) - hb;
+      s_in[threadIdx.x] = S;
+      fx_pow2_split(-S, s_pa[threadIdx.x], s_pb[threadIdx.x]);
+    }
+    __syncthreads();
+    long long* xo = reinterpret_cast<long long*>(zout);
+    for (int idx = threadIdx.x; idx < NOUT * N; idx += blockDim.x) {
+      const int f = idx / N, k = idx - f * N;
+      const long o = (long)f * 2 * ns + k;
+      xo[o] = df_to_fx(xout[o], s_pa[f], s_pb[f]);
+    }
+    __syncthreads();
+    cfx* zother = (zout == buf0) ? buf1 : buf0;
+    cfx* Z = fft_run_fx<false>(zout, zother, NOUT, ns, a.fft, twfx, kc);
+    for (int idx = threadIdx.x; idx < NOUT * ldm; idx += blockDim.x) {
+      const int q = idx / NOUT, f = idx - q * NOUT;  // fields fastest: contiguous global writes
+      const cfx* Zf = Z + (long)f * ns;
+      const cfx zq = Zf[q];
+      const cfx zn = fx_conj(Zf[q == 0 ? 0 : n - q]);
+      const cfx E2 = fx_add(zq, zn);             // 2 E
+      const cfx D = fx_sub(zq, zn);
+      const cfx O2 = cfx{D.im, -D.re};           // 2 O = -i D
+      const cfx R2 = fx_add(E2, fx_cmul<false>(O2, fx_ldw(&twfx[q])));
+      const int e = s_in[f] - 1;                 // R2 / 2 in units of 2^S
+      reinterpret_cast<longlong2*>(block)[(long)q * sq + f] = make_longlong2(pk_pack(R2.re, e), pk_pack(R2.im, e));
+    }
+  } else {
+    for (int idx = threadIdx.x; idx < NOUT * ldm; idx += blockDim.x) {
+      const int q = idx / NOUT, f = idx - q * NOUT;
+      const df* x = xout + (long)f * 2 * ns;
+      df sr = df{0.f, 0.f}, si = df{0.f, 0.f};
+      int e = 0;
+      for (int k = 0; k < N; ++k) {
+        const cdf w = cdf_from_f4(__ldg(&twdf[e]));
+        sr = df_add_fast(sr, df_mul(x[k], w.re));
+        si = df_add_fast(si, df_mul(x[k], w.im));
+        e += q;
+        while (e >= N) e -= N;
+      }
+      reinterpret_cast<longlong2*>(block)[(long)q * sq + f] = make_longlong2(df_to_pk(sr), df_to_pk(si));
+    }
+  }
+}
+
+template <class Pw, int IN_MODE, int OUT_MODE>
+__global__ void __launch_bounds__(256) row_kernel_fx(RowArgs a, Pw pw, const FxW* __restrict__ twfx,
+                                                     const float4* __restrict__ twdf, FxConst kc) {
+  row_fx_body<Pw, IN_MODE, OUT_MODE>(a, pw, twfx, twdf, kc, blockIdx.x, blockIdx.y);
+}
+
+}  // namespace aeolus

@@ -7,6 +7,7 @@
 
 #include "common.cuh"
 #include "df.cuh"
+#include "fx.cuh"
 #include "legendre.cuh"
 #include "tc.cuh"
 
@@ -117,84 +118,7 @@ __device__ inline double scaled_to_double(long long T, int e) {
                                                      (mant & 0xFFFFFFFFFFFFFull)));
 }
 
-// ------------------------------------------------ double-float conversions
-// Round a > 0 to 24 significant bits: a ~ q 2^sh with q < 2^24 (RNE).
-__device__ inline void round24(unsigned long long a, unsigned long long& q, int& sh) {
-  const int msb = 63 - __clzll(static_cast<long long>(a));
-  if (msb <= 23) {
-    q = a;
-    sh = 0;
-    return;
-  }
-  sh = msb - 23;
-  q = a >> sh;
-  const unsigned long long rem = a & ((1ull << sh) - 1), half = 1ull << (sh - 1);
-  if (rem > half || (rem == half && (q & 1ull))) {
-    ++q;
-    if (q >> 24) {
-      q >>= 1;
-      ++sh;
-    }
-  }
-}
-
-// q 2^(sh+e) as a float (q < 2^24 exact); below the normal range -> 0.
-__device__ inline float make_float(unsigned long long q, int sh, int e, bool neg) {
-  if (q == 0) return 0.0f;
-  const int msb = 63 - __clzll(static_cast<long long>(q));
-  const int ex = msb + sh + e + 127;
-  if (ex <= 0) return 0.0f;
-  if (ex >= 255) return neg ? -INFINITY : INFINITY;
-  const unsigned m = static_cast<unsigned>((q << (23 - msb)) & 0x7FFFFFull);
-  return __uint_as_float((neg ? 0x80000000u : 0u) | (static_cast<unsigned>(ex) << 23) | m);
-}
-
-// T 2^e as a double-float (hi = fl(T 2^e), lo = fl((T - hi) 2^e)), integer ops.
-__device__ inline df scaled_to_df(long long T, int e) {
-  if (T == 0) return df{0.f, 0.f};
-  const bool neg = T < 0;
-  const unsigned long long a = neg ? static_cast<unsigned long long>(-T) : static_cast<unsigned long long>(T);
-  unsigned long long q;
-  int sh;
-  round24(a, q, sh);
-  const float hi = make_float(q, sh, e, neg);
-  const long long r = static_cast<long long>(a) - static_cast<long long>(q << sh);
-  if (r == 0) return df{hi, 0.f};
-  const bool rneg = (r < 0) != neg;
-  unsigned long long q2;
-  int sh2;
-  round24(static_cast<unsigned long long>(r < 0 ? -r : r), q2, sh2);
-  return df{hi, make_float(q2, sh2, e, rneg)};
-}
-
-// rint(f 2^(48-E)) for a float f, integer ops (|result| < 2^47 by choice of E).
-__device__ inline long long fixed_point_f(float f, int E) {
-  const unsigned b = __float_as_uint(f);
-  const int ex = static_cast<int>((b >> 23) & 0xFF);
-  if (ex == 0 || E == -1000) return 0;
-  const unsigned long long m = (b & 0x7FFFFFu) | 0x800000u;  // |f| = m 2^(ex-150)
-  const int sh = 150 - kShift + E - ex;
-  unsigned long long q;
-  if (sh >= 25) {
-    q = 0;
-  } else if (sh <= 0) {
-    q = m << (-sh);
-  } else {
-    q = m >> sh;
-    const unsigned long long rem = m & ((1ull << sh) - 1), half = 1ull << (sh - 1);
-    if (rem > half || (rem == half && (q & 1ull))) ++q;
-  }
-  const long long X = static_cast<long long>(q);
-  return (b >> 31) ? -X : X;
-}
-
-// Exponent for a column of double-floats from the largest |hi| bit key:
-// |hi + lo| 2^-E < 1/4 (one spare bit for the lo word).
-__device__ inline int exponent_for_fkey(unsigned k) {
-  const int ex = static_cast<int>(k >> 23);
-  return ex == 0 ? -1000 : ex - 124;
-}
-
+// Balanced base-256 digits of a fixed-point integer X (|X| <= 2^47).
 __device__ inline void digits_from_fixed(long long X, float* d) {
 #pragma unroll
   for (int i = kSlices - 1; i >= 1; --i) {
@@ -336,15 +260,14 @@ __global__ void __launch_bounds__(256) split_synth_slice_kernel(SplitDims dm, co
 }
 
 // ------------------------------------------------- analysis data slicing
-// Reads the double-float G blocks (float4 per complex value), grid (m, chunk).
+// Reads the packed G words (fx.cuh; two per complex value), grid (m, chunk).
 template <int NF>
 __device__ __forceinline__ void split_anal_slice_body(const SplitDims& dm, int batch, int mb, int nblk,
-                                                      const float4* __restrict__ FG, __nv_bfloat16* __restrict__ dana,
+                                                      const long long* __restrict__ FG, __nv_bfloat16* __restrict__ dana,
                                                       int* __restrict__ ecol, int bx, int by, int gy) {
-  extern __shared__ df s_dval[];  // [mb*NF*2][nlat]
+  extern __shared__ long long s_wval[];  // [mb*NF*2][nlat]
   __shared__ int s_exp[256];
   const int m = bx, L = dm.L, nlat = dm.nlat, NK = dm.NK;
-  const int ldm = L + 1;
   const int b0 = by * mb;
   const int nb = min(mb, batch - b0);
   const int nc = nb * NF * 2;
@@ -352,18 +275,18 @@ __device__ __forceinline__ void split_anal_slice_body(const SplitDims& dm, int b
     const int f = idx % NF;
     const int r = idx / NF;
     const int j = r % nlat, bl = r / nlat;
-    const float4 g = FG[fg_index(b0 + bl, m, f, j, L, nblk, nlat)];
-    s_dval[((bl * NF + f) * 2 + 0) * nlat + j] = df{g.x, g.y};
-    s_dval[((bl * NF + f) * 2 + 1) * nlat + j] = df{g.z, g.w};
+    const longlong2 g = *reinterpret_cast<const longlong2*>(FG + 2 * fg_index(b0 + bl, m, f, j, L, nblk, nlat));
+    s_wval[((bl * NF + f) * 2 + 0) * nlat + j] = g.x;
+    s_wval[((bl * NF + f) * 2 + 1) * nlat + j] = g.y;
   }
   __syncthreads();
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
   for (int c = warp; c < nc; c += nwarp) {
-    unsigned mx = 0u;
-    for (int j = lane; j < nlat; j += 32) mx = max(mx, __float_as_uint(s_dval[c * nlat + j].hi) & 0x7FFFFFFFu);
+    int mx = -100000;
+    for (int j = lane; j < nlat; j += 32) mx = max(mx, pk_mag(s_wval[c * nlat + j]));
     for (int o = 16; o > 0; o >>= 1) mx = max(mx, __shfl_xor_sync(0xffffffffu, mx, o));
     if (lane == 0) {
-      const int E = exponent_for_fkey(mx);
+      const int E = mx == -100000 ? -1000 : mx + 1;  // |x| 2^-E < 1/2
       s_exp[c] = E;
       ecol[(long long)m * dm.ntiles * kNT + (long long)b0 * NF * 2 + c] = E;
     }
@@ -373,11 +296,8 @@ __device__ __forceinline__ void split_anal_slice_body(const SplitDims& dm, int b
     const int c = idx / NK, j = idx - c * NK;
     const int n = b0 * NF * 2 + c;
     float d[kSlices];
-    long long X = 0;
-    if (j < nlat) {
-      const df v = s_dval[c * nlat + j];
-      X = fixed_point_f(v.hi, s_exp[c]) + fixed_point_f(v.lo, s_exp[c]);
-    }
+    // X = rint(x 2^(48 - E)), |X| <= 2^47
+    const long long X = j < nlat ? pk_align(s_wval[c * nlat + j], s_exp[c] - kShift) : 0LL;
     digits_from_fixed(X, d);
     __nv_bfloat16* tile = dana + dana_tile(dm, m, n / kNT);
 #pragma unroll
@@ -397,7 +317,7 @@ __device__ __forceinline__ void split_anal_slice_body(const SplitDims& dm, int b
 
 template <int NF>
 __global__ void __launch_bounds__(256) split_anal_slice_kernel(SplitDims dm, int batch, int mb, int nblk,
-                                                              const float4* __restrict__ FG,
+                                                              const long long* __restrict__ FG,
                                                               __nv_bfloat16* __restrict__ dana,
                                                               int* __restrict__ ecol) {
   split_anal_slice_body<NF>(dm, batch, mb, nblk, FG, dana, ecol, blockIdx.x, blockIdx.y, gridDim.y);
@@ -680,7 +600,8 @@ struct SynthSched {
   }
 };
 
-// Writes double-float F blocks (float4 per complex value); NF fields.
+// Writes the F blocks as double-floats (float4 = re.hi, re.lo, im.hi, im.lo per
+// complex value); NF fields.
 template <int NF>
 struct SynthEpi {
   static constexpr int kWarps = 16, kCols = 4 * kNT / kWarps;
@@ -899,7 +820,8 @@ int launch_split_anal(const aeolus_plan_impl* p, const Epi& e, const double2* FG
   if (s) return s;
   {
     ProfScope prof("split_anal_slice", st);
-    k1<<<r.grid, 256, r.smem, st>>>(r.dm, batch, r.mb, nblk, reinterpret_cast<const float4*>(FG), r.digits, r.ecol);
+    k1<<<r.grid, 256, r.smem, st>>>(r.dm, batch, r.mb, nblk, reinterpret_cast<const long long*>(FG), r.digits,
+                                     r.ecol);
     AE_LAUNCH("split_anal_slice_kernel");
   }
   const size_t sm2 = tc_smem_bytes();

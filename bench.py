@@ -461,7 +461,6 @@ def _rel_l2_fields(a, b):
 NCU_TRAFFIC = {
     "split_synth_slice": 28.211712e6 + 89.324032e6,
     "tc_synth_bf16x6": 162.591744e6 + 171.899136e6,
-    "rows_df_c2r_products_r2c": 226.601472e6 + 94.253568e6,
     "split_anal_slice": 231.8528e6 + 104.237312e6,
     "tc_anal_bf16x6": 230.18496e6 + 67.749888e6,
 }
