@@ -122,6 +122,7 @@ struct aeolus_plan_impl {
   double2* tw = nullptr;     // [nlon] exp(-2 pi i q / nlon)
   float4* twdf = nullptr;    // [nlon] the same twiddles as double-float (re.hi, re.lo, im.hi, im.lo)
   FxW* twfx = nullptr;       // [nlon] the same twiddles as Q61 31-bit limbs (fixed-point rows)
+  int* fft_irev = nullptr;   // [fft.n] position of natural index q in digit-reversed order (in-place FFTs)
   double* invlap = nullptr;  // [L+1] 1 / (-l(l+1)/R^2), 0 at l = 0 (radius of the plan)
   double* xa = nullptr;      // [(L+1)^2] x Y_lm = xa_lm Y_{l+1,m} + xb_lm Y_{l-1,m}
   double* xb = nullptr;      // [(L+1)^2]

@@ -238,7 +238,7 @@ int ens_stage(const aeolus_ensemble_s* E, double2* const* y0, int stage, double 
     ra.nblk = 4;
     row_args(p, ra);
     grouped_add(gr, RowArg<JacPw>{ra, JacPw{}, p->twfx, p->twdf}, dim3(p->nlat, E->batch[k]));
-    sm_rows = std::max(sm_rows, row_smem_bytes<JacPw>(p->fft));
+    sm_rows = std::max(sm_rows, E->split ? row_fx_smem_bytes<JacPw>(p->fft) : row_smem_bytes<JacPw>(p->fft));
     row_thr = std::max(row_thr, row_threads(p));
   }
   if (!E->split) {

@@ -100,6 +100,7 @@ inline void row_args(const aeolus_plan_impl* p, RowArgs& a) {
   a.L = p->lmax;
   a.nlat = p->nlat;
   a.fft = p->fft;
+  a.irev = p->fft_irev;
   a.tw = p->tw;
   a.coslat = p->coslat;
   a.fgrid = p->fgrid;
@@ -109,10 +110,10 @@ inline void row_args(const aeolus_plan_impl* p, RowArgs& a) {
 template <class Pw, int IN_MODE, int OUT_MODE>
 int launch_rows(const aeolus_plan_impl* p, const Pw& pw, RowArgs a, cudaStream_t st) {
   row_args(p, a);
-  const size_t sm = row_smem_bytes<Pw>(p->fft);
   dim3 grid(p->nlat, a.batch);
   const int threads = row_threads(p);
   if (p->precision == AEOLUS_PREC_SPLIT_BF16) {
+    const size_t sm = row_fx_smem_bytes<Pw>(p->fft);
     // split-precision path: fixed-point FFTs, double-float products
     auto kern = row_kernel_fx<Pw, IN_MODE, OUT_MODE>;
     int s = allow_smem(kern, sm);
@@ -123,6 +124,7 @@ int launch_rows(const aeolus_plan_impl* p, const Pw& pw, RowArgs a, cudaStream_t
     AE_LAUNCH("row_kernel_fx");
     return AEOLUS_OK;
   }
+  const size_t sm = row_smem_bytes<Pw>(p->fft);
   auto kern = row_kernel<Pw, IN_MODE, OUT_MODE>;
   int s = allow_smem(kern, sm);
   if (s) return s;

@@ -246,12 +246,17 @@ void plan_fft(int N, int L, FftInfo& f) {
   if (N % 2 != 0) return;
   int n = N / 2;
   if (L > n - 1) return;  // Nyquist / aliased orders: direct DFT handles them
+  // Radix order: odd radices first, then 2, then 4s.  A stage with
+  // sub-transform length 1 touches shared memory at a stride of its radix,
+  // which is free of bank conflicts for an odd radix.
   int rem = n, nf = 0, fac[kMaxFactors];
-  while (rem % 4 == 0 && nf < kMaxFactors) { fac[nf++] = 4; rem /= 4; }
-  const int radices[3] = {2, 3, 5};
+  int c4 = 0;
+  while (rem % 4 == 0) { ++c4; rem /= 4; }
+  const int radices[3] = {3, 5, 2};
   for (int r : radices)
     while (rem % r == 0 && nf < kMaxFactors) { fac[nf++] = r; rem /= r; }
-  if (rem != 1 || n > kMaxFftHalf) return;
+  for (int i = 0; i < c4 && nf < kMaxFactors; ++i) fac[nf++] = 4;
+  if (rem != 1 || nf == kMaxFactors || n > kMaxFftHalf) return;
   f.use_fft = 1;
   f.n = n;
   f.nfac = nf;
@@ -327,6 +332,7 @@ void free_plan(aeolus_plan_impl* p) {
   if (p->tw) cudaFree(p->tw);
   if (p->twdf) cudaFree(p->twdf);
   if (p->twfx) cudaFree(p->twfx);
+  if (p->fft_irev) cudaFree(p->fft_irev);
 }
 
 }  // namespace
@@ -487,6 +493,25 @@ extern "C" int aeolus_plan_create_gauss(int nlat, int nlon, int lmax, double rad
     if ((s = cuda_check(cudaMalloc(&p->twfx, nlon * sizeof(FxW)), "cudaMalloc twfx"))) return bail(s);
     if ((s = cuda_check(cudaMemcpy(p->twfx, twx.data(), nlon * sizeof(FxW), cudaMemcpyHostToDevice), "twfx")))
       return bail(s);
+    if (p->fft.use_fft) {
+      // digit reversal of the in-place transforms: position t = t0 + R0 (t1 + R1 (...))
+      // holds natural index t0 n/R0 + t1 n/(R0 R1) + ...
+      const int n = p->fft.n;
+      std::vector<int> irev(n);
+      for (int t = 0; t < n; ++t) {
+        int rest = n, q = 0, u = t;
+        for (int k = 0; k < p->fft.nfac; ++k) {
+          const int r = p->fft.fac[k];
+          rest /= r;
+          q += (u % r) * rest;
+          u /= r;
+        }
+        irev[q] = t;
+      }
+      if ((s = cuda_check(cudaMalloc(&p->fft_irev, n * sizeof(int)), "cudaMalloc irev"))) return bail(s);
+      if ((s = cuda_check(cudaMemcpy(p->fft_irev, irev.data(), n * sizeof(int), cudaMemcpyHostToDevice), "irev")))
+        return bail(s);
+    }
   }
   if ((s = cuda_check(cudaMemcpy(p->tw, tw.data(), nlon * sizeof(double2), cudaMemcpyHostToDevice), "tw")))
     return bail(s);

@@ -17,6 +17,7 @@ enum { kOutGrid = 0, kOutG = 1 };
 struct RowArgs {
   int L, nlat, batch;
   FftInfo fft;
+  const int* irev;        // [n] digit-reversed position of index q (fixed-point in-place FFTs)
   const double2* tw;      // [N] exp(-2 pi i q / N)
   const double* coslat;   // [nlat] clamped cos(latitude)
   const double* fgrid;    // [nlat] synthesis of the unit (1,0) mode

@@ -6,15 +6,20 @@
 //      written by the tensor-core synthesis; each field's row is rounded to
 //      integers X at one block exponent S_f chosen from its largest element
 //      so that |X| < 2^hb, hb = min(52, 56 - ceil(log2 n));
-//   2. the half-length complex inverse FFT (Stockham, radix 4/2/3/5) runs in
+//   2. the half-length complex inverse FFT (in place, decimation in time,
+//      radix 3/5/2/4) runs in
 //      exact 64-bit additions and 31-bit-limb twiddle products -- the bound
 //      on hb keeps every butterfly below 2^59, and the error is ~2^-(hb+1) of
 //      the row's largest input (~2^-49 at n = 192);
 //   3. grid values become double-floats for the pointwise products
 //      (Pw::df_op), weighted by the quadrature weight of the row;
 //   4. each output field is aligned to its own block exponent, forward
-//      FFT'd in fixed point, and the order spectra G_m are written back as
-//      packed words for the analysis slicer.
+//      FFT'd in fixed point (in place, decimation in frequency), and the
+//      order spectra G_m are written back as packed words for the analysis
+//      slicer.
+// The in-place transforms need one row buffer per block (Stockham needs
+// two), so twice as many blocks fit an SM; the real-FFT pre- and post-
+// processing read and write the digit-reversed positions directly.
 // Lengths without a 2/3/5 FFT fall back to a direct double-float DFT.
 #pragma once
 
@@ -63,62 +68,74 @@ __device__ __forceinline__ void butterfly_fx(cfx* v, const FxConst& k) {
   }
 }
 
-// One Stockham stage.  TW = false for the first stage (Ls = 1, no
-// twiddles); later stages multiply every input, the k = 0 ones by the exact
-// unit twiddle, so the loop has no data-dependent branch.
-template <bool INV, int R, bool TW>
-__device__ __forceinline__ void fft_stage_fx(const cfx* __restrict__ src, cfx* __restrict__ dst, int nf, int n, int fs,
-                                             int Ls, unsigned nb_rcp, unsigned ls_rcp, const FxW* __restrict__ tw,
-                                             const FxConst& kc) {
+// One in-place stage over sub-transforms of length Ls -> Ls R: the
+// butterfly of (group g, offset k) owns elements g Ls R + k + t Ls, t < R.
+// DIT (inverse transforms, input in digit-reversed order): twiddles
+// w_{Ls R}^{k t} before the butterfly; DIF (forward, output digit-
+// reversed): after it.  TW = false for the stage with Ls = 1 (no twiddles).
+template <bool INV, int R, bool DIT, bool TW>
+__device__ __forceinline__ void fft_stage_ip(cfx* __restrict__ x, int nf, int n, int fs, int Ls, unsigned nb_rcp,
+                                             unsigned ls_rcp, const FxW* __restrict__ tw, const FxConst& kc) {
   const int nb = n / R, Ns = Ls * R, stride = n / Ns;
   for (int idx = threadIdx.x; idx < nf * nb; idx += blockDim.x) {
     const int f = div_rcp(idx, nb, nb_rcp), jj = idx - f * nb;
-    const int q = div_rcp(jj, Ls, ls_rcp), k = jj - q * Ls;
-    const cfx* x = src + (long)f * fs;
-    cfx* y = dst + (long)f * fs;
+    const int g = div_rcp(jj, Ls, ls_rcp), k = jj - g * Ls;
+    cfx* y = x + (long)f * fs + g * Ns + k;
     cfx v[R];
 #pragma unroll
-    for (int t = 0; t < R; ++t) v[t] = x[jj + t * nb];
-    if (TW) {
+    for (int t = 0; t < R; ++t) v[t] = y[t * Ls];
+    if (DIT && TW) {
 #pragma unroll
       for (int t = 1; t < R; ++t) v[t] = fx_cmul<INV>(v[t], fx_ldw(&tw[2 * (k * t * stride)]));
     }
     butterfly_fx<INV, R>(v, kc);
-    const int base = q * Ns + k;
+    if (!DIT && TW) {
 #pragma unroll
-    for (int t = 0; t < R; ++t) y[base + t * Ls] = v[t];
+      for (int t = 1; t < R; ++t) v[t] = fx_cmul<INV>(v[t], fx_ldw(&tw[2 * (k * t * stride)]));
+    }
+#pragma unroll
+    for (int t = 0; t < R; ++t) y[t * Ls] = v[t];
   }
 }
 
-template <bool INV>
-__device__ cfx* fft_run_fx(cfx* src, cfx* dst, int nf, int fs, const FftInfo& fi, const FxW* __restrict__ tw,
-                           const FxConst& kc) {
-  const int n = fi.n;
-  int Ls = 1;
-  for (int s = 0; s < fi.nfac; ++s) {
-    const int r = fi.fac[s];
-    if (s == 0) {
-      switch (r) {
-        case 4: fft_stage_fx<INV, 4, false>(src, dst, nf, n, fs, Ls, fi.nbm[s], fi.lsm[s], tw, kc); break;
-        case 2: fft_stage_fx<INV, 2, false>(src, dst, nf, n, fs, Ls, fi.nbm[s], fi.lsm[s], tw, kc); break;
-        case 3: fft_stage_fx<INV, 3, false>(src, dst, nf, n, fs, Ls, fi.nbm[s], fi.lsm[s], tw, kc); break;
-        default: fft_stage_fx<INV, 5, false>(src, dst, nf, n, fs, Ls, fi.nbm[s], fi.lsm[s], tw, kc); break;
-      }
-    } else {
-      switch (r) {
-        case 4: fft_stage_fx<INV, 4, true>(src, dst, nf, n, fs, Ls, fi.nbm[s], fi.lsm[s], tw, kc); break;
-        case 2: fft_stage_fx<INV, 2, true>(src, dst, nf, n, fs, Ls, fi.nbm[s], fi.lsm[s], tw, kc); break;
-        case 3: fft_stage_fx<INV, 3, true>(src, dst, nf, n, fs, Ls, fi.nbm[s], fi.lsm[s], tw, kc); break;
-        default: fft_stage_fx<INV, 5, true>(src, dst, nf, n, fs, Ls, fi.nbm[s], fi.lsm[s], tw, kc); break;
-      }
-    }
-    __syncthreads();
-    cfx* tmp = src;
-    src = dst;
-    dst = tmp;
-    Ls *= r;
+template <bool INV, bool DIT, bool TW>
+__device__ __forceinline__ void fft_stage_ip_r(int r, cfx* x, int nf, int n, int fs, int Ls, unsigned nbm,
+                                               unsigned lsm, const FxW* __restrict__ tw, const FxConst& kc) {
+  switch (r) {
+    case 4: fft_stage_ip<INV, 4, DIT, TW>(x, nf, n, fs, Ls, nbm, lsm, tw, kc); break;
+    case 2: fft_stage_ip<INV, 2, DIT, TW>(x, nf, n, fs, Ls, nbm, lsm, tw, kc); break;
+    case 3: fft_stage_ip<INV, 3, DIT, TW>(x, nf, n, fs, Ls, nbm, lsm, tw, kc); break;
+    default: fft_stage_ip<INV, 5, DIT, TW>(x, nf, n, fs, Ls, nbm, lsm, tw, kc); break;
   }
-  return src;
+}
+
+// In-place transform of nf rows (field stride fs) of length fi.n: inverse
+// by decimation in time (digit-reversed input, natural output), forward by
+// decimation in frequency (natural input, digit-reversed output).
+template <bool INV>
+__device__ void fft_ip(cfx* x, int nf, int fs, const FftInfo& fi, const FxW* __restrict__ tw, const FxConst& kc) {
+  const int n = fi.n;
+  if (INV) {
+    int Ls = 1;
+    for (int s = 0; s < fi.nfac; ++s) {
+      if (s == 0)
+        fft_stage_ip_r<INV, true, false>(fi.fac[s], x, nf, n, fs, Ls, fi.nbm[s], fi.lsm[s], tw, kc);
+      else
+        fft_stage_ip_r<INV, true, true>(fi.fac[s], x, nf, n, fs, Ls, fi.nbm[s], fi.lsm[s], tw, kc);
+      __syncthreads();
+      Ls *= fi.fac[s];
+    }
+  } else {
+    int Ls = n;
+    for (int s = fi.nfac - 1; s >= 0; --s) {
+      Ls /= fi.fac[s];
+      if (s == 0)
+        fft_stage_ip_r<INV, false, false>(fi.fac[s], x, nf, n, fs, Ls, fi.nbm[s], fi.lsm[s], tw, kc);
+      else
+        fft_stage_ip_r<INV, false, true>(fi.fac[s], x, nf, n, fs, Ls, fi.nbm[s], fi.lsm[s], tw, kc);
+      __syncthreads();
+    }
+  }
 }
 
 // X 2^S as a double-float for |X| < 2^59 (pa pb = 2^S), on the FMA/ALU
@@ -184,8 +201,8 @@ __device__ __forceinline__ void row_fx_body(const RowArgs& a, const Pw& pw, cons
   const int ns = n + 1;  // padded field stride of the smem rows (see row_body)
   const bool use_fft = a.fft.use_fft != 0;
   const int hb = min(52, 56 - (32 - __clz(max(n - 1, 1))));  // |fixed-point FFT input| < 2^hb
-  cfx* buf0 = smem_fx;
-  cfx* buf1 = smem_fx + (long)NF * ns;
+  cfx* buf0 = smem_fx;                 // the rows (all in-place FFT work)
+  cfx* buf1 = smem_fx + (long)NF * ns;  // staged spectra of the direct DFT (allocated only then)
   if (threadIdx.x == 0) s_bits = 0u;
   if (threadIdx.x < NF) {
     s_key[threadIdx.x] = 0u;
@@ -203,11 +220,11 @@ __device__ __forceinline__ void row_fx_body(const RowArgs& a, const Pw& pw, cons
     block = reinterpret_cast<float4*>(a.FG) + fg_index(b, 0, 0, j, L, a.nblk, a.nlat);
   __syncthreads();
 
-  // ---- 1. grid rows of the inputs
+  // ---- 1. grid rows of the inputs, in buf0
   // in_fx: fixed-point rows X (field stride 2 ns, value X 2^s_in[f]);
   // otherwise double-float rows.
   const bool in_fx = IN_MODE == kInF && use_fft;
-  void* xin = buf0;
+  const void* xin = buf0;
   if (IN_MODE == kInF) {
     // largest |hi| of each field's spectra (fields fastest: contiguous reads)
     for (int idx = threadIdx.x; idx < NIN * ldm; idx += blockDim.x) {
@@ -247,12 +264,12 @@ __device__ __forceinline__ void row_fx_body(const RowArgs& a, const Pw& pw, cons
         const cfx A = fx_add(hq, fx_conj(hn));
         const cfx B = fx_sub(hq, fx_conj(hn));
         const cfx P = fx_i<true>(fx_cmul<true>(B, fx_ldw(&twfx[q])));
-        cfx* z = buf0 + (long)f * ns;
-        z[q] = fx_add(A, P);
-        if (q > 0 && qn > q) z[qn] = fx_conj(fx_sub(A, P));
+        cfx* z = buf0 + (long)f * ns;  // digit-reversed positions for the in-place inverse FFT
+        z[__ldg(&a.irev[q])] = fx_add(A, P);
+        if (q > 0 && qn > q) z[__ldg(&a.irev[qn])] = fx_conj(fx_sub(A, P));
       }
       __syncthreads();
-      xin = fft_run_fx<true>(buf0, buf1, NIN, ns, a.fft, twfx, kc);
+      fft_ip<true>(buf0, NIN, ns, a.fft, twfx, kc);
     } else {
       // direct DFT in double-float: stage the spectra in buf1
       cdf* Fs = reinterpret_cast<cdf*>(buf1);
@@ -289,8 +306,10 @@ __device__ __forceinline__ void row_fx_body(const RowArgs& a, const Pw& pw, cons
     __syncthreads();
   }
 
-  // ---- 2. pointwise products (double-float), weighted by the row's quadrature weight
-  cfx* zout = (xin == static_cast<void*>(buf0)) ? buf1 : buf0;
+  // ---- 2. pointwise products (double-float), weighted by the row's quadrature
+  // weight; in place: the thread of grid point k reads every input at k before
+  // it writes the outputs there
+  cfx* zout = buf0;
   df* xout = reinterpret_cast<df*>(zout);
   {
     const RowDf rc = s_rc;
@@ -349,13 +368,12 @@ __device__ __forceinline__ void row_fx_body(const RowArgs& a, const Pw& pw, cons
       xo[o] = df_to_fx(xout[o], s_pa[f], s_pb[f]);
     }
     __syncthreads();
-    cfx* zother = (zout == buf0) ? buf1 : buf0;
-    cfx* Z = fft_run_fx<false>(zout, zother, NOUT, ns, a.fft, twfx, kc);
+    fft_ip<false>(zout, NOUT, ns, a.fft, twfx, kc);  // output in digit-reversed order
     for (int idx = threadIdx.x; idx < NOUT * ldm; idx += blockDim.x) {
       const int q = idx / NOUT, f = idx - q * NOUT;  // fields fastest: contiguous global writes
-      const cfx* Zf = Z + (long)f * ns;
-      const cfx zq = Zf[q];
-      const cfx zn = fx_conj(Zf[q == 0 ? 0 : n - q]);
+      const cfx* Zf = zout + (long)f * ns;
+      const cfx zq = Zf[__ldg(&a.irev[q])];
+      const cfx zn = fx_conj(Zf[__ldg(&a.irev[q == 0 ? 0 : n - q])]);
       const cfx E2 = fx_add(zq, zn);             // 2 E
       const cfx D = fx_sub(zq, zn);
       const cfx O2 = cfx{D.im, -D.re};           // 2 O = -i D
@@ -381,8 +399,16 @@ __device__ __forceinline__ void row_fx_body(const RowArgs& a, const Pw& pw, cons
   }
 }
 
+// Dynamic shared memory of row_kernel_fx: one row buffer for the in-place
+// FFTs, a second one for the staged spectra of the direct DFT.
+template <class Pw>
+inline size_t row_fx_smem_bytes(const FftInfo& f) {
+  constexpr int NF = Pw::NIN > Pw::NOUT ? Pw::NIN : Pw::NOUT;
+  return (size_t)(f.use_fft ? 1 : 2) * NF * (f.n + 1) * sizeof(cfx);
+}
+
 template <class Pw, int IN_MODE, int OUT_MODE>
-__global__ void __launch_bounds__(256) row_kernel_fx(RowArgs a, Pw pw, const FxW* __restrict__ twfx,
+__global__ void __launch_bounds__(256, 4) row_kernel_fx(RowArgs a, Pw pw, const FxW* __restrict__ twfx,
                                                      const float4* __restrict__ twdf, FxConst kc) {
   row_fx_body<Pw, IN_MODE, OUT_MODE>(a, pw, twfx, twdf, kc, blockIdx.x, blockIdx.y);
 }

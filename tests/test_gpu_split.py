@@ -111,3 +111,32 @@ def test_swe_autotune_is_bitwise_neutral(precision):
     assert len(out["chosen"]) == 4 and out["ms_per_step"] > 0
     after = model.rk4(y0, 300.0, 2, check=False)
     assert torch.equal(before, after)
+
+
+@pytest.mark.parametrize("nlat,nlon,L", [(96, 192, 63), (16, 1024, 15), (24, 47, 15), (192, 384, 127)])
+@pytest.mark.parametrize("scale", [1.0, 1e-20, 1e20])
+def test_split_worst_case_growth_matches_fp64(nlat, nlon, L, scale):
+    """Inputs that drive the longitude transforms to their largest growth: a
+    spectral delta (every order adds in phase at one grid point, the largest
+    value an inverse FFT can reach from its spectra) and grid rows that are
+    constant along longitude (the whole row sums into order 0), at extreme
+    magnitudes.  The fixed-point row stage picks its block exponents so that
+    no butterfly overflows; the results must stay within 1e-12 of FP64.
+    Includes a 512-point FFT and a 47-point direct DFT."""
+    p64 = Plan.gauss(nlat, nlon, L)
+    ps = Plan.gauss(nlat, nlon, L)
+    ps.set_precision(_lib.PREC_SPLIT_BF16)
+    delta = np.zeros((2, nlat * nlon))
+    delta[0, (nlat // 3) * nlon] = scale
+    delta[1, (nlat // 2) * nlon + nlon // 5] = -scale
+    a = analyze(p64.id, T(delta))
+    g64, gs = N(synthesize(p64.id, a)), N(synthesize(ps.id, a))
+    rows = np.zeros((2, nlat, nlon))
+    rows[0, nlat // 4, :] = scale
+    rows[1, :, :] = scale * np.cos(np.linspace(0.0, 3.0, nlat))[:, None]
+    rows = rows.reshape(2, -1)
+    c64, cs = N(analyze(p64.id, T(rows))), N(analyze(ps.id, T(rows)))
+    assert device_error(ps) == 0
+    for b in range(2):
+        assert rel_l2(gs[b], g64[b]) < 1e-12, (b, rel_l2(gs[b], g64[b]))
+        assert rel_l2(cs[b], c64[b]) < 1e-12, (b, rel_l2(cs[b], c64[b]))
