@@ -42,8 +42,8 @@ inline int points_analysis(const aeolus_plan_impl* p, const double* W, double* C
 
 template <int NIN, int NOUT>
 size_t full_chain_bytes(const aeolus_plan_impl* p, int batch) {
-  if (split_on(p))
-    return align256(fg_bytes(p, NIN > NOUT ? NIN : NOUT, batch)) +
+  if (split_on(p))  // F blocks, compact G blocks, slicing scratch
+    return align256(fg_bytes(p, NIN > NOUT ? NIN : NOUT, batch)) + align256(fg_bytes(p, NOUT, batch)) +
            std::max(split_synth_bytes(p, NIN, batch), split_anal_bytes(p, NOUT, batch));
   if (p->kind == kGauss) return align256(fg_bytes(p, NIN > NOUT ? NIN : NOUT, batch));
   const size_t nc = p->ncol, np = p->npoints;
@@ -77,17 +77,26 @@ int run_full_chain(const aeolus_plan_impl* p, const Derive& d, const Pw& pw, con
   if (p->kind == kGauss) {
     constexpr int NB = Pw::NIN > Pw::NOUT ? Pw::NIN : Pw::NOUT;
     double2* FG = static_cast<double2*>(work);
-    void* scratch = static_cast<char*>(work) + align256(fg_bytes(p, NB, batch));
     const bool split = split_on(p);
+    // split path: the row stage writes G into its own compact blocks (NOUT
+    // fields), so the analysis slicer reads only G; FP64 path: G overwrites
+    // the row's own F blocks
+    double2* G = split ? reinterpret_cast<double2*>(static_cast<char*>(work) + align256(fg_bytes(p, NB, batch)))
+                       : nullptr;
+    void* scratch = static_cast<char*>(work) + align256(fg_bytes(p, NB, batch)) +
+                    (split ? align256(fg_bytes(p, Pw::NOUT, batch)) : 0);
     int s = split ? launch_split_synth(p, d, FG, NB, batch, scratch, st) : launch_synth(p, d, FG, NB, batch, st);
     if (s) return s;
     RowArgs ra{};
     ra.batch = batch;
     ra.FG = FG;
     ra.nblk = NB;
+    ra.G = G;
+    ra.gblk = Pw::NOUT;
     ra.status = status;
     if ((s = launch_rows<Pw, kInF, kOutG>(p, pw, ra, st))) return s;
-    return split ? launch_split_anal(p, e, FG, NB, batch, scratch, st) : launch_analysis(p, e, FG, NB, batch, st);
+    return split ? launch_split_anal(p, e, G, Pw::NOUT, batch, scratch, st)
+                 : launch_analysis(p, e, FG, NB, batch, st);
   }
   const long nc = p->ncol, np = p->npoints;
   char* w = static_cast<char*>(work);

@@ -23,9 +23,12 @@ struct RowArgs {
   const double* fgrid;    // [nlat] synthesis of the unit (1,0) mode
   const double* wq;       // [nlat] quadrature weight of a point of row j (NULL: unit weights)
   int unit_weights;       // launch_rows: leave wq NULL (adjoint of synthesis)
-  // kInF: spectra F[b][j][nblk][L+1]; kOutG writes G into the same blocks
+  // kInF: spectra F[b][j][nblk][L+1]; kOutG writes G into the same blocks,
+  // or (fixed-point rows, G != NULL) into G with gblk fields per block
   double2* FG;
   int nblk;
+  double2* G;
+  int gblk;
   // kInGrid: grid[b * gin_b + f * gin_f + j * N + k]
   const double* gin;
   long gin_b, gin_f;

@@ -218,6 +218,10 @@ __device__ __forceinline__ void row_fx_body(const RowArgs& a, const Pw& pw, cons
   float4* block = nullptr;
   if (IN_MODE == kInF || OUT_MODE == kOutG)
     block = reinterpret_cast<float4*>(a.FG) + fg_index(b, 0, 0, j, L, a.nblk, a.nlat);
+  const long sqo = a.G ? (long)a.gblk * a.nlat : sq;  // output blocks
+  float4* oblock = nullptr;
+  if (OUT_MODE == kOutG)
+    oblock = a.G ? reinterpret_cast<float4*>(a.G) + fg_index(b, 0, 0, j, L, a.gblk, a.nlat) : block;
   __syncthreads();
 
   // ---- 1. grid rows of the inputs, in buf0
@@ -379,7 +383,7 @@ __device__ __forceinline__ void row_fx_body(const RowArgs& a, const Pw& pw, cons
       const cfx O2 = cfx{D.im, -D.re};           // 2 O = -i D
       const cfx R2 = fx_add(E2, fx_cmul<false>(O2, fx_ldw(&twfx[q])));
       const int e = s_in[f] - 1;                 // R2 / 2 in units of 2^S
-      reinterpret_cast<longlong2*>(block)[(long)q * sq + f] = make_longlong2(pk_pack(R2.re, e), pk_pack(R2.im, e));
+      reinterpret_cast<longlong2*>(oblock)[(long)q * sqo + f] = make_longlong2(pk_pack(R2.re, e), pk_pack(R2.im, e));
     }
   } else {
     for (int idx = threadIdx.x; idx < NOUT * ldm; idx += blockDim.x) {
@@ -394,7 +398,7 @@ __device__ __forceinline__ void row_fx_body(const RowArgs& a, const Pw& pw, cons
         e += q;
         while (e >= N) e -= N;
       }
-      reinterpret_cast<longlong2*>(block)[(long)q * sq + f] = make_longlong2(df_to_pk(sr), df_to_pk(si));
+      reinterpret_cast<longlong2*>(oblock)[(long)q * sqo + f] = make_longlong2(df_to_pk(sr), df_to_pk(si));
     }
   }
 }
