@@ -15,6 +15,7 @@ LIB_PATH = Path(__file__).resolve().parent / "libaeolus_gb300.so"
 
 OK, ERR_ARG, ERR_CUDA, ERR_WORKSPACE, ERR_STATE = 0, 1, 2, 3, 4
 PREC_FP64, PREC_SPLIT_BF16 = 0, 1
+TUNING_KNOBS = 5  # AEOLUS_TUNING_KNOBS
 (OP_SYNTHESIZE, OP_ANALYZE, OP_JACOBIAN, OP_WINDS, OP_BVE_TENDENCY, OP_SWE_TENDENCY,
  OP_BVE_RK4, OP_SWE_RK4, OP_SWE_VALIDATE, OP_SWE_INVARIANTS,
  OP_SYNTHESIZE_ADJOINT, OP_ANALYZE_ADJOINT, OP_BVE_TENDENCY_ADJOINT, OP_SWE_TENDENCY_ADJOINT,

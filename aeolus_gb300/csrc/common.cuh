@@ -110,8 +110,9 @@ struct aeolus_plan_impl {
   // launch shapes chosen by the autotuner (0: built-in heuristics): members
   // per CTA of the FP64 Legendre synthesis / analysis, threads of the row
   // stage, members per CTA of the split-path slicing kernels
-  int tune_bc_synth = 0, tune_bc_anal = 0, tune_row_threads = 0, tune_slice_mb = 0;
-  FftInfo fft{};
+  int tune_bc_synth = 0, tune_bc_anal = 0, tune_row_threads = 0, tune_slice_mb = 0, tune_slice_mb_anal = 0;
+  FftInfo fft{};   // FP64 row stage (radix 2..5)
+  FftInfo fftx{};  // fixed-point row stage (radix 2..5 and 8, in place)
   // device tables (Gauss)
   double* x = nullptr;       // [nlat] cos(colatitude) = sin(latitude)
   double* wq = nullptr;      // [nlat] w_gl * 2 pi / nlon
@@ -122,7 +123,7 @@ struct aeolus_plan_impl {
   double2* tw = nullptr;     // [nlon] exp(-2 pi i q / nlon)
   float4* twdf = nullptr;    // [nlon] the same twiddles as double-float (re.hi, re.lo, im.hi, im.lo)
   FxW* twfx = nullptr;       // [nlon] the same twiddles as Q61 31-bit limbs (fixed-point rows)
-  int* fft_irev = nullptr;   // [fft.n] position of natural index q in digit-reversed order (in-place FFTs)
+  int* fft_irev = nullptr;   // [fftx.n] position of natural index q in digit-reversed order (in-place FFTs)
   double* invlap = nullptr;  // [L+1] 1 / (-l(l+1)/R^2), 0 at l = 0 (radius of the plan)
   double* xa = nullptr;      // [(L+1)^2] x Y_lm = xa_lm Y_{l+1,m} + xb_lm Y_{l-1,m}
   double* xb = nullptr;      // [(L+1)^2]

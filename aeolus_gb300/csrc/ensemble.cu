@@ -237,8 +237,9 @@ int ens_stage(const aeolus_ensemble_s* E, double2* const* y0, int stage, double 
     ra.FG = reinterpret_cast<double2*>(gb[k].chain);
     ra.nblk = 4;
     row_args(p, ra);
+    if (E->split) ra.fft = p->fftx;
     grouped_add(gr, RowArg<JacPw>{ra, JacPw{}, p->twfx, p->twdf}, dim3(p->nlat, E->batch[k]));
-    sm_rows = std::max(sm_rows, E->split ? row_fx_smem_bytes<JacPw>(p->fft) : row_smem_bytes<JacPw>(p->fft));
+    sm_rows = std::max(sm_rows, E->split ? row_fx_smem_bytes<JacPw>(p->fftx) : row_smem_bytes<JacPw>(p->fft));
     row_thr = std::max(row_thr, row_threads(p));
   }
   if (!E->split) {
@@ -555,21 +556,24 @@ extern "C" int aeolus_ensemble_autotune(aeolus_ensemble e, double* const* zeta, 
         rep += line;
       }
     } else {
-      int best_v = p->tune_slice_mb;
-      float best = 1e30f;
-      for (int c : cands) {
-        p->tune_slice_mb = c;
-        float ms = 0.f;
-        if ((s = time_stage(e, y, w, st, reps, &ms))) return s;
-        if (ms < best) {
-          best = ms;
-          best_v = c;
+      for (int which = 0; which < 2; ++which) {  // synthesis, analysis slicing
+        int& knob = which == 0 ? p->tune_slice_mb : p->tune_slice_mb_anal;
+        int best_v = knob;
+        float best = 1e30f;
+        for (int c : cands) {
+          knob = c;
+          float ms = 0.f;
+          if ((s = time_stage(e, y, w, st, reps, &ms))) return s;
+          if (ms < best) {
+            best = ms;
+            best_v = c;
+          }
         }
+        knob = best_v;
+        std::snprintf(line, sizeof(line), "group %d (l_max %d, %d members): %s slicing members/CTA = %d (%.4f ms)\n",
+                      k, p->lmax, e->batch[k], which == 0 ? "synthesis" : "analysis", best_v, best);
+        rep += line;
       }
-      p->tune_slice_mb = best_v;
-      std::snprintf(line, sizeof(line), "group %d (l_max %d, %d members): slicing members/CTA = %d (%.4f ms)\n", k,
-                    p->lmax, e->batch[k], best_v, best);
-      rep += line;
     }
   }
   {

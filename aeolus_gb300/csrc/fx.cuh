@@ -43,9 +43,9 @@ struct FxW {  // complex twiddle, 16 bytes
   int ch, cl, sh, sl;
 };
 
-// Constants of the radix-3/5 butterflies.
+// Constants of the radix-3/5/8 butterflies.
 struct FxConst {
-  FxK h3, c1, c2, s1, s2;
+  FxK h3, c1, c2, s1, s2, r2;
 };
 
 // Q61 limbs of a constant |v| <= 1 v 2^61 = h 2^31 + l, l in [0, 2^31).
@@ -54,11 +54,11 @@ inline FxK fx_const(double v) {
   return FxK{static_cast<int>(W >> 31), static_cast<int>(W & 0x7FFFFFFFLL)};
 }
 
-// Radix-3/5 butterfly constants: sin(2pi/3), cos(2pi/5), cos(4pi/5), sin(2pi/5), sin(4pi/5).
+// Butterfly constants: sin(2pi/3), cos(2pi/5), cos(4pi/5), sin(2pi/5), sin(4pi/5), 1/sqrt(2).
 inline FxConst fx_consts() {
   return FxConst{fx_const(0.86602540378443864676), fx_const(0.30901699437494742410),
                  fx_const(-0.80901699437494742410), fx_const(0.95105651629515357212),
-                 fx_const(0.58778525229247312917)};
+                 fx_const(0.58778525229247312917), fx_const(0.70710678118654752440)};
 }
 
 // a b + c with a 32 x 32 -> 64-bit signed product (one wide multiply-add).

@@ -113,7 +113,8 @@ int launch_rows(const aeolus_plan_impl* p, const Pw& pw, RowArgs a, cudaStream_t
   dim3 grid(p->nlat, a.batch);
   const int threads = row_threads(p);
   if (p->precision == AEOLUS_PREC_SPLIT_BF16) {
-    const size_t sm = row_fx_smem_bytes<Pw>(p->fft);
+    a.fft = p->fftx;
+    const size_t sm = row_fx_smem_bytes<Pw>(p->fftx);
     // split-precision path: fixed-point FFTs, double-float products
     auto kern = row_kernel_fx<Pw, IN_MODE, OUT_MODE>;
     int s = allow_smem(kern, sm);

@@ -238,7 +238,7 @@ void twiddles(int N, std::vector<double2>& tw) {
   }
 }
 
-void plan_fft(int N, int L, FftInfo& f) {
+void plan_fft(int N, int L, FftInfo& f, bool radix8) {
   std::memset(&f, 0, sizeof(f));
   f.N = N;
   f.n = (N + 1) / 2;
@@ -246,16 +246,19 @@ void plan_fft(int N, int L, FftInfo& f) {
   if (N % 2 != 0) return;
   int n = N / 2;
   if (L > n - 1) return;  // Nyquist / aliased orders: direct DFT handles them
-  // Radix order: odd radices first, then 2, then 4s.  A stage with
-  // sub-transform length 1 touches shared memory at a stride of its radix,
-  // which is free of bank conflicts for an odd radix.
+  // Radix order: odd radices first, then 2 or 4, then 4s (or 8s with
+  // radix8).  A stage with sub-transform length 1 touches shared memory at a
+  // stride of its radix, which is free of bank conflicts for an odd radix.
   int rem = n, nf = 0, fac[kMaxFactors];
-  int c4 = 0;
-  while (rem % 4 == 0) { ++c4; rem /= 4; }
-  const int radices[3] = {3, 5, 2};
-  for (int r : radices)
+  int c2 = 0;
+  while (rem % 2 == 0) { ++c2; rem /= 2; }
+  const int odd[2] = {3, 5};
+  for (int r : odd)
     while (rem % r == 0 && nf < kMaxFactors) { fac[nf++] = r; rem /= r; }
-  for (int i = 0; i < c4 && nf < kMaxFactors; ++i) fac[nf++] = 4;
+  const int big = radix8 ? 3 : 2;  // log2 of the main power-of-two radix
+  const int lead = c2 % big;        // leading radix 2 or 4
+  if (lead > 0 && nf < kMaxFactors) fac[nf++] = 1 << lead;
+  for (int i = 0; i < c2 / big && nf < kMaxFactors; ++i) fac[nf++] = 1 << big;
   if (rem != 1 || nf == kMaxFactors || n > kMaxFftHalf) return;
   f.use_fft = 1;
   f.n = n;
@@ -436,7 +439,8 @@ extern "C" int aeolus_plan_create_gauss(int nlat, int nlon, int lmax, double rad
   p->radius = radius;
   cudaGetDevice(&p->device);
   cudaDeviceGetAttribute(&p->sm_count, cudaDevAttrMultiProcessorCount, p->device);
-  plan_fft(nlon, lmax, p->fft);
+  plan_fft(nlon, lmax, p->fft, false);
+  plan_fft(nlon, lmax, p->fftx, true);
   int s = AEOLUS_OK;
   auto bail = [&](int st) { free_plan(p); delete p; return st; };
   const int L = lmax, nh = p->nh;
@@ -493,15 +497,15 @@ extern "C" int aeolus_plan_create_gauss(int nlat, int nlon, int lmax, double rad
     if ((s = cuda_check(cudaMalloc(&p->twfx, nlon * sizeof(FxW)), "cudaMalloc twfx"))) return bail(s);
     if ((s = cuda_check(cudaMemcpy(p->twfx, twx.data(), nlon * sizeof(FxW), cudaMemcpyHostToDevice), "twfx")))
       return bail(s);
-    if (p->fft.use_fft) {
+    if (p->fftx.use_fft) {
       // digit reversal of the in-place transforms: position t = t0 + R0 (t1 + R1 (...))
       // holds natural index t0 n/R0 + t1 n/(R0 R1) + ...
-      const int n = p->fft.n;
+      const int n = p->fftx.n;
       std::vector<int> irev(n);
       for (int t = 0; t < n; ++t) {
         int rest = n, q = 0, u = t;
-        for (int k = 0; k < p->fft.nfac; ++k) {
-          const int r = p->fft.fac[k];
+        for (int k = 0; k < p->fftx.nfac; ++k) {
+          const int r = p->fftx.fac[k];
           rest /= r;
           q += (u % r) * rest;
           u /= r;

@@ -7,7 +7,7 @@
 //      integers X at one block exponent S_f chosen from its largest element
 //      so that |X| < 2^hb, hb = min(52, 56 - ceil(log2 n));
 //   2. the half-length complex inverse FFT (in place, decimation in time,
-//      radix 3/5/2/4) runs in
+//      radix 3/5, then 2/4, then 8) runs in
 //      exact 64-bit additions and 31-bit-limb twiddle products -- the bound
 //      on hb keeps every butterfly below 2^59, and the error is ~2^-(hb+1) of
 //      the row's largest input (~2^-49 at n = 192);
@@ -50,6 +50,28 @@ __device__ __forceinline__ void butterfly_fx(cfx* v, const FxConst& k) {
     v[0] = fx_add(v[0], s);
     v[1] = fx_add(t, id);
     v[2] = fx_sub(t, id);
+  } else if constexpr (R == 8) {
+    // radix-4 transforms of the even and odd inputs, combined with w8^t
+    cfx e[4] = {v[0], v[2], v[4], v[6]}, o[4] = {v[1], v[3], v[5], v[7]};
+    butterfly_fx<INV, 4>(e, k);
+    butterfly_fx<INV, 4>(o, k);
+    {  // o1 *= (1 +- i)/sqrt2, o3 *= (-1 +- i)/sqrt2 (+: inverse), o2 *= +-i
+      const long long s1 = o[1].re + o[1].im, d1 = o[1].re - o[1].im;
+      const long long s3 = o[3].re + o[3].im, d3 = o[3].re - o[3].im;
+      if (INV) {
+        o[1] = cfx{fx_mulk(d1, k.r2), fx_mulk(s1, k.r2)};
+        o[3] = cfx{-fx_mulk(s3, k.r2), fx_mulk(d3, k.r2)};
+      } else {
+        o[1] = cfx{fx_mulk(s1, k.r2), -fx_mulk(d1, k.r2)};
+        o[3] = cfx{-fx_mulk(d3, k.r2), -fx_mulk(s3, k.r2)};
+      }
+      o[2] = fx_i<INV>(o[2]);
+    }
+#pragma unroll
+    for (int t = 0; t < 4; ++t) {
+      v[t] = fx_add(e[t], o[t]);
+      v[t + 4] = fx_sub(e[t], o[t]);
+    }
   } else {  // R == 5
     const cfx a1 = fx_add(v[1], v[4]), a2 = fx_add(v[2], v[3]);
     const cfx b1 = fx_sub(v[1], v[4]), b2 = fx_sub(v[2], v[3]);
@@ -102,6 +124,7 @@ template <bool INV, bool DIT, bool TW>
 __device__ __forceinline__ void fft_stage_ip_r(int r, cfx* x, int nf, int n, int fs, int Ls, unsigned nbm,
                                                unsigned lsm, const FxW* __restrict__ tw, const FxConst& kc) {
   switch (r) {
+    case 8: fft_stage_ip<INV, 8, DIT, TW>(x, nf, n, fs, Ls, nbm, lsm, tw, kc); break;
     case 4: fft_stage_ip<INV, 4, DIT, TW>(x, nf, n, fs, Ls, nbm, lsm, tw, kc); break;
     case 2: fft_stage_ip<INV, 2, DIT, TW>(x, nf, n, fs, Ls, nbm, lsm, tw, kc); break;
     case 3: fft_stage_ip<INV, 3, DIT, TW>(x, nf, n, fs, Ls, nbm, lsm, tw, kc); break;

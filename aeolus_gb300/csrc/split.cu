@@ -258,7 +258,8 @@ extern "C" int aeolus_plan_set_precision(aeolus_plan plan, int precision, int sl
 
 extern "C" int aeolus_plan_set_tuning(aeolus_plan plan, const int* knobs) {
   if (!plan_ok(plan) || !knobs) return fail(AEOLUS_ERR_ARG, "aeolus_plan_set_tuning: bad arguments");
-  if (knobs[0] < 0 || knobs[1] < 0 || knobs[3] < 0 || knobs[0] > 64 || knobs[1] > 64 || knobs[3] > 64)
+  if (knobs[0] < 0 || knobs[1] < 0 || knobs[3] < 0 || knobs[4] < 0 || knobs[0] > 64 || knobs[1] > 64 ||
+      knobs[3] > 64 || knobs[4] > 64)
     return fail(AEOLUS_ERR_ARG, "aeolus_plan_set_tuning: members per CTA must be in 0..64");
   if (knobs[2] != 0 && (knobs[2] < 64 || knobs[2] > 256 || knobs[2] % 32 != 0))
     return fail(AEOLUS_ERR_ARG, "aeolus_plan_set_tuning: row threads must be 0 or a multiple of 32 in 64..256");
@@ -266,6 +267,7 @@ extern "C" int aeolus_plan_set_tuning(aeolus_plan plan, const int* knobs) {
   plan->tune_bc_anal = knobs[1];
   plan->tune_row_threads = knobs[2];
   plan->tune_slice_mb = knobs[3];
+  plan->tune_slice_mb_anal = knobs[4];
   return AEOLUS_OK;
 }
 
@@ -275,5 +277,6 @@ extern "C" int aeolus_plan_get_tuning(aeolus_plan plan, int* knobs) {
   knobs[1] = plan->tune_bc_anal;
   knobs[2] = plan->tune_row_threads;
   knobs[3] = plan->tune_slice_mb;
+  knobs[4] = plan->tune_slice_mb_anal;
   return AEOLUS_OK;
 }

@@ -780,7 +780,7 @@ SplitParts split_anal_parts(const aeolus_plan_impl* p, int batch, void* scratch)
   r.digits = reinterpret_cast<__nv_bfloat16*>(w);
   w += align256((size_t)(r.dm.L + 1) * r.dm.ntiles * kSlices * kNT * r.dm.NK * 2);
   r.ecol = reinterpret_cast<int*>(w);
-  r.mb = slice_members(NF, r.dm.nlat, p->tune_slice_mb);
+  r.mb = slice_members(NF, r.dm.nlat, p->tune_slice_mb_anal);
   r.smem = (size_t)r.mb * NF * 2 * r.dm.nlat * 8;
   r.grid = dim3(r.dm.L + 1, (batch + r.mb - 1) / r.mb);
   return r;

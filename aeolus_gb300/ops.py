@@ -16,7 +16,7 @@ import numpy as np
 import torch
 
 from . import _lib
-from ._lib import check
+from ._lib import TUNING_KNOBS, check
 
 _PLANS: dict[int, "Plan"] = {}
 _LOCK = threading.Lock()
@@ -86,14 +86,17 @@ class Plan:
         check(_lib.load().aeolus_plan_set_precision(self.handle, int(precision), int(slices)))
         self.precision = int(precision)
 
-    def tuning(self) -> tuple[int, int, int, int]:
-        """(bc_synth, bc_anal, row_threads, slice_members); 0 = heuristic."""
-        k = (c_int * 4)()
+    def tuning(self) -> tuple[int, int, int, int, int]:
+        """(bc_synth, bc_anal, row_threads, synth_slice_members,
+        anal_slice_members); 0 = heuristic."""
+        k = (c_int * TUNING_KNOBS)()
         check(_lib.load().aeolus_plan_get_tuning(self.handle, k))
         return tuple(k)
 
     def set_tuning(self, knobs) -> None:
-        k = (c_int * 4)(*[int(x) for x in knobs])
+        if len(knobs) != TUNING_KNOBS:
+            raise ValueError(f"set_tuning takes {TUNING_KNOBS} knobs")
+        k = (c_int * TUNING_KNOBS)(*[int(x) for x in knobs])
         check(_lib.load().aeolus_plan_set_tuning(self.handle, k))
 
     def workspace(self, op: int, batch: int) -> torch.Tensor:

@@ -146,8 +146,10 @@ class ShallowWaterModel:
         best_ms = time_knobs(best)
         results[tuple(best)] = best_ms
         B = coeffs.reshape(-1, 3, self.l_max + 1, self.l_max + 1).shape[0]
-        # knob 2: row-stage threads; 0/1: FP64 Legendre members per CTA; 3: split slicing members per CTA
-        choices = [(2, (128, 192, 256))] + ([(3, (1, 2, 4, 8))] if split else [(0, (1, 2, 3, 4)), (1, (1, 2, 3, 4))])
+        # knob 2: row-stage threads; 0/1: FP64 Legendre members per CTA;
+        # 3/4: split synthesis / analysis slicing members per CTA
+        choices = [(2, (128, 192, 256))] + ([(3, (1, 2, 4, 8)), (4, (1, 2, 4, 8))] if split
+                                            else [(0, (1, 2, 3, 4)), (1, (1, 2, 3, 4))])
         for idx, cands in choices:
             for c in cands:
                 if idx != 2 and c > B:

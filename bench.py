@@ -550,7 +550,7 @@ def main():
             for _ in range(warm):
                 y = m.rk4(y, DT, 1, check=False)
             tuned = m.autotune(y0, DT)   # launch shapes for this batch; results do not depend on them
-            tuning[name] = {"knobs_bc_synth_bc_anal_row_threads_slice_mb": list(tuned["chosen"]),
+            tuning[name] = {"knobs_bc_synth_bc_anal_row_threads_slice_synth_anal": list(tuned["chosen"]),
                             "ms_per_step": tuned["ms_per_step"]}
     barrier()
 

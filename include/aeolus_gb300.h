@@ -142,11 +142,14 @@ int aeolus_plan_set_precision(aeolus_plan plan, int precision, int slices);
  * counterpart (the reference has no device-side waits). */
 int aeolus_plan_device_error(aeolus_plan plan, int* flag);
 
-/* Launch shapes of the plan's kernels (no reference counterpart): knobs[0]
- * members per CTA of the FP64 Legendre synthesis, knobs[1] of the analysis,
- * knobs[2] threads per CTA of the longitude (row) stage, knobs[3] members per
- * CTA of the split-precision slicing kernels; 0 = built-in heuristic.
- * Results do not depend on these shapes (the autotuners set them). */
+/* Launch shapes of the plan's kernels (no reference counterpart), an array
+ * of AEOLUS_TUNING_KNOBS ints: knobs[0] members per CTA of the FP64 Legendre
+ * synthesis, knobs[1] of the analysis, knobs[2] threads per CTA of the
+ * longitude (row) stage, knobs[3] members per CTA of the split-precision
+ * synthesis slicing kernel, knobs[4] of the analysis slicing kernel;
+ * 0 = built-in heuristic.  Results do not depend on these shapes (the
+ * autotuners set them). */
+#define AEOLUS_TUNING_KNOBS 5
 int aeolus_plan_set_tuning(aeolus_plan plan, const int* knobs);
 int aeolus_plan_get_tuning(aeolus_plan plan, int* knobs);
 

@@ -108,7 +108,7 @@ def test_swe_autotune_is_bitwise_neutral(precision):
     y0 = torch.as_tensor(s, device="cuda")
     before = model.rk4(y0, 300.0, 2, check=False)
     out = model.autotune(y0, 300.0, reps=1)
-    assert len(out["chosen"]) == 4 and out["ms_per_step"] > 0
+    assert len(out["chosen"]) == 5 and out["ms_per_step"] > 0
     after = model.rk4(y0, 300.0, 2, check=False)
     assert torch.equal(before, after)
 
