@@ -29,6 +29,50 @@
 
 namespace aeolus {
 
+// X 2^S as a double-float for |X| < 2^59 (pa pb = 2^S), on the FMA/ALU
+// pipes: X = c2 2^40 + c1 2^20 + c0 with 20-bit limbs, each limb made exact
+// by the magic-number construction (the limb placed in the mantissa of a
+// float of known exponent, that float's offset subtracted), then summed
+// with error-free transformations.
+__device__ __forceinline__ df fx_to_df(long long X, float pa, float pb) {
+  const unsigned lo = static_cast<unsigned>(X), hi = static_cast<unsigned>(X >> 32);
+  const unsigned c0 = lo & 0xFFFFFu;
+  const unsigned c1 = __funnelshift_r(lo, hi, 20) & 0xFFFFFu;
+  const int c2 = static_cast<int>(X >> 40);
+  const float f0 = __int_as_float(0x4B000000 | c0) - 8388608.0f;                    // c0
+  const float f1 = __int_as_float((170u << 23) | c1) - 8796093022208.0f;            // c1 2^20
+  const float f2 = __int_as_float((190 << 23) + 0x400000 + c2) - 13835058055282163712.0f;  // c2 2^40
+  const float s = f2 + f1;
+  const float e1 = f1 - (s - f2);  // exact: |f2| >= |f1| or f2 = 0
+  const float t = e1 + f0;
+  const float h = s + t;
+  const float l = t - (h - s);
+  return df{h * pa * pb, l * pa * pb};
+}
+
+// rint(v 2^-S) for pa pb = 2^-S and |v 2^-S| < 2^52: the high word splits
+// into u 2^30 + r (u by the magic-number rounding, r exact by FMA), r and
+// the low word are rounded by 32-bit conversions.
+__device__ __forceinline__ long long df_to_fx(df v, float pa, float pb) {
+  const float th = v.hi * pa * pb, tl = v.lo * pa * pb;
+  const float um = fmaf(th, 9.31322574615478515625e-10f, 12582912.0f);  // th 2^-30 + 1.5 2^23
+  const int u = __float_as_int(um) - 0x4B400000;
+  const float r = fmaf(-(um - 12582912.0f), 1073741824.0f, th);
+  const int rl = __float2int_rn(r) + __float2int_rn(tl);
+  return fx_madw(u, 1 << 30, static_cast<long long>(rl));
+}
+// Exponent E with |x| < 2^E for every float whose |bits| <= key.
+__device__ __forceinline__ int fkey_exp(unsigned key) { return static_cast<int>(key >> 23) - 126; }
+// A double-float as a packed word (52-bit mantissa).
+__device__ __forceinline__ long long df_to_pk(df v) {
+  const unsigned key = __float_as_uint(v.hi) & 0x7FFFFFFFu;
+  if ((key >> 23) == 0) return 0;
+  const int S = fkey_exp(key) - kPackMant;
+  float pa, pb;
+  fx_pow2_split(-S, pa, pb);
+  return pk_pack(df_to_fx(v, pa, pb), S);
+}
+
 template <bool INV, int R>
 __device__ __forceinline__ void butterfly_fx(cfx* v, const FxConst& k) {
   if constexpr (R == 2) {
@@ -95,17 +139,30 @@ __device__ __forceinline__ void butterfly_fx(cfx* v, const FxConst& k) {
 // DIT (inverse transforms, input in digit-reversed order): twiddles
 // w_{Ls R}^{k t} before the butterfly; DIF (forward, output digit-
 // reversed): after it.  TW = false for the stage with Ls = 1 (no twiddles).
-template <bool INV, int R, bool DIT, bool TW>
+// CONV: the rows still hold double-float reals (two per complex slot); they
+// are rounded to the fixed-point block exponent of their field (scale
+// factors pa pb = 2^-S) as they are loaded.
+template <bool INV, int R, bool DIT, bool TW, bool CONV>
 __device__ __forceinline__ void fft_stage_ip(cfx* __restrict__ x, int nf, int n, int fs, int Ls, unsigned nb_rcp,
-                                             unsigned ls_rcp, const FxW* __restrict__ tw, const FxConst& kc) {
+                                             unsigned ls_rcp, const FxW* __restrict__ tw, const FxConst& kc,
+                                             const float* sqa, const float* sqb) {
   const int nb = n / R, Ns = Ls * R, stride = n / Ns;
   for (int idx = threadIdx.x; idx < nf * nb; idx += blockDim.x) {
     const int f = div_rcp(idx, nb, nb_rcp), jj = idx - f * nb;
     const int g = div_rcp(jj, Ls, ls_rcp), k = jj - g * Ls;
     cfx* y = x + (long)f * fs + g * Ns + k;
     cfx v[R];
+    if (CONV) {
+      const float pa = sqa[f], pb = sqb[f];
 #pragma unroll
-    for (int t = 0; t < R; ++t) v[t] = y[t * Ls];
+      for (int t = 0; t < R; ++t) {
+        const float4 w = reinterpret_cast<const float4*>(y)[t * Ls];
+        v[t] = cfx{df_to_fx(df{w.x, w.y}, pa, pb), df_to_fx(df{w.z, w.w}, pa, pb)};
+      }
+    } else {
+#pragma unroll
+      for (int t = 0; t < R; ++t) v[t] = y[t * Ls];
+    }
     if (DIT && TW) {
 #pragma unroll
       for (int t = 1; t < R; ++t) v[t] = fx_cmul<INV>(v[t], fx_ldw(&tw[2 * (k * t * stride)]));
@@ -120,31 +177,34 @@ __device__ __forceinline__ void fft_stage_ip(cfx* __restrict__ x, int nf, int n,
   }
 }
 
-template <bool INV, bool DIT, bool TW>
+template <bool INV, bool DIT, bool TW, bool CONV>
 __device__ __forceinline__ void fft_stage_ip_r(int r, cfx* x, int nf, int n, int fs, int Ls, unsigned nbm,
-                                               unsigned lsm, const FxW* __restrict__ tw, const FxConst& kc) {
+                                               unsigned lsm, const FxW* __restrict__ tw, const FxConst& kc,
+                                               const float* sqa, const float* sqb) {
   switch (r) {
-    case 8: fft_stage_ip<INV, 8, DIT, TW>(x, nf, n, fs, Ls, nbm, lsm, tw, kc); break;
-    case 4: fft_stage_ip<INV, 4, DIT, TW>(x, nf, n, fs, Ls, nbm, lsm, tw, kc); break;
-    case 2: fft_stage_ip<INV, 2, DIT, TW>(x, nf, n, fs, Ls, nbm, lsm, tw, kc); break;
-    case 3: fft_stage_ip<INV, 3, DIT, TW>(x, nf, n, fs, Ls, nbm, lsm, tw, kc); break;
-    default: fft_stage_ip<INV, 5, DIT, TW>(x, nf, n, fs, Ls, nbm, lsm, tw, kc); break;
+    case 8: fft_stage_ip<INV, 8, DIT, TW, CONV>(x, nf, n, fs, Ls, nbm, lsm, tw, kc, sqa, sqb); break;
+    case 4: fft_stage_ip<INV, 4, DIT, TW, CONV>(x, nf, n, fs, Ls, nbm, lsm, tw, kc, sqa, sqb); break;
+    case 2: fft_stage_ip<INV, 2, DIT, TW, CONV>(x, nf, n, fs, Ls, nbm, lsm, tw, kc, sqa, sqb); break;
+    case 3: fft_stage_ip<INV, 3, DIT, TW, CONV>(x, nf, n, fs, Ls, nbm, lsm, tw, kc, sqa, sqb); break;
+    default: fft_stage_ip<INV, 5, DIT, TW, CONV>(x, nf, n, fs, Ls, nbm, lsm, tw, kc, sqa, sqb); break;
   }
 }
 
 // In-place transform of nf rows (field stride fs) of length fi.n: inverse
 // by decimation in time (digit-reversed input, natural output), forward by
-// decimation in frequency (natural input, digit-reversed output).
+// decimation in frequency (natural input, digit-reversed output; with sqa,
+// the input rows are double-floats converted by the first stage).
 template <bool INV>
-__device__ void fft_ip(cfx* x, int nf, int fs, const FftInfo& fi, const FxW* __restrict__ tw, const FxConst& kc) {
+__device__ void fft_ip(cfx* x, int nf, int fs, const FftInfo& fi, const FxW* __restrict__ tw, const FxConst& kc,
+                       const float* sqa = nullptr, const float* sqb = nullptr) {
   const int n = fi.n;
   if (INV) {
     int Ls = 1;
     for (int s = 0; s < fi.nfac; ++s) {
       if (s == 0)
-        fft_stage_ip_r<INV, true, false>(fi.fac[s], x, nf, n, fs, Ls, fi.nbm[s], fi.lsm[s], tw, kc);
+        fft_stage_ip_r<INV, true, false, false>(fi.fac[s], x, nf, n, fs, Ls, fi.nbm[s], fi.lsm[s], tw, kc, sqa, sqb);
       else
-        fft_stage_ip_r<INV, true, true>(fi.fac[s], x, nf, n, fs, Ls, fi.nbm[s], fi.lsm[s], tw, kc);
+        fft_stage_ip_r<INV, true, true, false>(fi.fac[s], x, nf, n, fs, Ls, fi.nbm[s], fi.lsm[s], tw, kc, sqa, sqb);
       __syncthreads();
       Ls *= fi.fac[s];
     }
@@ -152,57 +212,21 @@ __device__ void fft_ip(cfx* x, int nf, int fs, const FftInfo& fi, const FxW* __r
     int Ls = n;
     for (int s = fi.nfac - 1; s >= 0; --s) {
       Ls /= fi.fac[s];
-      if (s == 0)
-        fft_stage_ip_r<INV, false, false>(fi.fac[s], x, nf, n, fs, Ls, fi.nbm[s], fi.lsm[s], tw, kc);
-      else
-        fft_stage_ip_r<INV, false, true>(fi.fac[s], x, nf, n, fs, Ls, fi.nbm[s], fi.lsm[s], tw, kc);
+      const bool conv = sqa && s == fi.nfac - 1;
+      if (s == 0) {
+        if (conv)
+          fft_stage_ip_r<INV, false, false, true>(fi.fac[s], x, nf, n, fs, Ls, fi.nbm[s], fi.lsm[s], tw, kc, sqa, sqb);
+        else
+          fft_stage_ip_r<INV, false, false, false>(fi.fac[s], x, nf, n, fs, Ls, fi.nbm[s], fi.lsm[s], tw, kc, sqa, sqb);
+      } else {
+        if (conv)
+          fft_stage_ip_r<INV, false, true, true>(fi.fac[s], x, nf, n, fs, Ls, fi.nbm[s], fi.lsm[s], tw, kc, sqa, sqb);
+        else
+          fft_stage_ip_r<INV, false, true, false>(fi.fac[s], x, nf, n, fs, Ls, fi.nbm[s], fi.lsm[s], tw, kc, sqa, sqb);
+      }
       __syncthreads();
     }
   }
-}
-
-// X 2^S as a double-float for |X| < 2^59 (pa pb = 2^S), on the FMA/ALU
-// pipes: X = c2 2^40 + c1 2^20 + c0 with 20-bit limbs, each limb made exact
-// by the magic-number construction (the limb placed in the mantissa of a
-// float of known exponent, that float's offset subtracted), then summed
-// with error-free transformations.
-__device__ __forceinline__ df fx_to_df(long long X, float pa, float pb) {
-  const unsigned lo = static_cast<unsigned>(X), hi = static_cast<unsigned>(X >> 32);
-  const unsigned c0 = lo & 0xFFFFFu;
-  const unsigned c1 = __funnelshift_r(lo, hi, 20) & 0xFFFFFu;
-  const int c2 = static_cast<int>(X >> 40);
-  const float f0 = __int_as_float(0x4B000000 | c0) - 8388608.0f;                    // c0
-  const float f1 = __int_as_float((170u << 23) | c1) - 8796093022208.0f;            // c1 2^20
-  const float f2 = __int_as_float((190 << 23) + 0x400000 + c2) - 13835058055282163712.0f;  // c2 2^40
-  const float s = f2 + f1;
-  const float e1 = f1 - (s - f2);  // exact: |f2| >= |f1| or f2 = 0
-  const float t = e1 + f0;
-  const float h = s + t;
-  const float l = t - (h - s);
-  return df{h * pa * pb, l * pa * pb};
-}
-
-// rint(v 2^-S) for pa pb = 2^-S and |v 2^-S| < 2^52: the high word splits
-// into u 2^30 + r (u by the magic-number rounding, r exact by FMA), r and
-// the low word are rounded by 32-bit conversions.
-__device__ __forceinline__ long long df_to_fx(df v, float pa, float pb) {
-  const float th = v.hi * pa * pb, tl = v.lo * pa * pb;
-  const float um = fmaf(th, 9.31322574615478515625e-10f, 12582912.0f);  // th 2^-30 + 1.5 2^23
-  const int u = __float_as_int(um) - 0x4B400000;
-  const float r = fmaf(-(um - 12582912.0f), 1073741824.0f, th);
-  const int rl = __float2int_rn(r) + __float2int_rn(tl);
-  return fx_madw(u, 1 << 30, static_cast<long long>(rl));
-}
-// Exponent E with |x| < 2^E for every float whose |bits| <= key.
-__device__ __forceinline__ int fkey_exp(unsigned key) { return static_cast<int>(key >> 23) - 126; }
-// A double-float as a packed word (52-bit mantissa).
-__device__ __forceinline__ long long df_to_pk(df v) {
-  const unsigned key = __float_as_uint(v.hi) & 0x7FFFFFFFu;
-  if ((key >> 23) == 0) return 0;
-  const int S = fkey_exp(key) - kPackMant;
-  float pa, pb;
-  fx_pow2_split(-S, pa, pb);
-  return pk_pack(df_to_fx(v, pa, pb), S);
 }
 
 template <class Pw, int IN_MODE, int OUT_MODE>
@@ -380,7 +404,7 @@ __device__ __forceinline__ void row_fx_body(const RowArgs& a, const Pw& pw, cons
       a.gout[(long)b * a.gout_b + (long)f * a.gout_f + (long)j * N + k] = df_to_double(xout[(long)f * 2 * ns + k]);
     }
   } else if (use_fft) {
-    // output block exponents (|X| < 2^hb), rows to fixed point in place
+    // output block exponents (|X| < 2^hb)
     if (threadIdx.x < NOUT) {
       const unsigned key = s_omax[threadIdx.x];
       const int S = (key >> 23) == 0 ? 0 : fkey_exp(key) - hb;
@@ -388,14 +412,8 @@ __device__ __forceinline__ void row_fx_body(const RowArgs& a, const Pw& pw, cons
       fx_pow2_split(-S, s_pa[threadIdx.x], s_pb[threadIdx.x]);
     }
     __syncthreads();
-    long long* xo = reinterpret_cast<long long*>(zout);
-    for (int idx = threadIdx.x; idx < NOUT * N; idx += blockDim.x) {
-      const int f = idx / N, k = idx - f * N;
-      const long o = (long)f * 2 * ns + k;
-      xo[o] = df_to_fx(xout[o], s_pa[f], s_pb[f]);
-    }
-    __syncthreads();
-    fft_ip<false>(zout, NOUT, ns, a.fft, twfx, kc);  // output in digit-reversed order
+    // rows to fixed point inside the first stage; output in digit-reversed order
+    fft_ip<false>(zout, NOUT, ns, a.fft, twfx, kc, s_pa, s_pb);
     for (int idx = threadIdx.x; idx < NOUT * ldm; idx += blockDim.x) {
       const int q = idx / NOUT, f = idx - q * NOUT;  // fields fastest: contiguous global writes
       const cfx* Zf = zout + (long)f * ns;

@@ -252,7 +252,7 @@ __device__ __forceinline__ void split_synth_slice_body(const SplitDims& dm, cons
 }
 
 template <class Derive>
-__global__ void __launch_bounds__(256) split_synth_slice_kernel(SplitDims dm, const long long* __restrict__ kcum,
+__global__ void __launch_bounds__(256, 3) split_synth_slice_kernel(SplitDims dm, const long long* __restrict__ kcum,
                                                                int batch, int mb, Derive der,
                                                                __nv_bfloat16* __restrict__ dsyn,
                                                                int* __restrict__ ecol) {
