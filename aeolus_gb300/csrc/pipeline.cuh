@@ -107,23 +107,35 @@ inline void row_args(const aeolus_plan_impl* p, RowArgs& a) {
   a.wq = a.unit_weights ? nullptr : p->wq;
 }
 
+template <class Pw, int IN_MODE, int OUT_MODE, class FFT>
+int launch_rows_fx(const aeolus_plan_impl* p, const Pw& pw, const RowArgs& a, cudaStream_t st) {
+  const size_t sm = row_fx_smem_bytes<Pw>(p->fftx);
+  auto kern = row_kernel_fx<Pw, IN_MODE, OUT_MODE, FFT>;
+  int s = allow_smem(kern, sm);
+  if (s) return s;
+  ProfScope prof(IN_MODE == kInF ? (OUT_MODE == kOutG ? "rows_fx_c2r_products_r2c" : "rows_fx_c2r") : "rows_fx_r2c",
+                 st);
+  kern<<<dim3(p->nlat, a.batch), row_threads(p), sm, st>>>(a, pw, p->twfx, p->twdf, fx_consts());
+  AE_LAUNCH("row_kernel_fx");
+  return AEOLUS_OK;
+}
+
 template <class Pw, int IN_MODE, int OUT_MODE>
 int launch_rows(const aeolus_plan_impl* p, const Pw& pw, RowArgs a, cudaStream_t st) {
   row_args(p, a);
   dim3 grid(p->nlat, a.batch);
   const int threads = row_threads(p);
   if (p->precision == AEOLUS_PREC_SPLIT_BF16) {
+    // split-precision path: fixed-point FFTs, double-float products; the
+    // model chains get kernels compiled for the common radix sequences
     a.fft = p->fftx;
-    const size_t sm = row_fx_smem_bytes<Pw>(p->fftx);
-    // split-precision path: fixed-point FFTs, double-float products
-    auto kern = row_kernel_fx<Pw, IN_MODE, OUT_MODE>;
-    int s = allow_smem(kern, sm);
-    if (s) return s;
-    ProfScope prof(IN_MODE == kInF ? (OUT_MODE == kOutG ? "rows_fx_c2r_products_r2c" : "rows_fx_c2r") : "rows_fx_r2c",
-                   st);
-    kern<<<grid, threads, sm, st>>>(a, pw, p->twfx, p->twdf, fx_consts());
-    AE_LAUNCH("row_kernel_fx");
-    return AEOLUS_OK;
+    if constexpr (IN_MODE == kInF && OUT_MODE == kOutG) {
+      using F388 = FftFixed<3, 8, 8>;  // nlon 384
+      using F288 = FftFixed<2, 8, 8>;  // nlon 256
+      if (F388::matches(p->fftx)) return launch_rows_fx<Pw, IN_MODE, OUT_MODE, F388>(p, pw, a, st);
+      if (F288::matches(p->fftx)) return launch_rows_fx<Pw, IN_MODE, OUT_MODE, F288>(p, pw, a, st);
+    }
+    return launch_rows_fx<Pw, IN_MODE, OUT_MODE, FftRuntime>(p, pw, a, st);
   }
   const size_t sm = row_smem_bytes<Pw>(p->fft);
   auto kern = row_kernel<Pw, IN_MODE, OUT_MODE>;

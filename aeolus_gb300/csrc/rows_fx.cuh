@@ -229,7 +229,71 @@ __device__ void fft_ip(cfx* x, int nf, int fs, const FftInfo& fi, const FxW* __r
   }
 }
 
-template <class Pw, int IN_MODE, int OUT_MODE>
+// FFT policies of the row body.  FftRuntime dispatches every stage on the
+// plan's radix at run time (all radix bodies are compiled in); FftFixed
+// compiles exactly the plan's radix sequence, which keeps the kernel small
+// enough for the instruction caches.  The host picks FftFixed when the
+// plan's factors match.
+struct FftRuntime {
+  template <bool INV>
+  static __device__ __forceinline__ void run(cfx* x, int nf, int fs, const FftInfo& fi, const FxW* __restrict__ tw,
+                                             const FxConst& kc, const float* sqa = nullptr,
+                                             const float* sqb = nullptr) {
+    fft_ip<INV>(x, nf, fs, fi, tw, kc, sqa, sqb);
+  }
+};
+
+template <int... Rs>
+struct FftFixed {
+  static constexpr int S = sizeof...(Rs);
+  static __host__ __device__ constexpr int radix(int s) {
+    constexpr int f[S] = {Rs...};
+    return f[s];
+  }
+  static bool matches(const FftInfo& fi) {
+    if (!fi.use_fft || fi.nfac != S) return false;
+    for (int s = 0; s < S; ++s)
+      if (fi.fac[s] != radix(s)) return false;
+    return true;
+  }
+  template <bool INV, int s>
+  static __device__ __forceinline__ void dit(cfx* x, int nf, int n, int fs, int Ls, const FftInfo& fi,
+                                             const FxW* __restrict__ tw, const FxConst& kc) {
+    if constexpr (s < S) {
+      constexpr int R = radix(s);
+      fft_stage_ip<INV, R, true, (s > 0), false>(x, nf, n, fs, Ls, fi.nbm[s], fi.lsm[s], tw, kc, nullptr, nullptr);
+      __syncthreads();
+      dit<INV, s + 1>(x, nf, n, fs, Ls * R, fi, tw, kc);
+    }
+  }
+  template <bool INV, int s, bool CONV>
+  static __device__ __forceinline__ void dif(cfx* x, int nf, int n, int fs, int Ls, const FftInfo& fi,
+                                             const FxW* __restrict__ tw, const FxConst& kc, const float* sqa,
+                                             const float* sqb) {
+    if constexpr (s >= 0) {
+      constexpr int R = radix(s);
+      const int ls = Ls / R;
+      fft_stage_ip<INV, R, false, (s > 0), CONV>(x, nf, n, fs, ls, fi.nbm[s], fi.lsm[s], tw, kc, sqa, sqb);
+      __syncthreads();
+      dif<INV, s - 1, false>(x, nf, n, fs, ls, fi, tw, kc, sqa, sqb);
+    }
+  }
+  template <bool INV>
+  static __device__ __forceinline__ void run(cfx* x, int nf, int fs, const FftInfo& fi, const FxW* __restrict__ tw,
+                                             const FxConst& kc, const float* sqa = nullptr,
+                                             const float* sqb = nullptr) {
+    if constexpr (INV) {
+      dit<INV, 0>(x, nf, fi.n, fs, 1, fi, tw, kc);
+    } else {
+      if (sqa)
+        dif<INV, S - 1, true>(x, nf, fi.n, fs, fi.n, fi, tw, kc, sqa, sqb);
+      else
+        dif<INV, S - 1, false>(x, nf, fi.n, fs, fi.n, fi, tw, kc, sqa, sqb);
+    }
+  }
+};
+
+template <class Pw, int IN_MODE, int OUT_MODE, class FFT = FftRuntime>
 __device__ __forceinline__ void row_fx_body(const RowArgs& a, const Pw& pw, const FxW* __restrict__ twfx,
                                             const float4* __restrict__ twdf, const FxConst& kc, int bx, int by) {
   constexpr int NIN = Pw::NIN, NOUT = Pw::NOUT;
@@ -320,7 +384,7 @@ __device__ __forceinline__ void row_fx_body(const RowArgs& a, const Pw& pw, cons
         if (q > 0 && qn > q) z[__ldg(&a.irev[qn])] = fx_conj(fx_sub(A, P));
       }
       __syncthreads();
-      fft_ip<true>(buf0, NIN, ns, a.fft, twfx, kc);
+      FFT::template run<true>(buf0, NIN, ns, a.fft, twfx, kc);
     } else {
       // direct DFT in double-float: stage the spectra in buf1
       cdf* Fs = reinterpret_cast<cdf*>(buf1);
@@ -413,7 +477,7 @@ __device__ __forceinline__ void row_fx_body(const RowArgs& a, const Pw& pw, cons
     }
     __syncthreads();
     // rows to fixed point inside the first stage; output in digit-reversed order
-    fft_ip<false>(zout, NOUT, ns, a.fft, twfx, kc, s_pa, s_pb);
+    FFT::template run<false>(zout, NOUT, ns, a.fft, twfx, kc, s_pa, s_pb);
     for (int idx = threadIdx.x; idx < NOUT * ldm; idx += blockDim.x) {
       const int q = idx / NOUT, f = idx - q * NOUT;  // fields fastest: contiguous global writes
       const cfx* Zf = zout + (long)f * ns;
@@ -452,10 +516,10 @@ inline size_t row_fx_smem_bytes(const FftInfo& f) {
   return (size_t)(f.use_fft ? 1 : 2) * NF * (f.n + 1) * sizeof(cfx);
 }
 
-template <class Pw, int IN_MODE, int OUT_MODE>
+template <class Pw, int IN_MODE, int OUT_MODE, class FFT>
 __global__ void __launch_bounds__(256, 4) row_kernel_fx(RowArgs a, Pw pw, const FxW* __restrict__ twfx,
                                                      const float4* __restrict__ twdf, FxConst kc) {
-  row_fx_body<Pw, IN_MODE, OUT_MODE>(a, pw, twfx, twdf, kc, blockIdx.x, blockIdx.y);
+  row_fx_body<Pw, IN_MODE, OUT_MODE, FFT>(a, pw, twfx, twdf, kc, blockIdx.x, blockIdx.y);
 }
 
 }  // namespace aeolus

@@ -62,6 +62,9 @@ def parse():
     ap.add_argument("--cpu-rows", type=int, default=8, help="latitude rows in the CPU sample")
     ap.add_argument("--no-extras", action="store_true",
                     help="skip the ensemble (uneven l_max BVE) and adjoint (SWE gradient) side measurements")
+    ap.add_argument("--knobs", default="",
+                    help="launch shapes of the measured model as 5 comma-separated ints (bc_synth, bc_anal, "
+                         "row_threads, slice_synth, slice_anal) instead of autotuning; for profiling runs")
     return ap.parse_args()
 
 
@@ -547,8 +550,14 @@ def main():
     for name, m in (("split" if args.precision == "split" else "fp64", model), ("fp64", other)):
         if m is not None:
             y = y0
+            if args.knobs and m is model:
+                m._plan.set_tuning([int(x) for x in args.knobs.split(",")])
+                tuning[name] = {"knobs_bc_synth_bc_anal_row_threads_slice_synth_anal": list(m._plan.tuning()),
+                                "ms_per_step": None, "source": "--knobs"}
             for _ in range(warm):
                 y = m.rk4(y, DT, 1, check=False)
+            if args.knobs and m is model:
+                continue
             tuned = m.autotune(y0, DT)   # launch shapes for this batch; results do not depend on them
             tuning[name] = {"knobs_bc_synth_bc_anal_row_threads_slice_synth_anal": list(tuned["chosen"]),
                             "ms_per_step": tuned["ms_per_step"]}
