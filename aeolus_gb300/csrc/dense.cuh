@@ -143,10 +143,10 @@ static __global__ void __launch_bounds__(256) dense_slice_kernel(const double* _
   const int E = s_e;
   __nv_bfloat16* tile = out + (long long)(n / kNT) * nkc * chunk_elems(kNT);
   for (int k = threadIdx.x; k < nkc * kKC; k += blockDim.x) {
-    float dg[kSlices];
+    __nv_bfloat16 dg[kSlices];
     digits((n < N && k < K) ? x[k] : 0.0, E, dg);
 #pragma unroll
-    for (int s = 0; s < kSlices; ++s) tile[tile_elem(kNT, s, n % kNT, k)] = __float2bfloat16(dg[s]);
+    for (int s = 0; s < kSlices; ++s) tile[tile_elem(kNT, s, n % kNT, k)] = dg[s];
   }
 }
 

@@ -76,9 +76,9 @@ __global__ void split_psyn_kernel(int L, int nlat, int nh, int Mt, const double*
   for (int t = 0; t < Kp; ++t) {
     double v = 0.0;
     if (t < K) v = Pm[(long)t * nh] * ((south && (t & 1)) ? -1.0 : 1.0);
-    float d[kSlices];
+    __nv_bfloat16 d[kSlices];
     digits(v, E, d);
-    for (int s = 0; s < kSlices; ++s) blk[tile_elem(128, s, r, t)] = __float2bfloat16(d[s]);
+    for (int s = 0; s < kSlices; ++s) blk[tile_elem(128, s, r, t)] = d[s];
   }
 }
 
@@ -102,9 +102,9 @@ __global__ void split_pana_kernel(int L, int nlat, int nh, int NK, const double*
       const bool south = j >= nh;
       v = Pm[south ? nlat - 1 - j : j] * ((south && (t & 1)) ? -1.0 : 1.0);
     }
-    float d[kSlices];
+    __nv_bfloat16 d[kSlices];
     digits(v, E, d);
-    for (int s = 0; s < kSlices; ++s) blk[tile_elem(128, s, t, j)] = __float2bfloat16(d[s]);
+    for (int s = 0; s < kSlices; ++s) blk[tile_elem(128, s, t, j)] = d[s];
   }
 }
 
@@ -129,9 +129,9 @@ __global__ void dense_bsyn_kernel(long np, int ncol, int nkc, const double* __re
   __nv_bfloat16* tile = out + (long long)blockIdx.x * nkc * chunk_elems(128);
   const int c0 = blockIdx.y * 8 * kKC, c1 = min(nkc * kKC, c0 + 8 * kKC);
   for (int c = c0; c < c1; ++c) {
-    float d[kSlices];
+    __nv_bfloat16 d[kSlices];
     digits((p < np && c < ncol) ? B[(long)c * np + p] : 0.0, E, d);
-    for (int s = 0; s < kSlices; ++s) tile[tile_elem(128, s, threadIdx.x, c)] = __float2bfloat16(d[s]);
+    for (int s = 0; s < kSlices; ++s) tile[tile_elem(128, s, threadIdx.x, c)] = d[s];
   }
 }
 
@@ -159,9 +159,9 @@ __global__ void __launch_bounds__(256) dense_bana_kernel(long np, int ncol, int 
   const int E = s_e;
   __nv_bfloat16* tile = out + (long long)(c / 128) * nkc * chunk_elems(128);
   for (long p = threadIdx.x; p < (long)nkc * kKC; p += blockDim.x) {
-    float d[kSlices];
+    __nv_bfloat16 d[kSlices];
     digits((c < ncol && p < np) ? col[p] : 0.0, E, d);
-    for (int s = 0; s < kSlices; ++s) tile[tile_elem(128, s, c % 128, (int)p)] = __float2bfloat16(d[s]);
+    for (int s = 0; s < kSlices; ++s) tile[tile_elem(128, s, c % 128, (int)p)] = d[s];
   }
 }
 

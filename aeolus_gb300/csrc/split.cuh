@@ -78,17 +78,29 @@ __device__ inline long long fixed_point(double x, int E) {
   return (b >> 63) ? -X : X;
 }
 
-// Balanced base-256 digits of rint(x 2^(48-E)), most significant first.
-__device__ inline void digits(double x, int E, float* d) {
-  long long X = fixed_point(x, E);
+// One digit (|r| <= 128) as a bf16, exactly: the magic-number construction
+// puts r in the mantissa of 1.5 2^23 (FMA pipe, no integer-to-float
+// conversion, which would run on the FP64 pipe for 64-bit operands), and a
+// float holding a small integer is its own bf16 upper half.
+__device__ __forceinline__ __nv_bfloat16 digit_bf16(int r) {
+  const float f = __int_as_float(0x4B400000 + r) - 12582912.0f;
+  return __ushort_as_bfloat16(static_cast<unsigned short>(__float_as_uint(f) >> 16));
+}
+
+// Balanced base-256 digits of a fixed-point integer X (|X| <= 2^47), most
+// significant first.
+__device__ inline void digits_from_fixed(long long X, __nv_bfloat16* d) {
 #pragma unroll
   for (int i = kSlices - 1; i >= 1; --i) {
-    const long long r = ((X + 128) & 255) - 128;
-    d[i] = (float)r;
+    const int r = static_cast<int>(((X + 128) & 255) - 128);
+    d[i] = digit_bf16(r);
     X = (X - r) >> 8;
   }
-  d[0] = (float)X;
+  d[0] = digit_bf16(static_cast<int>(X));
 }
+
+// Balanced base-256 digits of rint(x 2^(48-E)), most significant first.
+__device__ inline void digits(double x, int E, __nv_bfloat16* d) { digits_from_fixed(fixed_point(x, E), d); }
 
 // T 2^e as a double (round to nearest even; results below the normal range
 // flush to zero), integer instructions only.
@@ -116,17 +128,6 @@ __device__ inline double scaled_to_double(long long T, int e) {
   if (ex <= 0) return 0.0;
   return __longlong_as_double(static_cast<long long>(sign | (static_cast<unsigned long long>(ex) << 52) |
                                                      (mant & 0xFFFFFFFFFFFFFull)));
-}
-
-// Balanced base-256 digits of a fixed-point integer X (|X| <= 2^47).
-__device__ inline void digits_from_fixed(long long X, float* d) {
-#pragma unroll
-  for (int i = kSlices - 1; i >= 1; --i) {
-    const long long r = ((X + 128) & 255) - 128;
-    d[i] = (float)r;
-    X = (X - r) >> 8;
-  }
-  d[0] = (float)X;
 }
 
 // Level recombination on the f32 pipe: every accumulator holds an exact
@@ -233,11 +234,11 @@ __device__ __forceinline__ void split_synth_slice_body(const SplitDims& dm, cons
   for (int idx = threadIdx.x; idx < nc * Kp; idx += blockDim.x) {
     const int c = idx / Kp, t = idx - c * Kp;
     const int n = b0 * NF * 2 + c;
-    float d[kSlices];
+    __nv_bfloat16 d[kSlices];
     digits(t < K ? s_val[c * K + t] : 0.0, s_exp[c], d);
     __nv_bfloat16* tile = dsyn + dsyn_tile(kcum, dm, m, n / kNT);
 #pragma unroll
-    for (int s = 0; s < kSlices; ++s) tile[tile_elem(kNT, s, n % kNT, t)] = __float2bfloat16(d[s]);
+    for (int s = 0; s < kSlices; ++s) tile[tile_elem(kNT, s, n % kNT, t)] = d[s];
   }
   if (by == gy - 1) {  // zero the columns that pad the last tile
     const int n0 = batch * NF * 2, n1 = dm.ntiles * kNT;
@@ -295,13 +296,13 @@ __device__ __forceinline__ void split_anal_slice_body(const SplitDims& dm, int b
   for (int idx = threadIdx.x; idx < nc * NK; idx += blockDim.x) {
     const int c = idx / NK, j = idx - c * NK;
     const int n = b0 * NF * 2 + c;
-    float d[kSlices];
+    __nv_bfloat16 d[kSlices];
     // X = rint(x 2^(48 - E)), |X| <= 2^47
     const long long X = j < nlat ? pk_align(s_wval[c * nlat + j], s_exp[c] - kShift) : 0LL;
     digits_from_fixed(X, d);
     __nv_bfloat16* tile = dana + dana_tile(dm, m, n / kNT);
 #pragma unroll
-    for (int s = 0; s < kSlices; ++s) tile[tile_elem(kNT, s, n % kNT, j)] = __float2bfloat16(d[s]);
+    for (int s = 0; s < kSlices; ++s) tile[tile_elem(kNT, s, n % kNT, j)] = d[s];
   }
   if (by == gy - 1) {
     const int n0 = batch * NF * 2, n1 = dm.ntiles * kNT;
