@@ -462,10 +462,11 @@ def _rel_l2_fields(a, b):
 # workload: dram__bytes_read.sum + dram__bytes_write.sum from one ncu capture
 # of the first RK4 stage (cold L2).
 NCU_TRAFFIC = {
-    "split_synth_slice": 28.211712e6 + 89.324032e6,
-    "tc_synth_bf16x6": 162.591744e6 + 171.899136e6,
-    "split_anal_slice": 231.8528e6 + 104.237312e6,
-    "tc_anal_bf16x6": 230.18496e6 + 67.749888e6,
+    "split_synth_slice": 28.503296e6 + 89.448448e6,
+    "tc_synth_bf16x6": 163.137024e6 + 172.440064e6,
+    "rows_fx_c2r_products_r2c": 226.85056e6 + 76.300032e6,
+    "split_anal_slice": 106.87104e6 + 99.851008e6,
+    "tc_anal_bf16x6": 230.490624e6 + 68.117248e6,
 }
 
 
@@ -490,7 +491,7 @@ def _roofline(kstats, B, peaks):
             entries[name] = {"kernel": name, "bound": "hbm", "achieved": byt / t / 1e9, "peak": hbm, "unit": "GB/s",
                              "frac": byt / t / 1e9 / hbm, "traffic": NCU_TRAFFIC.get(name), "launch_ms": t * 1000.0,
                              "work_per_launch": f"{B} members x {NLAT} rows x 13 spectra x (L+1) x 16 B",
-                             "note": "issue-bound on double-float FFT arithmetic, not on HBM"}
+                             "note": "bound by integer issue and barrier latency of the fixed-point FFTs, not by HBM"}
         elif name.endswith("_f64"):
             fields = 9 if "synth" in name else 4
             useful = ftx * fields * B
@@ -618,7 +619,7 @@ def main():
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
                 "warmup": warm, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None,
-                "dtype": "bf16x6-digit/f32x2/f64" if args.precision == "split" else "f64", "data": "synthetic",
+                "dtype": "bf16x6-digit/i64-fixed/f32x2/f64" if args.precision == "split" else "f64", "data": "synthetic",
                 "config": dict(workload_config(args, B), l2="flushed between steps (256 MiB write)"
                                if flush is not None else "not flushed"),
                 "member_steps_per_s": value * B,
