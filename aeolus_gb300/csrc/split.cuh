@@ -102,6 +102,12 @@ __device__ inline void digits_from_fixed(long long X, __nv_bfloat16* d) {
 // Balanced base-256 digits of rint(x 2^(48-E)), most significant first.
 __device__ inline void digits(double x, int E, __nv_bfloat16* d) { digits_from_fixed(fixed_point(x, E), d); }
 
+// Digits of 8 fixed-point values at contraction indices k0..k0+7 (k0 a
+// multiple of 8) of data row r of a kNT-row tile: in the core-matrix layout
+// those 8 indices are one contiguous 16-byte run per slice, so each slice is
+// one vector store.  Defined after tile_elem (below).
+__device__ inline void store_digits8(__nv_bfloat16* tile, int r, int k0, const long long* X);
+
 // T 2^e as a double (round to nearest even; results below the normal range
 // flush to zero), integer instructions only.
 __device__ inline double scaled_to_double(long long T, int e) {
@@ -193,6 +199,24 @@ __host__ __device__ inline long long tile_elem(int rows, int s, int r, int k) {
   return (long long)(k / kKC) * chunk_elems(rows) + (long long)s * rows * kKC + tc::core_index(r, k % kKC, kKC);
 }
 
+__device__ inline void store_digits8(__nv_bfloat16* tile, int r, int k0, const long long* X) {
+  uint32_t w[kSlices][4];
+#pragma unroll
+  for (int u = 0; u < 8; u += 2) {
+    __nv_bfloat16 a[kSlices], b[kSlices];
+    digits_from_fixed(X[u], a);
+    digits_from_fixed(X[u + 1], b);
+#pragma unroll
+    for (int s = 0; s < kSlices; ++s)
+      w[s][u >> 1] = static_cast<uint32_t>(__bfloat16_as_ushort(a[s])) |
+                     (static_cast<uint32_t>(__bfloat16_as_ushort(b[s])) << 16);
+  }
+  __nv_bfloat16* base = tile + tile_elem(kNT, 0, r, k0);
+#pragma unroll
+  for (int s = 0; s < kSlices; ++s)
+    *reinterpret_cast<uint4*>(base + (long long)s * kNT * kKC) = make_uint4(w[s][0], w[s][1], w[s][2], w[s][3]);
+}
+
 // ------------------------------------------------- synthesis data slicing
 // grid (m, member chunk of `mb` members); columns (b, f, re/im).
 template <class Derive>
@@ -201,10 +225,11 @@ __device__ __forceinline__ void split_synth_slice_body(const SplitDims& dm, cons
                                                        __nv_bfloat16* __restrict__ dsyn, int* __restrict__ ecol,
                                                        int bx, int by, int gy) {
   constexpr int NF = Derive::NF;
-  extern __shared__ double s_val[];  // [mb*NF*2][K]
+  extern __shared__ double s_val[];  // [mb*NF*2][ks]
   __shared__ int s_exp[256];
   const int m = bx, L = dm.L;
   const int K = L + 1 - m, Kp = kpad(K);
+  const int ks = K | 1;  // odd row stride: column-strided reads are free of bank conflicts
   const int b0 = by * mb;
   const int nb = min(mb, batch - b0);
   const int nc = nb * NF * 2;
@@ -214,15 +239,15 @@ __device__ __forceinline__ void split_synth_slice_body(const SplitDims& dm, cons
     der.column(b0 + bl, m + t, m, v);
 #pragma unroll
     for (int f = 0; f < NF; ++f) {
-      s_val[((bl * NF + f) * 2 + 0) * K + t] = v[f].x;
-      s_val[((bl * NF + f) * 2 + 1) * K + t] = v[f].y;
+      s_val[((bl * NF + f) * 2 + 0) * ks + t] = v[f].x;
+      s_val[((bl * NF + f) * 2 + 1) * ks + t] = v[f].y;
     }
   }
   __syncthreads();
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
   for (int c = warp; c < nc; c += nwarp) {
     unsigned long long mx = 0ull;
-    for (int t = lane; t < K; t += 32) mx = max(mx, abs_key(s_val[c * K + t]));
+    for (int t = lane; t < K; t += 32) mx = max(mx, abs_key(s_val[c * ks + t]));
     for (int o = 16; o > 0; o >>= 1) mx = max(mx, __shfl_xor_sync(0xffffffffu, mx, o));
     if (lane == 0) {
       const int E = exponent_for_key(mx);
@@ -231,14 +256,14 @@ __device__ __forceinline__ void split_synth_slice_body(const SplitDims& dm, cons
     }
   }
   __syncthreads();
-  for (int idx = threadIdx.x; idx < nc * Kp; idx += blockDim.x) {
-    const int c = idx / Kp, t = idx - c * Kp;
-    const int n = b0 * NF * 2 + c;
-    __nv_bfloat16 d[kSlices];
-    digits(t < K ? s_val[c * K + t] : 0.0, s_exp[c], d);
-    __nv_bfloat16* tile = dsyn + dsyn_tile(kcum, dm, m, n / kNT);
+  // 8 consecutive degrees of one column per thread, columns fastest
+  for (int idx = threadIdx.x; idx < nc * (Kp / 8); idx += blockDim.x) {
+    const int g = idx / nc, c = idx - g * nc;
+    const int n = b0 * NF * 2 + c, t0 = 8 * g, E = s_exp[c];
+    long long X[8];
 #pragma unroll
-    for (int s = 0; s < kSlices; ++s) tile[tile_elem(kNT, s, n % kNT, t)] = d[s];
+    for (int u = 0; u < 8; ++u) X[u] = t0 + u < K ? fixed_point(s_val[c * ks + t0 + u], E) : 0LL;
+    store_digits8(dsyn + dsyn_tile(kcum, dm, m, n / kNT), n % kNT, t0, X);
   }
   if (by == gy - 1) {  // zero the columns that pad the last tile
     const int n0 = batch * NF * 2, n1 = dm.ntiles * kNT;
@@ -266,9 +291,10 @@ template <int NF>
 __device__ __forceinline__ void split_anal_slice_body(const SplitDims& dm, int batch, int mb, int nblk,
                                                       const long long* __restrict__ FG, __nv_bfloat16* __restrict__ dana,
                                                       int* __restrict__ ecol, int bx, int by, int gy) {
-  extern __shared__ long long s_wval[];  // [mb*NF*2][nlat]
+  extern __shared__ long long s_wval[];  // [mb*NF*2][ns]
   __shared__ int s_exp[256];
   const int m = bx, L = dm.L, nlat = dm.nlat, NK = dm.NK;
+  const int ns = nlat | 1;  // odd row stride: column-strided reads are free of bank conflicts
   const int b0 = by * mb;
   const int nb = min(mb, batch - b0);
   const int nc = nb * NF * 2;
@@ -277,14 +303,14 @@ __device__ __forceinline__ void split_anal_slice_body(const SplitDims& dm, int b
     const int r = idx / NF;
     const int j = r % nlat, bl = r / nlat;
     const longlong2 g = *reinterpret_cast<const longlong2*>(FG + 2 * fg_index(b0 + bl, m, f, j, L, nblk, nlat));
-    s_wval[((bl * NF + f) * 2 + 0) * nlat + j] = g.x;
-    s_wval[((bl * NF + f) * 2 + 1) * nlat + j] = g.y;
+    s_wval[((bl * NF + f) * 2 + 0) * ns + j] = g.x;
+    s_wval[((bl * NF + f) * 2 + 1) * ns + j] = g.y;
   }
   __syncthreads();
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
   for (int c = warp; c < nc; c += nwarp) {
     int mx = -100000;
-    for (int j = lane; j < nlat; j += 32) mx = max(mx, pk_mag(s_wval[c * nlat + j]));
+    for (int j = lane; j < nlat; j += 32) mx = max(mx, pk_mag(s_wval[c * ns + j]));
     for (int o = 16; o > 0; o >>= 1) mx = max(mx, __shfl_xor_sync(0xffffffffu, mx, o));
     if (lane == 0) {
       const int E = mx == -100000 ? -1000 : mx + 1;  // |x| 2^-E < 1/2
@@ -293,16 +319,15 @@ __device__ __forceinline__ void split_anal_slice_body(const SplitDims& dm, int b
     }
   }
   __syncthreads();
-  for (int idx = threadIdx.x; idx < nc * NK; idx += blockDim.x) {
-    const int c = idx / NK, j = idx - c * NK;
-    const int n = b0 * NF * 2 + c;
-    __nv_bfloat16 d[kSlices];
-    // X = rint(x 2^(48 - E)), |X| <= 2^47
-    const long long X = j < nlat ? pk_align(s_wval[c * nlat + j], s_exp[c] - kShift) : 0LL;
-    digits_from_fixed(X, d);
-    __nv_bfloat16* tile = dana + dana_tile(dm, m, n / kNT);
+  // 8 consecutive latitudes of one column per thread, columns fastest;
+  // X = rint(x 2^(48 - E)), |X| <= 2^47
+  for (int idx = threadIdx.x; idx < nc * (NK / 8); idx += blockDim.x) {
+    const int g = idx / nc, c = idx - g * nc;
+    const int n = b0 * NF * 2 + c, j0 = 8 * g, S = s_exp[c] - kShift;
+    long long X[8];
 #pragma unroll
-    for (int s = 0; s < kSlices; ++s) tile[tile_elem(kNT, s, n % kNT, j)] = d[s];
+    for (int u = 0; u < 8; ++u) X[u] = j0 + u < nlat ? pk_align(s_wval[c * ns + j0 + u], S) : 0LL;
+    store_digits8(dana + dana_tile(dm, m, n / kNT), n % kNT, j0, X);
   }
   if (by == gy - 1) {
     const int n0 = batch * NF * 2, n1 = dm.ntiles * kNT;
@@ -767,8 +792,8 @@ SplitParts split_synth_parts(const aeolus_plan_impl* p, int batch, void* scratch
   r.digits = reinterpret_cast<__nv_bfloat16*>(w);
   w += align256((size_t)p->split->h_kcum[r.dm.L + 1] * r.dm.ntiles * kSlices * kNT * 2);
   r.ecol = reinterpret_cast<int*>(w);
-  r.mb = slice_members(NF, r.dm.L + 1, p->tune_slice_mb);
-  r.smem = (size_t)r.mb * NF * 2 * (r.dm.L + 1) * 8;
+  r.mb = slice_members(NF, r.dm.L + 2, p->tune_slice_mb);
+  r.smem = (size_t)r.mb * NF * 2 * ((r.dm.L + 1) | 1) * 8;
   r.grid = dim3(r.dm.L + 1, (batch + r.mb - 1) / r.mb);
   return r;
 }
@@ -781,8 +806,8 @@ SplitParts split_anal_parts(const aeolus_plan_impl* p, int batch, void* scratch)
   r.digits = reinterpret_cast<__nv_bfloat16*>(w);
   w += align256((size_t)(r.dm.L + 1) * r.dm.ntiles * kSlices * kNT * r.dm.NK * 2);
   r.ecol = reinterpret_cast<int*>(w);
-  r.mb = slice_members(NF, r.dm.nlat, p->tune_slice_mb_anal);
-  r.smem = (size_t)r.mb * NF * 2 * r.dm.nlat * 8;
+  r.mb = slice_members(NF, r.dm.nlat + 1, p->tune_slice_mb_anal);
+  r.smem = (size_t)r.mb * NF * 2 * (r.dm.nlat | 1) * 8;
   r.grid = dim3(r.dm.L + 1, (batch + r.mb - 1) / r.mb);
   return r;
 }
