@@ -142,11 +142,12 @@ static __global__ void __launch_bounds__(256) dense_slice_kernel(const double* _
   __syncthreads();
   const int E = s_e;
   __nv_bfloat16* tile = out + (long long)(n / kNT) * nkc * chunk_elems(kNT);
-  for (int k = threadIdx.x; k < nkc * kKC; k += blockDim.x) {
-    __nv_bfloat16 dg[kSlices];
-    digits((n < N && k < K) ? x[k] : 0.0, E, dg);
+  for (int g = threadIdx.x; g < nkc * kKC / 8; g += blockDim.x) {  // 8 contraction indices per thread
+    const int k0 = 8 * g;
+    long long Xs[8];
 #pragma unroll
-    for (int s = 0; s < kSlices; ++s) tile[tile_elem(kNT, s, n % kNT, k)] = dg[s];
+    for (int u = 0; u < 8; ++u) Xs[u] = (n < N && k0 + u < K) ? fixed_point(x[k0 + u], E) : 0LL;
+    store_digits8(tile, n % kNT, k0, Xs);
   }
 }
 

@@ -517,7 +517,7 @@ inline size_t row_fx_smem_bytes(const FftInfo& f) {
 }
 
 template <class Pw, int IN_MODE, int OUT_MODE, class FFT>
-__global__ void __launch_bounds__(256, 4) row_kernel_fx(RowArgs a, Pw pw, const FxW* __restrict__ twfx,
+__global__ void __launch_bounds__(256, 3) row_kernel_fx(RowArgs a, Pw pw, const FxW* __restrict__ twfx,
                                                      const float4* __restrict__ twdf, FxConst kc) {
   row_fx_body<Pw, IN_MODE, OUT_MODE, FFT>(a, pw, twfx, twdf, kc, blockIdx.x, blockIdx.y);
 }
