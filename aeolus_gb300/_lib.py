@@ -19,7 +19,7 @@ TUNING_KNOBS = 5  # AEOLUS_TUNING_KNOBS
 (OP_SYNTHESIZE, OP_ANALYZE, OP_JACOBIAN, OP_WINDS, OP_BVE_TENDENCY, OP_SWE_TENDENCY,
  OP_BVE_RK4, OP_SWE_RK4, OP_SWE_VALIDATE, OP_SWE_INVARIANTS,
  OP_SYNTHESIZE_ADJOINT, OP_ANALYZE_ADJOINT, OP_BVE_TENDENCY_ADJOINT, OP_SWE_TENDENCY_ADJOINT,
- OP_BVE_RK4_ADJOINT, OP_SWE_RK4_ADJOINT) = range(16)
+ OP_BVE_RK4_ADJOINT, OP_SWE_RK4_ADJOINT, OP_VECTOR_CURL_DIV) = range(17)
 STATE_NONFINITE, STATE_MONOPOLE, STATE_THICKNESS = 1, 2, 4
 
 # Spectral operator ids of aeolus_spectral_op.
@@ -57,6 +57,8 @@ SIGNATURES = {
     "aeolus_workspace_bytes": (c_int, [c_void_p, c_int, c_int, POINTER(c_size_t)]),
     "aeolus_synthesize": (c_int, [c_void_p, c_void_p, c_void_p, c_int, c_void_p, c_size_t, c_void_p]),
     "aeolus_analyze": (c_int, [c_void_p, c_void_p, c_void_p, c_int, c_void_p, c_size_t, c_void_p]),
+    "aeolus_vector_curl_div": (c_int, [c_void_p, c_double, c_void_p, c_void_p, c_void_p, c_int, c_int, c_void_p,
+                                       c_size_t, c_void_p]),
     "aeolus_synthesize_noalloc": (c_int, [c_void_p, c_void_p, c_void_p, c_int, c_void_p]),
     "aeolus_spectral_op": (c_int, [c_int, c_int, c_double, c_void_p, c_void_p, c_int, c_void_p]),
     "aeolus_jacobian": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p, c_int, c_void_p, c_size_t, c_void_p]),

@@ -331,6 +331,8 @@ int bve_vjp(const aeolus_plan_impl* plan, const aeolus_bve_params* p, const doub
 
 }  // namespace
 
+size_t vector_op_bytes(const aeolus_plan_impl* p, int batch);  // vector.cu
+
 size_t adjoint_op_bytes(const aeolus_plan_impl* p, int op, int batch) {
   switch (op) {
     case AEOLUS_OP_SYNTHESIZE_ADJOINT:
@@ -347,6 +349,8 @@ size_t adjoint_op_bytes(const aeolus_plan_impl* p, int op, int batch) {
     case AEOLUS_OP_SWE_RK4_ADJOINT:
       return std::max(swe_tadj_bytes(p, batch), full_chain_bytes<9, 4>(p, batch)) +
              7 * align256(state_bytes(p, 3, batch)) + align256(state_bytes(p, 2, batch));
+    case AEOLUS_OP_VECTOR_CURL_DIV:
+      return vector_op_bytes(p, batch);
     default:
       return 0;
   }

@@ -368,7 +368,7 @@ using namespace aeolus;
 
 extern "C" int aeolus_workspace_bytes(aeolus_plan plan, int op, int batch, size_t* bytes) {
   if (!plan_ok(plan) || !bytes) return fail(AEOLUS_ERR_ARG, "aeolus_workspace_bytes: bad arguments");
-  if (op < 0 || op > AEOLUS_OP_SWE_RK4_ADJOINT) return fail(AEOLUS_ERR_ARG, "aeolus_workspace_bytes: unknown op");
+  if (op < 0 || op > AEOLUS_OP_VECTOR_CURL_DIV) return fail(AEOLUS_ERR_ARG, "aeolus_workspace_bytes: unknown op");
   if (batch < 0) return fail(AEOLUS_ERR_ARG, "aeolus_workspace_bytes: negative batch");
   *bytes = std::max<size_t>(op_bytes(plan, op, std::max(batch, 1)), 256);
   return AEOLUS_OK;

@@ -162,6 +162,30 @@ def analyze(plan_id: int, grid: torch.Tensor) -> torch.Tensor:
     return out.reshape(lead + _spec_shape(p.lmax))
 
 
+@torch.library.custom_op("aeolus::vector_curl_div", mutates_args=())
+def vector_curl_div(plan_id: int, radius: float, f_east: torch.Tensor, f_north: torch.Tensor,
+                    truncate: bool) -> torch.Tensor:
+    """[2, ..., L+1, L+1] (curl, div) of tangent fields on the plan's points by
+    the weak form, spectral_operators.py:399-492; the plan is the one-degree-
+    extended analysis plan (l_max = L + 1) on the product points."""
+    p = _PLANS[plan_id]
+    _require_cuda(f_east, "eastward component")
+    _require_cuda(f_north, "northward component")
+    if f_east.shape != f_north.shape or f_east.shape[-1] != p.n_points:
+        raise ValueError(f"expected two [..., {p.n_points}] components, got {tuple(f_east.shape)} and "
+                         f"{tuple(f_north.shape)}")
+    lead = tuple(f_east.shape[:-1])
+    fe = torch.stack((f_east.to(torch.float64).reshape(-1, p.n_points),
+                      f_north.to(torch.float64).reshape(-1, p.n_points)), dim=1).contiguous()
+    B, L = fe.shape[0], p.lmax - 1
+    out = torch.empty((2, B, L + 1, L + 1), dtype=torch.complex128, device=fe.device)
+    if B:
+        w = p.workspace(_lib.OP_VECTOR_CURL_DIV, B)
+        check(_lib.load().aeolus_vector_curl_div(p.handle, float(radius), _ptr(fe), _ptr(out[0]), _ptr(out[1]), B,
+                                                 1 if truncate else 0, _ptr(w), w.numel(), _stream(fe.device)))
+    return out.reshape((2,) + lead + (L + 1, L + 1))
+
+
 @torch.library.custom_op("aeolus::spectral_op", mutates_args=())
 def spectral_op(op: int, radius: float, coeffs: torch.Tensor) -> torch.Tensor:
     """Diagonal / tridiagonal spectral operator (aeolus_spectral_op ids)."""

@@ -10,7 +10,7 @@ from __future__ import annotations
 import torch
 
 from . import _lib
-from .ops import jacobian, spectral_op, winds
+from .ops import Plan, jacobian, spectral_op, vector_curl_div, winds
 from .spherical_backend import make_backend
 
 
@@ -28,6 +28,7 @@ class SpectralOperators:
         dev = getattr(sh, "weights").device
         l = torch.arange(self.l_max + 1, dtype=torch.float64, device=dev)
         self.lap_eigs = -l * (l + 1.0) / self.R ** 2          # :114
+        self._vector_plan = None  # one-degree-extended analysis plan (:474-492), built on first use
 
     # -- diagonal / tridiagonal operators (one kernel each) --------------
     def laplacian_coeffs(self, coeffs):
@@ -85,6 +86,32 @@ class SpectralOperators:
         if sh_p is self.sh:
             return J_grid
         return self.sh.inv_transform(sh_p.transform(J_grid))
+
+    # -- vector fields ---------------------------------------------------------
+    def vector_curl_div_spectral(self, f_east, f_north, *, truncate: bool = True):
+        """(curl_lm, div_lm) of a tangent field sampled on the product points by
+        the weak form with one-degree-extended analyses, :399-492 (one analysis
+        chain on the extended plan, one spectral kernel)."""
+        plan = self._extended_plan()
+        dev = plan.device
+        fe = torch.as_tensor(f_east, dtype=torch.float64, device=dev)
+        fn = torch.as_tensor(f_north, dtype=torch.float64, device=dev)
+        out = vector_curl_div(plan.id, self.R, fe, fn, bool(truncate))
+        return out[0], out[1]
+
+    def _extended_plan(self):
+        """The product points and weights with the basis extended to degree
+        l_max + 1 (_vector_analysis_pieces, :474-492)."""
+        if self._vector_plan is None:
+            from .latlon_grid import GaussLatLonSphericalHarmonics
+            sh_p = self._product_space.sh
+            if isinstance(sh_p, GaussLatLonSphericalHarmonics):
+                g = sh_p.grid
+                self._vector_plan = Plan.gauss(g.nlat, g.nlon, self.l_max + 1, g.radius, g.device)
+            else:
+                lat, lon, w = (x.detach().cpu().numpy() for x in (sh_p.latitudes, sh_p.longitudes, sh_p.weights))
+                self._vector_plan = Plan.points(lat, lon, w, self.l_max + 1, self.R, sh_p.weights.device)
+        return self._vector_plan
 
     def velocity_from_streamfunction(self, psi_lm):
         """(u, v) on the state sampling, |cos lat| < 1e-6 -> 0; :517-538."""

@@ -66,7 +66,8 @@ enum aeolus_op {
   AEOLUS_OP_BVE_TENDENCY_ADJOINT = 12,
   AEOLUS_OP_SWE_TENDENCY_ADJOINT = 13,
   AEOLUS_OP_BVE_RK4_ADJOINT = 14,
-  AEOLUS_OP_SWE_RK4_ADJOINT = 15
+  AEOLUS_OP_SWE_RK4_ADJOINT = 15,
+  AEOLUS_OP_VECTOR_CURL_DIV = 16
 };
 
 /* SWE state-check bits (physics/shallow_water.py:494-539). */
@@ -180,6 +181,17 @@ int aeolus_synthesize_noalloc(aeolus_plan plan, const double* coeffs,
  * fast_geodesic_sh.py:68-87. */
 int aeolus_analyze(aeolus_plan plan, const double* grid, double* coeffs,
                    int batch, void* work, size_t work_bytes, void* stream);
+
+/* Curl and divergence of tangent vector fields by the weak form with
+ * one-degree-extended analyses, spectral_operators.py:399-492
+ * (vector_curl_div_spectral): plan_ext is a plan on the product points with
+ * the product weights and l_max = L + 1 (L the state degree); f_en is
+ * [batch][2][n_points] (eastward, northward components); curl and div are
+ * [batch][L+1][L+1] complex; truncate != 0 applies the 2/3 cut of rows and
+ * columns (cut = floor(2L/3)).  Workspace: AEOLUS_OP_VECTOR_CURL_DIV. */
+int aeolus_vector_curl_div(aeolus_plan plan_ext, double radius, const double* f_en, double* curl,
+                           double* div, int batch, int truncate, void* work, size_t work_bytes,
+                           void* stream);
 
 /* ---- spectral operators (numerics/spectral_operators.py) -------------- */
 

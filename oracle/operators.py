@@ -93,6 +93,35 @@ class Operators:
         J = (a_snt * b_lam - a_lam * b_snt) / self.coslat_p ** 2
         return self.truncate(sp.transform(J))
 
+    def vector_curl_div_spectral(self, f_east, f_north, sh_ext, truncate: bool = True):
+        """Weak-form curl/div of a tangent field on the product points,
+        spectral_operators.py:399-492: one-degree-extended half-metric
+        analyses a = A(F_east/cos), b = A(F_north/cos) (``sh_ext``: the
+        product points and weights with l_max + 1), then
+        div = (i m/R) a + S^T b / R, curl = (i m/R) b - S^T a / R with the
+        unclipped C+ at l = L reading the extended degree (:474-492)."""
+        L = self.l_max
+        n = L + 1
+        a = sh_ext.transform(np.asarray(f_east) / self.coslat_p)
+        b = sh_ext.transform(np.asarray(f_north) / self.coslat_p)
+        Lb = np.broadcast_to(np.arange(n, dtype=np.float64)[:, None], (n, n))
+        Mb = np.broadcast_to(np.arange(n, dtype=np.float64)[None, :], (n, n))
+        c_plus_true = Lb * np.sqrt(np.maximum((Lb + 1.0) ** 2 - Mb ** 2, 0.0)
+                                   / np.maximum((2.0 * Lb + 1.0) * (2.0 * Lb + 3.0), 1.0))
+        c_plus_true = np.where(Mb <= Lb, c_plus_true, 0.0)
+
+        def adjoint_ext(c_ext):
+            out = c_plus_true * c_ext[1:n + 1, :n]
+            out[1:, :] += self.C_minus[1:, :] * c_ext[:n - 1, :n]
+            return out
+
+        div = self.d_lambda_coeffs(a[:n, :n]) + adjoint_ext(b) / self.R
+        curl = self.d_lambda_coeffs(b[:n, :n]) - adjoint_ext(a) / self.R
+        if truncate:
+            self.truncate(curl)
+            self.truncate(div)
+        return curl, div
+
     def velocity_from_streamfunction(self, psi_lm):
         """Winds on the state sampling, spectral_operators.py:517-538."""
         coslat = np.cos(self.sh.latitudes)

@@ -7,8 +7,9 @@ NumPy stand-in for CuPy in ``tests/golden/refshim``; its CUDA-C basis kernel
 Omega = 7.292e-5 1/s, as the workloads specify (``Planet.generate`` would
 derive different constants and random terrain).
 
-Run:  PYTHONDONTWRITEBYTECODE=1 python tests/golden/make_golden.py
-Writes ``tests/golden/*.npz``.  Only l_max <= 85 fixtures are made: above
+Run:  PYTHONDONTWRITEBYTECODE=1 python tests/golden/make_golden.py [vector]
+Writes ``tests/golden/*.npz`` (with ``vector``: only the weak-form curl/div
+fixtures).  Only l_max <= 85 fixtures are made: above
 that the reference basis kernel underflows (l + m >= ~175) and is not a
 valid oracle.
 """
@@ -125,6 +126,29 @@ def geodesic_case(name, res, lmax, seed=3):
     print(f"{name}: {time.time() - t0:.1f}s")
 
 
+def vector_case(name, planet, seed):
+    """Weak-form curl/div of a random tangent field on the product points
+    (spectral_operators.py:399-492, truncate=True)."""
+    t0 = time.time()
+    so = planet.so
+    ps = so._product_space
+    lat = np.asarray(ps.sh.latitudes)
+    rng = np.random.default_rng(seed)
+    f_east = rng.standard_normal(lat.size)
+    f_north = rng.standard_normal(lat.size)
+    curl, div = so.vector_curl_div_spectral(f_east, f_north)
+    np.savez_compressed(
+        HERE / f"{name}.npz", lmax=so.l_max, radius=R, lat=lat, lon=np.asarray(ps.sh.longitudes),
+        weights=np.asarray(ps.sh.weights), f_east=f_east, f_north=f_north, curl=np.asarray(curl),
+        div=np.asarray(div))
+    print(f"{name}: {time.time() - t0:.1f}s")
+
+
+def vector_cases():
+    vector_case("vector_gauss16x32_L15_fine23x46", latlon_planet(16, 32, 15), seed=13)
+    vector_case("vector_geodesic_res3_L10", geodesic_planet(3, 10), seed=17)
+
+
 def main():
     # Small BVE workload: Gauss 32x64, l_max=21, one RK4 step at dt=600 s.
     bve_case("bve_gauss32x64_L21", 32, 64, 21)
@@ -135,7 +159,11 @@ def main():
     # Shallow-water workload grid: Gauss 128x256, l_max=85.
     swe_case("swe_gauss128x256_L85", 128, 256, 85, seed=2, dt=300.0)
     geodesic_case("geodesic_res3_L10", 3, 10)
+    vector_cases()
 
 
 if __name__ == "__main__":
-    main()
+    if sys.argv[1:] == ["vector"]:
+        vector_cases()
+    else:
+        main()

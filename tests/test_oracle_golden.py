@@ -107,3 +107,44 @@ def test_basis_matches_scipy():
             ref = sp.sph_harm_y(l, m, np.pi / 2 - lat, lon)
             k = l * (l + 1) // 2 + m
             assert np.allclose(Y[:, k], ref, rtol=1e-10, atol=1e-14), (l, m)
+
+
+@pytest.mark.parametrize("name", ["vector_gauss16x32_L15_fine23x46", "vector_geodesic_res3_L10"])
+def test_vector_curl_div_golden(golden, name):
+    """Weak-form curl/div with one-degree-extended analyses
+    (spectral_operators.py:399-492) against the reference's own output."""
+    g = golden(name)
+    L, R = int(g["lmax"]), float(g["radius"])
+    lat, lon, w = g["lat"], g["lon"], g["weights"]
+    sh_p = oracle.PointSetSH(lat, lon, L, weights=w)
+    sh_ext = oracle.PointSetSH(lat, lon, L + 1, weights=w)
+    ops = oracle.Operators(sh_p, R, sh_p=sh_p)
+    curl, div = ops.vector_curl_div_spectral(g["f_east"], g["f_north"], sh_ext)
+    assert rel_l2(curl, g["curl"]) < TOL
+    assert rel_l2(div, g["div"]) < TOL
+
+
+def test_vector_curl_div_recovers_potentials():
+    """On the 3/2-rule Gauss product grid the weak integrands of fields built
+    from band-limited potentials are integrated exactly: curl = lap(psi),
+    div = lap(chi) to round-off (the property the reference documents at
+    spectral_operators.py:433-437)."""
+    L, R = 12, 6.371e6
+    nf, mf = oracle.fine_dims(L + 1, 2 * L + 2, L)
+    sh_p = oracle.GaussSH(nf, mf, L)
+    ops = oracle.Operators(oracle.GaussSH(L + 1, 2 * L + 2, L), R, sh_p=sh_p)
+    rng = np.random.default_rng(0)
+    cut = (2 * L) // 3
+    psi = np.zeros((L + 1, L + 1), complex)
+    chi = np.zeros_like(psi)
+    for a in (psi, chi):
+        for l in range(1, cut + 1):
+            a[l, 1:l + 1] = rng.standard_normal(l) + 1j * rng.standard_normal(l)
+            a[l, 0] = rng.standard_normal()
+    snt = lambda c: sh_p.inv_transform(ops.sin_theta_d_theta_coeffs(c)) / R
+    lam = lambda c: sh_p.inv_transform(ops.d_lambda_coeffs(c))
+    u = (snt(psi) + lam(chi)) / ops.coslat_p   # shallow_water.py:305-319 winds
+    v = (lam(psi) - snt(chi)) / ops.coslat_p
+    curl, div = ops.vector_curl_div_spectral(u, v, oracle.GaussSH(nf, mf, L + 1))
+    assert rel_l2(curl, ops.laplacian_coeffs(psi)) < 1e-13
+    assert rel_l2(div, ops.laplacian_coeffs(chi)) < 1e-13
