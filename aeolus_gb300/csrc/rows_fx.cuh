@@ -235,6 +235,7 @@ __device__ void fft_ip(cfx* x, int nf, int fs, const FftInfo& fi, const FxW* __r
 // enough for the instruction caches.  The host picks FftFixed when the
 // plan's factors match.
 struct FftRuntime {
+  static constexpr bool kFixed = false;  // the plan may fall back to the direct DFT
   template <bool INV>
   static __device__ __forceinline__ void run(cfx* x, int nf, int fs, const FftInfo& fi, const FxW* __restrict__ tw,
                                              const FxConst& kc, const float* sqa = nullptr,
@@ -245,6 +246,7 @@ struct FftRuntime {
 
 template <int... Rs>
 struct FftFixed {
+  static constexpr bool kFixed = true;  // always an FFT plan: the DFT branches are not compiled
   static constexpr int S = sizeof...(Rs);
   static __host__ __device__ constexpr int radix(int s) {
     constexpr int f[S] = {Rs...};
@@ -310,7 +312,7 @@ __device__ __forceinline__ void row_fx_body(const RowArgs& a, const Pw& pw, cons
   const int N = a.fft.N, n = a.fft.n, L = a.L;
   const int ldm = L + 1;
   const int ns = n + 1;  // padded field stride of the smem rows (see row_body)
-  const bool use_fft = a.fft.use_fft != 0;
+  const bool use_fft = FFT::kFixed || a.fft.use_fft != 0;
   const int hb = min(52, 56 - (32 - __clz(max(n - 1, 1))));  // |fixed-point FFT input| < 2^hb
   cfx* buf0 = smem_fx;                 // the rows (all in-place FFT work)
   cfx* buf1 = smem_fx + (long)NF * ns;  // staged spectra of the direct DFT (allocated only then)

@@ -138,14 +138,18 @@ __device__ inline double scaled_to_double(long long T, int e) {
 
 // Level recombination on the f32 pipe: every accumulator holds an exact
 // integer below 2^24, so acc_k 256^(5-k) is an exact float; their double-
-// float sum (smallest first, error-free two-sums) is T to ~2^-48, and the
-// power-of-two scaling 2^e is applied in two exact steps.
+// float sum is T to ~2^-48, and the power-of-two scaling 2^e is applied in
+// two exact steps.
 __device__ inline float pow2f(int p) { return __int_as_float((p + 127) << 23); }  // p in [-126, 127]
 
 __device__ inline df levels_to_df(const float* acc, int e) {
-  df s = df{acc[kLevels - 1], 0.f};
-#pragma unroll
-  for (int k = kLevels - 2; k >= 0; --k) s = df_add_f(s, acc[k] * pow2f(8 * (kLevels - 1 - k)));
+  // pairwise: three exact two-sums of neighbouring levels, then two Dekker
+  // additions (error ~2^-48 of the operands) -- half the dependency depth of
+  // a sequential sum, for the latency-bound epilogue warps
+  const df p0 = two_sum(acc[0] * pow2f(40), acc[1] * pow2f(32));
+  const df p1 = two_sum(acc[2] * pow2f(24), acc[3] * pow2f(16));
+  const df p2 = two_sum(acc[4] * pow2f(8), acc[5]);
+  const df s = df_add_fast(df_add_fast(p0, p1), p2);
   // s * 2^e, e = e1 + e2 with both factors normal floats
   const int e1 = max(-126, min(127, e)), e2 = max(-126, min(127, e - e1));
   return df{s.hi * pow2f(e1) * pow2f(e2), s.lo * pow2f(e1) * pow2f(e2)};
