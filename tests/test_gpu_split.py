@@ -61,8 +61,12 @@ def _swe(nlat, nlon, L, precision, members=4, seed=3):
     return planet, ShallowWaterModel(planet, gravity=W.GRAVITY, mean_depth=depth), s
 
 
-@pytest.mark.parametrize("nlat,nlon,L", [(32, 64, 21), (128, 256, 85), (192, 384, 127)])
+@pytest.mark.parametrize("nlat,nlon,L", [(32, 64, 21), (128, 256, 85), (192, 384, 127), (24, 47, 15),
+                                         (80, 160, 52)])
 def test_split_swe_tendency_and_steps(nlat, nlon, L):
+    """Radix sequences: 64 x 2 (runtime FFT), 128 = (2,8,8) and 192 = (3,8,8)
+    (kernels compiled for the sequence), 80 = (5,2,8) (runtime), and an odd
+    longitude count (47: direct double-float DFT rows)."""
     _, m64, s = _swe(nlat, nlon, L, "fp64")
     planet, ms, _ = _swe(nlat, nlon, L, "split")
     t64, ts = N(m64.tendency(T(s))), N(ms.tendency(T(s)))
