@@ -462,11 +462,11 @@ def _rel_l2_fields(a, b):
 # workload: dram__bytes_read.sum + dram__bytes_write.sum from one ncu capture
 # of the first RK4 stage (cold L2).
 NCU_TRAFFIC = {
-    "split_synth_slice": 28.503296e6 + 89.448448e6,
-    "tc_synth_bf16x6": 163.137024e6 + 172.440064e6,
-    "rows_fx_c2r_products_r2c": 226.85056e6 + 76.300032e6,
-    "split_anal_slice": 106.87104e6 + 99.851008e6,
-    "tc_anal_bf16x6": 230.490624e6 + 68.117248e6,
+    "split_synth_slice": 27.497728e6 + 86.54464e6,
+    "tc_synth_bf16x6": 162.184192e6 + 171.406848e6,
+    "rows_fx_c2r_products_r2c": 226.575104e6 + 77.05216e6,
+    "split_anal_slice": 100.69504e6 + 95.401472e6,
+    "tc_anal_bf16x6": 230.352896e6 + 67.960576e6,
 }
 
 
