@@ -89,6 +89,9 @@ SIGNATURES = {
                                        c_size_t, c_void_p]),
     "aeolus_ensemble_create": (c_int, [c_int, POINTER(c_void_p), POINTER(c_int), POINTER(BveParams),
                                        POINTER(c_void_p)]),
+    "aeolus_ensemble_create_swe": (c_int, [c_int, POINTER(c_void_p), POINTER(c_int), POINTER(SweParams),
+                                           POINTER(c_void_p)]),
+    "aeolus_ensemble_swe_rk4": (c_int, [c_void_p, POINTER(c_void_p), c_double, c_int, c_void_p, c_size_t, c_void_p]),
     "aeolus_ensemble_destroy": (c_int, [c_void_p]),
     "aeolus_ensemble_workspace_bytes": (c_int, [c_void_p, POINTER(c_size_t)]),
     "aeolus_ensemble_bve_rk4": (c_int, [c_void_p, POINTER(c_void_p), c_double, c_int, c_void_p, c_size_t, c_void_p]),

@@ -16,9 +16,11 @@
 
 struct aeolus_ensemble_s {
   int ng = 0;
+  int model = 0;  // 0: barotropic vorticity, 1: shallow water
   aeolus_plan plan[8] = {};
   int batch[8] = {};
   aeolus_bve_params prm[8] = {};
+  aeolus_swe_params sprm[8] = {};
   int split = 0;
   int device = 0;
   cudaGraph_t graph = nullptr;
@@ -182,90 +184,161 @@ struct GroupedEpi<Sched, Epi, true> {
   }
 };
 
-// Workspace of one group: chain scratch, stage input, RK4 accumulator.
-size_t group_bytes(const aeolus_plan_impl* p, int batch) {
-  return align256(full_chain_bytes<4, 1>(p, batch)) + 2 * align256(state_bytes(p, 1, batch));
-}
-
-struct GroupBufs {
-  char* chain;
-  double2* ystage;
-  double2* acc;
+// Per-model pieces of a grouped RK4 stage: the functors of the chain and
+// the group workspace (chain scratch, stage inputs, RK4 accumulator).
+struct BveModel {
+  using Derive = BveDerive;
+  using Pw = JacPw;
+  using Epi = BveEpi;
+  static constexpr int NIN = 4, NOUT = 1;
+  struct Bufs {
+    char* chain;
+    double2* ystage;
+    double2* acc;
+  };
+  static size_t bytes(const aeolus_plan_impl* p, int B) {
+    return align256(full_chain_bytes<4, 1>(p, B)) + 2 * align256(state_bytes(p, 1, B));
+  }
+  static Bufs bufs(const aeolus_plan_impl* p, int B, char* base) {
+    Bufs b;
+    b.chain = base;
+    base += align256(full_chain_bytes<4, 1>(p, B));
+    b.ystage = reinterpret_cast<double2*>(base);
+    base += align256(state_bytes(p, 1, B));
+    b.acc = reinterpret_cast<double2*>(base);
+    return b;
+  }
+  // The functors of stage `stage` of group k (BarotropicVorticity.rk4).
+  static void make(const aeolus_ensemble_s* E, int k, const Bufs& b, double2* y0, int stage, double dt, Derive& d,
+                   Pw& pw, Epi& e) {
+    const aeolus_plan_impl* p = E->plan[k];
+    const Spec sp = make_spec(p, E->prm[k].radius);
+    const double2* in = stage == 1 ? y0 : b.ystage;
+    d = BveDerive{sp, in, 2.0 * E->prm[k].omega * kSqrt4PiOver3};
+    pw = JacPw{};
+    e = BveEpi{sp, in, nullptr, E->prm[k].viscosity, Rk4{stage, dt, y0, b.ystage, b.acc, nullptr}};
+  }
 };
 
-GroupBufs group_bufs(const aeolus_plan_impl* p, int batch, char* base) {
-  GroupBufs b;
-  b.chain = base;
-  base += align256(full_chain_bytes<4, 1>(p, batch));
-  b.ystage = reinterpret_cast<double2*>(base);
-  base += align256(state_bytes(p, 1, batch));
-  b.acc = reinterpret_cast<double2*>(base);
-  return b;
+struct SweModel {
+  using Derive = SweDerive;
+  using Pw = SwePw;
+  using Epi = SweEpi;
+  static constexpr int NIN = 9, NOUT = 4;
+  struct Bufs {
+    char* chain;
+    double2* stage[2];
+    double2* acc;
+    double2* cor;
+  };
+  static size_t bytes(const aeolus_plan_impl* p, int B) {
+    return align256(full_chain_bytes<9, 4>(p, B)) + 3 * align256(state_bytes(p, 3, B)) +
+           align256(state_bytes(p, 2, B));
+  }
+  static Bufs bufs(const aeolus_plan_impl* p, int B, char* base) {
+    Bufs b;
+    b.chain = base;
+    base += align256(full_chain_bytes<9, 4>(p, B));
+    for (int i = 0; i < 2; ++i) {
+      b.stage[i] = reinterpret_cast<double2*>(base);
+      base += align256(state_bytes(p, 3, B));
+    }
+    b.acc = reinterpret_cast<double2*>(base);
+    base += align256(state_bytes(p, 3, B));
+    b.cor = reinterpret_cast<double2*>(base);
+    return b;
+  }
+  // The functors of stage `stage` of group k, as in aeolus_swe_rk4: two stage
+  // buffers in turn (the epilogue reads neighbouring degrees of its input
+  // while writing the next input) and, on the split path, the Coriolis
+  // spectra of the stage input added spectrally.
+  static void make(const aeolus_ensemble_s* E, int k, const Bufs& b, double2* y0, int stage, double dt, Derive& d,
+                   Pw& pw, Epi& e) {
+    const aeolus_plan_impl* p = E->plan[k];
+    const aeolus_swe_params& q = E->sprm[k];
+    const Spec sp = make_spec(p, q.radius);
+    const double f10 = 2.0 * q.omega * kSqrt4PiOver3;
+    const double phi0 = q.gravity * q.mean_depth;
+    const bool spec_cor = p->precision == AEOLUS_PREC_SPLIT_BF16;
+    double2* cor = spec_cor ? b.cor : nullptr;
+    const double fp = spec_cor ? 0.0 : f10;
+    const double2* in = stage == 1 ? y0 : b.stage[stage & 1];
+    double2* next = b.stage[(stage + 1) & 1];
+    d = SweDerive{sp, in, fp, cor, 2.0 * q.omega};
+    pw = SwePw{fp, phi0, (float)phi0};
+    e = SweEpi{sp, in, phi0, q.nu4, Rk4{stage, dt, y0, next, b.acc, nullptr}, spec_cor ? 2.0 * q.omega : 0.0, cor};
+  }
+};
+
+size_t group_bytes(const aeolus_ensemble_s* E, int k) {
+  return E->model == 1 ? SweModel::bytes(E->plan[k], E->batch[k]) : BveModel::bytes(E->plan[k], E->batch[k]);
 }
 
 size_t ens_bytes(const aeolus_ensemble_s* e) {
   size_t n = 0;
-  for (int k = 0; k < e->ng; ++k) n += group_bytes(e->plan[k], e->batch[k]);
+  for (int k = 0; k < e->ng; ++k) n += group_bytes(e, k);
   return n;
 }
 
 // One RK4 stage of every group: 3 (FP64) or 5 (split) grouped launches.
-int ens_stage(const aeolus_ensemble_s* E, double2* const* y0, int stage, double dt, char* work, cudaStream_t st) {
+template <class M>
+int ens_stage_m(const aeolus_ensemble_s* E, double2* const* y0, int stage, double dt, char* work, cudaStream_t st) {
+  using Derive = typename M::Derive;
+  using Pw = typename M::Pw;
+  using Epi = typename M::Epi;
+  constexpr int NIN = M::NIN, NOUT = M::NOUT, NB = NIN > NOUT ? NIN : NOUT;
   const int ng = E->ng;
-  BveDerive der[kMaxGroups];
-  BveEpi epi[kMaxGroups];
-  GroupBufs gb[kMaxGroups];
+  Derive der[kMaxGroups];
+  Pw pws[kMaxGroups];
+  Epi epi[kMaxGroups];
+  char* chain[kMaxGroups];
   char* w = work;
   for (int k = 0; k < ng; ++k) {
-    const aeolus_plan_impl* p = E->plan[k];
-    gb[k] = group_bufs(p, E->batch[k], w);
-    w += group_bytes(p, E->batch[k]);
-    const Spec sp = make_spec(p, E->prm[k].radius);
-    const double2* in = stage == 1 ? y0[k] : gb[k].ystage;
-    der[k] = BveDerive{sp, in, 2.0 * E->prm[k].omega * kSqrt4PiOver3};
-    epi[k] = BveEpi{sp, in, nullptr, E->prm[k].viscosity, Rk4{stage, dt, y0[k], gb[k].ystage, gb[k].acc, nullptr}};
+    const typename M::Bufs b = M::bufs(E->plan[k], E->batch[k], w);
+    w += M::bytes(E->plan[k], E->batch[k]);
+    chain[k] = b.chain;
+    M::make(E, k, b, y0[k], stage, dt, der[k], pws[k], epi[k]);
   }
   int s;
   // rows (shared by both paths)
-  Grouped<RowArg<JacPw>> gr{};
+  Grouped<RowArg<Pw>> gr{};
   size_t sm_rows = 0;
   int row_thr = 0;
   for (int k = 0; k < ng; ++k) {
     const aeolus_plan_impl* p = E->plan[k];
     RowArgs ra{};
     ra.batch = E->batch[k];
-    ra.FG = reinterpret_cast<double2*>(gb[k].chain);
-    ra.nblk = 4;
+    ra.FG = reinterpret_cast<double2*>(chain[k]);
+    ra.nblk = NB;
     row_args(p, ra);
     if (E->split) ra.fft = p->fftx;
-    grouped_add(gr, RowArg<JacPw>{ra, JacPw{}, p->twfx, p->twdf}, dim3(p->nlat, E->batch[k]));
-    sm_rows = std::max(sm_rows, E->split ? row_fx_smem_bytes<JacPw>(p->fftx) : row_smem_bytes<JacPw>(p->fft));
+    grouped_add(gr, RowArg<Pw>{ra, pws[k], p->twfx, p->twdf}, dim3(p->nlat, E->batch[k]));
+    sm_rows = std::max(sm_rows, E->split ? row_fx_smem_bytes<Pw>(p->fftx) : row_smem_bytes<Pw>(p->fft));
     row_thr = std::max(row_thr, row_threads(p));
   }
   if (!E->split) {
-    Grouped<SynthArg<BveDerive>> gs{};
-    Grouped<AnalArg<BveEpi>> ga{};
+    Grouped<SynthArg<Derive>> gs{};
+    Grouped<AnalArg<Epi>> ga{};
     size_t sm_s = 0, sm_a = 0;
     int thr_s = 64, thr_a = 64;
     for (int k = 0; k < ng; ++k) {
       const aeolus_plan_impl* p = E->plan[k];
-      double2* FG = reinterpret_cast<double2*>(gb[k].chain);
-      const LegCfg cs = synth_cfg<BveDerive>(p, E->batch[k]);
-      const LegCfg ca = analysis_cfg<BveEpi>(p, E->batch[k]);
-      grouped_add(gs, SynthArg<BveDerive>{LegArgs{p->lmax, p->nlat, p->nh, E->batch[k], cs.bc, p->P, p->PT, FG, 4},
-                                          der[k]},
+      double2* FG = reinterpret_cast<double2*>(chain[k]);
+      const LegCfg cs = synth_cfg<Derive>(p, E->batch[k]);
+      const LegCfg ca = analysis_cfg<Epi>(p, E->batch[k]);
+      grouped_add(gs, SynthArg<Derive>{LegArgs{p->lmax, p->nlat, p->nh, E->batch[k], cs.bc, p->P, p->PT, FG, NB},
+                                       der[k]},
                   cs.grid);
-      grouped_add(ga, AnalArg<BveEpi>{LegArgs{p->lmax, p->nlat, p->nh, E->batch[k], ca.bc, p->P, p->PT, FG, 4},
-                                      epi[k]},
+      grouped_add(ga, AnalArg<Epi>{LegArgs{p->lmax, p->nlat, p->nh, E->batch[k], ca.bc, p->P, p->PT, FG, NB}, epi[k]},
                   ca.grid);
       sm_s = std::max(sm_s, cs.smem);
       sm_a = std::max(sm_a, ca.smem);
       thr_s = std::max(thr_s, cs.threads);
       thr_a = std::max(thr_a, ca.threads);
     }
-    auto k1 = g_legendre_synth<BveDerive, kSynthCPT>;
-    auto k2 = g_rows<JacPw>;
-    auto k3 = g_legendre_analysis<BveEpi>;
+    auto k1 = g_legendre_synth<Derive, kSynthCPT>;
+    auto k2 = g_rows<Pw>;
+    auto k3 = g_legendre_analysis<Epi>;
     if ((s = allow_smem(k1, sm_s)) || (s = allow_smem(k2, sm_rows)) || (s = allow_smem(k3, sm_a))) return s;
     {
       ProfScope prof("ens_legendre_synth_f64", st);
@@ -283,46 +356,46 @@ int ens_stage(const aeolus_ensemble_s* E, double2* const* y0, int stage, double 
     return AEOLUS_OK;
   }
   // split precision
-  Grouped<SliceSynthArg<BveDerive>> gss{};
+  Grouped<SliceSynthArg<Derive>> gss{};
   Grouped<SliceAnalArg> gsa{};
   GroupedSched<SynthSched> tsyn{};
-  GroupedEpi<SynthSched, SynthEpi<4>> esyn{};
+  GroupedEpi<SynthSched, SynthEpi<NIN>> esyn{};
   GroupedSched<AnalSched> tana{};
-  GroupedEpi<AnalSched, AnalEpi<BveEpi>> eana{};
+  GroupedEpi<AnalSched, AnalEpi<Epi>> eana{};
   size_t sm_ss = 0, sm_sa = 0;
   int sm_count = 1;
   int* err = nullptr;
   for (int k = 0; k < ng; ++k) {
     const aeolus_plan_impl* p = E->plan[k];
     const int B = E->batch[k];
-    double2* FG = reinterpret_cast<double2*>(gb[k].chain);
-    void* scratch = gb[k].chain + align256(fg_bytes(p, 4, B));
-    const SplitParts r1 = split_synth_parts<4>(p, B, scratch);
-    const SplitParts r2 = split_anal_parts<1>(p, B, scratch);
-    grouped_add(gss, SliceSynthArg<BveDerive>{r1.dm, p->split->kcum, B, r1.mb, der[k], r1.digits, r1.ecol}, r1.grid);
-    grouped_add(gsa, SliceAnalArg{r2.dm, B, r2.mb, 4, reinterpret_cast<const long long*>(FG), r2.digits, r2.ecol},
+    double2* FG = reinterpret_cast<double2*>(chain[k]);
+    void* scratch = chain[k] + align256(fg_bytes(p, NB, B));
+    const SplitParts r1 = split_synth_parts<NIN>(p, B, scratch);
+    const SplitParts r2 = split_anal_parts<NOUT>(p, B, scratch);
+    grouped_add(gss, SliceSynthArg<Derive>{r1.dm, p->split->kcum, B, r1.mb, der[k], r1.digits, r1.ecol}, r1.grid);
+    grouped_add(gsa, SliceAnalArg{r2.dm, B, r2.mb, NB, reinterpret_cast<const long long*>(FG), r2.digits, r2.ecol},
                 r2.grid);
     sm_ss = std::max(sm_ss, r1.smem);
     sm_sa = std::max(sm_sa, r2.smem);
     const SynthSched sc{r1.dm, p->split->kcum, p->split->psyn, r1.digits};
     tsyn.s[k] = sc;
     tsyn.start[k + 1] = tsyn.start[k] + sc.count_host();
-    esyn.e[k] = SynthEpi<4>{r1.dm, p->split->esyn, r1.ecol, 4, reinterpret_cast<float4*>(FG)};
+    esyn.e[k] = SynthEpi<NIN>{r1.dm, p->split->esyn, r1.ecol, NB, reinterpret_cast<float4*>(FG)};
     const AnalSched sa{r2.dm, p->split->pana, r2.digits};
     tana.s[k] = sa;
     tana.start[k + 1] = tana.start[k] + sa.count_host();
-    eana.e[k] = AnalEpi<BveEpi>{r2.dm, p->split->eana, r2.ecol, B, epi[k]};
+    eana.e[k] = AnalEpi<Epi>{r2.dm, p->split->eana, r2.ecol, B, epi[k]};
     sm_count = std::max(sm_count, p->sm_count);
     err = p->split->err;  // any group's flag: a device error marks every plan's kernels suspect
   }
   tsyn.n = tana.n = ng;
   esyn.gs = tsyn;
   eana.gs = tana;
-  auto k1 = g_slice_synth<BveDerive>;
-  auto k2 = tc_persistent_kernel<GroupedSched<SynthSched>, GroupedEpi<SynthSched, SynthEpi<4>>>;
-  auto k3 = g_rows_fx<JacPw>;
-  auto k4 = g_slice_anal<1>;
-  auto k5 = tc_persistent_kernel<GroupedSched<AnalSched>, GroupedEpi<AnalSched, AnalEpi<BveEpi>>>;
+  auto k1 = g_slice_synth<Derive>;
+  auto k2 = tc_persistent_kernel<GroupedSched<SynthSched>, GroupedEpi<SynthSched, SynthEpi<NIN>>>;
+  auto k3 = g_rows_fx<Pw>;
+  auto k4 = g_slice_anal<NOUT>;
+  auto k5 = tc_persistent_kernel<GroupedSched<AnalSched>, GroupedEpi<AnalSched, AnalEpi<Epi>>>;
   const size_t smt = tc_smem_bytes();
   if ((s = allow_smem(k1, sm_ss)) || (s = allow_smem(k2, smt)) || (s = allow_smem(k3, sm_rows)) ||
       (s = allow_smem(k4, sm_sa)) || (s = allow_smem(k5, smt)))
@@ -334,8 +407,8 @@ int ens_stage(const aeolus_ensemble_s* E, double2* const* y0, int stage, double 
   }
   {
     ProfScope prof("ens_tc_synth_bf16x6", st);
-    k2<<<std::max(1, std::min(tsyn.start[ng], sm_count)), tc_threads<GroupedEpi<SynthSched, SynthEpi<4>>>(), smt, st>>>(
-        tsyn, esyn, err);
+    k2<<<std::max(1, std::min(tsyn.start[ng], sm_count)), tc_threads<GroupedEpi<SynthSched, SynthEpi<NIN>>>(), smt,
+         st>>>(tsyn, esyn, err);
     AE_LAUNCH("tc_persistent_kernel(ensemble synthesis)");
   }
   {
@@ -349,10 +422,15 @@ int ens_stage(const aeolus_ensemble_s* E, double2* const* y0, int stage, double 
     AE_LAUNCH("g_slice_anal");
   }
   ProfScope prof("ens_tc_anal_bf16x6", st);
-  k5<<<std::max(1, std::min(tana.start[ng], sm_count)), tc_threads<GroupedEpi<AnalSched, AnalEpi<BveEpi>>>(), smt,
+  k5<<<std::max(1, std::min(tana.start[ng], sm_count)), tc_threads<GroupedEpi<AnalSched, AnalEpi<Epi>>>(), smt,
      st>>>(tana, eana, err);
   AE_LAUNCH("tc_persistent_kernel(ensemble analysis)");
   return AEOLUS_OK;
+}
+
+int ens_stage(const aeolus_ensemble_s* E, double2* const* y0, int stage, double dt, char* work, cudaStream_t st) {
+  return E->model == 1 ? ens_stage_m<SweModel>(E, y0, stage, dt, work, st)
+                       : ens_stage_m<BveModel>(E, y0, stage, dt, work, st);
 }
 
 int ens_step(const aeolus_ensemble_s* E, double2* const* y0, double dt, char* work, cudaStream_t st) {
@@ -399,38 +477,65 @@ int time_stage(const aeolus_ensemble_s* E, double2* const* y0, char* work, cudaS
 
 using namespace aeolus;
 
-extern "C" int aeolus_ensemble_create(int ngroups, const aeolus_plan* plans, const int* batch,
-                                      const aeolus_bve_params* params, aeolus_ensemble* out) {
-  if (!out || !plans || !batch || !params || ngroups < 1 || ngroups > kMaxGroups)
-    return fail(AEOLUS_ERR_ARG, "aeolus_ensemble_create: need 1.." + std::to_string(kMaxGroups) + " groups");
+namespace {
+
+// Shared checks of the two create calls; params_ok(k) validates group k's model parameters.
+template <class F>
+int ens_create(int model, int ngroups, const aeolus_plan* plans, const int* batch, const char* who, F params_ok,
+               aeolus_ensemble* out) {
+  if (!out || !plans || !batch || ngroups < 1 || ngroups > kMaxGroups)
+    return fail(AEOLUS_ERR_ARG, std::string(who) + ": need 1.." + std::to_string(kMaxGroups) + " groups");
+  *out = nullptr;
   int prec = -1, dev = -1;
   for (int k = 0; k < ngroups; ++k) {
     const aeolus_plan_impl* p = plans[k];
     if (!plan_ok(p) || p->kind != kGauss)
-      return fail(AEOLUS_ERR_ARG, "aeolus_ensemble_create: group " + std::to_string(k) + " needs a Gauss plan");
+      return fail(AEOLUS_ERR_ARG, std::string(who) + ": group " + std::to_string(k) + " needs a Gauss plan");
     if (batch[k] < 1 || batch[k] > 65535)
-      return fail(AEOLUS_ERR_ARG, "aeolus_ensemble_create: group " + std::to_string(k) + " batch out of range");
-    int s = bve_check(plans[k], &params[k], "aeolus_ensemble_create");
+      return fail(AEOLUS_ERR_ARG, std::string(who) + ": group " + std::to_string(k) + " batch out of range");
+    int s = params_ok(k);
     if (s) return s;
     if (prec >= 0 && p->precision != prec)
-      return fail(AEOLUS_ERR_ARG, "aeolus_ensemble_create: all groups must use the same contraction precision");
+      return fail(AEOLUS_ERR_ARG, std::string(who) + ": all groups must use the same contraction precision");
     if (dev >= 0 && p->device != dev)
-      return fail(AEOLUS_ERR_ARG, "aeolus_ensemble_create: all groups must live on one device");
+      return fail(AEOLUS_ERR_ARG, std::string(who) + ": all groups must live on one device");
     if (p->precision == AEOLUS_PREC_SPLIT_BF16 && !p->split)
-      return fail(AEOLUS_ERR_ARG, "aeolus_ensemble_create: split precision without split tables");
+      return fail(AEOLUS_ERR_ARG, std::string(who) + ": split precision without split tables");
     prec = p->precision;
     dev = p->device;
   }
   auto* e = new aeolus_ensemble_s;
   e->ng = ngroups;
+  e->model = model;
   for (int k = 0; k < ngroups; ++k) {
     e->plan[k] = plans[k];
     e->batch[k] = batch[k];
-    e->prm[k] = params[k];
   }
   e->split = prec == AEOLUS_PREC_SPLIT_BF16;
   e->device = dev;
   *out = e;
+  return AEOLUS_OK;
+}
+
+}  // namespace
+
+extern "C" int aeolus_ensemble_create(int ngroups, const aeolus_plan* plans, const int* batch,
+                                      const aeolus_bve_params* params, aeolus_ensemble* out) {
+  if (!params) return fail(AEOLUS_ERR_ARG, "aeolus_ensemble_create: NULL params");
+  int s = ens_create(0, ngroups, plans, batch, "aeolus_ensemble_create",
+                     [&](int k) { return bve_check(plans[k], &params[k], "aeolus_ensemble_create"); }, out);
+  if (s) return s;
+  for (int k = 0; k < ngroups; ++k) (*out)->prm[k] = params[k];
+  return AEOLUS_OK;
+}
+
+extern "C" int aeolus_ensemble_create_swe(int ngroups, const aeolus_plan* plans, const int* batch,
+                                          const aeolus_swe_params* params, aeolus_ensemble* out) {
+  if (!params) return fail(AEOLUS_ERR_ARG, "aeolus_ensemble_create_swe: NULL params");
+  int s = ens_create(1, ngroups, plans, batch, "aeolus_ensemble_create_swe",
+                     [&](int k) { return swe_check(&params[k], "aeolus_ensemble_create_swe"); }, out);
+  if (s) return s;
+  for (int k = 0; k < ngroups; ++k) (*out)->sprm[k] = params[k];
   return AEOLUS_OK;
 }
 
@@ -457,10 +562,14 @@ extern "C" int aeolus_ensemble_workspace_bytes(aeolus_ensemble e, size_t* bytes)
                                             std::to_string(ens_bytes(e)) + " bytes needed)");              \
   } while (0)
 
-extern "C" int aeolus_ensemble_bve_rk4(aeolus_ensemble e, double* const* zeta, double dt, int nsteps, void* work,
-                                       size_t work_bytes, void* stream) {
-  ENS_CHECK("aeolus_ensemble_bve_rk4");
-  if (!std::isfinite(dt)) return fail(AEOLUS_ERR_ARG, "aeolus_ensemble_bve_rk4: dt must be finite");
+namespace {
+
+int ens_rk4(aeolus_ensemble e, double* const* zeta, double dt, int nsteps, void* work, size_t work_bytes,
+            void* stream, int model, const char* who) {
+  ENS_CHECK(who);
+  if (e->model != model)
+    return fail(AEOLUS_ERR_ARG, std::string(who) + ": the ensemble was created for the other model");
+  if (!std::isfinite(dt)) return fail(AEOLUS_ERR_ARG, std::string(who) + ": dt must be finite");
   double2* y[kMaxGroups];
   for (int k = 0; k < e->ng; ++k) y[k] = reinterpret_cast<double2*>(zeta[k]);
   const cudaStream_t st = static_cast<cudaStream_t>(stream);
@@ -469,6 +578,18 @@ extern "C" int aeolus_ensemble_bve_rk4(aeolus_ensemble e, double* const* zeta, d
     if (s) return s;
   }
   return AEOLUS_OK;
+}
+
+}  // namespace
+
+extern "C" int aeolus_ensemble_bve_rk4(aeolus_ensemble e, double* const* zeta, double dt, int nsteps, void* work,
+                                       size_t work_bytes, void* stream) {
+  return ens_rk4(e, zeta, dt, nsteps, work, work_bytes, stream, 0, "aeolus_ensemble_bve_rk4");
+}
+
+extern "C" int aeolus_ensemble_swe_rk4(aeolus_ensemble e, double* const* state, double dt, int nsteps, void* work,
+                                       size_t work_bytes, void* stream) {
+  return ens_rk4(e, state, dt, nsteps, work, work_bytes, stream, 1, "aeolus_ensemble_swe_rk4");
 }
 
 extern "C" int aeolus_ensemble_capture(aeolus_ensemble e, double* const* zeta, double dt, void* work,

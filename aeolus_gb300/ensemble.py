@@ -1,15 +1,17 @@
-"""Batched uneven ensembles: BVE members of different l_max advanced together.
+"""Batched uneven ensembles: members of different l_max advanced together.
 
-Each group is a :class:`~aeolus_gb300.barotropic.BarotropicVorticity` model
-(its own Gauss grid and product-space plan) with a batch of members; every
-RK4 stage launches each stage kernel once for all groups
-(``aeolus_ensemble_bve_rk4``), a whole step can be captured into a CUDA graph
+Each group is a model (:class:`~aeolus_gb300.barotropic.BarotropicVorticity`
+or :class:`~aeolus_gb300.shallow_water.ShallowWaterModel`, each with its own
+Gauss grid and product-space plan) with a batch of members; every RK4 stage
+launches each stage kernel once for all groups (``aeolus_ensemble_bve_rk4``,
+``aeolus_ensemble_swe_rk4``), a whole step can be captured into a CUDA graph
 and replayed (``aeolus_ensemble_capture`` / ``aeolus_ensemble_launch``), and
 ``autotune`` times candidate launch shapes per group on the ensemble's own
 states (``aeolus_ensemble_autotune``).
 
-The reference runs one state per process (run/bve/runner.py:211-216); the
-per-member arithmetic here is that of ``BarotropicVorticity.rk4``.
+The reference runs one state per process (run/bve/runner.py:211-216,
+run/engine.py:406-431); the per-member arithmetic here is that of the
+models' own ``rk4``.
 """
 from __future__ import annotations
 
@@ -23,23 +25,14 @@ from ._lib import check
 from .ops import _stream
 
 
-class BarotropicEnsemble:
-    def __init__(self, models, batches):
-        if len(models) != len(batches) or not models:
-            raise ValueError("need one batch size per model")
-        self.models = list(models)
-        self.batches = [int(b) for b in batches]
-        self.device = self.models[0].f_lm.device
-        lib = _lib.load()
-        n = len(models)
-        plans = (c_void_p * n)(*[m._plan.handle.value for m in self.models])
-        bs = (c_int * n)(*self.batches)
-        prm = (_lib.BveParams * n)(*[_lib.BveParams(m.R, m.Omega, m.nu) for m in self.models])
-        self.handle = c_void_p()
-        check(lib.aeolus_ensemble_create(n, ctypes.cast(plans, ctypes.POINTER(c_void_p)), bs, prm,
-                                         byref(self.handle)))
+class _Ensemble:
+    """Shared workspace, graph capture / replay and autotuning."""
+
+    _fields = 1  # state fields per member
+
+    def _finish_init(self):
         nbytes = c_size_t()
-        check(lib.aeolus_ensemble_workspace_bytes(self.handle, byref(nbytes)))
+        check(_lib.load().aeolus_ensemble_workspace_bytes(self.handle, byref(nbytes)))
         self.work = torch.empty(nbytes.value, dtype=torch.uint8, device=self.device)
         self._captured = None
 
@@ -52,17 +45,15 @@ class BarotropicEnsemble:
             raise ValueError("need one state tensor per group")
         for k, (s, m, b) in enumerate(zip(states, self.models, self.batches)):
             L = m.sh.l_max
-            if (tuple(s.shape) != (b, L + 1, L + 1) or s.dtype != torch.complex128 or not s.is_cuda
-                    or not s.is_contiguous()):
-                raise ValueError(f"group {k}: expected a contiguous complex128 CUDA tensor [{b}, {L + 1}, {L + 1}]")
+            shape = (b, L + 1, L + 1) if self._fields == 1 else (b, self._fields, L + 1, L + 1)
+            if tuple(s.shape) != shape or s.dtype != torch.complex128 or not s.is_cuda or not s.is_contiguous():
+                raise ValueError(f"group {k}: expected a contiguous complex128 CUDA tensor {list(shape)}")
         return (c_void_p * len(states))(*[s.data_ptr() for s in states])
 
-    def rk4(self, states, dt: float, nsteps: int = 1):
-        """nsteps RK4 steps of every group, in place."""
+    def _step(self, fn, states, dt: float, nsteps: int):
         p = self._ptrs(states)
-        check(_lib.load().aeolus_ensemble_bve_rk4(self.handle, ctypes.cast(p, ctypes.POINTER(c_void_p)), float(dt),
-                                                  int(nsteps), c_void_p(self.work.data_ptr()), self.work.numel(),
-                                                  _stream(self.device)))
+        check(fn(self.handle, ctypes.cast(p, ctypes.POINTER(c_void_p)), float(dt), int(nsteps),
+                 c_void_p(self.work.data_ptr()), self.work.numel(), _stream(self.device)))
         return states
 
     def capture(self, states, dt: float, stream: torch.cuda.Stream | None = None):
@@ -94,7 +85,7 @@ class BarotropicEnsemble:
         return buf.value.decode()
 
     def close(self):
-        if self.handle:
+        if getattr(self, "handle", None):
             _lib.load().aeolus_ensemble_destroy(self.handle)
             self.handle = c_void_p()
 
@@ -103,3 +94,55 @@ class BarotropicEnsemble:
             self.close()
         except Exception:
             pass
+
+
+def _check_groups(models, batches):
+    if len(models) != len(batches) or not models:
+        raise ValueError("need one batch size per model")
+    return list(models), [int(b) for b in batches]
+
+
+class BarotropicEnsemble(_Ensemble):
+    """BVE groups; states [batch, L+1, L+1] per group."""
+
+    _fields = 1
+
+    def __init__(self, models, batches):
+        self.models, self.batches = _check_groups(models, batches)
+        self.device = self.models[0].f_lm.device
+        n = len(self.models)
+        plans = (c_void_p * n)(*[m._plan.handle.value for m in self.models])
+        bs = (c_int * n)(*self.batches)
+        prm = (_lib.BveParams * n)(*[_lib.BveParams(m.R, m.Omega, m.nu) for m in self.models])
+        self.handle = c_void_p()
+        check(_lib.load().aeolus_ensemble_create(n, ctypes.cast(plans, ctypes.POINTER(c_void_p)), bs, prm,
+                                                 byref(self.handle)))
+        self._finish_init()
+
+    def rk4(self, states, dt: float, nsteps: int = 1):
+        """nsteps RK4 steps of every group, in place."""
+        return self._step(_lib.load().aeolus_ensemble_bve_rk4, states, dt, nsteps)
+
+
+class ShallowWaterEnsemble(_Ensemble):
+    """SWE groups; states [batch, 3, L+1, L+1] per group (no in-step state
+    checks: the members' status bits are those of the single-model rk4)."""
+
+    _fields = 3
+
+    def __init__(self, models, batches):
+        self.models, self.batches = _check_groups(models, batches)
+        self.device = self.models[0]._plan.device
+        n = len(self.models)
+        plans = (c_void_p * n)(*[m._plan.handle.value for m in self.models])
+        bs = (c_int * n)(*self.batches)
+        prm = (_lib.SweParams * n)(*[_lib.SweParams(m.R, m.Omega, m.gravity, m.mean_depth, m.nu4)
+                                     for m in self.models])
+        self.handle = c_void_p()
+        check(_lib.load().aeolus_ensemble_create_swe(n, ctypes.cast(plans, ctypes.POINTER(c_void_p)), bs, prm,
+                                                     byref(self.handle)))
+        self._finish_init()
+
+    def rk4(self, states, dt: float, nsteps: int = 1):
+        """nsteps RK4 steps of every group, in place."""
+        return self._step(_lib.load().aeolus_ensemble_swe_rk4, states, dt, nsteps)

@@ -266,13 +266,15 @@ int aeolus_swe_invariants(aeolus_plan state_plan, const aeolus_swe_params* p,
                           const double* state, double* out, int batch,
                           void* work, size_t work_bytes, void* stream);
 
-/* ---- batched uneven ensembles (BVE) --------------------------------------
- * Groups of BVE members, each group on its own Gauss product-space plan
- * (any l_max; all plans on one device and one contraction precision),
- * advanced together: every RK4 stage launches each stage kernel once for all
- * groups.  The reference runs one state per process (run/bve/runner.py:
- * 211-216); this has no counterpart there.  zeta[g] is group g's device
- * state [batch_g][L_g+1][L_g+1], advanced in place. */
+/* ---- batched uneven ensembles (BVE and SWE) ------------------------------
+ * Groups of members, each group on its own Gauss product-space plan (any
+ * l_max; all plans on one device and one contraction precision), advanced
+ * together: every RK4 stage launches each stage kernel once for all groups.
+ * The reference runs one state per process (run/bve/runner.py:211-216,
+ * run/engine.py:406-431); this has no counterpart there.  State pointer g is
+ * group g's device state, advanced in place: BVE [batch_g][L_g+1][L_g+1],
+ * SWE [batch_g][3][L_g+1][L_g+1].  Capture, launch and autotune serve both
+ * models. */
 typedef struct aeolus_ensemble_s* aeolus_ensemble;
 
 int aeolus_ensemble_create(int ngroups, const aeolus_plan* plans,
@@ -281,6 +283,14 @@ int aeolus_ensemble_create(int ngroups, const aeolus_plan* plans,
 int aeolus_ensemble_destroy(aeolus_ensemble e);
 int aeolus_ensemble_workspace_bytes(aeolus_ensemble e, size_t* bytes);
 int aeolus_ensemble_bve_rk4(aeolus_ensemble e, double* const* zeta, double dt,
+                            int nsteps, void* work, size_t work_bytes,
+                            void* stream);
+/* Shallow-water ensemble: per-group SWE parameters; steps as aeolus_swe_rk4
+ * does for each group. */
+int aeolus_ensemble_create_swe(int ngroups, const aeolus_plan* plans,
+                               const int* batch, const aeolus_swe_params* params,
+                               aeolus_ensemble* out);
+int aeolus_ensemble_swe_rk4(aeolus_ensemble e, double* const* state, double dt,
                             int nsteps, void* work, size_t work_bytes,
                             void* stream);
 
