@@ -7,9 +7,10 @@ NumPy stand-in for CuPy in ``tests/golden/refshim``; its CUDA-C basis kernel
 Omega = 7.292e-5 1/s, as the workloads specify (``Planet.generate`` would
 derive different constants and random terrain).
 
-Run:  PYTHONDONTWRITEBYTECODE=1 python tests/golden/make_golden.py [vector]
+Run:  PYTHONDONTWRITEBYTECODE=1 python tests/golden/make_golden.py [vector|runs]
 Writes ``tests/golden/*.npz`` (with ``vector``: only the weak-form curl/div
-fixtures).  Only l_max <= 85 fixtures are made: above
+fixtures; with ``runs``: only the integration-engine events and the run
+capsules of the reference's BVE/SWE runners).  Only l_max <= 85 fixtures are made: above
 that the reference basis kernel underflows (l + m >= ~175) and is not a
 valid oracle.
 """
@@ -162,8 +163,177 @@ def main():
     vector_cases()
 
 
+# ----------------------------------------------------------- run driver
+def _events_hex(events):
+    return [[k, float(dt).hex(), float(t).hex()] for k, dt, t in events]
+
+
+def _outcome(fn, *a, **kw):
+    try:
+        return {"value": float(fn(*a, **kw)).hex()}
+    except Exception as exc:  # the reference's error contract is part of the pin
+        return {"raises": type(exc).__name__}
+
+
+def schedule_cases():
+    """Events of the reference's IntegrationScheduler (engine.py) for fixed and
+    state-adaptive ceilings, plus its schedule and CFL helpers' outcomes."""
+    import json
+    from planetary_sandbox.run import engine as E
+
+    cases = []
+
+    def plan(name, t_end, dt_cfl, **kw):
+        cases.append({"name": name, "kind": "plan", "t_end": t_end, "dt_cfl": dt_cfl, "kw": kw,
+                      "events": _events_hex(E.integration_plan(t_end, dt_cfl, **kw))})
+
+    plan("count_aligned", 3600.0, 600.0, mode="count", snapshot_times=E.count_snapshot_times(4, 3600.0))
+    plan("count_nonaligned", 1000.0, 300.0, mode="count", snapshot_times=E.count_snapshot_times(3, 1000.0))
+    plan("count_one", 1234.5, 500.0, mode="count", snapshot_times=E.count_snapshot_times(1, 1234.5))
+    plan("count_empty", 900.0, 400.0, mode="count", snapshot_times=[])
+    plan("count_thirds", 86400.0 / 3, 977.0, mode="count", snapshot_times=E.count_snapshot_times(7, 86400.0 / 3))
+    plan("interval_aligned", 3600.0, 500.0, mode="interval", dt_snapshots=1200.0)
+    plan("interval_nonaligned", 8640.0, 700.0, mode="interval", dt_snapshots=5000.0)
+    plan("interval_tolerance", 3600.0 + 1e-4, 450.0, mode="interval", dt_snapshots=900.0)
+    plan("interval_big_ceiling", 1000.0, 1e6, mode="interval", dt_snapshots=300.0)
+
+    def adaptive(name, t_end, speeds, length_scale, **kw):
+        sch = E.IntegrationScheduler(t_end, **kw)
+        events = []
+
+        def on_store(t):
+            events.append(("store", 0.0, t))
+
+        def on_step(t0, t1, dt, k):
+            events.append(("step", dt, t1))
+            return speeds[(k - 1) % len(speeds)]
+
+        dt0 = E.advective_cfl_timestep(length_scale, speeds[-1])
+        out = E.integrate(sch, dt0, length_scale, on_step=on_step, on_store=on_store)
+        cases.append({"name": name, "kind": "adaptive", "t_end": t_end, "speeds": speeds,
+                      "length_scale": length_scale, "kw": kw, "events": _events_hex(events),
+                      "final": [float(out[0]).hex(), out[1]]})
+
+    adaptive("adaptive_count", 7200.0, [35.0, 80.0, 20.0, 55.5], 6.2e5 / 4,
+             mode="count", snapshot_times=E.count_snapshot_times(5, 7200.0))
+    adaptive("adaptive_interval", 7200.0, [120.0, 300.0, 75.0], 2.0e5,
+             mode="interval", dt_snapshots=2500.0)
+    adaptive("adaptive_motionless", 2000.0, [0.0], 1.0e5, mode="count", snapshot_times=[0.0, 2000.0])
+    adaptive("adaptive_no_length_scale", 2000.0, [10.0], None, mode="interval", dt_snapshots=1000.0)
+
+    # A ceiling below one ulp of t cannot advance the clock: the planner raises.
+    sch = E.IntegrationScheduler(1.0e6, mode="count", snapshot_times=[5.0e5, 1.0e6])
+    seq = [5.0e5, 1e-12]
+    got = []
+    try:
+        for dt in [seq[0]] + [seq[1]] * 4:
+            got.append(sch.next_event(dt))
+        stagnation = "none"
+    except Exception as exc:
+        stagnation = type(exc).__name__
+    cases.append({"name": "count_stagnation", "kind": "stagnation", "raises": stagnation,
+                  "events": _events_hex([e for e in got if e is not None])})
+
+    helpers = {
+        "cfl": [[ls, sp, _outcome(E.advective_cfl_timestep, ls, sp)] for ls, sp in
+                [(6.2e5, 40.0), (None, 40.0), (0.0, 40.0), (6.2e5, 0.0), (1.0, 1e-300), (-1.0, 3.0),
+                 (6.2e5, -1.0), (6.2e5, float("nan")), (float("inf"), 3.0), (1e308, 1e-300)]],
+        "validate": [],
+        "interval_times": [[d, t, [float(x).hex() for x in E.interval_snapshot_times(d, t)]]
+                           for d, t in [(600.0, 3600.0), (700.0, 3600.0), (900.0, 3600.0 + 1e-4),
+                                        (1000.0, 999.9)]],
+        "count_times": [[n, t, [float(x).hex() for x in E.count_snapshot_times(n, t)]]
+                        for n, t in [(0, 100.0), (1, 100.0), (2, 100.0), (7, 86400.0 / 3)]],
+    }
+    for times, t_end in [([0.0, 50.0, 100.0], 100.0), ([-1e-8, 100.0 + 1e-8], 100.0), ([0.0, 0.0], 100.0),
+                         ([10.0, 5.0], 100.0), ([-1.0], 100.0), ([101.0], 100.0), ([float("nan")], 100.0),
+                         ([1.0], 0.0), ([1.0], float("inf"))]:
+        try:
+            helpers["validate"].append([times, t_end, {"value": [float(x).hex() for x in
+                                                                 E.validate_snapshot_schedule(times, t_end)]}])
+        except Exception as exc:
+            helpers["validate"].append([times, t_end, {"raises": type(exc).__name__}])
+    for bad in [float("nan"), 0.0, -5.0]:
+        try:
+            E.IntegrationScheduler(100.0, mode="count", snapshot_times=[100.0]).next_event(bad)
+            helpers.setdefault("bad_ceiling", []).append([bad, "none"])
+        except Exception as exc:
+            helpers.setdefault("bad_ceiling", []).append([bad, type(exc).__name__])
+    with open(HERE / "schedule_events.json", "w") as f:
+        json.dump({"source": "planetary_sandbox.run.engine (reference), made by make_golden.py runs",
+                   "cases": cases, "helpers": helpers}, f, indent=0, allow_nan=True)
+    print(f"schedule_events.json: {len(cases)} cases")
+
+
+def _csv_table(path):
+    import csv
+    with open(path) as f:
+        rows = list(csv.DictReader(f))
+    cols = list(rows[0].keys())
+    return np.array(cols), np.array([[float(r[c]) for c in cols] for r in rows], dtype=np.float64)
+
+
+def run_cases():
+    """The reference's own run_swe / run_bve (no figures) on small Gauss
+    planets, in count and interval mode; their capsule arrays and CSV rows."""
+    import tempfile
+    from planetary_sandbox.physics.shallow_water import ShallowWaterState
+    from planetary_sandbox.run.swe.runner import run_swe
+    from planetary_sandbox.run.bve.runner import run_bve
+
+    def swe(name, nlat, nlon, lmax, seed, t_end_days, **kw):
+        t0 = time.time()
+        p = latlon_planet(nlat, nlon, lmax)
+        state, depth = W.perturbed_williamson2(lmax, seed)
+        model = ShallowWaterModel(p, gravity=G, mean_depth=depth)
+        with tempfile.TemporaryDirectory() as d:
+            out = Path(d)
+            run_swe(model, ShallowWaterState(state.copy()), out_dir=out, t_end_days=t_end_days, plots=(), **kw)
+            cols, rows = _csv_table(out / "diagnostics" / "timeseries.csv")
+            np.savez_compressed(
+                HERE / f"{name}.npz", nlat=nlat, nlon=nlon, lmax=lmax, radius=R, omega=OMEGA, gravity=G,
+                mean_depth=depth, state0=state, t_end_days=t_end_days,
+                mode=kw["snapshot_mode"], snapshot_times=np.asarray(kw.get("snapshot_times") or [], np.float64),
+                dt_snapshots=np.float64(kw.get("dt_snapshots") or 0.0),
+                coeffs=np.load(out / "swe_coeffs.npy"), times=np.load(out / "swe_snapshot_times.npy"),
+                csv_cols=cols, csv_rows=rows)
+        print(f"{name}: {time.time() - t0:.1f}s, {rows.shape[0]} rows")
+
+    def bve(name, nlat, nlon, lmax, seed, nu, t_end_days, **kw):
+        t0 = time.time()
+        p = latlon_planet(nlat, nlon, lmax)
+        zeta = W.bve_vorticity(lmax, seed)
+        with tempfile.TemporaryDirectory() as d:
+            out = Path(d)
+            run_bve(p, zeta.copy(), out_dir=out, t_end_days=t_end_days, viscosity=nu, plots=(), **kw)
+            cols, rows = _csv_table(out / "diagnostics" / "timeseries.csv")
+            spec = np.load(out / "diagnostics" / "spectra.npz")
+            np.savez_compressed(
+                HERE / f"{name}.npz", nlat=nlat, nlon=nlon, lmax=lmax, radius=R, omega=OMEGA, nu=nu,
+                zeta0=zeta, t_end_days=t_end_days, mode=kw["snapshot_mode"],
+                snapshot_times=np.asarray(kw.get("snapshot_times") or [], np.float64),
+                dt_snapshots=np.float64(kw.get("dt_snapshots") or 0.0),
+                coeffs=np.load(out / "vorticity_coeffs.npy"), grid=np.load(out / "vorticity_grid.npy"),
+                times=np.load(out / "bve_snapshot_times.npy"), csv_cols=cols, csv_rows=rows,
+                spec_times=spec["times"], energy_l=spec["energy_l"], enstrophy_l=spec["enstrophy_l"])
+        print(f"{name}: {time.time() - t0:.1f}s, {rows.shape[0]} rows")
+
+    from planetary_sandbox.run import engine as E
+    t_end = 0.08
+    swe("run_swe_gauss32x64_L21_count", 32, 64, 21, 21, t_end, dt_snapshots=None,
+        snapshot_times=E.count_snapshot_times(4, t_end * 86400.0), snapshot_mode="count")
+    swe("run_swe_gauss16x32_L15_interval", 16, 32, 15, 23, 0.1, dt_snapshots=5000.0, snapshot_mode="interval")
+    bve("run_bve_gauss32x64_L21_count", 32, 64, 21, 0, 1e5, 3.0, dt_snapshots=None,
+        snapshot_times=E.count_snapshot_times(3, 3.0 * 86400.0), snapshot_mode="count")
+    bve("run_bve_gauss16x32_L15_interval", 16, 32, 15, 4, 0.0, 1.5, dt_snapshots=40000.0,
+        snapshot_mode="interval")
+
+
 if __name__ == "__main__":
     if sys.argv[1:] == ["vector"]:
         vector_cases()
+    elif sys.argv[1:] == ["runs"]:
+        schedule_cases()
+        run_cases()
     else:
         main()

@@ -1,0 +1,133 @@
+"""GPU runs of ``aeolus run bve|swe`` against the reference's own runners.
+
+The golden capsules (``tests/golden/run_*.npz``, made by
+``tests/golden/make_golden.py runs``) are what the reference's ``run_swe`` /
+``run_bve`` wrote for the same planets and initial states: the stored
+coefficient snapshots, their times, and every diagnostics row.  The GB300
+runner must store the same snapshots at bit-identical times, take the same
+number of steps, match the coefficients to 1e-12 relative L2 and every
+diagnostics column to 1e-10 of that column's scale (step lengths come from
+the state-adaptive CFL ceiling, so they carry the FP64 round-off of the
+characteristic speed).
+"""
+import numpy as np
+import pytest
+import torch
+
+from helpers import rel_l2, tri
+
+import aeolus_gb300 as ae
+from aeolus_gb300 import runner as RN
+from aeolus_gb300.shallow_water import ShallowWaterModel, ShallowWaterState, ShallowWaterStateError
+
+pytestmark = pytest.mark.gpu
+DEV = "cuda"
+COEFF_TOL = 1e-12
+ROW_TOL = 1e-10
+
+
+def _read_csv(path):
+    import csv
+    with open(path) as f:
+        rows = list(csv.DictReader(f))
+    return list(rows[0].keys()), np.array([[float(r[c]) for c in rows[0]] for r in rows])
+
+
+def _compare_rows(out_dir, g):
+    cols, rows = _read_csv(out_dir / "diagnostics" / "timeseries.csv")
+    assert cols == [str(c) for c in g["csv_cols"]]
+    ref = g["csv_rows"]
+    assert rows.shape == ref.shape
+    for j, c in enumerate(cols):
+        a, b = rows[:, j], ref[:, j]
+        assert np.array_equal(np.isnan(a), np.isnan(b)), c
+        ok = ~np.isnan(b)
+        scale = max(np.abs(b[ok]).max() if ok.any() else 0.0, 1e-300)
+        if c == "roundtrip_residual":
+            scale = 1.0            # a ~1e-15 residual: compare absolutely
+        assert np.all(np.abs(a[ok] - b[ok]) <= ROW_TOL * scale), (c, a, b)
+    assert np.array_equal(rows[:, cols.index("step")], ref[:, cols.index("step")])
+
+
+def _schedule(g):
+    mode = str(g["mode"])
+    if mode == "count":
+        return dict(snapshot_mode="count", snapshot_times=list(g["snapshot_times"]), dt_snapshots=None)
+    return dict(snapshot_mode="interval", dt_snapshots=float(g["dt_snapshots"]))
+
+
+@pytest.mark.parametrize("name", ["run_swe_gauss32x64_L21_count", "run_swe_gauss16x32_L15_interval"])
+def test_swe_run_matches_reference_runner(name, golden, tmp_path):
+    g = golden(name)
+    nlat, nlon, L = int(g["nlat"]), int(g["nlon"]), int(g["lmax"])
+    planet = ae.make_planet("latlon", nlat=nlat, nlon=nlon, l_max=L, device=DEV)
+    model = ShallowWaterModel(planet, gravity=float(g["gravity"]), mean_depth=float(g["mean_depth"]))
+    state0 = ShallowWaterState(torch.as_tensor(g["state0"], device=DEV))
+    RN.run_swe(model, state0, out_dir=tmp_path, t_end_days=float(g["t_end_days"]), plots=(), **_schedule(g))
+    times = np.load(tmp_path / "swe_snapshot_times.npy")
+    assert [t.hex() for t in times] == [t.hex() for t in g["times"]]
+    coeffs = np.load(tmp_path / "swe_coeffs.npy")
+    assert coeffs.shape == g["coeffs"].shape and coeffs.dtype == np.complex128
+    for k in range(coeffs.shape[0]):
+        assert rel_l2(tri(coeffs[k]), tri(g["coeffs"][k])) <= COEFF_TOL
+    _compare_rows(tmp_path, g)
+
+
+@pytest.mark.parametrize("name", ["run_bve_gauss32x64_L21_count", "run_bve_gauss16x32_L15_interval"])
+def test_bve_run_matches_reference_runner(name, golden, tmp_path):
+    g = golden(name)
+    nlat, nlon, L = int(g["nlat"]), int(g["nlon"]), int(g["lmax"])
+    planet = ae.make_planet("latlon", nlat=nlat, nlon=nlon, l_max=L, device=DEV)
+    RN.run_bve(planet, g["zeta0"], out_dir=tmp_path, t_end_days=float(g["t_end_days"]),
+               viscosity=float(g["nu"]), plots=(), **_schedule(g))
+    times = np.load(tmp_path / RN.BVE_SNAPSHOT_TIMES_FILENAME)
+    assert [t.hex() for t in times] == [t.hex() for t in g["times"]]
+    coeffs = np.load(tmp_path / "vorticity_coeffs.npy")
+    grid = np.load(tmp_path / "vorticity_grid.npy")
+    assert coeffs.shape == g["coeffs"].shape and grid.shape == g["grid"].shape
+    for k in range(coeffs.shape[0]):
+        assert rel_l2(tri(coeffs[k]), tri(g["coeffs"][k])) <= COEFF_TOL
+        assert rel_l2(grid[k], g["grid"][k]) <= COEFF_TOL
+    _compare_rows(tmp_path, g)
+    spec = np.load(tmp_path / "diagnostics" / "spectra.npz")
+    # record times of intermediate steps accumulate CFL step lengths: not bitwise
+    np.testing.assert_allclose(spec["times"], g["spec_times"], rtol=ROW_TOL, atol=0)
+    assert rel_l2(spec["energy_l"], g["energy_l"]) <= COEFF_TOL
+    assert rel_l2(spec["enstrophy_l"], g["enstrophy_l"]) <= COEFF_TOL
+
+
+def test_swe_run_aborts_on_invalid_state_and_keeps_rows(tmp_path):
+    """An invalid initial state is refused before any step; a state that
+    turns invalid mid-run (NaN injected on the host into the step result of
+    step 2) stops the run with ShallowWaterStateError naming the step, and
+    the rows written before it stay on disk."""
+    planet = ae.make_planet("latlon", nlat=16, nlon=32, l_max=10, device=DEV)
+    model = ShallowWaterModel(planet, gravity=9.80616, mean_depth=10.0)
+    bad = ShallowWaterState.zeros(10, device=DEV)
+    bad.coeffs[2, 2, 0] = -1.0e4          # Phi0 + phi < 0 near the poles
+    with pytest.raises(ShallowWaterStateError, match="initial state"):
+        RN.run_swe(model, bad, dt_snapshots=600.0, t_end_days=0.01, out_dir=tmp_path, plots=())
+    ok = ShallowWaterState.zeros(10, device=DEV)
+    ok.coeffs[0, 3, 1] = 2e-5
+    real_rk4, calls = model.rk4, []
+
+    def faulty_rk4(coeffs, dt, nsteps=1, check=True):
+        calls.append(dt)
+        y = real_rk4(coeffs, dt, nsteps, check)
+        return y * float("nan") if len(calls) == 2 else y
+
+    model.rk4 = faulty_rk4
+    with pytest.raises(ShallowWaterStateError, match=r"NaN/Inf.*\(step 2\)"):
+        RN.run_swe(model, ok, dt_snapshots=3600.0, t_end_days=1.0, out_dir=tmp_path, plots=())
+    cols, rows = _read_csv(tmp_path / "diagnostics" / "timeseries.csv")
+    assert rows[:, cols.index("step")].tolist() == [0.0, 1.0]
+
+
+def test_empty_count_schedule_writes_empty_stacks(tmp_path):
+    planet = ae.make_planet("latlon", nlat=16, nlon=32, l_max=10, device=DEV)
+    z = np.zeros((11, 11), complex)
+    z[3, 1] = 1e-5
+    RN.run_bve(planet, z, None, 0.05, tmp_path, 0.0, snapshot_times=[], snapshot_mode="count", plots=())
+    assert np.load(tmp_path / "vorticity_coeffs.npy").shape == (0, 11, 11)
+    assert np.load(tmp_path / "vorticity_grid.npy").shape[0] == 0
+    assert np.load(tmp_path / RN.BVE_SNAPSHOT_TIMES_FILENAME).shape == (0,)
