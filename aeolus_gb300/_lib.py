@@ -60,6 +60,9 @@ SIGNATURES = {
     "aeolus_vector_curl_div": (c_int, [c_void_p, c_double, c_void_p, c_void_p, c_void_p, c_int, c_int, c_void_p,
                                        c_size_t, c_void_p]),
     "aeolus_synthesize_noalloc": (c_int, [c_void_p, c_void_p, c_void_p, c_int, c_void_p]),
+    "aeolus_geodesic_sizes": (c_int, [c_int, POINTER(c_long), POINTER(c_long), POINTER(c_size_t)]),
+    "aeolus_geodesic_build": (c_int, [c_int, c_double, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p,
+                                      c_void_p, c_void_p, c_size_t, c_void_p]),
     "aeolus_spectral_op": (c_int, [c_int, c_int, c_double, c_void_p, c_void_p, c_int, c_void_p]),
     "aeolus_jacobian": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p, c_int, c_void_p, c_size_t, c_void_p]),
     "aeolus_winds": (c_int, [c_void_p, c_double, c_void_p, c_void_p, c_void_p, c_int, c_void_p, c_size_t,

@@ -4,8 +4,8 @@ Mirrors src/planetary_sandbox/numerics/geodesic_grid.py (geometry, point
 order, Voronoi areas), numerics/fast_geodesic_sh.py
 (``PointSetSphericalHarmonics``) and numerics/optimized_geodesic_sh.py
 (``GeodesicSphericalHarmonics`` with "voronoi" / "uniform" / explicit
-weights).  The geometry is built on the host with vectorised NumPy; the
-transform is a dense real basis built and contracted on the device
+weights).  The geometry is built on the device (``csrc/geodesic.cu``); the transform
+is a dense real basis built and contracted on the device
 (``csrc/points.cu``).
 """
 from __future__ import annotations
@@ -15,70 +15,35 @@ import warnings
 import numpy as np
 import torch
 
-from .ops import Plan, analyze, synthesize
-
-_PHI = (1.0 + np.sqrt(5.0)) / 2.0
-# Icosahedron, geodesic_grid.py:15-28 (the point order depends on it).
-_ICO_V = np.array([[-1, _PHI, 0], [1, _PHI, 0], [-1, -_PHI, 0], [1, -_PHI, 0],
-                   [0, -1, _PHI], [0, 1, _PHI], [0, -1, -_PHI], [0, 1, -_PHI],
-                   [_PHI, 0, -1], [_PHI, 0, 1], [-_PHI, 0, -1], [-_PHI, 0, 1]]) / np.hypot(1, _PHI)
-_ICO_F = np.array([[0, 11, 5], [0, 5, 1], [0, 1, 7], [0, 7, 10], [0, 10, 11],
-                   [1, 5, 9], [5, 11, 4], [11, 10, 2], [10, 7, 6], [7, 1, 8],
-                   [3, 9, 4], [3, 4, 2], [3, 2, 6], [3, 6, 8], [3, 8, 9],
-                   [4, 9, 5], [2, 4, 11], [6, 2, 10], [8, 6, 7], [9, 8, 1]])
+from .ops import Plan, analyze, geodesic_build, synthesize
 
 MIN_POINTS_PER_BASIS = 6  # optimized_geodesic_sh.py:23
 
 
-def _subdivide_once(verts: np.ndarray, faces: np.ndarray):
-    """One midpoint refinement; new vertices numbered in order of first use
-    by (face, edge 12 / 23 / 31), the order of geodesic_grid.py:116-131."""
-    e = np.stack([faces[:, [0, 1]], faces[:, [1, 2]], faces[:, [2, 0]]], axis=1).reshape(-1, 2)
-    key = np.sort(e, axis=1)
-    code = key[:, 0].astype(np.int64) * (len(verts) + 1) + key[:, 1]
-    uniq, first, inv = np.unique(code, return_index=True, return_inverse=True)
-    order = np.argsort(first, kind="stable")          # first-appearance order
-    rank = np.empty_like(order)
-    rank[order] = np.arange(order.size)
-    mid_id = len(verts) + rank[inv].reshape(-1, 3)      # m12, m23, m31 per face
-    a, b = key[first[order], 0], key[first[order], 1]
-    mid = (verts[a] + verts[b]) / 2.0
-    mid /= np.linalg.norm(mid, axis=1)[:, None]
-    v1, v2, v3 = faces[:, 0], faces[:, 1], faces[:, 2]
-    m12, m23, m31 = mid_id[:, 0], mid_id[:, 1], mid_id[:, 2]
-    nf = np.stack([np.stack([v1, m12, m31], 1), np.stack([v2, m23, m12], 1),
-                   np.stack([v3, m31, m23], 1), np.stack([m12, m23, m31], 1)], axis=1).reshape(-1, 3)
-    return np.concatenate([verts, mid]), nf
-
-
 class GeodesicGridGeometry:
-    """Icosahedral geodesic grid, geodesic_grid.py:11-266."""
+    """Icosahedral geodesic grid, geodesic_grid.py:11-266, built on the
+    device (``aeolus_geodesic_build``): the subdivision keeps the reference's
+    point and face order, the cell areas are its barycentric "Voronoi"
+    areas.  ``points`` and ``faces`` are also kept as host arrays, as the
+    reference exposes them."""
 
     def __init__(self, resolution: int = 0, radius: float = 1.0, device=None):
         self.resolution = int(resolution)
         self.radius = float(radius)
         self.device = torch.device(device) if device is not None else torch.device("cuda")
-        c, s = np.cos(1e-2), np.sin(1e-2)                     # :37-38 rotation about x
-        rot = np.array([[1.0, 0.0, 0.0], [0.0, c, -s], [0.0, s, c]])
-        verts, faces = _ICO_V @ rot.T, _ICO_F.copy()
-        for _ in range(self.resolution):
-            verts, faces = _subdivide_once(verts, faces)
-        self.points = self.radius * verts
-        self.faces = faces.astype(np.int32)
+        g = geodesic_build(self.resolution, self.radius, self.device)
+        self.points = g["points"].cpu().numpy()
+        self.faces = g["faces"].cpu().numpy()
         self.n_points = len(self.points)
         self.n_faces = len(self.faces)
-        x, y, z = self.points[:, 0], self.points[:, 1], self.points[:, 2]
-        self._lat_np = np.arctan2(z, np.hypot(x, y))            # cartesian_to_spherical.py
-        self._lon_np = np.arctan2(y, x)
-        edges = np.concatenate([faces[:, [0, 1]], faces[:, [1, 2]], faces[:, [2, 0]]])
-        d = np.linalg.norm(self.points[edges[:, 0]] - self.points[edges[:, 1]], axis=1)
-        self.min_edge_length = float(d[d > 0].min()) if np.any(d > 0) else 0.0
-        dev = self.device
-        self.latitudes = torch.from_numpy(self._lat_np).to(dev)
-        self.longitudes = torch.from_numpy(self._lon_np).to(dev)
+        self.min_edge_length = g["min_edge"]
+        self.latitudes = g["lat"]
+        self.longitudes = g["lon"]
+        self._lat_np = self.latitudes.cpu().numpy()
+        self._lon_np = self.longitudes.cpu().numpy()
         self.sinlat = torch.sin(self.latitudes)
         self.coslat = torch.cos(self.latitudes)
-        self._cell_areas = None
+        self._cell_areas = g["areas"]
 
     point_latitudes = property(lambda self: self.latitudes)
     point_longitudes = property(lambda self: self.longitudes)
@@ -92,24 +57,9 @@ class GeodesicGridGeometry:
 
     @property
     def cell_areas(self) -> torch.Tensor:
-        """Barycentric 'Voronoi' areas: 1/3 of each spherical triangle
-        (L'Huilier excess), geodesic_grid.py:200-266."""
-        if self._cell_areas is None:
-            self._cell_areas = torch.from_numpy(self.voronoi_areas_np()).to(self.device)
+        """Barycentric 'Voronoi' areas (1/3 of each spherical triangle,
+        L'Huilier excess), geodesic_grid.py:200-266."""
         return self._cell_areas
-
-    def voronoi_areas_np(self) -> np.ndarray:
-        u = self.points / np.linalg.norm(self.points, axis=1)[:, None]
-        f = self.faces
-        a, b, c = u[f[:, 0]], u[f[:, 1]], u[f[:, 2]]
-        ang = lambda p, q: np.arccos(np.clip(np.einsum("ij,ij->i", p, q), -1.0, 1.0))  # noqa: E731
-        sa, sb, sc = ang(b, c), ang(a, c), ang(a, b)
-        s = 0.5 * (sa + sb + sc)
-        t = np.sqrt(np.tan(s / 2) * np.tan((s - sa) / 2) * np.tan((s - sb) / 2) * np.tan((s - sc) / 2))
-        area = 4.0 * np.arctan(t) * self.radius ** 2 / 3.0
-        out = np.zeros(self.n_points)
-        np.add.at(out, f.ravel(), np.repeat(area, 3))
-        return out
 
 
 def _warn_if_underresolved(n_points: int, l_max: int):
@@ -192,8 +142,8 @@ class GeodesicSphericalHarmonics:
             if isinstance(weights, str):
                 mode = weights.lower()
                 if mode == "voronoi":
-                    a = grid.voronoi_areas_np() / grid.radius ** 2
-                    w = a * (4.0 * np.pi) / np.sum(a)
+                    a = grid.cell_areas / grid.radius ** 2          # optimized_geodesic_sh.py:127-133
+                    w = a * (4.0 * np.pi) / torch.sum(a)
                 elif mode == "optimize":
                     raise ValueError("weights='optimize' (host least-squares fitting) is not available on the "
                                      "GB300 path; use 'voronoi', 'uniform' or explicit weights")

@@ -118,6 +118,31 @@ class Plan:
             pass
 
 
+def geodesic_build(resolution: int, radius: float = 1.0, device=None) -> dict:
+    """Icosahedral geodesic point set built on the device by
+    ``aeolus_geodesic_build`` (geodesic_grid.py:31-266): points, faces,
+    lat/lon, barycentric cell areas and the minimum edge length."""
+    device = torch.device(device or "cuda")
+    lib = _lib.load()
+    nv, nf, nb = c_long(), c_long(), c_size_t()
+    check(lib.aeolus_geodesic_sizes(int(resolution), byref(nv), byref(nf), byref(nb)))
+    f64 = dict(dtype=torch.float64, device=device)
+    with torch.cuda.device(device):
+        pts = torch.empty((nv.value, 3), **f64)
+        faces = torch.empty((nf.value, 3), dtype=torch.int32, device=device)
+        lat, lon, areas = (torch.empty(nv.value, **f64) for _ in range(3))
+        min_edge = torch.empty(1, **f64)
+        status = torch.zeros(1, dtype=torch.int32, device=device)
+        work = torch.empty(max(nb.value, 1), dtype=torch.uint8, device=device)
+        check(lib.aeolus_geodesic_build(int(resolution), float(radius), _ptr(pts), _ptr(faces), _ptr(lat), _ptr(lon),
+                                        _ptr(areas), _ptr(min_edge), _ptr(status), _ptr(work), nb.value,
+                                        _stream(device)))
+    if int(status.item()) != 0:
+        raise RuntimeError("geodesic build: a vertex has more than 6 incident faces")
+    return {"points": pts, "faces": faces, "lat": lat, "lon": lon, "areas": areas,
+            "min_edge": float(min_edge.item())}
+
+
 def _spec_shape(L: int):
     return (L + 1, L + 1)
 

@@ -193,6 +193,27 @@ int aeolus_vector_curl_div(aeolus_plan plan_ext, double radius, const double* f_
                            double* div, int batch, int truncate, void* work, size_t work_bytes,
                            void* stream);
 
+/* ---- icosahedral geodesic point set (numerics/geodesic_grid.py) -------- */
+
+/* Point, face and workspace counts of a geodesic point set with
+ * `resolution` midpoint subdivisions (0..9): n_points = 10 * 4^r + 2,
+ * n_faces = 20 * 4^r.  Host only (no device work). */
+int aeolus_geodesic_sizes(int resolution, long* n_points, long* n_faces, size_t* work_bytes);
+
+/* Builds the point set on the device, replacing the host construction of
+ * geodesic_grid.py:31-266 (icosahedron rotated 1e-2 rad about x, midpoint
+ * subdivision in the reference's point and face order, :103-160;
+ * cartesian_to_spherical.py coordinates; min edge length, :162-190;
+ * barycentric "Voronoi" areas, one third of each L'Huilier triangle,
+ * :212-266).  Outputs (device, caller-owned): points [n_points][3] scaled
+ * by radius, faces [n_faces][3] int32, lat / lon [n_points] (lon in
+ * [-pi, pi]), areas [n_points] in radius^2 units, min_edge [1], status [1]
+ * int32 (nonzero: a vertex had more than 6 incident faces, which a valid
+ * subdivision never produces).  Workspace from aeolus_geodesic_sizes. */
+int aeolus_geodesic_build(int resolution, double radius, double* points, int* faces, double* lat,
+                          double* lon, double* areas, double* min_edge, int* status, void* work,
+                          size_t work_bytes, void* stream);
+
 /* ---- spectral operators (numerics/spectral_operators.py) -------------- */
 
 /* op: 0 laplacian (:213-218), 1 inverse laplacian with l=0 -> l=0 * R^2

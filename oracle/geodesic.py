@@ -43,7 +43,9 @@ def subdivide(resolution: int):
             if key in mid:
                 return mid[key]
             p = (verts[a] + verts[b]) / 2.0
-            verts.append(p / np.linalg.norm(p))
+            # normalize() of geodesic_grid.py:9: the axis form sums x*x + y*y
+            # + z*z in order (the axis-free norm would go through a BLAS dot)
+            verts.append(p / np.linalg.norm(p, axis=-1)[..., None])
             mid[key] = len(verts) - 1
             return mid[key]
 

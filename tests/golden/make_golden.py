@@ -7,7 +7,7 @@ NumPy stand-in for CuPy in ``tests/golden/refshim``; its CUDA-C basis kernel
 Omega = 7.292e-5 1/s, as the workloads specify (``Planet.generate`` would
 derive different constants and random terrain).
 
-Run:  PYTHONDONTWRITEBYTECODE=1 python tests/golden/make_golden.py [vector|runs]
+Run:  PYTHONDONTWRITEBYTECODE=1 python tests/golden/make_golden.py [vector|runs|geodesic_fine]
 Writes ``tests/golden/*.npz`` (with ``vector``: only the weak-form curl/div
 fixtures; with ``runs``: only the integration-engine events and the run
 capsules of the reference's BVE/SWE runners).  Only l_max <= 85 fixtures are made: above
@@ -51,11 +51,11 @@ def latlon_planet(nlat, nlon, lmax, mode="fine"):
     return SimpleNamespace(sh=sh, so=so, grid=grid, params=params)
 
 
-def geodesic_planet(res, lmax):
+def geodesic_planet(res, lmax, mode="coarse"):
     grid = N.GeodesicGridGeometry(res, R)
     sh = N.GeodesicSphericalHarmonics(grid, lmax, weights="voronoi")
     backend = N.GeodesicBackend(grid, sh)
-    so = N.SpectralOperators(sh, R, grid, product_quadrature="coarse", backend=backend)
+    so = N.SpectralOperators(sh, R, grid, product_quadrature=mode, backend=backend)
     params = SimpleNamespace(radius=R, angular_velocity=OMEGA)
     return SimpleNamespace(sh=sh, so=so, grid=grid, params=params)
 
@@ -145,6 +145,30 @@ def vector_case(name, planet, seed):
     print(f"{name}: {time.time() - t0:.1f}s")
 
 
+def geodesic_fine_case(name, res, lmax, seed=19, dt=600.0):
+    """BVE and SWE on a geodesic planet whose product space is the reference's
+    'fine' co-grid (resolution res+1, Voronoi weights)."""
+    t0 = time.time()
+    p = geodesic_planet(res, lmax, mode="fine")
+    ps = p.so.backend.product_space("fine")
+    zeta = W.bve_vorticity(lmax, seed)
+    bve = BarotropicVorticity(p, viscosity=1e5)
+    bve_t = bve.tendency(BarotropicState(zeta.copy()), None)
+    bve_y = rk4_step(bve, BarotropicState(zeta.copy()), 0.0, dt).coeffs
+    state, depth = W.perturbed_williamson2(lmax, seed + 1)
+    swe = ShallowWaterModel(p, gravity=G, mean_depth=depth)
+    swe_t = swe.tendency(state.copy())
+    swe_y = rk4_step_array(swe.tendency, state.copy(), 0.0, dt)
+    np.savez_compressed(
+        HERE / f"{name}.npz", res=res, lmax=lmax, dt=dt, radius=R, omega=OMEGA, gravity=G, mean_depth=depth,
+        fine_lat=np.asarray(ps.sh.latitudes), fine_lon=np.asarray(ps.sh.longitudes),
+        fine_weights=np.asarray(ps.sh.weights), zeta=zeta, bve_tendency=bve_t, bve_rk4=bve_y,
+        state=state, swe_tendency=swe_t, swe_rk4=swe_y,
+        phi_extrema=np.array(swe.total_geopotential_extrema(SimpleNamespace(coeffs=state))),
+        cfl_length_scale=np.float64(p.grid.cfl_length_scale))
+    print(f"{name}: {time.time() - t0:.1f}s")
+
+
 def vector_cases():
     vector_case("vector_gauss16x32_L15_fine23x46", latlon_planet(16, 32, 15), seed=13)
     vector_case("vector_geodesic_res3_L10", geodesic_planet(3, 10), seed=17)
@@ -160,6 +184,7 @@ def main():
     # Shallow-water workload grid: Gauss 128x256, l_max=85.
     swe_case("swe_gauss128x256_L85", 128, 256, 85, seed=2, dt=300.0)
     geodesic_case("geodesic_res3_L10", 3, 10)
+    geodesic_fine_case("geodesic_fine_res3_L10", 3, 10)
     vector_cases()
 
 
@@ -332,6 +357,8 @@ def run_cases():
 if __name__ == "__main__":
     if sys.argv[1:] == ["vector"]:
         vector_cases()
+    elif sys.argv[1:] == ["geodesic_fine"]:
+        geodesic_fine_case("geodesic_fine_res3_L10", 3, 10)
     elif sys.argv[1:] == ["runs"]:
         schedule_cases()
         run_cases()

@@ -314,6 +314,32 @@ def test_geodesic_golden(golden):
     assert rel_l2(N(model.tendency(BarotropicState(T(g["zeta"])))), g["bve_tendency"]) < TOL
 
 
+def test_geodesic_fine_cogrid_golden(golden):
+    """Geodesic BVE and SWE with products on the resolution r+1 co-grid
+    (the reference's 'fine' geodesic product space): tendencies, RK4 steps,
+    co-grid points/weights and geopotential extrema over both samplings."""
+    g = golden("geodesic_fine_res3_L10")
+    planet = ae.make_planet("geodesic", resolution=int(g["res"]), l_max=int(g["lmax"]),
+                            product_quadrature="fine")
+    ps = planet.so.backend.product_space("fine")
+    assert ps.sh.latitudes.numel() == g["fine_lat"].size
+    np.testing.assert_allclose(N(ps.sh.latitudes), g["fine_lat"], rtol=0, atol=1e-14)
+    np.testing.assert_allclose(N(ps.sh.longitudes), g["fine_lon"], rtol=0, atol=1e-14)
+    np.testing.assert_allclose(N(ps.sh.weights), g["fine_weights"], rtol=1e-12)
+    assert planet.grid.cfl_length_scale == pytest.approx(float(g["cfl_length_scale"]), rel=1e-14)
+    dt = float(g["dt"])
+    bve = BarotropicVorticity(planet, viscosity=1e5)
+    z = T(g["zeta"])
+    assert rel_l2(tri(N(bve.tendency(BarotropicState(z)))), tri(g["bve_tendency"])) < TOL
+    assert rel_l2(tri(N(bve.rk4(z, dt, 1))), tri(g["bve_rk4"])) < TOL
+    swe = ShallowWaterModel(planet, gravity=float(g["gravity"]), mean_depth=float(g["mean_depth"]))
+    s0 = T(g["state"])
+    assert rel_l2(tri(N(swe.tendency(s0))), tri(g["swe_tendency"])) < TOL
+    assert rel_l2(tri(N(swe.rk4(s0, dt, 1))), tri(g["swe_rk4"])) < TOL
+    np.testing.assert_allclose(swe.total_geopotential_extrema(ShallowWaterState(s0)), g["phi_extrema"],
+                               rtol=1e-13)
+
+
 def test_point_set_batch_matches_oracle():
     rng = np.random.default_rng(8)
     lat = np.arcsin(rng.uniform(-1, 1, 3000))

@@ -1,6 +1,7 @@
 """CPU-only checks: the C-ABI library loads and exports every declared
 symbol, the ctypes table matches the header, and host-side geometry and
 workload generators agree with the oracle."""
+import ctypes
 import re
 from pathlib import Path
 
@@ -9,7 +10,6 @@ import pytest
 
 import oracle
 from aeolus_gb300 import _lib, workloads
-from aeolus_gb300.geodesic_grid import _ICO_F, _ICO_V, _subdivide_once
 from aeolus_gb300.latlon_grid import fine_dims
 
 HEADER = Path(__file__).resolve().parents[1] / "include" / "aeolus_gb300.h"
@@ -46,17 +46,26 @@ def test_bad_arguments_rejected_without_gpu():
         _lib.check(_lib.ERR_ARG)
 
 
-@pytest.mark.parametrize("res", [0, 1, 2, 3])
-def test_geodesic_point_order_matches_oracle(res):
-    c, s = np.cos(1e-2), np.sin(1e-2)
-    rot = np.array([[1.0, 0.0, 0.0], [0.0, c, -s], [0.0, s, c]])
-    v, f = _ICO_V @ rot.T, _ICO_F.copy()
-    for _ in range(res):
-        v, f = _subdivide_once(v, f)
-    ov, of = oracle.geodesic.subdivide(res)
-    np.testing.assert_array_equal(f, of)
-    np.testing.assert_allclose(v, ov, rtol=0, atol=1e-15)
-    assert len(v) == 10 * 4 ** res + 2
+def test_geodesic_sizes_and_argument_checks():
+    """Counts of the device geodesic build (host only) and its refusals
+    before any launch."""
+    lib = _lib.load()
+    nv, nf, nb = ctypes.c_long(), ctypes.c_long(), ctypes.c_size_t()
+    for r in range(0, 10):
+        assert lib.aeolus_geodesic_sizes(r, ctypes.byref(nv), ctypes.byref(nf), ctypes.byref(nb)) == _lib.OK
+        assert nv.value == 10 * 4 ** r + 2 and nf.value == 20 * 4 ** r
+        assert nb.value >= 4 * 3 * nf.value * 3
+        ov, of = oracle.geodesic.subdivide(min(r, 2)) if r <= 2 else (None, None)
+        if ov is not None:
+            assert (len(ov), len(of)) == (nv.value, nf.value)
+    for bad in (-1, 10):
+        assert lib.aeolus_geodesic_sizes(bad, None, None, None) == _lib.ERR_ARG
+        assert b"resolution" in lib.aeolus_last_error()
+    lib.aeolus_geodesic_sizes(3, None, None, ctypes.byref(nb))
+    dummy = ctypes.c_void_p(16)  # never dereferenced: every call below is refused first
+    assert lib.aeolus_geodesic_build(3, -1.0, *[dummy] * 7, dummy, nb.value, None) == _lib.ERR_ARG
+    assert lib.aeolus_geodesic_build(3, 1.0, None, *[dummy] * 6, dummy, nb.value, None) == _lib.ERR_ARG
+    assert lib.aeolus_geodesic_build(3, 1.0, *[dummy] * 7, dummy, nb.value - 1, None) == _lib.ERR_WORKSPACE
 
 
 def test_fine_dims_rule():

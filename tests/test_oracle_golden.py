@@ -80,6 +80,27 @@ def test_geodesic_golden(golden):
     assert rel_l2(t, g["bve_tendency"]) < TOL
 
 
+def test_geodesic_fine_cogrid_golden(golden):
+    """Geodesic planet whose products are formed on the resolution r+1
+    co-grid (spherical_backend.py:159-168): BVE and SWE tendencies and RK4
+    steps of the reference, restated."""
+    g = golden("geodesic_fine_res3_L10")
+    res, L, R = int(g["res"]), int(g["lmax"]), float(g["radius"])
+    lat, lon, w = oracle.geodesic.geodesic_point_set(res, R)
+    flat, flon, fw = oracle.geodesic.geodesic_point_set(res + 1, R)
+    np.testing.assert_allclose(flat, g["fine_lat"], rtol=0, atol=1e-14)
+    np.testing.assert_allclose(flon, g["fine_lon"], rtol=0, atol=1e-14)
+    np.testing.assert_allclose(fw, g["fine_weights"], rtol=1e-12)
+    sh = oracle.PointSetSH(lat, lon, L, weights=w)
+    ops = oracle.Operators(sh, R, sh_p=oracle.PointSetSH(flat, flon, L, weights=fw))
+    om, dt = float(g["omega"]), float(g["dt"])
+    assert rel_l2(models.bve_tendency(ops, g["zeta"], om, 1e5), g["bve_tendency"]) < TOL
+    assert rel_l2(models.bve_rk4_step(ops, g["zeta"], dt, om, 1e5), g["bve_rk4"]) < TOL
+    m = models.SWE(ops, om, float(g["gravity"]), float(g["mean_depth"]))
+    assert rel_l2(m.tendency(g["state"]), g["swe_tendency"]) < TOL
+    assert rel_l2(models.rk4_step_array(m.tendency, g["state"], dt), g["swe_rk4"]) < TOL
+
+
 def test_factored_equals_dense():
     """GaussSH (Legendre + DFT) equals PointSetSH (reference dense form)."""
     rng = np.random.default_rng(1)
