@@ -31,6 +31,10 @@ class BveParams(ctypes.Structure):
     _fields_ = [("radius", c_double), ("omega", c_double), ("viscosity", c_double)]
 
 
+class PeParams(ctypes.Structure):
+    _fields_ = [("radius", c_double), ("omega", c_double), ("r_dry", c_double), ("cp_dry", c_double)]
+
+
 class SweParams(ctypes.Structure):
     _fields_ = [("radius", c_double), ("omega", c_double), ("gravity", c_double),
                 ("mean_depth", c_double), ("nu4", c_double)]
@@ -60,6 +64,11 @@ SIGNATURES = {
     "aeolus_vector_curl_div": (c_int, [c_void_p, c_double, c_void_p, c_void_p, c_void_p, c_int, c_int, c_void_p,
                                        c_size_t, c_void_p]),
     "aeolus_synthesize_noalloc": (c_int, [c_void_p, c_void_p, c_void_p, c_int, c_void_p]),
+    "aeolus_pe_derive": (c_int, [c_void_p, POINTER(PeParams), c_int, c_void_p, c_void_p, c_int, c_void_p]),
+    "aeolus_pe_columns": (c_int, [c_void_p, POINTER(PeParams), c_int, c_void_p, c_void_p, c_void_p, c_void_p, c_int,
+                                  c_void_p]),
+    "aeolus_pe_spectral": (c_int, [c_int, POINTER(PeParams), c_int, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p,
+                                   c_void_p, c_void_p, c_int, c_void_p]),
     "aeolus_geodesic_sizes": (c_int, [c_int, POINTER(c_long), POINTER(c_long), POINTER(c_size_t)]),
     "aeolus_geodesic_build": (c_int, [c_int, c_double, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p,
                                       c_void_p, c_void_p, c_size_t, c_void_p]),

@@ -1,0 +1,290 @@
+// Dry hydrostatic primitive-equation tendency in sigma coordinates,
+// src/planetary_sandbox/physics/primitive_equations.py:482-753 with the
+// column operators of physics/sigma_coordinate.py:164-398, batched over
+// levels and members on the library's transforms:
+//
+//   aeolus_pe_derive    spectral: per level u cos, v cos (from the inverse
+//                       Laplacians of zeta, delta), zeta, delta, T, dT/dlambda,
+//                       sin(theta) dT/dtheta / R, the same two of eta = zeta + f,
+//                       eta; per member the two derivatives of ln p_s
+//   (synthesis of all 10 K + 2 fields on the product plan)
+//   aeolus_pe_columns   pointwise, one thread per product point and member,
+//                       the whole column in registers: G = delta + V.grad ln p_s,
+//                       d ln p_s/dt, interface sigma_dot, omega/p, centred
+//                       vertical advection of u, v, T; the thermodynamic
+//                       integrand, -div(eta V), curl(eta V), kinetic energy, and
+//                       the residual vector Z = sigma_dot dV/dsigma + R_d T grad ln p_s
+//   (analysis of the 4 K + 1 integrands; weak-form curl/div of Z on the
+//   one-degree-extended plan)
+//   aeolus_pe_spectral  spectral: 2/3 cuts, Simmons-Burridge geopotential of
+//                       the spectral T, -lap(KE + Phi), l = 0 rows of the
+//                       momentum tendencies pinned.
+#include "models.cuh"
+
+namespace aeolus {
+namespace {
+
+constexpr int kPeMaxLevels = 64;
+constexpr int kPeLevelFields = 10;  // U, V, zeta, delta, T, T_lam, T_snt, eta_lam, eta_snt, eta
+constexpr int kPeOutFields = 4;     // thermodynamic integrand, -div(eta V), curl(eta V), KE
+
+// Lorenz sigma grid, sigma_coordinate.py:43-149: interfaces s[0] = 0 (top)
+// .. s[K] = 1 (surface), thickness, interface log ratios beta (beta[0], the
+// infinite top entry, is never read) and the Simmons-Burridge alpha.
+struct PeSigma {
+  int K;
+  double s[kPeMaxLevels + 1], dsig[kPeMaxLevels], beta[kPeMaxLevels], alpha[kPeMaxLevels];
+};
+
+int make_sigma(const double* interfaces, int nlev, PeSigma* g) {
+  if (nlev < 1 || nlev > kPeMaxLevels)
+    return fail(AEOLUS_ERR_ARG, "nlev must be in [1, " + std::to_string(kPeMaxLevels) + "], got " +
+                                    std::to_string(nlev));
+  if (!interfaces) return fail(AEOLUS_ERR_ARG, "NULL sigma interfaces");
+  if (interfaces[0] != 0.0 || interfaces[nlev] != 1.0)
+    return fail(AEOLUS_ERR_ARG, "sigma interfaces must start at exactly 0.0 and end at exactly 1.0");
+  g->K = nlev;
+  for (int k = 0; k <= nlev; ++k) {
+    if (!std::isfinite(interfaces[k]) || (k > 0 && !(interfaces[k] > interfaces[k - 1])))
+      return fail(AEOLUS_ERR_ARG, "sigma interfaces must be finite and strictly increasing");
+    g->s[k] = interfaces[k];
+  }
+  for (int k = 0; k < nlev; ++k) g->dsig[k] = g->s[k + 1] - g->s[k];
+  g->beta[0] = 0.0;
+  g->alpha[0] = std::log(2.0);
+  for (int k = 1; k < nlev; ++k) {
+    g->beta[k] = std::log(g->s[k + 1] / g->s[k]);
+    g->alpha[k] = 1.0 - (g->s[k] / g->dsig[k]) * g->beta[k];
+  }
+  return AEOLUS_OK;
+}
+
+int pe_check(const aeolus_pe_params* prm) {
+  if (!prm) return fail(AEOLUS_ERR_ARG, "NULL primitive-equation parameters");
+  if (!(std::isfinite(prm->radius) && prm->radius > 0) || !std::isfinite(prm->omega))
+    return fail(AEOLUS_ERR_ARG, "primitive equations: bad radius/omega");
+  if (!(std::isfinite(prm->r_dry) && prm->r_dry > 0))
+    return fail(AEOLUS_ERR_ARG, "r_dry must be finite and > 0, got " + std::to_string(prm->r_dry));
+  if (!(std::isfinite(prm->cp_dry) && prm->cp_dry > prm->r_dry))
+    return fail(AEOLUS_ERR_ARG, "cp_dry must be finite and > r_dry, got " + std::to_string(prm->cp_dry));
+  return AEOLUS_OK;
+}
+
+// One thread per (member, l, m): every level's derived spectra.
+__global__ void pe_derive_kernel(Spec s, int K, int batch, double f10, const double2* __restrict__ st,
+                                 double2* __restrict__ out) {
+  const int L = s.L;
+  const long n2 = (long)(L + 1) * (L + 1);
+  const long idx = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= n2 * batch) return;
+  const int b = (int)(idx / n2);
+  const long r = idx - b * n2;
+  const int l = (int)(r / (L + 1)), m = (int)(r - (long)l * (L + 1));
+  const double2* S = st + (long)b * (3 * K + 1) * n2;
+  double2* O = out + (long)b * (kPeLevelFields * K + 2) * n2 + r;
+  const double2 zero = make_double2(0.0, 0.0);
+  if (m > l) {
+    for (int f = 0; f < kPeLevelFields * K + 2; ++f) O[f * n2] = zero;
+    return;
+  }
+  const bool lo = l >= 1 && l - 1 >= m, hi = l + 1 <= L;
+  auto val = [&](const double2* a, int ll) { return a[(long)ll * (L + 1) + m]; };
+  auto inv = [&](const double2* a, int ll) { return s.invlap0(a, ll, m); };
+  auto snt_r = [&](double2 vlo, double2 vhi) { return cscale(s.ir, s.snt(vlo, vhi, l, m)); };
+  for (int k = 0; k < K; ++k) {
+    const double2* z = S + (long)k * n2;
+    const double2* d = S + (long)(K + k) * n2;
+    const double2* T = S + (long)(2 * K + k) * n2;
+    const double2 psi = inv(z, l), chi = inv(d, l);
+    const double2 psi_lo = lo ? inv(z, l - 1) : zero, psi_hi = hi ? inv(z, l + 1) : zero;
+    const double2 chi_lo = lo ? inv(d, l - 1) : zero, chi_hi = hi ? inv(d, l + 1) : zero;
+    double2 e = val(z, l), e_lo = lo ? val(z, l - 1) : zero, e_hi = hi ? val(z, l + 1) : zero;
+    if (m == 0) {  // eta = zeta + f, f = 2 Omega sin(lat): the (1, 0) mode
+      if (l == 1) e.x += f10;
+      if (l - 1 == 1) e_lo.x += f10;
+      if (l + 1 == 1) e_hi.x += f10;
+    }
+    const double2 Tl = val(T, l);
+    double2* o = O + (long)kPeLevelFields * k * n2;
+    o[0 * n2] = cadd(snt_r(psi_lo, psi_hi), s.dlam(chi, m));   // u cos
+    o[1 * n2] = csub(s.dlam(psi, m), snt_r(chi_lo, chi_hi));   // v cos
+    o[2 * n2] = val(z, l);
+    o[3 * n2] = val(d, l);
+    o[4 * n2] = Tl;
+    o[5 * n2] = s.dlam(Tl, m);
+    o[6 * n2] = snt_r(lo ? val(T, l - 1) : zero, hi ? val(T, l + 1) : zero);
+    o[7 * n2] = s.dlam(e, m);
+    o[8 * n2] = snt_r(e_lo, e_hi);
+    o[9 * n2] = e;
+  }
+  const double2* q = S + (long)3 * K * n2;
+  O[(long)kPeLevelFields * K * n2] = s.dlam(val(q, l), m);
+  O[((long)kPeLevelFields * K + 1) * n2] = snt_r(lo ? val(q, l - 1) : zero, hi ? val(q, l + 1) : zero);
+}
+
+// One thread per (member, product point): the column.
+__global__ void __launch_bounds__(128) pe_columns_kernel(PeSigma sg, long np, int nlon, const double* __restrict__ coslat,
+                                                         int batch, double r_dry, double kappa,
+                                                         const double* __restrict__ grid, double* __restrict__ prod,
+                                                         double* __restrict__ fen) {
+  const long idx = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= np * batch) return;
+  const int K = sg.K;
+  const int b = (int)(idx / np);
+  const long p = idx - b * np;
+  const double ic = 1.0 / coslat[nlon > 0 ? p / nlon : p];
+  const double* Gd = grid + (long)b * (kPeLevelFields * K + 2) * np + p;
+  double* P = prod + (long)b * (kPeOutFields * K + 1) * np + p;
+  const double lp_lam = Gd[(long)kPeLevelFields * K * np], lp_snt = Gd[((long)kPeLevelFields * K + 1) * np];
+  double u[kPeMaxLevels], v[kPeMaxLevels], T[kPeMaxLevels], G[kPeMaxLevels], A[kPeMaxLevels];
+  double part[kPeMaxLevels], sd[kPeMaxLevels + 1];
+  double acc = 0.0, total = 0.0;
+  for (int k = 0; k < K; ++k) {
+    const double* f = Gd + (long)kPeLevelFields * k * np;
+    u[k] = f[0] * ic;
+    v[k] = f[np] * ic;
+    T[k] = f[4 * np];
+    A[k] = (u[k] * lp_lam - v[k] * lp_snt) * ic;      // V . grad(ln p_s)
+    G[k] = f[3 * np] + A[k];                          // delta + A
+    const double w = sg.dsig[k] * G[k];
+    acc = k == 0 ? w : acc + w;                       // cumulative thickness-weighted G
+    part[k] = acc;
+  }
+  total = part[K - 1];
+  // interface sigma_dot: exact zeros at the top and (total - total) at the surface
+  sd[0] = 0.0;
+  for (int k = 1; k < K; ++k) sd[k] = sg.s[k] * total - part[k - 1];
+  sd[K] = total - total;
+  P[(long)kPeOutFields * K * np] = -total;            // d ln p_s / dt
+  const double gu = lp_lam * ic, gv = -lp_snt * ic;   // grad(ln p_s)
+  auto vadv = [&](const double* X, int k) {
+    double a = 0.0;
+    bool any = false;
+    if (k < K - 1) {
+      a = sd[k + 1] * (X[k + 1] - X[k]);
+      any = true;
+    }
+    if (k > 0) {
+      const double up = sd[k] * (X[k] - X[k - 1]);
+      a = any ? a + up : up;
+      any = true;
+    }
+    return any ? a / (2.0 * sg.dsig[k]) : 0.0;
+  };
+  for (int k = 0; k < K; ++k) {
+    const double* f = Gd + (long)kPeLevelFields * k * np;
+    const double wp = k == 0 ? A[0] - sg.alpha[0] * G[0]
+                             : A[k] - (sg.beta[k] / sg.dsig[k]) * part[k - 1] - sg.alpha[k] * G[k];
+    const double t_lam = f[5 * np], t_snt = f[6 * np];
+    const double e_lam = f[7 * np], e_snt = f[8 * np], eta = f[9 * np];
+    const double adv_t = (u[k] * t_lam - v[k] * t_snt) * ic;
+    double* o = P + (long)kPeOutFields * k * np;
+    o[0] = -adv_t - vadv(T, k) + kappa * T[k] * wp;
+    o[np] = -((u[k] * e_lam - v[k] * e_snt) * ic + eta * f[3 * np]);
+    o[2 * np] = eta * f[2 * np] + (v[k] * e_lam + u[k] * e_snt) * ic;
+    o[3 * np] = 0.5 * (u[k] * u[k] + v[k] * v[k]);
+    const double rt = r_dry * T[k];
+    double* z = fen + ((long)b * K + k) * 2 * np + p;
+    z[0] = vadv(u, k) + rt * gu;
+    z[np] = vadv(v, k) + rt * gv;
+  }
+}
+
+// One thread per (member, l, m): every level's tendencies.
+__global__ void pe_spectral_kernel(PeSigma sg, int L, double R, double r_dry, int batch,
+                                   const double2* __restrict__ st, const double2* __restrict__ an,
+                                   const double2* __restrict__ cz, const double2* __restrict__ dz,
+                                   const double2* __restrict__ phis, double2* __restrict__ out) {
+  const int K = sg.K;
+  const long n2 = (long)(L + 1) * (L + 1);
+  const long idx = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= n2 * batch) return;
+  const int b = (int)(idx / n2);
+  const long r = idx - b * n2;
+  const int l = (int)(r / (L + 1)), m = (int)(r - (long)l * (L + 1));
+  double2* O = out + (long)b * (3 * K + 1) * n2 + r;
+  const double2 zero = make_double2(0.0, 0.0);
+  if (m > l) {
+    for (int f = 0; f < 3 * K + 1; ++f) O[f * n2] = zero;
+    return;
+  }
+  const int cut = (2 * L) / 3;
+  const bool keep = l <= cut && m <= cut;
+  const double lap = -(double)l * (l + 1.0) / (R * R);
+  const double2* A = an + (long)b * (kPeOutFields * K + 1) * n2 + r;
+  const double2* T = st + (long)b * (3 * K + 1) * n2 + (long)2 * K * n2 + r;
+  // Simmons-Burridge on the spectral T, upward from Phi_s at the surface
+  double2 below = phis[r];
+  for (int k = K - 1; k >= 0; --k) {
+    const double2 Tk = T[(long)k * n2];
+    const double2 phi = cadd(below, cscale(r_dry * sg.alpha[k], Tk));
+    if (k > 0) below = cadd(below, cscale(r_dry * sg.beta[k], Tk));
+    const double2* a = A + (long)kPeOutFields * k * n2;
+    const long zk = ((long)b * K + k) * n2 + r;
+    const double2 ke = keep ? a[3 * n2] : zero;
+    O[(long)(2 * K + k) * n2] = keep ? a[0] : zero;
+    O[(long)k * n2] = (l == 0 || !keep) ? zero : csub(a[n2], cz[zk]);
+    const double2 dd = keep ? csub(a[2 * n2], dz[zk]) : zero;
+    O[(long)(K + k) * n2] = l == 0 ? zero : csub(dd, cscale(lap, cadd(ke, phi)));
+  }
+  O[(long)3 * K * n2] = keep ? A[(long)kPeOutFields * K * n2] : zero;
+}
+
+}  // namespace
+}  // namespace aeolus
+
+using namespace aeolus;
+
+extern "C" int aeolus_pe_derive(aeolus_plan plan, const aeolus_pe_params* prm, int nlev, const double* state,
+                                double* fields, int batch, void* stream) {
+  if (int s = check_common(plan, "aeolus_pe_derive", batch, state, fields)) return s;
+  if (int s = pe_check(prm)) return s;
+  if (nlev < 1 || nlev > kPeMaxLevels) return fail(AEOLUS_ERR_ARG, "aeolus_pe_derive: bad nlev");
+  if (batch == 0) return AEOLUS_OK;
+  const long n2 = (long)(plan->lmax + 1) * (plan->lmax + 1);
+  ProfScope prof("pe_derive", static_cast<cudaStream_t>(stream));
+  pe_derive_kernel<<<blocks_for(n2 * batch, 128), 128, 0, static_cast<cudaStream_t>(stream)>>>(
+      make_spec(plan, prm->radius), nlev, batch, 2.0 * prm->omega * kSqrt4PiOver3,
+      reinterpret_cast<const double2*>(state), reinterpret_cast<double2*>(fields));
+  AE_LAUNCH("pe_derive_kernel");
+  return AEOLUS_OK;
+}
+
+extern "C" int aeolus_pe_columns(aeolus_plan plan, const aeolus_pe_params* prm, int nlev, const double* interfaces,
+                                 const double* grid, double* prod, double* f_en, int batch, void* stream) {
+  if (int s = check_common(plan, "aeolus_pe_columns", batch, grid, prod)) return s;
+  if (int s = pe_check(prm)) return s;
+  PeSigma sg;
+  if (int s = make_sigma(interfaces, nlev, &sg)) return s;
+  if (batch > 0 && !f_en) return fail(AEOLUS_ERR_ARG, "aeolus_pe_columns: NULL f_en");
+  if (batch == 0) return AEOLUS_OK;
+  const long np = plan->npoints;
+  const int nlon = plan->kind == kGauss ? plan->nlon : 0;
+  ProfScope prof("pe_columns", static_cast<cudaStream_t>(stream));
+  pe_columns_kernel<<<blocks_for(np * batch, 128), 128, 0, static_cast<cudaStream_t>(stream)>>>(
+      sg, np, nlon, plan->coslat, batch, prm->r_dry, prm->r_dry / prm->cp_dry, grid, prod, f_en);
+  AE_LAUNCH("pe_columns_kernel");
+  return AEOLUS_OK;
+}
+
+extern "C" int aeolus_pe_spectral(int lmax, const aeolus_pe_params* prm, int nlev, const double* interfaces,
+                                  const double* state, const double* analysed, const double* curl_z,
+                                  const double* div_z, const double* phi_s, double* tendency, int batch,
+                                  void* stream) {
+  if (lmax < 0 || batch < 0) return fail(AEOLUS_ERR_ARG, "aeolus_pe_spectral: bad lmax/batch");
+  if (int s = pe_check(prm)) return s;
+  PeSigma sg;
+  if (int s = make_sigma(interfaces, nlev, &sg)) return s;
+  if (batch == 0) return AEOLUS_OK;
+  if (!state || !analysed || !curl_z || !div_z || !phi_s || !tendency)
+    return fail(AEOLUS_ERR_ARG, "aeolus_pe_spectral: NULL array");
+  const long n2 = (long)(lmax + 1) * (lmax + 1);
+  ProfScope prof("pe_spectral", static_cast<cudaStream_t>(stream));
+  pe_spectral_kernel<<<blocks_for(n2 * batch, 128), 128, 0, static_cast<cudaStream_t>(stream)>>>(
+      sg, lmax, prm->radius, prm->r_dry, batch, reinterpret_cast<const double2*>(state),
+      reinterpret_cast<const double2*>(analysed), reinterpret_cast<const double2*>(curl_z),
+      reinterpret_cast<const double2*>(div_z), reinterpret_cast<const double2*>(phi_s),
+      reinterpret_cast<double2*>(tendency));
+  AE_LAUNCH("pe_spectral_kernel");
+  return AEOLUS_OK;
+}

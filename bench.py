@@ -236,6 +236,56 @@ def geodesic_measure(dev, fields: int = 64, reps: int = 3):
     return out
 
 
+def pe_measure(dev, members: int = 4, nlev: int = 20, reps: int = 5):
+    """Dry hydrostatic primitive-equation tendency (physics/primitive_equations.py
+    :727-753) on the headline grid: Gauss 192x384, l_max 127, `nlev` uniform
+    sigma levels, `members` perturbed isothermal states, FP64; tendency
+    evaluations/s and the library kernels' share (their own CUDA events)."""
+    import torch
+    import aeolus_gb300 as ae
+    from aeolus_gb300 import _lib
+    from aeolus_gb300.primitive_equations import PrimitiveEquationsModel, SigmaGrid, isothermal_rest_state
+
+    L, K = LMAX, nlev
+    planet = ae.make_planet("latlon", nlat=NLAT, nlon=NLON, l_max=L, device=dev)
+    model = PrimitiveEquationsModel(planet, SigmaGrid.uniform(K))
+    rng = np.random.default_rng(17)
+    n, cut = L + 1, (2 * L) // 3
+    states = []
+    for b in range(members):
+        st = isothermal_rest_state(L, K, temperature=260.0, surface_pressure=101325.0, device=dev).coeffs
+        for i in range(3 * K + 1):
+            a = rng.standard_normal((n, n)) + 1j * rng.standard_normal((n, n))
+            a[:, 0] = a[:, 0].real
+            a *= np.tril(np.ones((n, n)))
+            a[cut + 1:] = 0
+            if i < 2 * K or i == 3 * K:
+                a[0, 0] = 0
+            st[i] += torch.as_tensor(a * (2e-6 if i < 2 * K else (0.5 if i < 3 * K else 1e-3)), device=dev)
+        states.append(st)
+    x = torch.stack(states)
+    model.tendency(x)
+    torch.cuda.synchronize(dev)
+    lib = _lib.load()
+    lib.aeolus_profile_reset()
+    lib.aeolus_profile_enable(1)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(reps):
+        model.tendency(x)
+    e1.record()
+    torch.cuda.synchronize(dev)
+    lib.aeolus_profile_enable(0)
+    ms = e0.elapsed_time(e1) / reps
+    ks = _collect_kernels(lib, _lib)
+    tot = sum(v for _, v in ks.values()) or 1.0
+    return {"workload": f"pe_tendency_gauss{NLAT}x{NLON}_lmax{L}_{K}levels_members{members}", "precision": "fp64",
+            "ms_per_tendency": ms, "member_tendencies_per_s": members * 1e3 / ms,
+            "transforms_per_tendency": {"syntheses": members * (10 * K + 2),
+                                        "analyses": members * (4 * K + 1) + 2 * members * K},
+            "kernel_share": {k: round(v / tot, 4) for k, (_, v) in sorted(ks.items(), key=lambda kv: -kv[1][1])}}
+
+
 # ------------------------------------------------------------ CPU baseline
 def cpu_reference_sample(B: int, rows: int, reps: int = 1):
     """Time the reference algorithm for one RK4 step on a row sample.
@@ -608,6 +658,7 @@ def main():
         extras["ensemble"] = ensemble_measure(dev)
         extras["adjoint"] = adjoint_measure(dev)
         extras["geodesic"] = geodesic_measure(dev)
+        extras["pe"] = pe_measure(dev)
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:

@@ -193,6 +193,50 @@ int aeolus_vector_curl_div(aeolus_plan plan_ext, double radius, const double* f_
                            double* div, int batch, int truncate, void* work, size_t work_bytes,
                            void* stream);
 
+/* ---- dry hydrostatic primitive equations (physics/primitive_equations.py)
+ * The tendency of primitive_equations.py:727-753 is five library calls
+ * (aeolus_pe_derive -> aeolus_synthesize -> aeolus_pe_columns ->
+ * aeolus_analyze + aeolus_vector_curl_div -> aeolus_pe_spectral) on a
+ * product plan of degree L and its one-degree-extended plan.  States are
+ * [batch][3K+1][L+1][L+1] complex, rows zeta_1..K, delta_1..K, T_1..K,
+ * ln p_s (top to bottom, :76-136); sigma interfaces are a HOST array of
+ * K + 1 values rising from exactly 0 to exactly 1 (sigma_coordinate.py:43-81);
+ * 1 <= K <= 64.  No scratch: the callers own every intermediate. */
+typedef struct {
+  double radius;  /* m */
+  double omega;   /* 1/s */
+  double r_dry;   /* J/(kg K), primitive_equations.py:49 */
+  double cp_dry;  /* J/(kg K), > r_dry */
+} aeolus_pe_params;
+
+/* fields [batch][10K+2][L+1][L+1]: per level u cos(lat), v cos(lat) (from
+ * the l=0-zeroed inverse Laplacians of zeta and delta, :266-287), zeta, delta,
+ * T, (1/R) dT/dlambda, (1/R) sin(theta) dT/dtheta, the same two of
+ * eta = zeta + f, eta; then (1/R) d(ln p_s)/dlambda and
+ * (1/R) sin(theta) d(ln p_s)/dtheta (:272-278, :531-548). */
+int aeolus_pe_derive(aeolus_plan plan, const aeolus_pe_params* params, int nlev, const double* state,
+                     double* fields, int batch, void* stream);
+
+/* Column physics on the product points of `plan` (:482-587, sigma_coordinate.py
+ * :212-398): grid = synthesis of the derive fields, [batch][10K+2][n_points];
+ * prod [batch][4K+1][n_points] = per level the thermodynamic integrand
+ * -V.grad T - sigma_dot dT/dsigma + kappa T omega/p (:615-619), -div(eta V),
+ * curl(eta V), |V|^2/2 (:695-711), then d ln p_s/dt; f_en
+ * [batch*K][2][n_points] = the residual vector Z = sigma_dot dV/dsigma +
+ * R_d T grad(ln p_s) (east, north; :713-716). */
+int aeolus_pe_columns(aeolus_plan plan, const aeolus_pe_params* params, int nlev, const double* interfaces,
+                      const double* grid, double* prod, double* f_en, int batch, void* stream);
+
+/* tendency [batch][3K+1][L+1][L+1] from the analysed integrands
+ * (analysed [batch][4K+1][L+1][L+1]), the untruncated weak-form curl/div of
+ * Z (curl_z, div_z [batch*K][L+1][L+1]), the state (for the
+ * Simmons-Burridge geopotential of the spectral T, :691-693) and the
+ * surface geopotential phi_s [L+1][L+1]: 2/3 cuts, -lap(KE + Phi), l = 0
+ * rows of the zeta/delta tendencies zero (:718-724). */
+int aeolus_pe_spectral(int lmax, const aeolus_pe_params* params, int nlev, const double* interfaces,
+                       const double* state, const double* analysed, const double* curl_z, const double* div_z,
+                       const double* phi_s, double* tendency, int batch, void* stream);
+
 /* ---- icosahedral geodesic point set (numerics/geodesic_grid.py) -------- */
 
 /* Point, face and workspace counts of a geodesic point set with

@@ -7,7 +7,7 @@ NumPy stand-in for CuPy in ``tests/golden/refshim``; its CUDA-C basis kernel
 Omega = 7.292e-5 1/s, as the workloads specify (``Planet.generate`` would
 derive different constants and random terrain).
 
-Run:  PYTHONDONTWRITEBYTECODE=1 python tests/golden/make_golden.py [vector|runs|geodesic_fine]
+Run:  PYTHONDONTWRITEBYTECODE=1 python tests/golden/make_golden.py [vector|runs|geodesic_fine|pe]
 Writes ``tests/golden/*.npz`` (with ``vector``: only the weak-form curl/div
 fixtures; with ``runs``: only the integration-engine events and the run
 capsules of the reference's BVE/SWE runners).  Only l_max <= 85 fixtures are made: above
@@ -169,6 +169,67 @@ def geodesic_fine_case(name, res, lmax, seed=19, dt=600.0):
     print(f"{name}: {time.time() - t0:.1f}s")
 
 
+def pe_state(lmax, nlev, seed, l_band=None, t0=260.0, ps0=101325.0):
+    """Isothermal rest state plus seeded band-limited perturbations of every
+    prognostic (the recipe of the reference's tests/test_pe_tendency.py:80-108)."""
+    n = lmax + 1
+    l_band = (2 * lmax) // 3 if l_band is None else l_band
+    rng = np.random.default_rng(seed)
+    s = np.zeros((3 * nlev + 1, n, n), complex)
+    s[2 * nlev:3 * nlev, 0, 0] = t0 * np.sqrt(4 * np.pi)
+    s[3 * nlev, 0, 0] = np.log(ps0) * np.sqrt(4 * np.pi)
+
+    def pert(amp, zero_monopole):
+        p = amp * (rng.standard_normal((n, n)) + 1j * rng.standard_normal((n, n)))
+        p[:, 0] = p[:, 0].real
+        p *= np.tril(np.ones((n, n)))
+        p[l_band + 1:, :] = 0.0
+        if zero_monopole:
+            p[0, 0] = 0.0
+        return p
+
+    for k in range(nlev):
+        s[k] += pert(2e-6, True)
+        s[nlev + k] += pert(2e-6, True)
+        s[2 * nlev + k] += pert(0.5, False)
+    s[3 * nlev] += pert(1e-3, True)
+    return s
+
+
+def pe_case(name, planet, interfaces, seed, phi_s_amp=0.0):
+    """The reference's dry hydrostatic primitive-equation tendency
+    (physics/primitive_equations.py:727-753) on a seeded state."""
+    from planetary_sandbox.physics.primitive_equations import PrimitiveEquationsModel
+    from planetary_sandbox.physics.sigma_coordinate import SigmaGrid
+    t0 = time.time()
+    L = planet.sh.l_max
+    sigma = SigmaGrid(tuple(interfaces))
+    phi_s = None
+    if phi_s_amp:
+        rng = np.random.default_rng(seed + 100)
+        cut = (2 * L) // 3
+        phi_s = np.zeros((L + 1, L + 1), complex)
+        phi_s[:cut + 1, :cut + 1] = phi_s_amp * (rng.standard_normal((cut + 1, cut + 1))
+                                                 + 1j * rng.standard_normal((cut + 1, cut + 1)))
+        phi_s[:, 0] = phi_s[:, 0].real
+        phi_s *= np.tril(np.ones((L + 1, L + 1)))
+    model = PrimitiveEquationsModel(planet, sigma, surface_geopotential_lm=phi_s)
+    state = pe_state(L, sigma.nlev, seed)
+    tend = model.tendency(state.copy())
+    np.savez_compressed(
+        HERE / f"{name}.npz", lmax=L, interfaces=np.asarray(interfaces, float), radius=R, omega=OMEGA,
+        r_dry=model.r_dry, cp_dry=model.cp_dry,
+        phi_s=np.zeros((L + 1, L + 1), complex) if phi_s is None else phi_s, state=state, tendency=tend)
+    print(f"{name}: {time.time() - t0:.1f}s")
+
+
+def pe_cases():
+    pe_case("pe_gauss16x32_L15_fine23x46_K5", latlon_planet(16, 32, 15), [k / 5 for k in range(6)], seed=31)
+    pe_case("pe_gauss24x48_L15_K4_nonuniform_phis", latlon_planet(24, 48, 15), [0.0, 0.12, 0.35, 0.7, 1.0],
+            seed=37, phi_s_amp=300.0)
+    pe_case("pe_geodesic_res3_L10_K3", geodesic_planet(3, 10), [0.0, 0.3, 0.65, 1.0], seed=41)
+
+
 def vector_cases():
     vector_case("vector_gauss16x32_L15_fine23x46", latlon_planet(16, 32, 15), seed=13)
     vector_case("vector_geodesic_res3_L10", geodesic_planet(3, 10), seed=17)
@@ -185,6 +246,7 @@ def main():
     swe_case("swe_gauss128x256_L85", 128, 256, 85, seed=2, dt=300.0)
     geodesic_case("geodesic_res3_L10", 3, 10)
     geodesic_fine_case("geodesic_fine_res3_L10", 3, 10)
+    pe_cases()
     vector_cases()
 
 
@@ -357,6 +419,8 @@ def run_cases():
 if __name__ == "__main__":
     if sys.argv[1:] == ["vector"]:
         vector_cases()
+    elif sys.argv[1:] == ["pe"]:
+        pe_cases()
     elif sys.argv[1:] == ["geodesic_fine"]:
         geodesic_fine_case("geodesic_fine_res3_L10", 3, 10)
     elif sys.argv[1:] == ["runs"]:

@@ -85,3 +85,35 @@ def test_workload_generators():
     z = workloads.bve_vorticity(21, 0)
     assert np.all(z[0] == 0) and np.all(z[:, 0].imag == 0)
     assert np.all(z[~workloads.triangle_mask(21)] == 0)
+
+
+def test_sigma_grid_matches_oracle_and_rejects_bad_grids():
+    from aeolus_gb300.primitive_equations import SigmaGrid, SigmaGridError
+    from oracle import pe as ope
+    for s in ([0.0, 1.0], [k / 7 for k in range(8)], [0.0, 0.05, 0.2, 0.5, 0.8, 1.0]):
+        g, o = SigmaGrid(tuple(s)), ope.Sigma(s)
+        assert g.nlev == o.K and g.thickness == tuple(o.dsig) and g.alpha == tuple(o.alpha)
+        assert g.interface_log_ratios[1:] == tuple(o.beta[1:])
+    assert SigmaGrid.uniform(4).interfaces == (0.0, 0.25, 0.5, 0.75, 1.0)
+    for bad in ([0.1, 1.0], [0.0, 0.99], [0.0, 0.5, 0.5, 1.0], [0.0, float("nan"), 1.0], [0.0], ["a", 1.0]):
+        with pytest.raises(SigmaGridError):
+            SigmaGrid(tuple(bad))
+    with pytest.raises(SigmaGridError):
+        SigmaGrid.uniform(65)
+
+
+def test_pe_entry_points_refuse_bad_arguments_without_gpu():
+    lib = _lib.load()
+    prm = _lib.PeParams(6.371e6, 7.292e-5, 287.04, 1004.64)
+    sig = (ctypes.c_double * 3)(0.0, 0.5, 1.0)
+    bad_sig = (ctypes.c_double * 3)(0.0, 0.5, 0.9)
+    d = ctypes.c_void_p(16)  # never dereferenced: each call below is refused first
+    assert lib.aeolus_pe_spectral(10, ctypes.byref(prm), 2, bad_sig, d, d, d, d, d, d, 1, None) == _lib.ERR_ARG
+    assert b"sigma" in lib.aeolus_last_error()
+    assert lib.aeolus_pe_spectral(10, ctypes.byref(prm), 0, sig, d, d, d, d, d, d, 1, None) == _lib.ERR_ARG
+    assert lib.aeolus_pe_spectral(10, ctypes.byref(prm), 2, sig, None, d, d, d, d, d, 1, None) == _lib.ERR_ARG
+    bad = _lib.PeParams(6.371e6, 7.292e-5, 287.04, 200.0)
+    assert lib.aeolus_pe_spectral(10, ctypes.byref(bad), 2, sig, d, d, d, d, d, d, 1, None) == _lib.ERR_ARG
+    assert b"cp_dry" in lib.aeolus_last_error()
+    assert lib.aeolus_pe_derive(None, ctypes.byref(prm), 2, d, d, 1, None) == _lib.ERR_ARG
+    assert lib.aeolus_pe_columns(None, ctypes.byref(prm), 2, sig, d, d, d, 1, None) == _lib.ERR_ARG
