@@ -162,9 +162,10 @@ struct GroupedEpi {
   static constexpr int kWarps = Epi::kWarps, kCols = Epi::kCols;
   GroupedSched<Sched> gs;  // for the tile -> group map
   Epi e[kMaxGroups];
-  __device__ void run(int t, uint32_t tbuf, int q, int row, int c0, int etid) const {
+  template <class Rel>
+  __device__ void run(int t, uint32_t tbuf, int q, int row, int c0, int etid, Rel release) const {
     const int k = gs.find(t);
-    e[k].run(t - gs.start[k], tbuf, q, row, c0, etid);
+    e[k].run(t - gs.start[k], tbuf, q, row, c0, etid, release);
   }
 };
 

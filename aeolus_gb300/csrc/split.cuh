@@ -452,9 +452,12 @@ constexpr int tc_threads() { return 64 + 32 * Epi::kWarps; }
 // Sched: int count() const; TcTile tile(int t) const; kSegChunks (0: one
 //        K segment per tile, else K segments of that many chunks).
 // Epi:   kWarps (4, 8 or 16 epilogue warps), kCols = 4 kNT / kWarps, and
-//        void run(int t, uint32_t tbuf, int q, int row, int c0, int etid) const
-//        -- consumes columns [c0, c0 + kCols) of the accumulators of tile t
-//        for TMEM lane row = q * 32 + lane (etid = epilogue thread index);
+//        template <class Rel> void run(int t, uint32_t tbuf, int q, int row,
+//        int c0, int etid, Rel release) const -- consumes columns
+//        [c0, c0 + kCols) of the accumulators of tile t for TMEM lane
+//        row = q * 32 + lane (etid = epilogue thread index) and calls
+//        release() once they are in registers (the buffer goes back to the
+//        MMA warp before the epilogue's math and stores);
 //        with K segments instead State, seg_begin(State&), seg_add(State&,
 //        tbuf, q, c0) per segment and seg_end(t, State, row, c0, etid).
 template <class Sched, class Epi>
@@ -596,8 +599,10 @@ __global__ void __launch_bounds__(tc_threads<Epi>(), 1) tc_persistent_kernel(Sch
       } else {
         if (!(ok = wait_full(i))) break;
         tc::fence_after_sync();
-        ep.run(t, tmem + (uint32_t)((i & 1) * kTmemBuf), q, q * 32 + lane, c0, etid);
-        release(i);
+        // the epilogue hands the buffer back as soon as its accumulators are
+        // in registers, so the next tile's MMAs overlap its math and stores
+        const int unit = i;
+        ep.run(t, tmem + (uint32_t)((i & 1) * kTmemBuf), q, q * 32 + lane, c0, etid, [&] { release(unit); });
         ++i;
       }
     }
@@ -640,7 +645,8 @@ struct SynthEpi {
   const int* ecol;
   int nblk;
   float4* F;
-  __device__ void run(int t, uint32_t tbuf, int q, int row, int c0, int) const {
+  template <class Rel>
+  __device__ void run(int t, uint32_t tbuf, int q, int row, int c0, int, Rel release) const {
     const int per_m = dm.Mt * dm.ntiles;
     const int m = t / per_m, r = t - m * per_m;
     const int mt = r / dm.ntiles, tile = r - mt * dm.ntiles;
@@ -653,6 +659,7 @@ struct SynthEpi {
     for (int i = 0; i < kCols; ++i) e[i] = Ej + __ldg(ec + i) - kOut;
     float acc[kCols][kAccs];
     tc_read<kCols>(tbuf, q, c0, acc);
+    release();
     if (j < dm.nlat) {
 #pragma unroll
       for (int i = 0; i < kCols; i += 2) {
