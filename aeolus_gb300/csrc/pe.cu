@@ -31,9 +31,13 @@ constexpr int kPeOutFields = 4;     // thermodynamic integrand, -div(eta V), cur
 // Lorenz sigma grid, sigma_coordinate.py:43-149: interfaces s[0] = 0 (top)
 // .. s[K] = 1 (surface), thickness, interface log ratios beta (beta[0], the
 // infinite top entry, is never read) and the Simmons-Burridge alpha.
+// The column kernel multiplies by host-computed reciprocals instead of
+// dividing (FP64 divides would dominate its FP64 pipe): h2[k] = 1/(2 Dsigma_k)
+// and bd[k] = beta_k / Dsigma_k, within an ulp of the reference's quotients.
 struct PeSigma {
   int K;
   double s[kPeMaxLevels + 1], dsig[kPeMaxLevels], beta[kPeMaxLevels], alpha[kPeMaxLevels];
+  double h2[kPeMaxLevels], bd[kPeMaxLevels];
 };
 
 int make_sigma(const double* interfaces, int nlev, PeSigma* g) {
@@ -49,12 +53,17 @@ int make_sigma(const double* interfaces, int nlev, PeSigma* g) {
       return fail(AEOLUS_ERR_ARG, "sigma interfaces must be finite and strictly increasing");
     g->s[k] = interfaces[k];
   }
-  for (int k = 0; k < nlev; ++k) g->dsig[k] = g->s[k + 1] - g->s[k];
+  for (int k = 0; k < nlev; ++k) {
+    g->dsig[k] = g->s[k + 1] - g->s[k];
+    g->h2[k] = 1.0 / (2.0 * g->dsig[k]);
+  }
   g->beta[0] = 0.0;
+  g->bd[0] = 0.0;
   g->alpha[0] = std::log(2.0);
   for (int k = 1; k < nlev; ++k) {
     g->beta[k] = std::log(g->s[k + 1] / g->s[k]);
     g->alpha[k] = 1.0 - (g->s[k] / g->dsig[k]) * g->beta[k];
+    g->bd[k] = g->beta[k] / g->dsig[k];
   }
   return AEOLUS_OK;
 }
@@ -169,12 +178,12 @@ __global__ void __launch_bounds__(128) pe_columns_kernel(PeSigma sg, long np, in
       a = any ? a + up : up;
       any = true;
     }
-    return any ? a / (2.0 * sg.dsig[k]) : 0.0;
+    return any ? a * sg.h2[k] : 0.0;
   };
   for (int k = 0; k < K; ++k) {
     const double* f = Gd + (long)kPeLevelFields * k * np;
     const double wp = k == 0 ? A[0] - sg.alpha[0] * G[0]
-                             : A[k] - (sg.beta[k] / sg.dsig[k]) * part[k - 1] - sg.alpha[k] * G[k];
+                             : A[k] - sg.bd[k] * part[k - 1] - sg.alpha[k] * G[k];
     const double t_lam = f[5 * np], t_snt = f[6 * np];
     const double e_lam = f[7 * np], e_snt = f[8 * np], eta = f[9 * np];
     const double adv_t = (u[k] * t_lam - v[k] * t_snt) * ic;

@@ -62,6 +62,8 @@ def parse():
     ap.add_argument("--cpu-rows", type=int, default=8, help="latitude rows in the CPU sample")
     ap.add_argument("--no-extras", action="store_true",
                     help="skip the ensemble (uneven l_max BVE) and adjoint (SWE gradient) side measurements")
+    ap.add_argument("--side", choices=["ensemble", "adjoint", "geodesic", "pe"], default=None,
+                    help="run only this side measurement (one JSON object); for profiling runs")
     ap.add_argument("--knobs", default="",
                     help="launch shapes of the measured model as 5 comma-separated ints (bc_synth, bc_anal, "
                          "row_threads, slice_synth, slice_anal) instead of autotuning; for profiling runs")
@@ -264,26 +266,42 @@ def pe_measure(dev, members: int = 4, nlev: int = 20, reps: int = 5):
             st[i] += torch.as_tensor(a * (2e-6 if i < 2 * K else (0.5 if i < 3 * K else 1e-3)), device=dev)
         states.append(st)
     x = torch.stack(states)
-    model.tendency(x)
-    torch.cuda.synchronize(dev)
     lib = _lib.load()
-    lib.aeolus_profile_reset()
-    lib.aeolus_profile_enable(1)
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    e0.record()
-    for _ in range(reps):
+    out = {"workload": f"pe_tendency_gauss{NLAT}x{NLON}_lmax{L}_{K}levels_members{members}",
+           "transforms_per_tendency": {"syntheses": members * (10 * K + 2),
+                                       "analyses": members * (4 * K + 1) + 2 * members * K}}
+    res = {}
+    for prec in ("fp64", "split"):
+        # split: the product plan's Legendre contractions on the bf16-digit
+        # tensor-core path; the degree-(L+1) vector analysis stays FP64
+        model._plan.set_precision(_lib.PREC_SPLIT_BF16 if prec == "split" else _lib.PREC_FP64)
         model.tendency(x)
-    e1.record()
-    torch.cuda.synchronize(dev)
-    lib.aeolus_profile_enable(0)
-    ms = e0.elapsed_time(e1) / reps
-    ks = _collect_kernels(lib, _lib)
-    tot = sum(v for _, v in ks.values()) or 1.0
-    return {"workload": f"pe_tendency_gauss{NLAT}x{NLON}_lmax{L}_{K}levels_members{members}", "precision": "fp64",
-            "ms_per_tendency": ms, "member_tendencies_per_s": members * 1e3 / ms,
-            "transforms_per_tendency": {"syntheses": members * (10 * K + 2),
-                                        "analyses": members * (4 * K + 1) + 2 * members * K},
-            "kernel_share": {k: round(v / tot, 4) for k, (_, v) in sorted(ks.items(), key=lambda kv: -kv[1][1])}}
+        torch.cuda.synchronize(dev)
+        lib.aeolus_profile_reset()
+        lib.aeolus_profile_enable(1)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(reps):
+            y = model.tendency(x)
+        e1.record()
+        torch.cuda.synchronize(dev)
+        lib.aeolus_profile_enable(0)
+        ms = e0.elapsed_time(e1) / reps
+        ks = _collect_kernels(lib, _lib)
+        tot = sum(v for _, v in ks.values()) or 1.0
+        res[prec] = y
+        out[prec] = {"ms_per_tendency": ms, "member_tendencies_per_s": members * 1e3 / ms,
+                     "kernel_share": {k: round(v / tot, 4)
+                                      for k, (_, v) in sorted(ks.items(), key=lambda kv: -kv[1][1])}}
+    model._plan.set_precision(_lib.PREC_FP64)
+    d = res["split"] - res["fp64"]
+    blk = lambda t, a, b: float(torch.linalg.vector_norm(t[:, a:b]))  # noqa: E731
+    out["rel_l2_split_vs_fp64"] = {
+        name: blk(d, a, b) / blk(res["fp64"], a, b)
+        for name, a, b in (("zeta", 0, K), ("delta", K, 2 * K), ("temperature", 2 * K, 3 * K),
+                           ("ln_ps", 3 * K, 3 * K + 1))}
+    out["split_vs_fp64_speedup"] = out["fp64"]["ms_per_tendency"] / out["split"]["ms_per_tendency"]
+    return out
 
 
 # ------------------------------------------------------------ CPU baseline
@@ -569,6 +587,11 @@ def main():
         dist.init_process_group("nccl")
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
+    if args.side:
+        fn = {"ensemble": ensemble_measure, "adjoint": adjoint_measure, "geodesic": geodesic_measure,
+              "pe": pe_measure}[args.side]
+        print(json.dumps({args.side: fn(dev)}))
+        return 0
 
     import aeolus_gb300 as ae
     from aeolus_gb300 import _lib, workloads as W
