@@ -126,15 +126,13 @@ int launch_rows(const aeolus_plan_impl* p, const Pw& pw, RowArgs a, cudaStream_t
   dim3 grid(p->nlat, a.batch);
   const int threads = row_threads(p);
   if (p->precision == AEOLUS_PREC_SPLIT_BF16) {
-    // split-precision path: fixed-point FFTs, double-float products; the
-    // model chains get kernels compiled for the common radix sequences
+    // split-precision path: fixed-point FFTs, double-float products; every
+    // row stage gets kernels compiled for the common radix sequences
     a.fft = p->fftx;
-    if constexpr (IN_MODE == kInF && OUT_MODE == kOutG) {
-      using F388 = FftFixed<3, 8, 8>;  // nlon 384
-      using F288 = FftFixed<2, 8, 8>;  // nlon 256
-      if (F388::matches(p->fftx)) return launch_rows_fx<Pw, IN_MODE, OUT_MODE, F388>(p, pw, a, st);
-      if (F288::matches(p->fftx)) return launch_rows_fx<Pw, IN_MODE, OUT_MODE, F288>(p, pw, a, st);
-    }
+    using F388 = FftFixed<3, 8, 8>;  // nlon 384
+    using F288 = FftFixed<2, 8, 8>;  // nlon 256
+    if (F388::matches(p->fftx)) return launch_rows_fx<Pw, IN_MODE, OUT_MODE, F388>(p, pw, a, st);
+    if (F288::matches(p->fftx)) return launch_rows_fx<Pw, IN_MODE, OUT_MODE, F288>(p, pw, a, st);
     return launch_rows_fx<Pw, IN_MODE, OUT_MODE, FftRuntime>(p, pw, a, st);
   }
   const size_t sm = row_smem_bytes<Pw>(p->fft);
