@@ -1,8 +1,9 @@
-"""NumPy stand-in for CuPy, used only to run the reference on this CPU.
+"""NumPy stand-in for CuPy, used only to run the reference on host cores.
 
-Test infrastructure for ``tests/golden/make_golden.py``: every ``cupy.X``
-forwards to ``numpy.X``; ``RawModule`` runs the reference's own basis kernel
-compiled for the CPU by ``oracle/ref_build.py``.
+Used by ``tests/golden/make_golden.py`` (golden vectors) and by the timed
+CPU baseline (``baseline/reference_timing.py``): every ``cupy.X`` forwards to
+``numpy.X``; ``RawModule`` runs the reference's own basis kernel compiled
+for the CPU by ``oracle/ref_build.py``.
 """
 import ctypes
 import sys
@@ -58,7 +59,7 @@ def get_default_pinned_memory_pool():
     return SimpleNamespace(free_all_blocks=lambda: None)
 
 
-_REPO = Path(__file__).resolve().parents[4]
+_REPO = Path(__file__).resolve().parents[3]
 if str(_REPO) not in sys.path:
     sys.path.insert(0, str(_REPO))
 

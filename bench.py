@@ -18,9 +18,11 @@ relative L2 between the two after the timed steps.  `value` is device-timed
 with the state resident in HBM (CUDA events around each step, L2 flushed
 between steps);
 `e2e` goes through the public API with the state copied host->device from
-pinned memory and back every step.  `--impl reference` times the
-reference's algorithm (dense complex basis matrix-vector transforms, the
-CPU restatement in oracle/) on the host cores over a bounded row sample.
+pinned memory and back every step.  `--impl reference` (and the
+`cpu_baseline` key) times the reference's own SWE tendency on the host cores
+over a bounded row sample: its package installed unmodified in baseline/_ref
+and run with NumPy in place of CuPy (baseline/reference_timing.py), or the
+CPU restatement in oracle/ where that package is absent ("kind": "port").
 """
 from __future__ import annotations
 
@@ -341,25 +343,61 @@ def cpu_reference_sample(B: int, rows: int, reps: int = 1):
     return 1.0 / (step_member * B), desc, t * reps
 
 
+def reference_own_sample(B: int, rows: int, reps: int = 1):
+    """The reference's own SWE tendency (its package in baseline/_ref, run with
+    the NumPy stand-in for CuPy in a child process by
+    baseline/reference_timing.py) on `rows` of the 192 Gauss rows, scaled to
+    the full grid, 4 stages and B members.  Returns (steps/s, description,
+    seconds) or None when the reference package or its CPU-built basis
+    kernel is not available on this host."""
+    script = ROOT / "baseline" / "reference_timing.py"
+    if not (ROOT / "baseline" / "_ref" / "planetary_sandbox").is_dir():
+        return None
+    env = dict(os.environ, PYTHONDONTWRITEBYTECODE="1")
+    t0 = time.perf_counter()
+    r = subprocess.run([sys.executable, str(script), str(rows), str(reps)], capture_output=True, text=True,
+                       env=env, timeout=900)
+    if r.returncode != 0:
+        print(f"reference CPU timing unavailable: {r.stderr.strip().splitlines()[-1:]}", file=sys.stderr)
+        return None
+    d = json.loads(r.stdout.strip().splitlines()[-1])
+    t = d["seconds_per_tendency"]
+    step_member = t * (NLAT / rows) * 4.0
+    desc = (f"the reference's own ShallowWaterModel.tendency (planetary_sandbox, NumPy in place of CuPy, its "
+            f"CUDA-C basis kernel built for the CPU) on {rows} of {NLAT} Gauss rows ({d['points']} points x "
+            f"{d['modes']} modes), timed {reps}x, scaled x{NLAT / rows:g} rows x4 stages x{B} members")
+    return 1.0 / (step_member * B), desc, time.perf_counter() - t0
+
+
+def cpu_baseline_sample(B: int, rows: int, reps: int = 1):
+    """(steps/s, description, seconds, kind): the reference's own code when
+    it runs here ("reference"), else the oracle restatement ("port")."""
+    own = reference_own_sample(B, rows, reps)
+    if own is not None:
+        return own + ("reference",)
+    return cpu_reference_sample(B, rows, reps) + ("port",)
+
+
 def run_reference(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return 0
     B = args.members
     cores = int(os.environ.get("OPENBLAS_NUM_THREADS", os.cpu_count() or 1))
+    kind = "port"
     if args.warmup > 0:
-        cpu_reference_sample(B, max(2, args.cpu_rows // 4), 1)
+        cpu_baseline_sample(B, max(2, args.cpu_rows // 4), 1)
     vals = []
     desc = ""
     for _ in range(max(args.steps, 1)):
-        v, desc, _ = cpu_reference_sample(B, args.cpu_rows, 1)
+        v, desc, _, kind = cpu_baseline_sample(B, args.cpu_rows, 1)
         vals.append(v)
     v = statistics.median(vals)
     line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 / v, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
             "config": workload_config(args, B),
-            "cpu_baseline": {"value": v, "unit": UNIT, "cores": cores, "kind": "port", "sample": desc},
+            "cpu_baseline": {"value": v, "unit": UNIT, "cores": cores, "kind": kind, "sample": desc},
             "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
     return 0
@@ -685,9 +723,9 @@ def main():
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
-        v, desc, _ = cpu_reference_sample(B, args.cpu_rows, 1)
+        v, desc, _, kind = cpu_baseline_sample(B, args.cpu_rows, 1)
         cpu = {"value": v, "unit": UNIT, "cores": int(os.environ.get("OPENBLAS_NUM_THREADS", "1")),
-               "kind": "port", "sample": desc}
+               "kind": kind, "sample": desc}
 
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,

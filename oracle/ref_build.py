@@ -1,7 +1,8 @@
 """Build recipe: compile the reference's basis kernel for the CPU (TEST INFRASTRUCTURE).
 
 Compiles src/planetary_sandbox/numerics/cuda/sh_matrix.cu from the reference
-checkout, where it lies, as plain C++ with g++: a prelude header turns
+checkout, where it lies (or from the reference package installed into the
+git-ignored baseline/_ref/ where the checkout is absent), as plain C++ with g++: a prelude header turns
 ``__global__`` into nothing and supplies ``blockIdx``/``blockDim``/
 ``threadIdx``; a stub ``cupy/complex.cuh`` maps ``complex<double>`` to
 ``std::complex<double>``; a generated launcher walks the launch grid.  The
@@ -20,7 +21,12 @@ from pathlib import Path
 HERE = Path(__file__).resolve().parent
 OUT = HERE / "_ref"
 REF_ROOT = Path(os.environ.get("AEOLUS_REFERENCE_ROOT", "/root/reference"))
-SH_MATRIX = REF_ROOT / "src/planetary_sandbox/numerics/cuda/sh_matrix.cu"
+# the checkout's source, else the copy installed with the reference package
+# into baseline/_ref (where the checkout is absent)
+_SRC = "planetary_sandbox/numerics/cuda/sh_matrix.cu"
+SH_MATRIX = REF_ROOT / "src" / _SRC
+if not SH_MATRIX.is_file():
+    SH_MATRIX = HERE.parent / "baseline" / "_ref" / _SRC
 LIB = OUT / "libref_sh_matrix.so"
 
 _PRELUDE = r"""

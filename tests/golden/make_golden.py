@@ -1,7 +1,7 @@
 """Generate golden vectors by running the reference's own code on this CPU.
 
 The reference (planetary_sandbox) is imported from its checkout with the
-NumPy stand-in for CuPy in ``tests/golden/refshim``; its CUDA-C basis kernel
+NumPy stand-in for CuPy in ``baseline/standin``; its CUDA-C basis kernel
 (src/planetary_sandbox/numerics/cuda/sh_matrix.cu) runs as C++ built by
 ``oracle/ref_build.py``.  Operators are built directly with a = 6.371e6 m and
 Omega = 7.292e-5 1/s, as the workloads specify (``Planet.generate`` would
@@ -28,7 +28,7 @@ HERE = Path(__file__).resolve().parent
 REPO = HERE.parents[1]
 REF_SRC = Path(os.environ.get("AEOLUS_REFERENCE_ROOT", "/root/reference")) / "src"
 sys.dont_write_bytecode = True
-sys.path[:0] = [str(HERE / "refshim"), str(REF_SRC), str(REPO)]
+sys.path[:0] = [str(REPO / "baseline" / "standin"), str(REF_SRC), str(REPO)]
 
 import planetary_sandbox.numerics as N  # noqa: E402
 from planetary_sandbox.physics.barotropic import BarotropicVorticity, BarotropicState  # noqa: E402
