@@ -24,7 +24,7 @@ import torch
 
 from . import _lib
 from ._lib import check
-from .ops import analyze, synthesize, vector_curl_div
+from .ops import analyze, spectral_op, synthesize, vector_curl_div, winds
 
 R_DRY = 287.04          # J kg^-1 K^-1, primitive_equations.py:49
 CP_DRY = 1004.64        # J kg^-1 K^-1
@@ -235,3 +235,64 @@ class PrimitiveEquationsModel:
 
     def tendency_state(self, state: PrimitiveEquationsState) -> PrimitiveEquationsState:
         return PrimitiveEquationsState(self.tendency(state.coeffs))
+
+    # -- state-grid reconstructions, characteristic speed, validation ------
+    def wind_on_state_grid(self, state: PrimitiveEquationsState):
+        """Per-level (u, v) on the state sampling, (nlev, n_points) each (:289-307)."""
+        psi = spectral_op(_lib.SOP_INV_LAPLACIAN_ZERO, self.R, state.zeta)
+        chi = spectral_op(_lib.SOP_INV_LAPLACIAN_ZERO, self.R, state.delta)
+        uv = winds(self.sh.plan.id, self.R, psi, chi)           # [2, nlev, n_points]
+        return uv[0], uv[1]
+
+    def temperature_on_state_grid(self, state: PrimitiveEquationsState) -> torch.Tensor:
+        return synthesize(self.sh.plan.id, state.temperature)
+
+    def surface_pressure_on_state_grid(self, state: PrimitiveEquationsState) -> torch.Tensor:
+        return torch.exp(synthesize(self.sh.plan.id, state.ln_ps))
+
+    def temperature_extrema(self, state: PrimitiveEquationsState):
+        """(min, max) of T over every level on the state and product samplings (:764-781)."""
+        plans = [self.sh.plan] + ([self._plan] if self._plan is not self.sh.plan else [])
+        ext = torch.stack([torch.stack(torch.aminmax(synthesize(p.id, state.temperature))) for p in plans])
+        lo, hi = ext[:, 0].min(), ext[:, 1].max()
+        return float(lo), float(hi)
+
+    def max_characteristic_speed(self, state: PrimitiveEquationsState) -> float:
+        """max_k max|V_k| + sqrt(gamma R_d T_max) (:783-797)."""
+        u, v = self.wind_on_state_grid(state)
+        wind_max = float(torch.sqrt(u * u + v * v).max())
+        _, t_max = self.temperature_extrema(state)
+        return wind_max + math.sqrt(self.gamma * self.r_dry * max(t_max, 0.0))
+
+    _MONOPOLE_RTOL = 1e-10
+
+    def validate_state(self, state: PrimitiveEquationsState, *, context: str = "") -> None:
+        """Raise PrimitiveEquationsStateError on a hard violation (:808-854):
+        shape, NaN/Inf, per-level zeta/delta monopoles, T > 0 over the state
+        and product samplings, finite exp(ln p_s) on the state grid."""
+        where = f" {context}" if context else ""
+        n = self.l_max + 1
+        expected = (3 * self.nlev + 1, n, n)
+        if tuple(state.coeffs.shape) != expected:
+            raise PrimitiveEquationsStateError(
+                f"state shape {tuple(state.coeffs.shape)} does not match the model's expected {expected}{where}")
+        if not bool(torch.isfinite(torch.view_as_real(state.coeffs)).all()):
+            raise PrimitiveEquationsStateError(f"primitive-equation state contains NaN/Inf coefficients{where}")
+        for name, stack in (("zeta", state.zeta), ("delta", state.delta)):
+            mono = stack[:, 0, 0].abs()
+            scale = torch.linalg.vector_norm(stack.reshape(self.nlev, -1), dim=1)
+            bad = (mono > self._MONOPOLE_RTOL * torch.clamp(scale, min=1e-30)).nonzero()
+            if bad.numel():
+                k = int(bad[0, 0])
+                raise PrimitiveEquationsStateError(
+                    f"{name} monopole is nonzero at level {k + 1}{where}: |a00| = {float(mono[k]):g} "
+                    f"(field norm {float(scale[k]):g}); the global mean of {name} must stay exactly zero on every "
+                    "level")
+        t_min, _ = self.temperature_extrema(state)
+        if not (t_min > 0.0):
+            raise PrimitiveEquationsStateError(
+                f"temperature is not strictly positive{where}: min(T) = {t_min:g} K over the state/product "
+                "samplings")
+        if not bool(torch.isfinite(self.surface_pressure_on_state_grid(state)).all()):
+            raise PrimitiveEquationsStateError(
+                f"surface pressure exp(ln p_s) overflowed to a non-finite value on the state grid{where}")

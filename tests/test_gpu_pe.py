@@ -21,7 +21,8 @@ from helpers import rel_l2, tri
 
 import aeolus_gb300 as ae
 from aeolus_gb300.barotropic import BarotropicState, BarotropicVorticity
-from aeolus_gb300.primitive_equations import (PrimitiveEquationsModel, PrimitiveEquationsStateError, SigmaGrid,
+from aeolus_gb300.primitive_equations import (PrimitiveEquationsModel, PrimitiveEquationsState,
+                                              PrimitiveEquationsStateError, SigmaGrid,
                                               isothermal_rest_state)
 
 pytestmark = pytest.mark.gpu
@@ -135,3 +136,50 @@ def test_pe_rejects_bad_inputs():
     with pytest.raises(ValueError, match="above the dealiased"):
         PrimitiveEquationsModel(planet, SigmaGrid.uniform(3), surface_geopotential_lm=bad)
     assert m.tendency(torch.zeros((0, 10, 11, 11), dtype=torch.complex128, device="cuda")).shape == (0, 10, 11, 11)
+
+
+def test_pe_characteristic_speed_and_extrema_match_oracle(golden):
+    """max|V| + sqrt(gamma R_d T_max) and the temperature extrema over the
+    state and product samplings (primitive_equations.py:764-797)."""
+    g = golden("pe_gauss16x32_L15_fine23x46_K5")
+    m = _model(g, *CASES["pe_gauss16x32_L15_fine23x46_K5"])
+    st = PrimitiveEquationsState(T(g["state"]))
+    K, L, R = m.nlev, m.l_max, float(g["radius"])
+    sh = oracle.GaussSH(16, 32, L)
+    nf, mf = oracle.fine_dims(16, 32, L)
+    shp = oracle.GaussSH(nf, mf, L)
+    s = g["state"]
+    tg = [x.inv_transform(s[2 * K + k]) for x in (sh, shp) for k in range(K)]
+    lo, hi = min(t.min() for t in tg), max(t.max() for t in tg)
+    assert m.temperature_extrema(st) == pytest.approx((lo, hi), rel=1e-13)
+    ops = oracle.Operators(sh, R)
+    inv = lambda c: ops.inv_laplacian_zero(c)  # noqa: E731
+    cosl = np.maximum(np.cos(sh.latitudes), 1e-8)
+    wmax = 0.0
+    for k in range(K):
+        psi, chi = inv(s[k]), inv(s[K + k])
+        lam = lambda c: sh.inv_transform(ops.d_lambda_coeffs(c))  # noqa: E731
+        snt = lambda c: sh.inv_transform(ops.sin_theta_d_theta_coeffs(c)) / R  # noqa: E731
+        u = (snt(psi) + lam(chi)) / cosl
+        v = (lam(psi) - snt(chi)) / cosl
+        wmax = max(wmax, float(np.sqrt(u * u + v * v).max()))
+    ref = wmax + np.sqrt(m.gamma * m.r_dry * hi)
+    assert m.max_characteristic_speed(st) == pytest.approx(ref, rel=1e-12)
+
+
+def test_pe_validate_state_faults_injected_on_host(golden):
+    g = golden("pe_gauss16x32_L15_fine23x46_K5")
+    m = _model(g, *CASES["pe_gauss16x32_L15_fine23x46_K5"])
+    K = m.nlev
+    good = T(g["state"])
+    m.validate_state(PrimitiveEquationsState(good))
+    cases = []
+    x = good.clone(); x[3, 4, 2] = complex(float("nan"), 0.0); cases.append((x, "NaN/Inf"))
+    x = good.clone(); x[K + 1, 0, 0] = 1e-3; cases.append((x, "delta monopole is nonzero at level 2"))
+    x = good.clone(); x[2 * K + 2, 0, 0] = -10.0; cases.append((x, "temperature is not strictly positive"))
+    x = good.clone(); x[3 * K, 0, 0] = 3000.0; cases.append((x, "overflowed"))
+    for bad, msg in cases:
+        with pytest.raises(PrimitiveEquationsStateError, match=msg):
+            m.validate_state(PrimitiveEquationsState(bad), context="in the test")
+    with pytest.raises(PrimitiveEquationsStateError, match="does not match"):
+        m.validate_state(PrimitiveEquationsState(good[:-3]))
