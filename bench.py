@@ -450,7 +450,11 @@ class ClockSampler:
         self.proc = None
         self.nvml = None
         self.samples = []
-        self.path = ROOT / "gpurun_out" / f"clocks_rank{index}.csv"
+        # the nvidia-smi fallback's raw samples (a directory chosen by the
+        # caller, else the system temporary directory)
+        import tempfile
+        out = os.environ.get("AEOLUS_BENCH_CLOCKS_DIR") or tempfile.gettempdir()
+        self.path = Path(out) / f"aeolus_clocks_rank{index}.csv"
 
     def _poll(self):
         while not self._stop.is_set():
@@ -471,7 +475,7 @@ class ClockSampler:
             self._thr.start()
             return self
         try:
-            self.path.parent.mkdir(exist_ok=True)
+            self.path.parent.mkdir(parents=True, exist_ok=True)
             self.fh = open(self.path, "w")
             self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.FIELDS}",
                                           "--format=csv,noheader,nounits", "-lms", "200"],
