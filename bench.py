@@ -580,6 +580,14 @@ NCU_TRAFFIC = {
 }
 
 
+# Warp instructions per launch of the same kernels (smsp__inst_executed.sum
+# of the same capture), for the instruction-issue roofline of the row stage.
+NCU_WARP_INSTRUCTIONS = {
+    "rows_fx_c2r_products_r2c": 344.3e6,
+}
+SM_COUNT, ISSUE_PER_SM_CLK = 152, 4  # GB300: 4 schedulers per SM, one warp instruction each per clock
+
+
 def _roofline(kstats, B, peaks):
     """Roofline entry for every library kernel; the dominant one first."""
     ftx = 2.0 * NLAT * (LMAX + 1) * (LMAX + 2)  # flops of one real-field Legendre transform (no fold credit)
@@ -602,6 +610,15 @@ def _roofline(kstats, B, peaks):
                              "frac": byt / t / 1e9 / hbm, "traffic": NCU_TRAFFIC.get(name), "launch_ms": t * 1000.0,
                              "work_per_launch": f"{B} members x {NLAT} rows x 13 spectra x (L+1) x 16 B",
                              "note": "bound by integer issue and barrier latency of the fixed-point FFTs, not by HBM"}
+            inst = NCU_WARP_INSTRUCTIONS.get(name)
+            if inst is not None and B == 64:
+                # instruction-issue roofline: warp instructions of one launch (ncu, same workload) over
+                # its event-timed duration, against 4 issue slots per SM per clock at the sampled clock
+                clk = peaks.get("_sm_mhz") or peaks.get("sm_max_mhz", 2070.0)
+                peak_issue = SM_COUNT * ISSUE_PER_SM_CLK * clk * 1e6
+                entries[name]["issue"] = {"warp_instructions_per_launch": inst, "achieved_per_s": inst / t,
+                                          "peak_per_s": peak_issue, "frac": inst / t / peak_issue,
+                                          "clock_mhz": clk}
         elif name.endswith("_f64"):
             fields = 9 if "synth" in name else 4
             useful = ftx * fields * B
@@ -715,6 +732,9 @@ def main():
     bytes_state = host_in.numel() * host_in.element_size()
 
     peaks = json.loads(PEAKS_FILE.read_text()) if PEAKS_FILE.exists() else {}
+    clock_summary = clk.summary()
+    if isinstance(clock_summary, dict) and clock_summary.get("sm_mhz"):
+        peaks["_sm_mhz"] = float(clock_summary["sm_mhz"])   # issue peak at the clock seen while timing
     roof, roof_all = _roofline(kstats, B, peaks)
     launches = sum(n for n, _ in kstats.values())
 
@@ -746,7 +766,7 @@ def main():
                         "wall_ms": e2e_wall_ms},
                 "gpu_launches": launches,
                 "kernels": {k: {"launches": n, "ms": ms} for k, (n, ms) in kstats.items()},
-                "roofline": roof, "roofline_all": roof_all, "cpu_baseline": cpu, "clocks": clk.summary()}
+                "roofline": roof, "roofline_all": roof_all, "cpu_baseline": cpu, "clocks": clock_summary}
         line.update(extras)
         print(json.dumps(line), flush=True)
     if world > 1:
