@@ -415,6 +415,25 @@ def run_cases():
     bve("run_bve_gauss16x32_L15_interval", 16, 32, 15, 4, 0.0, 1.5, dt_snapshots=40000.0,
         snapshot_mode="interval")
 
+    # geodesic planet with the res r+1 product co-grid: CFL from the minimum edge length
+    t0 = time.time()
+    p = geodesic_planet(3, 10, mode="fine")
+    zeta = W.bve_vorticity(10, 6)
+    with tempfile.TemporaryDirectory() as d:
+        out = Path(d)
+        times = E.count_snapshot_times(3, 1.0 * 86400.0)
+        run_bve(p, zeta.copy(), None, 1.0, out, 1e5, snapshot_times=times, snapshot_mode="count", plots=())
+        cols, rows = _csv_table(out / "diagnostics" / "timeseries.csv")
+        spec = np.load(out / "diagnostics" / "spectra.npz")
+        np.savez_compressed(
+            HERE / "run_bve_geodesic_res3_L10_fine_count.npz", res=3, lmax=10, radius=R, omega=OMEGA, nu=1e5,
+            zeta0=zeta, t_end_days=1.0, mode="count", snapshot_times=np.asarray(times, np.float64),
+            dt_snapshots=np.float64(0.0), coeffs=np.load(out / "vorticity_coeffs.npy"),
+            grid=np.load(out / "vorticity_grid.npy"), times=np.load(out / "bve_snapshot_times.npy"),
+            csv_cols=cols, csv_rows=rows, spec_times=spec["times"], energy_l=spec["energy_l"],
+            enstrophy_l=spec["enstrophy_l"])
+    print(f"run_bve_geodesic_res3_L10_fine_count: {time.time() - t0:.1f}s, {rows.shape[0]} rows")
+
 
 if __name__ == "__main__":
     if sys.argv[1:] == ["vector"]:

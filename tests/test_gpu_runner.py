@@ -131,3 +131,20 @@ def test_empty_count_schedule_writes_empty_stacks(tmp_path):
     assert np.load(tmp_path / "vorticity_coeffs.npy").shape == (0, 11, 11)
     assert np.load(tmp_path / "vorticity_grid.npy").shape[0] == 0
     assert np.load(tmp_path / RN.BVE_SNAPSHOT_TIMES_FILENAME).shape == (0,)
+
+
+def test_bve_run_on_geodesic_fine_cogrid_matches_reference_runner(golden, tmp_path):
+    """The reference's run_bve on a level-3 geodesic planet with the level-4
+    product co-grid: the CFL ceiling comes from the minimum edge length."""
+    g = golden("run_bve_geodesic_res3_L10_fine_count")
+    planet = ae.make_planet("geodesic", resolution=int(g["res"]), l_max=int(g["lmax"]), product_quadrature="fine",
+                            device=DEV)
+    RN.run_bve(planet, g["zeta0"], out_dir=tmp_path, t_end_days=float(g["t_end_days"]), viscosity=float(g["nu"]),
+               plots=(), **_schedule(g))
+    times = np.load(tmp_path / RN.BVE_SNAPSHOT_TIMES_FILENAME)
+    assert [t.hex() for t in times] == [t.hex() for t in g["times"]]
+    coeffs = np.load(tmp_path / "vorticity_coeffs.npy")
+    assert coeffs.shape == g["coeffs"].shape
+    for k in range(coeffs.shape[0]):
+        assert rel_l2(tri(coeffs[k]), tri(g["coeffs"][k])) <= COEFF_TOL
+    _compare_rows(tmp_path, g)
