@@ -66,6 +66,8 @@ def parse():
                     help="skip the ensemble (uneven l_max BVE) and adjoint (SWE gradient) side measurements")
     ap.add_argument("--side", choices=["ensemble", "adjoint", "geodesic", "pe"], default=None,
                     help="run only this side measurement (one JSON object); for profiling runs")
+    ap.add_argument("--geo-res", type=int, default=6, help="geodesic level of --side geodesic (profiling runs)")
+    ap.add_argument("--geo-lmax", type=int, default=127, help="l_max of --side geodesic (profiling runs)")
     ap.add_argument("--knobs", default="",
                     help="launch shapes of the measured model as 5 comma-separated ints (bc_synth, bc_anal, "
                          "row_threads, slice_synth, slice_anal) instead of autotuning; for profiling runs")
@@ -192,7 +194,7 @@ def adjoint_measure(dev, members: int = 8, nsteps: int = 48, every: int = 8, dt:
     return out
 
 
-def geodesic_measure(dev, fields: int = 64, reps: int = 3):
+def geodesic_measure(dev, fields: int = 64, reps: int = 3, res: int = 6, lmax: int = 127):
     """Config c3: level-6 icosahedral grid (40,962 points, Voronoi weights),
     l_max 127 (16,384 real basis columns), one synthesis and one quadrature
     analysis of `fields` seeded fields, FP64 basis GEMMs vs the bf16-digit
@@ -203,18 +205,19 @@ def geodesic_measure(dev, fields: int = 64, reps: int = 3):
     from aeolus_gb300.ops import Plan, analyze, synthesize
 
     t0 = time.perf_counter()
-    sh = GeodesicSphericalHarmonics(GeodesicGridGeometry(6, 6.371e6, dev), 127, weights="voronoi")
+    sh = GeodesicSphericalHarmonics(GeodesicGridGeometry(res, 6.371e6, dev), lmax, weights="voronoi")
     p64 = sh.plan
-    psp = Plan.points(sh.latitudes.cpu().numpy(), sh.longitudes.cpu().numpy(), sh.weights.cpu().numpy(), 127,
+    psp = Plan.points(sh.latitudes.cpu().numpy(), sh.longitudes.cpu().numpy(), sh.weights.cpu().numpy(), lmax,
                       device=dev)
     psp.set_precision(_lib.PREC_SPLIT_BF16)
     torch.cuda.synchronize(dev)
     build_s = time.perf_counter() - t0
     rng = np.random.default_rng(5)
-    a = torch.as_tensor(np.stack([W.random_spectrum(rng, 127, -1.5, 1.0, zero_monopole=False)
+    a = torch.as_tensor(np.stack([W.random_spectrum(rng, lmax, -1.5, 1.0, zero_monopole=False)
                                   for _ in range(fields)]), device=dev)
-    out = {"workload": "geodesic_level6_40962pts_lmax127_64fields", "points": p64.n_points,
-           "basis_columns": 128 * 128, "fields": fields, "plans_build_s": build_s}
+    ncols = (lmax + 1) ** 2
+    out = {"workload": f"geodesic_level{res}_{p64.n_points}pts_lmax{lmax}_{fields}fields", "points": p64.n_points,
+           "basis_columns": ncols, "fields": fields, "plans_build_s": build_s}
     res = {}
     for name, plan in (("fp64", p64), ("split", psp)):
         g = synthesize(plan.id, a)
@@ -228,7 +231,7 @@ def geodesic_measure(dev, fields: int = 64, reps: int = 3):
         e1.record()
         torch.cuda.synchronize(dev)
         ms = e0.elapsed_time(e1) / reps
-        useful = 2.0 * 2.0 * p64.n_points * 128 * 128 * fields
+        useful = 2.0 * 2.0 * p64.n_points * ncols * fields
         res[name] = (g, c)
         out[name] = {"ms_synthesis_plus_analysis": ms, "useful_tflops": useful / ms / 1e9}
     out["rel_l2_split_vs_fp64"] = {
@@ -647,9 +650,11 @@ def main():
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
     if args.side:
-        fn = {"ensemble": ensemble_measure, "adjoint": adjoint_measure, "geodesic": geodesic_measure,
-              "pe": pe_measure}[args.side]
-        print(json.dumps({args.side: fn(dev)}))
+        if args.side == "geodesic":
+            res = geodesic_measure(dev, res=args.geo_res, lmax=args.geo_lmax)
+        else:
+            res = {"ensemble": ensemble_measure, "adjoint": adjoint_measure, "pe": pe_measure}[args.side](dev)
+        print(json.dumps({args.side: res}))
         return 0
 
     import aeolus_gb300 as ae
