@@ -144,3 +144,22 @@ def test_split_worst_case_growth_matches_fp64(nlat, nlon, L, scale):
     for b in range(2):
         assert rel_l2(gs[b], g64[b]) < 1e-12, (b, rel_l2(gs[b], g64[b]))
         assert rel_l2(cs[b], c64[b]) < 1e-12, (b, rel_l2(cs[b], c64[b]))
+
+
+def test_c2_williamson2_100_steps_split_vs_fp64():
+    """The shallow-water plain-vs-split workload: Gauss 128x256, l_max 85,
+    Williamson-2 plus the seeded 1 % perturbation, dt = 300 s, 100 RK4 steps
+    on both paths; every field within 1e-10 relative L2 of the FP64 path."""
+    L, nlat, nlon = 85, 128, 256
+    s0, depth = W.perturbed_williamson2(L, seed=2)
+    out = {}
+    for prec in ("fp64", "split"):
+        planet = ae.make_planet("latlon", nlat=nlat, nlon=nlon, l_max=L)
+        if prec == "split":
+            planet.so._product_space.sh.plan.set_precision(_lib.PREC_SPLIT_BF16)
+        m = ShallowWaterModel(planet, gravity=W.GRAVITY, mean_depth=depth)
+        out[prec] = N(m.rk4(T(s0), 300.0, 100))
+    for f in range(3):
+        err = rel_l2(out["split"][f], out["fp64"][f])
+        assert err < 1e-10, (f, err)
+    assert np.isfinite(out["fp64"]).all()
