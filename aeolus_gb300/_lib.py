@@ -37,7 +37,7 @@ class PeParams(ctypes.Structure):
 
 class SweParams(ctypes.Structure):
     _fields_ = [("radius", c_double), ("omega", c_double), ("gravity", c_double),
-                ("mean_depth", c_double), ("nu4", c_double)]
+                ("mean_depth", c_double), ("nu4", c_double), ("forcing", c_void_p)]
 
 
 # name -> (restype, argtypes); mirrors include/aeolus_gb300.h exactly.

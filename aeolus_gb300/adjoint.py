@@ -50,7 +50,8 @@ class _SweRk4Checkpointed(torch.autograd.Function):
             for _ in range(n - 1):
                 states.append(m.rk4(states[-1], ctx.dt, 1, check=False))
             for i in range(n - 1, -1, -1):
-                yb = swe_rk4_adjoint(m._plan.id, m.R, m.Omega, m.gravity, m.mean_depth, m.nu4, states[i], yb, ctx.dt)
+                yb = swe_rk4_adjoint(m._plan.id, m.R, m.Omega, m.gravity, m.mean_depth, m.nu4, states[i], yb, ctx.dt,
+                                     m.forcing)
         return yb, None, None, None, None
 
 

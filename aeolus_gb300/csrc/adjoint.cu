@@ -461,6 +461,7 @@ extern "C" int aeolus_swe_rk4_adjoint(aeolus_plan plan, const aeolus_swe_params*
     SweDerive d{sp, in, fp, cor, 2.0 * p->omega};
     Rk4 rk{stage, dt, y0, next[stage - 1], kacc, nullptr};
     SweEpi e{sp, in, phi0, p->nu4, rk, spec_cor ? 2.0 * p->omega : 0.0, cor};
+    e.forcing = reinterpret_cast<const double2*>(p->forcing);
     if ((s = run_full_chain(plan, d, pw, e, batch, chain, nullptr, st))) return s;
     in = next[stage - 1];
   }

@@ -268,6 +268,7 @@ struct SweModel {
     d = SweDerive{sp, in, fp, cor, 2.0 * q.omega};
     pw = SwePw{fp, phi0, (float)phi0};
     e = SweEpi{sp, in, phi0, q.nu4, Rk4{stage, dt, y0, next, b.acc, nullptr}, spec_cor ? 2.0 * q.omega : 0.0, cor};
+    e.forcing = reinterpret_cast<const double2*>(q.forcing);
   }
 };
 

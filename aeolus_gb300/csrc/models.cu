@@ -439,6 +439,7 @@ extern "C" int aeolus_swe_tendency(aeolus_plan plan, const aeolus_swe_params* p,
   SwePw pw{fp, phi0, (float)phi0};
   Rk4 rk{0, 0.0, nullptr, nullptr, nullptr, reinterpret_cast<double2*>(tend)};
   SweEpi e{sp, reinterpret_cast<const double2*>(state), phi0, p->nu4, rk, spec_cor ? 2.0 * p->omega : 0.0, cor};
+  e.forcing = reinterpret_cast<const double2*>(p->forcing);
   return run_full_chain(plan, d, pw, e, batch, work, nullptr, static_cast<cudaStream_t>(stream));
 }
 
@@ -504,6 +505,7 @@ extern "C" int aeolus_swe_rk4(aeolus_plan plan, const aeolus_swe_params* p, doub
       SweDerive d{sp, in, fp, cor, 2.0 * p->omega};
       Rk4 rk{stage, dt, y0, next, acc, nullptr};
       SweEpi e{sp, in, phi0, p->nu4, rk, spec_cor ? 2.0 * p->omega : 0.0, cor};
+      e.forcing = reinterpret_cast<const double2*>(p->forcing);
       if ((s = run_full_chain(plan, d, pw, e, batch, chain, status, st))) return s;
     }
   return AEOLUS_OK;

@@ -353,6 +353,7 @@ struct SweEpi {
   Rk4 rk;
   double two_omega;      // > 0: add the Coriolis terms spectrally
   const double2* cor = nullptr;  // their spectra tabulated by SweDerive (else computed here)
+  const double2* forcing = nullptr;  // constant [3][L+1][L+1] terms (bottom topography), or none
   __device__ void finish(int b, int l, int m, const double2* an_in) const {
     const int L = s.L;
     const int cut = (2 * L) / 3;
@@ -389,12 +390,18 @@ struct SweEpi {
     double2 k0 = a0;
     double2 k1 = csub(a1, cscale(lap, cadd(a2, ps)));
     double2 k2 = csub(a3, cscale(phi0, ds));
+    const long fo = (long)l * (L + 1) + m;
+    if (forcing) {  // -lap(phi_s) joins the divergence tendency before the hyperdiffusion
+      k0 = cadd(k0, forcing[fo]);
+      k1 = cadd(k1, forcing[n2 + fo]);
+    }
     if (nu4 > 0.0) {
       const double h = nu4 * (lap * lap);
       k0 = csub(k0, cscale(h, zs));
       k1 = csub(k1, cscale(h, ds));
       k2 = csub(k2, cscale(h, ps));
     }
+    if (forcing) k2 = cadd(k2, forcing[2 * n2 + fo]);  // after it, as -nu4 lap^2 phi_s
     if (l == 0) k0 = k1 = k2 = z0;
     rk.apply(base, k0);
     rk.apply(base + n2, k1);

@@ -136,7 +136,8 @@ class ShallowWaterEnsemble(_Ensemble):
         n = len(self.models)
         plans = (c_void_p * n)(*[m._plan.handle.value for m in self.models])
         bs = (c_int * n)(*self.batches)
-        prm = (_lib.SweParams * n)(*[_lib.SweParams(m.R, m.Omega, m.gravity, m.mean_depth, m.nu4)
+        # each model keeps its forcing tensor (bottom topography) alive for the ensemble's lifetime
+        prm = (_lib.SweParams * n)(*[_lib.SweParams(m.R, m.Omega, m.gravity, m.mean_depth, m.nu4, m.forcing_ptr())
                                      for m in self.models])
         self.handle = c_void_p()
         check(_lib.load().aeolus_ensemble_create_swe(n, ctypes.cast(plans, ctypes.POINTER(c_void_p)), bs, prm,

@@ -256,8 +256,16 @@ def _bve_params(radius, omega, nu):
     return _lib.BveParams(float(radius), float(omega), float(nu))
 
 
-def _swe_params(radius, omega, gravity, mean_depth, nu4):
-    return _lib.SweParams(float(radius), float(omega), float(gravity), float(mean_depth), float(nu4))
+def _swe_params(radius, omega, gravity, mean_depth, nu4, forcing=None, L=None, device=None):
+    """The C parameter block; `forcing` is the constant [3, L+1, L+1] complex
+    spectral forcing of bottom topography (or None)."""
+    fp = None
+    if forcing is not None:
+        if forcing.dtype != torch.complex128 or tuple(forcing.shape) != (3, L + 1, L + 1) \
+                or not forcing.is_contiguous() or forcing.device != device:
+            raise ValueError(f"forcing must be a contiguous complex128 [3, {L + 1}, {L + 1}] tensor on {device}")
+        fp = forcing.data_ptr()
+    return _lib.SweParams(float(radius), float(omega), float(gravity), float(mean_depth), float(nu4), fp)
 
 
 @torch.library.custom_op("aeolus::bve_tendency", mutates_args=())
@@ -278,14 +286,14 @@ def bve_tendency(plan_id: int, radius: float, omega: float, nu: float, zeta: tor
 
 @torch.library.custom_op("aeolus::swe_tendency", mutates_args=())
 def swe_tendency(plan_id: int, radius: float, omega: float, gravity: float, mean_depth: float, nu4: float,
-                 state: torch.Tensor) -> torch.Tensor:
+                 state: torch.Tensor, forcing: torch.Tensor | None = None) -> torch.Tensor:
     p = _PLANS[plan_id]
     s, lead = _flat_spec(state, p.lmax, 3)
     out = torch.empty_like(s)
     B = s.shape[0]
     if B:
         w = p.workspace(_lib.OP_SWE_TENDENCY, B)
-        prm = _swe_params(radius, omega, gravity, mean_depth, nu4)
+        prm = _swe_params(radius, omega, gravity, mean_depth, nu4, forcing, p.lmax, s.device)
         check(_lib.load().aeolus_swe_tendency(p.handle, byref(prm), _ptr(s), _ptr(out), B, _ptr(w), w.numel(),
                                               _stream(s.device)))
     return out.reshape(lead + (3,) + _spec_shape(p.lmax))
@@ -308,7 +316,8 @@ def bve_rk4(plan_id: int, radius: float, omega: float, nu: float, zeta: torch.Te
 
 @torch.library.custom_op("aeolus::swe_rk4", mutates_args=())
 def swe_rk4(plan_id: int, radius: float, omega: float, gravity: float, mean_depth: float, nu4: float,
-            state: torch.Tensor, dt: float, nsteps: int) -> tuple[torch.Tensor, torch.Tensor]:
+            state: torch.Tensor, dt: float, nsteps: int,
+            forcing: torch.Tensor | None = None) -> tuple[torch.Tensor, torch.Tensor]:
     """(new state, per-member status bits OR-ed over every stage)."""
     p = _PLANS[plan_id]
     s, lead = _flat_spec(state, p.lmax, 3)
@@ -317,7 +326,7 @@ def swe_rk4(plan_id: int, radius: float, omega: float, gravity: float, mean_dept
     status = torch.zeros(B, dtype=torch.int32, device=y.device)
     if B and nsteps > 0:
         w = p.workspace(_lib.OP_SWE_RK4, B)
-        prm = _swe_params(radius, omega, gravity, mean_depth, nu4)
+        prm = _swe_params(radius, omega, gravity, mean_depth, nu4, forcing, p.lmax, y.device)
         check(_lib.load().aeolus_swe_rk4(p.handle, byref(prm), _ptr(y), B, float(dt), int(nsteps), _ptr(status),
                                          _ptr(w), w.numel(), _stream(y.device)))
     return y.reshape(lead + (3,) + _spec_shape(p.lmax)), status.reshape(lead)
@@ -436,16 +445,18 @@ def bve_tendency_adjoint(plan_id: int, radius: float, omega: float, nu: float, z
 
 @torch.library.custom_op("aeolus::swe_rk4_adjoint", mutates_args=())
 def swe_rk4_adjoint(plan_id: int, radius: float, omega: float, gravity: float, mean_depth: float, nu4: float,
-                    state: torch.Tensor, state_bar: torch.Tensor, dt: float) -> torch.Tensor:
+                    state: torch.Tensor, state_bar: torch.Tensor, dt: float,
+                    forcing: torch.Tensor | None = None) -> torch.Tensor:
     """Adjoint of one RK4 step taken from `state`: maps the adjoint of the
-    step's output to that of its input."""
+    step's output to that of its input (a constant forcing only shifts the
+    recomputed stage inputs)."""
     p = _PLANS[plan_id]
     s, lead = _flat_spec(state, p.lmax, 3)
     yb = _flat_spec(state_bar, p.lmax, 3)[0].clone()
     B = s.shape[0]
     if B:
         w = p.workspace(_lib.OP_SWE_RK4_ADJOINT, B)
-        prm = _swe_params(radius, omega, gravity, mean_depth, nu4)
+        prm = _swe_params(radius, omega, gravity, mean_depth, nu4, forcing, p.lmax, s.device)
         check(_lib.load().aeolus_swe_rk4_adjoint(p.handle, byref(prm), _ptr(s), _ptr(yb), B, float(dt), _ptr(w),
                                                  w.numel(), _stream(s.device)))
     return yb.reshape(lead + (3,) + _spec_shape(p.lmax))

@@ -409,7 +409,8 @@ class SWEDiagnosticsRecorder:
     """Shallow-water rows (run/swe/diagnostics.py:90-173): winds and total
     geopotential on the state grid, extrema over the state and product
     samplings from the library's validation kernel, spectral mass,
-    quadrature energy and L2 norms from its invariant kernel (flat bottom)."""
+    quadrature energy and L2 norms from its invariant kernel, plus the
+    topographic terms of the energy and free-surface anomaly over terrain."""
 
     def __init__(self, model, out_dir):
         self.model = model
@@ -422,9 +423,19 @@ class SWEDiagnosticsRecorder:
         m = self.model
         f = m.characteristic_fields(state)
         phi_min, phi_max = f["phi_total_extrema"]
-        eta = (f["phi_total"] - m.phi0) / m.gravity
-        w_max, e_min, e_max = torch.stack([f["wind_speed"].max(), eta.min(), eta.max()]).tolist()
+        phi_s = m.surface_geopotential_on_state_grid()
+        if phi_s is None:
+            eta = (f["phi_total"] - m.phi0) / m.gravity
+            topo_energy = torch.zeros((), dtype=torch.float64, device=eta.device)
+        else:
+            # free-surface anomaly and the topographic potential energy Phi phi_s
+            mean_phi_s = float(m.phi_s_lm[0, 0].real) / math.sqrt(4.0 * math.pi)
+            eta = (f["phi_total"] - m.phi0 + (phi_s - mean_phi_s)) / m.gravity
+            topo_energy = torch.sum(m.sh.weights * self.R ** 2 * f["phi_total"] * phi_s)
+        w_max, e_min, e_max, e_topo = torch.stack([f["wind_speed"].max(), eta.min(), eta.max(),
+                                                   topo_energy]).tolist()
         inv = m.invariants(state)
+        inv["total_energy"] += e_topo
         max_char = w_max + math.sqrt(max(phi_max, 0.0))
         row = {"time_s": t, "dt_s": dt, "step": step, "max_wind_ms": w_max, "max_char_speed_ms": max_char,
                "cfl": (max_char * dt / self.length_scale) if (self.length_scale and dt > 0) else float("nan"),

@@ -1,7 +1,8 @@
 """Rotating shallow-water core on the GB300 path.
 
-Mirrors src/planetary_sandbox/physics/shallow_water.py:102-539 (flat
-bottom).  ``tendency`` is one fused chain on the product space: nine
+Mirrors src/planetary_sandbox/physics/shallow_water.py:102-539, bottom
+topography included (constant spectral forcing terms).  ``tendency`` is one
+fused chain on the product space: nine
 syntheses (u cos, v cos, eta_lam, eta_snt, phi_lam, phi_snt, zeta, delta,
 phi), the pointwise flux products, four analyses, the 2/3 cut and the exact
 linear terms.  ``rk4`` advances whole steps on the device and checks every
@@ -62,8 +63,6 @@ class ShallowWaterModel:
             raise ValueError(f"mean_depth must be finite and > 0, got {mean_depth}")
         if not (math.isfinite(hyperdiffusion_nu4) and hyperdiffusion_nu4 >= 0):
             raise ValueError(f"hyperdiffusion_nu4 must be finite and >= 0, got {hyperdiffusion_nu4}")
-        if topography is not None and not getattr(topography, "is_flat", False):
-            raise ValueError("bottom topography is not part of the GB300 shallow-water path (flat bottom only)")
         self.planet = planet
         self.sh = planet.sh
         self.so = planet.so
@@ -83,8 +82,50 @@ class ShallowWaterModel:
         self._ps = self.so.backend.product_space(self.so.product_quadrature)
         self._plan = self._ps.sh.plan
         self._state_plan = self.sh.plan
-        self.has_topography = False
-        self.surface_elevation_extrema = (0.0, 0.0)
+        self._set_topography(topography)
+
+    # -- bottom topography (shallow_water.py:226-271) ------------------------
+    def _set_topography(self, topography):
+        """phi_s = g h_s enters as constant spectral terms: -lap(phi_s) in the
+        divergence tendency and, with hyperdiffusion, -nu4 lap^2 phi_s' (the
+        mean-removed anomaly) in the geopotential tendency.  They are handed
+        to the kernels as one [3, L+1, L+1] forcing array; a flat bottom
+        passes none, so its path is unchanged."""
+        from .topography import Topography
+
+        n = self.l_max + 1
+        dev = self.lap_eigs.device
+        if topography is None:
+            topography = Topography.flat(self.l_max)
+        if topography.l_max != self.l_max:
+            raise ValueError(f"topography truncation l_max={topography.l_max} does not match the model's "
+                             f"l_max={self.l_max}")
+        self.topography = topography
+        self.has_topography = not topography.is_flat
+        self.forcing = None
+        if self.has_topography:
+            self.phi_s_lm = topography.surface_geopotential_lm(self.gravity).to(dev)
+            self.phi_s_anom_lm = self.phi_s_lm.clone()
+            self.phi_s_anom_lm[0, 0] = 0.0
+            lap = self.lap_eigs[:, None]
+            f = torch.zeros((3, n, n), dtype=torch.complex128, device=dev)
+            f[DELTA] = -(lap * self.phi_s_lm)
+            if self.nu4 > 0.0:
+                f[PHI] = -(self.nu4 * lap ** 2 * self.phi_s_anom_lm)
+            f[:, 0, :] = 0.0
+            self.forcing = f.contiguous()
+            samplings = [self.sh] + ([self._ps.sh] if self._ps.sh is not self.sh else [])
+            ext = [torch.aminmax(topography.elevation_on(sh)) for sh in samplings]
+            self.surface_elevation_extrema = (min(float(e.min) for e in ext), max(float(e.max) for e in ext))
+            self._phi_s_state = self.sh.inv_transform(self.phi_s_lm)
+        else:
+            self.phi_s_lm = torch.zeros((n, n), dtype=torch.complex128, device=dev)
+            self.phi_s_anom_lm = torch.zeros((n, n), dtype=torch.complex128, device=dev)
+            self.surface_elevation_extrema = (0.0, 0.0)
+            self._phi_s_state = None
+
+    def forcing_ptr(self):
+        return None if self.forcing is None else self.forcing.data_ptr()
 
     # -- Helmholtz / winds -------------------------------------------------
     def _inv_laplacian(self, coeffs):
@@ -99,12 +140,14 @@ class ShallowWaterModel:
         return uv[0], uv[1]
 
     def surface_geopotential_on_state_grid(self):
-        return None
+        """phi_s on the state sampling, or None for a flat bottom (:327-334)."""
+        return self._phi_s_state
 
     # -- tendencies ----------------------------------------------------------
     def tendency(self, coeffs: torch.Tensor) -> torch.Tensor:
         """d/dt of the (..., 3, L+1, L+1) stack, shallow_water.py:347-418."""
-        return swe_tendency(self._plan.id, self.R, self.Omega, self.gravity, self.mean_depth, self.nu4, coeffs)
+        return swe_tendency(self._plan.id, self.R, self.Omega, self.gravity, self.mean_depth, self.nu4, coeffs,
+                            self.forcing)
 
     def tendency_state(self, state: ShallowWaterState) -> ShallowWaterState:
         return ShallowWaterState(self.tendency(state.coeffs))
@@ -114,7 +157,7 @@ class ShallowWaterModel:
         grid on the device; with ``check`` the bits are read once at the end
         and a violation raises ShallowWaterStateError."""
         y, status = swe_rk4(self._plan.id, self.R, self.Omega, self.gravity, self.mean_depth, self.nu4, coeffs,
-                            float(dt), int(nsteps))
+                            float(dt), int(nsteps), self.forcing)
         if check:
             bits = _or_bits(status)
             if bits:
@@ -193,8 +236,13 @@ class ShallowWaterModel:
         if bits & _lib.STATE_MONOPOLE:
             parts.append("a monopole (zeta, delta or phi a00) is nonzero; the global mean must stay exactly zero")
         if bits & _lib.STATE_THICKNESS:
+            terrain = ""
+            if self.has_topography:
+                terrain = (f" (bottom topography {self.topography.describe()}, max surface elevation "
+                           f"{self.surface_elevation_extrema[1]:g} m vs mean fluid thickness {self.mean_depth:g} m "
+                           "— the terrain may protrude through the fluid layer)")
             parts.append(f"fluid thickness is not strictly positive (min(Phi0 + phi) <= 0, Phi0 = {self.phi0:g}); "
-                         "the fluid depth has collapsed")
+                         f"the fluid depth has collapsed{terrain}")
         return "; ".join(parts) + (f" {where}" if where else "")
 
     def validate_state(self, state: ShallowWaterState, *, context: str = "") -> None:

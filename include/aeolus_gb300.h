@@ -89,6 +89,11 @@ typedef struct {
   double gravity;      /* g [m/s^2]                                       */
   double mean_depth;   /* H [m]; Phi0 = g H                               */
   double nu4;          /* hyperdiffusion [m^4/s], shallow_water.py:405-413 */
+  const double* forcing;  /* NULL, or a constant DEVICE spectral forcing
+                           * [3][L+1][L+1] complex added to every tendency
+                           * evaluation: bottom topography's -lap(phi_s) on
+                           * delta and -nu4 lap^2 phi_s' on phi
+                           * (shallow_water.py:397-413); row l = 0 ignored */
 } aeolus_swe_params;
 
 const char* aeolus_last_error(void);

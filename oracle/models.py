@@ -52,7 +52,7 @@ class SWE:
     """Shallow-water model, shallow_water.py:144-418 (flat bottom, nu4 >= 0)."""
 
     def __init__(self, ops, omega: float, gravity: float, mean_depth: float,
-                 nu4: float = 0.0):
+                 nu4: float = 0.0, elevation_lm=None):
         self.ops = ops
         self.R = ops.R
         self.Omega = float(omega)
@@ -64,6 +64,13 @@ class SWE:
         self.f_lm = f_lm(self.l_max, omega)
         l = np.arange(self.l_max + 1.0)
         self.lap_eigs = -l * (l + 1.0) / self.R ** 2
+        # bottom topography, shallow_water.py:226-271: phi_s = g h_s and its
+        # mean-removed anomaly enter as constant spectral terms
+        self.phi_s = None
+        if elevation_lm is not None and np.any(elevation_lm):
+            self.phi_s = self.gravity * np.asarray(elevation_lm, complex)
+            self.phi_s_anom = self.phi_s.copy()
+            self.phi_s_anom[0, 0] = 0.0
 
     def _inv_lap(self, c):                                    # :277-281
         out = np.zeros_like(c)
@@ -109,9 +116,13 @@ class SWE:
         ke_c = o.truncate(sh.transform(ke_g))
         phi_dot = o.truncate(sh.transform(phi_dot_g)) - self.phi0 * delta
         delta_dot = curl_c - self.lap_eigs[:, None] * (ke_c + phi)
+        if self.phi_s is not None:                            # :397-401
+            delta_dot = delta_dot - self.lap_eigs[:, None] * self.phi_s
         out = np.stack([zeta_dot, delta_dot, phi_dot])
         if self.nu4 > 0.0:
             out -= self.nu4 * (self.lap_eigs[None, :, None] ** 2) * coeffs
+            if self.phi_s is not None:                        # :408-413
+                out[2] -= self.nu4 * (self.lap_eigs[:, None] ** 2) * self.phi_s_anom
         out[:, 0, :] = 0.0
         return out
 

@@ -7,7 +7,7 @@ NumPy stand-in for CuPy in ``baseline/standin``; its CUDA-C basis kernel
 Omega = 7.292e-5 1/s, as the workloads specify (``Planet.generate`` would
 derive different constants and random terrain).
 
-Run:  PYTHONDONTWRITEBYTECODE=1 python tests/golden/make_golden.py [vector|runs|geodesic_fine|pe]
+Run:  PYTHONDONTWRITEBYTECODE=1 python tests/golden/make_golden.py [vector|runs|geodesic_fine|pe|topo]
 Writes ``tests/golden/*.npz`` (with ``vector``: only the weak-form curl/div
 fixtures; with ``runs``: only the integration-engine events and the run
 capsules of the reference's BVE/SWE runners).  Only l_max <= 85 fixtures are made: above
@@ -169,6 +169,48 @@ def geodesic_fine_case(name, res, lmax, seed=19, dt=600.0):
     print(f"{name}: {time.time() - t0:.1f}s")
 
 
+def topo_cases():
+    """The reference's shallow-water model over a Gaussian mountain
+    (physics/topography.py:207-292, shallow_water.py:226-271, :397-413):
+    terrain coefficients, tendency and RK4 steps, with and without
+    hyperdiffusion, and a run capsule of run_swe."""
+    import tempfile
+    from planetary_sandbox.physics.topography import Topography
+    from planetary_sandbox.physics.shallow_water import ShallowWaterState
+    from planetary_sandbox.run.swe.runner import run_swe
+    from planetary_sandbox.run import engine as E
+    t0 = time.time()
+    nlat, nlon, L = 32, 64, 21
+    p = latlon_planet(nlat, nlon, L)
+    topo = Topography.mountain(p, height_m=2000.0, lat_deg=30.0, lon_deg=90.0, width_deg=20.0)
+    state, depth = W.perturbed_williamson2(L, 29)
+    out = {}
+    for nu4 in (0.0, 1.0e16):
+        m = ShallowWaterModel(p, gravity=G, mean_depth=depth, hyperdiffusion_nu4=nu4, topography=topo)
+        key = "nu4" if nu4 else "plain"
+        out[f"tendency_{key}"] = m.tendency(state.copy())
+        y = state.copy()
+        for _ in range(2):
+            y = rk4_step_array(m.tendency, y, 0.0, 300.0)
+        out[f"rk4_{key}"] = y
+    m = ShallowWaterModel(p, gravity=G, mean_depth=depth, topography=topo)
+    ext = m.surface_elevation_extrema
+    with tempfile.TemporaryDirectory() as d:
+        o = Path(d)
+        times = E.count_snapshot_times(3, 0.05 * 86400.0)
+        run_swe(m, ShallowWaterState(state.copy()), None, 0.05, o, snapshot_times=times, snapshot_mode="count",
+                plots=())
+        cols, rows = _csv_table(o / "diagnostics" / "timeseries.csv")
+        np.savez_compressed(
+            HERE / "topo_swe_gauss32x64_L21_mountain.npz", nlat=nlat, nlon=nlon, lmax=L, radius=R, omega=OMEGA,
+            gravity=G, mean_depth=depth, nu4=1.0e16, dt=300.0, steps=2, height_m=2000.0, lat_deg=30.0,
+            lon_deg=90.0, width_deg=20.0, elevation_lm=np.asarray(topo.elevation_lm), state=state,
+            elevation_extrema=np.array(ext), t_end_days=0.05, snapshot_times=np.asarray(times, np.float64),
+            coeffs=np.load(o / "swe_coeffs.npy"), times=np.load(o / "swe_snapshot_times.npy"), csv_cols=cols,
+            csv_rows=rows, **out)
+    print(f"topo_swe_gauss32x64_L21_mountain: {time.time() - t0:.1f}s")
+
+
 def pe_state(lmax, nlev, seed, l_band=None, t0=260.0, ps0=101325.0):
     """Isothermal rest state plus seeded band-limited perturbations of every
     prognostic (the recipe of the reference's tests/test_pe_tendency.py:80-108)."""
@@ -247,6 +289,7 @@ def main():
     geodesic_case("geodesic_res3_L10", 3, 10)
     geodesic_fine_case("geodesic_fine_res3_L10", 3, 10)
     pe_cases()
+    topo_cases()
     vector_cases()
 
 
@@ -438,6 +481,8 @@ def run_cases():
 if __name__ == "__main__":
     if sys.argv[1:] == ["vector"]:
         vector_cases()
+    elif sys.argv[1:] == ["topo"]:
+        topo_cases()
     elif sys.argv[1:] == ["pe"]:
         pe_cases()
     elif sys.argv[1:] == ["geodesic_fine"]:
