@@ -7,7 +7,7 @@ NumPy stand-in for CuPy in ``baseline/standin``; its CUDA-C basis kernel
 Omega = 7.292e-5 1/s, as the workloads specify (``Planet.generate`` would
 derive different constants and random terrain).
 
-Run:  PYTHONDONTWRITEBYTECODE=1 python tests/golden/make_golden.py [vector|runs|geodesic_fine|pe|topo]
+Run:  PYTHONDONTWRITEBYTECODE=1 python tests/golden/make_golden.py [vector|runs|geodesic_fine|pe|topo|ic]
 Writes ``tests/golden/*.npz`` (with ``vector``: only the weak-form curl/div
 fixtures; with ``runs``: only the integration-engine events and the run
 capsules of the reference's BVE/SWE runners).  Only l_max <= 85 fixtures are made: above
@@ -211,6 +211,28 @@ def topo_cases():
     print(f"topo_swe_gauss32x64_L21_mountain: {time.time() - t0:.1f}s")
 
 
+def ic_cases():
+    """The reference's run initial conditions (run/bve/initial_conditions.py,
+    run/swe/initial_conditions.py) on a Gauss 32x64 / l_max 21 planet, flat and
+    over its mountain."""
+    from planetary_sandbox.run.bve.initial_conditions import INITIAL_CONDITIONS, make_ic
+    from planetary_sandbox.run.swe.initial_conditions import make_swe_ic
+    from planetary_sandbox.physics.topography import Topography
+    p = latlon_planet(32, 64, 21)
+    out = {}
+    for name in INITIAL_CONDITIONS:
+        if name != "random_low_l":
+            out[f"bve_{name}"] = np.asarray(make_ic(name, p))
+    topo = Topography.mountain(p, height_m=1500.0, lat_deg=-20.0, lon_deg=45.0, width_deg=25.0)
+    for tag, tp in (("flat", None), ("mountain", topo)):
+        m = ShallowWaterModel(p, gravity=G, mean_depth=8000.0, topography=tp)
+        for name in ("rest", "gravity_wave", "williamson2"):
+            out[f"swe_{tag}_{name}"] = np.asarray(make_swe_ic(name, m).coeffs)
+    np.savez_compressed(HERE / "ic_gauss32x64_L21.npz", nlat=32, nlon=64, lmax=21, radius=R, omega=OMEGA,
+                        gravity=G, mean_depth=8000.0, elevation_lm=np.asarray(topo.elevation_lm), **out)
+    print(f"ic_gauss32x64_L21: {len(out)} states")
+
+
 def pe_state(lmax, nlev, seed, l_band=None, t0=260.0, ps0=101325.0):
     """Isothermal rest state plus seeded band-limited perturbations of every
     prognostic (the recipe of the reference's tests/test_pe_tendency.py:80-108)."""
@@ -290,6 +312,7 @@ def main():
     geodesic_fine_case("geodesic_fine_res3_L10", 3, 10)
     pe_cases()
     topo_cases()
+    ic_cases()
     vector_cases()
 
 
@@ -483,6 +506,8 @@ if __name__ == "__main__":
         vector_cases()
     elif sys.argv[1:] == ["topo"]:
         topo_cases()
+    elif sys.argv[1:] == ["ic"]:
+        ic_cases()
     elif sys.argv[1:] == ["pe"]:
         pe_cases()
     elif sys.argv[1:] == ["geodesic_fine"]:

@@ -148,3 +148,29 @@ def test_bve_run_on_geodesic_fine_cogrid_matches_reference_runner(golden, tmp_pa
     for k in range(coeffs.shape[0]):
         assert rel_l2(tri(coeffs[k]), tri(g["coeffs"][k])) <= COEFF_TOL
     _compare_rows(tmp_path, g)
+
+
+def test_initial_conditions_match_reference(golden):
+    """run/bve/initial_conditions.py and run/swe/initial_conditions.py on a
+    Gauss 32x64 / l_max 21 planet, flat and over a mountain."""
+    from aeolus_gb300 import initial_conditions as IC
+    from aeolus_gb300.topography import Topography
+    g = golden("ic_gauss32x64_L21")
+    planet = ae.make_planet("latlon", nlat=32, nlon=64, l_max=21, device=DEV)
+    for name in IC.INITIAL_CONDITIONS:
+        z = IC.make_ic(name, planet)
+        assert tuple(z.shape) == (32, 64) or name == "random_low_l"
+        if name != "random_low_l":
+            ref = g[f"bve_{name}"]
+            assert np.abs(z.cpu().numpy() - ref).max() <= 1e-13 * np.abs(ref).max(), name
+    topo = Topography.mountain(planet, height_m=1500.0, lat_deg=-20.0, lon_deg=45.0, width_deg=25.0)
+    for tag, tp in (("flat", None), ("mountain", topo)):
+        m = ShallowWaterModel(planet, gravity=float(g["gravity"]), mean_depth=float(g["mean_depth"]), topography=tp)
+        for name in IC.SWE_INITIAL_CONDITIONS:
+            st = IC.make_swe_ic(name, m).coeffs.cpu().numpy()
+            ref = g[f"swe_{tag}_{name}"]
+            assert rel_l2(tri(st), tri(ref)) <= COEFF_TOL if np.any(ref) else not np.any(st), (tag, name)
+    with pytest.raises(ValueError, match="Unknown"):
+        IC.make_ic("hurricane", planet)
+    with pytest.raises(ValueError, match="Unknown"):
+        IC.make_swe_ic("tsunami", m)
