@@ -99,6 +99,31 @@ class SpectralOperators:
         out = vector_curl_div(plan.id, self.R, fe, fn, bool(truncate))
         return out[0], out[1]
 
+    def vector_curl_div_roundtrip(self, f_east, f_north, *, truncate: bool = True):
+        """Scalar round-trip curl/div of a tangent field on the product points
+        (:336-397; the reference's own comparison pathway, not its production
+        one): analyse each component, synthesize their derivatives, assemble
+        div = (fu_lam - fv_snt)/cos - tan/R fv, curl = (fu_snt + fv_lam)/cos +
+        tan/R fu from the round-tripped components, analyse (2/3 cut)."""
+        ps = self._product_space
+        sh_p, coslat = ps.sh, ps.coslat
+        dev = sh_p.weights.device
+        fe = torch.as_tensor(f_east, dtype=torch.float64, device=dev).reshape(-1)
+        fn = torch.as_tensor(f_north, dtype=torch.float64, device=dev).reshape(-1)
+        cl = coslat.reshape(-1)
+        sinlat = torch.sin(torch.as_tensor(sh_p.latitudes, dtype=torch.float64, device=dev)).reshape(-1)
+        fu_lm, fv_lm = sh_p.transform(fe), sh_p.transform(fn)
+        lam = lambda c: sh_p.inv_transform(self.d_lambda_coeffs(c))  # noqa: E731
+        snt = lambda c: sh_p.inv_transform(self.sin_theta_d_theta_coeffs(c)) / self.R  # noqa: E731
+        fu_rt, fv_rt = sh_p.inv_transform(fu_lm), sh_p.inv_transform(fv_lm)
+        tan_over_r = sinlat / (self.R * cl)
+        div_g = (lam(fu_lm) - snt(fv_lm)) / cl - tan_over_r * fv_rt
+        curl_g = (snt(fu_lm) + lam(fv_lm)) / cl + tan_over_r * fu_rt
+        curl_lm, div_lm = sh_p.transform(curl_g), sh_p.transform(div_g)
+        if truncate:
+            curl_lm, div_lm = self._truncate_product(curl_lm), self._truncate_product(div_lm)
+        return curl_lm, div_lm
+
     def _extended_plan(self):
         """The product points and weights with the basis extended to degree
         l_max + 1 (_vector_analysis_pieces, :474-492)."""

@@ -7,7 +7,7 @@ NumPy stand-in for CuPy in ``baseline/standin``; its CUDA-C basis kernel
 Omega = 7.292e-5 1/s, as the workloads specify (``Planet.generate`` would
 derive different constants and random terrain).
 
-Run:  PYTHONDONTWRITEBYTECODE=1 python tests/golden/make_golden.py [vector|runs|geodesic_fine|pe|topo|ic]
+Run:  PYTHONDONTWRITEBYTECODE=1 python tests/golden/make_golden.py [vector|runs|geodesic_fine|pe|topo|ic|misc]
 Writes ``tests/golden/*.npz`` (with ``vector``: only the weak-form curl/div
 fixtures; with ``runs``: only the integration-engine events and the run
 capsules of the reference's BVE/SWE runners).  Only l_max <= 85 fixtures are made: above
@@ -211,6 +211,19 @@ def topo_cases():
     print(f"topo_swe_gauss32x64_L21_mountain: {time.time() - t0:.1f}s")
 
 
+def misc_cases():
+    """The reference's scalar round-trip curl/div (numerics/spectral_operators.py:336-397)."""
+    p = latlon_planet(16, 32, 15)
+    ps = p.so.backend.product_space("fine")
+    rng = np.random.default_rng(12)
+    fe = rng.standard_normal(np.asarray(ps.sh.latitudes).size)
+    fn = rng.standard_normal(fe.size)
+    curl, div = p.so.vector_curl_div_roundtrip(fe, fn)
+    np.savez_compressed(HERE / "misc_gauss16x32_L15.npz", f_east=fe, f_north=fn, rt_curl=np.asarray(curl),
+                        rt_div=np.asarray(div))
+    print("misc_gauss16x32_L15")
+
+
 def ic_cases():
     """The reference's run initial conditions (run/bve/initial_conditions.py,
     run/swe/initial_conditions.py) on a Gauss 32x64 / l_max 21 planet, flat and
@@ -313,6 +326,7 @@ def main():
     pe_cases()
     topo_cases()
     ic_cases()
+    misc_cases()
     vector_cases()
 
 
@@ -508,6 +522,8 @@ if __name__ == "__main__":
         topo_cases()
     elif sys.argv[1:] == ["ic"]:
         ic_cases()
+    elif sys.argv[1:] == ["misc"]:
+        misc_cases()
     elif sys.argv[1:] == ["pe"]:
         pe_cases()
     elif sys.argv[1:] == ["geodesic_fine"]:

@@ -15,7 +15,7 @@ import torch
 import aeolus_gb300 as ae
 from aeolus_gb300 import _lib
 from aeolus_gb300.ops import Plan, spectral_op, synthesize, vector_curl_div
-from helpers import rel_l2
+from helpers import rel_l2, tri
 
 pytestmark = pytest.mark.gpu
 DEV = "cuda"
@@ -90,3 +90,13 @@ def test_vector_curl_div_rejects_bad_arguments():
         vector_curl_div(p.id, 1.0, x, x[:-1], True)
     with pytest.raises(Exception):
         vector_curl_div(p.id, -1.0, x, x, True)
+
+
+def test_roundtrip_curl_div_matches_reference(golden):
+    """The reference's scalar round-trip pathway (spectral_operators.py:336-397)
+    on the 23x46 product grid of a Gauss 16x32 / l_max 15 planet."""
+    g = golden("misc_gauss16x32_L15")
+    planet = ae.make_planet("latlon", nlat=16, nlon=32, l_max=15)
+    curl, div = planet.so.vector_curl_div_roundtrip(g["f_east"], g["f_north"])
+    assert rel_l2(tri(curl.cpu().numpy()), tri(g["rt_curl"])) < 1e-12
+    assert rel_l2(tri(div.cpu().numpy()), tri(g["rt_div"])) < 1e-12
