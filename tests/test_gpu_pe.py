@@ -183,3 +183,33 @@ def test_pe_validate_state_faults_injected_on_host(golden):
             m.validate_state(PrimitiveEquationsState(bad), context="in the test")
     with pytest.raises(PrimitiveEquationsStateError, match="does not match"):
         m.validate_state(PrimitiveEquationsState(good[:-3]))
+
+
+def test_pe_rk4_steps_match_oracle(golden):
+    """Two RK4 steps through the generic engine (run/engine.py:406-431) with
+    validate_state as the stage validator, against the oracle."""
+    from aeolus_gb300.engine import rk4_step_array
+    name = "pe_gauss16x32_L15_fine23x46_K5"
+    g = golden(name)
+    m = _model(g, *CASES[name])
+    stages = []
+
+    def validator(y):
+        stages.append(1)
+        m.validate_state(PrimitiveEquationsState(y), context="in an RK4 stage")
+
+    y = T(g["state"])
+    for _ in range(2):
+        y = rk4_step_array(m.tendency, y, 0.0, 300.0, stage_validator=validator)
+    assert len(stages) == 6
+    L, R = int(g["lmax"]), float(g["radius"])
+    nf, mf = oracle.fine_dims(16, 32, L)
+    ops = oracle.Operators(oracle.GaussSH(16, 32, L), R, sh_p=oracle.GaussSH(nf, mf, L))
+    ref_m = ope.PE(ops, ope.Sigma(g["interfaces"]), float(g["omega"]), oracle.GaussSH(nf, mf, L + 1),
+                   phi_s_lm=g["phi_s"], r_dry=float(g["r_dry"]), cp_dry=float(g["cp_dry"]))
+    from oracle import models as om
+    r = g["state"]
+    for _ in range(2):
+        r = om.rk4_step_array(ref_m.tendency, r, 300.0)
+    for a, b in zip(_blocks(N(y), m.nlev), _blocks(r, m.nlev)):
+        assert rel_l2(tri(a), tri(b)) < TOL
