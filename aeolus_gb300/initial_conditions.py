@@ -142,3 +142,30 @@ def make_swe_ic(name: str, model: ShallowWaterModel) -> ShallowWaterState:
     if name not in SWE_INITIAL_CONDITIONS:
         raise ValueError(f"Unknown swe initial condition: {name}. Available: {sorted(SWE_INITIAL_CONDITIONS)}")
     return SWE_INITIAL_CONDITIONS[name](model)
+
+
+# ---------------------------------------------------------------- PE
+THERMAL_WAVE_DEGREE, THERMAL_WAVE_ORDER = 2, 2
+
+
+def make_pe_ic(name: str, model, *, temperature: float, surface_pressure: float, thermal_amplitude: float = 0.0):
+    """Primitive-equation initial states (run/pe/initial_conditions.py), all
+    built spectrally on the isothermal rest state: ``isothermal_rest``;
+    ``thermal_wave`` (T at (l, m) = (2, 2) set to ``thermal_amplitude`` on every
+    level); ``orographic_isothermal_rest`` (ln p_s lowered by
+    phi_s / (R_d T0), the balanced rest over the model's terrain)."""
+    from .primitive_equations import isothermal_rest_state
+
+    if name not in ("isothermal_rest", "thermal_wave", "orographic_isothermal_rest"):
+        raise ValueError(f"Unknown pe initial condition: {name}. "
+                         f"Available: {sorted(['isothermal_rest', 'orographic_isothermal_rest', 'thermal_wave'])}")
+    dev = model.phi_surface_lm.device
+    st = isothermal_rest_state(model.l_max, model.nlev, temperature=temperature,
+                               surface_pressure=surface_pressure, device=dev)
+    if name == "thermal_wave":
+        if model.l_max < THERMAL_WAVE_DEGREE:
+            raise ValueError(f"thermal_wave needs l_max >= {THERMAL_WAVE_DEGREE}, got {model.l_max}")
+        st.coeffs[2 * model.nlev:3 * model.nlev, THERMAL_WAVE_DEGREE, THERMAL_WAVE_ORDER] = float(thermal_amplitude)
+    elif name == "orographic_isothermal_rest":
+        st.coeffs[3 * model.nlev] -= model.phi_surface_lm / (model.r_dry * float(temperature))
+    return st

@@ -505,3 +505,107 @@ def run_swe(model, state0, dt_snapshots: float | None, t_end_days: float, out_di
     np.save(out_dir / "swe_coeffs.npy", stack)
     np.save(out_dir / "swe_snapshot_times.npy", np.asarray(stored, dtype=np.float64))
     return 0
+
+
+# ------------------------------------------------------------------ PE run
+PE_CSV_COLUMNS = ["time_s", "dt_s", "step", "t_min", "t_max", "ps_min", "ps_max", "max_wind_ms", "max_abs_zeta",
+                  "max_abs_delta", "max_char_speed_ms", "courant", "total_mass", "mass_rel_drift"]
+
+
+class PEDiagnosticsRecorder:
+    """Primitive-equation rows (run/pe/diagnostics.py:62-140): temperature
+    extrema over both samplings, surface-pressure extrema, winds, zeta and
+    delta maxima on the state grid, the characteristic speed, a diagnostic
+    Courant number and the quadrature mass with its drift from the first
+    row."""
+
+    def __init__(self, model, out_dir):
+        self.model = model
+        self.R = model.R
+        self.length_scale = getattr(model.grid, "cfl_length_scale", None)
+        self._csv = _CsvRows(out_dir, PE_CSV_COLUMNS)
+        self.dir = self._csv.dir
+        self._mass0 = None
+
+    def record(self, t: float, state, dt: float, step: int) -> dict:
+        from .ops import synthesize
+
+        m = self.model
+        t_min, t_max = m.temperature_extrema(state)
+        ps = m.surface_pressure_on_state_grid(state)
+        u, v = m.wind_on_state_grid(state)
+        zd = synthesize(m.sh.plan.id, state.coeffs[:2 * m.nlev])
+        mass_t = torch.sum(m.sh.weights * self.R ** 2 * ps)
+        vals = torch.stack([ps.min(), ps.max(), torch.sqrt(u * u + v * v).max(), zd[:m.nlev].abs().max(),
+                            zd[m.nlev:].abs().max(), mass_t]).tolist()
+        max_char = m.max_characteristic_speed(state)
+        total_mass = vals[5]
+        if self._mass0 is None:
+            self._mass0 = total_mass
+        row = {"time_s": t, "dt_s": dt, "step": step, "t_min": t_min, "t_max": t_max, "ps_min": vals[0],
+               "ps_max": vals[1], "max_wind_ms": vals[2], "max_abs_zeta": vals[3], "max_abs_delta": vals[4],
+               "max_char_speed_ms": max_char,
+               "courant": (max_char * dt / self.length_scale) if (self.length_scale and dt > 0) else float("nan"),
+               "total_mass": total_mass,
+               "mass_rel_drift": (total_mass - self._mass0) / self._mass0 if self._mass0 else 0.0}
+        self._csv.write(row)
+        return row
+
+    def close(self):
+        self._csv.close()
+
+
+def run_pe(model, state0, *, dt_seconds: float, t_end_days: float, out_dir, snapshot_times: Sequence[float],
+           snapshot_mode: str = "count", dt_snapshots: float | None = None, figure_metadata: dict | None = None,
+           plots: Sequence[str] | None = None, scenario: str = "pe") -> int:
+    """Fixed-step primitive-equation run (run/pe/runner.py:48-165): the
+    scheduler driven with a constant ceiling (steps clipped only to land on
+    output times and t_end), every RK4 stage and accepted state validated,
+    a diagnostics row per step, ``pe_coeffs.npy`` and ``pe_snapshot_times.npy``."""
+    from .engine import rk4_step_array
+    from .primitive_equations import PrimitiveEquationsState
+
+    out_dir = pathlib.Path(out_dir)
+    t_end = t_end_days * SECONDS_PER_DAY
+    if not (math.isfinite(dt_seconds) and dt_seconds > 0):
+        raise ValueError(f"dt_seconds must be finite and > 0, got {dt_seconds}")
+    if snapshot_mode not in ("count", "interval"):
+        raise ValueError(f"unknown snapshot_mode: {snapshot_mode!r}")
+    _no_figures(plots)
+    model.validate_state(state0, context="initial state")
+    dev = model.phi_surface_lm.device
+    state = PrimitiveEquationsState(torch.as_tensor(state0.coeffs, dtype=torch.complex128, device=dev).clone())
+    recorder = PEDiagnosticsRecorder(model, out_dir)
+    last = recorder.record(0.0, state, dt=0.0, step=0)
+    snaps, stored = [], []
+    step = 0
+
+    def validate_stage(y):
+        model.validate_state(PrimitiveEquationsState(y), context=f"in an RK4 stage after step {step}")
+
+    sch = IntegrationScheduler(t_end, mode=snapshot_mode, snapshot_times=snapshot_times, dt_snapshots=dt_snapshots)
+    try:
+        t = 0.0
+        while (ev := sch.next_event(dt_seconds)) is not None:
+            kind, dt, t_ev = ev
+            if kind == "store":
+                snaps.append(state.coeffs.cpu().numpy())
+                stored.append(t_ev)
+                print(f"Time: {t_ev / 3600.0:8.3f} hrs | Step: {step} ")
+                continue
+            step += 1
+            state = PrimitiveEquationsState(rk4_step_array(model.tendency, state.coeffs, t, dt,
+                                                           stage_validator=validate_stage))
+            model.validate_state(state, context=f"at t={t_ev:g} s (step {step})")
+            last = recorder.record(t_ev, state, dt=dt, step=step)
+            t = t_ev
+    finally:
+        recorder.close()
+    stack = np.stack(snaps) if snaps else np.empty((0, *state.coeffs.shape), dtype=np.complex128)
+    np.save(out_dir / "pe_coeffs.npy", stack)
+    np.save(out_dir / "pe_snapshot_times.npy", np.asarray(stored, dtype=np.float64))
+    print(f"Stored {len(stored)} snapshot(s) over {step} fixed {dt_seconds:g} s step(s).")
+    print(f"Final diagnostics @ t={last['time_s'] / 3600.0:.3f} h: T[min,max]=[{last['t_min']:.2f}, "
+          f"{last['t_max']:.2f}] K, p_s[min,max]=[{last['ps_min']:.1f}, {last['ps_max']:.1f}] Pa, "
+          f"max|V|={last['max_wind_ms']:.3g} m/s, mass drift={last['mass_rel_drift']:.2e}")
+    return 0

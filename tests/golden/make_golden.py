@@ -7,7 +7,7 @@ NumPy stand-in for CuPy in ``baseline/standin``; its CUDA-C basis kernel
 Omega = 7.292e-5 1/s, as the workloads specify (``Planet.generate`` would
 derive different constants and random terrain).
 
-Run:  PYTHONDONTWRITEBYTECODE=1 python tests/golden/make_golden.py [vector|runs|geodesic_fine|pe|topo|ic|misc]
+Run:  PYTHONDONTWRITEBYTECODE=1 python tests/golden/make_golden.py [vector|runs|geodesic_fine|pe|topo|ic|misc|pe_run]
 Writes ``tests/golden/*.npz`` (with ``vector``: only the weak-form curl/div
 fixtures; with ``runs``: only the integration-engine events and the run
 capsules of the reference's BVE/SWE runners).  Only l_max <= 85 fixtures are made: above
@@ -224,6 +224,36 @@ def misc_cases():
     print("misc_gauss16x32_L15")
 
 
+def pe_run_cases():
+    """The reference's fixed-step PE runner (run/pe/runner.py) on a thermal
+    wave, and its balanced orographic rest state (run/pe/initial_conditions.py)."""
+    import tempfile
+    from planetary_sandbox.physics.primitive_equations import PrimitiveEquationsModel
+    from planetary_sandbox.physics.sigma_coordinate import SigmaGrid
+    from planetary_sandbox.physics.topography import Topography
+    from planetary_sandbox.run.pe.initial_conditions import make_pe_ic
+    from planetary_sandbox.run.pe.runner import run_pe
+    from planetary_sandbox.run import engine as E
+    p = latlon_planet(16, 32, 10)
+    model = PrimitiveEquationsModel(p, SigmaGrid.uniform(3))
+    st = make_pe_ic("thermal_wave", model, temperature=260.0, surface_pressure=1.0e5, thermal_amplitude=1.0)
+    topo = Topography.mountain(p, height_m=1000.0, lat_deg=20.0, lon_deg=60.0, width_deg=30.0, l_cut=6)
+    mo = PrimitiveEquationsModel(p, SigmaGrid.uniform(3), surface_geopotential_lm=topo.surface_geopotential_lm(G))
+    oro = make_pe_ic("orographic_isothermal_rest", mo, temperature=260.0, surface_pressure=1.0e5)
+    with tempfile.TemporaryDirectory() as d:
+        o = Path(d)
+        times = E.count_snapshot_times(3, 0.05 * 86400.0)
+        run_pe(model, st, dt_seconds=700.0, t_end_days=0.05, out_dir=o, snapshot_times=times, plots=())
+        cols, rows = _csv_table(o / "diagnostics" / "timeseries.csv")
+        np.savez_compressed(
+            HERE / "run_pe_gauss16x32_L10_K3_thermal_wave.npz", lmax=10, nlev=3, radius=R, omega=OMEGA,
+            state0=np.asarray(st.coeffs), dt=700.0, t_end_days=0.05, snapshot_times=np.asarray(times, np.float64),
+            coeffs=np.load(o / "pe_coeffs.npy"), times=np.load(o / "pe_snapshot_times.npy"), csv_cols=cols,
+            csv_rows=rows, phi_s=np.asarray(topo.surface_geopotential_lm(G)), oro_state=np.asarray(oro.coeffs),
+            oro_tendency=np.asarray(mo.tendency(oro.coeffs.copy())))
+    print("run_pe_gauss16x32_L10_K3_thermal_wave")
+
+
 def ic_cases():
     """The reference's run initial conditions (run/bve/initial_conditions.py,
     run/swe/initial_conditions.py) on a Gauss 32x64 / l_max 21 planet, flat and
@@ -327,6 +357,7 @@ def main():
     topo_cases()
     ic_cases()
     misc_cases()
+    pe_run_cases()
     vector_cases()
 
 
@@ -522,6 +553,8 @@ if __name__ == "__main__":
         topo_cases()
     elif sys.argv[1:] == ["ic"]:
         ic_cases()
+    elif sys.argv[1:] == ["pe_run"]:
+        pe_run_cases()
     elif sys.argv[1:] == ["misc"]:
         misc_cases()
     elif sys.argv[1:] == ["pe"]:

@@ -174,3 +174,44 @@ def test_initial_conditions_match_reference(golden):
         IC.make_ic("hurricane", planet)
     with pytest.raises(ValueError, match="Unknown"):
         IC.make_swe_ic("tsunami", m)
+
+
+def test_pe_run_matches_reference_runner(golden, tmp_path):
+    """The reference's fixed-step PE runner (run/pe/runner.py) on a thermal
+    wave: stored states, times and every diagnostics row (the mass drift,
+    a ~1e-13 round-off quantity, absolutely to 1e-12); and the balanced
+    orographic rest state with its tendency."""
+    from aeolus_gb300.initial_conditions import make_pe_ic
+    from aeolus_gb300.primitive_equations import PrimitiveEquationsModel, SigmaGrid
+    g = golden("run_pe_gauss16x32_L10_K3_thermal_wave")
+    planet = ae.make_planet("latlon", nlat=16, nlon=32, l_max=int(g["lmax"]), device=DEV)
+    model = PrimitiveEquationsModel(planet, SigmaGrid.uniform(int(g["nlev"])))
+    st = make_pe_ic("thermal_wave", model, temperature=260.0, surface_pressure=1.0e5, thermal_amplitude=1.0)
+    assert np.array_equal(st.coeffs.cpu().numpy(), g["state0"])
+    RN.run_pe(model, st, dt_seconds=float(g["dt"]), t_end_days=float(g["t_end_days"]), out_dir=tmp_path,
+              snapshot_times=list(g["snapshot_times"]), plots=())
+    times = np.load(tmp_path / "pe_snapshot_times.npy")
+    assert [t.hex() for t in times] == [t.hex() for t in g["times"]]
+    coeffs = np.load(tmp_path / "pe_coeffs.npy")
+    assert coeffs.shape == g["coeffs"].shape
+    for k in range(coeffs.shape[0]):
+        assert rel_l2(tri(coeffs[k]), tri(g["coeffs"][k])) <= COEFF_TOL
+    cols, rows = _read_csv(tmp_path / "diagnostics" / "timeseries.csv")
+    assert cols == [str(c) for c in g["csv_cols"]]
+    ref = g["csv_rows"]
+    assert rows.shape == ref.shape
+    for j, c in enumerate(cols):
+        a, b = rows[:, j], ref[:, j]
+        assert np.array_equal(np.isnan(a), np.isnan(b)), c
+        ok = ~np.isnan(b)
+        tol = 1e-12 if c == "mass_rel_drift" else ROW_TOL * max(np.abs(b[ok]).max() if ok.any() else 0.0, 1e-300)
+        assert np.all(np.abs(a[ok] - b[ok]) <= tol), (c, a, b)
+    mo = PrimitiveEquationsModel(planet, SigmaGrid.uniform(int(g["nlev"])), surface_geopotential_lm=T(g["phi_s"]))
+    oro = make_pe_ic("orographic_isothermal_rest", mo, temperature=260.0, surface_pressure=1.0e5)
+    assert rel_l2(tri(oro.coeffs.cpu().numpy()), tri(g["oro_state"])) <= COEFF_TOL
+    t = mo.tendency(oro.coeffs).cpu().numpy()
+    assert np.abs(t).max() <= 1e-18 + 10 * np.abs(g["oro_tendency"]).max()
+
+
+def T(x):
+    return torch.as_tensor(np.asarray(x), device=DEV)
