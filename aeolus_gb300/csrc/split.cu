@@ -226,9 +226,46 @@ int split_build(aeolus_plan_impl* p) {
   return AEOLUS_OK;
 }
 
+// One thread waits on an mbarrier phase that nothing completes: the bounded
+// wait must give up after `limit_ns` and report it.  The phase is then
+// completed by the waiter itself, so the kernel leaves nothing pending.
+__global__ void mbar_timeout_selftest_kernel(unsigned long long limit_ns, int* timed_out,
+                                             unsigned long long* elapsed_ns) {
+  __shared__ __align__(8) uint64_t bar;
+  if (threadIdx.x == 0) {
+    tc::mbar_init(&bar, 1);
+    tc::fence_mbar_init();
+    const uint64_t t0 = tc::globaltimer_ns();
+    const bool ok = tc::mbar_wait(&bar, 0, limit_ns);
+    *elapsed_ns = tc::globaltimer_ns() - t0;
+    *timed_out = ok ? 0 : 1;
+    tc::mbar_arrive(&bar);
+  }
+}
+
 }  // namespace aeolus
 
 using namespace aeolus;
+
+extern "C" int aeolus_selftest_wait_timeout(unsigned long long limit_ns, int* timed_out,
+                                            unsigned long long* elapsed_ns) {
+  if (!timed_out || !elapsed_ns || limit_ns == 0 || limit_ns > 10000000000ull)
+    return fail(AEOLUS_ERR_ARG, "aeolus_selftest_wait_timeout: bad arguments (limit in (0, 10 s])");
+  int* d_flag = nullptr;
+  unsigned long long* d_ns = nullptr;
+  AE_CUDA(cudaMalloc(&d_flag, sizeof(int)));
+  cudaError_t e = cudaMalloc(&d_ns, sizeof(unsigned long long));
+  if (e == cudaSuccess) {
+    mbar_timeout_selftest_kernel<<<1, 32>>>(limit_ns, d_flag, d_ns);
+    e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaMemcpy(timed_out, d_flag, sizeof(int), cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess) e = cudaMemcpy(elapsed_ns, d_ns, sizeof(unsigned long long), cudaMemcpyDeviceToHost);
+  }
+  cudaFree(d_flag);
+  if (d_ns) cudaFree(d_ns);
+  if (e != cudaSuccess) return fail(AEOLUS_ERR_CUDA, std::string("aeolus_selftest_wait_timeout: ") + cudaGetErrorString(e));
+  return AEOLUS_OK;
+}
 
 extern "C" int aeolus_plan_device_error(aeolus_plan plan, int* flag) {
   if (!plan || !flag) return fail(AEOLUS_ERR_ARG, "aeolus_plan_device_error: bad arguments");

@@ -53,12 +53,29 @@ __device__ inline bool mbar_try_wait(uint64_t* bar, uint32_t phase) {
   return ok != 0;
 }
 
-// Bounded wait: returns false after `limit` polls (the caller records an
-// error and bails out instead of spinning forever).
-__device__ inline bool mbar_wait(uint64_t* bar, uint32_t phase, uint32_t limit = 1u << 26) {
-  for (uint32_t i = 0; i < limit; ++i)
-    if (mbar_try_wait(bar, phase)) return true;
-  return false;
+__device__ inline uint64_t globaltimer_ns() {
+  uint64_t t;
+  asm volatile("mov.u64 %0, %globaltimer;" : "=l"(t));
+  return t;
+}
+
+// Waits longer than this are treated as lost arrivals (a pipeline handoff
+// completes in microseconds).
+constexpr uint64_t kWaitLimitNs = 1000000000ull;  // 1 s
+
+// Bounded wait: returns false once `limit_ns` of wall time has passed
+// without the phase completing (the caller records an error and bails out
+// instead of spinning forever).  The limit is on elapsed time, not on the
+// number of polls, because one try_wait may itself suspend the thread for
+// a time the hardware chooses.
+__device__ inline bool mbar_wait(uint64_t* bar, uint32_t phase, uint64_t limit_ns = kWaitLimitNs) {
+  if (mbar_try_wait(bar, phase)) return true;
+  const uint64_t t0 = globaltimer_ns();
+  for (;;) {
+    for (int i = 0; i < 32; ++i)
+      if (mbar_try_wait(bar, phase)) return true;
+    if (globaltimer_ns() - t0 > limit_ns) return false;
+  }
 }
 
 // 1-D bulk copy global -> shared through the TMA engine, completing on `bar`

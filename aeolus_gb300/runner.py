@@ -593,9 +593,11 @@ def run_pe(model, state0, *, dt_seconds: float, t_end_days: float, out_dir, snap
                 stored.append(t_ev)
                 print(f"Time: {t_ev / 3600.0:8.3f} hrs | Step: {step} ")
                 continue
+            # `step` still names the last accepted step while the stages run
+            # (a stage fault reads "after step k-1", run/pe/runner.py:96-106)
+            y = rk4_step_array(model.tendency, state.coeffs, t, dt, stage_validator=validate_stage)
             step += 1
-            state = PrimitiveEquationsState(rk4_step_array(model.tendency, state.coeffs, t, dt,
-                                                           stage_validator=validate_stage))
+            state = PrimitiveEquationsState(y)
             model.validate_state(state, context=f"at t={t_ev:g} s (step {step})")
             last = recorder.record(t_ev, state, dt=dt, step=step)
             t = t_ev

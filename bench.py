@@ -11,10 +11,13 @@ step of the whole member batch (4 fused tendency chains).  Synthetic inputs
   python bench.py [--gpus N] [--steps K] [--warmup W] [--members B]
                   [--precision fp64|split] [--impl ours|reference]
 
-Prints one JSON line (rank 0).  `value` is the split-precision path (bf16-
-digit tcgen05 contractions, double-float longitude stage); `split_vs_fp64`
-times the plain FP64 path on the same states and reports the per-field
-relative L2 between the two after the timed steps.  `value` is device-timed
+Rank 0 prints two JSON lines: first the side measurements (configs c3-c5,
+the primitive equations, the directly timed c1/c2 steps beside the
+reference's own, per-kernel times), then the headline line, last.  `value`
+is the split-precision path (bf16-digit tcgen05 contractions, fixed-point
+longitude stage); `split_vs_fp64` times the plain FP64 path on the same
+states and reports the per-field relative L2 between the two after the
+timed steps.  `value` is device-timed
 with the state resident in HBM (CUDA events around each step, L2 flushed
 between steps);
 `e2e` goes through the public API with the state copied host->device from
@@ -308,6 +311,104 @@ def pe_measure(dev, members: int = 4, nlev: int = 20, reps: int = 5):
     return out
 
 
+# ------------------------------------------------------------ c1 / c2 full steps
+DIRECT_CONFIGS = {"c1": dict(model="bve", nlat=32, nlon=64, lmax=21, dt=600.0),
+                  "c2": dict(model="swe", nlat=128, nlon=256, lmax=85, dt=300.0)}
+
+
+def direct_gpu_steps(dev, reps: int = 50):
+    """One RK4 step of configs c1 (BVE, Gauss 32x64, l_max 21, dt 600 s) and
+    c2 (SWE, Gauss 128x256, l_max 85, dt 300 s) for one member, on the same
+    seeded inputs as the reference's directly timed steps: steps/s (CUDA
+    events over `reps` steps from the same state) and the state after one
+    step, FP64 (c1, c2) and split precision (c2)."""
+    import torch
+    import aeolus_gb300 as ae
+    from aeolus_gb300 import _lib, workloads as W
+    from aeolus_gb300.barotropic import BarotropicVorticity
+    from aeolus_gb300.shallow_water import ShallowWaterModel
+
+    out = {}
+    for name, c in DIRECT_CONFIGS.items():
+        for prec in (("fp64",) if c["model"] == "bve" else ("fp64", "split")):
+            planet = ae.make_planet("latlon", nlat=c["nlat"], nlon=c["nlon"], l_max=c["lmax"], device=dev)
+            if prec == "split":
+                planet.so._product_space.sh.plan.set_precision(_lib.PREC_SPLIT_BF16)
+            if c["model"] == "bve":
+                model = BarotropicVorticity(planet, viscosity=0.0)
+                y0 = torch.as_tensor(W.bve_vorticity(c["lmax"], 0), device=dev)[None]
+                step = lambda y: model.rk4(y, c["dt"], 1)  # noqa: E731
+            else:
+                s0, depth = W.perturbed_williamson2(c["lmax"], seed=0)
+                model = ShallowWaterModel(planet, gravity=W.GRAVITY, mean_depth=depth)
+                y0 = torch.as_tensor(s0, device=dev)[None]
+                step = lambda y: model.rk4(y, c["dt"], 1, check=False)  # noqa: E731
+            for _ in range(3):
+                y1 = step(y0)
+            torch.cuda.synchronize(dev)
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            for _ in range(reps):
+                y1 = step(y0)
+            e1.record()
+            torch.cuda.synchronize(dev)
+            ms = e0.elapsed_time(e1) / reps
+            out[f"{name}_{prec}"] = {"steps_per_s": 1000.0 / ms, "ms_per_step": ms,
+                                     "state1": y1[0].cpu().numpy()}
+    return out
+
+
+def direct_reference_steps(reps_c1: int = 5, reps_c2: int = 1):
+    """The reference's own RK4 steps at c1 and c2, timed directly (no
+    scaling) on the host cores by baseline/reference_timing.py in a child
+    process; None where the reference package is absent."""
+    import tempfile
+    if not (ROOT / "baseline" / "_ref" / "planetary_sandbox").is_dir():
+        return None
+    script = ROOT / "baseline" / "reference_timing.py"
+    env = dict(os.environ, PYTHONDONTWRITEBYTECODE="1")
+    out = {}
+    with tempfile.TemporaryDirectory() as tmp:
+        for name, reps in (("c1", reps_c1), ("c2", reps_c2)):
+            npz = Path(tmp) / f"{name}.npz"
+            r = subprocess.run([sys.executable, str(script), name, str(reps), str(npz)], capture_output=True,
+                               text=True, env=env, timeout=900)
+            if r.returncode != 0:
+                print(f"reference {name} step unavailable: {r.stderr.strip().splitlines()[-1:]}", file=sys.stderr)
+                continue
+            d = json.loads(r.stdout.strip().splitlines()[-1])
+            z = np.load(npz)
+            d["state1"] = z["state1"]
+            out[name] = d
+    return out
+
+
+def direct_steps_report(gpu, ref, cores: int):
+    """c1 / c2: GPU steps/s beside the reference's directly timed CPU step on
+    the same inputs, and the relative L2 between the two final states."""
+    rep = {}
+    for name, c in DIRECT_CONFIGS.items():
+        r = (ref or {}).get(name)
+        e = {"workload": f"{c['model']}_rk4_gauss{c['nlat']}x{c['nlon']}_lmax{c['lmax']}_dt{c['dt']:g}_1member"}
+        if r is not None:
+            e["reference_cpu"] = {"steps_per_s": 1.0 / r["seconds_per_step"], "seconds_per_step": r["seconds_per_step"],
+                                  "reps": r["reps"], "cores": cores, "extrapolated": False,
+                                  "code": "planetary_sandbox rk4_step (run/bve/runner.py:211-216)" if c["model"] == "bve"
+                                  else "planetary_sandbox rk4_step_array over ShallowWaterModel.tendency "
+                                       "(run/engine.py:406-431)"}
+        for prec in ("fp64", "split"):
+            g = gpu.get(f"{name}_{prec}")
+            if g is None:
+                continue
+            e[f"gpu_{prec}"] = {"steps_per_s": g["steps_per_s"], "ms_per_step": g["ms_per_step"]}
+            if r is not None:
+                a, b = g["state1"], r["state1"]
+                e[f"gpu_{prec}"]["rel_l2_vs_reference_step"] = float(np.linalg.norm(a - b) / np.linalg.norm(b))
+                e[f"gpu_{prec}"]["speedup_vs_reference_cpu"] = g["steps_per_s"] * r["seconds_per_step"]
+        rep[name] = e
+    return rep
+
+
 # ------------------------------------------------------------ CPU baseline
 def cpu_reference_sample(B: int, rows: int, reps: int = 1):
     """Time the reference algorithm for one RK4 step on a row sample.
@@ -342,7 +443,9 @@ def cpu_reference_sample(B: int, rows: int, reps: int = 1):
     desc = (f"reference dense-basis SWE tendency (12 syntheses x 2 GEMV + 4 analyses) on {rows} of {NLAT} "
             f"Gauss rows ({rows * NLON} points x {oracle.n_coeff(LMAX)} modes), timed {reps}x, scaled x{NLAT / rows:g} "
             f"rows x4 stages x{B} members")
-    return 1.0 / (step_member * B), desc, t * reps
+    extra = {"extrapolated": True, "measured_s_per_sample_tendency": t, "rows": rows,
+             "scale": (NLAT / rows) * 4.0 * B}
+    return 1.0 / (step_member * B), desc, t * reps, extra
 
 
 def reference_own_sample(B: int, rows: int, reps: int = 1):
@@ -368,12 +471,16 @@ def reference_own_sample(B: int, rows: int, reps: int = 1):
     desc = (f"the reference's own ShallowWaterModel.tendency (planetary_sandbox, NumPy in place of CuPy, its "
             f"CUDA-C basis kernel built for the CPU) on {rows} of {NLAT} Gauss rows ({d['points']} points x "
             f"{d['modes']} modes), timed {reps}x, scaled x{NLAT / rows:g} rows x4 stages x{B} members")
-    return 1.0 / (step_member * B), desc, time.perf_counter() - t0
+    extra = {"extrapolated": True, "measured_s_per_sample_tendency": t, "rows": rows,
+             "scale": (NLAT / rows) * 4.0 * B}
+    return 1.0 / (step_member * B), desc, time.perf_counter() - t0, extra
 
 
 def cpu_baseline_sample(B: int, rows: int, reps: int = 1):
-    """(steps/s, description, seconds, kind): the reference's own code when
-    it runs here ("reference"), else the oracle restatement ("port")."""
+    """(steps/s, description, seconds, extrapolation fields, kind): the
+    reference's own code when it runs here ("reference"), else the oracle
+    restatement ("port").  The step rate is extrapolated from a row sample:
+    a full 64-member step of the reference takes hours on the host cores."""
     own = reference_own_sample(B, rows, reps)
     if own is not None:
         return own + ("reference",)
@@ -391,15 +498,16 @@ def run_reference(args):
         cpu_baseline_sample(B, max(2, args.cpu_rows // 4), 1)
     vals = []
     desc = ""
+    extra = {}
     for _ in range(max(args.steps, 1)):
-        v, desc, _, kind = cpu_baseline_sample(B, args.cpu_rows, 1)
+        v, desc, _, extra, kind = cpu_baseline_sample(B, args.cpu_rows, 1)
         vals.append(v)
     v = statistics.median(vals)
     line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 / v, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
             "config": workload_config(args, B),
-            "cpu_baseline": {"value": v, "unit": UNIT, "cores": cores, "kind": kind, "sample": desc},
+            "cpu_baseline": dict({"value": v, "unit": UNIT, "cores": cores, "kind": kind, "sample": desc}, **extra),
             "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
     return 0
@@ -743,19 +851,32 @@ def main():
     launches = sum(n for n, _ in kstats.values())
 
     extras = {}
+    direct_gpu = None
     if rank == 0 and not args.no_extras:
         extras["ensemble"] = ensemble_measure(dev)
         extras["adjoint"] = adjoint_measure(dev)
         extras["geodesic"] = geodesic_measure(dev)
         extras["pe"] = pe_measure(dev)
+        direct_gpu = direct_gpu_steps(dev)
 
+    cores = int(os.environ.get("OPENBLAS_NUM_THREADS", "1"))
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
-        v, desc, _, kind = cpu_baseline_sample(B, args.cpu_rows, 1)
-        cpu = {"value": v, "unit": UNIT, "cores": int(os.environ.get("OPENBLAS_NUM_THREADS", "1")),
-               "kind": kind, "sample": desc}
+        v, desc, _, extra, kind = cpu_baseline_sample(B, args.cpu_rows, 1)
+        cpu = dict({"value": v, "unit": UNIT, "cores": cores, "kind": kind, "sample": desc}, **extra)
+    direct = None
+    if direct_gpu is not None:
+        ref = None if args.no_cpu_baseline else direct_reference_steps()
+        direct = direct_steps_report(direct_gpu, ref, cores)
 
     if rank == 0:
+        # side measurements and per-kernel detail first, on a line of their
+        # own; the headline line (with the split-vs-FP64 ratio) comes last
+        side = {"side_measurements": dict(extras, direct_steps=direct, autotune=tuning,
+                                          kernels={k: {"launches": n, "ms": ms} for k, (n, ms) in kstats.items()},
+                                          roofline_all=roof_all,
+                                          fp64_kernels=comparison.pop("fp64_kernels") if comparison else None)}
+        print(json.dumps(side), flush=True)
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
                 "warmup": warm, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None,
@@ -763,15 +884,17 @@ def main():
                 "config": dict(workload_config(args, B), l2="flushed between steps (256 MiB write)"
                                if flush is not None else "not flushed"),
                 "member_steps_per_s": value * B,
-                "autotune": tuning,
-                "split_vs_fp64": comparison,
                 "e2e": {"value": world * args.steps / (e2e_ms / 1000.0), "unit": UNIT,
                         "h2d_bytes_per_step": bytes_state, "d2h_bytes_per_step": bytes_state + 4 * B,
                         "wall_ms": e2e_wall_ms},
                 "gpu_launches": launches,
-                "kernels": {k: {"launches": n, "ms": ms} for k, (n, ms) in kstats.items()},
-                "roofline": roof, "roofline_all": roof_all, "cpu_baseline": cpu, "clocks": clock_summary}
-        line.update(extras)
+                "roofline": roof, "cpu_baseline": cpu, "clocks": clock_summary}
+        if direct is not None:
+            line["direct_steps_vs_reference"] = {
+                k: {kk: {m: round(x, 6) if isinstance(x, float) else x for m, x in vv.items()
+                         if m in ("steps_per_s", "rel_l2_vs_reference_step")}
+                    for kk, vv in v.items() if isinstance(vv, dict)} for k, v in direct.items()}
+        line["split_vs_fp64"] = comparison
         print(json.dumps(line), flush=True)
     if world > 1:
         dist.destroy_process_group()

@@ -148,6 +148,13 @@ int aeolus_plan_set_precision(aeolus_plan plan, int precision, int slices);
  * counterpart (the reference has no device-side waits). */
 int aeolus_plan_device_error(aeolus_plan plan, int* flag);
 
+/* Self-test of the bounded device-side waits (no reference counterpart): one
+ * thread waits on an mbarrier phase that nothing completes, with a wall-time
+ * limit of limit_ns (at most 10 s).  *timed_out = 1 when the wait gave up,
+ * *elapsed_ns = the wait's duration on the device clock.  Synchronous. */
+int aeolus_selftest_wait_timeout(unsigned long long limit_ns, int* timed_out,
+                                 unsigned long long* elapsed_ns);
+
 /* Launch shapes of the plan's kernels (no reference counterpart), an array
  * of AEOLUS_TUNING_KNOBS ints: knobs[0] members per CTA of the FP64 Legendre
  * synthesis, knobs[1] of the analysis, knobs[2] threads per CTA of the
@@ -177,8 +184,10 @@ int aeolus_synthesize(aeolus_plan plan, const double* coeffs, double* grid,
  * loads it until process exit; batches needing more scratch are rejected
  * with AEOLUS_ERR_WORKSPACE.  The first call on a device looks up the
  * array's device address (cudaGetSymbolAddress) and must come before any
- * stream capture.  All calls share the array: calls that overlap on the GPU
- * (different streams, or threads without ordering) race on it. */
+ * stream capture; that address is kept for the life of the process, so a
+ * device reset (cudaDeviceReset) between calls is not supported.  All calls
+ * share the array: calls that overlap on the GPU (different streams, or
+ * threads without ordering) race on it. */
 int aeolus_synthesize_noalloc(aeolus_plan plan, const double* coeffs,
                               double* grid, int batch, void* stream);
 

@@ -1,8 +1,8 @@
 """Build recipe: compile the reference's basis kernel for the CPU (TEST INFRASTRUCTURE).
 
-Compiles src/planetary_sandbox/numerics/cuda/sh_matrix.cu from the reference
-checkout, where it lies (or from the reference package installed into the
-git-ignored baseline/_ref/ where the checkout is absent), as plain C++ with g++: a prelude header turns
+Compiles planetary_sandbox/numerics/cuda/sh_matrix.cu where it lies in the
+reference package installed into the git-ignored baseline/_ref/ (or in the
+reference checkout named by AEOLUS_REFERENCE_ROOT), as plain C++ with g++: a prelude header turns
 ``__global__`` into nothing and supplies ``blockIdx``/``blockDim``/
 ``threadIdx``; a stub ``cupy/complex.cuh`` maps ``complex<double>`` to
 ``std::complex<double>``; a generated launcher walks the launch grid.  The
@@ -10,7 +10,7 @@ output goes only to ``oracle/_ref/`` (git-ignored).  Nothing is copied from
 the reference into the repository.
 
 Used by ``tests/golden/make_golden.py`` (through the NumPy stand-in for CuPy)
-and by the CPU-only pin tests when the reference checkout is present.
+and by the CPU-only pin tests when the reference source is present.
 """
 from __future__ import annotations
 
@@ -20,13 +20,12 @@ from pathlib import Path
 
 HERE = Path(__file__).resolve().parent
 OUT = HERE / "_ref"
-REF_ROOT = Path(os.environ.get("AEOLUS_REFERENCE_ROOT", "/root/reference"))
-# the checkout's source, else the copy installed with the reference package
-# into baseline/_ref (where the checkout is absent)
+# the reference package installed into the git-ignored baseline/_ref, or a
+# reference checkout named by AEOLUS_REFERENCE_ROOT (its src/ tree)
 _SRC = "planetary_sandbox/numerics/cuda/sh_matrix.cu"
-SH_MATRIX = REF_ROOT / "src" / _SRC
-if not SH_MATRIX.is_file():
-    SH_MATRIX = HERE.parent / "baseline" / "_ref" / _SRC
+SH_MATRIX = HERE.parent / "baseline" / "_ref" / _SRC
+if os.environ.get("AEOLUS_REFERENCE_ROOT"):
+    SH_MATRIX = Path(os.environ["AEOLUS_REFERENCE_ROOT"]) / "src" / _SRC
 LIB = OUT / "libref_sh_matrix.so"
 
 _PRELUDE = r"""

@@ -1,6 +1,7 @@
 """Generate golden vectors by running the reference's own code on this CPU.
 
-The reference (planetary_sandbox) is imported from its checkout with the
+The reference (planetary_sandbox) is imported from its unmodified install in
+the git-ignored baseline/_ref (or the checkout named by AEOLUS_REFERENCE_ROOT) with the
 NumPy stand-in for CuPy in ``baseline/standin``; its CUDA-C basis kernel
 (src/planetary_sandbox/numerics/cuda/sh_matrix.cu) runs as C++ built by
 ``oracle/ref_build.py``.  Operators are built directly with a = 6.371e6 m and
@@ -26,7 +27,10 @@ import numpy as np
 
 HERE = Path(__file__).resolve().parent
 REPO = HERE.parents[1]
-REF_SRC = Path(os.environ.get("AEOLUS_REFERENCE_ROOT", "/root/reference")) / "src"
+# the reference package installed into the git-ignored baseline/_ref, or a
+# reference checkout named by AEOLUS_REFERENCE_ROOT (its src/ tree)
+REF_SRC = (Path(os.environ["AEOLUS_REFERENCE_ROOT"]) / "src" if os.environ.get("AEOLUS_REFERENCE_ROOT")
+           else REPO / "baseline" / "_ref")
 sys.dont_write_bytecode = True
 sys.path[:0] = [str(REPO / "baseline" / "standin"), str(REF_SRC), str(REPO)]
 

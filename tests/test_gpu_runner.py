@@ -213,5 +213,30 @@ def test_pe_run_matches_reference_runner(golden, tmp_path):
     assert np.abs(t).max() <= 1e-18 + 10 * np.abs(g["oro_tendency"]).max()
 
 
+def test_pe_run_stage_fault_names_last_accepted_step(tmp_path):
+    """A stage that fails validation during the second step is reported
+    "in an RK4 stage after step 1", the last accepted step, as the reference
+    runner does (run/pe/runner.py:93-106).  The fault is made on the host: the
+    tendency turns non-finite from its fifth call on."""
+    from aeolus_gb300.initial_conditions import make_pe_ic
+    from aeolus_gb300.primitive_equations import (PrimitiveEquationsModel, PrimitiveEquationsStateError,
+                                                  SigmaGrid)
+    planet = ae.make_planet("latlon", nlat=16, nlon=32, l_max=10, device=DEV)
+    model = PrimitiveEquationsModel(planet, SigmaGrid.uniform(3))
+    st = make_pe_ic("thermal_wave", model, temperature=260.0, surface_pressure=1.0e5, thermal_amplitude=1.0)
+    calls = [0]
+    real = model.tendency
+
+    def faulty(y):
+        calls[0] += 1
+        t = real(y)
+        return t * float("nan") if calls[0] > 4 else t
+
+    model.tendency = faulty
+    with pytest.raises(PrimitiveEquationsStateError, match="in an RK4 stage after step 1"):
+        RN.run_pe(model, st, dt_seconds=700.0, t_end_days=0.05, out_dir=tmp_path,
+                  snapshot_times=[0.0, 2160.0, 4320.0], plots=())
+
+
 def T(x):
     return torch.as_tensor(np.asarray(x), device=DEV)

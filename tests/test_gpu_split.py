@@ -94,6 +94,18 @@ def test_split_bve_matches_fp64():
     assert rel_l2(N(ms.rk4(T(z), 900.0, 5)), N(m64.rk4(T(z), 900.0, 5))) < 1e-11
 
 
+def test_bounded_wait_gives_up_and_reports():
+    """The tensor-core kernels' mbarrier waits are bounded in wall time: a
+    wait on a phase that nothing completes gives up after its limit (20 ms
+    here), reports it, and leaves the context usable."""
+    import ctypes
+    flag, ns = ctypes.c_int(-1), ctypes.c_ulonglong(0)
+    _lib.check(_lib.load().aeolus_selftest_wait_timeout(20_000_000, ctypes.byref(flag), ctypes.byref(ns)))
+    assert flag.value == 1
+    assert 20_000_000 <= ns.value < 1_000_000_000
+    assert float(torch.ones(4, device=DEV).sum()) == 4.0
+
+
 def test_split_rejects_unsupported_shapes():
     p = Plan.gauss(256, 512, 170)
     with pytest.raises(ValueError, match="l_max"):
