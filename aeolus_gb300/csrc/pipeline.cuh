@@ -120,6 +120,21 @@ int launch_rows_fx(const aeolus_plan_impl* p, const Pw& pw, const RowArgs& a, cu
   return AEOLUS_OK;
 }
 
+// Fixed radix sequence (R0, 8, 8): compile-time lengths, kFx8Threads threads
+// (the plan's row-thread knob does not apply).
+template <class Pw, int IN_MODE, int OUT_MODE, int R0>
+int launch_rows_fx8(const aeolus_plan_impl* p, const Pw& pw, const RowArgs& a, cudaStream_t st) {
+  const size_t sm = row_fx8_smem_bytes<Pw>(R0);
+  auto kern = row_kernel_fx8<Pw, IN_MODE, OUT_MODE, R0>;
+  int s = allow_smem(kern, sm);
+  if (s) return s;
+  ProfScope prof(IN_MODE == kInF ? (OUT_MODE == kOutG ? "rows_fx_c2r_products_r2c" : "rows_fx_c2r") : "rows_fx_r2c",
+                 st);
+  kern<<<dim3(p->nlat, a.batch), kFx8Threads, sm, st>>>(a, pw, p->twfx, fx_consts());
+  AE_LAUNCH("row_kernel_fx8");
+  return AEOLUS_OK;
+}
+
 template <class Pw, int IN_MODE, int OUT_MODE>
 int launch_rows(const aeolus_plan_impl* p, const Pw& pw, RowArgs a, cudaStream_t st) {
   row_args(p, a);
@@ -131,8 +146,8 @@ int launch_rows(const aeolus_plan_impl* p, const Pw& pw, RowArgs a, cudaStream_t
     a.fft = p->fftx;
     using F388 = FftFixed<3, 8, 8>;  // nlon 384
     using F288 = FftFixed<2, 8, 8>;  // nlon 256
-    if (F388::matches(p->fftx)) return launch_rows_fx<Pw, IN_MODE, OUT_MODE, F388>(p, pw, a, st);
-    if (F288::matches(p->fftx)) return launch_rows_fx<Pw, IN_MODE, OUT_MODE, F288>(p, pw, a, st);
+    if (F388::matches(p->fftx)) return launch_rows_fx8<Pw, IN_MODE, OUT_MODE, 3>(p, pw, a, st);
+    if (F288::matches(p->fftx)) return launch_rows_fx8<Pw, IN_MODE, OUT_MODE, 2>(p, pw, a, st);
     return launch_rows_fx<Pw, IN_MODE, OUT_MODE, FftRuntime>(p, pw, a, st);
   }
   const size_t sm = row_smem_bytes<Pw>(p->fft);

@@ -510,6 +510,298 @@ __device__ __forceinline__ void row_fx_body(const RowArgs& a, const Pw& pw, cons
   }
 }
 
+// ------------------------------------------------------------------------
+// Row stage for the radix sequences (R0, 8, 8), n = 64 R0 (nlon 384 and
+// 256), with every length a compile-time constant and kFx8Threads threads.
+// The arithmetic and its order are those of row_fx_body (the results are
+// bitwise the same); the data movement differs:
+//  * complex element i of a field's row lives in slot swz(i), a rotation
+//    inside each group of 8 slots (16-byte slots: 8 slots span the 32
+//    banks): rotation 3 (i / 24) for R0 = 3, i / 8 for R0 = 2.  With it every
+//    8-lane phase of every butterfly pass of the three stages touches 8
+//    distinct bank groups (the plain layout had up to 3-way conflicts);
+//  * for R0 = 3 the radix-8 stage at sub-length 3 runs its butterflies
+//    k-major, which keeps the stage conflict-free and gives whole warps
+//    k = 0, whose twiddles are 1 and are skipped (exact: a Q61 twiddle of 1
+//    multiplies exactly);
+//  * loops over (order, field) pairs stride by a multiple of the field
+//    count, so a thread keeps one field: one running maximum per thread
+//    instead of a shared atomic per element, block scales in registers;
+//  * the digit reversal of the in-place DIT input is arithmetic:
+//    natural index q = 64 t0 + 8 t1 + t2 sits at t0 + R0 (t1 + 8 t2).
+constexpr int kFx8Threads = 128;
+
+template <int R0>
+struct Fx8 {
+  static constexpr int n = 64 * R0, N = 2 * n, fs = n + 1;  // fs odd: field-fastest passes spread over banks
+  static constexpr int hb = (R0 == 3 ? 56 - 8 : 56 - 7);     // min(52, 56 - ceil(log2 n))
+  static __device__ __forceinline__ int swz(int i) {
+    return R0 == 3 ? ((i & ~7) | ((i + 3 * (i / 24)) & 7)) : ((i & ~7) | ((i + (i >> 3)) & 7));
+  }
+  static __device__ __forceinline__ int rev(int q) { return (q >> 6) + R0 * (((q >> 3) & 7) + 8 * (q & 7)); }
+};
+
+template <int R0, bool INV, int R, int LS, bool DIT, bool TW, bool CONV, int NFLD>
+__device__ __forceinline__ void fx8_stage(cfx* __restrict__ x, const FxW* __restrict__ tw, const FxConst& kc,
+                                          const float* sqa, const float* sqb) {
+  using Row = Fx8<R0>;
+  constexpr int n = Row::n, nb = n / R, NS = LS * R, stride = n / NS, G = nb / LS;
+  constexpr bool kmajor = R0 == 3 && LS == R0;
+#pragma unroll 1
+  for (int idx = threadIdx.x; idx < NFLD * nb; idx += kFx8Threads) {
+    int f, g, k;
+    if constexpr (kmajor) {
+      g = idx % G;
+      const int r = idx / G;
+      f = r % NFLD;
+      k = r / NFLD;
+    } else {
+      f = idx / nb;
+      const int jj = idx - f * nb;
+      g = jj / LS;
+      k = jj - g * LS;
+    }
+    cfx* y = x + f * Row::fs;
+    const int base = g * NS + k;
+    cfx v[R];
+    if constexpr (CONV) {
+      const float pa = sqa[f], pb = sqb[f];
+#pragma unroll
+      for (int t = 0; t < R; ++t) {
+        const float4 w = reinterpret_cast<const float4*>(y)[Row::swz(base + t * LS)];
+        v[t] = cfx{df_to_fx(df{w.x, w.y}, pa, pb), df_to_fx(df{w.z, w.w}, pa, pb)};
+      }
+    } else {
+#pragma unroll
+      for (int t = 0; t < R; ++t) v[t] = y[Row::swz(base + t * LS)];
+    }
+    const bool tw_on = TW && (!kmajor || k != 0);
+    if (DIT && tw_on) {
+#pragma unroll
+      for (int t = 1; t < R; ++t) v[t] = fx_cmul<INV>(v[t], fx_ldw(&tw[2 * (k * t * stride)]));
+    }
+    butterfly_fx<INV, R>(v, kc);
+    if (!DIT && tw_on) {
+#pragma unroll
+      for (int t = 1; t < R; ++t) v[t] = fx_cmul<INV>(v[t], fx_ldw(&tw[2 * (k * t * stride)]));
+    }
+#pragma unroll
+    for (int t = 0; t < R; ++t) y[Row::swz(base + t * LS)] = v[t];
+  }
+}
+
+// In-place inverse (DIT, digit-reversed input) or forward (DIF, with the
+// double-float rows rounded to fixed point by its first stage) transforms.
+template <int R0, bool INV, int NFLD>
+__device__ __forceinline__ void fx8_fft(cfx* x, const FxW* __restrict__ tw, const FxConst& kc, const float* sqa,
+                                        const float* sqb) {
+  if constexpr (INV) {
+    fx8_stage<R0, true, R0, 1, true, false, false, NFLD>(x, tw, kc, nullptr, nullptr);
+    __syncthreads();
+    fx8_stage<R0, true, 8, R0, true, true, false, NFLD>(x, tw, kc, nullptr, nullptr);
+    __syncthreads();
+    fx8_stage<R0, true, 8, 8 * R0, true, true, false, NFLD>(x, tw, kc, nullptr, nullptr);
+    __syncthreads();
+  } else {
+    fx8_stage<R0, false, 8, 8 * R0, false, true, true, NFLD>(x, tw, kc, sqa, sqb);
+    __syncthreads();
+    fx8_stage<R0, false, 8, R0, false, true, false, NFLD>(x, tw, kc, nullptr, nullptr);
+    __syncthreads();
+    fx8_stage<R0, false, R0, 1, false, false, false, NFLD>(x, tw, kc, nullptr, nullptr);
+    __syncthreads();
+  }
+}
+
+template <class Pw, int IN_MODE, int OUT_MODE, int R0>
+__device__ __forceinline__ void row_fx8_body(const RowArgs& a, const Pw& pw, const FxW* __restrict__ twfx,
+                                             const FxConst& kc, int bx, int by) {
+  using Row = Fx8<R0>;
+  constexpr int NIN = Pw::NIN, NOUT = Pw::NOUT;
+  constexpr int NF = NIN > NOUT ? NIN : NOUT;
+  constexpr int n = Row::n, N = Row::N, fs = Row::fs, hb = Row::hb, T = kFx8Threads;
+  // (order, field) passes: stride PS, a multiple of the field count
+  constexpr int PSI = (T / NIN) * NIN, QSI = T / NIN;
+  constexpr int PSO = (T / NOUT) * NOUT, QSO = T / NOUT;
+  extern __shared__ cfx smem_fx[];
+  __shared__ unsigned s_bits;
+  __shared__ int s_in[NF];
+  __shared__ unsigned s_key[NF];
+  __shared__ unsigned s_omax[NF];
+  __shared__ float s_pa[NF], s_pb[NF], s_qa[NF], s_qb[NF];
+  __shared__ RowDf s_rc;
+  __shared__ df s_wj;
+  const int j = bx, b = by, tid = threadIdx.x;
+  const int L = a.L, ldm = L + 1;
+  cfx* buf0 = smem_fx;
+  if (tid == 0) s_bits = 0u;
+  if (tid < NF) {
+    s_key[tid] = 0u;
+    s_omax[tid] = 0u;
+  }
+  if (tid == 0) {
+    s_rc = pw.df_row(a.coslat[j], a.fgrid ? a.fgrid[j] : 0.0);
+    s_wj = (OUT_MODE == kOutG && a.wq) ? df_from_double(a.wq[j]) : df{1.f, 0.f};
+  }
+  const long sq = (long)a.nblk * a.nlat;
+  float4* block = nullptr;
+  if (IN_MODE == kInF || OUT_MODE == kOutG)
+    block = reinterpret_cast<float4*>(a.FG) + fg_index(b, 0, 0, j, L, a.nblk, a.nlat);
+  const long sqo = a.G ? (long)a.gblk * a.nlat : sq;
+  float4* oblock = nullptr;
+  if (OUT_MODE == kOutG)
+    oblock = a.G ? reinterpret_cast<float4*>(a.G) + fg_index(b, 0, 0, j, L, a.gblk, a.nlat) : block;
+  __syncthreads();
+
+  // ---- 1. grid rows of the inputs, in buf0
+  if constexpr (IN_MODE == kInF) {
+    if (tid < PSI) {  // largest |hi| of this thread's field over its orders
+      const int f = tid % NIN;
+      unsigned mx = 0u;
+      for (int q = tid / NIN; q < ldm; q += QSI) {
+        const float4 w = block[(long)q * sq + f];
+        mx = max(mx, max(__float_as_uint(w.x) & 0x7FFFFFFFu, q == 0 ? 0u : __float_as_uint(w.z) & 0x7FFFFFFFu));
+      }
+      if (mx) atomicMax(&s_key[f], mx);
+    }
+    __syncthreads();
+    if (tid < NIN) {
+      const unsigned key = s_key[tid];
+      const int S = (key >> 23) == 0 ? 0 : fkey_exp(key) - hb;
+      s_in[tid] = S;
+      fx_pow2_split(S, s_pa[tid], s_pb[tid]);
+      fx_pow2_split(-S, s_qa[tid], s_qb[tid]);
+    }
+    __syncthreads();
+    if (tid < PSI) {
+      // half-length complex input of the real inverse FFT, by pairs (q, n-q)
+      // (as row_fx_body), written to the digit-reversed slots
+      const int f = tid % NIN;
+      const float qa = s_qa[f], qb = s_qb[f];
+      cfx* z = buf0 + f * fs;
+      for (int q = tid / NIN; q <= n / 2; q += QSI) {
+        const int qn = n - q;
+        cfx hq = cfx{0, 0}, hn = cfx{0, 0};
+        if (q <= L) {
+          const float4 w = block[(long)q * sq + f];
+          hq = cfx{df_to_fx(df{w.x, w.y}, qa, qb), q == 0 ? 0LL : df_to_fx(df{w.z, w.w}, qa, qb)};
+        }
+        if (q > 0 && qn <= L) {
+          const float4 w = block[(long)qn * sq + f];
+          hn = cfx{df_to_fx(df{w.x, w.y}, qa, qb), df_to_fx(df{w.z, w.w}, qa, qb)};
+        }
+        const cfx A = fx_add(hq, fx_conj(hn));
+        const cfx B = fx_sub(hq, fx_conj(hn));
+        const cfx P = fx_i<true>(fx_cmul<true>(B, fx_ldw(&twfx[q])));
+        z[Row::swz(Row::rev(q))] = fx_add(A, P);
+        if (q > 0 && qn > q) z[Row::swz(Row::rev(qn))] = fx_conj(fx_sub(A, P));
+      }
+    }
+    __syncthreads();
+    fx8_fft<R0, true, NIN>(buf0, twfx, kc, nullptr, nullptr);
+  } else {
+    df* x0 = reinterpret_cast<df*>(buf0);
+    for (int idx = tid; idx < NIN * N; idx += T) {
+      const int f = idx / N, k = idx - f * N;
+      x0[2 * (f * fs + Row::swz(k >> 1)) + (k & 1)] =
+          df_from_double(a.gin[(long)b * a.gin_b + (long)f * a.gin_f + (long)j * N + k]);
+    }
+    __syncthreads();
+  }
+
+  // ---- 2. pointwise products (double-float), weighted by the row's quadrature
+  // weight; in place (each point is read before it is written, by one thread)
+  df* xout = reinterpret_cast<df*>(buf0);
+  {
+    const RowDf rc = s_rc;
+    const df wj = s_wj;
+    const long long* xi = reinterpret_cast<const long long*>(buf0);
+    const df* xd = reinterpret_cast<const df*>(buf0);
+    unsigned bits = 0u;
+    unsigned omax[NOUT];
+#pragma unroll
+    for (int f = 0; f < NOUT; ++f) omax[f] = 0u;
+    float pa[NIN], pb[NIN];
+    if constexpr (IN_MODE == kInF) {
+#pragma unroll
+      for (int f = 0; f < NIN; ++f) {
+        pa[f] = s_pa[f];
+        pb[f] = s_pb[f];
+      }
+    }
+#pragma unroll 1
+    for (int it = 0; it < N / T; ++it) {
+      const int k = tid + it * T;
+      const int slot = 2 * Row::swz(k >> 1) + (k & 1);
+      df in[NIN], out[NOUT];
+#pragma unroll
+      for (int f = 0; f < NIN; ++f)
+        in[f] = IN_MODE == kInF ? fx_to_df(xi[2 * f * fs + slot], pa[f], pb[f]) : xd[2 * f * fs + slot];
+      bits |= pw.df_op(rc, in, out);
+#pragma unroll
+      for (int f = 0; f < NOUT; ++f) {
+        if (OUT_MODE == kOutG && a.wq) out[f] = df_mul(out[f], wj);
+        xout[2 * f * fs + slot] = out[f];
+        omax[f] = max(omax[f], __float_as_uint(out[f].hi) & 0x7FFFFFFFu);
+      }
+    }
+    if (a.status && bits) atomicOr(&s_bits, bits);
+    if (OUT_MODE == kOutG) {
+#pragma unroll
+      for (int f = 0; f < NOUT; ++f) {
+        unsigned v = omax[f];
+        for (int o = 16; o > 0; o >>= 1) v = max(v, __shfl_xor_sync(0xffffffffu, v, o));
+        if ((tid & 31) == 0 && v) atomicMax(&s_omax[f], v);
+      }
+    }
+  }
+  __syncthreads();
+  if (a.status && tid == 0 && s_bits) atomicOr(&a.status[b], s_bits);
+
+  // ---- 3. outputs
+  if constexpr (OUT_MODE == kOutGrid) {
+    for (int idx = tid; idx < NOUT * N; idx += T) {
+      const int f = idx / N, k = idx - f * N;
+      a.gout[(long)b * a.gout_b + (long)f * a.gout_f + (long)j * N + k] =
+          df_to_double(xout[2 * (f * fs + Row::swz(k >> 1)) + (k & 1)]);
+    }
+  } else {
+    if (tid < NOUT) {
+      const unsigned key = s_omax[tid];
+      const int S = (key >> 23) == 0 ? 0 : fkey_exp(key) - hb;
+      s_in[tid] = S;
+      fx_pow2_split(-S, s_pa[tid], s_pb[tid]);
+    }
+    __syncthreads();
+    fx8_fft<R0, false, NOUT>(buf0, twfx, kc, s_pa, s_pb);
+    if (tid < PSO) {
+      const int f = tid % NOUT;
+      const int e = s_in[f] - 1;  // R2 / 2 in units of 2^S
+      const cfx* Zf = buf0 + f * fs;
+      for (int q = tid / NOUT; q < ldm; q += QSO) {
+        const cfx zq = Zf[Row::swz(Row::rev(q))];
+        const cfx zn = fx_conj(Zf[Row::swz(Row::rev(q == 0 ? 0 : n - q))]);
+        const cfx E2 = fx_add(zq, zn);
+        const cfx D = fx_sub(zq, zn);
+        const cfx O2 = cfx{D.im, -D.re};
+        const cfx R2 = fx_add(E2, fx_cmul<false>(O2, fx_ldw(&twfx[q])));
+        reinterpret_cast<longlong2*>(oblock)[(long)q * sqo + f] = make_longlong2(pk_pack(R2.re, e), pk_pack(R2.im, e));
+      }
+    }
+  }
+}
+
+template <class Pw, int IN_MODE, int OUT_MODE, int R0>
+__global__ void __launch_bounds__(kFx8Threads, 6) row_kernel_fx8(RowArgs a, Pw pw, const FxW* __restrict__ twfx,
+                                                                 FxConst kc) {
+  row_fx8_body<Pw, IN_MODE, OUT_MODE, R0>(a, pw, twfx, kc, blockIdx.x, blockIdx.y);
+}
+
+template <class Pw>
+constexpr size_t row_fx8_smem_bytes(int R0) {
+  constexpr int NF = Pw::NIN > Pw::NOUT ? Pw::NIN : Pw::NOUT;
+  return (size_t)NF * (64 * R0 + 1) * sizeof(cfx);
+}
+
 // Dynamic shared memory of row_kernel_fx: one row buffer for the in-place
 // FFTs, a second one for the staged spectra of the direct DFT.
 template <class Pw>

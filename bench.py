@@ -891,7 +891,7 @@ def main():
                 "roofline": roof, "cpu_baseline": cpu, "clocks": clock_summary}
         if direct is not None:
             line["direct_steps_vs_reference"] = {
-                k: {kk: {m: round(x, 6) if isinstance(x, float) else x for m, x in vv.items()
+                k: {kk: {m: float(f"{x:.4g}") for m, x in vv.items()
                          if m in ("steps_per_s", "rel_l2_vs_reference_step")}
                     for kk, vv in v.items() if isinstance(vv, dict)} for k, v in direct.items()}
         line["split_vs_fp64"] = comparison
