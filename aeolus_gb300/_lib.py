@@ -56,6 +56,7 @@ SIGNATURES = {
     "aeolus_plan_nodes": (c_int, [c_void_p, c_void_p, c_void_p]),
     "aeolus_plan_set_precision": (c_int, [c_void_p, c_int, c_int]),
     "aeolus_plan_device_error": (c_int, [c_void_p, POINTER(c_int)]),
+    "aeolus_rk4_stage": (c_int, [c_int, c_double, c_void_p, c_void_p, c_void_p, c_void_p, c_long, c_void_p]),
     "aeolus_selftest_wait_timeout": (c_int, [ctypes.c_ulonglong, POINTER(c_int), POINTER(ctypes.c_ulonglong)]),
     "aeolus_plan_set_tuning": (c_int, [c_void_p, POINTER(c_int)]),
     "aeolus_plan_get_tuning": (c_int, [c_void_p, POINTER(c_int)]),

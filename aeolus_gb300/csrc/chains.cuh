@@ -72,9 +72,27 @@ size_t anal_chain_bytes(const aeolus_plan_impl* p, int batch) {
 template <class Derive, class Pw, class Epi>
 int run_full_chain(const aeolus_plan_impl* p, const Derive& d, const Pw& pw, const Epi& e, int batch,
                    void* work, unsigned* status, cudaStream_t st) {
-  static_assert(Derive::NF == Pw::NIN, "derive/pointwise field count");
+  static_assert(SynthOut<Derive>::NBLK == Pw::NIN, "derive/pointwise field count");
   static_assert(Pw::NOUT == Epi::NF, "pointwise/epilogue field count");
-  if (p->kind == kGauss) {
+  if constexpr (SynthOut<Derive>::kLam) {
+    // fields formed by the tensor-core synthesis epilogue: split Gauss plans only
+    if (!split_on(p)) return fail(AEOLUS_ERR_ARG, "derived-field synthesis needs a split-precision Gauss plan");
+    double2* FG = static_cast<double2*>(work);
+    constexpr int NB = Pw::NIN > Pw::NOUT ? Pw::NIN : Pw::NOUT;
+    double2* G = reinterpret_cast<double2*>(static_cast<char*>(work) + align256(fg_bytes(p, NB, batch)));
+    void* scratch = static_cast<char*>(work) + align256(fg_bytes(p, NB, batch)) + align256(fg_bytes(p, Pw::NOUT, batch));
+    int s = launch_split_synth(p, d, FG, NB, batch, scratch, st);
+    if (s) return s;
+    RowArgs ra{};
+    ra.batch = batch;
+    ra.FG = FG;
+    ra.nblk = NB;
+    ra.G = G;
+    ra.gblk = Pw::NOUT;
+    ra.status = status;
+    if ((s = launch_rows<Pw, kInF, kOutG>(p, pw, ra, st))) return s;
+    return launch_split_anal(p, e, G, Pw::NOUT, batch, scratch, st);
+  } else if (p->kind == kGauss) {
     constexpr int NB = Pw::NIN > Pw::NOUT ? Pw::NIN : Pw::NOUT;
     double2* FG = static_cast<double2*>(work);
     const bool split = split_on(p);

@@ -162,10 +162,15 @@ struct GroupedEpi {
   static constexpr int kWarps = Epi::kWarps, kCols = Epi::kCols;
   GroupedSched<Sched> gs;  // for the tile -> group map
   Epi e[kMaxGroups];
-  template <class Rel>
-  __device__ void run(int t, uint32_t tbuf, int q, int row, int c0, int etid, Rel release) const {
+  using Pre = typename Epi::Pre;
+  __device__ Pre prefetch(int t, int row, int c0) const {
     const int k = gs.find(t);
-    e[k].run(t - gs.start[k], tbuf, q, row, c0, etid, release);
+    return e[k].prefetch(t - gs.start[k], row, c0);
+  }
+  template <class Rel>
+  __device__ void run(int t, uint32_t tbuf, int q, int row, int c0, int etid, Rel release, const Pre& pre) const {
+    const int k = gs.find(t);
+    e[k].run(t - gs.start[k], tbuf, q, row, c0, etid, release, pre);
   }
 };
 
@@ -178,6 +183,10 @@ struct GroupedEpi<Sched, Epi, true> {
   GroupedSched<Sched> gs;
   Epi e[kMaxGroups];
   __device__ void seg_begin(State& st) const { e[0].seg_begin(st); }
+  __device__ void seg_prefetch(State& st, int t, int row, int c0) const {
+    const int k = gs.find(t);
+    e[k].seg_prefetch(st, t - gs.start[k], row, c0);
+  }
   __device__ void seg_add(State& st, uint32_t tbuf, int q, int c0) const { e[0].seg_add(st, tbuf, q, c0); }
   __device__ void seg_end(int t, const State& st, int row, int c0, int etid) const {
     const int k = gs.find(t);
@@ -189,6 +198,8 @@ struct GroupedEpi<Sched, Epi, true> {
 // the group workspace (chain scratch, stage inputs, RK4 accumulator).
 struct BveModel {
   using Derive = BveDerive;
+  using SplitDerive = BveDerive;  // the split path's synthesis functor
+  static SplitDerive split_derive(const Derive& d) { return d; }
   using Pw = JacPw;
   using Epi = BveEpi;
   static constexpr int NIN = 4, NOUT = 1;
@@ -223,6 +234,10 @@ struct BveModel {
 
 struct SweModel {
   using Derive = SweDerive;
+  // split path: 7 contracted fields, the longitude derivatives formed by the
+  // synthesis epilogue (as aeolus_swe_rk4 does)
+  using SplitDerive = SweDerive7;
+  static SplitDerive split_derive(const Derive& d) { return SweDerive7{d}; }
   using Pw = SwePw;
   using Epi = SweEpi;
   static constexpr int NIN = 9, NOUT = 4;
@@ -358,10 +373,13 @@ int ens_stage_m(const aeolus_ensemble_s* E, double2* const* y0, int stage, doubl
     return AEOLUS_OK;
   }
   // split precision
-  Grouped<SliceSynthArg<Derive>> gss{};
+  using SDerive = typename M::SplitDerive;
+  constexpr int NS = SDerive::NF;  // contracted fields
+  using SEpi = SynthEpi<NS, SynthOut<SDerive>>;
+  Grouped<SliceSynthArg<SDerive>> gss{};
   Grouped<SliceAnalArg> gsa{};
   GroupedSched<SynthSched> tsyn{};
-  GroupedEpi<SynthSched, SynthEpi<NIN>> esyn{};
+  GroupedEpi<SynthSched, SEpi> esyn{};
   GroupedSched<AnalSched> tana{};
   GroupedEpi<AnalSched, AnalEpi<Epi>> eana{};
   size_t sm_ss = 0, sm_sa = 0;
@@ -372,9 +390,10 @@ int ens_stage_m(const aeolus_ensemble_s* E, double2* const* y0, int stage, doubl
     const int B = E->batch[k];
     double2* FG = reinterpret_cast<double2*>(chain[k]);
     void* scratch = chain[k] + align256(fg_bytes(p, NB, B));
-    const SplitParts r1 = split_synth_parts<NIN>(p, B, scratch);
+    const SplitParts r1 = split_synth_parts<NS>(p, B, scratch);
     const SplitParts r2 = split_anal_parts<NOUT>(p, B, scratch);
-    grouped_add(gss, SliceSynthArg<Derive>{r1.dm, p->split->kcum, B, r1.mb, der[k], r1.digits, r1.ecol}, r1.grid);
+    const SDerive sd = M::split_derive(der[k]);
+    grouped_add(gss, SliceSynthArg<SDerive>{r1.dm, p->split->kcum, B, r1.mb, sd, r1.digits, r1.ecol}, r1.grid);
     grouped_add(gsa, SliceAnalArg{r2.dm, B, r2.mb, NB, reinterpret_cast<const long long*>(FG), r2.digits, r2.ecol},
                 r2.grid);
     sm_ss = std::max(sm_ss, r1.smem);
@@ -382,7 +401,9 @@ int ens_stage_m(const aeolus_ensemble_s* E, double2* const* y0, int stage, doubl
     const SynthSched sc{r1.dm, p->split->kcum, p->split->psyn, r1.digits};
     tsyn.s[k] = sc;
     tsyn.start[k + 1] = tsyn.start[k] + sc.count_host();
-    esyn.e[k] = SynthEpi<NIN>{r1.dm, p->split->esyn, r1.ecol, NB, reinterpret_cast<float4*>(FG)};
+    esyn.e[k] = SEpi{r1.dm, p->split->esyn, r1.ecol, NB, reinterpret_cast<float4*>(FG)};
+    esyn.e[k].ir_hi = (float)SynthOut<SDerive>::ir(sd);
+    esyn.e[k].ir_lo = (float)(SynthOut<SDerive>::ir(sd) - (double)esyn.e[k].ir_hi);
     const AnalSched sa{r2.dm, p->split->pana, r2.digits};
     tana.s[k] = sa;
     tana.start[k + 1] = tana.start[k] + sa.count_host();
@@ -393,8 +414,8 @@ int ens_stage_m(const aeolus_ensemble_s* E, double2* const* y0, int stage, doubl
   tsyn.n = tana.n = ng;
   esyn.gs = tsyn;
   eana.gs = tana;
-  auto k1 = g_slice_synth<Derive>;
-  auto k2 = tc_persistent_kernel<GroupedSched<SynthSched>, GroupedEpi<SynthSched, SynthEpi<NIN>>>;
+  auto k1 = g_slice_synth<SDerive>;
+  auto k2 = tc_persistent_kernel<GroupedSched<SynthSched>, GroupedEpi<SynthSched, SEpi>>;
   auto k3 = g_rows_fx<Pw>;
   auto k4 = g_slice_anal<NOUT>;
   auto k5 = tc_persistent_kernel<GroupedSched<AnalSched>, GroupedEpi<AnalSched, AnalEpi<Epi>>>;
@@ -409,7 +430,7 @@ int ens_stage_m(const aeolus_ensemble_s* E, double2* const* y0, int stage, doubl
   }
   {
     ProfScope prof("ens_tc_synth_bf16x6", st);
-    k2<<<std::max(1, std::min(tsyn.start[ng], sm_count)), tc_threads<GroupedEpi<SynthSched, SynthEpi<NIN>>>(), smt,
+    k2<<<std::max(1, std::min(tsyn.start[ng], sm_count)), tc_threads<GroupedEpi<SynthSched, SEpi>>(), smt,
          st>>>(tsyn, esyn, err);
     AE_LAUNCH("tc_persistent_kernel(ensemble synthesis)");
   }

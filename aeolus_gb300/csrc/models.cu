@@ -440,6 +440,8 @@ extern "C" int aeolus_swe_tendency(aeolus_plan plan, const aeolus_swe_params* p,
   Rk4 rk{0, 0.0, nullptr, nullptr, nullptr, reinterpret_cast<double2*>(tend)};
   SweEpi e{sp, reinterpret_cast<const double2*>(state), phi0, p->nu4, rk, spec_cor ? 2.0 * p->omega : 0.0, cor};
   e.forcing = reinterpret_cast<const double2*>(p->forcing);
+  // split path: 7 contracted fields, the two longitude derivatives formed in the synthesis epilogue
+  if (spec_cor) return run_full_chain(plan, SweDerive7{d}, pw, e, batch, work, nullptr, static_cast<cudaStream_t>(stream));
   return run_full_chain(plan, d, pw, e, batch, work, nullptr, static_cast<cudaStream_t>(stream));
 }
 
@@ -506,7 +508,9 @@ extern "C" int aeolus_swe_rk4(aeolus_plan plan, const aeolus_swe_params* p, doub
       Rk4 rk{stage, dt, y0, next, acc, nullptr};
       SweEpi e{sp, in, phi0, p->nu4, rk, spec_cor ? 2.0 * p->omega : 0.0, cor};
       e.forcing = reinterpret_cast<const double2*>(p->forcing);
-      if ((s = run_full_chain(plan, d, pw, e, batch, chain, status, st))) return s;
+      s = spec_cor ? run_full_chain(plan, SweDerive7{d}, pw, e, batch, chain, status, st)
+                   : run_full_chain(plan, d, pw, e, batch, chain, status, st);
+      if (s) return s;
     }
   return AEOLUS_OK;
 }

@@ -336,6 +336,32 @@ struct SwePw {
   }
 };
 
+// Split-precision form of the SWE derive: the tensor-core synthesis
+// contracts 7 fields [U, V, eta_snt, phi_snt, zeta, delta, phi] and its
+// epilogue writes the 9 spectra blocks of SwePw, forming the longitude
+// derivatives eta_lam = i m/R zeta and phi_lam = i m/R phi from the zeta
+// and phi order spectra (d/dlambda is diagonal in m, so it needs no
+// contraction of its own; see SynthOut in split.cuh).
+struct SweDerive7 {
+  static constexpr int NF = 7;
+  static constexpr int NBLK = 9;  // spectra blocks written by the synthesis epilogue
+  __host__ __device__ static constexpr int blk(int f) { return f == 0 ? 0 : f == 1 ? 1 : f == 2 ? 3 : f == 3 ? 5 : f + 2; }
+  __host__ __device__ static constexpr int lam_blk(int f) { return f == 4 ? 2 : f == 6 ? 4 : -1; }
+  SweDerive d9;
+  double lam_ir() const { return d9.s.ir; }  // 1 / R of the i m / R factor
+  __device__ void column(int b, int l, int m, double2* v) const {
+    double2 w[9];
+    d9.column(b, l, m, w);
+    v[0] = w[0];
+    v[1] = w[1];
+    v[2] = w[3];
+    v[3] = w[5];
+    v[4] = w[6];
+    v[5] = w[7];
+    v[6] = w[8];
+  }
+};
+
 // Spectral epilogue of the SWE tendency.  With `coriolis` set (split-
 // precision path) the pointwise products carry only the relative vorticity
 // and the planetary-vorticity terms are added here exactly:

@@ -82,20 +82,24 @@ __global__ void split_psyn_kernel(int L, int nlat, int nh, int Mt, const double*
   }
 }
 
-// Analysis: one thread per (m, degree row).
+// Analysis: one thread per (row tile, degree row); row tile rt holds
+// degrees m + 128 mt + r of order m (ana_row_tile).
 __global__ void split_pana_kernel(int L, int nlat, int nh, int NK, const double* __restrict__ P,
                                   __nv_bfloat16* __restrict__ out, int* __restrict__ eout) {
-  const int m = blockIdx.y;
-  const int t = blockIdx.x * blockDim.x + threadIdx.x;
-  if (m > L || t >= 128) return;
+  const int rt = blockIdx.y;
+  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (rt >= ana_row_tiles(L) || r >= 128) return;
+  int m, mt;
+  ana_row_tile(L, rt, m, mt);
   const int K = L + 1 - m;
-  __nv_bfloat16* blk = out + pana_tile(NK, m);
+  const int t = mt * 128 + r;  // degree offset l - m
+  __nv_bfloat16* blk = out + pana_tile(NK, rt);
   const double* Pm = P + tri_off(m, L) * nh + (long)t * nh;
   unsigned long long mx = 0ull;
   if (t < K)
     for (int jn = 0; jn < nh; ++jn) mx = max(mx, abs_key(Pm[jn]));
   const int E = t < K ? exponent_for_key(mx) : 0;
-  eout[m * 128 + t] = E;
+  eout[rt * 128 + r] = E;
   for (int j = 0; j < NK; ++j) {
     double v = 0.0;
     if (t < K && j < nlat) {
@@ -104,7 +108,7 @@ __global__ void split_pana_kernel(int L, int nlat, int nh, int NK, const double*
     }
     __nv_bfloat16 d[kSlices];
     digits(v, E, d);
-    for (int s = 0; s < kSlices; ++s) blk[tile_elem(128, s, t, j)] = d[s];
+    for (int s = 0; s < kSlices; ++s) blk[tile_elem(128, s, r, j)] = d[s];
   }
 }
 
@@ -196,7 +200,7 @@ int split_build(aeolus_plan_impl* p) {
   if (p->split) return AEOLUS_OK;
   if (p->kind == kPoints) return split_build_points(p);
   const int L = p->lmax;
-  if (L > 127) return fail(AEOLUS_ERR_ARG, "split precision supports l_max <= 127");
+  if (L > kMaxL) return fail(AEOLUS_ERR_ARG, "split precision supports l_max <= 159 (exact f32 synthesis segments)");
   if (p->nlat > 192) return fail(AEOLUS_ERR_ARG, "split precision supports nlat <= 192 (exact f32 accumulation)");
   auto* t = new SplitTables();
   p->split = t;
@@ -208,19 +212,19 @@ int split_build(aeolus_plan_impl* p) {
   t->h_kcum.assign(L + 2, 0);
   for (int m = 0; m <= L; ++m) t->h_kcum[m + 1] = t->h_kcum[m] + kpad(L + 1 - m);
   const size_t nsyn = (size_t)t->h_kcum[L + 1] * t->Mt * kSlices * 128;
-  const size_t nana = (size_t)(L + 1) * kSlices * 128 * t->NK;
+  const size_t nana = (size_t)ana_row_tiles(L) * kSlices * 128 * t->NK;
   AE_CUDA(cudaMalloc(&t->kcum, (L + 2) * sizeof(long long)));
   AE_CUDA(cudaMemcpy(t->kcum, t->h_kcum.data(), (L + 2) * sizeof(long long), cudaMemcpyHostToDevice));
   AE_CUDA(cudaMalloc(&t->psyn, nsyn * sizeof(__nv_bfloat16)));
   AE_CUDA(cudaMalloc(&t->pana, nana * sizeof(__nv_bfloat16)));
   AE_CUDA(cudaMalloc(&t->esyn, (size_t)(L + 1) * t->Mt * 128 * sizeof(int)));
-  AE_CUDA(cudaMalloc(&t->eana, (size_t)(L + 1) * 128 * sizeof(int)));
+  AE_CUDA(cudaMalloc(&t->eana, (size_t)ana_row_tiles(L) * 128 * sizeof(int)));
   AE_CUDA(cudaMalloc(&t->err, sizeof(int)));
   AE_CUDA(cudaMemset(t->err, 0, sizeof(int)));
   split_psyn_kernel<<<dim3((t->Mt * 128 + 127) / 128, L + 1), 128>>>(L, p->nlat, p->nh, t->Mt, p->P, t->kcum, t->psyn,
                                                                       t->esyn);
   AE_LAUNCH("split_psyn_kernel");
-  split_pana_kernel<<<dim3(1, L + 1), 128>>>(L, p->nlat, p->nh, t->NK, p->P, t->pana, t->eana);
+  split_pana_kernel<<<dim3(1, ana_row_tiles(L)), 128>>>(L, p->nlat, p->nh, t->NK, p->P, t->pana, t->eana);
   AE_LAUNCH("split_pana_kernel");
   AE_CUDA(cudaDeviceSynchronize());
   return AEOLUS_OK;

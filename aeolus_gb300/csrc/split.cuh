@@ -5,6 +5,9 @@
 
 #include <cuda_bf16.h>
 
+#include <type_traits>
+#include <utility>
+
 #include "common.cuh"
 #include "df.cuh"
 #include "fx.cuh"
@@ -19,14 +22,14 @@ constexpr int kAccs = 6;     // TMEM accumulators, one per kept level
 constexpr int kNT = 32;      // data columns per tensor-core tile (one digit slice of the MMA N)
 constexpr int kKC = 16;      // contraction depth per pipeline chunk (one MMA K step)
 constexpr int kShift = 8 * kSlices;  // X = rint(x 2^(kShift - E))
-constexpr int kMaxKp = 128;  // degrees per order (l_max <= 127)
+constexpr int kMaxL = 159;   // l_max <= 159: a synthesis tile (K <= 160) is one exact segment
 
 struct SplitTables {
   int L = 0, nlat = 0, nh = 0, NK = 0, Mt = 1;
   __nv_bfloat16* psyn = nullptr;  // synthesis basis digits
   __nv_bfloat16* pana = nullptr;  // analysis basis digits
   int* esyn = nullptr;            // [m][Mt*128] latitude-row exponents
-  int* eana = nullptr;            // [m][128] degree-row exponents
+  int* eana = nullptr;            // [row tile][128] degree-row exponents
   long long* kcum = nullptr;      // [L+2] prefix sums of padded degree counts
   int* err = nullptr;             // sticky device error flag (bounded waits)
   std::vector<long long> h_kcum;
@@ -187,8 +190,16 @@ __host__ __device__ constexpr long long chunk_elems(int rows) { return (long lon
 __host__ __device__ inline long long psyn_tile(const long long* kcum, int Mt, int m, int mt, int Kp) {
   return kcum[m] * (long long)Mt * kSlices * 128 + (long long)mt * kSlices * 128 * Kp;
 }
-// Analysis basis, tile m: NK/16 chunks of 128 degree rows.
-__host__ __device__ inline long long pana_tile(int NK, int m) { return (long long)m * kSlices * 128 * NK; }
+// Analysis basis, row tile rt: NK/16 chunks of 128 degree rows.  Orders
+// with more than 128 degrees (m < L - 127) take a second row tile: row
+// tiles 0..L are (m = rt, degrees m..m+127), row tiles L+1.. are
+// (m = rt - L - 1, degrees m+128..L).
+__host__ __device__ inline long long pana_tile(int NK, int rt) { return (long long)rt * kSlices * 128 * NK; }
+__host__ __device__ inline int ana_row_tiles(int L) { return L + 1 + (L > 127 ? L - 127 : 0); }
+__host__ __device__ inline void ana_row_tile(int L, int rt, int& m, int& mt) {
+  m = rt <= L ? rt : rt - L - 1;
+  mt = rt <= L ? 0 : 1;
+}
 // Synthesis data, tile (m, ntile): Kp/16 chunks of kNT rows.
 __host__ __device__ inline long long dsyn_tile(const long long* kcum, const SplitDims& d, int m, int ntile) {
   const int Kp = kpad(d.L + 1 - m);
@@ -449,6 +460,21 @@ __device__ inline void tc_read(uint32_t tbuf, int q, int c0, float (*acc)[kAccs]
 template <class Epi>
 constexpr int tc_threads() { return 64 + 32 * Epi::kWarps; }
 
+// Epilogues with a Pre type load their per-tile inputs that do not depend on
+// the accumulators (prefetch) before waiting for them, so those global
+// loads are off the path from "accumulators ready" to "buffer released".
+template <class E, class = void>
+struct EpiHasPre : std::false_type {};
+template <class E>
+struct EpiHasPre<E, std::void_t<typename E::Pre>> : std::true_type {};
+// K-segmented epilogues may load the same kind of inputs into their State
+// (seg_prefetch) before the first segment's wait.
+template <class E, class = void>
+struct EpiHasSegPrefetch : std::false_type {};
+template <class E>
+struct EpiHasSegPrefetch<E, std::void_t<decltype(std::declval<const E&>().seg_prefetch(
+                                std::declval<typename E::State&>(), 0, 0, 0))>> : std::true_type {};
+
 // Sched: int count() const; TcTile tile(int t) const; kSegChunks (0: one
 //        K segment per tile, else K segments of that many chunks).
 // Epi:   kWarps (4, 8 or 16 epilogue warps), kCols = 4 kNT / kWarps, and
@@ -589,6 +615,7 @@ __global__ void __launch_bounds__(tc_threads<Epi>(), 1) tc_persistent_kernel(Sch
         const int nseg = (sc.tile(t).nchunks + Sched::kSegChunks - 1) / Sched::kSegChunks;
         typename Epi::State es;
         ep.seg_begin(es);
+        if constexpr (EpiHasSegPrefetch<Epi>::value) ep.seg_prefetch(es, t, q * 32 + lane, c0);
         for (int sg = 0; sg < nseg; ++sg, ++i) {
           if (!(ok = wait_full(i))) break;
           tc::fence_after_sync();
@@ -597,12 +624,19 @@ __global__ void __launch_bounds__(tc_threads<Epi>(), 1) tc_persistent_kernel(Sch
         }
         if (ok) ep.seg_end(t, es, q * 32 + lane, c0, etid);
       } else {
-        if (!(ok = wait_full(i))) break;
-        tc::fence_after_sync();
         // the epilogue hands the buffer back as soon as its accumulators are
         // in registers, so the next tile's MMAs overlap its math and stores
         const int unit = i;
-        ep.run(t, tmem + (uint32_t)((i & 1) * kTmemBuf), q, q * 32 + lane, c0, etid, [&] { release(unit); });
+        if constexpr (EpiHasPre<Epi>::value) {
+          const typename Epi::Pre pre = ep.prefetch(t, q * 32 + lane, c0);
+          if (!(ok = wait_full(i))) break;
+          tc::fence_after_sync();
+          ep.run(t, tmem + (uint32_t)((i & 1) * kTmemBuf), q, q * 32 + lane, c0, etid, [&] { release(unit); }, pre);
+        } else {
+          if (!(ok = wait_full(i))) break;
+          tc::fence_after_sync();
+          ep.run(t, tmem + (uint32_t)((i & 1) * kTmemBuf), q, q * 32 + lane, c0, etid, [&] { release(unit); });
+        }
         ++i;
       }
     }
@@ -619,7 +653,7 @@ __global__ void __launch_bounds__(tc_threads<Epi>(), 1) tc_persistent_kernel(Sch
 // Tiles (m, latitude tile, data tile), m-major so tiles of equal depth are
 // adjacent (largest depth first: a greedy balance of the static schedule).
 struct SynthSched {
-  static constexpr int kSegChunks = 0;  // K <= 128: one exact segment per tile
+  static constexpr int kSegChunks = 0;  // K <= 160: one exact segment per tile
   SplitDims dm;
   const long long* kcum;
   const __nv_bfloat16* psyn;
@@ -635,9 +669,38 @@ struct SynthSched {
   }
 };
 
-// Writes the F blocks as double-floats (float4 = re.hi, re.lo, im.hi, im.lo per
-// complex value); NF fields.
+// Spectra blocks written by the synthesis epilogue for a Derive's NF
+// contracted fields: by default field f -> block f.  A Derive may declare
+// NBLK blocks, blk(f) and lam_blk(f) >= 0 for fields whose order spectra
+// times i m / R (a longitude derivative, diagonal in m) fill a further block.
+// Identity placement of NF fields.
 template <int NF>
+struct SynthOutPlain {
+  static constexpr int NBLK = NF;
+  static constexpr bool kLam = false;
+  __host__ __device__ static constexpr int blk(int f) { return f; }
+  __host__ __device__ static constexpr int lam_blk(int) { return -1; }
+};
+template <class Derive, class = void>
+struct SynthOut {
+  static constexpr int NBLK = Derive::NF;
+  static constexpr bool kLam = false;
+  __host__ __device__ static constexpr int blk(int f) { return f; }
+  __host__ __device__ static constexpr int lam_blk(int) { return -1; }
+  static double ir(const Derive&) { return 0.0; }
+};
+template <class Derive>
+struct SynthOut<Derive, std::void_t<decltype(Derive::NBLK)>> {
+  static constexpr int NBLK = Derive::NBLK;
+  static constexpr bool kLam = true;
+  __host__ __device__ static constexpr int blk(int f) { return Derive::blk(f); }
+  __host__ __device__ static constexpr int lam_blk(int f) { return Derive::lam_blk(f); }
+  static double ir(const Derive& d) { return d.lam_ir(); }
+};
+
+// Writes the F blocks as double-floats (float4 = re.hi, re.lo, im.hi, im.lo per
+// complex value); NF contracted fields, placed by Out (SynthOut).
+template <int NF, class Out = SynthOutPlain<NF>>
 struct SynthEpi {
   static constexpr int kWarps = 16, kCols = 4 * kNT / kWarps;
   SplitDims dm;
@@ -645,32 +708,65 @@ struct SynthEpi {
   const int* ecol;
   int nblk;
   float4* F;
-  template <class Rel>
-  __device__ void run(int t, uint32_t tbuf, int q, int row, int c0, int, Rel release) const {
+  float ir_hi = 0.f, ir_lo = 0.f;  // 1 / R as a double-float (Out::kLam)
+  struct Pre {
+    int e[kCols];  // result exponents of this thread's outputs
+  };
+  __device__ Pre prefetch(int t, int row, int c0) const {
     const int per_m = dm.Mt * dm.ntiles;
     const int m = t / per_m, r = t - m * per_m;
     const int mt = r / dm.ntiles, tile = r - mt * dm.ntiles;
-    const int L = dm.L;
     const int j = mt * 128 + row;
     const int Ej = j < dm.nlat ? esyn[m * dm.Mt * 128 + j] : 0;
     const int* ec = ecol + (long long)m * dm.ntiles * kNT + tile * kNT + c0;
-    int e[kCols];
+    Pre p;
 #pragma unroll
-    for (int i = 0; i < kCols; ++i) e[i] = Ej + __ldg(ec + i) - kOut;
+    for (int i = 0; i < kCols; ++i) p.e[i] = Ej + __ldg(ec + i) - kOut;
+    return p;
+  }
+  template <class Rel>
+  __device__ void run(int t, uint32_t tbuf, int q, int row, int c0, int, Rel release, const Pre& pre) const {
+    const int per_m = dm.Mt * dm.ntiles;
+    const int m = t / per_m, r = t - m * per_m;
+    const int mt = r / dm.ntiles, tile = r - mt * dm.ntiles;
+    const int j = mt * 128 + row;
     float acc[kCols][kAccs];
     tc_read<kCols>(tbuf, q, c0, acc);
     release();
-    if (j < dm.nlat) {
+    if (j >= dm.nlat) return;
+    // every recombination first (independent dependency chains that the
+    // compiler interleaves), then the stores
+    df v[kCols];
 #pragma unroll
-      for (int i = 0; i < kCols; i += 2) {
-        const int n = tile * kNT + c0 + i;  // even: real part, n + 1: imaginary part
-        if (n < dm.ncol) {
-          const df re = levels_to_df(acc[i], e[i]);
-          const df im = levels_to_df(acc[i + 1], e[i + 1]);
-          const int bf = n >> 1;
-          const int b = bf / NF, f = bf - b * NF;
-          F[fg_index(b, m, f, j, L, nblk, dm.nlat)] = make_float4(re.hi, re.lo, im.hi, im.lo);
+    for (int i = 0; i < kCols; ++i) v[i] = levels_to_df(acc[i], pre.e[i]);
+    // F block of (member b, order m, row j): fg_index, with b advanced per column pair
+    const long sb = (long)(dm.L + 1) * dm.nlat * nblk;
+    float4* Fj = F + ((long)m * dm.nlat + j) * nblk;
+    const int k0 = (tile * kNT + c0) >> 1;  // first complex column (member, field) of this thread
+    int b = k0 / NF, f = k0 - b * NF;
+    df mr = df{0.f, 0.f};
+    if constexpr (Out::kLam) {  // m / R on the f32 pipe (m exact as a float; no FP64 instruction)
+      const float mf = __int_as_float(0x4B000000 | m) - 8388608.0f;
+      const float ph = mf * ir_hi;
+      mr = df{ph, fmaf(mf, ir_hi, -ph) + mf * ir_lo};
+    }
+#pragma unroll
+    for (int i = 0; i < kCols; i += 2) {
+      if (tile * kNT + c0 + i < dm.ncol) {  // even: real part, odd: imaginary part
+        float4* Fb = Fj + (long)b * sb;
+        Fb[Out::blk(f)] = make_float4(v[i].hi, v[i].lo, v[i + 1].hi, v[i + 1].lo);
+        if constexpr (Out::kLam) {
+          // the columns of a warp are one field for all its lanes: no divergence
+          const int lb = Out::lam_blk(f);
+          if (lb >= 0) {
+            const df lre = df_neg(df_mul(v[i + 1], mr)), lim = df_mul(v[i], mr);
+            Fb[lb] = make_float4(lre.hi, lre.lo, lim.hi, lim.lo);
+          }
         }
+      }
+      if (++f == NF) {
+        f = 0;
+        ++b;
       }
     }
   }
@@ -682,11 +778,13 @@ struct AnalSched {
   SplitDims dm;
   const __nv_bfloat16* pana;
   const __nv_bfloat16* dana;
-  __host__ __device__ int count() const { return (dm.L + 1) * dm.ntiles; }
+  __host__ __device__ int count() const { return ana_row_tiles(dm.L) * dm.ntiles; }
   int count_host() const { return count(); }
   __device__ TcTile tile(int t) const {
-    const int m = t / dm.ntiles, nt = t - m * dm.ntiles;
-    return TcTile{pana + pana_tile(dm.NK, m), dana + dana_tile(dm, m, nt), dm.NK / kKC};
+    const int rt = t / dm.ntiles, nt = t - rt * dm.ntiles;
+    int m, mt;
+    ana_row_tile(dm.L, rt, m, mt);
+    return TcTile{pana + pana_tile(dm.NK, rt), dana + dana_tile(dm, m, nt), dm.NK / kKC};
   }
 };
 
@@ -698,6 +796,7 @@ struct AnalEpi {
   static constexpr int kWarps = 16, kCols = 4 * kNT / kWarps;  // FP64 epilogue: 8 columns per warp
   struct State {
     long long T[kCols];
+    int e[kCols];  // result exponents of this thread's outputs (loaded before the first wait)
   };
   SplitDims dm;
   const int* eana;
@@ -708,6 +807,15 @@ struct AnalEpi {
 #pragma unroll
     for (int i = 0; i < kCols; ++i) st.T[i] = 0;
   }
+  __device__ void seg_prefetch(State& st, int tt, int row, int c0) const {
+    const int rt = tt / dm.ntiles, tile = tt - rt * dm.ntiles;
+    int m, mt;
+    ana_row_tile(dm.L, rt, m, mt);
+    const int Et = eana[rt * 128 + row];
+    const int* ec = ecol + (long long)m * dm.ntiles * kNT + tile * kNT + c0;
+#pragma unroll
+    for (int i = 0; i < kCols; ++i) st.e[i] = Et + __ldg(ec + i) - kOut;
+  }
   __device__ void seg_add(State& st, uint32_t tbuf, int q, int c0) const {
     float acc[kCols][kAccs];
     tc_read<kCols>(tbuf, q, c0, acc);
@@ -717,11 +825,11 @@ struct AnalEpi {
   __device__ void seg_end(int tt, const State& st, int row, int c0, int etid) const {
     constexpr int NF = Epi::NF;
     constexpr bool kWhole = kCols % (2 * NF) == 0;
-    const int m = tt / dm.ntiles, tile = tt - m * dm.ntiles;
+    const int rt = tt / dm.ntiles, tile = tt - rt * dm.ntiles;
+    int m, mt;
+    ana_row_tile(dm.L, rt, m, mt);
     const int K = dm.L + 1 - m;
-    const int t = row;
-    const int Et = eana[m * 128 + t];
-    const int* ec = ecol + (long long)m * dm.ntiles * kNT + tile * kNT;
+    const int t = mt * 128 + row;  // degree offset l - m
     if (t < K) {
       if constexpr (kWhole) {
 #pragma unroll
@@ -732,8 +840,8 @@ struct AnalEpi {
           double2 a[NF];
 #pragma unroll
           for (int f = 0; f < NF; ++f) {
-            a[f].x = scaled_to_double(st.T[i + 2 * f], Et + ec[c0 + i + 2 * f] - kOut);
-            a[f].y = scaled_to_double(st.T[i + 2 * f + 1], Et + ec[c0 + i + 2 * f + 1] - kOut);
+            a[f].x = scaled_to_double(st.T[i + 2 * f], st.e[i + 2 * f]);
+            a[f].y = scaled_to_double(st.T[i + 2 * f + 1], st.e[i + 2 * f + 1]);
           }
           epi.finish(b, m + t, m, a);
         }
@@ -745,15 +853,17 @@ struct AnalEpi {
           const int b = bf / NF, f = bf - b * NF;
           if (b >= batch) break;
           double2 a;
-          a.x = scaled_to_double(st.T[i], Et + ec[c0 + i] - kOut);
-          a.y = scaled_to_double(st.T[i + 1], Et + ec[c0 + i + 1] - kOut);
+          a.x = scaled_to_double(st.T[i], st.e[i]);
+          a.y = scaled_to_double(st.T[i + 1], st.e[i + 1]);
           epi.finish_field(b, f, m + t, m, a);
         }
       }
     }
-    // slots l < m of column m for the members this tile touches
-    const int mb0 = tile * kNT / (2 * NF), mb1 = min(batch, ((tile + 1) * kNT + 2 * NF - 1) / (2 * NF));
-    for (int idx = etid; idx < (mb1 - mb0) * m; idx += 32 * kWarps) epi.zero(mb0 + idx / m, idx % m, m);
+    // slots l < m of column m for the members this tile touches (once per order)
+    if (mt == 0) {
+      const int mb0 = tile * kNT / (2 * NF), mb1 = min(batch, ((tile + 1) * kNT + 2 * NF - 1) / (2 * NF));
+      for (int idx = etid; idx < (mb1 - mb0) * m; idx += 32 * kWarps) epi.zero(mb0 + idx / m, idx % m, m);
+    }
   }
 };
 
@@ -837,12 +947,16 @@ int launch_split_synth(const aeolus_plan_impl* p, const Derive& d, double2* FG, 
     AE_LAUNCH("split_synth_slice_kernel");
   }
   const size_t sm2 = tc_smem_bytes();
-  auto k2 = tc_persistent_kernel<SynthSched, SynthEpi<NF>>;
+  using Out = SynthOut<Derive>;
+  using Epi = SynthEpi<NF, Out>;
+  auto k2 = tc_persistent_kernel<SynthSched, Epi>;
   if ((s = allow_smem(k2, sm2))) return s;
   const SynthSched sc{r.dm, p->split->kcum, p->split->psyn, r.digits};
-  const SynthEpi<NF> ep{r.dm, p->split->esyn, r.ecol, nblk, reinterpret_cast<float4*>(FG)};
+  Epi ep{r.dm, p->split->esyn, r.ecol, nblk, reinterpret_cast<float4*>(FG)};
+  ep.ir_hi = (float)Out::ir(d);
+  ep.ir_lo = (float)(Out::ir(d) - (double)ep.ir_hi);
   ProfScope prof("tc_synth_bf16x6", st);
-  k2<<<tc_grid(p, sc.count_host()), tc_threads<SynthEpi<NF>>(), sm2, st>>>(sc, ep, p->split->err);
+  k2<<<tc_grid(p, sc.count_host()), tc_threads<Epi>(), sm2, st>>>(sc, ep, p->split->err);
   AE_LAUNCH("tc_synth_kernel");
   return AEOLUS_OK;
 }

@@ -507,3 +507,16 @@ torch.library.register_autograd("aeolus::analyze_adjoint", _anal_adj_backward, s
 def f10(omega: float) -> float:
     """Spectral (1,0) coefficient of f = 2 Omega sin(lat), barotropic.py:59-61."""
     return 2.0 * omega * math.sqrt(4.0 * math.pi / 3.0)
+
+
+def rk4_stage(stage: int, dt: float, y0: torch.Tensor, k: torch.Tensor, ystage: torch.Tensor,
+              acc: torch.Tensor) -> None:
+    """In place: one RK4 stage update on the device (aeolus_rk4_stage), the
+    reference's rk4_step_array order of operations (run/engine.py:406-431);
+    complex128 CUDA tensors of one shape, contiguous."""
+    for name, t in (("y0", y0), ("k", k), ("ystage", ystage), ("acc", acc)):
+        _require_cuda(t, name)
+        if t.dtype != torch.complex128 or not t.is_contiguous() or t.shape != y0.shape:
+            raise ValueError(f"rk4_stage: {name} must be a contiguous complex128 tensor shaped like y0")
+    check(_lib.load().aeolus_rk4_stage(int(stage), float(dt), _ptr(y0), _ptr(k), _ptr(ystage), _ptr(acc),
+                                       y0.numel(), _stream(y0.device)))

@@ -236,6 +236,18 @@ class PrimitiveEquationsModel:
     def tendency_state(self, state: PrimitiveEquationsState) -> PrimitiveEquationsState:
         return PrimitiveEquationsState(self.tendency(state.coeffs))
 
+    def rk4(self, coeffs: torch.Tensor, dt: float, nsteps: int = 1, *, stage_validator=None) -> torch.Tensor:
+        """`nsteps` classical RK4 steps of the (..., 3K+1, L+1, L+1) stack, each
+        the reference's rk4_step_array (run/engine.py:406-431, as the PE runner
+        uses it, run/pe/runner.py:104) with its stage combinations fused on the
+        device (aeolus_rk4_stage): bitwise the generic engine's step."""
+        from .engine import rk4_step_device
+
+        y = torch.as_tensor(coeffs).to(torch.complex128).contiguous()
+        for _ in range(int(nsteps)):
+            y = rk4_step_device(self.tendency, y, 0.0, dt, stage_validator=stage_validator)
+        return y
+
     # -- state-grid reconstructions, characteristic speed, validation ------
     def wind_on_state_grid(self, state: PrimitiveEquationsState):
         """Per-level (u, v) on the state sampling, (nlev, n_points) each (:289-307)."""

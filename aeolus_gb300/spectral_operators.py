@@ -126,7 +126,15 @@ class SpectralOperators:
 
     def _extended_plan(self):
         """The product points and weights with the basis extended to degree
-        l_max + 1 (_vector_analysis_pieces, :474-492)."""
+        l_max + 1 (_vector_analysis_pieces, :474-492), in the product plan's
+        precision mode."""
+        plan = self._extended_plan_base()
+        want = self._product_space.sh.plan.precision
+        if plan.precision != want:
+            plan.set_precision(want)
+        return plan
+
+    def _extended_plan_base(self):
         if self._vector_plan is None:
             from .latlon_grid import GaussLatLonSphericalHarmonics
             sh_p = self._product_space.sh

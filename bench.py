@@ -683,8 +683,8 @@ def _rel_l2_fields(a, b):
 # of the first RK4 stage (cold L2).
 NCU_TRAFFIC = {
     "split_synth_slice": 27.497728e6 + 86.54464e6,
-    "tc_synth_bf16x6": 162.184192e6 + 171.406848e6,
-    "rows_fx_c2r_products_r2c": 226.575104e6 + 77.05216e6,
+    "tc_synth_bf16x6": 138.119424e6 + 174.368e6,
+    "rows_fx_c2r_products_r2c": 226.581248e6 + 75.634176e6,
     "split_anal_slice": 100.69504e6 + 95.401472e6,
     "tc_anal_bf16x6": 230.352896e6 + 67.960576e6,
 }
@@ -693,7 +693,7 @@ NCU_TRAFFIC = {
 # Warp instructions per launch of the same kernels (smsp__inst_executed.sum
 # of the same capture), for the instruction-issue roofline of the row stage.
 NCU_WARP_INSTRUCTIONS = {
-    "rows_fx_c2r_products_r2c": 344.3e6,
+    "rows_fx_c2r_products_r2c": 358.77e6,
 }
 SM_COUNT, ISSUE_PER_SM_CLK = 152, 4  # GB300: 4 schedulers per SM, one warp instruction each per clock
 
@@ -707,7 +707,9 @@ def _roofline(kstats, B, peaks):
     for name, (n, ms) in kstats.items():
         t = ms / n / 1000.0
         if name.startswith("tc_synth") or name.startswith("tc_anal"):
-            fields = 9 if name.startswith("tc_synth") else 4
+            # synthesis: the 7 contracted fields (the two longitude derivatives
+            # the model also needs are formed in its epilogue, not contracted)
+            fields = 7 if name.startswith("tc_synth") else 4
             useful = ftx * fields * B
             entries[name] = {"kernel": name, "bound": "tensor", "achieved": useful / t / 1e12, "peak": tensor,
                              "unit": "TFLOP/s", "frac": useful / t / 1e12 / tensor,

@@ -251,6 +251,19 @@ int aeolus_pe_spectral(int lmax, const aeolus_pe_params* params, int nlev, const
                        const double* state, const double* analysed, const double* curl_z, const double* div_z,
                        const double* phi_s, double* tendency, int batch, void* stream);
 
+/* One classical RK4 stage update of n complex values (y0, k, ystage, acc
+ * are [n] complex128 device arrays), the device form of the reference's
+ * rk4_step_array (run/engine.py:406-431) for any tendency (the primitive
+ * equations' fused RK4 uses it), in the reference's order of operations
+ * with every FP64 product and sum rounded separately:
+ *   stage 1: acc = k;         ystage = y0 + (dt/2) k
+ *   stage 2: acc = acc + 2 k; ystage = y0 + (dt/2) k
+ *   stage 3: acc = acc + 2 k; ystage = y0 + dt k
+ *   stage 4: ystage = y0 + (dt/6) (acc + k)   (the step's result)
+ * acc must not alias ystage or k; ystage may alias y0 at stage 4. */
+int aeolus_rk4_stage(int stage, double dt, const double* y0, const double* k, double* ystage, double* acc,
+                     long n, void* stream);
+
 /* ---- icosahedral geodesic point set (numerics/geodesic_grid.py) -------- */
 
 /* Point, face and workspace counts of a geodesic point set with

@@ -215,10 +215,38 @@ def test_pe_rk4_steps_match_oracle(golden):
         assert rel_l2(tri(a), tri(b)) < TOL
 
 
+def test_pe_fused_rk4_is_bitwise_the_generic_engine(golden):
+    """model.rk4 (stage combinations fused on the device, aeolus_rk4_stage)
+    gives bit for bit the generic engine's rk4_step_array steps (the
+    reference's order of operations), with the same stage validations."""
+    from aeolus_gb300.engine import rk4_step_array
+    name = "pe_gauss16x32_L15_fine23x46_K5"
+    g = golden(name)
+    m = _model(g, *CASES[name])
+    calls = {"a": 0, "b": 0}
+
+    def va(y):
+        calls["a"] += 1
+        m.validate_state(PrimitiveEquationsState(y), context="in an RK4 stage")
+
+    def vb(y):
+        calls["b"] += 1
+        m.validate_state(PrimitiveEquationsState(y), context="in an RK4 stage")
+
+    y = T(g["state"])
+    ya = y
+    for _ in range(3):
+        ya = rk4_step_array(m.tendency, ya, 0.0, 300.0, stage_validator=va)
+    yb = m.rk4(y, 300.0, 3, stage_validator=vb)
+    assert calls["a"] == calls["b"] == 9
+    assert torch.equal(ya, yb)
+
+
 def test_pe_split_precision_matches_fp64():
-    """The product plan's Legendre contractions on the bf16-digit tensor-core
-    path (the degree-(L+1) vector analysis stays FP64): every prognostic
-    within 1e-10 of the FP64 tendency at 192x384 / l_max 127, 6 levels."""
+    """The Legendre contractions on the bf16-digit tensor-core path, the
+    degree-(L+1) weak-form vector analysis included (its plan follows the
+    product plan's mode): every prognostic within 1e-10 of the FP64 tendency
+    at 192x384 / l_max 127, 6 levels."""
     from aeolus_gb300 import _lib
     L, K = 127, 6
     planet = ae.make_planet("latlon", nlat=192, nlon=384, l_max=L)

@@ -37,8 +37,10 @@ def device_error(plan):
 
 
 @pytest.mark.parametrize("nlat,nlon,L", [(32, 64, 21), (17, 40, 12), (128, 256, 85), (160, 320, 106),
-                                         (192, 384, 127)])
+                                         (192, 384, 127), (192, 384, 128), (160, 320, 140)])
 def test_split_transforms_match_fp64(nlat, nlon, L):
+    """Transforms within 1e-12; l_max 128 (the degree-(L+1) extended plan of
+    l_max 127) and 140 give the low orders a second 128-degree analysis tile."""
     rng = np.random.default_rng(L)
     p64 = Plan.gauss(nlat, nlon, L)
     ps = Plan.gauss(nlat, nlon, L)

@@ -100,3 +100,22 @@ def test_roundtrip_curl_div_matches_reference(golden):
     curl, div = planet.so.vector_curl_div_roundtrip(g["f_east"], g["f_north"])
     assert rel_l2(tri(curl.cpu().numpy()), tri(g["rt_curl"])) < 1e-12
     assert rel_l2(tri(div.cpu().numpy()), tri(g["rt_div"])) < 1e-12
+
+
+def test_vector_curl_div_split_extended_plan_matches_fp64():
+    """The weak-form curl/div on the degree-128 extended plan of the 192x384 /
+    l_max 127 grid in split precision (order 0, with 129 degrees, takes a
+    second degree tile in the tensor-core analysis) against the FP64 plan, within 1e-12 of
+    the FP64 result (truncated and full)."""
+    R, L = 6.371e6, 127
+    p64 = Plan.gauss(192, 384, L + 1, R)
+    ps = Plan.gauss(192, 384, L + 1, R)
+    ps.set_precision(_lib.PREC_SPLIT_BF16)
+    rng = np.random.default_rng(9)
+    fe = T(rng.standard_normal((4, p64.n_points)))
+    fn = T(rng.standard_normal((4, p64.n_points)))
+    for trunc in (True, False):
+        a = N(vector_curl_div(p64.id, R, fe, fn, trunc))
+        b = N(vector_curl_div(ps.id, R, fe, fn, trunc))
+        for k in range(2):
+            assert rel_l2(b[k], a[k]) < 1e-12, (trunc, k, rel_l2(b[k], a[k]))
