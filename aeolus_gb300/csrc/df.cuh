@@ -68,6 +68,78 @@ __device__ __forceinline__ df df_mul(df a, df b) {
 // Multiplication by a power of two (exact).
 __device__ __forceinline__ df df_scale2(df a, float p2) { return df{a.hi * p2, a.lo * p2}; }
 
+// ---------------------------------------------------------------------
+// Two double-floats side by side.  An f2 word holds two f32 lanes, and
+// Blackwell's packed two-lane FP32 instructions (add/sub/mul/fma .f32x2)
+// operate on both with one instruction, each lane rounded exactly as its
+// scalar form: df2 arithmetic below is the df arithmetic above in the same
+// order of operations, two values at a time, in half the instructions.
+typedef unsigned long long f2;
+
+__device__ __forceinline__ f2 f2_pack(float a, float b) {
+  f2 r;
+  asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(a), "f"(b));
+  return r;
+}
+__device__ __forceinline__ void f2_unpack(f2 r, float& a, float& b) {
+  asm("mov.b64 {%0, %1}, %2;" : "=f"(a), "=f"(b) : "l"(r));
+}
+__device__ __forceinline__ f2 f2_add(f2 a, f2 b) {
+  f2 d;
+  asm("add.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+  return d;
+}
+__device__ __forceinline__ f2 f2_sub(f2 a, f2 b) {
+  f2 d;
+  asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+  return d;
+}
+__device__ __forceinline__ f2 f2_mul(f2 a, f2 b) {
+  f2 d;
+  asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+  return d;
+}
+__device__ __forceinline__ f2 f2_fma(f2 a, f2 b, f2 c) {
+  f2 d;
+  asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c));
+  return d;
+}
+__device__ __forceinline__ f2 f2_neg(f2 a) { return a ^ 0x8000000080000000ull; }
+__device__ __forceinline__ f2 f2_splat(float a) { return f2_pack(a, a); }
+
+struct df2 {
+  f2 hi, lo;
+};
+
+__device__ __forceinline__ df2 df2_pack(df a, df b) { return df2{f2_pack(a.hi, b.hi), f2_pack(a.lo, b.lo)}; }
+__device__ __forceinline__ void df2_unpack(df2 v, df& a, df& b) {
+  f2_unpack(v.hi, a.hi, b.hi);
+  f2_unpack(v.lo, a.lo, b.lo);
+}
+__device__ __forceinline__ df2 two_sum2(f2 a, f2 b) {
+  const f2 s = f2_add(a, b);
+  const f2 bb = f2_sub(s, a);
+  return df2{s, f2_add(f2_sub(a, f2_sub(s, bb)), f2_sub(b, bb))};
+}
+__device__ __forceinline__ df2 fast_two_sum2(f2 a, f2 b) {
+  const f2 s = f2_add(a, b);
+  return df2{s, f2_sub(b, f2_sub(s, a))};
+}
+__device__ __forceinline__ df2 df2_add_fast(df2 a, df2 b) {
+  df2 s = two_sum2(a.hi, b.hi);
+  s.lo = f2_add(s.lo, f2_add(a.lo, b.lo));
+  return fast_two_sum2(s.hi, s.lo);
+}
+__device__ __forceinline__ df2 df2_neg(df2 a) { return df2{f2_neg(a.hi), f2_neg(a.lo)}; }
+__device__ __forceinline__ df2 df2_mul(df2 a, df2 b) {
+  const f2 p = f2_mul(a.hi, b.hi);
+  f2 e = f2_fma(a.hi, b.hi, f2_neg(p));
+  e = f2_fma(a.hi, b.lo, e);
+  e = f2_fma(a.lo, b.hi, e);
+  return fast_two_sum2(p, e);
+}
+__device__ __forceinline__ df2 df2_scale2(df2 a, f2 p2) { return df2{f2_mul(a.hi, p2), f2_mul(a.lo, p2)}; }
+
 // From / to double (f64 conversions: used only at stage boundaries).
 __device__ __forceinline__ df df_from_double(double x) {
   const float h = __double2float_rn(x);

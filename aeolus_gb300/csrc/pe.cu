@@ -131,22 +131,15 @@ __global__ void pe_derive_kernel(Spec s, int K, int batch, double f10, const dou
   O[((long)kPeLevelFields * K + 1) * n2] = snt_r(lo ? val(q, l - 1) : zero, hi ? val(q, l + 1) : zero);
 }
 
-// One thread per (member, product point): the column, in two passes over
-// the levels and no per-level arrays (thread-local arrays spilled through L1
-// to L2/DRAM; shared-memory columns capped the occupancy).  Pass 1 forms the
-// thickness-weighted G = delta + V.grad(ln p_s) sums; pass 2 re-reads the
-// level fields (L2-resident after pass 1), repeats the same running sum for
-// the interface sigma_dot and keeps a three-level window of u, v, T in
-// registers for the vertical advection -- the same expressions in the same
-// order as a single pass with arrays, so the results are the same.
-constexpr int kPeColThreads = 128;
-
-__global__ void __launch_bounds__(kPeColThreads) pe_columns_kernel(PeSigma sg, long np, int nlon,
-                                                                   const double* __restrict__ coslat, int batch,
-                                                                   double r_dry, double kappa,
-                                                                   const double* __restrict__ grid,
-                                                                   double* __restrict__ prod,
-                                                                   double* __restrict__ fen) {
+// One thread per (member, product point): the column in thread-local
+// arrays.  The kernel is FP64-bound (84 % FP64-pipe active at 192x384,
+// 20 levels); the arrays spill through L1 to L2, which doubles its DRAM
+// traffic but not its time: a shared-memory column (occupancy-capped) and a
+// two-pass form without arrays (recomputing the FP64 terms) both ran slower.
+__global__ void __launch_bounds__(128) pe_columns_kernel(PeSigma sg, long np, int nlon, const double* __restrict__ coslat,
+                                                         int batch, double r_dry, double kappa,
+                                                         const double* __restrict__ grid, double* __restrict__ prod,
+                                                         double* __restrict__ fen) {
   const long idx = (long)blockIdx.x * blockDim.x + threadIdx.x;
   if (idx >= np * batch) return;
   const int K = sg.K;
@@ -156,77 +149,57 @@ __global__ void __launch_bounds__(kPeColThreads) pe_columns_kernel(PeSigma sg, l
   const double* Gd = grid + (long)b * (kPeLevelFields * K + 2) * np + p;
   double* P = prod + (long)b * (kPeOutFields * K + 1) * np + p;
   const double lp_lam = Gd[(long)kPeLevelFields * K * np], lp_snt = Gd[((long)kPeLevelFields * K + 1) * np];
-  auto lev = [&](int k) { return Gd + (long)kPeLevelFields * k * np; };
-  // pass 1: the cumulative thickness-weighted G
-  double acc = 0.0;
+  double u[kPeMaxLevels], v[kPeMaxLevels], T[kPeMaxLevels], G[kPeMaxLevels], A[kPeMaxLevels];
+  double part[kPeMaxLevels], sd[kPeMaxLevels + 1];
+  double acc = 0.0, total = 0.0;
   for (int k = 0; k < K; ++k) {
-    const double* f = lev(k);
-    const double uk = f[0] * ic, vk = f[np] * ic;
-    const double A = (uk * lp_lam - vk * lp_snt) * ic;  // V . grad(ln p_s)
-    const double G = f[3 * np] + A;                     // delta + A
-    const double w = sg.dsig[k] * G;
-    acc = k == 0 ? w : acc + w;
+    const double* f = Gd + (long)kPeLevelFields * k * np;
+    u[k] = f[0] * ic;
+    v[k] = f[np] * ic;
+    T[k] = f[4 * np];
+    A[k] = (u[k] * lp_lam - v[k] * lp_snt) * ic;      // V . grad(ln p_s)
+    G[k] = f[3 * np] + A[k];                          // delta + A
+    const double w = sg.dsig[k] * G[k];
+    acc = k == 0 ? w : acc + w;                       // cumulative thickness-weighted G
+    part[k] = acc;
   }
-  const double total = acc;
-  P[(long)kPeOutFields * K * np] = -total;              // d ln p_s / dt
-  const double gu = lp_lam * ic, gv = -lp_snt * ic;     // grad(ln p_s)
-  // vertical advection of X at level k from the window (X[k-1], X[k], X[k+1])
-  // with the interface sigma_dot above (sd_k) and below (sd_k1) level k
-  auto vadv = [&](double xm, double x0, double xp, int k, double sd_k, double sd_k1) {
+  total = part[K - 1];
+  // interface sigma_dot: exact zeros at the top and (total - total) at the surface
+  sd[0] = 0.0;
+  for (int k = 1; k < K; ++k) sd[k] = sg.s[k] * total - part[k - 1];
+  sd[K] = total - total;
+  P[(long)kPeOutFields * K * np] = -total;            // d ln p_s / dt
+  const double gu = lp_lam * ic, gv = -lp_snt * ic;   // grad(ln p_s)
+  auto vadv = [&](const double* X, int k) {
     double a = 0.0;
     bool any = false;
     if (k < K - 1) {
-      a = sd_k1 * (xp - x0);
+      a = sd[k + 1] * (X[k + 1] - X[k]);
       any = true;
     }
     if (k > 0) {
-      const double up = sd_k * (x0 - xm);
+      const double up = sd[k] * (X[k] - X[k - 1]);
       a = any ? a + up : up;
       any = true;
     }
     return any ? a * sg.h2[k] : 0.0;
   };
-  // pass 2
-  double um = 0.0, vm = 0.0, Tm = 0.0;  // level k-1
-  double u0 = lev(0)[0] * ic, v0 = lev(0)[np] * ic, T0 = lev(0)[4 * np];
-  double run = 0.0, part_prev = 0.0;    // running sum through level k (part[k]) and k-1
   for (int k = 0; k < K; ++k) {
-    const double* f = lev(k);
-    double up = 0.0, vp = 0.0, Tp = 0.0;  // level k+1
-    if (k + 1 < K) {
-      const double* g = lev(k + 1);
-      up = g[0] * ic;
-      vp = g[np] * ic;
-      Tp = g[4 * np];
-    }
-    const double dk = f[3 * np];
-    const double A = (u0 * lp_lam - v0 * lp_snt) * ic;
-    const double G = dk + A;
-    const double w = sg.dsig[k] * G;
-    run = k == 0 ? w : run + w;
-    // interface sigma_dot: exact zeros at the top and (total - total) at the surface
-    const double sd_k = k == 0 ? 0.0 : sg.s[k] * total - part_prev;
-    const double sd_k1 = k + 1 == K ? total - total : sg.s[k + 1] * total - run;
-    const double wp = k == 0 ? A - sg.alpha[0] * G : A - sg.bd[k] * part_prev - sg.alpha[k] * G;
+    const double* f = Gd + (long)kPeLevelFields * k * np;
+    const double wp = k == 0 ? A[0] - sg.alpha[0] * G[0]
+                             : A[k] - sg.bd[k] * part[k - 1] - sg.alpha[k] * G[k];
     const double t_lam = f[5 * np], t_snt = f[6 * np];
     const double e_lam = f[7 * np], e_snt = f[8 * np], eta = f[9 * np];
-    const double adv_t = (u0 * t_lam - v0 * t_snt) * ic;
+    const double adv_t = (u[k] * t_lam - v[k] * t_snt) * ic;
     double* o = P + (long)kPeOutFields * k * np;
-    o[0] = -adv_t - vadv(Tm, T0, Tp, k, sd_k, sd_k1) + kappa * T0 * wp;
-    o[np] = -((u0 * e_lam - v0 * e_snt) * ic + eta * dk);
-    o[2 * np] = eta * f[2 * np] + (v0 * e_lam + u0 * e_snt) * ic;
-    o[3 * np] = 0.5 * (u0 * u0 + v0 * v0);
-    const double rt = r_dry * T0;
+    o[0] = -adv_t - vadv(T, k) + kappa * T[k] * wp;
+    o[np] = -((u[k] * e_lam - v[k] * e_snt) * ic + eta * f[3 * np]);
+    o[2 * np] = eta * f[2 * np] + (v[k] * e_lam + u[k] * e_snt) * ic;
+    o[3 * np] = 0.5 * (u[k] * u[k] + v[k] * v[k]);
+    const double rt = r_dry * T[k];
     double* z = fen + ((long)b * K + k) * 2 * np + p;
-    z[0] = vadv(um, u0, up, k, sd_k, sd_k1) + rt * gu;
-    z[np] = vadv(vm, v0, vp, k, sd_k, sd_k1) + rt * gv;
-    part_prev = run;
-    um = u0;
-    vm = v0;
-    Tm = T0;
-    u0 = up;
-    v0 = vp;
-    T0 = Tp;
+    z[0] = vadv(u, k) + rt * gu;
+    z[np] = vadv(v, k) + rt * gv;
   }
 }
 
@@ -345,7 +318,7 @@ extern "C" int aeolus_pe_columns(aeolus_plan plan, const aeolus_pe_params* prm, 
   const long np = plan->npoints;
   const int nlon = plan->kind == kGauss ? plan->nlon : 0;
   ProfScope prof("pe_columns", static_cast<cudaStream_t>(stream));
-  pe_columns_kernel<<<blocks_for(np * batch, kPeColThreads), kPeColThreads, 0, static_cast<cudaStream_t>(stream)>>>(
+  pe_columns_kernel<<<blocks_for(np * batch, 128), 128, 0, static_cast<cudaStream_t>(stream)>>>(
       sg, np, nlon, plan->coslat, batch, prm->r_dry, prm->r_dry / prm->cp_dry, grid, prod, f_en);
   AE_LAUNCH("pe_columns_kernel");
   return AEOLUS_OK;

@@ -158,6 +158,21 @@ __device__ inline df levels_to_df(const float* acc, int e) {
   return df{s.hi * pow2f(e1) * pow2f(e2), s.lo * pow2f(e1) * pow2f(e2)};
 }
 
+// levels_to_df of two outputs at once (packed two-lane FP32; the same
+// operations, so the same results).
+__device__ inline void levels_to_df2(const float* a, const float* b, int ea, int eb, df& ra, df& rb) {
+  const f2 c40 = f2_splat(pow2f(40)), c32 = f2_splat(pow2f(32)), c24 = f2_splat(pow2f(24));
+  const f2 c16 = f2_splat(pow2f(16)), c8 = f2_splat(pow2f(8));
+  const df2 p0 = two_sum2(f2_mul(f2_pack(a[0], b[0]), c40), f2_mul(f2_pack(a[1], b[1]), c32));
+  const df2 p1 = two_sum2(f2_mul(f2_pack(a[2], b[2]), c24), f2_mul(f2_pack(a[3], b[3]), c16));
+  const df2 p2 = two_sum2(f2_mul(f2_pack(a[4], b[4]), c8), f2_pack(a[5], b[5]));
+  const df2 s = df2_add_fast(df2_add_fast(p0, p1), p2);
+  const int ea1 = max(-126, min(127, ea)), ea2 = max(-126, min(127, ea - ea1));
+  const int eb1 = max(-126, min(127, eb)), eb2 = max(-126, min(127, eb - eb1));
+  const f2 s1 = f2_pack(pow2f(ea1), pow2f(eb1)), s2 = f2_pack(pow2f(ea2), pow2f(eb2));
+  df2_unpack(df2{f2_mul(f2_mul(s.hi, s1), s2), f2_mul(f2_mul(s.lo, s1), s2)}, ra, rb);
+}
+
 // Level recombination: T = sum_k I_k 256^(5-k), k = 0..5 <-> s+t = 2..7.
 // One K segment (<= 160 deep): |I_0| < 160 * 2^14, so |T| < 2^62.
 __device__ inline long long combine_levels(const float* acc) {
@@ -738,7 +753,7 @@ struct SynthEpi {
     // compiler interleaves), then the stores
     df v[kCols];
 #pragma unroll
-    for (int i = 0; i < kCols; ++i) v[i] = levels_to_df(acc[i], pre.e[i]);
+    for (int i = 0; i < kCols; i += 2) levels_to_df2(acc[i], acc[i + 1], pre.e[i], pre.e[i + 1], v[i], v[i + 1]);
     // F block of (member b, order m, row j): fg_index, with b advanced per column pair
     const long sb = (long)(dm.L + 1) * dm.nlat * nblk;
     float4* Fj = F + ((long)m * dm.nlat + j) * nblk;

@@ -139,7 +139,8 @@ int aeolus_plan_info(aeolus_plan plan, int* kind, int* nlat, int* nlon,
 int aeolus_plan_nodes(aeolus_plan plan, double* lat, double* w_gl);
 
 /* Contraction precision for later calls on this plan (slices: number of
- * bf16 slices per FP64 operand, 0 = default). */
+ * bf16 slices per FP64 operand, 0 = default).  AEOLUS_PREC_SPLIT_BF16 on a
+ * Gauss plan needs l_max <= 159 and nlat <= 192 (exact f32 digit sums). */
 int aeolus_plan_set_precision(aeolus_plan plan, int precision, int slices);
 
 /* Sticky device error flag of the plan's tensor-core kernels: nonzero when a
