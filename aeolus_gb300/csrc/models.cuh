@@ -334,6 +334,34 @@ struct SwePw {
     if (!(phi0f + phi.hi > 0.0f)) bits |= AEOLUS_STATE_THICKNESS;
     return bits;
   }
+  // df_op of two grid points on the packed two-lane f32 pipe (the same
+  // operations in the same order, lane by lane).
+  __device__ unsigned df_op2(const RowDf& r, const df2* in, df2* out) const {
+    const df2 invc = df2_pack(r.invc, r.invc), fj = df2_pack(r.fj, r.fj);
+    const df2 u = df2_mul(in[0], invc), v = df2_mul(in[1], invc);
+    const df2 eta_lam = in[2], eta_snt = in[3], phi_lam = in[4], phi_snt = in[5];
+    const df2 zeta = in[6], delta = in[7], phi = in[8];
+    const df2 eta = df2_add_fast(zeta, fj);
+    out[0] = df2_neg(df2_add_fast(df2_mul(df2_add_fast(df2_mul(u, eta_lam), df2_neg(df2_mul(v, eta_snt))), invc),
+                                  df2_mul(eta, delta)));
+    out[1] = df2_add_fast(df2_mul(eta, zeta), df2_mul(df2_add_fast(df2_mul(v, eta_lam), df2_mul(u, eta_snt)), invc));
+    out[2] = df2_scale2(df2_add_fast(df2_mul(u, u), df2_mul(v, v)), f2_splat(0.5f));
+    out[3] = df2_neg(df2_add_fast(df2_mul(df2_add_fast(df2_mul(u, phi_lam), df2_neg(df2_mul(v, phi_snt))), invc),
+                                  df2_mul(phi, delta)));
+    bool fin = true;
+#pragma unroll
+    for (int f = 0; f < 4; ++f) {
+      float x0, x1;
+      f2_unpack(out[f].hi, x0, x1);
+      fin = fin && isfinite(x0) && isfinite(x1);
+    }
+    float p0, p1;
+    f2_unpack(phi.hi, p0, p1);
+    unsigned bits = 0u;
+    if (!fin) bits |= AEOLUS_STATE_NONFINITE;
+    if (!(phi0f + p0 > 0.0f) || !(phi0f + p1 > 0.0f)) bits |= AEOLUS_STATE_THICKNESS;
+    return bits;
+  }
 };
 
 // Split-precision form of the SWE derive: the tensor-core synthesis

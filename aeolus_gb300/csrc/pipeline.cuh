@@ -9,6 +9,7 @@
 #include "legendre.cuh"
 #include "rows.cuh"
 #include "rows_fx.cuh"
+#include "rows_pfa.cuh"
 
 namespace aeolus {
 
@@ -135,6 +136,21 @@ int launch_rows_fx8(const aeolus_plan_impl* p, const Pw& pw, const RowArgs& a, c
   return AEOLUS_OK;
 }
 
+// nlon = 384: prime-factor 3 x 64 transforms (rows_pfa.cuh), kPfaThreads
+// threads (the plan's row-thread knob does not apply).
+template <class Pw, int IN_MODE, int OUT_MODE>
+int launch_rows_pfa(const aeolus_plan_impl* p, const Pw& pw, const RowArgs& a, cudaStream_t st) {
+  const size_t sm = row_pfa_smem_bytes<Pw>();
+  auto kern = row_kernel_pfa<Pw, IN_MODE, OUT_MODE>;
+  int s = allow_smem(kern, sm);
+  if (s) return s;
+  ProfScope prof(IN_MODE == kInF ? (OUT_MODE == kOutG ? "rows_fx_c2r_products_r2c" : "rows_fx_c2r") : "rows_fx_r2c",
+                 st);
+  kern<<<dim3(p->nlat, a.batch), kPfaThreads, sm, st>>>(a, pw, p->twfx, fx_consts());
+  AE_LAUNCH("row_kernel_pfa");
+  return AEOLUS_OK;
+}
+
 template <class Pw, int IN_MODE, int OUT_MODE>
 int launch_rows(const aeolus_plan_impl* p, const Pw& pw, RowArgs a, cudaStream_t st) {
   row_args(p, a);
@@ -146,7 +162,7 @@ int launch_rows(const aeolus_plan_impl* p, const Pw& pw, RowArgs a, cudaStream_t
     a.fft = p->fftx;
     using F388 = FftFixed<3, 8, 8>;  // nlon 384
     using F288 = FftFixed<2, 8, 8>;  // nlon 256
-    if (F388::matches(p->fftx)) return launch_rows_fx8<Pw, IN_MODE, OUT_MODE, 3>(p, pw, a, st);
+    if (F388::matches(p->fftx)) return launch_rows_pfa<Pw, IN_MODE, OUT_MODE>(p, pw, a, st);
     if (F288::matches(p->fftx)) return launch_rows_fx8<Pw, IN_MODE, OUT_MODE, 2>(p, pw, a, st);
     return launch_rows_fx<Pw, IN_MODE, OUT_MODE, FftRuntime>(p, pw, a, st);
   }

@@ -1,0 +1,409 @@
+// Longitude stage of the split-precision path for nlon = 384 (half-length
+// complex transforms of n = 192 = 3 x 64): the same arithmetic kinds as
+// row_fx8_body (64-bit fixed-point FFTs, double-float products), with
+//  * prime-factor (Good-Thomas) transforms: 192 = 3 x 64 with coprime
+//    factors needs no twiddles between the radix-3 stage and the 64-point
+//    transforms, so only the one twiddled radix-8 stage inside each 64-point
+//    transform multiplies (49 of 64 elements) -- 147 twiddle products per
+//    192-point transform against 273 for the 3 x 8 x 8 Cooley-Tukey order;
+//  * index maps: spectrum index q sits in block q mod 3 at position
+//    rev8(43 q mod 64) (43 = 3^-1 mod 64, rev8 swaps the two octal digits),
+//    grid index i in block i mod 3 at position i mod 64.  The inverse
+//    transform reads the spectrum map and writes the grid map, the forward
+//    transform reads the grid map and writes the spectrum map, so the
+//    pointwise products stay in place.  Positions inside a 64-slot block are
+//    XOR-swizzled (u ^ (u >> 3) in the low octal digit) so both radix-8
+//    passes and the radix-3 pass touch 8 distinct 16-byte bank groups per
+//    8-lane phase;
+//  * the row's spectra staged once into shared memory by cp.async, each at
+//    the slot of the thread that consumes it, while the row constants are
+//    formed; block exponents and the real-FFT pre-processing then read
+//    shared memory;
+//  * phases split so that their item counts fill the 128 threads (pre-
+//    processing pairs: 97 per field; radix-3: 64 per field), and the radix-3
+//    stage of the forward transform fused into its post-processing (32 items
+//    per field: orders c, 64-c, 64+c, 128-c, 128+c, 192-c);
+//  * the pointwise products of functors that provide df_op2 run two grid
+//    points at a time on the packed two-lane f32 pipe (fx_to_df2, df2).
+// The arithmetic of each butterfly, pre- and post-processing step and
+// product is that of row_fx8_body; only the FFT factorisation (and so the
+// rounding order) differs.
+#pragma once
+
+#include <type_traits>
+
+#include "rows_fx.cuh"
+
+namespace aeolus {
+
+struct Pfa {
+  static constexpr int n = 192, N = 384, fs = n + 1, hb = 48;  // hb = min(52, 56 - ceil(log2 n))
+  static __device__ __forceinline__ int rev8(int u) { return ((u & 7) << 3) | (u >> 3); }
+  static __device__ __forceinline__ int sw(int u) { return (u & ~7) | ((u ^ (u >> 3)) & 7); }
+  static __device__ __forceinline__ int upos(int q) { return sw(rev8((43 * q) & 63)); }
+  static __device__ __forceinline__ int spec(int q) { return (q % 3) * 64 + upos(q); }
+  static __device__ __forceinline__ int grid(int i) { return (i % 3) * 64 + sw(i & 63); }
+};
+constexpr int kPfaThreads = 128;
+
+__device__ __forceinline__ void cp_async16(void* sdst, const void* gsrc) {
+  const unsigned s = static_cast<unsigned>(__cvta_generic_to_shared(sdst));
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(s), "l"(gsrc) : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() {
+  asm volatile("cp.async.commit_group;" ::: "memory");
+  asm volatile("cp.async.wait_group 0;" ::: "memory");
+}
+
+// df_to_fx of a complex double-float (float4: re.hi, re.lo, im.hi, im.lo),
+// the float steps of both parts on the packed two-lane pipe.
+__device__ __forceinline__ cfx df_to_fx2(float4 w, f2 pa, f2 pb) {
+  const f2 th = f2_mul(f2_mul(f2_pack(w.x, w.z), pa), pb), tl = f2_mul(f2_mul(f2_pack(w.y, w.w), pa), pb);
+  const f2 c15 = f2_splat(12582912.0f);  // 1.5 2^23
+  const f2 um = f2_fma(th, f2_splat(9.31322574615478515625e-10f), c15);
+  const f2 r = f2_fma(f2_neg(f2_sub(um, c15)), f2_splat(1073741824.0f), th);
+  float um0, um1, r0, r1, tl0, tl1;
+  f2_unpack(um, um0, um1);
+  f2_unpack(r, r0, r1);
+  f2_unpack(tl, tl0, tl1);
+  const int u0 = __float_as_int(um0) - 0x4B400000, u1 = __float_as_int(um1) - 0x4B400000;
+  return cfx{fx_madw(u0, 1 << 30, static_cast<long long>(__float2int_rn(r0) + __float2int_rn(tl0))),
+             fx_madw(u1, 1 << 30, static_cast<long long>(__float2int_rn(r1) + __float2int_rn(tl1)))};
+}
+
+// fx_to_df of two values, the float steps packed.
+__device__ __forceinline__ df2 fx_to_df2(long long X0, long long X1, f2 pa, f2 pb) {
+  const unsigned l0 = static_cast<unsigned>(X0), h0 = static_cast<unsigned>(X0 >> 32);
+  const unsigned l1 = static_cast<unsigned>(X1), h1 = static_cast<unsigned>(X1 >> 32);
+  const unsigned a0 = l0 & 0xFFFFFu, b0 = l1 & 0xFFFFFu;
+  const unsigned a1 = __funnelshift_r(l0, h0, 20) & 0xFFFFFu, b1 = __funnelshift_r(l1, h1, 20) & 0xFFFFFu;
+  const int a2 = static_cast<int>(X0 >> 40), b2 = static_cast<int>(X1 >> 40);
+  const f2 f0 = f2_sub(f2_pack(__int_as_float(0x4B000000 | a0), __int_as_float(0x4B000000 | b0)), f2_splat(8388608.0f));
+  const f2 f1 = f2_sub(f2_pack(__int_as_float((170u << 23) | a1), __int_as_float((170u << 23) | b1)),
+                       f2_splat(8796093022208.0f));
+  const f2 fh = f2_sub(f2_pack(__int_as_float((190 << 23) + 0x400000 + a2), __int_as_float((190 << 23) + 0x400000 + b2)),
+                       f2_splat(13835058055282163712.0f));
+  const f2 s = f2_add(fh, f1);
+  const f2 e1 = f2_sub(f1, f2_sub(s, fh));
+  const f2 t = f2_add(e1, f0);
+  const f2 h = f2_add(s, t);
+  const f2 l = f2_sub(t, f2_sub(h, s));
+  return df2{f2_mul(f2_mul(h, pa), pb), f2_mul(f2_mul(l, pa), pb)};
+}
+
+// Functors with a packed two-point product (df_op2).
+template <class Pw, class = void>
+struct PwHasPairs : std::false_type {};
+template <class Pw>
+struct PwHasPairs<Pw, std::void_t<decltype(&Pw::df_op2)>> : std::true_type {};
+
+// One radix-8 pass over the 64-point blocks of NFLD fields: LS = 1 (8
+// consecutive positions, no twiddles) or LS = 8 (stride 8, twiddles
+// w64^(k t) before the butterfly (DIT, inverse) or after it (DIF,
+// forward)).  CONV: the rows still hold double-floats, rounded to the
+// field's fixed-point scale (pa pb = 2^-S) as they are loaded.
+template <bool INV, int LS, bool CONV, int NFLD>
+__device__ __forceinline__ void pfa_pass(cfx* __restrict__ x, const FxW* __restrict__ tw, const FxConst& kc,
+                                         const float* sqa, const float* sqb) {
+  constexpr int fs = Pfa::fs;
+  constexpr bool TW = LS == 8;
+#pragma unroll 1
+  for (int idx = threadIdx.x; idx < NFLD * 24; idx += kPfaThreads) {
+    const int f = idx / 24, rem = idx - f * 24, r = rem >> 3, k = rem & 7;
+    cfx* y = x + f * fs + r * 64;
+    cfx v[8];
+    if constexpr (CONV) {
+      const f2 pa = f2_splat(sqa[f]), pb = f2_splat(sqb[f]);
+#pragma unroll
+      for (int t = 0; t < 8; ++t)
+        v[t] = df_to_fx2(reinterpret_cast<const float4*>(y)[LS == 1 ? 8 * k + (t ^ k) : 8 * t + (k ^ t)], pa, pb);
+    } else {
+#pragma unroll
+      for (int t = 0; t < 8; ++t) v[t] = y[LS == 1 ? 8 * k + (t ^ k) : 8 * t + (k ^ t)];
+    }
+    if (INV && TW) {
+#pragma unroll
+      for (int t = 1; t < 8; ++t) v[t] = fx_cmul<INV>(v[t], fx_ldw(&tw[6 * k * t]));
+    }
+    butterfly_fx<INV, 8>(v, kc);
+    if (!INV && TW) {
+#pragma unroll
+      for (int t = 1; t < 8; ++t) v[t] = fx_cmul<INV>(v[t], fx_ldw(&tw[6 * k * t]));
+    }
+#pragma unroll
+    for (int t = 0; t < 8; ++t) y[LS == 1 ? 8 * k + (t ^ k) : 8 * t + (k ^ t)] = v[t];
+  }
+}
+
+// Real-FFT pre-processing of the pair (q, n - q) of one field, in place on
+// the spectrum map (as row_fx8_body: z_q = A + P, z_{n-q} = conj(A - P)).
+__device__ __forceinline__ void pfa_pre_pair(cfx* z, int q, int L, f2 qa, f2 qb, const FxW* __restrict__ twfx) {
+  const int qn = Pfa::n - q;
+  const int s0 = Pfa::spec(q), s1 = Pfa::spec(q == 0 ? 0 : qn);
+  const FxW w = fx_ldw(&twfx[q]);
+  cfx hq = cfx{0, 0}, hn = cfx{0, 0};
+  if (q <= L) {
+    hq = df_to_fx2(reinterpret_cast<const float4*>(z)[s0], qa, qb);
+    if (q == 0) hq.im = 0;  // Im(F_0) is dropped
+  }
+  if (q > 0 && qn <= L) hn = df_to_fx2(reinterpret_cast<const float4*>(z)[s1], qa, qb);
+  const cfx A = fx_add(hq, fx_conj(hn));
+  const cfx B = fx_sub(hq, fx_conj(hn));
+  const cfx P = fx_i<true>(fx_cmul<true>(B, w));
+  z[s0] = fx_add(A, P);
+  if (q > 0 && qn > q) z[s1] = fx_conj(fx_sub(A, P));
+}
+
+// Forward post-processing of order q from the spectrum map: the packed G
+// word pair of R2 / 2 (as row_fx8_body).
+__device__ __forceinline__ void pfa_post(const cfx* Z, int q, int e, const FxW* __restrict__ twfx, longlong2* out) {
+  const FxW w = fx_ldw(&twfx[q]);
+  const cfx zq = Z[Pfa::spec(q)];
+  const cfx zn = fx_conj(Z[Pfa::spec(q == 0 ? 0 : Pfa::n - q)]);
+  const cfx E2 = fx_add(zq, zn);
+  const cfx D = fx_sub(zq, zn);
+  const cfx O2 = cfx{D.im, -D.re};
+  const cfx R2 = fx_add(E2, fx_cmul<false>(O2, w));
+  *out = make_longlong2(pk_pack(R2.re, e), pk_pack(R2.im, e));
+}
+
+template <class Pw, int IN_MODE, int OUT_MODE>
+__device__ __forceinline__ void row_pfa_body(const RowArgs& a, const Pw& pw, const FxW* __restrict__ twfx,
+                                             const FxConst& kc, int bx, int by) {
+  constexpr int NIN = Pw::NIN, NOUT = Pw::NOUT;
+  constexpr int NF = NIN > NOUT ? NIN : NOUT;
+  constexpr int n = Pfa::n, N = Pfa::N, fs = Pfa::fs, hb = Pfa::hb, T = kPfaThreads;
+  constexpr int PSI = (T / NIN) * NIN, QSI = T / NIN;
+  constexpr bool kPairs = PwHasPairs<Pw>::value;
+  static_assert(n - T == T / 2, "pointwise split: one slot pair and one single point per thread");
+  extern __shared__ cfx smem_fx[];
+  __shared__ unsigned s_bits;
+  __shared__ int s_in[NF];        // block exponents (inputs, then outputs)
+  __shared__ unsigned s_key[NF];  // largest |hi| bit key of each input field
+  __shared__ unsigned s_omax[NF]; // largest |hi| bit key of each output field
+  __shared__ float s_pa[NF], s_pb[NF], s_qa[NF], s_qb[NF];
+  __shared__ RowDf s_rc;
+  __shared__ df s_wj;
+  const int j = bx, b = by, tid = threadIdx.x;
+  const int L = a.L, ldm = L + 1;
+  cfx* buf0 = smem_fx;
+  const long sq = (long)a.nblk * a.nlat;
+  const float4* block = nullptr;
+  if (IN_MODE == kInF || OUT_MODE == kOutG)
+    block = reinterpret_cast<const float4*>(a.FG) + fg_index(b, 0, 0, j, L, a.nblk, a.nlat);
+  const long sqo = a.G ? (long)a.gblk * a.nlat : sq;
+  longlong2* oblock = nullptr;
+  if (OUT_MODE == kOutG)
+    oblock = a.G ? reinterpret_cast<longlong2*>(a.G) + fg_index(b, 0, 0, j, L, a.gblk, a.nlat)
+                 : reinterpret_cast<longlong2*>(const_cast<float4*>(block));
+  if constexpr (IN_MODE == kInF) {
+    // stage F[q][f] at slot spec(q) of field f, fields fastest (coalesced)
+#pragma unroll 1
+    for (int idx = tid; idx < NIN * ldm; idx += T) {
+      const int q = idx / NIN, f = idx - q * NIN;
+      cp_async16(buf0 + f * fs + Pfa::spec(q), block + (long)q * sq + f);
+    }
+  }
+  if (tid == 0) s_bits = 0u;
+  if (tid < NF) {
+    s_key[tid] = 0u;
+    s_omax[tid] = 0u;
+  }
+  if (tid == 32) {  // row constants (FP64 work) while the copies fly
+    s_rc = pw.df_row(a.coslat[j], a.fgrid ? a.fgrid[j] : 0.0);
+    s_wj = (OUT_MODE == kOutG && a.wq) ? df_from_double(a.wq[j]) : df{1.f, 0.f};
+  }
+  if constexpr (IN_MODE == kInF) cp_async_wait_all();
+  __syncthreads();
+
+  // ---- 1. grid rows of the inputs
+  if constexpr (IN_MODE == kInF) {
+    if (tid < PSI) {  // largest |hi| per field (m = 0: Im dropped)
+      const int f = tid % NIN;
+      const float4* zf = reinterpret_cast<const float4*>(buf0 + f * fs);
+      unsigned mx = 0u;
+      for (int q = tid / NIN; q < ldm; q += QSI) {
+        const float4 w = zf[Pfa::spec(q)];
+        mx = max(mx, max(__float_as_uint(w.x) & 0x7FFFFFFFu, q == 0 ? 0u : __float_as_uint(w.z) & 0x7FFFFFFFu));
+      }
+      if (mx) atomicMax(&s_key[f], mx);
+    }
+    __syncthreads();
+    if (tid < NIN) {  // block exponent: |F| < 2^E -> |X| < 2^hb
+      const unsigned key = s_key[tid];
+      const int S = (key >> 23) == 0 ? 0 : fkey_exp(key) - hb;
+      s_in[tid] = S;
+      fx_pow2_split(S, s_pa[tid], s_pb[tid]);
+      fx_pow2_split(-S, s_qa[tid], s_qb[tid]);
+    }
+    __syncthreads();
+#pragma unroll 1
+    for (int idx = tid; idx < NIN * (n / 2 + 1); idx += T) {
+      const int q = idx / NIN, f = idx - q * NIN;
+      pfa_pre_pair(buf0 + f * fs, q, L, f2_splat(s_qa[f]), f2_splat(s_qb[f]), twfx);
+    }
+    __syncthreads();
+#pragma unroll 1
+    for (int idx = tid; idx < NIN * 64; idx += T) {  // radix-3 across the blocks (no twiddles)
+      cfx* z = buf0 + (idx >> 6) * fs + (idx & 63);
+      cfx v[3] = {z[0], z[64], z[128]};
+      butterfly_fx<true, 3>(v, kc);
+      z[0] = v[0];
+      z[64] = v[1];
+      z[128] = v[2];
+    }
+    __syncthreads();
+    pfa_pass<true, 1, false, NIN>(buf0, twfx, kc, nullptr, nullptr);
+    __syncthreads();
+    pfa_pass<true, 8, false, NIN>(buf0, twfx, kc, nullptr, nullptr);
+    __syncthreads();
+  } else {
+    df* x0 = reinterpret_cast<df*>(buf0);
+    for (int idx = tid; idx < NIN * N; idx += T) {
+      const int f = idx / N, k = idx - f * N;
+      x0[2 * (f * fs + Pfa::grid(k >> 1)) + (k & 1)] =
+          df_from_double(a.gin[(long)b * a.gin_b + (long)f * a.gin_f + (long)j * N + k]);
+    }
+    __syncthreads();
+  }
+
+  // ---- 2. pointwise products, weighted by the row's quadrature weight; in
+  // place (each point is read before it is written, by one thread)
+  {
+    const RowDf rc = s_rc;
+    const df wj = s_wj;
+    const bool wq = OUT_MODE == kOutG && a.wq != nullptr;
+    unsigned bits = 0u;
+    unsigned omax[NOUT];
+#pragma unroll
+    for (int f = 0; f < NOUT; ++f) omax[f] = 0u;
+    float pa[NIN], pb[NIN];
+    if constexpr (IN_MODE == kInF) {
+#pragma unroll
+      for (int f = 0; f < NIN; ++f) {
+        pa[f] = s_pa[f];
+        pb[f] = s_pb[f];
+      }
+    }
+    auto single = [&](int k) {
+      const int slot = 2 * Pfa::grid(k >> 1) + (k & 1);
+      const long long* xi = reinterpret_cast<const long long*>(buf0);
+      const df* xd = reinterpret_cast<const df*>(buf0);
+      df* xo = reinterpret_cast<df*>(buf0);
+      df in[NIN], out[NOUT];
+#pragma unroll
+      for (int f = 0; f < NIN; ++f)
+        in[f] = IN_MODE == kInF ? fx_to_df(xi[2 * f * fs + slot], pa[f], pb[f]) : xd[2 * f * fs + slot];
+      bits |= pw.df_op(rc, in, out);
+#pragma unroll
+      for (int f = 0; f < NOUT; ++f) {
+        if (wq) out[f] = df_mul(out[f], wj);
+        xo[2 * f * fs + slot] = out[f];
+        omax[f] = max(omax[f], __float_as_uint(out[f].hi) & 0x7FFFFFFFu);
+      }
+    };
+    if constexpr (kPairs) {
+      // slots 0 .. T-1 as pairs of grid points, the remaining 2 (n - T)
+      // points one per thread
+      {
+        const int s = Pfa::grid(tid);
+        df2 in[NIN], out[NOUT];
+#pragma unroll
+        for (int f = 0; f < NIN; ++f) {
+          if constexpr (IN_MODE == kInF) {
+            const cfx X = buf0[f * fs + s];
+            in[f] = fx_to_df2(X.re, X.im, f2_splat(pa[f]), f2_splat(pb[f]));
+          } else {
+            const float4 w = reinterpret_cast<const float4*>(buf0)[f * fs + s];
+            in[f] = df2{f2_pack(w.x, w.z), f2_pack(w.y, w.w)};
+          }
+        }
+        bits |= pw.df_op2(rc, in, out);
+        const df2 wj2 = df2_pack(wj, wj);
+#pragma unroll
+        for (int f = 0; f < NOUT; ++f) {
+          if (wq) out[f] = df2_mul(out[f], wj2);
+          df x0, x1;
+          df2_unpack(out[f], x0, x1);
+          reinterpret_cast<float4*>(buf0)[f * fs + s] = make_float4(x0.hi, x0.lo, x1.hi, x1.lo);
+          omax[f] = max(omax[f], max(__float_as_uint(x0.hi) & 0x7FFFFFFFu, __float_as_uint(x1.hi) & 0x7FFFFFFFu));
+        }
+      }
+      single(2 * T + tid);
+    } else {
+#pragma unroll 1
+      for (int it = 0; it < N / T; ++it) single(tid + it * T);
+    }
+    if (a.status && bits) atomicOr(&s_bits, bits);
+    if constexpr (OUT_MODE == kOutG) {
+#pragma unroll
+      for (int f = 0; f < NOUT; ++f) {
+        unsigned v = omax[f];
+        for (int o = 16; o > 0; o >>= 1) v = max(v, __shfl_xor_sync(0xffffffffu, v, o));
+        if ((tid & 31) == 0 && v) atomicMax(&s_omax[f], v);
+      }
+    }
+  }
+  __syncthreads();
+  if (a.status && tid == 0 && s_bits) atomicOr(&a.status[b], s_bits);
+
+  // ---- 3. outputs
+  if constexpr (OUT_MODE == kOutGrid) {
+    const df* xo = reinterpret_cast<const df*>(buf0);
+    for (int idx = tid; idx < NOUT * N; idx += T) {
+      const int f = idx / N, k = idx - f * N;
+      a.gout[(long)b * a.gout_b + (long)f * a.gout_f + (long)j * N + k] =
+          df_to_double(xo[2 * (f * fs + Pfa::grid(k >> 1)) + (k & 1)]);
+    }
+  } else {
+    if (tid < NOUT) {  // output block exponents (|X| < 2^hb)
+      const unsigned key = s_omax[tid];
+      const int S = (key >> 23) == 0 ? 0 : fkey_exp(key) - hb;
+      s_in[tid] = S;
+      fx_pow2_split(-S, s_pa[tid], s_pb[tid]);
+    }
+    __syncthreads();
+    pfa_pass<false, 8, true, NOUT>(buf0, twfx, kc, s_pa, s_pb);
+    __syncthreads();
+    pfa_pass<false, 1, false, NOUT>(buf0, twfx, kc, nullptr, nullptr);
+    __syncthreads();
+    // radix-3 across the blocks for the groups of c and 64 - c (item 0: 0
+    // and 32), then the real-FFT post-processing of their six orders
+#pragma unroll 1
+    for (int idx = tid; idx < NOUT * 32; idx += T) {
+      const int c = idx / NOUT, f = idx - c * NOUT;
+      const int e = s_in[f] - 1;  // R2 / 2 in units of 2^S
+      cfx* Z = buf0 + f * fs;
+      const int g1 = c == 0 ? 32 : 64 - c;
+#pragma unroll 1
+      for (int g = 0; g < 2; ++g) {
+        const int u = Pfa::upos(g == 0 ? c : g1);
+        cfx v[3] = {Z[u], Z[64 + u], Z[128 + u]};
+        butterfly_fx<false, 3>(v, kc);
+        Z[u] = v[0];
+        Z[64 + u] = v[1];
+        Z[128 + u] = v[2];
+      }
+#pragma unroll 1
+      for (int p = 0; p < 6; ++p) {
+        const int q = c == 0 ? 32 * p
+                             : (p == 0 ? c : p == 1 ? 64 - c : p == 2 ? 64 + c : p == 3 ? 128 - c : p == 4 ? 128 + c : 192 - c);
+        if (q <= L) pfa_post(Z, q, e, twfx, oblock + (long)q * sqo + f);
+      }
+    }
+  }
+}
+
+template <class Pw, int IN_MODE, int OUT_MODE>
+__global__ void __launch_bounds__(kPfaThreads, 6) row_kernel_pfa(RowArgs a, Pw pw, const FxW* __restrict__ twfx,
+                                                                 FxConst kc) {
+  row_pfa_body<Pw, IN_MODE, OUT_MODE>(a, pw, twfx, kc, blockIdx.x, blockIdx.y);
+}
+
+template <class Pw>
+constexpr size_t row_pfa_smem_bytes() {
+  constexpr int NF = Pw::NIN > Pw::NOUT ? Pw::NIN : Pw::NOUT;
+  return (size_t)NF * Pfa::fs * sizeof(cfx);
+}
+
+}  // namespace aeolus
