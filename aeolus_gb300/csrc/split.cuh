@@ -316,6 +316,10 @@ __global__ void __launch_bounds__(256, 3) split_synth_slice_kernel(SplitDims dm,
 }
 
 // ------------------------------------------------- analysis data slicing
+__device__ __forceinline__ void cp_async8(void* sdst, const void* gsrc) {
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(tc::smem_u32(sdst)), "l"(gsrc) : "memory");
+}
+
 // Reads the packed G words (fx.cuh; two per complex value), grid (m, chunk).
 template <int NF>
 __device__ __forceinline__ void split_anal_slice_body(const SplitDims& dm, int batch, int mb, int nblk,
@@ -328,14 +332,17 @@ __device__ __forceinline__ void split_anal_slice_body(const SplitDims& dm, int b
   const int b0 = by * mb;
   const int nb = min(mb, batch - b0);
   const int nc = nb * NF * 2;
+  // the words go straight to shared memory (8-byte cp.async): every load of
+  // the CTA is in flight at once instead of one register round trip each
   for (int idx = threadIdx.x; idx < nb * NF * nlat; idx += blockDim.x) {
     const int f = idx % NF;
     const int r = idx / NF;
     const int j = r % nlat, bl = r / nlat;
-    const longlong2 g = *reinterpret_cast<const longlong2*>(FG + 2 * fg_index(b0 + bl, m, f, j, L, nblk, nlat));
-    s_wval[((bl * NF + f) * 2 + 0) * ns + j] = g.x;
-    s_wval[((bl * NF + f) * 2 + 1) * ns + j] = g.y;
+    const long long* g = FG + 2 * fg_index(b0 + bl, m, f, j, L, nblk, nlat);
+    cp_async8(&s_wval[((bl * NF + f) * 2 + 0) * ns + j], g);
+    cp_async8(&s_wval[((bl * NF + f) * 2 + 1) * ns + j], g + 1);
   }
+  asm volatile("cp.async.commit_group;\n\tcp.async.wait_group 0;" ::: "memory");
   __syncthreads();
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
   for (int c = warp; c < nc; c += nwarp) {
