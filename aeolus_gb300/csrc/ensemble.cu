@@ -73,6 +73,7 @@ struct RowArg {
   Pw pw;
   const FxW* twfx;
   const float4* twdf;
+  int kind;  // SplitRowKind of the group's plan (split path)
 };
 template <class Derive>
 struct SliceSynthArg {
@@ -112,12 +113,19 @@ __global__ void __launch_bounds__(256) g_rows(Grouped<RowArg<Pw>> g) {
   row_body<Pw, kInF, kOutG>(g.arg[k].a, g.arg[k].pw, loc % g.gx[k], loc / g.gx[k]);
 }
 
+// Each group runs the row body its plan's single-plan chains run
+// (split_row_kind): the prime-factor and fixed-radix bodies need
+// kPfaThreads = kFx8Threads threads, which the launch then uses.
 template <class Pw>
-__global__ void __launch_bounds__(256) g_rows_fx(Grouped<RowArg<Pw>> g, FxConst kc) {
+__global__ void __launch_bounds__(256, 3) g_rows_fx(Grouped<RowArg<Pw>> g, FxConst kc) {
   const int k = g.find(blockIdx.x);
   const int loc = blockIdx.x - g.start[k];
-  row_fx_body<Pw, kInF, kOutG>(g.arg[k].a, g.arg[k].pw, g.arg[k].twfx, g.arg[k].twdf, kc, loc % g.gx[k],
-                               loc / g.gx[k]);
+  const RowArg<Pw>& r = g.arg[k];
+  switch (r.kind) {
+    case kRowsPfa: row_pfa_body<Pw, kInF, kOutG>(r.a, r.pw, r.twfx, kc, loc % g.gx[k], loc / g.gx[k]); break;
+    case kRowsFx8R2: row_fx8_body<Pw, kInF, kOutG, 2>(r.a, r.pw, r.twfx, kc, loc % g.gx[k], loc / g.gx[k]); break;
+    default: row_fx_body<Pw, kInF, kOutG>(r.a, r.pw, r.twfx, r.twdf, kc, loc % g.gx[k], loc / g.gx[k]);
+  }
 }
 
 template <class Derive>
@@ -321,6 +329,7 @@ int ens_stage_m(const aeolus_ensemble_s* E, double2* const* y0, int stage, doubl
   Grouped<RowArg<Pw>> gr{};
   size_t sm_rows = 0;
   int row_thr = 0;
+  bool fixed_thr = false;
   for (int k = 0; k < ng; ++k) {
     const aeolus_plan_impl* p = E->plan[k];
     RowArgs ra{};
@@ -329,10 +338,13 @@ int ens_stage_m(const aeolus_ensemble_s* E, double2* const* y0, int stage, doubl
     ra.nblk = NB;
     row_args(p, ra);
     if (E->split) ra.fft = p->fftx;
-    grouped_add(gr, RowArg<Pw>{ra, pws[k], p->twfx, p->twdf}, dim3(p->nlat, E->batch[k]));
-    sm_rows = std::max(sm_rows, E->split ? row_fx_smem_bytes<Pw>(p->fftx) : row_smem_bytes<Pw>(p->fft));
+    const int kind = E->split ? split_row_kind(p) : kRowsRuntime;
+    grouped_add(gr, RowArg<Pw>{ra, pws[k], p->twfx, p->twdf, kind}, dim3(p->nlat, E->batch[k]));
+    sm_rows = std::max(sm_rows, E->split ? split_row_smem_bytes<Pw>(p) : row_smem_bytes<Pw>(p->fft));
     row_thr = std::max(row_thr, row_threads(p));
+    if (kind != kRowsRuntime) fixed_thr = true;
   }
+  if (fixed_thr) row_thr = kPfaThreads;
   if (!E->split) {
     Grouped<SynthArg<Derive>> gs{};
     Grouped<AnalArg<Epi>> ga{};
@@ -720,7 +732,12 @@ extern "C" int aeolus_ensemble_autotune(aeolus_ensemble e, double* const* zeta, 
       }
     }
   }
-  {
+  bool fixed_rows = false;  // groups with prime-factor / fixed-radix bodies pin the row stage to their block size
+  if (e->split)
+    for (int k = 0; k < e->ng; ++k) fixed_rows = fixed_rows || split_row_kind(e->plan[k]) != kRowsRuntime;
+  if (fixed_rows) {
+    rep += "row stage: 128 threads/CTA (fixed by the prime-factor / fixed-radix row bodies)\n";
+  } else {
     const int thr[] = {128, 192, 256};
     int best_v = 256;
     float best = 1e30f;

@@ -151,6 +151,24 @@ int launch_rows_pfa(const aeolus_plan_impl* p, const Pw& pw, const RowArgs& a, c
   return AEOLUS_OK;
 }
 
+// Row-stage body of the split-precision path for a plan: every caller (the
+// single-plan chains and the grouped ensemble kernels) picks the same one,
+// so a plan's results do not depend on the route.
+enum SplitRowKind { kRowsRuntime = 0, kRowsFx8R2 = 1, kRowsPfa = 2 };
+inline int split_row_kind(const aeolus_plan_impl* p) {
+  if (FftFixed<3, 8, 8>::matches(p->fftx)) return kRowsPfa;    // nlon 384
+  if (FftFixed<2, 8, 8>::matches(p->fftx)) return kRowsFx8R2;  // nlon 256
+  return kRowsRuntime;
+}
+template <class Pw>
+size_t split_row_smem_bytes(const aeolus_plan_impl* p) {
+  switch (split_row_kind(p)) {
+    case kRowsPfa: return row_pfa_smem_bytes<Pw>();
+    case kRowsFx8R2: return row_fx8_smem_bytes<Pw>(2);
+    default: return row_fx_smem_bytes<Pw>(p->fftx);
+  }
+}
+
 template <class Pw, int IN_MODE, int OUT_MODE>
 int launch_rows(const aeolus_plan_impl* p, const Pw& pw, RowArgs a, cudaStream_t st) {
   row_args(p, a);
@@ -160,11 +178,11 @@ int launch_rows(const aeolus_plan_impl* p, const Pw& pw, RowArgs a, cudaStream_t
     // split-precision path: fixed-point FFTs, double-float products; every
     // row stage gets kernels compiled for the common radix sequences
     a.fft = p->fftx;
-    using F388 = FftFixed<3, 8, 8>;  // nlon 384
-    using F288 = FftFixed<2, 8, 8>;  // nlon 256
-    if (F388::matches(p->fftx)) return launch_rows_pfa<Pw, IN_MODE, OUT_MODE>(p, pw, a, st);
-    if (F288::matches(p->fftx)) return launch_rows_fx8<Pw, IN_MODE, OUT_MODE, 2>(p, pw, a, st);
-    return launch_rows_fx<Pw, IN_MODE, OUT_MODE, FftRuntime>(p, pw, a, st);
+    switch (split_row_kind(p)) {
+      case kRowsPfa: return launch_rows_pfa<Pw, IN_MODE, OUT_MODE>(p, pw, a, st);
+      case kRowsFx8R2: return launch_rows_fx8<Pw, IN_MODE, OUT_MODE, 2>(p, pw, a, st);
+      default: return launch_rows_fx<Pw, IN_MODE, OUT_MODE, FftRuntime>(p, pw, a, st);
+    }
   }
   const size_t sm = row_smem_bytes<Pw>(p->fft);
   auto kern = row_kernel<Pw, IN_MODE, OUT_MODE>;

@@ -45,6 +45,7 @@ struct Pfa {
   static __device__ __forceinline__ int grid(int i) { return (i % 3) * 64 + sw(i & 63); }
 };
 constexpr int kPfaThreads = 128;
+static_assert(kPfaThreads == kFx8Threads, "the grouped row kernel runs both bodies with one block size");
 
 __device__ __forceinline__ void cp_async16(void* sdst, const void* gsrc) {
   const unsigned s = static_cast<unsigned>(__cvta_generic_to_shared(sdst));

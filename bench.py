@@ -118,10 +118,15 @@ def ensemble_measure(dev, steps: int = 10, dt: float = 600.0):
         ens.rk4(states, dt, 3)                       # warm-up
         torch.cuda.synchronize(dev)
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        lib = _lib.load()
+        lib.aeolus_profile_reset()
+        lib.aeolus_profile_enable(1)
         e0.record()
         ens.rk4(states, dt, steps)
         e1.record()
         torch.cuda.synchronize(dev)
+        lib.aeolus_profile_enable(0)
+        kstats = _collect_kernels(lib, _lib)
         direct_ms = e0.elapsed_time(e1)
         graph_states = [x.clone() for x in init]
         ens.capture(graph_states, dt)
@@ -137,7 +142,8 @@ def ensemble_measure(dev, steps: int = 10, dt: float = 600.0):
         finals[prec] = states
         out[prec] = {"members_per_s": ens.members * steps / (graph_ms / 1000.0),
                      "ms_per_step_graph": graph_ms / steps, "ms_per_step_direct": direct_ms / steps,
-                     "graph_equals_direct": bool(same), "autotune": report.strip().splitlines()}
+                     "graph_equals_direct": bool(same), "autotune": report.strip().splitlines(),
+                     "kernel_ms_per_stage": {k: round(ms / n, 4) for k, (n, ms) in kstats.items()}}
         ens.close()
     rel = []
     for a, b in zip(finals["split"], finals["fp64"]):

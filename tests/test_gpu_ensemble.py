@@ -21,9 +21,9 @@ DEV = "cuda"
 GROUPS = [(21, 32, 64, 3), (42, 64, 128, 2), (31, 48, 96, 4)]   # (l_max, nlat, nlon, members)
 
 
-def _models(precision="fp64", nu=1e5):
+def _models(precision="fp64", nu=1e5, groups=None):
     ms = []
-    for L, nlat, nlon, _ in GROUPS:
+    for L, nlat, nlon, _ in groups or GROUPS:
         planet = ae.make_planet("latlon", nlat=nlat, nlon=nlon, l_max=L)
         if precision == "split":
             planet.so._product_space.sh.plan.set_precision(_lib.PREC_SPLIT_BF16)
@@ -31,9 +31,9 @@ def _models(precision="fp64", nu=1e5):
     return ms
 
 
-def _states(seed=0):
+def _states(seed=0, groups=None):
     out = []
-    for g, (L, _, _, B) in enumerate(GROUPS):
+    for g, (L, _, _, B) in enumerate(groups or GROUPS):
         out.append(torch.as_tensor(np.stack([W.bve_vorticity(L, seed + 100 * g + b) for b in range(B)]), device=DEV))
     return out
 
@@ -101,3 +101,18 @@ def test_ensemble_rejects_bad_input():
         ens.rk4(bad, 600.0)
     with pytest.raises(RuntimeError):
         ens.replay(1)
+
+
+# nlon 384 (prime-factor row body), 256 (fixed-radix row body) and 64
+# (runtime-radix row body) in one grouped launch
+FIXED_BODY_GROUPS = [(127, 192, 384, 2), (85, 128, 256, 2), (21, 32, 64, 2)]
+
+
+def test_grouped_split_step_equals_per_group_rk4_on_every_row_body():
+    models = _models("split", groups=FIXED_BODY_GROUPS)
+    ens = BarotropicEnsemble(models, [g[3] for g in FIXED_BODY_GROUPS])
+    states = _states(5, groups=FIXED_BODY_GROUPS)
+    ref = [m.rk4(s.clone(), 900.0, 2) for m, s in zip(models, states)]
+    ens.rk4(states, 900.0, 2)
+    for a, b in zip(states, ref):
+        assert torch.equal(a, b)

@@ -22,9 +22,9 @@ DEV = "cuda"
 GROUPS = [(21, 32, 64, 3), (42, 64, 128, 2), (31, 48, 96, 2)]   # (l_max, nlat, nlon, members)
 
 
-def _models(precision="fp64"):
+def _models(precision="fp64", groups=None):
     ms, depths = [], []
-    for g, (L, nlat, nlon, B) in enumerate(GROUPS):
+    for g, (L, nlat, nlon, B) in enumerate(groups or GROUPS):
         planet = ae.make_planet("latlon", nlat=nlat, nlon=nlon, l_max=L)
         if precision == "split":
             planet.so._product_space.sh.plan.set_precision(_lib.PREC_SPLIT_BF16)
@@ -33,9 +33,9 @@ def _models(precision="fp64"):
     return ms
 
 
-def _states():
+def _states(groups=None):
     return [torch.as_tensor(W.member_states(L, B, seed=11 + g)[0], device=DEV)
-            for g, (L, _, _, B) in enumerate(GROUPS)]
+            for g, (L, _, _, B) in enumerate(groups or GROUPS)]
 
 
 @pytest.mark.parametrize("precision", ["fp64", "split"])
@@ -92,3 +92,18 @@ def test_swe_ensemble_rejects_bad_input():
     zeta = [s[:, 0].contiguous() for s in _states()]
     with pytest.raises(Exception):
         BarotropicEnsemble.rk4(ens, zeta, 300.0)
+
+
+# nlon 384 (prime-factor row body), 256 (fixed-radix row body) and 64
+# (runtime-radix row body) in one grouped launch
+FIXED_BODY_GROUPS = [(127, 192, 384, 2), (85, 128, 256, 2), (21, 32, 64, 2)]
+
+
+def test_grouped_split_swe_step_equals_per_group_rk4_on_every_row_body():
+    models = _models("split", groups=FIXED_BODY_GROUPS)
+    ens = ShallowWaterEnsemble(models, [g[3] for g in FIXED_BODY_GROUPS])
+    states = _states(groups=FIXED_BODY_GROUPS)
+    ref = [m.rk4(s.clone(), 300.0, 2, check=False) for m, s in zip(models, states)]
+    ens.rk4(states, 300.0, 2)
+    for a, b in zip(states, ref):
+        assert torch.equal(a, b)
