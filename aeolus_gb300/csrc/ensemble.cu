@@ -121,10 +121,15 @@ __global__ void __launch_bounds__(256, 3) g_rows_fx(Grouped<RowArg<Pw>> g, FxCon
   const int k = g.find(blockIdx.x);
   const int loc = blockIdx.x - g.start[k];
   const RowArg<Pw>& r = g.arg[k];
+  const int bx = loc % g.gx[k], by = loc / g.gx[k];
   switch (r.kind) {
-    case kRowsPfa: row_pfa_body<Pw, kInF, kOutG>(r.a, r.pw, r.twfx, kc, loc % g.gx[k], loc / g.gx[k]); break;
-    case kRowsFx8R2: row_fx8_body<Pw, kInF, kOutG, 2>(r.a, r.pw, r.twfx, kc, loc % g.gx[k], loc / g.gx[k]); break;
-    default: row_fx_body<Pw, kInF, kOutG>(r.a, r.pw, r.twfx, r.twdf, kc, loc % g.gx[k], loc / g.gx[k]);
+    case kRowsPfa192: row_pfa_body<Pw, kInF, kOutG, Pfa192>(r.a, r.pw, r.twfx, kc, bx, by); break;
+    case kRowsPfa160: row_pfa_body<Pw, kInF, kOutG, Pfa160>(r.a, r.pw, r.twfx, kc, bx, by); break;
+    case kRowsPfa96: row_pfa_body<Pw, kInF, kOutG, Pfa96>(r.a, r.pw, r.twfx, kc, bx, by); break;
+    case kRowsPfa64: row_pfa_body<Pw, kInF, kOutG, Pfa64>(r.a, r.pw, r.twfx, kc, bx, by); break;
+    case kRowsPfa32: row_pfa_body<Pw, kInF, kOutG, Pfa32>(r.a, r.pw, r.twfx, kc, bx, by); break;
+    case kRowsFx8R2: row_fx8_body<Pw, kInF, kOutG, 2>(r.a, r.pw, r.twfx, kc, bx, by); break;
+    default: row_fx_body<Pw, kInF, kOutG>(r.a, r.pw, r.twfx, r.twdf, kc, bx, by);
   }
 }
 

@@ -136,12 +136,12 @@ int launch_rows_fx8(const aeolus_plan_impl* p, const Pw& pw, const RowArgs& a, c
   return AEOLUS_OK;
 }
 
-// nlon = 384: prime-factor 3 x 64 transforms (rows_pfa.cuh), kPfaThreads
+// nlon = 2 R0 R1 R2: prime-factor transforms (rows_pfa.cuh), kPfaThreads
 // threads (the plan's row-thread knob does not apply).
-template <class Pw, int IN_MODE, int OUT_MODE>
+template <class Pw, int IN_MODE, int OUT_MODE, class S>
 int launch_rows_pfa(const aeolus_plan_impl* p, const Pw& pw, const RowArgs& a, cudaStream_t st) {
-  const size_t sm = row_pfa_smem_bytes<Pw>();
-  auto kern = row_kernel_pfa<Pw, IN_MODE, OUT_MODE>;
+  const size_t sm = row_pfa_smem_bytes<Pw, S>();
+  auto kern = row_kernel_pfa<Pw, IN_MODE, OUT_MODE, S>;
   int s = allow_smem(kern, sm);
   if (s) return s;
   ProfScope prof(IN_MODE == kInF ? (OUT_MODE == kOutG ? "rows_fx_c2r_products_r2c" : "rows_fx_c2r") : "rows_fx_r2c",
@@ -154,16 +154,33 @@ int launch_rows_pfa(const aeolus_plan_impl* p, const Pw& pw, const RowArgs& a, c
 // Row-stage body of the split-precision path for a plan: every caller (the
 // single-plan chains and the grouped ensemble kernels) picks the same one,
 // so a plan's results do not depend on the route.
-enum SplitRowKind { kRowsRuntime = 0, kRowsFx8R2 = 1, kRowsPfa = 2 };
+enum SplitRowKind {
+  kRowsRuntime = 0,  // runtime radix sequence (row_fx_body)
+  kRowsFx8R2,        // nlon 256: 2 x 8 x 8 Cooley-Tukey (row_fx8_body)
+  kRowsPfa192,       // nlon 384: prime-factor 3 x (8 x 8)
+  kRowsPfa160,       // nlon 320: 5 x (4 x 8)
+  kRowsPfa96,        // nlon 192: 3 x (4 x 8)
+  kRowsPfa64,        // nlon 128: 8 x 8
+  kRowsPfa32,        // nlon 64: 4 x 8
+};
 inline int split_row_kind(const aeolus_plan_impl* p) {
-  if (FftFixed<3, 8, 8>::matches(p->fftx)) return kRowsPfa;    // nlon 384
-  if (FftFixed<2, 8, 8>::matches(p->fftx)) return kRowsFx8R2;  // nlon 256
+  const FftInfo& f = p->fftx;
+  if (Pfa192::matches(f)) return kRowsPfa192;
+  if (Pfa160::matches(f)) return kRowsPfa160;
+  if (Pfa96::matches(f)) return kRowsPfa96;
+  if (Pfa64::matches(f)) return kRowsPfa64;
+  if (Pfa32::matches(f)) return kRowsPfa32;
+  if (FftFixed<2, 8, 8>::matches(f)) return kRowsFx8R2;
   return kRowsRuntime;
 }
 template <class Pw>
 size_t split_row_smem_bytes(const aeolus_plan_impl* p) {
   switch (split_row_kind(p)) {
-    case kRowsPfa: return row_pfa_smem_bytes<Pw>();
+    case kRowsPfa192: return row_pfa_smem_bytes<Pw, Pfa192>();
+    case kRowsPfa160: return row_pfa_smem_bytes<Pw, Pfa160>();
+    case kRowsPfa96: return row_pfa_smem_bytes<Pw, Pfa96>();
+    case kRowsPfa64: return row_pfa_smem_bytes<Pw, Pfa64>();
+    case kRowsPfa32: return row_pfa_smem_bytes<Pw, Pfa32>();
     case kRowsFx8R2: return row_fx8_smem_bytes<Pw>(2);
     default: return row_fx_smem_bytes<Pw>(p->fftx);
   }
@@ -179,7 +196,11 @@ int launch_rows(const aeolus_plan_impl* p, const Pw& pw, RowArgs a, cudaStream_t
     // row stage gets kernels compiled for the common radix sequences
     a.fft = p->fftx;
     switch (split_row_kind(p)) {
-      case kRowsPfa: return launch_rows_pfa<Pw, IN_MODE, OUT_MODE>(p, pw, a, st);
+      case kRowsPfa192: return launch_rows_pfa<Pw, IN_MODE, OUT_MODE, Pfa192>(p, pw, a, st);
+      case kRowsPfa160: return launch_rows_pfa<Pw, IN_MODE, OUT_MODE, Pfa160>(p, pw, a, st);
+      case kRowsPfa96: return launch_rows_pfa<Pw, IN_MODE, OUT_MODE, Pfa96>(p, pw, a, st);
+      case kRowsPfa64: return launch_rows_pfa<Pw, IN_MODE, OUT_MODE, Pfa64>(p, pw, a, st);
+      case kRowsPfa32: return launch_rows_pfa<Pw, IN_MODE, OUT_MODE, Pfa32>(p, pw, a, st);
       case kRowsFx8R2: return launch_rows_fx8<Pw, IN_MODE, OUT_MODE, 2>(p, pw, a, st);
       default: return launch_rows_fx<Pw, IN_MODE, OUT_MODE, FftRuntime>(p, pw, a, st);
     }

@@ -1,28 +1,29 @@
-// Longitude stage of the split-precision path for nlon = 384 (half-length
-// complex transforms of n = 192 = 3 x 64): the same arithmetic kinds as
-// row_fx8_body (64-bit fixed-point FFTs, double-float products), with
-//  * prime-factor (Good-Thomas) transforms: 192 = 3 x 64 with coprime
-//    factors needs no twiddles between the radix-3 stage and the 64-point
-//    transforms, so only the one twiddled radix-8 stage inside each 64-point
-//    transform multiplies (49 of 64 elements) -- 147 twiddle products per
-//    192-point transform against 273 for the 3 x 8 x 8 Cooley-Tukey order;
-//  * index maps: spectrum index q sits in block q mod 3 at position
-//    rev8(43 q mod 64) (43 = 3^-1 mod 64, rev8 swaps the two octal digits),
-//    grid index i in block i mod 3 at position i mod 64.  The inverse
-//    transform reads the spectrum map and writes the grid map, the forward
-//    transform reads the grid map and writes the spectrum map, so the
-//    pointwise products stay in place.  Positions inside a 64-slot block are
-//    XOR-swizzled (u ^ (u >> 3) in the low octal digit) so both radix-8
-//    passes and the radix-3 pass touch 8 distinct 16-byte bank groups per
-//    8-lane phase;
+// Longitude stage of the split-precision path for half-length transforms
+// n = R0 x R1 x R2 (nlon = 2n) with R0 in {1, 3, 5} and R1 R2 = 32 or 64:
+// the same arithmetic kinds as row_fx8_body (64-bit fixed-point FFTs,
+// double-float products), with
+//  * prime-factor (Good-Thomas) transforms: n = R0 x P with R0 and P = R1 R2
+//    coprime needs no twiddles between the radix-R0 pass and the P-point
+//    transforms, so only the one twiddled pass inside each P-point transform
+//    multiplies -- 147 twiddle products per 192-point transform against 273
+//    for the 3 x 8 x 8 Cooley-Tukey order;
+//  * index maps: spectrum index q sits in block (P^-1 q) mod R0 at position
+//    rev(R0^-1 q mod P) (rev: the mixed-radix digit reversal n2 ->
+//    R2 (n2 mod R1) + n2 div R1), grid index i in block i mod R0 at position
+//    i mod P.  The inverse transform reads the spectrum map and writes the
+//    grid map, the forward transform reads the grid map and writes the
+//    spectrum map, so the pointwise products stay in place.  Positions inside
+//    a block are XOR-swizzled (u ^ (u >> 3) in the low octal digit) so the
+//    radix-8 passes and the radix-R0 pass touch 8 distinct 16-byte bank
+//    groups per 8-lane phase;
 //  * the row's spectra staged once into shared memory by cp.async, each at
 //    the slot of the thread that consumes it, while the row constants are
 //    formed; block exponents and the real-FFT pre-processing then read
 //    shared memory;
 //  * phases split so that their item counts fill the 128 threads (pre-
-//    processing pairs: 97 per field; radix-3: 64 per field), and the radix-3
-//    stage of the forward transform fused into its post-processing (32 items
-//    per field: orders c, 64-c, 64+c, 128-c, 128+c, 192-c);
+//    processing pairs: n/2 + 1 per field; radix-R0: P per field), and the
+//    radix-R0 pass of the forward transform fused into its post-processing
+//    (P/2 items per field: the order groups c + jP and P - c + jP);
 //  * the pointwise products of functors that provide df_op2 run two grid
 //    points at a time on the packed two-lane f32 pipe (fx_to_df2, df2).
 // The arithmetic of each butterfly, pre- and post-processing step and
@@ -36,14 +37,38 @@
 
 namespace aeolus {
 
-struct Pfa {
-  static constexpr int n = 192, N = 384, fs = n + 1, hb = 48;  // hb = min(52, 56 - ceil(log2 n))
-  static __device__ __forceinline__ int rev8(int u) { return ((u & 7) << 3) | (u >> 3); }
+constexpr int pfa_inv_mod(int a, int m) {
+  for (int x = 0; x < m; ++x)
+    if ((a * x) % m == 1 % m) return x;
+  return 0;
+}
+constexpr int pfa_ceil_log2(int v) {
+  int b = 0;
+  while ((1 << b) < v) ++b;
+  return b;
+}
+
+template <int R0_, int R1_, int R2_>
+struct PfaShape {
+  static constexpr int R0 = R0_, R1 = R1_, R2 = R2_, P = R1 * R2, n = R0 * P, N = 2 * n, fs = n + 1;
+  static constexpr int hb = 56 - pfa_ceil_log2(n) < 52 ? 56 - pfa_ceil_log2(n) : 52;  // |FFT input| < 2^hb
+  static constexpr int Pinv = pfa_inv_mod(P, R0), R0inv = pfa_inv_mod(R0, P);
+  static_assert(P == 32 || P == 64, "P-point transforms of 32 or 64 points");
+  static_assert(R0 == 1 || R0 == 3 || R0 == 5, "radix-R0 pass of 1, 3 or 5");
   static __device__ __forceinline__ int sw(int u) { return (u & ~7) | ((u ^ (u >> 3)) & 7); }
-  static __device__ __forceinline__ int upos(int q) { return sw(rev8((43 * q) & 63)); }
-  static __device__ __forceinline__ int spec(int q) { return (q % 3) * 64 + upos(q); }
-  static __device__ __forceinline__ int grid(int i) { return (i % 3) * 64 + sw(i & 63); }
+  static __device__ __forceinline__ int upos(int q) {
+    const int n2 = (R0inv * q) & (P - 1);
+    return sw(R2 * (n2 & (R1 - 1)) + n2 / R1);
+  }
+  static __device__ __forceinline__ int spec(int q) { return R0 == 1 ? upos(q) : ((Pinv * q) % R0) * P + upos(q); }
+  static __device__ __forceinline__ int grid(int i) { return R0 == 1 ? sw(i) : (i % R0) * P + sw(i & (P - 1)); }
+  static bool matches(const FftInfo& f) { return f.use_fft && f.n == n; }
 };
+using Pfa192 = PfaShape<3, 8, 8>;  // nlon 384
+using Pfa160 = PfaShape<5, 4, 8>;  // nlon 320
+using Pfa96 = PfaShape<3, 4, 8>;   // nlon 192
+using Pfa64 = PfaShape<1, 8, 8>;   // nlon 128
+using Pfa32 = PfaShape<1, 4, 8>;   // nlon 64
 constexpr int kPfaThreads = 128;
 static_assert(kPfaThreads == kFx8Threads, "the grouped row kernel runs both bodies with one block size");
 
@@ -98,49 +123,53 @@ struct PwHasPairs : std::false_type {};
 template <class Pw>
 struct PwHasPairs<Pw, std::void_t<decltype(&Pw::df_op2)>> : std::true_type {};
 
-// One radix-8 pass over the 64-point blocks of NFLD fields: LS = 1 (8
-// consecutive positions, no twiddles) or LS = 8 (stride 8, twiddles
-// w64^(k t) before the butterfly (DIT, inverse) or after it (DIF,
-// forward)).  CONV: the rows still hold double-floats, rounded to the
-// field's fixed-point scale (pa pb = 2^-S) as they are loaded.
-template <bool INV, int LS, bool CONV, int NFLD>
+// One pass over the P-point blocks of NFLD fields.  PASS1: R1 butterflies
+// of radix R2 over R2 consecutive positions, no twiddles; otherwise R2
+// butterflies of radix R1 at stride R2 with the twiddles w_P^(a k) before
+// the butterfly (inverse, DIT) or after it (forward, DIF).  The inverse runs
+// PASS1 then the strided pass, the forward the strided pass then PASS1.
+// CONV: the rows still hold double-floats, rounded to the field's fixed-
+// point scale (pa pb = 2^-S) as they are loaded.
+template <class S, bool INV, bool PASS1, bool CONV, int NFLD>
 __device__ __forceinline__ void pfa_pass(cfx* __restrict__ x, const FxW* __restrict__ tw, const FxConst& kc,
                                          const float* sqa, const float* sqb) {
-  constexpr int fs = Pfa::fs;
-  constexpr bool TW = LS == 8;
+  constexpr int R = PASS1 ? S::R2 : S::R1;        // butterfly radix
+  constexpr int NB = PASS1 ? S::R1 : S::R2;       // butterflies per block
+  constexpr int TWS = 2 * S::R0;                  // w_P = w_N^(N / P)
 #pragma unroll 1
-  for (int idx = threadIdx.x; idx < NFLD * 24; idx += kPfaThreads) {
-    const int f = idx / 24, rem = idx - f * 24, r = rem >> 3, k = rem & 7;
-    cfx* y = x + f * fs + r * 64;
-    cfx v[8];
+  for (int idx = threadIdx.x; idx < NFLD * S::R0 * NB; idx += kPfaThreads) {
+    const int f = idx / (S::R0 * NB), rem = idx - f * (S::R0 * NB), r = rem / NB, k = rem - r * NB;
+    cfx* y = x + f * S::fs + r * S::P;
+    auto pos = [&](int t) { return S::sw(PASS1 ? S::R2 * k + t : S::R2 * t + k); };
+    cfx v[R];
     if constexpr (CONV) {
       const f2 pa = f2_splat(sqa[f]), pb = f2_splat(sqb[f]);
 #pragma unroll
-      for (int t = 0; t < 8; ++t)
-        v[t] = df_to_fx2(reinterpret_cast<const float4*>(y)[LS == 1 ? 8 * k + (t ^ k) : 8 * t + (k ^ t)], pa, pb);
+      for (int t = 0; t < R; ++t) v[t] = df_to_fx2(reinterpret_cast<const float4*>(y)[pos(t)], pa, pb);
     } else {
 #pragma unroll
-      for (int t = 0; t < 8; ++t) v[t] = y[LS == 1 ? 8 * k + (t ^ k) : 8 * t + (k ^ t)];
+      for (int t = 0; t < R; ++t) v[t] = y[pos(t)];
     }
-    if (INV && TW) {
+    if (INV && !PASS1) {
 #pragma unroll
-      for (int t = 1; t < 8; ++t) v[t] = fx_cmul<INV>(v[t], fx_ldw(&tw[6 * k * t]));
+      for (int t = 1; t < R; ++t) v[t] = fx_cmul<INV>(v[t], fx_ldw(&tw[TWS * k * t]));
     }
-    butterfly_fx<INV, 8>(v, kc);
-    if (!INV && TW) {
+    butterfly_fx<INV, R>(v, kc);
+    if (!INV && !PASS1) {
 #pragma unroll
-      for (int t = 1; t < 8; ++t) v[t] = fx_cmul<INV>(v[t], fx_ldw(&tw[6 * k * t]));
+      for (int t = 1; t < R; ++t) v[t] = fx_cmul<INV>(v[t], fx_ldw(&tw[TWS * k * t]));
     }
 #pragma unroll
-    for (int t = 0; t < 8; ++t) y[LS == 1 ? 8 * k + (t ^ k) : 8 * t + (k ^ t)] = v[t];
+    for (int t = 0; t < R; ++t) y[pos(t)] = v[t];
   }
 }
 
 // Real-FFT pre-processing of the pair (q, n - q) of one field, in place on
 // the spectrum map (as row_fx8_body: z_q = A + P, z_{n-q} = conj(A - P)).
+template <class S>
 __device__ __forceinline__ void pfa_pre_pair(cfx* z, int q, int L, f2 qa, f2 qb, const FxW* __restrict__ twfx) {
-  const int qn = Pfa::n - q;
-  const int s0 = Pfa::spec(q), s1 = Pfa::spec(q == 0 ? 0 : qn);
+  const int qn = S::n - q;
+  const int s0 = S::spec(q), s1 = S::spec(q == 0 ? 0 : qn);
   const FxW w = fx_ldw(&twfx[q]);
   cfx hq = cfx{0, 0}, hn = cfx{0, 0};
   if (q <= L) {
@@ -157,10 +186,11 @@ __device__ __forceinline__ void pfa_pre_pair(cfx* z, int q, int L, f2 qa, f2 qb,
 
 // Forward post-processing of order q from the spectrum map: the packed G
 // word pair of R2 / 2 (as row_fx8_body).
+template <class S>
 __device__ __forceinline__ void pfa_post(const cfx* Z, int q, int e, const FxW* __restrict__ twfx, longlong2* out) {
   const FxW w = fx_ldw(&twfx[q]);
-  const cfx zq = Z[Pfa::spec(q)];
-  const cfx zn = fx_conj(Z[Pfa::spec(q == 0 ? 0 : Pfa::n - q)]);
+  const cfx zq = Z[S::spec(q)];
+  const cfx zn = fx_conj(Z[S::spec(q == 0 ? 0 : S::n - q)]);
   const cfx E2 = fx_add(zq, zn);
   const cfx D = fx_sub(zq, zn);
   const cfx O2 = cfx{D.im, -D.re};
@@ -168,15 +198,17 @@ __device__ __forceinline__ void pfa_post(const cfx* Z, int q, int e, const FxW* 
   *out = make_longlong2(pk_pack(R2.re, e), pk_pack(R2.im, e));
 }
 
-template <class Pw, int IN_MODE, int OUT_MODE>
+template <class Pw, int IN_MODE, int OUT_MODE, class S>
 __device__ __forceinline__ void row_pfa_body(const RowArgs& a, const Pw& pw, const FxW* __restrict__ twfx,
                                              const FxConst& kc, int bx, int by) {
   constexpr int NIN = Pw::NIN, NOUT = Pw::NOUT;
   constexpr int NF = NIN > NOUT ? NIN : NOUT;
-  constexpr int n = Pfa::n, N = Pfa::N, fs = Pfa::fs, hb = Pfa::hb, T = kPfaThreads;
+  constexpr int n = S::n, N = S::N, fs = S::fs, hb = S::hb, P = S::P, R0 = S::R0, T = kPfaThreads;
   constexpr int PSI = (T / NIN) * NIN, QSI = T / NIN;
   constexpr bool kPairs = PwHasPairs<Pw>::value;
-  static_assert(n - T == T / 2, "pointwise split: one slot pair and one single point per thread");
+  // pointwise: slot pairs in rounds of T, and for n = 3T/2 the last T/2
+  // slots as one single point per thread
+  constexpr bool kSplitTail = n - T == T / 2;
   extern __shared__ cfx smem_fx[];
   __shared__ unsigned s_bits;
   __shared__ int s_in[NF];        // block exponents (inputs, then outputs)
@@ -202,7 +234,7 @@ __device__ __forceinline__ void row_pfa_body(const RowArgs& a, const Pw& pw, con
 #pragma unroll 1
     for (int idx = tid; idx < NIN * ldm; idx += T) {
       const int q = idx / NIN, f = idx - q * NIN;
-      cp_async16(buf0 + f * fs + Pfa::spec(q), block + (long)q * sq + f);
+      cp_async16(buf0 + f * fs + S::spec(q), block + (long)q * sq + f);
     }
   }
   if (tid == 0) s_bits = 0u;
@@ -224,7 +256,7 @@ __device__ __forceinline__ void row_pfa_body(const RowArgs& a, const Pw& pw, con
       const float4* zf = reinterpret_cast<const float4*>(buf0 + f * fs);
       unsigned mx = 0u;
       for (int q = tid / NIN; q < ldm; q += QSI) {
-        const float4 w = zf[Pfa::spec(q)];
+        const float4 w = zf[S::spec(q)];
         mx = max(mx, max(__float_as_uint(w.x) & 0x7FFFFFFFu, q == 0 ? 0u : __float_as_uint(w.z) & 0x7FFFFFFFu));
       }
       if (mx) atomicMax(&s_key[f], mx);
@@ -241,28 +273,31 @@ __device__ __forceinline__ void row_pfa_body(const RowArgs& a, const Pw& pw, con
 #pragma unroll 1
     for (int idx = tid; idx < NIN * (n / 2 + 1); idx += T) {
       const int q = idx / NIN, f = idx - q * NIN;
-      pfa_pre_pair(buf0 + f * fs, q, L, f2_splat(s_qa[f]), f2_splat(s_qb[f]), twfx);
+      pfa_pre_pair<S>(buf0 + f * fs, q, L, f2_splat(s_qa[f]), f2_splat(s_qb[f]), twfx);
     }
     __syncthreads();
+    if constexpr (R0 > 1) {
 #pragma unroll 1
-    for (int idx = tid; idx < NIN * 64; idx += T) {  // radix-3 across the blocks (no twiddles)
-      cfx* z = buf0 + (idx >> 6) * fs + (idx & 63);
-      cfx v[3] = {z[0], z[64], z[128]};
-      butterfly_fx<true, 3>(v, kc);
-      z[0] = v[0];
-      z[64] = v[1];
-      z[128] = v[2];
+      for (int idx = tid; idx < NIN * P; idx += T) {  // radix-R0 across the blocks (no twiddles)
+        cfx* z = buf0 + (idx / P) * fs + (idx & (P - 1));
+        cfx v[R0];
+#pragma unroll
+        for (int r = 0; r < R0; ++r) v[r] = z[r * P];
+        butterfly_fx<true, R0>(v, kc);
+#pragma unroll
+        for (int r = 0; r < R0; ++r) z[r * P] = v[r];
+      }
+      __syncthreads();
     }
+    pfa_pass<S, true, true, false, NIN>(buf0, twfx, kc, nullptr, nullptr);
     __syncthreads();
-    pfa_pass<true, 1, false, NIN>(buf0, twfx, kc, nullptr, nullptr);
-    __syncthreads();
-    pfa_pass<true, 8, false, NIN>(buf0, twfx, kc, nullptr, nullptr);
+    pfa_pass<S, true, false, false, NIN>(buf0, twfx, kc, nullptr, nullptr);
     __syncthreads();
   } else {
     df* x0 = reinterpret_cast<df*>(buf0);
     for (int idx = tid; idx < NIN * N; idx += T) {
       const int f = idx / N, k = idx - f * N;
-      x0[2 * (f * fs + Pfa::grid(k >> 1)) + (k & 1)] =
+      x0[2 * (f * fs + S::grid(k >> 1)) + (k & 1)] =
           df_from_double(a.gin[(long)b * a.gin_b + (long)f * a.gin_f + (long)j * N + k]);
     }
     __syncthreads();
@@ -287,7 +322,7 @@ __device__ __forceinline__ void row_pfa_body(const RowArgs& a, const Pw& pw, con
       }
     }
     auto single = [&](int k) {
-      const int slot = 2 * Pfa::grid(k >> 1) + (k & 1);
+      const int slot = 2 * S::grid(k >> 1) + (k & 1);
       const long long* xi = reinterpret_cast<const long long*>(buf0);
       const df* xd = reinterpret_cast<const df*>(buf0);
       df* xo = reinterpret_cast<df*>(buf0);
@@ -304,10 +339,9 @@ __device__ __forceinline__ void row_pfa_body(const RowArgs& a, const Pw& pw, con
       }
     };
     if constexpr (kPairs) {
-      // slots 0 .. T-1 as pairs of grid points, the remaining 2 (n - T)
-      // points one per thread
-      {
-        const int s = Pfa::grid(tid);
+#pragma unroll 1
+      for (int i = tid; i < (kSplitTail ? T : n); i += T) {
+        const int s = S::grid(i);
         df2 in[NIN], out[NOUT];
 #pragma unroll
         for (int f = 0; f < NIN; ++f) {
@@ -330,10 +364,10 @@ __device__ __forceinline__ void row_pfa_body(const RowArgs& a, const Pw& pw, con
           omax[f] = max(omax[f], max(__float_as_uint(x0.hi) & 0x7FFFFFFFu, __float_as_uint(x1.hi) & 0x7FFFFFFFu));
         }
       }
-      single(2 * T + tid);
+      if constexpr (kSplitTail) single(2 * T + tid);
     } else {
 #pragma unroll 1
-      for (int it = 0; it < N / T; ++it) single(tid + it * T);
+      for (int k = tid; k < N; k += T) single(k);
     }
     if (a.status && bits) atomicOr(&s_bits, bits);
     if constexpr (OUT_MODE == kOutG) {
@@ -354,7 +388,7 @@ __device__ __forceinline__ void row_pfa_body(const RowArgs& a, const Pw& pw, con
     for (int idx = tid; idx < NOUT * N; idx += T) {
       const int f = idx / N, k = idx - f * N;
       a.gout[(long)b * a.gout_b + (long)f * a.gout_f + (long)j * N + k] =
-          df_to_double(xo[2 * (f * fs + Pfa::grid(k >> 1)) + (k & 1)]);
+          df_to_double(xo[2 * (f * fs + S::grid(k >> 1)) + (k & 1)]);
     }
   } else {
     if (tid < NOUT) {  // output block exponents (|X| < 2^hb)
@@ -364,47 +398,50 @@ __device__ __forceinline__ void row_pfa_body(const RowArgs& a, const Pw& pw, con
       fx_pow2_split(-S, s_pa[tid], s_pb[tid]);
     }
     __syncthreads();
-    pfa_pass<false, 8, true, NOUT>(buf0, twfx, kc, s_pa, s_pb);
+    pfa_pass<S, false, false, true, NOUT>(buf0, twfx, kc, s_pa, s_pb);
     __syncthreads();
-    pfa_pass<false, 1, false, NOUT>(buf0, twfx, kc, nullptr, nullptr);
+    pfa_pass<S, false, true, false, NOUT>(buf0, twfx, kc, nullptr, nullptr);
     __syncthreads();
-    // radix-3 across the blocks for the groups of c and 64 - c (item 0: 0
-    // and 32), then the real-FFT post-processing of their six orders
+    // radix-R0 across the blocks for the order groups c + jP and P - c + jP
+    // (item 0: the self-paired groups 0 and P/2), then the real-FFT
+    // post-processing of their 2 R0 orders (partners n - q in the same item)
 #pragma unroll 1
-    for (int idx = tid; idx < NOUT * 32; idx += T) {
+    for (int idx = tid; idx < NOUT * (P / 2); idx += T) {
       const int c = idx / NOUT, f = idx - c * NOUT;
       const int e = s_in[f] - 1;  // R2 / 2 in units of 2^S
       cfx* Z = buf0 + f * fs;
-      const int g1 = c == 0 ? 32 : 64 - c;
+      const int g1 = c == 0 ? P / 2 : P - c;
+      if constexpr (R0 > 1) {
 #pragma unroll 1
-      for (int g = 0; g < 2; ++g) {
-        const int u = Pfa::upos(g == 0 ? c : g1);
-        cfx v[3] = {Z[u], Z[64 + u], Z[128 + u]};
-        butterfly_fx<false, 3>(v, kc);
-        Z[u] = v[0];
-        Z[64 + u] = v[1];
-        Z[128 + u] = v[2];
+        for (int g = 0; g < 2; ++g) {
+          cfx* z = Z + S::upos(g == 0 ? c : g1);
+          cfx v[R0];
+#pragma unroll
+          for (int r = 0; r < R0; ++r) v[r] = z[r * P];
+          butterfly_fx<false, R0>(v, kc);
+#pragma unroll
+          for (int r = 0; r < R0; ++r) z[r * P] = v[r];
+        }
       }
 #pragma unroll 1
-      for (int p = 0; p < 6; ++p) {
-        const int q = c == 0 ? 32 * p
-                             : (p == 0 ? c : p == 1 ? 64 - c : p == 2 ? 64 + c : p == 3 ? 128 - c : p == 4 ? 128 + c : 192 - c);
-        if (q <= L) pfa_post(Z, q, e, twfx, oblock + (long)q * sqo + f);
+      for (int p = 0; p < 2 * R0; ++p) {
+        const int q = (p < R0 ? c : g1) + (p < R0 ? p : p - R0) * P;
+        if (q <= L) pfa_post<S>(Z, q, e, twfx, oblock + (long)q * sqo + f);
       }
     }
   }
 }
 
-template <class Pw, int IN_MODE, int OUT_MODE>
+template <class Pw, int IN_MODE, int OUT_MODE, class S>
 __global__ void __launch_bounds__(kPfaThreads, 6) row_kernel_pfa(RowArgs a, Pw pw, const FxW* __restrict__ twfx,
                                                                  FxConst kc) {
-  row_pfa_body<Pw, IN_MODE, OUT_MODE>(a, pw, twfx, kc, blockIdx.x, blockIdx.y);
+  row_pfa_body<Pw, IN_MODE, OUT_MODE, S>(a, pw, twfx, kc, blockIdx.x, blockIdx.y);
 }
 
-template <class Pw>
+template <class Pw, class S>
 constexpr size_t row_pfa_smem_bytes() {
   constexpr int NF = Pw::NIN > Pw::NOUT ? Pw::NIN : Pw::NOUT;
-  return (size_t)NF * Pfa::fs * sizeof(cfx);
+  return (size_t)NF * S::fs * sizeof(cfx);
 }
 
 }  // namespace aeolus
