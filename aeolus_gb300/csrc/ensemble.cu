@@ -344,7 +344,9 @@ int ens_stage_m(const aeolus_ensemble_s* E, double2* const* y0, int stage, doubl
     row_args(p, ra);
     if (E->split) ra.fft = p->fftx;
     const int kind = E->split ? split_row_kind(p) : kRowsRuntime;
-    grouped_add(gr, RowArg<Pw>{ra, pws[k], p->twfx, p->twdf, kind}, dim3(p->nlat, E->batch[k]));
+    const bool pfa = kind >= kRowsPfa192;
+    grouped_add(gr, RowArg<Pw>{ra, pws[k], p->twfx, p->twdf, kind},
+                pfa ? row_pfa_grid<Pw>(p->nlat, E->batch[k]) : dim3(p->nlat, E->batch[k]));
     sm_rows = std::max(sm_rows, E->split ? split_row_smem_bytes<Pw>(p) : row_smem_bytes<Pw>(p->fft));
     row_thr = std::max(row_thr, row_threads(p));
     if (kind != kRowsRuntime) fixed_thr = true;

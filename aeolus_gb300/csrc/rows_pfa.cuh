@@ -53,7 +53,7 @@ struct PfaShape {
   static constexpr int R0 = R0_, R1 = R1_, R2 = R2_, P = R1 * R2, n = R0 * P, N = 2 * n, fs = n + 1;
   static constexpr int hb = 56 - pfa_ceil_log2(n) < 52 ? 56 - pfa_ceil_log2(n) : 52;  // |FFT input| < 2^hb
   static constexpr int Pinv = pfa_inv_mod(P, R0), R0inv = pfa_inv_mod(R0, P);
-  static_assert(P == 32 || P == 64, "P-point transforms of 32 or 64 points");
+  static_assert(R2 == 8 && (R1 == 4 || R1 == 8), "P-point transforms of 4 x 8 or 8 x 8 points");
   static_assert(R0 == 1 || R0 == 3 || R0 == 5, "radix-R0 pass of 1, 3 or 5");
   static __device__ __forceinline__ int sw(int u) { return (u & ~7) | ((u ^ (u >> 3)) & 7); }
   static __device__ __forceinline__ int upos(int q) {
@@ -123,14 +123,14 @@ struct PwHasPairs : std::false_type {};
 template <class Pw>
 struct PwHasPairs<Pw, std::void_t<decltype(&Pw::df_op2)>> : std::true_type {};
 
-// One pass over the P-point blocks of NFLD fields.  PASS1: R1 butterflies
+// One pass over the P-point blocks of NFLD (member row, field) pairs.  PASS1: R1 butterflies
 // of radix R2 over R2 consecutive positions, no twiddles; otherwise R2
 // butterflies of radix R1 at stride R2 with the twiddles w_P^(a k) before
 // the butterfly (inverse, DIT) or after it (forward, DIF).  The inverse runs
 // PASS1 then the strided pass, the forward the strided pass then PASS1.
 // CONV: the rows still hold double-floats, rounded to the field's fixed-
 // point scale (pa pb = 2^-S) as they are loaded.
-template <class S, bool INV, bool PASS1, bool CONV, int NFLD>
+template <class S, bool INV, bool PASS1, bool CONV, int NFLD, int NPER, int RS>
 __device__ __forceinline__ void pfa_pass(cfx* __restrict__ x, const FxW* __restrict__ tw, const FxConst& kc,
                                          const float* sqa, const float* sqb) {
   constexpr int R = PASS1 ? S::R2 : S::R1;        // butterfly radix
@@ -138,9 +138,11 @@ __device__ __forceinline__ void pfa_pass(cfx* __restrict__ x, const FxW* __restr
   constexpr int TWS = 2 * S::R0;                  // w_P = w_N^(N / P)
 #pragma unroll 1
   for (int idx = threadIdx.x; idx < NFLD * S::R0 * NB; idx += kPfaThreads) {
+    // f: (member row, field) pair, NPER fields of each row's RS slots
     const int f = idx / (S::R0 * NB), rem = idx - f * (S::R0 * NB), r = rem / NB, k = rem - r * NB;
-    cfx* y = x + f * S::fs + r * S::P;
-    auto pos = [&](int t) { return S::sw(PASS1 ? S::R2 * k + t : S::R2 * t + k); };
+    cfx* y = x + (NFLD == NPER ? f * S::fs : (f / NPER) * RS + (f % NPER) * S::fs) + r * S::P;
+    // swizzled positions, R2 = 8: sw(8k + t) = 8k + (t ^ k), sw(8t + k) = 8t + (k ^ t)
+    auto pos = [&](int t) { return PASS1 ? 8 * k + (t ^ k) : 8 * t + (k ^ t); };
     cfx v[R];
     if constexpr (CONV) {
       const f2 pa = f2_splat(sqa[f]), pb = f2_splat(sqb[f]);
@@ -198,47 +200,66 @@ __device__ __forceinline__ void pfa_post(const cfx* Z, int q, int e, const FxW* 
   *out = make_longlong2(pk_pack(R2.re, e), pk_pack(R2.im, e));
 }
 
+// Member rows per CTA: functors with few fields take several members of
+// the same latitude row per CTA, so every phase still has work for the 128
+// threads (and the shared memory stays within the 1-row SWE footprint).
+template <class Pw>
+constexpr int pfa_rows_per_cta() {
+  constexpr int NF = Pw::NIN > Pw::NOUT ? Pw::NIN : Pw::NOUT;
+  return NF >= 5 ? 1 : NF >= 3 ? 2 : NF == 2 ? 4 : 8;
+}
+
 template <class Pw, int IN_MODE, int OUT_MODE, class S>
 __device__ __forceinline__ void row_pfa_body(const RowArgs& a, const Pw& pw, const FxW* __restrict__ twfx,
                                              const FxConst& kc, int bx, int by) {
   constexpr int NIN = Pw::NIN, NOUT = Pw::NOUT;
   constexpr int NF = NIN > NOUT ? NIN : NOUT;
+  constexpr int NR = pfa_rows_per_cta<Pw>();
+  constexpr int NRI = NR * NIN, NRO = NR * NOUT;  // (member row, field) pairs in and out
   constexpr int n = S::n, N = S::N, fs = S::fs, hb = S::hb, P = S::P, R0 = S::R0, T = kPfaThreads;
-  constexpr int PSI = (T / NIN) * NIN, QSI = T / NIN;
+  constexpr int RS = NF * fs;  // slots of one member row
+  constexpr int PSI = (T / NRI) * NRI, QSI = T / NRI;
+  static_assert(NRI <= T && NRO <= T, "one thread per (row, field) for the block exponents");
   constexpr bool kPairs = PwHasPairs<Pw>::value;
-  // pointwise: slot pairs in rounds of T, and for n = 3T/2 the last T/2
+  // pointwise: slot pairs in rounds of T, and for NR n = 3T/2 the last T/2
   // slots as one single point per thread
-  constexpr bool kSplitTail = n - T == T / 2;
+  constexpr bool kSplitTail = NR * n - T == T / 2;
   extern __shared__ cfx smem_fx[];
-  __shared__ unsigned s_bits;
-  __shared__ int s_in[NF];        // block exponents (inputs, then outputs)
-  __shared__ unsigned s_key[NF];  // largest |hi| bit key of each input field
-  __shared__ unsigned s_omax[NF]; // largest |hi| bit key of each output field
-  __shared__ float s_pa[NF], s_pb[NF], s_qa[NF], s_qb[NF];
+  __shared__ unsigned s_bits[NR];
+  __shared__ int s_in[NR * NF];        // block exponents (inputs, then outputs)
+  __shared__ unsigned s_key[NR * NF];  // largest |hi| bit key of each input field
+  __shared__ unsigned s_omax[NR * NF]; // largest |hi| bit key of each output field
+  __shared__ float s_pa[NR * NF], s_pb[NR * NF], s_qa[NR * NF], s_qb[NR * NF];
   __shared__ RowDf s_rc;
   __shared__ df s_wj;
-  const int j = bx, b = by, tid = threadIdx.x;
+  const int j = bx, b0 = NR * by, tid = threadIdx.x;
+  const int nrow = min(NR, a.batch - b0);  // members of this CTA
   const int L = a.L, ldm = L + 1;
   cfx* buf0 = smem_fx;
+  // (member row, field) -> its row buffer
+  auto zrow = [&](int row, int f) { return buf0 + row * RS + f * fs; };
   const long sq = (long)a.nblk * a.nlat;
+  const long bsi = (long)ldm * a.nlat * a.nblk;  // member stride of the F blocks
   const float4* block = nullptr;
   if (IN_MODE == kInF || OUT_MODE == kOutG)
-    block = reinterpret_cast<const float4*>(a.FG) + fg_index(b, 0, 0, j, L, a.nblk, a.nlat);
+    block = reinterpret_cast<const float4*>(a.FG) + fg_index(b0, 0, 0, j, L, a.nblk, a.nlat);
   const long sqo = a.G ? (long)a.gblk * a.nlat : sq;
+  const long bso = a.G ? (long)ldm * a.nlat * a.gblk : bsi;
   longlong2* oblock = nullptr;
   if (OUT_MODE == kOutG)
-    oblock = a.G ? reinterpret_cast<longlong2*>(a.G) + fg_index(b, 0, 0, j, L, a.gblk, a.nlat)
+    oblock = a.G ? reinterpret_cast<longlong2*>(a.G) + fg_index(b0, 0, 0, j, L, a.gblk, a.nlat)
                  : reinterpret_cast<longlong2*>(const_cast<float4*>(block));
   if constexpr (IN_MODE == kInF) {
     // stage F[q][f] at slot spec(q) of field f, fields fastest (coalesced)
 #pragma unroll 1
-    for (int idx = tid; idx < NIN * ldm; idx += T) {
-      const int q = idx / NIN, f = idx - q * NIN;
-      cp_async16(buf0 + f * fs + S::spec(q), block + (long)q * sq + f);
+    for (int idx = tid; idx < NRI * ldm; idx += T) {
+      const int row = NR == 1 ? 0 : idx / (NIN * ldm), rem = idx - row * (NIN * ldm);
+      const int q = rem / NIN, f = rem - q * NIN;
+      if (row < nrow) cp_async16(zrow(row, f) + S::spec(q), block + row * bsi + (long)q * sq + f);
     }
   }
-  if (tid == 0) s_bits = 0u;
-  if (tid < NF) {
+  if (tid < NR) s_bits[tid] = 0u;
+  if (tid < NR * NF) {
     s_key[tid] = 0u;
     s_omax[tid] = 0u;
   }
@@ -251,35 +272,39 @@ __device__ __forceinline__ void row_pfa_body(const RowArgs& a, const Pw& pw, con
 
   // ---- 1. grid rows of the inputs
   if constexpr (IN_MODE == kInF) {
-    if (tid < PSI) {  // largest |hi| per field (m = 0: Im dropped)
-      const int f = tid % NIN;
-      const float4* zf = reinterpret_cast<const float4*>(buf0 + f * fs);
+    if (tid < PSI) {  // largest |hi| per (row, field) (m = 0: Im dropped)
+      const int rf = tid % NRI, row = NR == 1 ? 0 : rf / NIN, f = rf - row * NIN;
+      const float4* zf = reinterpret_cast<const float4*>(zrow(row, f));
       unsigned mx = 0u;
-      for (int q = tid / NIN; q < ldm; q += QSI) {
-        const float4 w = zf[S::spec(q)];
-        mx = max(mx, max(__float_as_uint(w.x) & 0x7FFFFFFFu, q == 0 ? 0u : __float_as_uint(w.z) & 0x7FFFFFFFu));
-      }
-      if (mx) atomicMax(&s_key[f], mx);
+      if (row < nrow)
+        for (int q = tid / NRI; q < ldm; q += QSI) {
+          const float4 w = zf[S::spec(q)];
+          mx = max(mx, max(__float_as_uint(w.x) & 0x7FFFFFFFu, q == 0 ? 0u : __float_as_uint(w.z) & 0x7FFFFFFFu));
+        }
+      if (mx) atomicMax(&s_key[row * NF + f], mx);
     }
     __syncthreads();
-    if (tid < NIN) {  // block exponent: |F| < 2^E -> |X| < 2^hb
-      const unsigned key = s_key[tid];
-      const int S = (key >> 23) == 0 ? 0 : fkey_exp(key) - hb;
-      s_in[tid] = S;
-      fx_pow2_split(S, s_pa[tid], s_pb[tid]);
-      fx_pow2_split(-S, s_qa[tid], s_qb[tid]);
+    if (tid < NRI) {  // block exponent: |F| < 2^E -> |X| < 2^hb
+      const int row = tid / NIN, f = tid - row * NIN, i = row * NF + f;
+      const unsigned key = s_key[i];
+      const int S0 = (key >> 23) == 0 ? 0 : fkey_exp(key) - hb;
+      s_in[i] = S0;
+      fx_pow2_split(S0, s_pa[i], s_pb[i]);
+      fx_pow2_split(-S0, s_qa[i], s_qb[i]);
     }
     __syncthreads();
 #pragma unroll 1
-    for (int idx = tid; idx < NIN * (n / 2 + 1); idx += T) {
-      const int q = idx / NIN, f = idx - q * NIN;
-      pfa_pre_pair<S>(buf0 + f * fs, q, L, f2_splat(s_qa[f]), f2_splat(s_qb[f]), twfx);
+    for (int idx = tid; idx < NRI * (n / 2 + 1); idx += T) {
+      const int q = idx / NRI, rf = idx - q * NRI, row = NR == 1 ? 0 : rf / NIN, f = rf - row * NIN;
+      pfa_pre_pair<S>(zrow(row, f), q, row < nrow ? L : -1, f2_splat(s_qa[row * NF + f]), f2_splat(s_qb[row * NF + f]),
+                      twfx);
     }
     __syncthreads();
     if constexpr (R0 > 1) {
 #pragma unroll 1
-      for (int idx = tid; idx < NIN * P; idx += T) {  // radix-R0 across the blocks (no twiddles)
-        cfx* z = buf0 + (idx / P) * fs + (idx & (P - 1));
+      for (int idx = tid; idx < NRI * P; idx += T) {  // radix-R0 across the blocks (no twiddles)
+        const int rf = idx / P, row = NR == 1 ? 0 : rf / NIN, f = rf - row * NIN;
+        cfx* z = zrow(row, f) + (idx & (P - 1));
         cfx v[R0];
 #pragma unroll
         for (int r = 0; r < R0; ++r) v[r] = z[r * P];
@@ -289,47 +314,78 @@ __device__ __forceinline__ void row_pfa_body(const RowArgs& a, const Pw& pw, con
       }
       __syncthreads();
     }
-    pfa_pass<S, true, true, false, NIN>(buf0, twfx, kc, nullptr, nullptr);
+    pfa_pass<S, true, true, false, NRI, NIN, RS>(buf0, twfx, kc, nullptr, nullptr);
     __syncthreads();
-    pfa_pass<S, true, false, false, NIN>(buf0, twfx, kc, nullptr, nullptr);
+    pfa_pass<S, true, false, false, NRI, NIN, RS>(buf0, twfx, kc, nullptr, nullptr);
     __syncthreads();
   } else {
-    df* x0 = reinterpret_cast<df*>(buf0);
-    for (int idx = tid; idx < NIN * N; idx += T) {
-      const int f = idx / N, k = idx - f * N;
-      x0[2 * (f * fs + S::grid(k >> 1)) + (k & 1)] =
-          df_from_double(a.gin[(long)b * a.gin_b + (long)f * a.gin_f + (long)j * N + k]);
+#pragma unroll 1
+    for (int idx = tid; idx < NRI * N; idx += T) {
+      const int rf = idx / N, k = idx - rf * N, row = rf / NIN, f = rf - row * NIN;
+      if (row < nrow)
+        reinterpret_cast<df*>(zrow(row, f))[2 * S::grid(k >> 1) + (k & 1)] =
+            df_from_double(a.gin[(long)(b0 + row) * a.gin_b + (long)f * a.gin_f + (long)j * N + k]);
     }
     __syncthreads();
   }
 
   // ---- 2. pointwise products, weighted by the row's quadrature weight; in
-  // place (each point is read before it is written, by one thread)
+  // place (each point is read before it is written, by one thread).  A
+  // warp's points in one round lie in one member row (n and N are
+  // multiples of 32).
   {
     const RowDf rc = s_rc;
     const df wj = s_wj;
     const bool wq = OUT_MODE == kOutG && a.wq != nullptr;
-    unsigned bits = 0u;
     unsigned omax[NOUT];
 #pragma unroll
     for (int f = 0; f < NOUT; ++f) omax[f] = 0u;
-    float pa[NIN], pb[NIN];
-    if constexpr (IN_MODE == kInF) {
+    unsigned bits = 0u;
+    int orow = -1;  // member row of omax and bits (NR > 1: flushed when the row changes)
+    auto flush = [&]() {
+      if (orow < 0) return;
+      if (a.status && bits && (NR == 1 || orow < nrow)) atomicOr(&s_bits[orow], bits);
+      bits = 0u;
+      if constexpr (OUT_MODE == kOutG) {
+#pragma unroll
+        for (int f = 0; f < NOUT; ++f) {
+          unsigned v = omax[f];
+          for (int o = 16; o > 0; o >>= 1) v = max(v, __shfl_xor_sync(0xffffffffu, v, o));
+          if ((tid & 31) == 0 && v && (NR == 1 || orow < nrow)) atomicMax(&s_omax[orow * NF + f], v);
+          omax[f] = 0u;
+        }
+      }
+    };
+    auto at_row = [&](int row) {
+      if (NR > 1 && row != orow) {
+        flush();
+        orow = row;
+      }
+      if (NR == 1) orow = 0;
+    };
+    // input scales of a one-row CTA in registers
+    float pa1[NIN], pb1[NIN];
+    if constexpr (NR == 1 && IN_MODE == kInF) {
 #pragma unroll
       for (int f = 0; f < NIN; ++f) {
-        pa[f] = s_pa[f];
-        pb[f] = s_pb[f];
+        pa1[f] = s_pa[f];
+        pb1[f] = s_pb[f];
       }
     }
-    auto single = [&](int k) {
-      const int slot = 2 * S::grid(k >> 1) + (k & 1);
-      const long long* xi = reinterpret_cast<const long long*>(buf0);
-      const df* xd = reinterpret_cast<const df*>(buf0);
-      df* xo = reinterpret_cast<df*>(buf0);
+    auto spa = [&](int row, int f) { return NR == 1 ? pa1[f] : s_pa[row * NF + f]; };
+    auto spb = [&](int row, int f) { return NR == 1 ? pb1[f] : s_pb[row * NF + f]; };
+    auto single = [&](int k) {  // real grid point k of the CTA's rows
+      const int row = NR == 1 ? 0 : k / N, kk = k - row * N;
+      at_row(row);
+      const int slot = 2 * S::grid(kk >> 1) + (kk & 1);
+      cfx* zb = zrow(row, 0);
+      const long long* xi = reinterpret_cast<const long long*>(zb);
+      const df* xd = reinterpret_cast<const df*>(zb);
+      df* xo = reinterpret_cast<df*>(zb);
       df in[NIN], out[NOUT];
 #pragma unroll
       for (int f = 0; f < NIN; ++f)
-        in[f] = IN_MODE == kInF ? fx_to_df(xi[2 * f * fs + slot], pa[f], pb[f]) : xd[2 * f * fs + slot];
+        in[f] = IN_MODE == kInF ? fx_to_df(xi[2 * f * fs + slot], spa(row, f), spb(row, f)) : xd[2 * f * fs + slot];
       bits |= pw.df_op(rc, in, out);
 #pragma unroll
       for (int f = 0; f < NOUT; ++f) {
@@ -340,16 +396,19 @@ __device__ __forceinline__ void row_pfa_body(const RowArgs& a, const Pw& pw, con
     };
     if constexpr (kPairs) {
 #pragma unroll 1
-      for (int i = tid; i < (kSplitTail ? T : n); i += T) {
-        const int s = S::grid(i);
+      for (int i = tid; i < (kSplitTail ? T : NR * n); i += T) {
+        const int row = NR == 1 ? 0 : i / n, ii = i - row * n;
+        at_row(row);
+        const int s = S::grid(ii);
+        cfx* zb = zrow(row, 0);
         df2 in[NIN], out[NOUT];
 #pragma unroll
         for (int f = 0; f < NIN; ++f) {
           if constexpr (IN_MODE == kInF) {
-            const cfx X = buf0[f * fs + s];
-            in[f] = fx_to_df2(X.re, X.im, f2_splat(pa[f]), f2_splat(pb[f]));
+            const cfx X = zb[f * fs + s];
+            in[f] = fx_to_df2(X.re, X.im, f2_splat(spa(row, f)), f2_splat(spb(row, f)));
           } else {
-            const float4 w = reinterpret_cast<const float4*>(buf0)[f * fs + s];
+            const float4 w = reinterpret_cast<const float4*>(zb)[f * fs + s];
             in[f] = df2{f2_pack(w.x, w.z), f2_pack(w.y, w.w)};
           }
         }
@@ -360,56 +419,50 @@ __device__ __forceinline__ void row_pfa_body(const RowArgs& a, const Pw& pw, con
           if (wq) out[f] = df2_mul(out[f], wj2);
           df x0, x1;
           df2_unpack(out[f], x0, x1);
-          reinterpret_cast<float4*>(buf0)[f * fs + s] = make_float4(x0.hi, x0.lo, x1.hi, x1.lo);
+          reinterpret_cast<float4*>(zb)[f * fs + s] = make_float4(x0.hi, x0.lo, x1.hi, x1.lo);
           omax[f] = max(omax[f], max(__float_as_uint(x0.hi) & 0x7FFFFFFFu, __float_as_uint(x1.hi) & 0x7FFFFFFFu));
         }
       }
       if constexpr (kSplitTail) single(2 * T + tid);
     } else {
 #pragma unroll 1
-      for (int k = tid; k < N; k += T) single(k);
+      for (int k = tid; k < NR * N; k += T) single(k);
     }
-    if (a.status && bits) atomicOr(&s_bits, bits);
-    if constexpr (OUT_MODE == kOutG) {
-#pragma unroll
-      for (int f = 0; f < NOUT; ++f) {
-        unsigned v = omax[f];
-        for (int o = 16; o > 0; o >>= 1) v = max(v, __shfl_xor_sync(0xffffffffu, v, o));
-        if ((tid & 31) == 0 && v) atomicMax(&s_omax[f], v);
-      }
-    }
+    flush();
   }
   __syncthreads();
-  if (a.status && tid == 0 && s_bits) atomicOr(&a.status[b], s_bits);
+  if (a.status && tid < nrow && s_bits[tid]) atomicOr(&a.status[b0 + tid], s_bits[tid]);
 
   // ---- 3. outputs
   if constexpr (OUT_MODE == kOutGrid) {
-    const df* xo = reinterpret_cast<const df*>(buf0);
-    for (int idx = tid; idx < NOUT * N; idx += T) {
-      const int f = idx / N, k = idx - f * N;
-      a.gout[(long)b * a.gout_b + (long)f * a.gout_f + (long)j * N + k] =
-          df_to_double(xo[2 * (f * fs + S::grid(k >> 1)) + (k & 1)]);
+#pragma unroll 1
+    for (int idx = tid; idx < NRO * N; idx += T) {
+      const int rf = idx / N, k = idx - rf * N, row = rf / NOUT, f = rf - row * NOUT;
+      if (row < nrow)
+        a.gout[(long)(b0 + row) * a.gout_b + (long)f * a.gout_f + (long)j * N + k] =
+            df_to_double(reinterpret_cast<const df*>(zrow(row, f))[2 * S::grid(k >> 1) + (k & 1)]);
     }
   } else {
-    if (tid < NOUT) {  // output block exponents (|X| < 2^hb)
-      const unsigned key = s_omax[tid];
-      const int S = (key >> 23) == 0 ? 0 : fkey_exp(key) - hb;
-      s_in[tid] = S;
-      fx_pow2_split(-S, s_pa[tid], s_pb[tid]);
+    if (tid < NRO) {  // output block exponents (|X| < 2^hb)
+      const int row = tid / NOUT, f = tid - row * NOUT, i = row * NF + f;
+      const unsigned key = s_omax[i];
+      const int S0 = (key >> 23) == 0 ? 0 : fkey_exp(key) - hb;
+      s_in[i] = S0;
+      fx_pow2_split(-S0, s_pa[tid], s_pb[tid]);  // indexed by (row, output field) for the passes
     }
     __syncthreads();
-    pfa_pass<S, false, false, true, NOUT>(buf0, twfx, kc, s_pa, s_pb);
+    pfa_pass<S, false, false, true, NRO, NOUT, RS>(buf0, twfx, kc, s_pa, s_pb);
     __syncthreads();
-    pfa_pass<S, false, true, false, NOUT>(buf0, twfx, kc, nullptr, nullptr);
+    pfa_pass<S, false, true, false, NRO, NOUT, RS>(buf0, twfx, kc, nullptr, nullptr);
     __syncthreads();
     // radix-R0 across the blocks for the order groups c + jP and P - c + jP
     // (item 0: the self-paired groups 0 and P/2), then the real-FFT
     // post-processing of their 2 R0 orders (partners n - q in the same item)
 #pragma unroll 1
-    for (int idx = tid; idx < NOUT * (P / 2); idx += T) {
-      const int c = idx / NOUT, f = idx - c * NOUT;
-      const int e = s_in[f] - 1;  // R2 / 2 in units of 2^S
-      cfx* Z = buf0 + f * fs;
+    for (int idx = tid; idx < NRO * (P / 2); idx += T) {
+      const int c = idx / NRO, rf = idx - c * NRO, row = NR == 1 ? 0 : rf / NOUT, f = rf - row * NOUT;
+      const int e = s_in[row * NF + f] - 1;  // R2 / 2 in units of 2^S
+      cfx* Z = zrow(row, f);
       const int g1 = c == 0 ? P / 2 : P - c;
       if constexpr (R0 > 1) {
 #pragma unroll 1
@@ -423,10 +476,13 @@ __device__ __forceinline__ void row_pfa_body(const RowArgs& a, const Pw& pw, con
           for (int r = 0; r < R0; ++r) z[r * P] = v[r];
         }
       }
+      if (row < nrow) {
+        longlong2* ob = oblock + row * bso + f;
 #pragma unroll 1
-      for (int p = 0; p < 2 * R0; ++p) {
-        const int q = (p < R0 ? c : g1) + (p < R0 ? p : p - R0) * P;
-        if (q <= L) pfa_post<S>(Z, q, e, twfx, oblock + (long)q * sqo + f);
+        for (int p = 0; p < 2 * R0; ++p) {
+          const int q = (p < R0 ? c : g1) + (p < R0 ? p : p - R0) * P;
+          if (q <= L) pfa_post<S>(Z, q, e, twfx, ob + (long)q * sqo);
+        }
       }
     }
   }
@@ -441,7 +497,13 @@ __global__ void __launch_bounds__(kPfaThreads, 6) row_kernel_pfa(RowArgs a, Pw p
 template <class Pw, class S>
 constexpr size_t row_pfa_smem_bytes() {
   constexpr int NF = Pw::NIN > Pw::NOUT ? Pw::NIN : Pw::NOUT;
-  return (size_t)NF * S::fs * sizeof(cfx);
+  return (size_t)pfa_rows_per_cta<Pw>() * NF * S::fs * sizeof(cfx);
+}
+// Grid of a prime-factor row launch: (latitude rows, member groups).
+template <class Pw>
+inline dim3 row_pfa_grid(int nlat, int batch) {
+  constexpr int NR = pfa_rows_per_cta<Pw>();
+  return dim3(nlat, (batch + NR - 1) / NR);
 }
 
 }  // namespace aeolus
