@@ -308,7 +308,7 @@ __device__ __forceinline__ void split_synth_slice_body(const SplitDims& dm, cons
 }
 
 template <class Derive>
-__global__ void __launch_bounds__(256, 3) split_synth_slice_kernel(SplitDims dm, const long long* __restrict__ kcum,
+__global__ void __launch_bounds__(256, 4) split_synth_slice_kernel(SplitDims dm, const long long* __restrict__ kcum,
                                                                int batch, int mb, Derive der,
                                                                __nv_bfloat16* __restrict__ dsyn,
                                                                int* __restrict__ ecol) {
@@ -909,12 +909,12 @@ inline size_t split_anal_bytes(const aeolus_plan_impl* p, int nf, int batch) {
          align256((size_t)(d.L + 1) * d.ntiles * kNT * 4);
 }
 
-inline int slice_members(int nf, int K, int tuned) {
+inline int slice_members(int nf, int K, int tuned, int cap_bytes = 64 * 1024) {
   // members per slicing CTA: at most 256 columns (the exponent array) and the
-  // staged values within 64 KB, or the tuned count within 160 KB
+  // staged values within cap_bytes, or the tuned count within 160 KB
   const int cap_cols = std::max(1, 256 / (2 * nf));
   if (tuned > 0) return std::max(1, std::min({tuned, cap_cols, (160 * 1024) / (2 * nf * K * 8)}));
-  return std::max(1, std::min(cap_cols, (64 * 1024) / (2 * nf * K * 8)));
+  return std::max(1, std::min(cap_cols, cap_bytes / (2 * nf * K * 8)));
 }
 
 // Scratch carving and slicing shapes of the two split stages.
@@ -935,7 +935,8 @@ SplitParts split_synth_parts(const aeolus_plan_impl* p, int batch, void* scratch
   r.digits = reinterpret_cast<__nv_bfloat16*>(w);
   w += align256((size_t)p->split->h_kcum[r.dm.L + 1] * r.dm.ntiles * kSlices * kNT * 2);
   r.ecol = reinterpret_cast<int*>(w);
-  r.mb = slice_members(NF, r.dm.L + 2, p->tune_slice_mb);
+  // 32 KB of staged values: four 256-thread CTAs per SM (64 registers each)
+  r.mb = slice_members(NF, r.dm.L + 2, p->tune_slice_mb, 32 * 1024);
   r.smem = (size_t)r.mb * NF * 2 * ((r.dm.L + 1) | 1) * 8;
   r.grid = dim3(r.dm.L + 1, (batch + r.mb - 1) / r.mb);
   return r;
