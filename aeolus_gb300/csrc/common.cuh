@@ -5,6 +5,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 #include <string>
+#include <utility>
 #include <vector>
 
 #include "../../include/aeolus_gb300.h"
@@ -19,6 +20,33 @@ int fail(int code, const std::string& msg);
 int cuda_check(cudaError_t e, const char* what);
 #define AE_CUDA(call) do { int _s = ::aeolus::cuda_check((call), #call); if (_s) return _s; } while (0)
 #define AE_LAUNCH(what) do { int _s = ::aeolus::cuda_check(cudaGetLastError(), what); if (_s) return _s; } while (0)
+
+// ---------------------------------------- programmatic dependent launch
+// The split-precision stage kernels are launched with programmatic stream
+// serialisation: a kernel's CTAs may be scheduled while the previous kernel
+// in the stream drains (each CTA of a kernel triggers its dependents at its
+// start), and every such kernel waits (griddepcontrol.wait) for the previous
+// grid to complete, with its memory visible, before it touches global memory
+// that grid may read or write.  Only the launch and the CTA prologues
+// overlap; a kernel launched without the attribute waits for nothing.
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void pdl_trigger() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+
+template <typename... KArgs, typename... Args>
+inline cudaError_t launch_pdl(void (*kern)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t st,
+                              Args&&... args) {
+  cudaLaunchConfig_t cfg{};
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = st;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, kern, std::forward<Args>(args)...);
+}
 
 // ------------------------------------------------------------- profiling
 // Optional per-kernel CUDA-event timing (aeolus_profile_*).  When enabled,

@@ -146,7 +146,8 @@ int launch_rows_pfa(const aeolus_plan_impl* p, const Pw& pw, const RowArgs& a, c
   if (s) return s;
   ProfScope prof(IN_MODE == kInF ? (OUT_MODE == kOutG ? "rows_fx_c2r_products_r2c" : "rows_fx_c2r") : "rows_fx_r2c",
                  st);
-  kern<<<row_pfa_grid<Pw>(p->nlat, a.batch), kPfaThreads, sm, st>>>(a, pw, p->twfx, fx_consts());
+  launch_pdl(kern, row_pfa_grid<Pw>(p->nlat, a.batch), dim3(kPfaThreads), sm, st, a, pw,
+             static_cast<const FxW*>(p->twfx), fx_consts());
   AE_LAUNCH("row_kernel_pfa");
   return AEOLUS_OK;
 }

@@ -491,6 +491,8 @@ __device__ __forceinline__ void row_pfa_body(const RowArgs& a, const Pw& pw, con
 template <class Pw, int IN_MODE, int OUT_MODE, class S>
 __global__ void __launch_bounds__(kPfaThreads, 6) row_kernel_pfa(RowArgs a, Pw pw, const FxW* __restrict__ twfx,
                                                                  FxConst kc) {
+  pdl_trigger();
+  pdl_wait();
   row_pfa_body<Pw, IN_MODE, OUT_MODE, S>(a, pw, twfx, kc, blockIdx.x, blockIdx.y);
 }
 

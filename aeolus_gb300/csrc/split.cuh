@@ -312,6 +312,8 @@ __global__ void __launch_bounds__(256, 4) split_synth_slice_kernel(SplitDims dm,
                                                                int batch, int mb, Derive der,
                                                                __nv_bfloat16* __restrict__ dsyn,
                                                                int* __restrict__ ecol) {
+  pdl_trigger();
+  pdl_wait();
   split_synth_slice_body<Derive>(dm, kcum, batch, mb, der, dsyn, ecol, blockIdx.x, blockIdx.y, gridDim.y);
 }
 
@@ -383,6 +385,8 @@ __global__ void __launch_bounds__(256) split_anal_slice_kernel(SplitDims dm, int
                                                               const long long* __restrict__ FG,
                                                               __nv_bfloat16* __restrict__ dana,
                                                               int* __restrict__ ecol) {
+  pdl_trigger();
+  pdl_wait();
   split_anal_slice_body<NF>(dm, batch, mb, nblk, FG, dana, ecol, blockIdx.x, blockIdx.y, gridDim.y);
 }
 
@@ -531,6 +535,8 @@ __global__ void __launch_bounds__(tc_threads<Epi>(), 1) tc_persistent_kernel(Sch
   tc::fence_after_sync();
   const uint32_t tmem = *sm.tmem_slot;
   const int ntiles = sc.count();
+  pdl_trigger();
+  pdl_wait();  // global memory only from here on
 
   if (warp == 0) {
     if (lane == 0) {  // ---------------- producer
@@ -966,7 +972,7 @@ int launch_split_synth(const aeolus_plan_impl* p, const Derive& d, double2* FG, 
   if (s) return s;
   {
     ProfScope prof("split_synth_slice", st);
-    k1<<<r.grid, 256, r.smem, st>>>(r.dm, p->split->kcum, batch, r.mb, d, r.digits, r.ecol);
+    launch_pdl(k1, r.grid, dim3(256), r.smem, st, r.dm, p->split->kcum, batch, r.mb, d, r.digits, r.ecol);
     AE_LAUNCH("split_synth_slice_kernel");
   }
   const size_t sm2 = tc_smem_bytes();
@@ -979,7 +985,7 @@ int launch_split_synth(const aeolus_plan_impl* p, const Derive& d, double2* FG, 
   ep.ir_hi = (float)Out::ir(d);
   ep.ir_lo = (float)(Out::ir(d) - (double)ep.ir_hi);
   ProfScope prof("tc_synth_bf16x6", st);
-  k2<<<tc_grid(p, sc.count_host()), tc_threads<Epi>(), sm2, st>>>(sc, ep, p->split->err);
+  launch_pdl(k2, dim3(tc_grid(p, sc.count_host())), dim3(tc_threads<Epi>()), sm2, st, sc, ep, p->split->err);
   AE_LAUNCH("tc_synth_kernel");
   return AEOLUS_OK;
 }
@@ -994,8 +1000,8 @@ int launch_split_anal(const aeolus_plan_impl* p, const Epi& e, const double2* FG
   if (s) return s;
   {
     ProfScope prof("split_anal_slice", st);
-    k1<<<r.grid, 256, r.smem, st>>>(r.dm, batch, r.mb, nblk, reinterpret_cast<const long long*>(FG), r.digits,
-                                     r.ecol);
+    launch_pdl(k1, r.grid, dim3(256), r.smem, st, r.dm, batch, r.mb, nblk, reinterpret_cast<const long long*>(FG),
+               r.digits, r.ecol);
     AE_LAUNCH("split_anal_slice_kernel");
   }
   const size_t sm2 = tc_smem_bytes();
@@ -1004,7 +1010,7 @@ int launch_split_anal(const aeolus_plan_impl* p, const Epi& e, const double2* FG
   const AnalSched sc{r.dm, p->split->pana, r.digits};
   const AnalEpi<Epi> ep{r.dm, p->split->eana, r.ecol, batch, e};
   ProfScope prof("tc_anal_bf16x6", st);
-  k2<<<tc_grid(p, sc.count_host()), tc_threads<AnalEpi<Epi>>(), sm2, st>>>(sc, ep, p->split->err);
+  launch_pdl(k2, dim3(tc_grid(p, sc.count_host())), dim3(tc_threads<AnalEpi<Epi>>()), sm2, st, sc, ep, p->split->err);
   AE_LAUNCH("tc_anal_kernel");
   return AEOLUS_OK;
 }

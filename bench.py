@@ -654,13 +654,14 @@ def _collect_kernels(lib, _lib):
     return out
 
 
-def _timed_steps(model, y0, steps, flush, stream, lib, _lib):
+def _timed_steps(model, y0, steps, flush, stream, lib, _lib, prof_steps: int = 2):
     """K RK4 steps from y0, each bracketed by CUDA events on the launching
-    stream, L2 flushed (outside the events) before each step."""
+    stream, L2 flushed (outside the events) before each step; the library's
+    per-kernel event profile is off while they run (its events would sit
+    between the kernels) and is taken over `prof_steps` further steps from
+    the same state, which do not count."""
     import torch
     evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
-    lib.aeolus_profile_reset()
-    lib.aeolus_profile_enable(1)
     y = y0
     for i in range(steps):
         if flush is not None:
@@ -669,9 +670,18 @@ def _timed_steps(model, y0, steps, flush, stream, lib, _lib):
         y = model.rk4(y, DT, 1, check=False)
         evs[i][1].record(stream)
     torch.cuda.synchronize()
+    total = sum(a.elapsed_time(b) for a, b in evs)
+    lib.aeolus_profile_reset()
+    lib.aeolus_profile_enable(1)
+    yp = y0
+    for _ in range(prof_steps):
+        if flush is not None:
+            flush.zero_()
+        yp = model.rk4(yp, DT, 1, check=False)
+    torch.cuda.synchronize()
     lib.aeolus_profile_enable(0)
     kstats = _collect_kernels(lib, _lib)
-    return sum(a.elapsed_time(b) for a, b in evs), kstats, y
+    return total, kstats, y
 
 
 def _rel_l2_fields(a, b):
