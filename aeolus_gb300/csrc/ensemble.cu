@@ -118,6 +118,8 @@ __global__ void __launch_bounds__(256) g_rows(Grouped<RowArg<Pw>> g) {
 // kPfaThreads = kFx8Threads threads, which the launch then uses.
 template <class Pw>
 __global__ void __launch_bounds__(256, 3) g_rows_fx(Grouped<RowArg<Pw>> g, FxConst kc) {
+  pdl_trigger();
+  pdl_wait();
   const int k = g.find(blockIdx.x);
   const int loc = blockIdx.x - g.start[k];
   const RowArg<Pw>& r = g.arg[k];
@@ -135,6 +137,8 @@ __global__ void __launch_bounds__(256, 3) g_rows_fx(Grouped<RowArg<Pw>> g, FxCon
 
 template <class Derive>
 __global__ void __launch_bounds__(256) g_slice_synth(Grouped<SliceSynthArg<Derive>> g) {
+  pdl_trigger();
+  pdl_wait();
   const int k = g.find(blockIdx.x);
   const int loc = blockIdx.x - g.start[k];
   const SliceSynthArg<Derive>& a = g.arg[k];
@@ -144,6 +148,8 @@ __global__ void __launch_bounds__(256) g_slice_synth(Grouped<SliceSynthArg<Deriv
 
 template <int NF>
 __global__ void __launch_bounds__(256) g_slice_anal(Grouped<SliceAnalArg> g) {
+  pdl_trigger();
+  pdl_wait();
   const int k = g.find(blockIdx.x);
   const int loc = blockIdx.x - g.start[k];
   const SliceAnalArg& a = g.arg[k];
@@ -444,28 +450,28 @@ int ens_stage_m(const aeolus_ensemble_s* E, double2* const* y0, int stage, doubl
     return s;
   {
     ProfScope prof("ens_split_synth_slice", st);
-    k1<<<gss.start[ng], 256, sm_ss, st>>>(gss);
+    launch_pdl(k1, dim3(gss.start[ng]), dim3(256), sm_ss, st, gss);
     AE_LAUNCH("g_slice_synth");
   }
   {
     ProfScope prof("ens_tc_synth_bf16x6", st);
-    k2<<<std::max(1, std::min(tsyn.start[ng], sm_count)), tc_threads<GroupedEpi<SynthSched, SEpi>>(), smt,
-         st>>>(tsyn, esyn, err);
+    launch_pdl(k2, dim3(std::max(1, std::min(tsyn.start[ng], sm_count))),
+               dim3(tc_threads<GroupedEpi<SynthSched, SEpi>>()), smt, st, tsyn, esyn, err);
     AE_LAUNCH("tc_persistent_kernel(ensemble synthesis)");
   }
   {
     ProfScope prof("ens_rows_fx", st);
-    k3<<<gr.start[ng], row_thr, sm_rows, st>>>(gr, fx_consts());
+    launch_pdl(k3, dim3(gr.start[ng]), dim3(row_thr), sm_rows, st, gr, fx_consts());
     AE_LAUNCH("g_rows_fx");
   }
   {
     ProfScope prof("ens_split_anal_slice", st);
-    k4<<<gsa.start[ng], 256, sm_sa, st>>>(gsa);
+    launch_pdl(k4, dim3(gsa.start[ng]), dim3(256), sm_sa, st, gsa);
     AE_LAUNCH("g_slice_anal");
   }
   ProfScope prof("ens_tc_anal_bf16x6", st);
-  k5<<<std::max(1, std::min(tana.start[ng], sm_count)), tc_threads<GroupedEpi<AnalSched, AnalEpi<Epi>>>(), smt,
-     st>>>(tana, eana, err);
+  launch_pdl(k5, dim3(std::max(1, std::min(tana.start[ng], sm_count))),
+             dim3(tc_threads<GroupedEpi<AnalSched, AnalEpi<Epi>>>()), smt, st, tana, eana, err);
   AE_LAUNCH("tc_persistent_kernel(ensemble analysis)");
   return AEOLUS_OK;
 }
