@@ -249,38 +249,47 @@ __device__ __forceinline__ void row_pfa_body(const RowArgs& a, const Pw& pw, con
   if (OUT_MODE == kOutG)
     oblock = a.G ? reinterpret_cast<longlong2*>(a.G) + fg_index(b0, 0, 0, j, L, a.gblk, a.nlat)
                  : reinterpret_cast<longlong2*>(const_cast<float4*>(block));
-  if constexpr (IN_MODE == kInF) {
-    // stage F[q][f] at slot spec(q) of field f, fields fastest (coalesced)
-#pragma unroll 1
-    for (int idx = tid; idx < NRI * ldm; idx += T) {
-      const int row = NR == 1 ? 0 : idx / (NIN * ldm), rem = idx - row * (NIN * ldm);
-      const int q = rem / NIN, f = rem - q * NIN;
-      if (row < nrow) cp_async16(zrow(row, f) + S::spec(q), block + row * bsi + (long)q * sq + f);
-    }
-  }
   if (tid < NR) s_bits[tid] = 0u;
   if (tid < NR * NF) {
     s_key[tid] = 0u;
     s_omax[tid] = 0u;
   }
-  if (tid == 32) {  // row constants (FP64 work) while the copies fly
+  if (tid == 32) {  // row constants (FP64 work) while the loads fly
     s_rc = pw.df_row(a.coslat[j], a.fgrid ? a.fgrid[j] : 0.0);
     s_wj = (OUT_MODE == kOutG && a.wq) ? df_from_double(a.wq[j]) : df{1.f, 0.f};
   }
-  if constexpr (IN_MODE == kInF) cp_async_wait_all();
   __syncthreads();
 
   // ---- 1. grid rows of the inputs
   if constexpr (IN_MODE == kInF) {
-    if (tid < PSI) {  // largest |hi| per (row, field) (m = 0: Im dropped)
+    // stage F[q][f] at slot spec(q) of field f: thread (row, field) = tid mod
+    // NRI, orders tid / NRI + QSI i (fields fastest across the threads:
+    // coalesced), four loads in flight per thread; the field's largest |hi|
+    // (m = 0: Im dropped) on the way
+    if (tid < PSI) {
       const int rf = tid % NRI, row = NR == 1 ? 0 : rf / NIN, f = rf - row * NIN;
-      const float4* zf = reinterpret_cast<const float4*>(zrow(row, f));
+      float4* zf = reinterpret_cast<float4*>(zrow(row, f));
+      const float4* src = block + row * bsi + f;
       unsigned mx = 0u;
-      if (row < nrow)
-        for (int q = tid / NRI; q < ldm; q += QSI) {
-          const float4 w = zf[S::spec(q)];
-          mx = max(mx, max(__float_as_uint(w.x) & 0x7FFFFFFFu, q == 0 ? 0u : __float_as_uint(w.z) & 0x7FFFFFFFu));
+      if (NR == 1 || row < nrow) {
+#pragma unroll 1
+        for (int q0 = tid / NRI; q0 < ldm; q0 += 4 * QSI) {
+          float4 w[4];
+#pragma unroll
+          for (int u = 0; u < 4; ++u) {
+            const int q = q0 + u * QSI;
+            if (q < ldm) w[u] = src[(long)q * sq];  // plain loads: the same blocks may take G later (a.G null)
+          }
+#pragma unroll
+          for (int u = 0; u < 4; ++u) {
+            const int q = q0 + u * QSI;
+            if (q < ldm) {
+              mx = max(mx, max(__float_as_uint(w[u].x) & 0x7FFFFFFFu, q == 0 ? 0u : __float_as_uint(w[u].z) & 0x7FFFFFFFu));
+              zf[S::spec(q)] = w[u];
+            }
+          }
         }
+      }
       if (mx) atomicMax(&s_key[row * NF + f], mx);
     }
     __syncthreads();
