@@ -380,8 +380,9 @@ __device__ __forceinline__ void split_anal_slice_body(const SplitDims& dm, int b
   }
 }
 
+constexpr int kAnalSliceThreads = 128;  // 8 CTAs per SM: more G loads in flight per SM
 template <int NF>
-__global__ void __launch_bounds__(256) split_anal_slice_kernel(SplitDims dm, int batch, int mb, int nblk,
+__global__ void __launch_bounds__(kAnalSliceThreads, 8) split_anal_slice_kernel(SplitDims dm, int batch, int mb, int nblk,
                                                               const long long* __restrict__ FG,
                                                               __nv_bfloat16* __restrict__ dana,
                                                               int* __restrict__ ecol) {
@@ -1000,7 +1001,7 @@ int launch_split_anal(const aeolus_plan_impl* p, const Epi& e, const double2* FG
   if (s) return s;
   {
     ProfScope prof("split_anal_slice", st);
-    launch_pdl(k1, r.grid, dim3(256), r.smem, st, r.dm, batch, r.mb, nblk, reinterpret_cast<const long long*>(FG),
+    launch_pdl(k1, r.grid, dim3(kAnalSliceThreads), r.smem, st, r.dm, batch, r.mb, nblk, reinterpret_cast<const long long*>(FG),
                r.digits, r.ecol);
     AE_LAUNCH("split_anal_slice_kernel");
   }
