@@ -332,6 +332,23 @@ def swe_rk4(plan_id: int, radius: float, omega: float, gravity: float, mean_dept
     return y.reshape(lead + (3,) + _spec_shape(p.lmax)), status.reshape(lead)
 
 
+def swe_rk4_inplace(plan_id: int, radius: float, omega: float, gravity: float, mean_depth: float, nu4: float,
+                    state: torch.Tensor, dt: float, nsteps: int, forcing: torch.Tensor | None = None) -> torch.Tensor:
+    """swe_rk4 on a contiguous [B, 3, L+1, L+1] device state in place (no
+    copy of the input); returns the per-member status bits."""
+    p = _PLANS[plan_id]
+    if not state.is_contiguous():
+        raise ValueError("swe_rk4_inplace needs a contiguous state")
+    B = state.shape[0]
+    status = torch.zeros(B, dtype=torch.int32, device=state.device)
+    if B and nsteps > 0:
+        w = p.workspace(_lib.OP_SWE_RK4, B)
+        prm = _swe_params(radius, omega, gravity, mean_depth, nu4, forcing, p.lmax, state.device)
+        check(_lib.load().aeolus_swe_rk4(p.handle, byref(prm), _ptr(state), B, float(dt), int(nsteps),
+                                         _ptr(status), _ptr(w), w.numel(), _stream(state.device)))
+    return status
+
+
 @torch.library.custom_op("aeolus::swe_validate", mutates_args=())
 def swe_validate(state_plan: int, product_plan: int, radius: float, omega: float, gravity: float,
                  mean_depth: float, state: torch.Tensor) -> tuple[torch.Tensor, torch.Tensor]:

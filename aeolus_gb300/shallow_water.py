@@ -16,7 +16,7 @@ from dataclasses import dataclass
 import torch
 
 from . import _lib
-from .ops import spectral_op, swe_invariants, swe_rk4, swe_tendency, swe_validate, winds
+from .ops import spectral_op, swe_invariants, swe_rk4, swe_rk4_inplace, swe_tendency, swe_validate, winds
 
 WILLIAMSON_GRAVITY = 9.80616
 ZETA, DELTA, PHI = 0, 1, 2
@@ -163,6 +163,51 @@ class ShallowWaterModel:
             if bits:
                 raise ShallowWaterStateError(self._describe_bits(bits, "during RK4 stages"))
         return y
+
+    def rk4_host(self, host_coeffs: torch.Tensor, dt: float, nsteps: int = 1, *, chunks: int = 2,
+                 out: torch.Tensor | None = None, check: bool = True) -> torch.Tensor:
+        """nsteps fused RK4 steps of a host-resident (preferably pinned)
+        ensemble [B, 3, L+1, L+1]; the result lands in ``out`` (pinned host
+        memory, allocated when None).  The members are independent, so they
+        are split into ``chunks`` groups, each copied to the device, stepped
+        and copied back on a CUDA stream of its own: one group's copies run on
+        the copy engines while another group's steps run on the SMs.  The
+        caller's current stream waits for every group.  With ``check`` the
+        status bits of all groups are read once at the end."""
+        if host_coeffs.is_cuda:
+            raise ValueError("rk4_host takes a host tensor (use rk4 for device-resident states)")
+        B = host_coeffs.shape[0]
+        if out is None:
+            out = torch.empty_like(host_coeffs).pin_memory()
+        dev = self.sh.weights.device
+        chunks = max(1, min(int(chunks), B))
+        cur = torch.cuda.current_stream(dev)
+        streams = getattr(self, "_host_streams", None)
+        if streams is None or len(streams) < chunks:
+            streams = self._host_streams = [torch.cuda.Stream(dev) for _ in range(chunks)]
+        statuses = []
+        edges = [B * k // chunks for k in range(chunks + 1)]
+        for k in range(chunks):
+            a, b = edges[k], edges[k + 1]
+            if a == b:
+                continue
+            s = streams[k]
+            s.wait_stream(cur)
+            with torch.cuda.stream(s):
+                d = host_coeffs[a:b].to(dev, non_blocking=True)  # stepped in place: no second device copy
+                status = swe_rk4_inplace(self._plan.id, self.R, self.Omega, self.gravity, self.mean_depth, self.nu4,
+                                         d, float(dt), int(nsteps), self.forcing)
+                out[a:b].copy_(d, non_blocking=True)
+                statuses.append(status)
+            for t in (d, status):
+                t.record_stream(s)
+        for k in range(chunks):
+            cur.wait_stream(streams[k])
+        if check:
+            bits = _or_bits(torch.cat(statuses)) if statuses else 0
+            if bits:
+                raise ShallowWaterStateError(self._describe_bits(bits, "during RK4 stages"))
+        return out
 
     def autotune(self, coeffs: torch.Tensor, dt: float, reps: int = 3) -> dict:
         """Pick the product plan's launch shapes for this batch by timing one

@@ -84,6 +84,8 @@ def workload_config(args, B):
             "parallelism": f"replicas x{max(args.gpus, 1)} (members shard, no collective)"}
 
 
+E2E_CHUNKS = 2   # member groups of the end-to-end step (ShallowWaterModel.rk4_host)
+
 # ------------------------------------------------------------ side measurements
 ENSEMBLE_GROUPS = [(42, 64, 128, 52), (63, 96, 192, 51), (85, 128, 256, 51), (106, 160, 320, 51),
                    (127, 192, 384, 51)]   # (l_max, nlat, nlon, members): 256 BVE members
@@ -845,15 +847,17 @@ def main():
     # end-to-end through the public API: pinned host state in, state out
     host_in = torch.as_tensor(states).pin_memory()
     host_out = torch.empty_like(host_in).pin_memory()
-    dev_state = torch.empty_like(y0)
+    for _ in range(warm):   # side streams and their workspaces exist before timing
+        model.rk4_host(host_in, DT, 1, chunks=E2E_CHUNKS, out=host_out, check=True)
+    torch.cuda.synchronize()
     barrier()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     t_wall = time.perf_counter()
     e0.record(stream)
     for _ in range(args.steps):
-        dev_state.copy_(host_in, non_blocking=True)
-        out = model.rk4(dev_state, DT, 1, check=True)   # reads the status word back
-        host_out.copy_(out, non_blocking=True)
+        # members in E2E_CHUNKS groups on streams of their own: copies of one
+        # group overlap the steps of the others; status read back every step
+        model.rk4_host(host_in, DT, 1, chunks=E2E_CHUNKS, out=host_out, check=True)
     e1.record(stream)
     barrier()
     e2e_ms = e0.elapsed_time(e1)

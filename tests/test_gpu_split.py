@@ -83,6 +83,20 @@ def test_split_swe_tendency_and_steps(nlat, nlon, L):
     assert device_error(planet.so._product_space.sh.plan) == 0
 
 
+@pytest.mark.parametrize("precision", ["fp64", "split"])
+def test_rk4_host_streams_equal_device_rk4(precision):
+    """ShallowWaterModel.rk4_host (member groups copied in, stepped and copied
+    back on streams of their own) gives the device rk4's result bit for bit,
+    for any number of groups."""
+    _, m, s = _swe(32, 64, 21, precision, members=5, seed=9)
+    ref = m.rk4(T(s), 300.0, 2).cpu()
+    host = torch.as_tensor(s).pin_memory()
+    for chunks in (1, 2, 3):
+        out = m.rk4_host(host, 300.0, 2, chunks=chunks)
+        torch.cuda.synchronize()
+        assert torch.equal(out, ref), chunks
+
+
 def test_split_bve_matches_fp64():
     L = 63
     p64 = ae.make_planet("latlon", nlat=96, nlon=192, l_max=L)
