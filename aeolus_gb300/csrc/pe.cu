@@ -203,6 +203,199 @@ __global__ void __launch_bounds__(128) pe_columns_kernel(PeSigma sg, long np, in
   }
 }
 
+// ---------------------------------------------------------------------------
+// The same column in double-float arithmetic, for split-precision plans (the
+// rest of their tendency is computed to ~48 bits already): the FP64 grid
+// values become double-floats and back through integer operations on their
+// bits, so the kernel issues no FP64 instruction (GB300's FP64 pipe is ~1/64
+// of its f32 pipe).  Values below 2^-126 in magnitude are taken as 0, values
+// beyond the float range as infinite.
+struct PeSigmaDf {
+  int K;
+  df s[kPeMaxLevels + 1], dsig[kPeMaxLevels], alpha[kPeMaxLevels], h2[kPeMaxLevels], bd[kPeMaxLevels];
+};
+
+inline df host_df(double x) {
+  const float h = static_cast<float>(x);
+  return df{h, static_cast<float>(x - static_cast<double>(h))};
+}
+
+PeSigmaDf sigma_df(const PeSigma& g) {
+  PeSigmaDf d;
+  d.K = g.K;
+  for (int k = 0; k <= g.K; ++k) d.s[k] = host_df(g.s[k]);
+  for (int k = 0; k < g.K; ++k) {
+    d.dsig[k] = host_df(g.dsig[k]);
+    d.alpha[k] = host_df(g.alpha[k]);
+    d.h2[k] = host_df(g.h2[k]);
+    d.bd[k] = host_df(g.bd[k]);
+  }
+  return d;
+}
+
+// 2^e as a float for e in [-126, 127]
+__device__ __forceinline__ float pe_pow2f(int e) { return __int_as_float((e + 127) << 23); }
+
+// x (FP64) as a double-float: hi = x truncated to 24 significant bits, lo =
+// the next 23 of the remaining 29 bits (|x - hi - lo| < 2^-46 |x|).
+__device__ __forceinline__ df dbl_to_df(double x) {
+  const unsigned long long b = static_cast<unsigned long long>(__double_as_longlong(x));
+  const unsigned sign = static_cast<unsigned>(b >> 32) & 0x80000000u;
+  const int e = static_cast<int>((b >> 52) & 0x7FF) - 1023;  // |x| in [2^e, 2^(e+1))
+  if (e < -126) return df{0.f, 0.f};
+  if (e > 127) return df{__int_as_float(sign | 0x7F800000u), 0.f};  // beyond float range (and NaN): infinite
+  const unsigned long long m = b & 0xFFFFFFFFFFFFFull;
+  const float hi = __int_as_float(sign | ((e + 127) << 23) | static_cast<unsigned>(m >> 29));
+  // lo = (m mod 2^29) 2^(e-52): its top 23 bits as an exact float integer
+  // (2^23 + ml - 2^23), scaled
+  const unsigned ml = static_cast<unsigned>(m & 0x1FFFFFFFull) >> 6;   // 23 bits
+  const float li = __int_as_float(0x4B000000 | ml) - 8388608.0f;        // exact
+  const int el = e - 46;                                                // 2^(e-52+6)
+  const int e1 = max(-126, el), e2 = max(-126, el - e1);
+  const float lo = li * pe_pow2f(e1) * pe_pow2f(e2);
+  return df{hi, sign ? -lo : lo};
+}
+
+// hi + lo as FP64, exactly (|lo| <= ulp(hi)/2 for normalised double-floats
+// is not assumed: the sum is formed in 64-bit integers at hi's scale).
+__device__ __forceinline__ double df_to_dbl(df v) {
+  const unsigned hb = __float_as_uint(v.hi), lb = __float_as_uint(v.lo);
+  const int eh = static_cast<int>((hb >> 23) & 0xFF);
+  if (eh == 0) return 0.0;
+  // hi = Mh 2^(eh - 150) with Mh a 24-bit integer; lo the same at its exponent
+  long long Mh = static_cast<long long>((hb & 0x7FFFFF) | 0x800000);
+  if (hb >> 31) Mh = -Mh;
+  long long T = Mh << 29;  // at 2^(eh - 179)
+  const int el = static_cast<int>((lb >> 23) & 0xFF);
+  if (el != 0) {
+    long long Ml = static_cast<long long>((lb & 0x7FFFFF) | 0x800000);
+    if (lb >> 31) Ml = -Ml;
+    const int sh = 29 - (eh - el);  // lo at 2^(el - 150) = 2^(eh - 179) 2^(29 - (eh - el))
+    if (sh >= 0) T += Ml << sh;
+    else if (sh > -63) T += Ml >> (-sh);  // below 2^-53 of hi: dropped bits are rounding-level
+  }
+  if (T == 0) return 0.0;
+  const unsigned long long a = static_cast<unsigned long long>(T < 0 ? -T : T);
+  const int nb = 64 - __clzll(static_cast<long long>(a));  // significant bits of |T|
+  const int sh = nb - 53;                                    // keep 53 bits
+  unsigned long long M = sh > 0 ? ((a >> (sh - 1)) + 1) >> 1 : a << (-sh);
+  int E = eh - 179 + sh + 52;  // value = M 2^(E - 52), M in [2^52, 2^53]
+  if (M >> 53) {               // rounding carried into a 54th bit
+    M >>= 1;
+    ++E;
+  }
+  const unsigned long long bits = (T < 0 ? 0x8000000000000000ull : 0ull) |
+                                  (static_cast<unsigned long long>(E + 1023) << 52) | (M & 0xFFFFFFFFFFFFFull);
+  return __longlong_as_double(static_cast<long long>(bits));
+}
+
+// 1 / c as a double-float: f32 reciprocal refined by one double-float Newton step.
+__device__ __forceinline__ df df_recip(df c) {
+  const float r0 = 1.0f / c.hi;
+  const df e = df_sub(df{1.0f, 0.0f}, df_mul(c, df{r0, 0.0f}));  // 1 - c r0
+  return df_add(df{r0, 0.0f}, df_mul(df{r0, 0.0f}, e));
+}
+
+// Two passes over the levels and no per-level arrays (in double-float the
+// recomputation is cheap, while thread-local column arrays would make the
+// kernel wait on local memory): pass 1 forms the cumulative thickness-weighted
+// G for the surface value; pass 2 repeats the same running sum for the
+// interface sigma_dot and keeps a three-level window of u, v, T for the
+// vertical advection (the same operations in the same order as one pass
+// with arrays).
+__global__ void __launch_bounds__(128) pe_columns_df_kernel(PeSigmaDf sg, long np, int nlon,
+                                                            const double* __restrict__ coslat, int batch, df r_dry,
+                                                            df kappa, const double* __restrict__ grid,
+                                                            double* __restrict__ prod, double* __restrict__ fen) {
+  const long idx = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= np * batch) return;
+  const int K = sg.K;
+  const int b = (int)(idx / np);
+  const long p = idx - b * np;
+  const df ic = df_recip(dbl_to_df(coslat[nlon > 0 ? p / nlon : p]));
+  const double* Gd = grid + (long)b * (kPeLevelFields * K + 2) * np + p;
+  double* P = prod + (long)b * (kPeOutFields * K + 1) * np + p;
+  const df lp_lam = dbl_to_df(Gd[(long)kPeLevelFields * K * np]), lp_snt = dbl_to_df(Gd[((long)kPeLevelFields * K + 1) * np]);
+  auto lev = [&](int k) { return Gd + (long)kPeLevelFields * k * np; };
+  auto AG = [&](int k, df uk, df vk, df& A, df& G) {
+    A = df_mul(df_sub(df_mul(uk, lp_lam), df_mul(vk, lp_snt)), ic);  // V . grad(ln p_s)
+    G = df_add(dbl_to_df(lev(k)[3 * np]), A);                        // delta + A
+  };
+  // pass 1: the cumulative thickness-weighted G
+  df acc = df{0.f, 0.f};
+  for (int k = 0; k < K; ++k) {
+    const double* f = lev(k);
+    df A, G;
+    AG(k, df_mul(dbl_to_df(f[0]), ic), df_mul(dbl_to_df(f[np]), ic), A, G);
+    const df w = df_mul(sg.dsig[k], G);
+    acc = k == 0 ? w : df_add(acc, w);
+  }
+  const df total = acc;
+  P[(long)kPeOutFields * K * np] = df_to_dbl(df_neg(total));  // d ln p_s / dt
+  const df gu = df_mul(lp_lam, ic), gv = df_neg(df_mul(lp_snt, ic));
+  const df zero = df{0.f, 0.f};
+  // vertical advection of X at level k from (X[k-1], X[k], X[k+1]) with the
+  // interface sigma_dot above (sdk) and below (sdk1) the level
+  auto vadv = [&](df xm, df x0, df xp, int k, df sdk, df sdk1) {
+    df a = zero;
+    bool any = false;
+    if (k < K - 1) {
+      a = df_mul(sdk1, df_sub(xp, x0));
+      any = true;
+    }
+    if (k > 0) {
+      const df up = df_mul(sdk, df_sub(x0, xm));
+      a = any ? df_add(a, up) : up;
+      any = true;
+    }
+    return any ? df_mul(a, sg.h2[k]) : zero;
+  };
+  // pass 2
+  df um = zero, vm = zero, Tm = zero;
+  df u0 = df_mul(dbl_to_df(lev(0)[0]), ic), v0 = df_mul(dbl_to_df(lev(0)[np]), ic), T0 = dbl_to_df(lev(0)[4 * np]);
+  df run = zero, part_prev = zero;
+  for (int k = 0; k < K; ++k) {
+    const double* f = lev(k);
+    df up = zero, vp = zero, Tp = zero;
+    if (k + 1 < K) {
+      const double* g = lev(k + 1);
+      up = df_mul(dbl_to_df(g[0]), ic);
+      vp = df_mul(dbl_to_df(g[np]), ic);
+      Tp = dbl_to_df(g[4 * np]);
+    }
+    df A, G;
+    AG(k, u0, v0, A, G);
+    const df w = df_mul(sg.dsig[k], G);
+    run = k == 0 ? w : df_add(run, w);
+    // interface sigma_dot: exact zeros at the top and (total - total) at the surface
+    const df sdk = k == 0 ? zero : df_sub(df_mul(sg.s[k], total), part_prev);
+    const df sdk1 = k + 1 == K ? zero : df_sub(df_mul(sg.s[k + 1], total), run);
+    const df wp = k == 0 ? df_sub(A, df_mul(sg.alpha[0], G))
+                         : df_sub(df_sub(A, df_mul(sg.bd[k], part_prev)), df_mul(sg.alpha[k], G));
+    const df t_lam = dbl_to_df(f[5 * np]), t_snt = dbl_to_df(f[6 * np]);
+    const df e_lam = dbl_to_df(f[7 * np]), e_snt = dbl_to_df(f[8 * np]), eta = dbl_to_df(f[9 * np]);
+    const df adv_t = df_mul(df_sub(df_mul(u0, t_lam), df_mul(v0, t_snt)), ic);
+    double* o = P + (long)kPeOutFields * k * np;
+    o[0] = df_to_dbl(df_add(df_sub(df_neg(adv_t), vadv(Tm, T0, Tp, k, sdk, sdk1)), df_mul(df_mul(kappa, T0), wp)));
+    o[np] = df_to_dbl(df_neg(df_add(df_mul(df_sub(df_mul(u0, e_lam), df_mul(v0, e_snt)), ic),
+                                    df_mul(eta, dbl_to_df(f[3 * np])))));
+    o[2 * np] = df_to_dbl(df_add(df_mul(eta, dbl_to_df(f[2 * np])),
+                                 df_mul(df_add(df_mul(v0, e_lam), df_mul(u0, e_snt)), ic)));
+    o[3 * np] = df_to_dbl(df_scale2(df_add(df_mul(u0, u0), df_mul(v0, v0)), 0.5f));
+    const df rt = df_mul(r_dry, T0);
+    double* z = fen + ((long)b * K + k) * 2 * np + p;
+    z[0] = df_to_dbl(df_add(vadv(um, u0, up, k, sdk, sdk1), df_mul(rt, gu)));
+    z[np] = df_to_dbl(df_add(vadv(vm, v0, vp, k, sdk, sdk1), df_mul(rt, gv)));
+    part_prev = run;
+    um = u0;
+    vm = v0;
+    Tm = T0;
+    u0 = up;
+    v0 = vp;
+    T0 = Tp;
+  }
+}
+
 // One thread per (member, l, m): every level's tendencies.
 __global__ void pe_spectral_kernel(PeSigma sg, int L, double R, double r_dry, int batch,
                                    const double2* __restrict__ st, const double2* __restrict__ an,
@@ -318,6 +511,13 @@ extern "C" int aeolus_pe_columns(aeolus_plan plan, const aeolus_pe_params* prm, 
   const long np = plan->npoints;
   const int nlon = plan->kind == kGauss ? plan->nlon : 0;
   ProfScope prof("pe_columns", static_cast<cudaStream_t>(stream));
+  if (plan->precision == AEOLUS_PREC_SPLIT_BF16) {  // split plans: the double-float column
+    pe_columns_df_kernel<<<blocks_for(np * batch, 128), 128, 0, static_cast<cudaStream_t>(stream)>>>(
+        sigma_df(sg), np, nlon, plan->coslat, batch, host_df(prm->r_dry), host_df(prm->r_dry / prm->cp_dry), grid,
+        prod, f_en);
+    AE_LAUNCH("pe_columns_df_kernel");
+    return AEOLUS_OK;
+  }
   pe_columns_kernel<<<blocks_for(np * batch, 128), 128, 0, static_cast<cudaStream_t>(stream)>>>(
       sg, np, nlon, plan->coslat, batch, prm->r_dry, prm->r_dry / prm->cp_dry, grid, prod, f_en);
   AE_LAUNCH("pe_columns_kernel");
