@@ -116,8 +116,15 @@ __global__ void __launch_bounds__(256) g_rows(Grouped<RowArg<Pw>> g) {
 // Each group runs the row body its plan's single-plan chains run
 // (split_row_kind): the prime-factor and fixed-radix bodies need
 // kPfaThreads = kFx8Threads threads, which the launch then uses.
-template <class Pw>
-__global__ void __launch_bounds__(256, 3) g_rows_fx(Grouped<RowArg<Pw>> g, FxConst kc) {
+// TH128: the 128-thread launch of groups with fixed row bodies, seven CTAs
+// per SM (72 registers; the grouped stage measured 0.391 -> 0.380 ms against
+// six); otherwise up to 256 threads (runtime body only), three CTAs per SM.
+// The single-plan row kernels stay at six: at seven their own launch is 1 %
+// faster but the programmatic-dependent-launch step of the SWE RK4 is 3 %
+// slower.
+template <class Pw, bool TH128>
+__global__ void __launch_bounds__(TH128 ? kPfaThreads : 256, TH128 ? 7 : 3)
+    g_rows_fx(Grouped<RowArg<Pw>> g, FxConst kc) {
   pdl_trigger();
   pdl_wait();
   const int k = g.find(blockIdx.x);
@@ -441,7 +448,7 @@ int ens_stage_m(const aeolus_ensemble_s* E, double2* const* y0, int stage, doubl
   eana.gs = tana;
   auto k1 = g_slice_synth<SDerive>;
   auto k2 = tc_persistent_kernel<GroupedSched<SynthSched>, GroupedEpi<SynthSched, SEpi>>;
-  auto k3 = g_rows_fx<Pw>;
+  auto k3 = row_thr == kPfaThreads ? g_rows_fx<Pw, true> : g_rows_fx<Pw, false>;
   auto k4 = g_slice_anal<NOUT>;
   auto k5 = tc_persistent_kernel<GroupedSched<AnalSched>, GroupedEpi<AnalSched, AnalEpi<Epi>>>;
   const size_t smt = tc_smem_bytes();
