@@ -156,6 +156,7 @@ struct aeolus_plan_impl {
   double* xa = nullptr;      // [(L+1)^2] x Y_lm = xa_lm Y_{l+1,m} + xb_lm Y_{l-1,m}
   double* xb = nullptr;      // [(L+1)^2]
   double* dcoef = nullptr;   // [(L+1)^2][8] SWE derive coefficients at the plan radius (see SweDerive)
+  float* dcoef_df = nullptr;  // the same as double-floats: [(L+1)^2][8] (hi, lo) float pairs
   // device tables (points)
   double* basis = nullptr;   // [npoints][ncol] real basis (cos / sin columns)
   double* wpts = nullptr;    // [npoints] quadrature weights

@@ -140,6 +140,46 @@ __device__ __forceinline__ df2 df2_mul(df2 a, df2 b) {
 }
 __device__ __forceinline__ df2 df2_scale2(df2 a, f2 p2) { return df2{f2_mul(a.hi, p2), f2_mul(a.lo, p2)}; }
 
+__device__ __forceinline__ df2 df2_splat(df a) { return df2{f2_splat(a.hi), f2_splat(a.lo)}; }
+__device__ __forceinline__ df2 df2_sub_fast(df2 a, df2 b) { return df2_add_fast(a, df2_neg(b)); }
+// i a for a complex value in the lanes (re, im): (-im, re).
+__device__ __forceinline__ f2 f2_times_i(f2 a) { return ((a >> 32) | (a << 32)) ^ 0x80000000ull; }
+__device__ __forceinline__ df2 df2_times_i(df2 a) { return df2{f2_times_i(a.hi), f2_times_i(a.lo)}; }
+
+// FP64 <-> double-float by integer operations on the bit patterns (no FP64
+// instruction; GB300's FP64 pipe is ~1/64 of its f32 pipe).
+// x as hi + lo: hi = x truncated to 24 significant bits, lo = the other 29
+// bits rounded to a float, so |x - hi - lo| <= 2^-48 |x| and |lo| < ulp(hi).
+// |x| below 2^-126 gives 0; |x| of 2^128 or more (and NaN) +-infinity.
+__device__ __forceinline__ df df_of_f64(double x) {
+  const unsigned l = static_cast<unsigned>(__double2loint(x)), h = static_cast<unsigned>(__double2hiint(x));
+  const unsigned sg = h & 0x80000000u, ah = h & 0x7FFFFFFFu;
+  const int ex = static_cast<int>(ah >> 20);  // biased exponent: 2^(ex - 1023) <= |x|
+  if (ex < 897) return df{0.f, 0.f};
+  if (ex > 1150) return df{__uint_as_float(sg | 0x7F800000u), 0.f};
+  const float hi = __uint_as_float(sg | __funnelshift_l(l, ah - (896u << 20), 3));
+  // (l mod 2^29) 2^(ex - 1075) = ((l mod 2^29) 2^-52) 2^(ex - 1023)
+  const float r = __uint2float_rn(l & 0x1FFFFFFFu) * 2.220446049250313080847e-16f;
+  const float lo = r * __uint_as_float(static_cast<unsigned>(ex - 896) << 23);
+  return df{hi, sg ? -lo : lo};
+}
+// A complex FP64 value as a df2 with the lanes (re, im).
+__device__ __forceinline__ df2 df2_of_f64x2(double2 v) { return df2_pack(df_of_f64(v.x), df_of_f64(v.y)); }
+// A float as the FP64 of the same value (denormal floats as 0), by its bits.
+__device__ __forceinline__ double f64_of_f32(float f) {
+  const unsigned u = __float_as_uint(f), e = (u >> 23) & 0xFFu;
+  if (e == 0) return 0.0;
+  const unsigned hw = (u & 0x80000000u) | ((e == 255u ? 2047u : e + 896u) << 20) | ((u & 0x7FFFFFu) >> 3);
+  return __hiloint2double(static_cast<int>(hw), static_cast<int>(u << 29));
+}
+// hi + lo rounded to FP64: the two words converted exactly, one FP64 addition.
+__device__ __forceinline__ double f64_of_df(df v) { return f64_of_f32(v.hi) + f64_of_f32(v.lo); }
+__device__ __forceinline__ double2 f64x2_of_df2(df2 v) {
+  df a, b;
+  df2_unpack(v, a, b);
+  return make_double2(f64_of_df(a), f64_of_df(b));
+}
+
 // From / to double (f64 conversions: used only at stage boundaries).
 __device__ __forceinline__ df df_from_double(double x) {
   const float h = __double2float_rn(x);

@@ -27,6 +27,7 @@ struct Spec {  // shared spectral context
   const double* xa;      // [(L+1)^2] x-multiplication coefficients (see xmul)
   const double* xb;
   const double* dcoef;   // [(L+1)^2][8] combined SWE derive coefficients (plan radius only)
+  const float2* dcoef_df;  // the same as double-floats (hi, lo), or none
   __device__ double lap(int l) const { return -(double)l * (l + 1.0) * ir2; }
   __device__ double2 at(const double2* a, int l, int m) const { return a[(long)l * (L + 1) + m]; }
   // Helmholtz inverse with l = 0 -> 0 (physics/barotropic.py:91); a
@@ -77,6 +78,7 @@ struct Spec {  // shared spectral context
 // ------------------------------------------------------------------ BVE
 struct BveDerive {  // psi_lam, psi_snt, eta_lam, eta_snt
   static constexpr int NF = 4;
+  static constexpr bool kColumnDf = true;  // column_df below
   Spec s;
   const double2* zeta;  // [b][L+1][L+1]
   double f10;           // 2 Omega sqrt(4 pi / 3)
@@ -114,6 +116,38 @@ struct BveDerive {  // psi_lam, psi_snt, eta_lam, eta_snt
     v[1] = cscale(s.ir, s.snt(psi_lo, psi_hi, l, m));
     v[2] = s.dlam(s.at(z, l, m), m);
     v[3] = cscale(s.ir, s.snt(eta_lo, eta_hi, l, m));
+  }
+  // The same fields in double-float arithmetic (lanes re, im) from the
+  // double-float coefficient table: the derive of the split path, whose
+  // digits carry 48 bits, issues no FP64 instruction.  Without the table
+  // (another radius) the FP64 fields, converted.
+  __device__ void column_df(int b, int l, int m, df2* v) const {
+    if (!s.dcoef_df) {
+      double2 w[NF];
+      column(b, l, m, w);
+#pragma unroll
+      for (int f = 0; f < NF; ++f) v[f] = df2_of_f64x2(w[f]);
+      return;
+    }
+    const int L = s.L;
+    const long r = (long)l * (L + 1) + m;
+    const double2* z = zeta + (long)b * (L + 1) * (L + 1);
+    const float2* c = s.dcoef_df + r * 8;
+    const df2 zero = df2{0ull, 0ull};
+    const bool lo = l >= 1 && l - 1 >= m, hi = l + 1 <= L;
+    const df2 izl = df2_times_i(df2_of_f64x2(z[r]));
+    df2 z_lo = lo ? df2_of_f64x2(z[r - (L + 1)]) : zero, z_hi = hi ? df2_of_f64x2(z[r + (L + 1)]) : zero;
+    auto k = [&](int i) { return df2_splat(df{c[i].x, c[i].y}); };
+    v[0] = df2_mul(k(2), izl);
+    v[1] = df2_add_fast(df2_mul(k(0), z_lo), df2_mul(k(1), z_hi));
+    v[2] = df2_mul(k(5), izl);
+    if (m == 0 && (l == 2 || l == 0)) {  // planetary vorticity of the (1, 0) mode in eta
+      df re, im;
+      df2_unpack(l == 2 ? z_lo : z_hi, re, im);
+      re = df_add(re, df_of_f64(f10));
+      (l == 2 ? z_lo : z_hi) = df2_pack(re, im);
+    }
+    v[3] = df2_add_fast(df2_mul(k(3), z_lo), df2_mul(k(4), z_hi));
   }
 };
 
@@ -372,6 +406,7 @@ struct SwePw {
 // contraction of its own; see SynthOut in split.cuh).
 struct SweDerive7 {
   static constexpr int NF = 7;
+  static constexpr bool kColumnDf = true;  // column_df below
   static constexpr int NBLK = 9;  // spectra blocks written by the synthesis epilogue
   __host__ __device__ static constexpr int blk(int f) { return f == 0 ? 0 : f == 1 ? 1 : f == 2 ? 3 : f == 3 ? 5 : f + 2; }
   __host__ __device__ static constexpr int lam_blk(int f) { return f == 4 ? 2 : f == 6 ? 4 : -1; }
@@ -387,6 +422,63 @@ struct SweDerive7 {
     v[4] = w[6];
     v[5] = w[7];
     v[6] = w[8];
+  }
+  // The same seven fields (and the Coriolis spectra) as SweDerive::column_tab
+  // in double-float arithmetic with the lanes (re, im), from the double-
+  // float coefficient table: no FP64 instruction but the four additions
+  // that round the Coriolis spectra to FP64.  Without the table (another
+  // radius) the FP64 fields, converted.
+  __device__ void column_df(int b, int l, int m, df2* v) const {
+    const Spec& s = d9.s;
+    if (!s.dcoef_df) {
+      double2 w[NF];
+      column(b, l, m, w);
+#pragma unroll
+      for (int f = 0; f < NF; ++f) v[f] = df2_of_f64x2(w[f]);
+      return;
+    }
+    const int L = s.L;
+    const long n2 = (long)(L + 1) * (L + 1);
+    const long r = (long)l * (L + 1) + m;
+    const double2* z = d9.state + (long)b * 3 * n2;
+    const double2* d = z + n2;
+    const double2* ph = d + n2;
+    const float2* c = s.dcoef_df + r * 8;
+    auto k = [&](int i) { return df2_splat(df{c[i].x, c[i].y}); };
+    const bool lo = l >= 1 && l - 1 >= m, hi = l + 1 <= L;
+    const df2 zero = df2{0ull, 0ull};
+    const df2 zl = df2_of_f64x2(z[r]), dl = df2_of_f64x2(d[r]), pl = df2_of_f64x2(ph[r]);
+    df2 z_lo = lo ? df2_of_f64x2(z[r - (L + 1)]) : zero, z_hi = hi ? df2_of_f64x2(z[r + (L + 1)]) : zero;
+    const df2 d_lo = lo ? df2_of_f64x2(d[r - (L + 1)]) : zero, d_hi = hi ? df2_of_f64x2(d[r + (L + 1)]) : zero;
+    const df2 p_lo = lo ? df2_of_f64x2(ph[r - (L + 1)]) : zero, p_hi = hi ? df2_of_f64x2(ph[r + (L + 1)]) : zero;
+    // U = A1 zeta_{l-1} + A2 zeta_{l+1} + i A3 delta_l, V = i A3 zeta_l - A1 delta_{l-1} - A2 delta_{l+1}
+    const df2 A1 = k(0), A2 = k(1), A3 = k(2);
+    const df2 U = df2_add_fast(df2_add_fast(df2_mul(A1, z_lo), df2_mul(A2, z_hi)), df2_mul(A3, df2_times_i(dl)));
+    const df2 V = df2_sub_fast(df2_mul(A3, df2_times_i(zl)), df2_add_fast(df2_mul(A1, d_lo), df2_mul(A2, d_hi)));
+    if (m == 0 && (l == 2 || l == 0) && d9.f10 != 0.0) {  // planetary vorticity of the (1, 0) mode in eta
+      df re, im;
+      df2_unpack(l == 2 ? z_lo : z_hi, re, im);
+      re = df_add(re, df_of_f64(d9.f10));
+      (l == 2 ? z_lo : z_hi) = df2_pack(re, im);
+    }
+    const df2 B1 = k(3), B2 = k(4);
+    v[0] = U;
+    v[1] = V;
+    v[2] = df2_add_fast(df2_mul(B1, z_lo), df2_mul(B2, z_hi));
+    v[3] = df2_add_fast(df2_mul(B1, p_lo), df2_mul(B2, p_hi));
+    v[4] = zl;
+    v[5] = dl;
+    v[6] = pl;
+    if (d9.cor) {  // zeta_dot += -(2 Omega/a) V - 2 Omega (x delta), curl += 2 Omega (x zeta) - (2 Omega/a) U
+      const df2 X1 = k(6), X2 = k(7);
+      const df tw = df_of_f64(d9.two_omega);
+      const df2 tw2 = df2_splat(tw), wr2 = df2_splat(df_mul(tw, df_of_f64(s.ir)));
+      const df2 xz = df2_add_fast(df2_mul(X1, z_lo), df2_mul(X2, z_hi));
+      const df2 xd = df2_add_fast(df2_mul(X1, d_lo), df2_mul(X2, d_hi));
+      double2* co = d9.cor + (long)b * 2 * n2 + r;
+      co[0] = f64x2_of_df2(df2_neg(df2_add_fast(df2_mul(wr2, V), df2_mul(tw2, xd))));
+      co[n2] = f64x2_of_df2(df2_sub_fast(df2_mul(tw2, xz), df2_mul(wr2, U)));
+    }
   }
 };
 
@@ -475,7 +567,8 @@ struct SweEpi {
 // different radius must not use it.
 Spec make_spec(const aeolus_plan_impl* p, double R) {
   return Spec{p->lmax, R, 1.0 / R, 1.0 / (R * R), p->cplus, p->cminus, R == p->radius ? p->invlap : nullptr,
-              p->xa, p->xb, R == p->radius ? p->dcoef : nullptr};
+              p->xa, p->xb, R == p->radius ? p->dcoef : nullptr,
+              R == p->radius ? reinterpret_cast<const float2*>(p->dcoef_df) : nullptr};
 }
 
 // ---------------------------------------------------------- helpers

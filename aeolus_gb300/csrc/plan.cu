@@ -273,9 +273,10 @@ void plan_fft(int N, int L, FftInfo& f, bool radix8) {
   }
 }
 
-int upload(double** dst, const std::vector<double>& src) {
-  AE_CUDA(cudaMalloc(dst, src.size() * sizeof(double)));
-  AE_CUDA(cudaMemcpy(*dst, src.data(), src.size() * sizeof(double), cudaMemcpyHostToDevice));
+template <class T>
+int upload(T** dst, const std::vector<T>& src) {
+  AE_CUDA(cudaMalloc(dst, src.size() * sizeof(T)));
+  AE_CUDA(cudaMemcpy(*dst, src.data(), src.size() * sizeof(T), cudaMemcpyHostToDevice));
   return AEOLUS_OK;
 }
 
@@ -324,6 +325,15 @@ int common_tables(aeolus_plan_impl* p) {
       c[7] = hi ? xb[(size_t)(l + 1) * n + m] : 0.0;
     }
   if ((s = upload(&p->dcoef, dc))) return s;
+  // as double-floats for the derive of the split path (hi = the nearest
+  // float, lo = the nearest float to the remainder)
+  std::vector<float> dcf(dc.size() * 2);
+  for (size_t i = 0; i < dc.size(); ++i) {
+    const float h = static_cast<float>(dc[i]);
+    dcf[2 * i] = h;
+    dcf[2 * i + 1] = static_cast<float>(dc[i] - static_cast<double>(h));
+  }
+  if ((s = upload(&p->dcoef_df, dcf))) return s;
   return AEOLUS_OK;
 }
 
@@ -332,6 +342,7 @@ void free_plan(aeolus_plan_impl* p) {
                     p->latp, p->cplus, p->cminus, p->cplus_true, p->invlap, p->xa, p->xb, p->dcoef};
   for (double* b : bufs)
     if (b) cudaFree(b);
+  if (p->dcoef_df) cudaFree(p->dcoef_df);
   if (p->tw) cudaFree(p->tw);
   if (p->twdf) cudaFree(p->twdf);
   if (p->twfx) cudaFree(p->twfx);

@@ -81,6 +81,26 @@ __device__ inline long long fixed_point(double x, int E) {
   return (b >> 63) ? -X : X;
 }
 
+// X = hi 2^p + lo 2^p rounded to an integer (within one unit of
+// rint((hi + lo) 2^p)) for 2^p = pa pb and |hi 2^p| < 2^47: the high word's
+// multiple of 2^30 from the float magic-number rounding, the rest (|r| <=
+// 2^29 and the scaled low word) rounded to 32-bit integers.
+__device__ __forceinline__ long long fixed_point_df(float2 v, float pa, float pb) {
+  const float th = v.x * pa * pb, tl = v.y * pa * pb;
+  const float c15 = 12582912.0f;                             // 1.5 2^23
+  const float um = fmaf(th, 9.31322574615478515625e-10f, c15);  // th 2^-30 rounded into the mantissa
+  const float r = fmaf(-(um - c15), 1073741824.0f, th);      // th - u 2^30, exact
+  const int u = __float_as_int(um) - 0x4B400000;
+  return fx_madw(u, 1 << 30, static_cast<long long>(__float2int_rn(r) + __float2int_rn(tl)));
+}
+
+// Derives with a double-float column (kColumnDf; column_df(b, l, m, v):
+// v[f] a df2 with the lanes re, im).
+template <class D, class = void>
+struct DeriveHasDf : std::false_type {};
+template <class D>
+struct DeriveHasDf<D, std::enable_if_t<D::kColumnDf>> : std::true_type {};
+
 // One digit (|r| <= 128) as a bf16, exactly: the magic-number construction
 // puts r in the mantissa of 1.5 2^23 (FMA pipe, no integer-to-float
 // conversion, which would run on the FP64 pipe for 64-bit operands), and a
@@ -263,24 +283,46 @@ __device__ __forceinline__ void split_synth_slice_body(const SplitDims& dm, cons
   const int b0 = by * mb;
   const int nb = min(mb, batch - b0);
   const int nc = nb * NF * 2;
+  constexpr bool kDf = DeriveHasDf<Derive>::value;
+  float2* s_vdf = reinterpret_cast<float2*>(s_val);  // kDf: (hi, lo) in the same slots
   for (int idx = threadIdx.x; idx < nb * K; idx += blockDim.x) {
     const int bl = idx / K, t = idx - bl * K;
-    double2 v[NF];
-    der.column(b0 + bl, m + t, m, v);
+    if constexpr (kDf) {
+      df2 v[NF];
+      der.column_df(b0 + bl, m + t, m, v);
 #pragma unroll
-    for (int f = 0; f < NF; ++f) {
-      s_val[((bl * NF + f) * 2 + 0) * ks + t] = v[f].x;
-      s_val[((bl * NF + f) * 2 + 1) * ks + t] = v[f].y;
+      for (int f = 0; f < NF; ++f) {
+        df re, im;
+        df2_unpack(v[f], re, im);
+        s_vdf[((bl * NF + f) * 2 + 0) * ks + t] = make_float2(re.hi, re.lo);
+        s_vdf[((bl * NF + f) * 2 + 1) * ks + t] = make_float2(im.hi, im.lo);
+      }
+    } else {
+      double2 v[NF];
+      der.column(b0 + bl, m + t, m, v);
+#pragma unroll
+      for (int f = 0; f < NF; ++f) {
+        s_val[((bl * NF + f) * 2 + 0) * ks + t] = v[f].x;
+        s_val[((bl * NF + f) * 2 + 1) * ks + t] = v[f].y;
+      }
     }
   }
   __syncthreads();
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
   for (int c = warp; c < nc; c += nwarp) {
-    unsigned long long mx = 0ull;
-    for (int t = lane; t < K; t += 32) mx = max(mx, abs_key(s_val[c * ks + t]));
-    for (int o = 16; o > 0; o >>= 1) mx = max(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+    int E;
+    if constexpr (kDf) {  // from the high words: |hi| < 2^(e - 126) bounds |hi + lo| too
+      unsigned mx = 0u;
+      for (int t = lane; t < K; t += 32) mx = max(mx, __float_as_uint(s_vdf[c * ks + t].x) & 0x7FFFFFFFu);
+      mx = __reduce_max_sync(0xffffffffu, mx);
+      E = (mx >> 23) == 0 ? -1000 : static_cast<int>(mx >> 23) - 125;
+    } else {
+      unsigned long long mx = 0ull;
+      for (int t = lane; t < K; t += 32) mx = max(mx, abs_key(s_val[c * ks + t]));
+      for (int o = 16; o > 0; o >>= 1) mx = max(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+      E = exponent_for_key(mx);
+    }
     if (lane == 0) {
-      const int E = exponent_for_key(mx);
       s_exp[c] = E;
       ecol[(long long)m * dm.ntiles * kNT + (long long)b0 * NF * 2 + c] = E;
     }
@@ -291,8 +333,16 @@ __device__ __forceinline__ void split_synth_slice_body(const SplitDims& dm, cons
     const int g = idx / nc, c = idx - g * nc;
     const int n = b0 * NF * 2 + c, t0 = 8 * g, E = s_exp[c];
     long long X[8];
+    if constexpr (kDf) {
+      float pa, pb;
+      fx_pow2_split(kShift - E, pa, pb);
 #pragma unroll
-    for (int u = 0; u < 8; ++u) X[u] = t0 + u < K ? fixed_point(s_val[c * ks + t0 + u], E) : 0LL;
+      for (int u = 0; u < 8; ++u)
+        X[u] = t0 + u < K && E != -1000 ? fixed_point_df(s_vdf[c * ks + t0 + u], pa, pb) : 0LL;
+    } else {
+#pragma unroll
+      for (int u = 0; u < 8; ++u) X[u] = t0 + u < K ? fixed_point(s_val[c * ks + t0 + u], E) : 0LL;
+    }
     store_digits8(dsyn + dsyn_tile(kcum, dm, m, n / kNT), n % kNT, t0, X);
   }
   if (by == gy - 1) {  // zero the columns that pad the last tile
@@ -307,8 +357,10 @@ __device__ __forceinline__ void split_synth_slice_body(const SplitDims& dm, cons
   }
 }
 
+// Four CTAs per SM (64 registers) for the FP64 derives; three (85) for the
+// double-float ones, whose packed columns spill at 64 registers.
 template <class Derive>
-__global__ void __launch_bounds__(256, 4) split_synth_slice_kernel(SplitDims dm, const long long* __restrict__ kcum,
+__global__ void __launch_bounds__(256, DeriveHasDf<Derive>::value ? 3 : 4) split_synth_slice_kernel(SplitDims dm, const long long* __restrict__ kcum,
                                                                int batch, int mb, Derive der,
                                                                __nv_bfloat16* __restrict__ dsyn,
                                                                int* __restrict__ ecol) {
