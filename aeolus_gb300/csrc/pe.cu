@@ -131,6 +131,72 @@ __global__ void pe_derive_kernel(Spec s, int K, int batch, double f10, const dou
   O[((long)kPeLevelFields * K + 1) * n2] = snt_r(lo ? val(q, l - 1) : zero, hi ? val(q, l + 1) : zero);
 }
 
+// The same spectra for split-precision plans (their synthesis digits carry
+// 48 bits) in packed double-float (lanes re, im): the coefficient products
+// of the double-float derive table at the plan radius (Spec::dcoef_df: the
+// same combinations of C+-, 1/lap and m/R as the SWE derive), the state
+// converted by integer operations on its bits, each derived spectrum
+// rounded to FP64 by one FP64 addition per word; zeta, delta, T and eta are
+// copied in FP64 as they are.
+__global__ void __launch_bounds__(128) pe_derive_df_kernel(Spec s, int K, int batch, double f10,
+                                                           const double2* __restrict__ st, double2* __restrict__ out) {
+  const int L = s.L;
+  const long n2 = (long)(L + 1) * (L + 1);
+  const long idx = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= n2 * batch) return;
+  const int b = (int)(idx / n2);
+  const long r = idx - b * n2;
+  const int l = (int)(r / (L + 1)), m = (int)(r - (long)l * (L + 1));
+  const double2* S = st + (long)b * (3 * K + 1) * n2;
+  double2* O = out + (long)b * (kPeLevelFields * K + 2) * n2 + r;
+  if (m > l) {
+    const double2 zero = make_double2(0.0, 0.0);
+    for (int f = 0; f < kPeLevelFields * K + 2; ++f) O[f * n2] = zero;
+    return;
+  }
+  const bool lo = l >= 1 && l - 1 >= m, hi = l + 1 <= L;
+  const float2* c = s.dcoef_df + r * 8;
+  auto kc = [&](int i) { return df2_splat(df{c[i].x, c[i].y}); };
+  const df2 A1 = kc(0), A2 = kc(1), A3 = kc(2), B1 = kc(3), B2 = kc(4), B3 = kc(5);
+  const df2 zero = df2{0ull, 0ull};
+  auto cv = [&](const double2* a, int ll) { return df2_of_f64x2(a[(long)ll * (L + 1) + m]); };
+  auto cvlo = [&](const double2* a) { return lo ? cv(a, l - 1) : zero; };
+  auto cvhi = [&](const double2* a) { return hi ? cv(a, l + 1) : zero; };
+  // eta = zeta + f at the (1, 0) mode, in the neighbour slots
+  auto add_f = [&](df2 v, bool at) {
+    if (!at) return v;
+    df re, im;
+    df2_unpack(v, re, im);
+    return df2_pack(df_add(re, df_of_f64(f10)), im);
+  };
+  for (int k = 0; k < K; ++k) {
+    const double2* z = S + (long)k * n2;
+    const double2* d = S + (long)(K + k) * n2;
+    const double2* T = S + (long)(2 * K + k) * n2;
+    const long rl = (long)l * (L + 1) + m;
+    const double2 z64 = z[rl], d64 = d[rl], T64 = T[rl];
+    const df2 zl = df2_of_f64x2(z64), dl = df2_of_f64x2(d64), Tl = df2_of_f64x2(T64);
+    const df2 z_lo = cvlo(z), z_hi = cvhi(z), d_lo = cvlo(d), d_hi = cvhi(d);
+    double2* o = O + (long)kPeLevelFields * k * n2;
+    o[0 * n2] = f64x2_of_df2(df2_add_fast(df2_add_fast(df2_mul(A1, z_lo), df2_mul(A2, z_hi)),
+                                          df2_mul(A3, df2_times_i(dl))));    // u cos
+    o[1 * n2] = f64x2_of_df2(df2_sub_fast(df2_mul(A3, df2_times_i(zl)),
+                                          df2_add_fast(df2_mul(A1, d_lo), df2_mul(A2, d_hi))));  // v cos
+    o[2 * n2] = z64;
+    o[3 * n2] = d64;
+    o[4 * n2] = T64;
+    o[5 * n2] = f64x2_of_df2(df2_mul(B3, df2_times_i(Tl)));
+    o[6 * n2] = f64x2_of_df2(df2_add_fast(df2_mul(B1, cvlo(T)), df2_mul(B2, cvhi(T))));
+    o[7 * n2] = f64x2_of_df2(df2_mul(B3, df2_times_i(zl)));  // m = 0 (the only f slot) has B3 = 0
+    o[8 * n2] = f64x2_of_df2(df2_add_fast(df2_mul(B1, add_f(z_lo, m == 0 && l == 2)),
+                                          df2_mul(B2, add_f(z_hi, m == 0 && l == 0))));
+    o[9 * n2] = (m == 0 && l == 1) ? make_double2(z64.x + f10, z64.y) : z64;
+  }
+  const double2* q = S + (long)3 * K * n2;
+  O[(long)kPeLevelFields * K * n2] = f64x2_of_df2(df2_mul(B3, df2_times_i(cv(q, l))));
+  O[((long)kPeLevelFields * K + 1) * n2] = f64x2_of_df2(df2_add_fast(df2_mul(B1, cvlo(q)), df2_mul(B2, cvhi(q))));
+}
+
 // One thread per (member, product point): the column in thread-local
 // arrays.  The kernel is FP64-bound (84 % FP64-pipe active at 192x384,
 // 20 levels); the arrays spill through L1 to L2, which doubles its DRAM
@@ -206,9 +272,10 @@ __global__ void __launch_bounds__(128) pe_columns_kernel(PeSigma sg, long np, in
 // ---------------------------------------------------------------------------
 // The same column in double-float arithmetic, for split-precision plans (the
 // rest of their tendency is computed to ~48 bits already): the FP64 grid
-// values become double-floats and back through integer operations on their
-// bits, so the kernel issues no FP64 instruction (GB300's FP64 pipe is ~1/64
-// of its f32 pipe).  Values below 2^-126 in magnitude are taken as 0, values
+// values become double-floats through integer operations on their bits
+// (df_of_f64) and the results FP64 with one FP64 addition each (f64_of_df),
+// the only FP64 instructions of the kernel (GB300's FP64 pipe is ~1/64 of
+// its f32 pipe).  Values below 2^-126 in magnitude are taken as 0, values
 // beyond the float range as infinite.
 struct PeSigmaDf {
   int K;
@@ -231,62 +298,6 @@ PeSigmaDf sigma_df(const PeSigma& g) {
     d.bd[k] = host_df(g.bd[k]);
   }
   return d;
-}
-
-// 2^e as a float for e in [-126, 127]
-__device__ __forceinline__ float pe_pow2f(int e) { return __int_as_float((e + 127) << 23); }
-
-// x (FP64) as a double-float: hi = x truncated to 24 significant bits, lo =
-// the next 23 of the remaining 29 bits (|x - hi - lo| < 2^-46 |x|).
-__device__ __forceinline__ df dbl_to_df(double x) {
-  const unsigned long long b = static_cast<unsigned long long>(__double_as_longlong(x));
-  const unsigned sign = static_cast<unsigned>(b >> 32) & 0x80000000u;
-  const int e = static_cast<int>((b >> 52) & 0x7FF) - 1023;  // |x| in [2^e, 2^(e+1))
-  if (e < -126) return df{0.f, 0.f};
-  if (e > 127) return df{__int_as_float(sign | 0x7F800000u), 0.f};  // beyond float range (and NaN): infinite
-  const unsigned long long m = b & 0xFFFFFFFFFFFFFull;
-  const float hi = __int_as_float(sign | ((e + 127) << 23) | static_cast<unsigned>(m >> 29));
-  // lo = (m mod 2^29) 2^(e-52): its top 23 bits as an exact float integer
-  // (2^23 + ml - 2^23), scaled
-  const unsigned ml = static_cast<unsigned>(m & 0x1FFFFFFFull) >> 6;   // 23 bits
-  const float li = __int_as_float(0x4B000000 | ml) - 8388608.0f;        // exact
-  const int el = e - 46;                                                // 2^(e-52+6)
-  const int e1 = max(-126, el), e2 = max(-126, el - e1);
-  const float lo = li * pe_pow2f(e1) * pe_pow2f(e2);
-  return df{hi, sign ? -lo : lo};
-}
-
-// hi + lo as FP64, exactly (|lo| <= ulp(hi)/2 for normalised double-floats
-// is not assumed: the sum is formed in 64-bit integers at hi's scale).
-__device__ __forceinline__ double df_to_dbl(df v) {
-  const unsigned hb = __float_as_uint(v.hi), lb = __float_as_uint(v.lo);
-  const int eh = static_cast<int>((hb >> 23) & 0xFF);
-  if (eh == 0) return 0.0;
-  // hi = Mh 2^(eh - 150) with Mh a 24-bit integer; lo the same at its exponent
-  long long Mh = static_cast<long long>((hb & 0x7FFFFF) | 0x800000);
-  if (hb >> 31) Mh = -Mh;
-  long long T = Mh << 29;  // at 2^(eh - 179)
-  const int el = static_cast<int>((lb >> 23) & 0xFF);
-  if (el != 0) {
-    long long Ml = static_cast<long long>((lb & 0x7FFFFF) | 0x800000);
-    if (lb >> 31) Ml = -Ml;
-    const int sh = 29 - (eh - el);  // lo at 2^(el - 150) = 2^(eh - 179) 2^(29 - (eh - el))
-    if (sh >= 0) T += Ml << sh;
-    else if (sh > -63) T += Ml >> (-sh);  // below 2^-53 of hi: dropped bits are rounding-level
-  }
-  if (T == 0) return 0.0;
-  const unsigned long long a = static_cast<unsigned long long>(T < 0 ? -T : T);
-  const int nb = 64 - __clzll(static_cast<long long>(a));  // significant bits of |T|
-  const int sh = nb - 53;                                    // keep 53 bits
-  unsigned long long M = sh > 0 ? ((a >> (sh - 1)) + 1) >> 1 : a << (-sh);
-  int E = eh - 179 + sh + 52;  // value = M 2^(E - 52), M in [2^52, 2^53]
-  if (M >> 53) {               // rounding carried into a 54th bit
-    M >>= 1;
-    ++E;
-  }
-  const unsigned long long bits = (T < 0 ? 0x8000000000000000ull : 0ull) |
-                                  (static_cast<unsigned long long>(E + 1023) << 52) | (M & 0xFFFFFFFFFFFFFull);
-  return __longlong_as_double(static_cast<long long>(bits));
 }
 
 // 1 / c as a double-float: f32 reciprocal refined by one double-float Newton step.
@@ -312,26 +323,26 @@ __global__ void __launch_bounds__(128) pe_columns_df_kernel(PeSigmaDf sg, long n
   const int K = sg.K;
   const int b = (int)(idx / np);
   const long p = idx - b * np;
-  const df ic = df_recip(dbl_to_df(coslat[nlon > 0 ? p / nlon : p]));
+  const df ic = df_recip(df_of_f64(coslat[nlon > 0 ? p / nlon : p]));
   const double* Gd = grid + (long)b * (kPeLevelFields * K + 2) * np + p;
   double* P = prod + (long)b * (kPeOutFields * K + 1) * np + p;
-  const df lp_lam = dbl_to_df(Gd[(long)kPeLevelFields * K * np]), lp_snt = dbl_to_df(Gd[((long)kPeLevelFields * K + 1) * np]);
+  const df lp_lam = df_of_f64(Gd[(long)kPeLevelFields * K * np]), lp_snt = df_of_f64(Gd[((long)kPeLevelFields * K + 1) * np]);
   auto lev = [&](int k) { return Gd + (long)kPeLevelFields * k * np; };
   auto AG = [&](int k, df uk, df vk, df& A, df& G) {
     A = df_mul(df_sub(df_mul(uk, lp_lam), df_mul(vk, lp_snt)), ic);  // V . grad(ln p_s)
-    G = df_add(dbl_to_df(lev(k)[3 * np]), A);                        // delta + A
+    G = df_add(df_of_f64(lev(k)[3 * np]), A);                        // delta + A
   };
   // pass 1: the cumulative thickness-weighted G
   df acc = df{0.f, 0.f};
   for (int k = 0; k < K; ++k) {
     const double* f = lev(k);
     df A, G;
-    AG(k, df_mul(dbl_to_df(f[0]), ic), df_mul(dbl_to_df(f[np]), ic), A, G);
+    AG(k, df_mul(df_of_f64(f[0]), ic), df_mul(df_of_f64(f[np]), ic), A, G);
     const df w = df_mul(sg.dsig[k], G);
     acc = k == 0 ? w : df_add(acc, w);
   }
   const df total = acc;
-  P[(long)kPeOutFields * K * np] = df_to_dbl(df_neg(total));  // d ln p_s / dt
+  P[(long)kPeOutFields * K * np] = f64_of_df(df_neg(total));  // d ln p_s / dt
   const df gu = df_mul(lp_lam, ic), gv = df_neg(df_mul(lp_snt, ic));
   const df zero = df{0.f, 0.f};
   // vertical advection of X at level k from (X[k-1], X[k], X[k+1]) with the
@@ -352,16 +363,16 @@ __global__ void __launch_bounds__(128) pe_columns_df_kernel(PeSigmaDf sg, long n
   };
   // pass 2
   df um = zero, vm = zero, Tm = zero;
-  df u0 = df_mul(dbl_to_df(lev(0)[0]), ic), v0 = df_mul(dbl_to_df(lev(0)[np]), ic), T0 = dbl_to_df(lev(0)[4 * np]);
+  df u0 = df_mul(df_of_f64(lev(0)[0]), ic), v0 = df_mul(df_of_f64(lev(0)[np]), ic), T0 = df_of_f64(lev(0)[4 * np]);
   df run = zero, part_prev = zero;
   for (int k = 0; k < K; ++k) {
     const double* f = lev(k);
     df up = zero, vp = zero, Tp = zero;
     if (k + 1 < K) {
       const double* g = lev(k + 1);
-      up = df_mul(dbl_to_df(g[0]), ic);
-      vp = df_mul(dbl_to_df(g[np]), ic);
-      Tp = dbl_to_df(g[4 * np]);
+      up = df_mul(df_of_f64(g[0]), ic);
+      vp = df_mul(df_of_f64(g[np]), ic);
+      Tp = df_of_f64(g[4 * np]);
     }
     df A, G;
     AG(k, u0, v0, A, G);
@@ -372,20 +383,20 @@ __global__ void __launch_bounds__(128) pe_columns_df_kernel(PeSigmaDf sg, long n
     const df sdk1 = k + 1 == K ? zero : df_sub(df_mul(sg.s[k + 1], total), run);
     const df wp = k == 0 ? df_sub(A, df_mul(sg.alpha[0], G))
                          : df_sub(df_sub(A, df_mul(sg.bd[k], part_prev)), df_mul(sg.alpha[k], G));
-    const df t_lam = dbl_to_df(f[5 * np]), t_snt = dbl_to_df(f[6 * np]);
-    const df e_lam = dbl_to_df(f[7 * np]), e_snt = dbl_to_df(f[8 * np]), eta = dbl_to_df(f[9 * np]);
+    const df t_lam = df_of_f64(f[5 * np]), t_snt = df_of_f64(f[6 * np]);
+    const df e_lam = df_of_f64(f[7 * np]), e_snt = df_of_f64(f[8 * np]), eta = df_of_f64(f[9 * np]);
     const df adv_t = df_mul(df_sub(df_mul(u0, t_lam), df_mul(v0, t_snt)), ic);
     double* o = P + (long)kPeOutFields * k * np;
-    o[0] = df_to_dbl(df_add(df_sub(df_neg(adv_t), vadv(Tm, T0, Tp, k, sdk, sdk1)), df_mul(df_mul(kappa, T0), wp)));
-    o[np] = df_to_dbl(df_neg(df_add(df_mul(df_sub(df_mul(u0, e_lam), df_mul(v0, e_snt)), ic),
-                                    df_mul(eta, dbl_to_df(f[3 * np])))));
-    o[2 * np] = df_to_dbl(df_add(df_mul(eta, dbl_to_df(f[2 * np])),
+    o[0] = f64_of_df(df_add(df_sub(df_neg(adv_t), vadv(Tm, T0, Tp, k, sdk, sdk1)), df_mul(df_mul(kappa, T0), wp)));
+    o[np] = f64_of_df(df_neg(df_add(df_mul(df_sub(df_mul(u0, e_lam), df_mul(v0, e_snt)), ic),
+                                    df_mul(eta, df_of_f64(f[3 * np])))));
+    o[2 * np] = f64_of_df(df_add(df_mul(eta, df_of_f64(f[2 * np])),
                                  df_mul(df_add(df_mul(v0, e_lam), df_mul(u0, e_snt)), ic)));
-    o[3 * np] = df_to_dbl(df_scale2(df_add(df_mul(u0, u0), df_mul(v0, v0)), 0.5f));
+    o[3 * np] = f64_of_df(df_scale2(df_add(df_mul(u0, u0), df_mul(v0, v0)), 0.5f));
     const df rt = df_mul(r_dry, T0);
     double* z = fen + ((long)b * K + k) * 2 * np + p;
-    z[0] = df_to_dbl(df_add(vadv(um, u0, up, k, sdk, sdk1), df_mul(rt, gu)));
-    z[np] = df_to_dbl(df_add(vadv(vm, v0, vp, k, sdk, sdk1), df_mul(rt, gv)));
+    z[0] = f64_of_df(df_add(vadv(um, u0, up, k, sdk, sdk1), df_mul(rt, gu)));
+    z[np] = f64_of_df(df_add(vadv(vm, v0, vp, k, sdk, sdk1), df_mul(rt, gv)));
     part_prev = run;
     um = u0;
     vm = v0;
@@ -493,9 +504,17 @@ extern "C" int aeolus_pe_derive(aeolus_plan plan, const aeolus_pe_params* prm, i
   if (batch == 0) return AEOLUS_OK;
   const long n2 = (long)(plan->lmax + 1) * (plan->lmax + 1);
   ProfScope prof("pe_derive", static_cast<cudaStream_t>(stream));
+  const Spec sp = make_spec(plan, prm->radius);
+  if (plan->precision == AEOLUS_PREC_SPLIT_BF16 && sp.dcoef_df) {
+    pe_derive_df_kernel<<<blocks_for(n2 * batch, 128), 128, 0, static_cast<cudaStream_t>(stream)>>>(
+        sp, nlev, batch, 2.0 * prm->omega * kSqrt4PiOver3, reinterpret_cast<const double2*>(state),
+        reinterpret_cast<double2*>(fields));
+    AE_LAUNCH("pe_derive_df_kernel");
+    return AEOLUS_OK;
+  }
   pe_derive_kernel<<<blocks_for(n2 * batch, 128), 128, 0, static_cast<cudaStream_t>(stream)>>>(
-      make_spec(plan, prm->radius), nlev, batch, 2.0 * prm->omega * kSqrt4PiOver3,
-      reinterpret_cast<const double2*>(state), reinterpret_cast<double2*>(fields));
+      sp, nlev, batch, 2.0 * prm->omega * kSqrt4PiOver3, reinterpret_cast<const double2*>(state),
+      reinterpret_cast<double2*>(fields));
   AE_LAUNCH("pe_derive_kernel");
   return AEOLUS_OK;
 }
