@@ -58,6 +58,7 @@ SIGNATURES = {
     "aeolus_plan_device_error": (c_int, [c_void_p, POINTER(c_int)]),
     "aeolus_rk4_stage": (c_int, [c_int, c_double, c_void_p, c_void_p, c_void_p, c_void_p, c_long, c_void_p]),
     "aeolus_selftest_wait_timeout": (c_int, [ctypes.c_ulonglong, POINTER(c_int), POINTER(ctypes.c_ulonglong)]),
+    "aeolus_selftest_df_convert": (c_int, [c_void_p, c_int, c_void_p, c_void_p]),
     "aeolus_plan_set_tuning": (c_int, [c_void_p, POINTER(c_int)]),
     "aeolus_plan_get_tuning": (c_int, [c_void_p, POINTER(c_int)]),
     "aeolus_workspace_bytes": (c_int, [c_void_p, c_int, c_int, POINTER(c_size_t)]),

@@ -247,9 +247,29 @@ __global__ void mbar_timeout_selftest_kernel(unsigned long long limit_ns, int* t
   }
 }
 
+// The FP64 <-> double-float conversions of the split path on n values:
+// out[3i] = hi, out[3i+1] = lo of df_of_f64(x[i]) (as FP64, exactly),
+// out[3i+2] = f64_of_df of that double-float.
+__global__ void df_convert_selftest_kernel(const double* __restrict__ x, int n, double* __restrict__ out) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const df v = df_of_f64(x[i]);
+  out[3 * i] = f64_of_f32(v.hi);
+  out[3 * i + 1] = f64_of_f32(v.lo);
+  out[3 * i + 2] = f64_of_df(v);
+}
+
 }  // namespace aeolus
 
 using namespace aeolus;
+
+extern "C" int aeolus_selftest_df_convert(const double* x, int n, double* out, void* stream) {
+  if (n < 0 || (n > 0 && (!x || !out))) return fail(AEOLUS_ERR_ARG, "aeolus_selftest_df_convert: bad arguments");
+  if (n == 0) return AEOLUS_OK;
+  df_convert_selftest_kernel<<<(n + 127) / 128, 128, 0, static_cast<cudaStream_t>(stream)>>>(x, n, out);
+  AE_LAUNCH("df_convert_selftest_kernel");
+  return AEOLUS_OK;
+}
 
 extern "C" int aeolus_selftest_wait_timeout(unsigned long long limit_ns, int* timed_out,
                                             unsigned long long* elapsed_ns) {

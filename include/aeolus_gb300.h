@@ -156,6 +156,15 @@ int aeolus_plan_device_error(aeolus_plan plan, int* flag);
 int aeolus_selftest_wait_timeout(unsigned long long limit_ns, int* timed_out,
                                  unsigned long long* elapsed_ns);
 
+/* Self-test of the FP64 <-> double-float conversions the split path uses
+ * in its derive, PE and column kernels (no reference counterpart): for the
+ * n FP64 values x (device memory), out (device, 3 n doubles) receives per
+ * value hi and lo of its double-float (hi = x truncated to 24 significant
+ * bits, lo = the other 29 bits rounded to a float; |x| below 2^-126 gives
+ * 0, |x| of 2^128 or more +-infinity) and hi + lo rounded back to FP64.
+ * Ordered on `stream`. */
+int aeolus_selftest_df_convert(const double* x, int n, double* out, void* stream);
+
 /* Launch shapes of the plan's kernels (no reference counterpart), an array
  * of AEOLUS_TUNING_KNOBS ints: knobs[0] members per CTA of the FP64 Legendre
  * synthesis, knobs[1] of the analysis, knobs[2] threads per CTA of the

@@ -122,6 +122,41 @@ def test_bounded_wait_gives_up_and_reports():
     assert float(torch.ones(4, device=DEV).sum()) == 4.0
 
 
+def _hi24(x):
+    """x truncated to 24 significant bits (the low 29 mantissa bits cleared)."""
+    b = np.asarray(x, dtype=np.float64).view(np.uint64) & ~np.uint64((1 << 29) - 1)
+    return b.view(np.float64)
+
+
+def test_double_float_conversions_on_device():
+    """The FP64 <-> double-float conversions of the split derive, PE derive
+    and column kernels (integer operations on the bits): hi = x truncated
+    to 24 bits, lo = the rest rounded to a float, |x - hi - lo| <= 2^-48 |x|,
+    and the way back rounds hi + lo once; |x| below 2^-126 gives 0, 2^128
+    and above infinity."""
+    rng = np.random.default_rng(7)
+    mag = 10.0 ** rng.uniform(-25, 30, 20000)  # lo stays a normal float or an exact subnormal
+    edge = [1.0, -1.0, 2.0 ** -126, 2.0 ** 127, np.nextafter(2.0 ** 128, 0), 3.0, np.pi,
+            np.nextafter(1.0, 2.0), np.nextafter(2.0, 0.0), 1.0 + 2.0 ** -24 - 2.0 ** -52, -np.e * 1e-20]
+    x = np.concatenate([mag * rng.choice([-1.0, 1.0], mag.size), edge])
+    special = np.array([0.0, -0.0, 2.0 ** -127, -1e-300, 2.0 ** 128, -1e300])
+    allx = np.concatenate([x, special])
+    d_x = T(allx)
+    d_out = torch.empty(3 * allx.size, dtype=torch.float64, device=DEV)
+    _lib.check(_lib.load().aeolus_selftest_df_convert(d_x.data_ptr(), allx.size, d_out.data_ptr(),
+                                                      torch.cuda.current_stream().cuda_stream))
+    out = N(d_out).reshape(-1, 3)
+    hi, lo, back = out[: x.size, 0], out[: x.size, 1], out[: x.size, 2]
+    np.testing.assert_array_equal(hi, _hi24(x))
+    np.testing.assert_array_equal(lo, (x - _hi24(x)).astype(np.float32).astype(np.float64))
+    np.testing.assert_array_equal(back, hi + lo)
+    assert np.all(np.abs(x - (hi + lo)) <= 2.0 ** -48 * np.abs(x))
+    sp = out[x.size:]
+    np.testing.assert_array_equal(sp[:4], np.zeros((4, 3)))
+    assert sp[4, 0] == np.inf and sp[4, 1] == 0.0 and sp[4, 2] == np.inf
+    assert sp[5, 0] == -np.inf and sp[5, 1] == 0.0 and sp[5, 2] == -np.inf
+
+
 def test_split_rejects_unsupported_shapes():
     p = Plan.gauss(256, 512, 170)
     with pytest.raises(ValueError, match="l_max"):
