@@ -131,6 +131,15 @@ __device__ __forceinline__ df2 df2_add_fast(df2 a, df2 b) {
   return fast_two_sum2(s.hi, s.lo);
 }
 __device__ __forceinline__ df2 df2_neg(df2 a) { return df2{f2_neg(a.hi), f2_neg(a.lo)}; }
+// df_add of two pairs (the accurate addition, same operations lane by lane).
+__device__ __forceinline__ df2 df2_add(df2 a, df2 b) {
+  df2 s = two_sum2(a.hi, b.hi);
+  const df2 t = two_sum2(a.lo, b.lo);
+  s.lo = f2_add(s.lo, t.hi);
+  s = fast_two_sum2(s.hi, s.lo);
+  s.lo = f2_add(s.lo, t.lo);
+  return fast_two_sum2(s.hi, s.lo);
+}
 __device__ __forceinline__ df2 df2_mul(df2 a, df2 b) {
   const f2 p = f2_mul(a.hi, b.hi);
   f2 e = f2_fma(a.hi, b.hi, f2_neg(p));

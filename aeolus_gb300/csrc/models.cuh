@@ -163,6 +163,11 @@ struct JacPw {  // J = (a_snt b_lam - a_lam b_snt) / cos^2
     out[0] = df_mul(df_sub(df_mul(in[1], in[2]), df_mul(in[0], in[3])), r.invc);
     return 0u;
   }
+  // df_op at two grid points on the packed two-lane pipe (bitwise df_op)
+  __device__ unsigned df_op2(const RowDf& r, const df2* in, df2* out) const {
+    out[0] = df2_mul(df2_add(df2_mul(in[1], in[2]), df2_neg(df2_mul(in[0], in[3]))), df2_pack(r.invc, r.invc));
+    return 0u;
+  }
 };
 
 // RK4 stage bookkeeping shared by both models.  mode 0: tendency output;
