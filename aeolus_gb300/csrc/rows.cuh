@@ -296,6 +296,10 @@ struct PwCopy {
     out[0] = in[0];
     return 0u;
   }
+  __device__ unsigned df_op2(const RowDf&, const df2* in, df2* out) const {  // two grid points (packed)
+    out[0] = in[0];
+    return 0u;
+  }
 };
 
 }  // namespace aeolus

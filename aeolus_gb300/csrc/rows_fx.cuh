@@ -418,7 +418,7 @@ __device__ __forceinline__ void row_fx_body(const RowArgs& a, const Pw& pw, cons
     df* x0 = reinterpret_cast<df*>(buf0);
     for (int idx = threadIdx.x; idx < NIN * N; idx += blockDim.x) {
       const int f = idx / N, k = idx - f * N;
-      x0[(long)f * 2 * ns + k] = df_from_double(a.gin[(long)b * a.gin_b + (long)f * a.gin_f + (long)j * N + k]);
+      x0[(long)f * 2 * ns + k] = df_of_f64(a.gin[(long)b * a.gin_b + (long)f * a.gin_f + (long)j * N + k]);
     }
     __syncthreads();
   }
@@ -467,7 +467,7 @@ __device__ __forceinline__ void row_fx_body(const RowArgs& a, const Pw& pw, cons
   if (OUT_MODE == kOutGrid) {
     for (int idx = threadIdx.x; idx < NOUT * N; idx += blockDim.x) {
       const int f = idx / N, k = idx - f * N;
-      a.gout[(long)b * a.gout_b + (long)f * a.gout_f + (long)j * N + k] = df_to_double(xout[(long)f * 2 * ns + k]);
+      a.gout[(long)b * a.gout_b + (long)f * a.gout_f + (long)j * N + k] = f64_of_df(xout[(long)f * 2 * ns + k]);
     }
   } else if (use_fft) {
     // output block exponents (|X| < 2^hb)
@@ -703,7 +703,7 @@ __device__ __forceinline__ void row_fx8_body(const RowArgs& a, const Pw& pw, con
     for (int idx = tid; idx < NIN * N; idx += T) {
       const int f = idx / N, k = idx - f * N;
       x0[2 * (f * fs + Row::swz(k >> 1)) + (k & 1)] =
-          df_from_double(a.gin[(long)b * a.gin_b + (long)f * a.gin_f + (long)j * N + k]);
+          df_of_f64(a.gin[(long)b * a.gin_b + (long)f * a.gin_f + (long)j * N + k]);
     }
     __syncthreads();
   }
@@ -762,7 +762,7 @@ __device__ __forceinline__ void row_fx8_body(const RowArgs& a, const Pw& pw, con
     for (int idx = tid; idx < NOUT * N; idx += T) {
       const int f = idx / N, k = idx - f * N;
       a.gout[(long)b * a.gout_b + (long)f * a.gout_f + (long)j * N + k] =
-          df_to_double(xout[2 * (f * fs + Row::swz(k >> 1)) + (k & 1)]);
+          f64_of_df(xout[2 * (f * fs + Row::swz(k >> 1)) + (k & 1)]);
     }
   } else {
     if (tid < NOUT) {

@@ -333,7 +333,7 @@ __device__ __forceinline__ void row_pfa_body(const RowArgs& a, const Pw& pw, con
       const int rf = idx / N, k = idx - rf * N, row = rf / NIN, f = rf - row * NIN;
       if (row < nrow)
         reinterpret_cast<df*>(zrow(row, f))[2 * S::grid(k >> 1) + (k & 1)] =
-            df_from_double(a.gin[(long)(b0 + row) * a.gin_b + (long)f * a.gin_f + (long)j * N + k]);
+            df_of_f64(a.gin[(long)(b0 + row) * a.gin_b + (long)f * a.gin_f + (long)j * N + k]);
     }
     __syncthreads();
   }
@@ -449,7 +449,7 @@ __device__ __forceinline__ void row_pfa_body(const RowArgs& a, const Pw& pw, con
       const int rf = idx / N, k = idx - rf * N, row = rf / NOUT, f = rf - row * NOUT;
       if (row < nrow)
         a.gout[(long)(b0 + row) * a.gout_b + (long)f * a.gout_f + (long)j * N + k] =
-            df_to_double(reinterpret_cast<const df*>(zrow(row, f))[2 * S::grid(k >> 1) + (k & 1)]);
+            f64_of_df(reinterpret_cast<const df*>(zrow(row, f))[2 * S::grid(k >> 1) + (k & 1)]);
     }
   } else {
     if (tid < NRO) {  // output block exponents (|X| < 2^hb)
