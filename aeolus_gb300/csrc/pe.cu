@@ -140,28 +140,40 @@ __global__ void pe_derive_kernel(Spec s, int K, int batch, double f10, const dou
 // copied in FP64 as they are.
 __global__ void __launch_bounds__(128) pe_derive_df_kernel(Spec s, int K, int batch, double f10,
                                                            const double2* __restrict__ st, double2* __restrict__ out) {
+  // one thread per (member, level, l, m); "level" K is the pair of ln p_s
+  // spectra (the levels are independent, so the loads of all of them fly
+  // at once instead of one level after another)
   const int L = s.L;
   const long n2 = (long)(L + 1) * (L + 1);
   const long idx = (long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (idx >= n2 * batch) return;
-  const int b = (int)(idx / n2);
-  const long r = idx - b * n2;
+  if (idx >= n2 * (K + 1) * batch) return;
+  const long r = idx % n2;
+  const int k = (int)((idx / n2) % (K + 1)), b = (int)(idx / (n2 * (K + 1)));
   const int l = (int)(r / (L + 1)), m = (int)(r - (long)l * (L + 1));
   const double2* S = st + (long)b * (3 * K + 1) * n2;
   double2* O = out + (long)b * (kPeLevelFields * K + 2) * n2 + r;
+  const int nout = k < K ? kPeLevelFields : 2;
+  double2* o = O + (long)kPeLevelFields * k * n2;  // level k's fields, or the two ln p_s ones at k = K
   if (m > l) {
     const double2 zero = make_double2(0.0, 0.0);
-    for (int f = 0; f < kPeLevelFields * K + 2; ++f) O[f * n2] = zero;
+    for (int f = 0; f < nout; ++f) o[f * n2] = zero;
     return;
   }
   const bool lo = l >= 1 && l - 1 >= m, hi = l + 1 <= L;
   const float2* c = s.dcoef_df + r * 8;
   auto kc = [&](int i) { return df2_splat(df{c[i].x, c[i].y}); };
-  const df2 A1 = kc(0), A2 = kc(1), A3 = kc(2), B1 = kc(3), B2 = kc(4), B3 = kc(5);
   const df2 zero = df2{0ull, 0ull};
   auto cv = [&](const double2* a, int ll) { return df2_of_f64x2(a[(long)ll * (L + 1) + m]); };
   auto cvlo = [&](const double2* a) { return lo ? cv(a, l - 1) : zero; };
   auto cvhi = [&](const double2* a) { return hi ? cv(a, l + 1) : zero; };
+  const df2 B1 = kc(3), B2 = kc(4), B3 = kc(5);
+  if (k == K) {
+    const double2* q = S + (long)3 * K * n2;
+    o[0] = f64x2_of_df2(df2_mul(B3, df2_times_i(cv(q, l))));
+    o[n2] = f64x2_of_df2(df2_add_fast(df2_mul(B1, cvlo(q)), df2_mul(B2, cvhi(q))));
+    return;
+  }
+  const df2 A1 = kc(0), A2 = kc(1), A3 = kc(2);
   // eta = zeta + f at the (1, 0) mode, in the neighbour slots
   auto add_f = [&](df2 v, bool at) {
     if (!at) return v;
@@ -169,32 +181,25 @@ __global__ void __launch_bounds__(128) pe_derive_df_kernel(Spec s, int K, int ba
     df2_unpack(v, re, im);
     return df2_pack(df_add(re, df_of_f64(f10)), im);
   };
-  for (int k = 0; k < K; ++k) {
-    const double2* z = S + (long)k * n2;
-    const double2* d = S + (long)(K + k) * n2;
-    const double2* T = S + (long)(2 * K + k) * n2;
-    const long rl = (long)l * (L + 1) + m;
-    const double2 z64 = z[rl], d64 = d[rl], T64 = T[rl];
-    const df2 zl = df2_of_f64x2(z64), dl = df2_of_f64x2(d64), Tl = df2_of_f64x2(T64);
-    const df2 z_lo = cvlo(z), z_hi = cvhi(z), d_lo = cvlo(d), d_hi = cvhi(d);
-    double2* o = O + (long)kPeLevelFields * k * n2;
-    o[0 * n2] = f64x2_of_df2(df2_add_fast(df2_add_fast(df2_mul(A1, z_lo), df2_mul(A2, z_hi)),
-                                          df2_mul(A3, df2_times_i(dl))));    // u cos
-    o[1 * n2] = f64x2_of_df2(df2_sub_fast(df2_mul(A3, df2_times_i(zl)),
-                                          df2_add_fast(df2_mul(A1, d_lo), df2_mul(A2, d_hi))));  // v cos
-    o[2 * n2] = z64;
-    o[3 * n2] = d64;
-    o[4 * n2] = T64;
-    o[5 * n2] = f64x2_of_df2(df2_mul(B3, df2_times_i(Tl)));
-    o[6 * n2] = f64x2_of_df2(df2_add_fast(df2_mul(B1, cvlo(T)), df2_mul(B2, cvhi(T))));
-    o[7 * n2] = f64x2_of_df2(df2_mul(B3, df2_times_i(zl)));  // m = 0 (the only f slot) has B3 = 0
-    o[8 * n2] = f64x2_of_df2(df2_add_fast(df2_mul(B1, add_f(z_lo, m == 0 && l == 2)),
-                                          df2_mul(B2, add_f(z_hi, m == 0 && l == 0))));
-    o[9 * n2] = (m == 0 && l == 1) ? make_double2(z64.x + f10, z64.y) : z64;
-  }
-  const double2* q = S + (long)3 * K * n2;
-  O[(long)kPeLevelFields * K * n2] = f64x2_of_df2(df2_mul(B3, df2_times_i(cv(q, l))));
-  O[((long)kPeLevelFields * K + 1) * n2] = f64x2_of_df2(df2_add_fast(df2_mul(B1, cvlo(q)), df2_mul(B2, cvhi(q))));
+  const double2* z = S + (long)k * n2;
+  const double2* d = S + (long)(K + k) * n2;
+  const double2* T = S + (long)(2 * K + k) * n2;
+  const double2 z64 = z[r], d64 = d[r], T64 = T[r];
+  const df2 zl = df2_of_f64x2(z64), dl = df2_of_f64x2(d64), Tl = df2_of_f64x2(T64);
+  const df2 z_lo = cvlo(z), z_hi = cvhi(z), d_lo = cvlo(d), d_hi = cvhi(d);
+  o[0 * n2] = f64x2_of_df2(df2_add_fast(df2_add_fast(df2_mul(A1, z_lo), df2_mul(A2, z_hi)),
+                                        df2_mul(A3, df2_times_i(dl))));    // u cos
+  o[1 * n2] = f64x2_of_df2(df2_sub_fast(df2_mul(A3, df2_times_i(zl)),
+                                        df2_add_fast(df2_mul(A1, d_lo), df2_mul(A2, d_hi))));  // v cos
+  o[2 * n2] = z64;
+  o[3 * n2] = d64;
+  o[4 * n2] = T64;
+  o[5 * n2] = f64x2_of_df2(df2_mul(B3, df2_times_i(Tl)));
+  o[6 * n2] = f64x2_of_df2(df2_add_fast(df2_mul(B1, cvlo(T)), df2_mul(B2, cvhi(T))));
+  o[7 * n2] = f64x2_of_df2(df2_mul(B3, df2_times_i(zl)));  // m = 0 (the only f slot) has B3 = 0
+  o[8 * n2] = f64x2_of_df2(df2_add_fast(df2_mul(B1, add_f(z_lo, m == 0 && l == 2)),
+                                        df2_mul(B2, add_f(z_hi, m == 0 && l == 0))));
+  o[9 * n2] = (m == 0 && l == 1) ? make_double2(z64.x + f10, z64.y) : z64;
 }
 
 // One thread per (member, product point): the column in thread-local
@@ -506,7 +511,7 @@ extern "C" int aeolus_pe_derive(aeolus_plan plan, const aeolus_pe_params* prm, i
   ProfScope prof("pe_derive", static_cast<cudaStream_t>(stream));
   const Spec sp = make_spec(plan, prm->radius);
   if (plan->precision == AEOLUS_PREC_SPLIT_BF16 && sp.dcoef_df) {
-    pe_derive_df_kernel<<<blocks_for(n2 * batch, 128), 128, 0, static_cast<cudaStream_t>(stream)>>>(
+    pe_derive_df_kernel<<<blocks_for(n2 * (nlev + 1) * batch, 128), 128, 0, static_cast<cudaStream_t>(stream)>>>(
         sp, nlev, batch, 2.0 * prm->omega * kSqrt4PiOver3, reinterpret_cast<const double2*>(state),
         reinterpret_cast<double2*>(fields));
     AE_LAUNCH("pe_derive_df_kernel");
