@@ -169,9 +169,10 @@ __device__ __forceinline__ void pfa_pass(cfx* __restrict__ x, const FxW* __restr
 // Real-FFT pre-processing of the pair (q, n - q) of one field, in place on
 // the spectrum map (as row_fx8_body: z_q = A + P, z_{n-q} = conj(A - P)).
 template <class S>
-__device__ __forceinline__ void pfa_pre_pair(cfx* z, int q, int L, f2 qa, f2 qb, const FxW* __restrict__ twfx) {
+__device__ __forceinline__ void pfa_pre_pair(cfx* z, int q, int L, f2 qa, f2 qb, const FxW* __restrict__ twfx,
+                                             const unsigned short* spec) {
   const int qn = S::n - q;
-  const int s0 = S::spec(q), s1 = S::spec(q == 0 ? 0 : qn);
+  const int s0 = spec[q], s1 = spec[q == 0 ? 0 : qn];
   const FxW w = fx_ldw(&twfx[q]);
   cfx hq = cfx{0, 0}, hn = cfx{0, 0};
   if (q <= L) {
@@ -189,10 +190,11 @@ __device__ __forceinline__ void pfa_pre_pair(cfx* z, int q, int L, f2 qa, f2 qb,
 // Forward post-processing of order q from the spectrum map: the packed G
 // word pair of R2 / 2 (as row_fx8_body).
 template <class S>
-__device__ __forceinline__ void pfa_post(const cfx* Z, int q, int e, const FxW* __restrict__ twfx, longlong2* out) {
+__device__ __forceinline__ void pfa_post(const cfx* Z, int q, int e, const FxW* __restrict__ twfx, longlong2* out,
+                                         const unsigned short* spec) {
   const FxW w = fx_ldw(&twfx[q]);
-  const cfx zq = Z[S::spec(q)];
-  const cfx zn = fx_conj(Z[S::spec(q == 0 ? 0 : S::n - q)]);
+  const cfx zq = Z[spec[q]];
+  const cfx zn = fx_conj(Z[spec[q == 0 ? 0 : S::n - q]]);
   const cfx E2 = fx_add(zq, zn);
   const cfx D = fx_sub(zq, zn);
   const cfx O2 = cfx{D.im, -D.re};
@@ -232,6 +234,8 @@ __device__ __forceinline__ void row_pfa_body(const RowArgs& a, const Pw& pw, con
   __shared__ float s_pa[NR * NF], s_pb[NR * NF], s_qa[NR * NF], s_qb[NR * NF];
   __shared__ RowDf s_rc;
   __shared__ df s_wj;
+  __shared__ unsigned short s_spec[S::n + 1];  // the spectrum and grid maps (S::spec, S::grid),
+  __shared__ unsigned short s_grid[S::n];      // tabulated once per CTA
   const int j = bx, b0 = NR * by, tid = threadIdx.x;
   const int nrow = min(NR, a.batch - b0);  // members of this CTA
   const int L = a.L, ldm = L + 1;
@@ -249,6 +253,10 @@ __device__ __forceinline__ void row_pfa_body(const RowArgs& a, const Pw& pw, con
   if (OUT_MODE == kOutG)
     oblock = a.G ? reinterpret_cast<longlong2*>(a.G) + fg_index(b0, 0, 0, j, L, a.gblk, a.nlat)
                  : reinterpret_cast<longlong2*>(const_cast<float4*>(block));
+  for (int q = tid; q <= n; q += T) {
+    s_spec[q] = static_cast<unsigned short>(S::spec(q));
+    if (q < n) s_grid[q] = static_cast<unsigned short>(S::grid(q));
+  }
   if (tid < NR) s_bits[tid] = 0u;
   if (tid < NR * NF) {
     s_key[tid] = 0u;
@@ -285,7 +293,7 @@ __device__ __forceinline__ void row_pfa_body(const RowArgs& a, const Pw& pw, con
             const int q = q0 + u * QSI;
             if (q < ldm) {
               mx = max(mx, max(__float_as_uint(w[u].x) & 0x7FFFFFFFu, q == 0 ? 0u : __float_as_uint(w[u].z) & 0x7FFFFFFFu));
-              zf[S::spec(q)] = w[u];
+              zf[s_spec[q]] = w[u];
             }
           }
         }
@@ -306,7 +314,7 @@ __device__ __forceinline__ void row_pfa_body(const RowArgs& a, const Pw& pw, con
     for (int idx = tid; idx < NRI * (n / 2 + 1); idx += T) {
       const int q = idx / NRI, rf = idx - q * NRI, row = NR == 1 ? 0 : rf / NIN, f = rf - row * NIN;
       pfa_pre_pair<S>(zrow(row, f), q, row < nrow ? L : -1, f2_splat(s_qa[row * NF + f]), f2_splat(s_qb[row * NF + f]),
-                      twfx);
+                      twfx, s_spec);
     }
     __syncthreads();
     if constexpr (R0 > 1) {
@@ -332,7 +340,7 @@ __device__ __forceinline__ void row_pfa_body(const RowArgs& a, const Pw& pw, con
     for (int idx = tid; idx < NRI * N; idx += T) {
       const int rf = idx / N, k = idx - rf * N, row = rf / NIN, f = rf - row * NIN;
       if (row < nrow)
-        reinterpret_cast<df*>(zrow(row, f))[2 * S::grid(k >> 1) + (k & 1)] =
+        reinterpret_cast<df*>(zrow(row, f))[2 * s_grid[k >> 1] + (k & 1)] =
             df_of_f64(a.gin[(long)(b0 + row) * a.gin_b + (long)f * a.gin_f + (long)j * N + k]);
     }
     __syncthreads();
@@ -386,7 +394,7 @@ __device__ __forceinline__ void row_pfa_body(const RowArgs& a, const Pw& pw, con
     auto single = [&](int k) {  // real grid point k of the CTA's rows
       const int row = NR == 1 ? 0 : k / N, kk = k - row * N;
       at_row(row);
-      const int slot = 2 * S::grid(kk >> 1) + (kk & 1);
+      const int slot = 2 * s_grid[kk >> 1] + (kk & 1);
       cfx* zb = zrow(row, 0);
       const long long* xi = reinterpret_cast<const long long*>(zb);
       const df* xd = reinterpret_cast<const df*>(zb);
@@ -408,7 +416,7 @@ __device__ __forceinline__ void row_pfa_body(const RowArgs& a, const Pw& pw, con
       for (int i = tid; i < (kSplitTail ? T : NR * n); i += T) {
         const int row = NR == 1 ? 0 : i / n, ii = i - row * n;
         at_row(row);
-        const int s = S::grid(ii);
+        const int s = s_grid[ii];
         cfx* zb = zrow(row, 0);
         df2 in[NIN], out[NOUT];
 #pragma unroll
@@ -449,7 +457,7 @@ __device__ __forceinline__ void row_pfa_body(const RowArgs& a, const Pw& pw, con
       const int rf = idx / N, k = idx - rf * N, row = rf / NOUT, f = rf - row * NOUT;
       if (row < nrow)
         a.gout[(long)(b0 + row) * a.gout_b + (long)f * a.gout_f + (long)j * N + k] =
-            f64_of_df(reinterpret_cast<const df*>(zrow(row, f))[2 * S::grid(k >> 1) + (k & 1)]);
+            f64_of_df(reinterpret_cast<const df*>(zrow(row, f))[2 * s_grid[k >> 1] + (k & 1)]);
     }
   } else {
     if (tid < NRO) {  // output block exponents (|X| < 2^hb)
@@ -490,7 +498,7 @@ __device__ __forceinline__ void row_pfa_body(const RowArgs& a, const Pw& pw, con
 #pragma unroll 1
         for (int p = 0; p < 2 * R0; ++p) {
           const int q = (p < R0 ? c : g1) + (p < R0 ? p : p - R0) * P;
-          if (q <= L) pfa_post<S>(Z, q, e, twfx, ob + (long)q * sqo);
+          if (q <= L) pfa_post<S>(Z, q, e, twfx, ob + (long)q * sqo, s_spec);
         }
       }
     }
