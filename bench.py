@@ -702,7 +702,7 @@ def _rel_l2_fields(a, b):
 NCU_TRAFFIC = {
     "split_synth_slice": 27.497728e6 + 86.54464e6,
     "tc_synth_bf16x6": 138.119424e6 + 174.368e6,
-    "rows_fx_c2r_products_r2c": 226.568448e6 + 75.179520e6,
+    "rows_fx_c2r_products_r2c": 226.578432e6 + 75.243008e6,
     "split_anal_slice": 100.69504e6 + 95.401472e6,
     "tc_anal_bf16x6": 230.352896e6 + 67.960576e6,
 }
@@ -711,7 +711,7 @@ NCU_TRAFFIC = {
 # Warp instructions per launch of the same kernels (smsp__inst_executed.sum
 # of the same capture), for the instruction-issue roofline of the row stage.
 NCU_WARP_INSTRUCTIONS = {
-    "rows_fx_c2r_products_r2c": 306.43e6,
+    "rows_fx_c2r_products_r2c": 294.58e6,
 }
 SM_COUNT, ISSUE_PER_SM_CLK = 152, 4  # GB300: 4 schedulers per SM, one warp instruction each per clock
 
