@@ -234,8 +234,11 @@ __device__ __forceinline__ void row_pfa_body(const RowArgs& a, const Pw& pw, con
   __shared__ float s_pa[NR * NF], s_pb[NR * NF], s_qa[NR * NF], s_qb[NR * NF];
   __shared__ RowDf s_rc;
   __shared__ df s_wj;
-  __shared__ unsigned short s_spec[S::n + 1];  // the spectrum and grid maps (S::spec, S::grid),
-  __shared__ unsigned short s_grid[S::n];      // tabulated once per CTA
+  // the spectrum and grid maps (S::spec, S::grid), tabulated once per CTA
+  // after the row buffers (dynamic shared memory: the grouped row kernel,
+  // which holds every body, reserves only the running shape's tables)
+  unsigned short* s_spec = reinterpret_cast<unsigned short*>(smem_fx + NR * RS);
+  unsigned short* s_grid = s_spec + (S::n + 1);
   const int j = bx, b0 = NR * by, tid = threadIdx.x;
   const int nrow = min(NR, a.batch - b0);  // members of this CTA
   const int L = a.L, ldm = L + 1;
@@ -516,7 +519,8 @@ __global__ void __launch_bounds__(kPfaThreads, 6) row_kernel_pfa(RowArgs a, Pw p
 template <class Pw, class S>
 constexpr size_t row_pfa_smem_bytes() {
   constexpr int NF = Pw::NIN > Pw::NOUT ? Pw::NIN : Pw::NOUT;
-  return (size_t)pfa_rows_per_cta<Pw>() * NF * S::fs * sizeof(cfx);
+  return (size_t)pfa_rows_per_cta<Pw>() * NF * S::fs * sizeof(cfx) +  // row buffers
+         ((size_t)(2 * S::n + 1) * sizeof(unsigned short) + 15) / 16 * 16;  // index tables
 }
 // Grid of a prime-factor row launch: (latitude rows, member groups).
 template <class Pw>
