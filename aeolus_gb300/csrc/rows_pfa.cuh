@@ -211,6 +211,17 @@ constexpr int pfa_rows_per_cta() {
   return NF >= 5 ? 1 : NF >= 3 ? 2 : NF == 2 ? 4 : 8;
 }
 
+// Per-CTA scalars of a row body (NR member rows of NF fields).
+template <int NR, int NF>
+struct alignas(16) PfaCtaScratch {
+  unsigned bits[NR];
+  int in[NR * NF];
+  unsigned key[NR * NF], omax[NR * NF];
+  float pa[NR * NF], pb[NR * NF], qa[NR * NF], qb[NR * NF];
+  RowDf rc;
+  df wj;
+};
+
 template <class Pw, int IN_MODE, int OUT_MODE, class S>
 __device__ __forceinline__ void row_pfa_body(const RowArgs& a, const Pw& pw, const FxW* __restrict__ twfx,
                                              const FxConst& kc, int bx, int by) {
@@ -227,17 +238,19 @@ __device__ __forceinline__ void row_pfa_body(const RowArgs& a, const Pw& pw, con
   // slots as one single point per thread
   constexpr bool kSplitTail = NR * n - T == T / 2;
   extern __shared__ cfx smem_fx[];
-  __shared__ unsigned s_bits[NR];
-  __shared__ int s_in[NR * NF];        // block exponents (inputs, then outputs)
-  __shared__ unsigned s_key[NR * NF];  // largest |hi| bit key of each input field
-  __shared__ unsigned s_omax[NR * NF]; // largest |hi| bit key of each output field
-  __shared__ float s_pa[NR * NF], s_pb[NR * NF], s_qa[NR * NF], s_qb[NR * NF];
-  __shared__ RowDf s_rc;
-  __shared__ df s_wj;
-  // the spectrum and grid maps (S::spec, S::grid), tabulated once per CTA
-  // after the row buffers (dynamic shared memory: the grouped row kernel,
-  // which holds every body, reserves only the running shape's tables)
-  unsigned short* s_spec = reinterpret_cast<unsigned short*>(smem_fx + NR * RS);
+  // After the row buffers, in dynamic shared memory (the grouped row kernel
+  // holds every body, and static arrays of all of them would sit in every
+  // CTA): the per-CTA scalars and the spectrum and grid maps (S::spec,
+  // S::grid), tabulated once per CTA.
+  PfaCtaScratch<NR, NF>& sc = *reinterpret_cast<PfaCtaScratch<NR, NF>*>(smem_fx + NR * RS);
+  unsigned* s_bits = sc.bits;
+  int* s_in = sc.in;        // block exponents (inputs, then outputs)
+  unsigned* s_key = sc.key;  // largest |hi| bit key of each input field
+  unsigned* s_omax = sc.omax; // largest |hi| bit key of each output field
+  float *s_pa = sc.pa, *s_pb = sc.pb, *s_qa = sc.qa, *s_qb = sc.qb;
+  RowDf& s_rc = sc.rc;
+  df& s_wj = sc.wj;
+  unsigned short* s_spec = reinterpret_cast<unsigned short*>(&sc + 1);
   unsigned short* s_grid = s_spec + (S::n + 1);
   const int j = bx, b0 = NR * by, tid = threadIdx.x;
   const int nrow = min(NR, a.batch - b0);  // members of this CTA
@@ -519,7 +532,9 @@ __global__ void __launch_bounds__(kPfaThreads, 6) row_kernel_pfa(RowArgs a, Pw p
 template <class Pw, class S>
 constexpr size_t row_pfa_smem_bytes() {
   constexpr int NF = Pw::NIN > Pw::NOUT ? Pw::NIN : Pw::NOUT;
-  return (size_t)pfa_rows_per_cta<Pw>() * NF * S::fs * sizeof(cfx) +  // row buffers
+  constexpr int NR = pfa_rows_per_cta<Pw>();
+  return (size_t)NR * NF * S::fs * sizeof(cfx) +                           // row buffers
+         sizeof(PfaCtaScratch<NR, NF>) +                                   // per-CTA scalars
          ((size_t)(2 * S::n + 1) * sizeof(unsigned short) + 15) / 16 * 16;  // index tables
 }
 // Grid of a prime-factor row launch: (latitude rows, member groups).
