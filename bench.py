@@ -656,7 +656,10 @@ def _collect_kernels(lib, _lib):
     return out
 
 
-def _timed_steps(model, y0, steps, flush, stream, lib, _lib, prof_steps: int = 2):
+PROF_STEPS = 2  # steps run with the per-kernel event profile after the timed ones
+
+
+def _timed_steps(model, y0, steps, flush, stream, lib, _lib, prof_steps: int = PROF_STEPS):
     """K RK4 steps from y0, each bracketed by CUDA events on the launching
     stream, L2 flushed (outside the events) before each step; the library's
     per-kernel event profile is off while they run (its events would sit
@@ -870,7 +873,9 @@ def main():
     if isinstance(clock_summary, dict) and clock_summary.get("sm_mhz"):
         peaks["_sm_mhz"] = float(clock_summary["sm_mhz"])   # issue peak at the clock seen while timing
     roof, roof_all = _roofline(kstats, B, peaks)
-    launches = sum(n for n, _ in kstats.values())
+    # library kernels launched in the timed region: the profiled steps run the
+    # same launches per step as the timed ones
+    launches = sum(n for n, _ in kstats.values()) * args.steps // PROF_STEPS
 
     extras = {}
     direct_gpu = None
